@@ -1,0 +1,152 @@
+/*
+ * richmol_gb300 — C ABI of the GB300 (sm_103a) Krylov time-propagation step.
+ *
+ * The library replaces, for one GPU, the reference's per-step hot path
+ * (CFEL-CMI/richmol):
+ *
+ *   richmol/tdse.py:265-414   TDSE.update      (split-operator and full-H forms)
+ *   richmol/tdse.py:417-486   _expmv_lanczos   (in-house Lanczos exponential)
+ *   richmol/field.py:1073-1142 CarTens.field   (field contraction of M factors)
+ *   richmol/field.py:1145-1245 CarTens.vec     (Kronecker mat-vec)
+ *
+ * The reference has no FFI for this path (it is pure Python over scipy); the
+ * entry points below are what its Python layer binds through ctypes, see
+ * INTEGRATION.md. Conventions:
+ *
+ *   - every function returns an int status (KR_OK == 0); no exception or C++
+ *     type crosses the boundary; kr_last_error() gives the message;
+ *   - vectors and states are DEVICE pointers owned by the caller, complex128
+ *     stored as interleaved (re, im) doubles, row-major (nvec, dim);
+ *   - descriptor arrays (kr_op_desc) are HOST pointers, copied at creation;
+ *   - all work is ordered on the CUDA stream passed in (NULL: legacy stream);
+ *   - kr_step and kr_matvec allocate nothing: their scratch is sized and
+ *     allocated by kr_op_create;
+ *   - one kr_op must not be used from two threads at once.
+ */
+#ifndef RICHMOL_GB300_H
+#define RICHMOL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  KR_OK = 0,
+  KR_ERR_ARG = 1,        /* invalid argument / malformed descriptor          */
+  KR_ERR_CUDA = 2,       /* a CUDA runtime call failed                       */
+  KR_ERR_MAXORDER = 3,   /* Lanczos reached maxorder (tdse.py:480-484)       */
+  KR_ERR_TIMEOUT = 4,    /* a bounded device-side wait gave up               */
+  KR_ERR_UNSUPPORTED = 5 /* shape outside the compiled limits                */
+};
+
+/* K-factor storage kinds: the dense n_k1 x n_k2 block is complex, or purely
+ * real, or purely imaginary (then only its imaginary part is stored). */
+enum { KR_K_COMPLEX = 0, KR_K_REAL = 1, KR_K_IMAG = 2 };
+
+#define KR_MAXCART 9   /* Cartesian components of a rank-2 tensor         */
+#define KR_MAXPART 16  /* operator parts of one sum (A + B + ...)         */
+
+/* Flags of kr_step. */
+#define KR_STEP_SKIP_KRYLOV 1u /* H carries no field term (tdse.py:377): apply
+                                  only the H0 half-phases                   */
+
+typedef struct kr_ctx kr_ctx;
+typedef struct kr_op kr_op;
+
+/*
+ * Block-sparse Kronecker operator  Y_{s1} += sum_terms MF_t X_{s2} K_t^T,
+ * MF_t = scale_p * thresh_p( sum_c coef_{p,c} M_{g,c} ).
+ *
+ * Slabs follow the reference's flat vector order: Jlist x symlist[J], each slab
+ * a row-major (dim_m, dim_k) block (tdse.py:343-360, field.py:1229).
+ * M factors are stored per "group" in ELL form: rows x width entries with a
+ * column index (int32) and ncart complex values per entry; padding entries
+ * carry value 0. An MF instance is one (group, part) pair; a term names its
+ * output slab, input slab, K block and MF instance.
+ */
+typedef struct {
+  int32_t nslab_out, nslab_in;
+  const int32_t* out_dm; const int32_t* out_dk; const int64_t* out_off;
+  const int32_t* in_dm;  const int32_t* in_dk;  const int64_t* in_off;
+  int64_t dim_out, dim_in;
+
+  int32_t nk;                 /* K blocks                                   */
+  const int64_t* k_off;       /* offset (in doubles) into k_data            */
+  const int32_t* k_rows;      /* n_k1                                       */
+  const int32_t* k_cols;      /* n_k2                                       */
+  const int32_t* k_type;      /* KR_K_*                                     */
+  const double* k_data; int64_t k_data_len;
+
+  int32_t nm;                 /* M groups                                   */
+  const int32_t* m_rows;      /* dim_m1                                     */
+  const int32_t* m_width;     /* ELL width                                  */
+  const int32_t* m_ncart;     /* number of Cartesian components stored      */
+  const int64_t* m_col_off;   /* offset into m_col (entries)                */
+  const int64_t* m_val_off;   /* offset (in complex values) into m_val      */
+  const int32_t* m_col; int64_t m_col_len;
+  const double* m_val;  int64_t m_val_len;   /* complex interleaved; layout
+                                                [cart][row][width]          */
+  int32_t npart;              /* operator parts (<= KR_MAXPART)             */
+  int32_t nmf;                /* MF instances                               */
+  const int32_t* mf_group; const int32_t* mf_part;
+
+  int32_t nterm;
+  const int32_t* t_out; const int32_t* t_in; const int32_t* t_k; const int32_t* t_mf;
+
+  int32_t maxorder;           /* Lanczos basis capacity (reference: 100)    */
+} kr_op_desc;
+
+/* Context on one device. Replaces nothing in the reference (which keeps no
+ * device state); created once per process and device. */
+int kr_ctx_create(int device, kr_ctx** out);
+void kr_ctx_destroy(kr_ctx* ctx);
+/* Copies the last error message of ctx (or of the library if ctx is NULL). */
+int kr_last_error(const kr_ctx* ctx, char* buf, size_t len);
+
+/* Uploads the factors of one operator and allocates its scratch.
+ * Replaces the data held by CarTens.kmat / CarTens.mmat (field.py:58-170). */
+int kr_op_create(kr_ctx* ctx, const kr_op_desc* desc, kr_op** out);
+void kr_op_destroy(kr_op* op);
+
+/* Field contraction, one call per time step (field.py:1073-1142):
+ * MF = scale_p * (|x| < thresh_p ? 0 : x),  x = sum_c coef[p][c] M_c.
+ * coef: npart x KR_MAXCART complex (interleaved), scale: npart complex,
+ * thresh: npart doubles (<= 0: no element threshold). Host pointers. */
+int kr_set_field(kr_op* op, const double* coef, const double* scale,
+                 const double* thresh, void* stream);
+
+/* y = H x for nvec vectors (field.py:1145-1245). x: (nvec, dim_in),
+ * y: (nvec, dim_out), device pointers, complex128. */
+int kr_matvec(kr_op* op, const void* x, void* y, int64_t nvec, void* stream);
+
+/* One TDSE.update of nvec state vectors in place (tdse.py:265-414 with
+ * propag='internal'): if phase != NULL (split operator, tdse.py:365-394)
+ *   v <- phase * expmv(fac, H, phase * v), phase = exp(fac/2 diag(H0)),
+ * else (full H, tdse.py:396-402)  v <- expmv(fac, H, v), where expmv is the
+ * reference Lanczos recurrence (tdse.py:417-486) with tolerance tol on the
+ * squared distance of successive solutions. states: (nvec, dim) device,
+ * phase: dim complex device or NULL. If korder != NULL the call synchronises
+ * the stream and writes the Krylov order used for each vector (host array of
+ * nvec int32) and returns KR_ERR_MAXORDER if a vector did not converge;
+ * otherwise device-side errors are reported by the next kr_sync_status. */
+int kr_step(kr_op* op, void* states, int64_t nvec, const void* phase,
+            double fac_re, double fac_im, double tol, uint32_t flags,
+            int32_t* korder, void* stream);
+
+/* Synchronises the stream and returns the pending device-side status of op. */
+int kr_sync_status(kr_op* op, void* stream);
+
+/* Number of kernels launched by op since creation (instrumentation). */
+int64_t kr_op_launch_count(const kr_op* op);
+
+/* Algorithmic work of one mat-vec of op: FP64 fused multiply-adds and the
+ * minimum bytes moved (vector in + out + factors). */
+int kr_op_work(const kr_op* op, double* fma_per_matvec, double* bytes_per_matvec);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RICHMOL_GB300_H */

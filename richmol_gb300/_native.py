@@ -1,0 +1,138 @@
+"""ctypes binding of librichmol_gb300.so (C ABI in include/richmol_gb300.h).
+
+The shared library is built in-tree (``richmol_gb300/lib``) by ``build_library``
+for sm_103a. There is no CPU fallback: if the library or a CUDA device is
+missing, every GPU entry point raises.
+"""
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+LIB_DIR = os.path.join(PKG, "lib")
+LIB_PATH = os.path.join(LIB_DIR, "librichmol_gb300.so")
+INCLUDE = os.path.join(ROOT, "include")
+SOURCES = [os.path.join(PKG, "csrc", "kr_step.cu")]
+ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+KR_OK, KR_ERR_ARG, KR_ERR_CUDA, KR_ERR_MAXORDER, KR_ERR_TIMEOUT, KR_ERR_UNSUPPORTED = range(6)
+KR_K_COMPLEX, KR_K_REAL, KR_K_IMAG = 0, 1, 2
+KR_MAXCART = 9
+KR_MAXPART = 16
+KR_STEP_SKIP_KRYLOV = 1
+
+EXPORTED = [
+    "kr_ctx_create", "kr_ctx_destroy", "kr_last_error", "kr_op_create", "kr_op_destroy",
+    "kr_set_field", "kr_matvec", "kr_step", "kr_sync_status", "kr_op_launch_count", "kr_op_work",
+]
+
+
+class KrylovError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"[kr status {code}] {msg}")
+        self.code = code
+
+
+def build_library(verbose=False, nvcc="nvcc"):
+    """Compiles the CUDA sources into richmol_gb300/lib/librichmol_gb300.so."""
+    os.makedirs(LIB_DIR, exist_ok=True)
+    tmp = LIB_PATH + ".tmp"
+    cmd = [nvcc, *ARCH_FLAGS, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+           "-I", INCLUDE, "-o", tmp, *SOURCES]
+    if verbose:
+        cmd.insert(1, "-Xptxas=-v")
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("nvcc failed:\n" + res.stdout + res.stderr)
+    os.replace(tmp, LIB_PATH)
+    return res.stdout + res.stderr
+
+
+class kr_op_desc(ctypes.Structure):
+    P = ctypes.c_void_p
+    _fields_ = [
+        ("nslab_out", ctypes.c_int32), ("nslab_in", ctypes.c_int32),
+        ("out_dm", P), ("out_dk", P), ("out_off", P),
+        ("in_dm", P), ("in_dk", P), ("in_off", P),
+        ("dim_out", ctypes.c_int64), ("dim_in", ctypes.c_int64),
+        ("nk", ctypes.c_int32),
+        ("k_off", P), ("k_rows", P), ("k_cols", P), ("k_type", P),
+        ("k_data", P), ("k_data_len", ctypes.c_int64),
+        ("nm", ctypes.c_int32),
+        ("m_rows", P), ("m_width", P), ("m_ncart", P), ("m_col_off", P), ("m_val_off", P),
+        ("m_col", P), ("m_col_len", ctypes.c_int64),
+        ("m_val", P), ("m_val_len", ctypes.c_int64),
+        ("npart", ctypes.c_int32),
+        ("nmf", ctypes.c_int32), ("mf_group", P), ("mf_part", P),
+        ("nterm", ctypes.c_int32), ("t_out", P), ("t_in", P), ("t_k", P), ("t_mf", P),
+        ("maxorder", ctypes.c_int32),
+    ]
+
+
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def lib():
+    """Loads the library once; raises if it has not been built."""
+    global _lib
+    with _lib_lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run richmol_gb300._native.build_library() "
+                              "(or __graft_entry__.build()) first; there is no CPU fallback")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i32, i64, dbl = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+        L.kr_ctx_create.argtypes = [ctypes.c_int, ctypes.POINTER(vp)]
+        L.kr_ctx_create.restype = ctypes.c_int
+        L.kr_ctx_destroy.argtypes = [vp]
+        L.kr_ctx_destroy.restype = None
+        L.kr_last_error.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+        L.kr_last_error.restype = ctypes.c_int
+        L.kr_op_create.argtypes = [vp, ctypes.POINTER(kr_op_desc), ctypes.POINTER(vp)]
+        L.kr_op_create.restype = ctypes.c_int
+        L.kr_op_destroy.argtypes = [vp]
+        L.kr_op_destroy.restype = None
+        L.kr_set_field.argtypes = [vp, vp, vp, vp, vp]
+        L.kr_set_field.restype = ctypes.c_int
+        L.kr_matvec.argtypes = [vp, vp, vp, i64, vp]
+        L.kr_matvec.restype = ctypes.c_int
+        L.kr_step.argtypes = [vp, vp, i64, vp, dbl, dbl, dbl, ctypes.c_uint32, vp, vp]
+        L.kr_step.restype = ctypes.c_int
+        L.kr_sync_status.argtypes = [vp, vp]
+        L.kr_sync_status.restype = ctypes.c_int
+        L.kr_op_launch_count.argtypes = [vp]
+        L.kr_op_launch_count.restype = i64
+        L.kr_op_work.argtypes = [vp, ctypes.POINTER(dbl), ctypes.POINTER(dbl)]
+        L.kr_op_work.restype = ctypes.c_int
+        _lib = L
+        return L
+
+
+def last_error(ctx=None):
+    buf = ctypes.create_string_buffer(1024)
+    lib().kr_last_error(ctx, buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(code, ctx=None):
+    if code != KR_OK:
+        raise KrylovError(code, last_error(ctx))
+
+
+def ptr(a):
+    """Address of a contiguous numpy array or torch tensor."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        assert a.flags.c_contiguous
+        return a.ctypes.data
+    assert a.is_contiguous()
+    return a.data_ptr()

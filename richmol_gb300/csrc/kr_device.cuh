@@ -1,0 +1,246 @@
+// Device-side building blocks of the Krylov step: complex helpers, the bounded
+// grid barrier, deterministic reductions and the Kronecker mat-vec task loop.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define KR_WARPS 8                  // warps per CTA
+#define KR_THREADS (KR_WARPS * 32)
+#define KR_QMAX 4                   // output pairs per lane (n_k1 * rows <= 128)
+#define KR_BARRIER_TIMEOUT_NS 2000000000ull  // 2 s per grid-barrier wait
+
+// ---------------------------------------------------------------------------
+// complex helpers (double2 = re, im)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+// a += b * c
+__device__ __forceinline__ void cfma(double2& a, double2 b, double2 c) {
+  a.x = fma(b.x, c.x, a.x);
+  a.x = fma(-b.y, c.y, a.x);
+  a.y = fma(b.x, c.y, a.y);
+  a.y = fma(b.y, c.x, a.y);
+}
+// conj(a) * b
+__device__ __forceinline__ double2 cconjmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ double cabs2(double2 a) { return a.x * a.x + a.y * a.y; }
+
+__device__ __forceinline__ double2 ldcg2(const double2* p) { return __ldcg(p); }
+
+// ---------------------------------------------------------------------------
+// operator tables on the device
+// ---------------------------------------------------------------------------
+struct DevOp {
+  int nslab_out, nslab_in;
+  const int* out_dm; const int* out_dk; const long long* out_off;
+  const int* in_dm;  const int* in_dk;  const long long* in_off;
+  long long dim_out, dim_in;
+  // K blocks
+  const long long* k_off; const int* k_rows; const int* k_cols; const int* k_type; const double* k_data;
+  // MF instances (ELL): values at mf_val + mf_off[i], columns at m_col + mf_col_off[i]
+  const long long* mf_off; const long long* mf_col_off; const int* mf_width;
+  const int* m_col; double2* mf_val;
+  // terms grouped by output slab
+  const int* term_ptr; const int* t_in; const int* t_k; const int* t_mf;
+  // row tasks and their static assignment to warps
+  const int* task_slab; const int* task_row0; const int* task_nrows;
+  const int* warp_task_ptr; const int* warp_tasks;
+  int zmax;  // complex entries of the per-warp Z staging buffer
+};
+
+// ---------------------------------------------------------------------------
+// grid barrier with a bounded wait. Every CTA of a cooperative launch calls it
+// the same number of times. Returns false if the wait gave up or another CTA
+// reported an error; the caller then leaves the kernel.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
+__device__ bool grid_barrier(unsigned* count, unsigned* gen, int* status, int code_on_timeout) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    unsigned my_gen = ld_acquire_u32(gen);
+    __threadfence();
+    unsigned arrived = atomicAdd(count, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(count, 0u);
+      __threadfence();
+      st_release_u32(gen, my_gen + 1u);
+    } else {
+      unsigned long long t0 = globaltimer_ns();
+      while (ld_acquire_u32(gen) == my_gen) {
+        if (globaltimer_ns() - t0 > KR_BARRIER_TIMEOUT_NS) {
+          atomicCAS(status, 0, code_on_timeout);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (ok && *((volatile int*)status) != 0) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// ---------------------------------------------------------------------------
+// deterministic reductions
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double2 warp_sum2(double2 v) {
+  v.x = warp_sum(v.x);
+  v.y = warp_sum(v.y);
+  return v;
+}
+// Sum of one double2 per thread over the CTA; result valid in all threads.
+__device__ double2 block_sum2(double2 v, double2* scratch /* KR_WARPS */) {
+  v = warp_sum2(v);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) scratch[warp] = v;
+  __syncthreads();
+  double2 s = make_double2(0.0, 0.0);
+  for (int w = 0; w < KR_WARPS; ++w) s = cadd(s, scratch[w]);
+  __syncthreads();
+  return s;
+}
+// Sum of n values written by the CTAs of the grid, same order in every CTA.
+__device__ double2 grid_partials_sum2(const double2* part, int n, double2* scratch) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (warp == 0) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int i = lane; i < n; i += 32) s = cadd(s, ldcg2(part + i));
+    s = warp_sum2(s);
+    if (lane == 0) scratch[0] = s;
+  }
+  __syncthreads();
+  double2 r = scratch[0];
+  __syncthreads();
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// Kronecker mat-vec over the row tasks of one warp:
+//   y[s1][i, a] = sum_terms sum_b K_t[a, b] * Z_t[i, b],
+//   Z_t[i, b]   = xscale * sum_w MF_t[i, w] * x[s2][col_t(i, w), b]
+// (field.py:1229-1243 computes the same sum as MF (K X^T)^T per term.)
+// With ALPHA the warp also accumulates sum conj(y) * (xscale * x) over its
+// outputs: the Lanczos coefficient vdot(w, V_k) of tdse.py:468 for a square
+// operator, where V_k = xscale * x.
+// ---------------------------------------------------------------------------
+template <bool ALPHA>
+__device__ void matvec_warp_tasks(const DevOp& op, const double2* __restrict__ x, double xscale,
+                                  double2* __restrict__ y, int gwarp, double2* zbuf, double2& alpha_acc) {
+  const int lane = threadIdx.x & 31;
+  const int t_begin = __ldg(op.warp_task_ptr + gwarp), t_end = __ldg(op.warp_task_ptr + gwarp + 1);
+  for (int t = t_begin; t < t_end; ++t) {
+    const int task = __ldg(op.warp_tasks + t);
+    const int s1 = __ldg(op.task_slab + task);
+    const int i0 = __ldg(op.task_row0 + task);
+    const int nr = __ldg(op.task_nrows + task);
+    const int nk1 = __ldg(op.out_dk + s1);
+    const int npair = nr * nk1;
+    double2 acc[KR_QMAX];
+#pragma unroll
+    for (int q = 0; q < KR_QMAX; ++q) acc[q] = make_double2(0.0, 0.0);
+
+    const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
+    for (int term = tb; term < te; ++term) {
+      const int s2 = __ldg(op.t_in + term);
+      const int kb = __ldg(op.t_k + term);
+      const int mfi = __ldg(op.t_mf + term);
+      const int nk2 = __ldg(op.in_dk + s2);
+      const double2* X = x + __ldg(op.in_off + s2);
+      const int W = __ldg(op.mf_width + mfi);
+      const int* col = op.m_col + __ldg(op.mf_col_off + mfi);
+      const double2* mf = op.mf_val + __ldg(op.mf_off + mfi);
+      // stage Z for the nr rows of this task
+      const int nz = nr * nk2;
+      for (int p = lane; p < nz; p += 32) {
+        const int r = p / nk2;
+        const int b = p - r * nk2;
+        const int base = (i0 + r) * W;
+        double2 z = make_double2(0.0, 0.0);
+        for (int w = 0; w < W; ++w) {
+          const int j = __ldg(col + base + w);
+          const double2 m = __ldg(mf + base + w);
+          cfma(z, m, ldcg2(X + (long long)j * nk2 + b));
+        }
+        zbuf[p] = cscale(z, xscale);
+      }
+      __syncwarp();
+      const double* K = op.k_data + __ldg(op.k_off + kb);
+      const int ktype = __ldg(op.k_type + kb);
+#pragma unroll
+      for (int q = 0; q < KR_QMAX; ++q) {
+        const int p = lane + 32 * q;
+        if (p < npair) {
+          const int r = p / nk1;
+          const int a = p - r * nk1;
+          const double2* zr = zbuf + r * nk2;
+          double2 s = acc[q];
+          if (ktype == 1) {  // real K
+            const double* Ka = K + (long long)a * nk2;
+            for (int b = 0; b < nk2; ++b) {
+              const double kv = __ldg(Ka + b);
+              const double2 zv = zr[b];
+              s.x = fma(kv, zv.x, s.x);
+              s.y = fma(kv, zv.y, s.y);
+            }
+          } else if (ktype == 2) {  // K = i * Ki
+            const double* Ka = K + (long long)a * nk2;
+            for (int b = 0; b < nk2; ++b) {
+              const double kv = __ldg(Ka + b);
+              const double2 zv = zr[b];
+              s.x = fma(-kv, zv.y, s.x);
+              s.y = fma(kv, zv.x, s.y);
+            }
+          } else {  // complex K
+            const double2* Ka = reinterpret_cast<const double2*>(K) + (long long)a * nk2;
+            for (int b = 0; b < nk2; ++b) cfma(s, __ldg(Ka + b), zr[b]);
+          }
+          acc[q] = s;
+        }
+      }
+      __syncwarp();
+    }
+    const long long obase = __ldg(op.out_off + s1) + (long long)i0 * nk1;
+#pragma unroll
+    for (int q = 0; q < KR_QMAX; ++q) {
+      const int p = lane + 32 * q;
+      if (p < npair) {
+        y[obase + p] = acc[q];
+        if (ALPHA) {
+          const double2 v = cscale(ldcg2(x + obase + p), xscale);
+          alpha_acc = cadd(alpha_acc, cconjmul(acc[q], v));
+        }
+      }
+    }
+  }
+}

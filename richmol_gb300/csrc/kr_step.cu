@@ -1,0 +1,896 @@
+// Krylov time-propagation step for GB300 (sm_103a): field contraction,
+// Kronecker mat-vec and the persistent cooperative Lanczos kernel, plus the
+// C ABI declared in include/richmol_gb300.h.
+//
+// Reference behaviour (CFEL-CMI/richmol):
+//   richmol/tdse.py:365-414   split-operator / full-H update
+//   richmol/tdse.py:417-486   _expmv_lanczos
+//   richmol/field.py:1073-1142 CarTens.field
+//   richmol/field.py:1145-1245 CarTens.vec
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <queue>
+#include <string>
+#include <vector>
+
+#include "../../include/richmol_gb300.h"
+#include "kr_device.cuh"
+
+#define KR_EXPM_MAX 128  // capacity of the tridiagonal exponential (maxorder <= 128)
+
+// ===========================================================================
+// field contraction: MF = scale * thr(sum_c coef_c M_c)
+// ===========================================================================
+struct FieldCoef {
+  int npart;
+  double2 coef[KR_MAXPART][KR_MAXCART];
+  double2 scale[KR_MAXPART];
+  double thresh[KR_MAXPART];
+};
+
+struct DevField {
+  long long nent;
+  const int* ent_inst;          // MF instance of each entry
+  const long long* inst_ptr;    // first entry of each instance
+  const int* mf_group; const int* mf_part;
+  const long long* m_val_off; const int* m_ncart; const int* m_rows; const int* m_width;
+  const double2* m_val;
+  double2* mf_val;
+};
+
+__global__ void __launch_bounds__(256) kr_field_kernel(DevField f, FieldCoef c) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < f.nent;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int inst = __ldg(f.ent_inst + e);
+    const int g = __ldg(f.mf_group + inst);
+    const int p = __ldg(f.mf_part + inst);
+    const long long local = e - __ldg(f.inst_ptr + inst);
+    const long long stride = (long long)__ldg(f.m_rows + g) * __ldg(f.m_width + g);
+    const double2* M = f.m_val + __ldg(f.m_val_off + g) + local;
+    const int nc = __ldg(f.m_ncart + g);
+    double2 v = make_double2(0.0, 0.0);
+    for (int ci = 0; ci < nc; ++ci) cfma(v, c.coef[p][ci], __ldg(M + ci * stride));
+    // field.py:1133-1137: elements below the threshold are dropped
+    if (c.thresh[p] > 0.0 && sqrt(cabs2(v)) < c.thresh[p]) v = make_double2(0.0, 0.0);
+    f.mf_val[e] = cmul(c.scale[p], v);
+  }
+}
+
+// ===========================================================================
+// stand-alone mat-vec (CarTens.vec): grid.y runs over vectors
+// ===========================================================================
+__global__ void __launch_bounds__(KR_THREADS) kr_matvec_kernel(DevOp op, const double2* x, double2* y) {
+  extern __shared__ double2 smem[];
+  const int warp = threadIdx.x >> 5;
+  double2* zbuf = smem + warp * op.zmax;
+  const long long v = blockIdx.y;
+  double2 dummy = make_double2(0.0, 0.0);
+  matvec_warp_tasks<false>(op, x + v * op.dim_in, 1.0, y + v * op.dim_out, blockIdx.x * KR_WARPS + warp, zbuf,
+                           dummy);
+}
+
+// v <- (v * ph) * ph : the two H0 half-phases with no field term (tdse.py:375,394)
+__global__ void kr_phase2_kernel(double2* v, const double2* ph, long long dim, long long nvec) {
+  const long long n = dim * nvec;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const double2 p = ph[e % dim];
+    v[e] = cmul(cmul(v[e], p), p);
+  }
+}
+
+// ===========================================================================
+// exp(A) e0 for the (n x n) complex tridiagonal A = fac * T (one warp).
+// Truncated Taylor series applied to the vector with s sub-steps so that
+// ||A/s||_1 <= 1 (the action-of-exponential approach of Al-Mohy & Higham,
+// SIAM J. Sci. Comput. 33 (2011) 488, without its cost optimisation).
+// The reference forms the dense expm (scipy Pade, tdse.py:474) and takes
+// column 0; both agree to rounding.
+// ===========================================================================
+__device__ void warp_expm_e0(const double2* alpha, const double* beta, int n, double2 fac, double2* out,
+                             double2* term, double2* tmp) {
+  const int lane = threadIdx.x & 31;
+  // 1-norm of A
+  double nrm = 0.0;
+  for (int i = lane; i < n; i += 32) {
+    double cs = sqrt(cabs2(cmul(fac, alpha[i])));
+    const double fa = sqrt(cabs2(fac));
+    if (i > 0) cs += fa * fabs(beta[i - 1]);
+    if (i < n - 1) cs += fa * fabs(beta[i]);
+    nrm = fmax(nrm, cs);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nrm = fmax(nrm, __shfl_xor_sync(0xffffffffu, nrm, o));
+  int nsub = (int)ceil(nrm);
+  if (nsub < 1) nsub = 1;
+  if (nsub > 4096) nsub = 4096;
+  const double inv_s = 1.0 / (double)nsub;
+  for (int i = lane; i < n; i += 32) out[i] = make_double2(i == 0 ? 1.0 : 0.0, 0.0);
+  __syncwarp();
+  for (int sub = 0; sub < nsub; ++sub) {
+    for (int i = lane; i < n; i += 32) term[i] = out[i];
+    __syncwarp();
+    for (int j = 1; j <= 60; ++j) {
+      const double sc = inv_s / (double)j;
+      double tmax = 0.0, amax = 0.0;
+      for (int i = lane; i < n; i += 32) {
+        double2 r = cmul(cmul(fac, alpha[i]), term[i]);
+        if (i > 0) cfma(r, cscale(fac, beta[i - 1]), term[i - 1]);
+        if (i < n - 1) cfma(r, cscale(fac, beta[i]), term[i + 1]);
+        tmp[i] = cscale(r, sc);
+      }
+      __syncwarp();
+      for (int i = lane; i < n; i += 32) {
+        term[i] = tmp[i];
+        out[i] = cadd(out[i], tmp[i]);
+        tmax = fmax(tmax, sqrt(cabs2(tmp[i])));
+        amax = fmax(amax, sqrt(cabs2(out[i])));
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        tmax = fmax(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
+        amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+      }
+      __syncwarp();
+      if (tmax <= 1e-18 * amax) break;
+    }
+  }
+}
+
+// ===========================================================================
+// persistent cooperative Lanczos kernel: one TDSE.update of one vector
+// ===========================================================================
+struct StepArgs {
+  DevOp op;
+  double2* state;          // (dim) in/out
+  const double2* phase;    // (dim) or null
+  double2* V;              // maxorder x dim
+  double2* Wb[2];          // residual vectors W_{k-1}, W_k
+  double2* w;              // H V_k
+  double2* ub[2];          // successive solutions
+  double2* part_a;         // per-CTA partials
+  double* part_b;
+  double* part_c;
+  double2* alpha;          // T diagonal   (maxorder)
+  double* beta;            // T off-diagonal (maxorder)
+  unsigned* bar_count;
+  unsigned* bar_gen;
+  int* status;
+  int* kout;
+  double2 fac;
+  double tol;
+  int maxorder;
+  long long dim;
+};
+
+struct StepSmem {
+  double2 red[KR_WARPS];
+  double2 c[KR_EXPM_MAX];
+  double2 ta[KR_EXPM_MAX];
+  double tb[KR_EXPM_MAX];
+  double2 term[KR_EXPM_MAX];
+  double2 tmp[KR_EXPM_MAX];
+  double scalar[4];
+};
+
+__global__ void __launch_bounds__(KR_THREADS, 1) kr_step_kernel(StepArgs a) {
+  extern __shared__ double2 smem_dyn[];
+  __shared__ StepSmem ss;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nblk = gridDim.x;
+  const long long gtid = blockIdx.x * (long long)blockDim.x + tid;
+  const long long gstride = (long long)nblk * blockDim.x;
+  const long long n = a.dim;
+  double2* zbuf = smem_dyn + warp * a.op.zmax;
+  const int gwarp = blockIdx.x * KR_WARPS + warp;
+
+  if (*((volatile int*)a.status) != 0) return;  // sticky error from an earlier launch
+
+  // ---- V0 = phase * state (tdse.py:375) -----------------------------------
+  double2* V0 = a.V;
+  for (long long e = gtid; e < n; e += gstride) {
+    double2 v = a.state[e];
+    if (a.phase) v = cmul(v, a.phase[e]);
+    V0[e] = v;
+  }
+  if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
+
+  // ---- k = 0: w = H V0, T00 = vdot(w, V0), W0 = w - T00 V0 (tdse.py:443-446)
+  {
+    double2 al = make_double2(0.0, 0.0);
+    matvec_warp_tasks<true>(a.op, V0, 1.0, a.w, gwarp, zbuf, al);
+    al = block_sum2(al, ss.red);
+    if (tid == 0) a.part_a[blockIdx.x] = al;
+  }
+  if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
+  {
+    const double2 a0 = grid_partials_sum2(a.part_a, nblk, ss.red);
+    if (blockIdx.x == 0 && tid == 0) a.alpha[0] = a0;
+    double bp = 0.0;
+    double2* W0 = a.Wb[0];
+    for (long long e = gtid; e < n; e += gstride) {
+      double2 r = ldcg2(a.w + e);
+      const double2 v = ldcg2(V0 + e);
+      r = csub(r, cmul(a0, v));
+      W0[e] = r;
+      bp += cabs2(r);
+    }
+    const double2 s = block_sum2(make_double2(bp, 0.0), ss.red);
+    if (tid == 0) a.part_b[blockIdx.x] = s.x;
+  }
+  if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
+
+  // ---- Lanczos iterations (tdse.py:450-478) -------------------------------
+  int k = 1;
+  const double2* uprev = V0;
+  double2* unext = a.ub[1];
+  bool done = false;
+  while (!done) {
+    // beta_{k-1} = ||W_{k-1}|| (tdse.py:453)
+    double beta_k;
+    {
+      // sum of part_b (doubles) in a fixed order
+      __syncthreads();
+      if (warp == 0) {
+        double s = 0.0;
+        for (int i = lane; i < nblk; i += 32) s += __ldcg(a.part_b + i);
+        s = warp_sum(s);
+        if (lane == 0) ss.scalar[0] = s;
+      }
+      __syncthreads();
+      beta_k = sqrt(ss.scalar[0]);
+      __syncthreads();
+    }
+    if (blockIdx.x == 0 && tid == 0) a.beta[k - 1] = beta_k;
+    double2* Vk = a.V + (long long)k * n;
+    const double2* Vkm1 = a.V + (long long)(k - 1) * n;
+    const double2* xsrc;
+    double xscale;
+    if (beta_k != 0.0) {
+      const double2* Wprev = a.Wb[(k - 1) & 1];
+      xscale = 1.0 / beta_k;
+      xsrc = Wprev;
+      for (long long e = gtid; e < n; e += gstride) Vk[e] = cscale(ldcg2(Wprev + e), xscale);
+    } else {
+      // breakdown: orthonormalise a vector of ones against V_0..V_{k-1} (tdse.py:459-465)
+      for (long long e = gtid; e < n; e += gstride) Vk[e] = make_double2(1.0, 0.0);
+      for (int j = 0; j < k; ++j) {
+        if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
+        const double2* Vj = a.V + (long long)j * n;
+        double2 pp = make_double2(0.0, 0.0);
+        for (long long e = gtid; e < n; e += gstride) pp = cadd(pp, cconjmul(ldcg2(Vj + e), ldcg2(Vk + e)));
+        pp = block_sum2(pp, ss.red);
+        if (tid == 0) a.part_a[blockIdx.x] = pp;
+        if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
+        const double2 proj = grid_partials_sum2(a.part_a, nblk, ss.red);
+        for (long long e = gtid; e < n; e += gstride) Vk[e] = csub(ldcg2(Vk + e), cmul(proj, ldcg2(Vj + e)));
+      }
+      if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
+      double np_ = 0.0;
+      for (long long e = gtid; e < n; e += gstride) np_ += cabs2(ldcg2(Vk + e));
+      const double2 ns = block_sum2(make_double2(np_, 0.0), ss.red);
+      if (tid == 0) a.part_b[blockIdx.x] = ns.x;
+      if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
+      __syncthreads();
+      if (warp == 0) {
+        double s = 0.0;
+        for (int i = lane; i < nblk; i += 32) s += __ldcg(a.part_b + i);
+        s = warp_sum(s);
+        if (lane == 0) ss.scalar[1] = sqrt(s);
+      }
+      __syncthreads();
+      const double nrm = ss.scalar[1];
+      for (long long e = gtid; e < n; e += gstride) {
+        const double2 v = ldcg2(Vk + e);
+        Vk[e] = make_double2(v.x / nrm, v.y / nrm);
+      }
+      if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
+      xsrc = Vk;
+      xscale = 1.0;
+    }
+
+    // w = H V_k and T_kk = vdot(w, V_k) (tdse.py:467-468)
+    {
+      double2 al = make_double2(0.0, 0.0);
+      matvec_warp_tasks<true>(a.op, xsrc, xscale, a.w, gwarp, zbuf, al);
+      al = block_sum2(al, ss.red);
+      if (tid == 0) a.part_a[blockIdx.x] = al;
+    }
+    if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
+
+    // T_kk, then exp(fac T_{0..k}) e0 in every CTA (tdse.py:474)
+    const double2 ak = grid_partials_sum2(a.part_a, nblk, ss.red);
+    if (blockIdx.x == 0 && tid == 0) a.alpha[k] = ak;
+    __syncthreads();
+    if (warp == 0) {
+      for (int i = lane; i <= k; i += 32) {
+        ss.ta[i] = (i == k) ? ak : __ldcg(a.alpha + i);
+        if (i < k) ss.tb[i] = (i == k - 1) ? beta_k : __ldcg(a.beta + i);
+      }
+      __syncwarp();
+      warp_expm_e0(ss.ta, ss.tb, k + 1, a.fac, ss.c, ss.term, ss.tmp);
+    }
+    __syncthreads();
+
+    // W_k = w - T_kk V_k - beta_{k-1} V_{k-1} (tdse.py:469);
+    // u_k = sum_i c_i V_i, conv = ||u_k - u_{k-1}||^2 (tdse.py:475-476)
+    {
+      double bp = 0.0, cp = 0.0;
+      double2* Wk = a.Wb[k & 1];
+      for (long long e = gtid; e < n; e += gstride) {
+        const double2 vk = ldcg2(Vk + e);
+        double2 r = csub(ldcg2(a.w + e), cmul(ak, vk));
+        r = csub(r, cscale(ldcg2(Vkm1 + e), beta_k));
+        Wk[e] = r;
+        bp += cabs2(r);
+        double2 u = make_double2(0.0, 0.0);
+        for (int i = 0; i <= k; ++i) cfma(u, ss.c[i], ldcg2(a.V + (long long)i * n + e));
+        const double2 d = csub(u, ldcg2(uprev + e));
+        cp += cabs2(d);
+        unext[e] = u;
+      }
+      const double2 s = block_sum2(make_double2(bp, cp), ss.red);
+      if (tid == 0) {
+        a.part_b[blockIdx.x] = s.x;
+        a.part_c[blockIdx.x] = s.y;
+      }
+    }
+    if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
+
+    double conv;
+    __syncthreads();
+    if (warp == 0) {
+      double s = 0.0;
+      for (int i = lane; i < nblk; i += 32) s += __ldcg(a.part_c + i);
+      s = warp_sum(s);
+      if (lane == 0) ss.scalar[2] = s;
+    }
+    __syncthreads();
+    conv = ss.scalar[2];
+    __syncthreads();
+    k += 1;
+    uprev = unext;
+    unext = a.ub[k & 1];
+    if (!(conv > a.tol)) done = true;
+    if (k >= a.maxorder) {
+      if (blockIdx.x == 0 && tid == 0) atomicCAS(a.status, 0, KR_ERR_MAXORDER);
+      done = true;
+    }
+  }
+
+  // ---- state = phase * u_k (tdse.py:394) ---------------------------------
+  for (long long e = gtid; e < n; e += gstride) {
+    double2 u = ldcg2(uprev + e);
+    if (a.phase) u = cmul(u, a.phase[e]);
+    a.state[e] = u;
+  }
+  if (blockIdx.x == 0 && tid == 0) *a.kout = k;
+}
+
+// ===========================================================================
+// host side
+// ===========================================================================
+struct kr_ctx {
+  int device = 0;
+  int nsm = 0;
+  std::string err;
+};
+
+namespace {
+std::mutex g_err_mu;
+std::string g_err;
+
+int set_err(kr_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_err = msg;
+  return code;
+}
+}  // namespace
+
+#define KR_CUDA(ctx, call)                                                                 \
+  do {                                                                                     \
+    cudaError_t _e = (call);                                                               \
+    if (_e != cudaSuccess)                                                                 \
+      return set_err((ctx), KR_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+struct kr_op {
+  kr_ctx* ctx = nullptr;
+  DevOp dev{};
+  DevField field{};
+  std::vector<void*> allocs;
+  int grid = 1;
+  size_t smem = 0;
+  int maxorder = 100;
+  bool square = false;
+  int npart = 0;
+  int nmf = 0;
+  long long launches = 0;
+  double fma_per_matvec = 0, bytes_per_matvec = 0;
+  // step scratch
+  double2 *V = nullptr, *Wb0 = nullptr, *Wb1 = nullptr, *w = nullptr, *ub0 = nullptr, *ub1 = nullptr;
+  double2* part_a = nullptr;
+  double *part_b = nullptr, *part_c = nullptr;
+  double2* alpha = nullptr;
+  double* beta = nullptr;
+  unsigned* bar = nullptr;  // [count, gen]
+  int* status = nullptr;    // [status, kout]
+};
+
+template <typename T>
+static int upload(kr_op* op, const T* host, size_t count, T** dev) {
+  *dev = nullptr;
+  size_t bytes = sizeof(T) * std::max<size_t>(count, 1);
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) return set_err(op->ctx, KR_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  op->allocs.push_back(p);
+  if (count && host) {
+    e = cudaMemcpy(p, host, sizeof(T) * count, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return set_err(op->ctx, KR_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+  } else {
+    cudaMemset(p, 0, bytes);
+  }
+  *dev = static_cast<T*>(p);
+  return KR_OK;
+}
+
+extern "C" int kr_ctx_create(int device, kr_ctx** out) {
+  if (!out) return set_err(nullptr, KR_ERR_ARG, "kr_ctx_create: out is NULL");
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return set_err(nullptr, KR_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  if (device < 0 || device >= ndev) return set_err(nullptr, KR_ERR_ARG, "kr_ctx_create: bad device index");
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return set_err(nullptr, KR_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+  kr_ctx* c = new kr_ctx();
+  c->device = device;
+  cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+  if (!coop) {
+    delete c;
+    return set_err(nullptr, KR_ERR_UNSUPPORTED, "device does not support cooperative launch");
+  }
+  *out = c;
+  return KR_OK;
+}
+
+extern "C" void kr_ctx_destroy(kr_ctx* ctx) { delete ctx; }
+
+extern "C" int kr_last_error(const kr_ctx* ctx, char* buf, size_t len) {
+  if (!buf || len == 0) return KR_ERR_ARG;
+  std::string m;
+  if (ctx) {
+    m = ctx->err;
+  } else {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    m = g_err;
+  }
+  std::snprintf(buf, len, "%s", m.c_str());
+  return KR_OK;
+}
+
+extern "C" void kr_op_destroy(kr_op* op) {
+  if (!op) return;
+  for (void* p : op->allocs) cudaFree(p);
+  delete op;
+}
+
+namespace {
+
+// rows per warp task for an output slab with n_k1 columns: the largest useful
+// lane occupancy with at most KR_QMAX pairs per lane
+int pick_rows(int nk1, int dm1) {
+  if (nk1 <= 0) return 1;
+  int best_r = 1;
+  double best_eff = -1.0;
+  for (int r = 1; r <= 32 * KR_QMAX; ++r) {
+    if (r * nk1 > 32 * KR_QMAX) break;
+    if (r > dm1) break;
+    const int q = (r * nk1 + 31) / 32;
+    const double eff = double(r * nk1) / double(32 * q);
+    if (eff > best_eff + 1e-9) {
+      best_eff = eff;
+      best_r = r;
+    }
+  }
+  return best_r;
+}
+
+}  // namespace
+
+extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
+  if (!ctx || !d || !out) return set_err(ctx, KR_ERR_ARG, "kr_op_create: NULL argument");
+  *out = nullptr;
+  KR_CUDA(ctx, cudaSetDevice(ctx->device));
+  // ---- validation -------------------------------------------------------
+  if (d->nslab_out <= 0 || d->nslab_in <= 0) return set_err(ctx, KR_ERR_ARG, "empty basis");
+  if (d->npart < 0 || d->npart > KR_MAXPART) return set_err(ctx, KR_ERR_ARG, "npart out of range");
+  if (d->maxorder < 2 || d->maxorder > KR_EXPM_MAX) return set_err(ctx, KR_ERR_ARG, "maxorder out of range [2, 128]");
+  {
+    long long off = 0;
+    for (int s = 0; s < d->nslab_out; ++s) {
+      if (d->out_off[s] != off || d->out_dm[s] <= 0 || d->out_dk[s] <= 0)
+        return set_err(ctx, KR_ERR_ARG, "malformed output slab table");
+      if (d->out_dk[s] > 32 * KR_QMAX) return set_err(ctx, KR_ERR_UNSUPPORTED, "n_k above 128 not supported");
+      off += (long long)d->out_dm[s] * d->out_dk[s];
+    }
+    if (off != d->dim_out) return set_err(ctx, KR_ERR_ARG, "dim_out does not match the slab table");
+    off = 0;
+    for (int s = 0; s < d->nslab_in; ++s) {
+      if (d->in_off[s] != off || d->in_dm[s] <= 0 || d->in_dk[s] <= 0)
+        return set_err(ctx, KR_ERR_ARG, "malformed input slab table");
+      off += (long long)d->in_dm[s] * d->in_dk[s];
+    }
+    if (off != d->dim_in) return set_err(ctx, KR_ERR_ARG, "dim_in does not match the slab table");
+  }
+  for (int g = 0; g < d->nm; ++g) {
+    if (d->m_rows[g] <= 0 || d->m_width[g] < 0 || d->m_ncart[g] < 1 || d->m_ncart[g] > KR_MAXCART)
+      return set_err(ctx, KR_ERR_ARG, "malformed M group");
+    const long long ne = (long long)d->m_rows[g] * d->m_width[g];
+    if (d->m_col_off[g] < 0 || d->m_col_off[g] + ne > d->m_col_len) return set_err(ctx, KR_ERR_ARG, "M columns out of range");
+    if (d->m_val_off[g] < 0 || d->m_val_off[g] + ne * d->m_ncart[g] > d->m_val_len / 2)
+      return set_err(ctx, KR_ERR_ARG, "M values out of range");
+  }
+  for (int i = 0; i < d->nmf; ++i)
+    if (d->mf_group[i] < 0 || d->mf_group[i] >= d->nm || d->mf_part[i] < 0 || d->mf_part[i] >= d->npart)
+      return set_err(ctx, KR_ERR_ARG, "malformed MF instance");
+  for (int b = 0; b < d->nk; ++b) {
+    const int words = d->k_type[b] == KR_K_COMPLEX ? 2 : 1;
+    if (d->k_type[b] < 0 || d->k_type[b] > 2) return set_err(ctx, KR_ERR_ARG, "bad K type");
+    if (d->k_off[b] < 0 || d->k_off[b] + (long long)d->k_rows[b] * d->k_cols[b] * words > d->k_data_len)
+      return set_err(ctx, KR_ERR_ARG, "K block out of range");
+    if (d->k_type[b] == KR_K_COMPLEX && (d->k_off[b] & 1)) return set_err(ctx, KR_ERR_ARG, "complex K block misaligned");
+  }
+  std::vector<std::vector<int>> by_out(d->nslab_out);
+  for (int t = 0; t < d->nterm; ++t) {
+    const int s1 = d->t_out[t], s2 = d->t_in[t], kb = d->t_k[t], mi = d->t_mf[t];
+    if (s1 < 0 || s1 >= d->nslab_out || s2 < 0 || s2 >= d->nslab_in || kb < 0 || kb >= d->nk || mi < 0 || mi >= d->nmf)
+      return set_err(ctx, KR_ERR_ARG, "term index out of range");
+    const int g = d->mf_group[mi];
+    if (d->k_rows[kb] != d->out_dk[s1] || d->k_cols[kb] != d->in_dk[s2])
+      return set_err(ctx, KR_ERR_ARG, "K block shape does not match its slabs");
+    if (d->m_rows[g] != d->out_dm[s1]) return set_err(ctx, KR_ERR_ARG, "M group rows do not match the output slab");
+    const long long ne = (long long)d->m_rows[g] * d->m_width[g];
+    for (long long e = 0; e < ne; ++e) {
+      const int c = d->m_col[d->m_col_off[g] + e];
+      if (c < 0 || c >= d->in_dm[s2]) return set_err(ctx, KR_ERR_ARG, "M column outside the input slab");
+    }
+    by_out[s1].push_back(t);
+  }
+
+  kr_op* op = new kr_op();
+  op->ctx = ctx;
+  op->maxorder = d->maxorder;
+  op->npart = d->npart;
+  op->nmf = d->nmf;
+  op->square = (d->nslab_out == d->nslab_in) && (d->dim_out == d->dim_in);
+  if (op->square)
+    for (int s = 0; s < d->nslab_out; ++s)
+      if (d->out_dm[s] != d->in_dm[s] || d->out_dk[s] != d->in_dk[s]) op->square = false;
+
+  // ---- terms grouped by output slab ---------------------------------------
+  std::vector<int> term_ptr(d->nslab_out + 1, 0), t_in, t_k, t_mf;
+  for (int s = 0; s < d->nslab_out; ++s) {
+    term_ptr[s + 1] = term_ptr[s] + (int)by_out[s].size();
+    for (int t : by_out[s]) {
+      t_in.push_back(d->t_in[t]);
+      t_k.push_back(d->t_k[t]);
+      t_mf.push_back(d->t_mf[t]);
+    }
+  }
+  // ---- MF instances -----------------------------------------------------------
+  std::vector<long long> inst_ptr(d->nmf + 1, 0), mf_col_off(d->nmf);
+  std::vector<int> mf_width(d->nmf);
+  for (int i = 0; i < d->nmf; ++i) {
+    const int g = d->mf_group[i];
+    inst_ptr[i + 1] = inst_ptr[i] + (long long)d->m_rows[g] * d->m_width[g];
+    mf_col_off[i] = d->m_col_off[g];
+    mf_width[i] = d->m_width[g];
+  }
+  const long long nent = inst_ptr[d->nmf];
+  std::vector<int> ent_inst(nent);
+  for (int i = 0; i < d->nmf; ++i)
+    for (long long e = inst_ptr[i]; e < inst_ptr[i + 1]; ++e) ent_inst[e] = i;
+
+  // ---- algorithmic work --------------------------------------------------
+  std::vector<long long> group_nnz(d->nm, 0);
+  for (int g = 0; g < d->nm; ++g) {
+    const long long ne = (long long)d->m_rows[g] * d->m_width[g];
+    for (long long e = 0; e < ne; ++e) {
+      bool nz = false;
+      for (int c = 0; c < d->m_ncart[g] && !nz; ++c) {
+        const double* v = d->m_val + 2 * (d->m_val_off[g] + c * ne + e);
+        nz = v[0] != 0.0 || v[1] != 0.0;
+      }
+      group_nnz[g] += nz;
+    }
+  }
+  double fma = 0.0, kbytes = 0.0, mbytes = 0.0;
+  for (int t = 0; t < d->nterm; ++t) {
+    const int s1 = d->t_out[t], s2 = d->t_in[t], kb = d->t_k[t], g = d->mf_group[d->t_mf[t]];
+    const double nk1 = d->out_dk[s1], nk2 = d->in_dk[s2], dm1 = d->out_dm[s1];
+    const double kf = d->k_type[kb] == KR_K_COMPLEX ? 4.0 : 2.0;
+    fma += 4.0 * group_nnz[g] * nk2 + kf * dm1 * nk1 * nk2;
+  }
+  for (int b = 0; b < d->nk; ++b) kbytes += 8.0 * d->k_rows[b] * d->k_cols[b] * (d->k_type[b] == KR_K_COMPLEX ? 2 : 1);
+  for (int g = 0; g < d->nm; ++g) mbytes += 20.0 * group_nnz[g];
+  op->fma_per_matvec = fma;
+  op->bytes_per_matvec = 16.0 * (d->dim_in + d->dim_out) + kbytes + mbytes;
+
+  // ---- row tasks ----------------------------------------------------------
+  std::vector<int> task_slab, task_row0, task_nrows;
+  std::vector<double> task_cost;
+  int zmax = 1;
+  for (int s = 0; s < d->nslab_out; ++s) {
+    const int nk1 = d->out_dk[s], dm1 = d->out_dm[s];
+    const int R = pick_rows(nk1, dm1);
+    int maxnk2 = 0;
+    double per_row = 8.0;
+    for (int t : by_out[s]) {
+      const int nk2 = d->in_dk[d->t_in[t]];
+      const int g = d->mf_group[d->t_mf[t]];
+      maxnk2 = std::max(maxnk2, nk2);
+      const double kf = d->k_type[d->t_k[t]] == KR_K_COMPLEX ? 4.0 : 2.0;
+      per_row += 4.0 * d->m_width[g] * nk2 + kf * nk1 * nk2 + 16.0;
+    }
+    for (int i0 = 0; i0 < dm1; i0 += R) {
+      const int nr = std::min(R, dm1 - i0);
+      task_slab.push_back(s);
+      task_row0.push_back(i0);
+      task_nrows.push_back(nr);
+      // cost in lane-slots: pairs are processed 32 at a time
+      const int q = (nr * nk1 + 31) / 32;
+      task_cost.push_back(per_row * nr * double(32 * q) / double(std::max(1, nr * nk1)));
+      zmax = std::max(zmax, nr * std::max(1, maxnk2));
+    }
+  }
+  const int ntask = (int)task_slab.size();
+  op->smem = (size_t)KR_WARPS * zmax * sizeof(double2);
+  if (op->smem > 160 * 1024) {
+    kr_op_destroy(op);
+    return set_err(ctx, KR_ERR_UNSUPPORTED, "Z staging buffer exceeds shared memory");
+  }
+  cudaFuncSetAttribute(kr_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)op->smem);
+  cudaFuncSetAttribute(kr_matvec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)op->smem);
+  int occ = 0;
+  cudaError_t ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kr_step_kernel, KR_THREADS, op->smem);
+  if (ce != cudaSuccess || occ < 1) {
+    kr_op_destroy(op);
+    return set_err(ctx, KR_ERR_CUDA, "kr_step_kernel cannot be resident");
+  }
+  int grid = ctx->nsm * std::min(occ, 1);
+  const int by_work = (ntask + KR_WARPS - 1) / KR_WARPS;
+  grid = std::max(1, std::min(grid, by_work));
+  op->grid = grid;
+  const int nwarps = grid * KR_WARPS;
+
+  // longest-processing-time assignment of tasks to warps
+  std::vector<int> order(ntask);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return task_cost[x] > task_cost[y]; });
+  using Item = std::pair<double, int>;
+  std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
+  for (int w = 0; w < nwarps; ++w) heap.push({0.0, w});
+  std::vector<std::vector<int>> wl(nwarps);
+  for (int t : order) {
+    Item it = heap.top();
+    heap.pop();
+    wl[it.second].push_back(t);
+    heap.push({it.first + task_cost[t], it.second});
+  }
+  std::vector<int> warp_task_ptr(nwarps + 1, 0), warp_tasks;
+  for (int w = 0; w < nwarps; ++w) {
+    std::sort(wl[w].begin(), wl[w].end());
+    warp_task_ptr[w + 1] = warp_task_ptr[w] + (int)wl[w].size();
+    warp_tasks.insert(warp_tasks.end(), wl[w].begin(), wl[w].end());
+  }
+
+  // ---- uploads --------------------------------------------------------------
+  DevOp& D = op->dev;
+  int rc = KR_OK;
+#define UP(host, count, dst) \
+  if ((rc = upload(op, host, count, dst)) != KR_OK) { kr_op_destroy(op); return rc; }
+  D.nslab_out = d->nslab_out;
+  D.nslab_in = d->nslab_in;
+  D.dim_out = d->dim_out;
+  D.dim_in = d->dim_in;
+  int *p_i;
+  long long* p_l;
+  UP(d->out_dm, d->nslab_out, &p_i); D.out_dm = p_i;
+  UP(d->out_dk, d->nslab_out, &p_i); D.out_dk = p_i;
+  UP((const long long*)d->out_off, d->nslab_out, &p_l); D.out_off = p_l;
+  UP(d->in_dm, d->nslab_in, &p_i); D.in_dm = p_i;
+  UP(d->in_dk, d->nslab_in, &p_i); D.in_dk = p_i;
+  UP((const long long*)d->in_off, d->nslab_in, &p_l); D.in_off = p_l;
+  UP((const long long*)d->k_off, d->nk, &p_l); D.k_off = p_l;
+  UP(d->k_rows, d->nk, &p_i); D.k_rows = p_i;
+  UP(d->k_cols, d->nk, &p_i); D.k_cols = p_i;
+  UP(d->k_type, d->nk, &p_i); D.k_type = p_i;
+  double* p_d;
+  UP(d->k_data, d->k_data_len, &p_d); D.k_data = p_d;
+  UP((const long long*)inst_ptr.data(), d->nmf, &p_l); D.mf_off = p_l;
+  UP((const long long*)mf_col_off.data(), d->nmf, &p_l); D.mf_col_off = p_l;
+  UP(mf_width.data(), d->nmf, &p_i); D.mf_width = p_i;
+  UP(d->m_col, d->m_col_len, &p_i); D.m_col = p_i;
+  double2* p_c;
+  UP((const double2*)nullptr, nent, &p_c); D.mf_val = p_c;
+  UP(term_ptr.data(), term_ptr.size(), &p_i); D.term_ptr = p_i;
+  UP(t_in.data(), t_in.size(), &p_i); D.t_in = p_i;
+  UP(t_k.data(), t_k.size(), &p_i); D.t_k = p_i;
+  UP(t_mf.data(), t_mf.size(), &p_i); D.t_mf = p_i;
+  UP(task_slab.data(), ntask, &p_i); D.task_slab = p_i;
+  UP(task_row0.data(), ntask, &p_i); D.task_row0 = p_i;
+  UP(task_nrows.data(), ntask, &p_i); D.task_nrows = p_i;
+  UP(warp_task_ptr.data(), warp_task_ptr.size(), &p_i); D.warp_task_ptr = p_i;
+  UP(warp_tasks.data(), warp_tasks.size(), &p_i); D.warp_tasks = p_i;
+  D.zmax = zmax;
+
+  DevField& F = op->field;
+  F.nent = nent;
+  UP(ent_inst.data(), nent, &p_i); F.ent_inst = p_i;
+  F.inst_ptr = D.mf_off;
+  UP(d->mf_group, d->nmf, &p_i); F.mf_group = p_i;
+  UP(d->mf_part, d->nmf, &p_i); F.mf_part = p_i;
+  UP((const long long*)d->m_val_off, d->nm, &p_l); F.m_val_off = p_l;
+  UP(d->m_ncart, d->nm, &p_i); F.m_ncart = p_i;
+  UP(d->m_rows, d->nm, &p_i); F.m_rows = p_i;
+  UP(d->m_width, d->nm, &p_i); F.m_width = p_i;
+  UP((const double2*)d->m_val, d->m_val_len / 2, &p_c); F.m_val = p_c;
+  F.mf_val = D.mf_val;
+
+  // ---- step scratch (sized once: kr_step allocates nothing) -----------------
+  if (op->square) {
+    const long long n = d->dim_out;
+    UP((const double2*)nullptr, (size_t)n * d->maxorder, &p_c); op->V = p_c;
+    UP((const double2*)nullptr, (size_t)n, &p_c); op->Wb0 = p_c;
+    UP((const double2*)nullptr, (size_t)n, &p_c); op->Wb1 = p_c;
+    UP((const double2*)nullptr, (size_t)n, &p_c); op->w = p_c;
+    UP((const double2*)nullptr, (size_t)n, &p_c); op->ub0 = p_c;
+    UP((const double2*)nullptr, (size_t)n, &p_c); op->ub1 = p_c;
+    UP((const double2*)nullptr, (size_t)grid, &p_c); op->part_a = p_c;
+    UP((const double*)nullptr, (size_t)grid, &p_d); op->part_b = p_d;
+    UP((const double*)nullptr, (size_t)grid, &p_d); op->part_c = p_d;
+    UP((const double2*)nullptr, (size_t)d->maxorder + 1, &p_c); op->alpha = p_c;
+    UP((const double*)nullptr, (size_t)d->maxorder + 1, &p_d); op->beta = p_d;
+    unsigned* p_u;
+    UP((const unsigned*)nullptr, 2, &p_u); op->bar = p_u;
+    UP((const int*)nullptr, 2, &p_i); op->status = p_i;
+  }
+#undef UP
+  KR_CUDA(ctx, cudaDeviceSynchronize());
+  *out = op;
+  return KR_OK;
+}
+
+extern "C" int kr_set_field(kr_op* op, const double* coef, const double* scale, const double* thresh, void* stream) {
+  if (!op || !coef || !scale || !thresh) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_set_field: NULL argument");
+  FieldCoef c;
+  std::memset(&c, 0, sizeof(c));
+  c.npart = op->npart;
+  for (int p = 0; p < op->npart; ++p) {
+    for (int ci = 0; ci < KR_MAXCART; ++ci)
+      c.coef[p][ci] = make_double2(coef[2 * (p * KR_MAXCART + ci)], coef[2 * (p * KR_MAXCART + ci) + 1]);
+    c.scale[p] = make_double2(scale[2 * p], scale[2 * p + 1]);
+    c.thresh[p] = thresh[p];
+  }
+  if (op->field.nent == 0) return KR_OK;
+  const int threads = 256;
+  const int blocks = (int)std::min<long long>((op->field.nent + threads - 1) / threads, 4LL * op->ctx->nsm);
+  kr_field_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(op->field, c);
+  op->launches++;
+  KR_CUDA(op->ctx, cudaGetLastError());
+  return KR_OK;
+}
+
+extern "C" int kr_matvec(kr_op* op, const void* x, void* y, int64_t nvec, void* stream) {
+  if (!op || !x || !y || nvec < 0) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_matvec: bad argument");
+  if (nvec == 0) return KR_OK;
+  if (nvec > 65535) return set_err(op->ctx, KR_ERR_ARG, "kr_matvec: nvec above 65535");
+  dim3 g(op->grid, (unsigned)nvec);
+  kr_matvec_kernel<<<g, KR_THREADS, op->smem, (cudaStream_t)stream>>>(op->dev, (const double2*)x, (double2*)y);
+  op->launches++;
+  KR_CUDA(op->ctx, cudaGetLastError());
+  return KR_OK;
+}
+
+extern "C" int kr_step(kr_op* op, void* states, int64_t nvec, const void* phase, double fac_re, double fac_im,
+                       double tol, uint32_t flags, int32_t* korder, void* stream) {
+  if (!op || !states || nvec < 0) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_step: bad argument");
+  if (!op->square) return set_err(op->ctx, KR_ERR_ARG, "kr_step: operator is not square (bra basis != ket basis)");
+  if (nvec == 0) return KR_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long n = op->dev.dim_out;
+  if (flags & KR_STEP_SKIP_KRYLOV) {
+    if (phase) {
+      const int blocks = (int)std::min<long long>((n * nvec + 255) / 256, 8LL * op->ctx->nsm);
+      kr_phase2_kernel<<<blocks, 256, 0, st>>>((double2*)states, (const double2*)phase, n, nvec);
+      op->launches++;
+      KR_CUDA(op->ctx, cudaGetLastError());
+    }
+    if (korder)
+      for (int64_t v = 0; v < nvec; ++v) korder[v] = 0;
+    return KR_OK;
+  }
+  StepArgs a;
+  a.op = op->dev;
+  a.phase = (const double2*)phase;
+  a.V = op->V;
+  a.Wb[0] = op->Wb0;
+  a.Wb[1] = op->Wb1;
+  a.w = op->w;
+  a.ub[0] = op->ub0;
+  a.ub[1] = op->ub1;
+  a.part_a = op->part_a;
+  a.part_b = op->part_b;
+  a.part_c = op->part_c;
+  a.alpha = op->alpha;
+  a.beta = op->beta;
+  a.bar_count = op->bar;
+  a.bar_gen = op->bar + 1;
+  a.status = op->status;
+  a.kout = op->status + 1;
+  a.fac = make_double2(fac_re, fac_im);
+  a.tol = tol;
+  a.maxorder = op->maxorder;
+  a.dim = n;
+  for (int64_t v = 0; v < nvec; ++v) {
+    a.state = (double2*)states + v * n;
+    KR_CUDA(op->ctx, cudaMemsetAsync(op->bar, 0, sizeof(unsigned), st));  // arrival count only
+    void* args[] = {&a};
+    KR_CUDA(op->ctx, cudaLaunchCooperativeKernel((void*)kr_step_kernel, dim3(op->grid), dim3(KR_THREADS), args,
+                                                 op->smem, st));
+    op->launches++;
+    if (korder) {
+      int hs[2] = {0, 0};
+      KR_CUDA(op->ctx, cudaMemcpyAsync(hs, op->status, sizeof(hs), cudaMemcpyDeviceToHost, st));
+      KR_CUDA(op->ctx, cudaStreamSynchronize(st));
+      korder[v] = hs[1];
+      if (hs[0] != 0) {
+        cudaMemsetAsync(op->status, 0, sizeof(int), st);
+        cudaStreamSynchronize(st);
+        if (hs[0] == KR_ERR_MAXORDER)
+          return set_err(op->ctx, KR_ERR_MAXORDER,
+                         "Lanczos reached maximum order of '" + std::to_string(op->maxorder) + "' without convergence");
+        return set_err(op->ctx, hs[0], "device-side wait gave up (grid barrier timeout)");
+      }
+    }
+  }
+  return KR_OK;
+}
+
+extern "C" int kr_sync_status(kr_op* op, void* stream) {
+  if (!op) return set_err(nullptr, KR_ERR_ARG, "kr_sync_status: NULL op");
+  cudaStream_t st = (cudaStream_t)stream;
+  KR_CUDA(op->ctx, cudaStreamSynchronize(st));
+  KR_CUDA(op->ctx, cudaGetLastError());
+  if (!op->status) return KR_OK;
+  int hs = 0;
+  KR_CUDA(op->ctx, cudaMemcpy(&hs, op->status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (hs != 0) {
+    cudaMemset(op->status, 0, sizeof(int));
+    if (hs == KR_ERR_MAXORDER)
+      return set_err(op->ctx, KR_ERR_MAXORDER,
+                     "Lanczos reached maximum order of '" + std::to_string(op->maxorder) + "' without convergence");
+    return set_err(op->ctx, hs, "device-side wait gave up (grid barrier timeout)");
+  }
+  return KR_OK;
+}
+
+extern "C" int64_t kr_op_launch_count(const kr_op* op) { return op ? op->launches : -1; }
+
+extern "C" int kr_op_work(const kr_op* op, double* fma_per_matvec, double* bytes_per_matvec) {
+  if (!op) return KR_ERR_ARG;
+  if (fma_per_matvec) *fma_per_matvec = op->fma_per_matvec;
+  if (bytes_per_matvec) *bytes_per_matvec = op->bytes_per_matvec;
+  return KR_OK;
+}

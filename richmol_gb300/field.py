@@ -1,0 +1,377 @@
+"""CarTens: laboratory-frame Cartesian tensor operator, GPU drop-in for
+richmol.field.CarTens (CFEL-CMI/richmol, richmol/field.py:25-1301).
+
+The attribute surface follows the reference (Jlist1/2, symlist1/2, dim_m1/2,
+dim_k1/2, dim1/2, kmat, mmat, mfmat, rank, cart) and so do the operations on
+the propagation path:
+
+* ``field(E, thresh)``  records the field products (field.py:1094-1105); the
+  contraction MF = sum_c E_c M_c happens on the GPU at the next product;
+* ``vec(vec)``          the Kronecker mat-vec on the GPU (field.py:1145-1245);
+* ``tomat``             host (scipy) assembly for set-up and observables
+                        (field.py:449-569);
+* ``*``, ``+``, ``-``   scalar and field multiplication and sums
+                        (field.py:932-1070, 1248-1301).
+
+Internally a tensor is a list of parts, one per factor source, each with its
+K scale and field state; a sum concatenates the parts (the reference renames
+irreps '<w>_1', '<w>_2' and snapshots mfmat, field.py:1012-1068). Factor
+sources are immutable and their device copies are shared by every operator
+built from them.
+"""
+import copy
+import itertools
+from collections import defaultdict
+from collections.abc import Mapping
+
+import numpy as np
+import scipy.sparse
+from scipy.sparse import csr_matrix, kron
+
+from . import io as _io
+
+_SCALAR = (int, float, complex, np.integer, np.floating, np.complexfloating)
+
+CART_INDEX = {
+    1: ["x", "y", "z"],
+    2: ["xx", "xy", "xz", "yx", "yy", "yz", "zx", "zy", "zz"],
+}
+
+
+def _nested():
+    return defaultdict(_nested)
+
+
+class FactorSource:
+    """Immutable factor blocks of one tensor: bases, kmat, mmat, rank, cart."""
+
+    def __init__(self, basis, kmat, mmat, rank, carts):
+        for k, v in basis.items():
+            setattr(self, k, v)
+        for side in ("1", "2"):
+            dm = getattr(self, "dim_m" + side)
+            dk = getattr(self, "dim_k" + side)
+            setattr(self, "dim" + side, {J: {s: dm[J][s] * dk[J][s] for s in dm[J]} for J in dm})
+        self.kmat = kmat
+        self.mmat = mmat
+        self.rank = rank
+        self.carts = list(carts)
+
+    def basis(self, side):
+        Jl = getattr(self, "Jlist" + side)
+        sl = getattr(self, "symlist" + side)
+        dm = getattr(self, "dim_m" + side)
+        dk = getattr(self, "dim_k" + side)
+        return [(J, s, int(dm[J][s]), int(dk[J][s])) for J in Jl for s in sl[J]]
+
+
+class _Part:
+    __slots__ = ("src", "kscale", "prods", "thresh")
+
+    def __init__(self, src, kscale=1.0, prods=None, thresh=None):
+        self.src = src
+        self.kscale = kscale
+        self.prods = prods      # field products {cart: value} after field(); None before
+        self.thresh = thresh
+
+
+# plan cache: tuple of factor sources -> OperatorPlan (strong references keep
+# the sources alive while their plan exists)
+_PLANS = {}
+
+
+def clear_plan_cache():
+    _PLANS.clear()
+
+
+class CarTens:
+    """GPU drop-in for richmol.field.CarTens on the propagation path.
+
+    Args:
+        filename : str   factor file (``.npz``, see richmol_gb300.io)
+        name : str       tensor name inside the file
+    """
+
+    def __init__(self, filename=None, name=None, **kwargs):
+        self._parts = []
+        self._is_sum = False
+        if filename is not None:
+            if name is None:
+                raise ValueError(f"please specify the name of the data group in file '{filename}'")
+            basis, kmat, mmat, mfmat, rank, cart = _io.read_tensor(filename, name)
+            if not mmat and mfmat is not None:
+                # stored field-contracted operator: a frozen single-component source
+                mmat = _nested()
+                for Jp, mJ in mfmat.items():
+                    for sp, mS in mJ.items():
+                        for irrep, m in mS.items():
+                            mmat[Jp][sp][irrep]["0"] = m
+                rank, cart = 0, ["0"]
+            self._init_source(FactorSource(basis, kmat, mmat, rank, cart))
+
+    @classmethod
+    def from_factors(cls, basis, kmat, mmat, rank, cart):
+        T = cls()
+        T._init_source(FactorSource(basis, kmat, mmat, rank, cart))
+        return T
+
+    def _init_source(self, src):
+        self._parts = [_Part(src)]
+        self._is_sum = False
+
+    # ------------------------------------------------------------------
+    # reference attributes
+    # ------------------------------------------------------------------
+    def _first(self):
+        if not self._parts:
+            raise AttributeError("empty CarTens")
+        return self._parts[0].src
+
+    def __getattr__(self, name):
+        if name in ("Jlist1", "Jlist2", "symlist1", "symlist2", "dim_m1", "dim_m2", "dim_k1", "dim_k2",
+                    "dim1", "dim2"):
+            return getattr(self._first(), name)
+        if name in ("rank", "cart", "mmat") and not self.__dict__.get("_is_sum", False):
+            src = self._first()
+            return {"rank": src.rank, "cart": src.carts, "mmat": src.mmat}[name]
+        if name == "kmat":
+            return self._kmat()
+        if name == "mfmat":
+            return self._mfmat()
+        raise AttributeError(f"'{type(self).__name__}' object has no attribute '{name}'")
+
+    def _single_source(self):
+        if self._is_sum or len(self._parts) != 1:
+            raise AttributeError("operation needs a single (non-sum) tensor")
+        return self._parts[0].src
+
+    def _irrep_name(self, irrep, p):
+        return f"{irrep}_{p + 1}" if self._is_sum else irrep
+
+    def _kmat(self):
+        res = _nested()
+        for p, part in enumerate(self._parts):
+            for Jp, kJ in part.src.kmat.items():
+                for sp, kS in kJ.items():
+                    for irrep, km in kS.items():
+                        res[Jp][sp][self._irrep_name(irrep, p)] = km * part.kscale
+        return res
+
+    def _mfmat(self):
+        if not self._is_sum and self._parts[0].prods is None:
+            raise AttributeError("'CarTens' object has no attribute 'mfmat' (call field() first)")
+        res = _nested()
+        for p, part in enumerate(self._parts):
+            if part.prods is None:
+                continue
+            for Jp, mJ in part.src.mmat.items():
+                for sp, mS in mJ.items():
+                    blk = {}
+                    for irrep, mI in mS.items():
+                        mats = [part.prods[c] * mI[c].toarray() for c in set(mI.keys()) & set(part.prods.keys())]
+                        if not mats:
+                            continue
+                        mat = csr_matrix(sum(mats)) if len(mats) > 1 else csr_matrix(mats[0])
+                        if part.thresh is not None and part.thresh > 0:
+                            mat.data[np.abs(mat.data) < part.thresh] = 0
+                            mat.eliminate_zeros()
+                        if mat.nnz > 0:
+                            blk[self._irrep_name(irrep, p)] = mat
+                    if blk:
+                        res[Jp][sp].update(blk)
+        return res
+
+    # ------------------------------------------------------------------
+    # field.py:1073-1142
+    # ------------------------------------------------------------------
+    def field(self, field, thresh=None):
+        """In-place multiplication with the field (E_x, E_y, E_z)."""
+        if self._is_sum:
+            raise AttributeError("'CarTens' sum has no attribute 'rank' (field() needs a single tensor)")
+        try:
+            fx, fy, fz = field[:3]
+            fxyz = np.array([fx, fy, fz])
+        except (TypeError, IndexError):
+            raise IndexError("field variable must be an iterable with three items which represent "
+                             "field's X, Y, and Z components") from None
+        src = self._parts[0].src
+        prods = {"".join("xyz"[c] for c in comb): np.prod(fxyz[list(comb)])
+                 for comb in itertools.product((0, 1, 2), repeat=src.rank)}
+        prods["0"] = 1
+        if thresh is not None:
+            prods = {k: v for k, v in prods.items() if abs(v) >= thresh}
+        self._parts[0].prods = prods
+        self._parts[0].thresh = thresh
+
+    def _has_field_terms(self):
+        """True when the operator carries a non-zero field product for a
+        Cartesian component present in its M factors (len(mfmat) > 0 of
+        tdse.py:377, up to blocks whose elements all fall below thresh, which
+        contribute an exact zero)."""
+        for part in self._parts:
+            if part.prods is None:
+                continue
+            if any(v != 0 and c in part.src.carts for c, v in part.prods.items()):
+                return True
+        return False
+
+    # ------------------------------------------------------------------
+    # algebra: field.py:932-1070, 1248-1301
+    # ------------------------------------------------------------------
+    def mul(self, arg):
+        if not isinstance(arg, _SCALAR):
+            raise TypeError(f"bad argument type for `arg` : '{type(arg)}'")
+        for part in self._parts:
+            part.kscale = part.kscale * arg
+
+    def _copy(self):
+        res = CarTens()
+        res._parts = [_Part(p.src, p.kscale, None if p.prods is None else dict(p.prods), p.thresh)
+                      for p in self._parts]
+        res._is_sum = self._is_sum
+        return res
+
+    def __mul__(self, arg):
+        if isinstance(arg, _SCALAR):
+            res = self._copy()
+            res.mul(arg)
+        elif isinstance(arg, (np.ndarray, list, tuple)):
+            res = self._copy()
+            res.field(arg)
+        elif isinstance(arg, dict):
+            return self.vec(arg)
+        else:
+            raise TypeError(f"unsupported operand type(s) for '*': 'CarTens' and '{type(arg)}'")
+        return res
+
+    __rmul__ = __mul__
+
+    def __add__(self, arg):
+        if not isinstance(arg, CarTens):
+            raise TypeError(f"unsupported operand type(s) for '+': 'CarTens' and '{type(arg)}'")
+        for attr in ("Jlist1", "Jlist2", "symlist1", "symlist2", "dim1", "dim2", "dim_k1", "dim_k2",
+                     "dim_m1", "dim_m2"):
+            if getattr(self, attr) != getattr(arg, attr):
+                raise ValueError("tensors defined with respect to different basis sets")
+        for T in (self, arg):  # field.py:995-1004: H0-type tensors get field([0,0,1])
+            if not T._is_sum and T._parts[0].src.carts[0] == "0":
+                T.field([0, 0, 1])
+        res = CarTens()
+        res._parts = self._copy()._parts + arg._copy()._parts
+        res._is_sum = True
+        return res
+
+    __radd__ = __add__
+
+    def __sub__(self, arg):
+        if not isinstance(arg, CarTens):
+            raise TypeError(f"unsupported operand type(s) for '-': 'CarTens' and '{type(arg)}'")
+        return self.__add__(arg * (-1))
+
+    # ------------------------------------------------------------------
+    # GPU operator
+    # ------------------------------------------------------------------
+    def _plan(self, maxorder=100):
+        from .plan import OperatorPlan
+        key = (tuple(id(p.src) for p in self._parts), int(maxorder))
+        plan = _PLANS.get(key)
+        if plan is None:
+            src0 = self._parts[0].src
+            plan = OperatorPlan([p.src for p in self._parts], src0.basis("1"), src0.basis("2"), maxorder=maxorder)
+            _PLANS[key] = plan
+        return plan
+
+    def _part_states(self):
+        return [((p.prods or {}), p.kscale, p.thresh) for p in self._parts]
+
+    def device_operator(self, maxorder=100, stream=None):
+        """The OperatorPlan of this tensor with the current field applied."""
+        if not self._is_sum and self._parts[0].prods is None:
+            raise AttributeError("you need to multiply tensor with field before applying it to a vector")
+        plan = self._plan(maxorder)
+        plan.set_field(self._part_states(), stream)
+        return plan
+
+    def vec_device(self, x, out=None, stream=None):
+        """y = H x for complex128 CUDA tensors x (nvec, dim2) -> (nvec, dim1)."""
+        import torch
+        plan = self.device_operator(stream=stream)
+        x2 = x if x.dim() == 2 else x.reshape(1, -1)
+        if out is None:
+            out = torch.empty((x2.shape[0], plan.dim_out), dtype=torch.complex128, device=x.device)
+        plan.matvec(x2.contiguous(), out, stream)
+        return out if x.dim() == 2 else out.reshape(-1)
+
+    def vec(self, vec, matvec_lib="scipy"):
+        """Product with a {J: {sym: array}} vector (field.py:1145-1245) on the GPU."""
+        import torch
+        if not isinstance(vec, Mapping):
+            raise TypeError(f"bad argument type for `vec`: '{type(vec)}'")
+        assert matvec_lib in ["scipy", "numba", "cupy"], \
+            f"bad argument for `matvec_lib`: '{matvec_lib}' (must be 'scipy', 'numba', 'cupy')"
+        src = self._parts[0].src
+        x = np.concatenate([
+            np.asarray(vec[J][s], dtype=np.complex128).reshape(-1) if (J in vec and s in vec[J])
+            else np.zeros(src.dim2[J][s], np.complex128)
+            for J in src.Jlist2 for s in src.symlist2[J]])
+        xd = torch.from_numpy(x).cuda()
+        y = self.vec_device(xd).cpu().numpy()
+        out, ind = {}, 0
+        for J in src.Jlist1:
+            for s in src.symlist1[J]:
+                n = src.dim1[J][s]
+                out.setdefault(J, {})[s] = y[ind: ind + n]
+                ind += n
+        return out
+
+    # ------------------------------------------------------------------
+    # field.py:449-569, 659-695 (host assembly)
+    # ------------------------------------------------------------------
+    def tomat(self, form="block", repres="csr_matrix", thresh=None, cart=None):
+        assert form in ("block", "full"), f"`form` unknown: '{form}' (use 'block', 'full')"
+        blocks = {}
+        if cart is None:
+            mf = self.mfmat
+            km = self.kmat
+            for Jp in set(mf.keys()) & set(km.keys()):
+                for sp in set(mf[Jp].keys()) & set(km[Jp].keys()):
+                    me = sum(kron(mf[Jp][sp][i], km[Jp][sp][i]) for i in set(mf[Jp][sp]) & set(km[Jp][sp]))
+                    if not np.isscalar(me):
+                        blocks[(Jp, sp)] = me
+        else:
+            src = self._single_source()
+            if cart not in src.carts:
+                raise ValueError(f"specified Cartesian component '{cart}' is not contained in tensor "
+                                 f"components '{src.carts}'")
+            km = self.kmat
+            for Jp in set(src.mmat.keys()) & set(km.keys()):
+                for sp in set(src.mmat[Jp].keys()) & set(km[Jp].keys()):
+                    mm = {i: v[cart] for i, v in src.mmat[Jp][sp].items() if cart in v}
+                    me = sum(kron(mm[i], km[Jp][sp][i]) for i in set(mm) & set(km[Jp][sp]))
+                    if not np.isscalar(me):
+                        blocks[(Jp, sp)] = me
+        if thresh is not None and thresh > 0:
+            for key, m in blocks.items():
+                m = m.tocsr()
+                m.data[np.abs(m.data) <= thresh] = 0
+                m.eliminate_zeros()
+                blocks[key] = m
+        src = self._parts[0].src
+        if form == "block":
+            res = _nested()
+            for ((J1, J2), (s1, s2)), m in blocks.items():
+                res[(J1, J2)][(s1, s2)] = m.toarray() if repres == "dense" else getattr(scipy.sparse, repres)(m)
+            return res
+        rows = [(J, s) for J in src.Jlist1 for s in src.symlist1[J]]
+        cols = [(J, s) for J in src.Jlist2 for s in src.symlist2[J]]
+        full = scipy.sparse.bmat([
+            [blocks[((J1, J2), (s1, s2))] if ((J1, J2), (s1, s2)) in blocks
+             else csr_matrix((src.dim1[J1][s1], src.dim2[J2][s2]), dtype=np.complex128)
+             for (J2, s2) in cols] for (J1, s1) in rows])
+        if repres == "dense":
+            return full.toarray()
+        return getattr(scipy.sparse, repres)(full)
+
+    def store(self, filename, name):
+        """Writes the factors (K scale applied) to a factor file."""
+        _io.write_tensors(filename, {name: self})

@@ -1,0 +1,275 @@
+"""Compilation of CarTens factors into the device tables of one kr_op.
+
+A CarTens operator is a sum of parts; each part is one factor source (the
+kmat/mmat blocks of a tensor, field.py:58-170) with a K scale and a field
+state. The device operator holds, per source,
+
+* every K block  K[(J1,J2)][(s1,s2)][irrep]  as a dense n_k1 x n_k2 matrix,
+  stored real, imaginary or complex (D2 blocks are purely one or the other);
+* every M block set {cart: M[(J1,J2)][(s1,s2)][irrep][cart]} as one "group"
+  in ELL form over the union sparsity pattern of its Cartesian components,
+  de-duplicated by content (symmetry pairs share identical M blocks);
+
+and, per part, one MF instance for each group it uses. Terms are the
+(J1,s1) <- (J2,s2) products of field.py:1212-1243 present in both kmat and mmat.
+"""
+import ctypes
+import hashlib
+
+import numpy as np
+import torch
+
+from . import _native
+from .device import context, stream_ptr
+
+
+def _dense(m):
+    return np.asarray(m.toarray() if hasattr(m, "toarray") else m, dtype=np.complex128)
+
+
+def _ktype(K):
+    if not np.any(K.imag):
+        return _native.KR_K_REAL, np.ascontiguousarray(K.real)
+    if not np.any(K.real):
+        return _native.KR_K_IMAG, np.ascontiguousarray(K.imag)
+    return _native.KR_K_COMPLEX, np.ascontiguousarray(K).view(np.float64)
+
+
+def _ell(mats, nrows, ncols):
+    """Union-pattern ELL of a list of sparse matrices with equal shapes.
+    Returns (width, col[nrows*width] int32, val[ncart, nrows*width] complex)."""
+    coos = [m.tocoo() for m in mats]
+    rows = np.concatenate([c.row for c in coos]).astype(np.int64) if coos else np.zeros(0, np.int64)
+    cols = np.concatenate([c.col for c in coos]).astype(np.int64) if coos else np.zeros(0, np.int64)
+    keys = np.unique(rows * ncols + cols)
+    urow, ucol = keys // ncols, keys % ncols
+    counts = np.bincount(urow, minlength=nrows)
+    width = int(counts.max()) if len(keys) else 0
+    start = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    pos = np.arange(len(keys)) - start[urow]
+    slot = urow * width + pos
+    col = np.zeros(nrows * width, dtype=np.int32)
+    col[slot] = ucol
+    val = np.zeros((len(mats), nrows * width), dtype=np.complex128)
+    for ci, c in enumerate(coos):
+        idx = np.searchsorted(keys, c.row.astype(np.int64) * ncols + c.col)
+        np.add.at(val[ci], slot[idx], c.data)
+    return width, col, val
+
+
+class CompiledSource:
+    """Device-ready blocks of one factor source (cached on the source)."""
+
+    def __init__(self, src):
+        self.carts = list(src.carts)
+        cidx = {c: i for i, c in enumerate(self.carts)}
+        self.kblocks = []   # (ktype, data)
+        self.kshape = []
+        self.groups = []    # (rows, width, ncart, col, val)
+        self.terms = []     # (J1, s1, J2, s2, kidx, gidx)
+        gkey = {}
+        for (J1, J2), kJ in src.kmat.items():
+            mJ = src.mmat.get((J1, J2)) if hasattr(src.mmat, "get") else src.mmat[(J1, J2)]
+            if not mJ:
+                continue
+            for (s1, s2), kS in kJ.items():
+                mS = mJ.get((s1, s2))
+                if not mS:
+                    continue
+                for irrep, km in kS.items():
+                    mI = mS.get(irrep)
+                    if not mI:
+                        continue
+                    K = _dense(km)
+                    kt, kd = _ktype(K)
+                    kidx = len(self.kblocks)
+                    self.kblocks.append((kt, kd))
+                    self.kshape.append(K.shape)
+                    mats = [None] * len(self.carts)
+                    shape = None
+                    for cart, mm in mI.items():
+                        mats[cidx[cart]] = mm
+                        shape = mm.shape
+                    from scipy.sparse import csr_matrix
+                    mats = [m if m is not None else csr_matrix(shape, dtype=np.complex128) for m in mats]
+                    width, col, val = _ell(mats, shape[0], shape[1])
+                    h = hashlib.sha1()
+                    h.update(np.array([shape[0], shape[1], width], np.int64).tobytes())
+                    h.update(col.tobytes())
+                    h.update(val.tobytes())
+                    key = h.digest()
+                    if key not in gkey:
+                        gkey[key] = len(self.groups)
+                        self.groups.append((shape[0], width, len(self.carts), col, val))
+                    self.terms.append((J1, s1, J2, s2, kidx, gkey[key]))
+
+
+def compiled(src):
+    c = getattr(src, "_compiled", None)
+    if c is None:
+        c = CompiledSource(src)
+        src._compiled = c
+    return c
+
+
+class OperatorPlan:
+    """One kr_op: the device tables for a tuple of factor sources."""
+
+    def __init__(self, sources, basis_out, basis_in, maxorder=100, device=None):
+        if len(sources) > _native.KR_MAXPART:
+            raise ValueError(f"at most {_native.KR_MAXPART} operator parts are supported")
+        self.ctx = context(device)
+        self.sources = list(sources)
+        L = _native.lib()
+        slabs_out = [(J, s) for J, s, _, _ in basis_out]
+        slabs_in = [(J, s) for J, s, _, _ in basis_in]
+        sidx_out = {k: i for i, k in enumerate(slabs_out)}
+        sidx_in = {k: i for i, k in enumerate(slabs_in)}
+        out_dm = np.array([b[2] for b in basis_out], np.int32)
+        out_dk = np.array([b[3] for b in basis_out], np.int32)
+        in_dm = np.array([b[2] for b in basis_in], np.int32)
+        in_dk = np.array([b[3] for b in basis_in], np.int32)
+        out_off = np.concatenate([[0], np.cumsum(out_dm.astype(np.int64) * out_dk)[:-1]]).astype(np.int64)
+        in_off = np.concatenate([[0], np.cumsum(in_dm.astype(np.int64) * in_dk)[:-1]]).astype(np.int64)
+        self.dim_out = int((out_dm.astype(np.int64) * out_dk).sum())
+        self.dim_in = int((in_dm.astype(np.int64) * in_dk).sum())
+
+        k_off, k_rows, k_cols, k_type, k_data = [], [], [], [], []
+        m_rows, m_width, m_ncart, m_col_off, m_val_off, m_col, m_val = [], [], [], [], [], [], []
+        mf_group, mf_part = [], []
+        t_out, t_in, t_k, t_mf = [], [], [], []
+        koff = 0
+        coff = 0
+        voff = 0
+        src_base = {}
+        self.part_carts = []
+        for p, src in enumerate(self.sources):
+            cs = compiled(src)
+            self.part_carts.append(cs.carts)
+            if id(src) not in src_base:
+                kb0, g0 = len(k_type), len(m_rows)
+                for (kt, kd), (r, c) in zip(cs.kblocks, cs.kshape):
+                    if kt == _native.KR_K_COMPLEX and koff % 2:
+                        k_data.append(np.zeros(1))
+                        koff += 1
+                    k_off.append(koff)
+                    k_rows.append(r)
+                    k_cols.append(c)
+                    k_type.append(kt)
+                    flat = np.ascontiguousarray(kd, dtype=np.float64).reshape(-1)
+                    k_data.append(flat)
+                    koff += flat.size
+                for rows, width, ncart, col, val in cs.groups:
+                    m_rows.append(rows)
+                    m_width.append(width)
+                    m_ncart.append(ncart)
+                    m_col_off.append(coff)
+                    m_val_off.append(voff)
+                    m_col.append(col)
+                    m_val.append(val.reshape(-1))
+                    coff += col.size
+                    voff += val.size
+                src_base[id(src)] = (kb0, g0)
+            kb0, g0 = src_base[id(src)]
+            inst = {}
+            for J1, s1, J2, s2, kidx, gidx in cs.terms:
+                if (J1, s1) not in sidx_out or (J2, s2) not in sidx_in:
+                    continue
+                g = g0 + gidx
+                if g not in inst:
+                    inst[g] = len(mf_group)
+                    mf_group.append(g)
+                    mf_part.append(p)
+                t_out.append(sidx_out[(J1, s1)])
+                t_in.append(sidx_in[(J2, s2)])
+                t_k.append(kb0 + kidx)
+                t_mf.append(inst[g])
+
+        A = lambda x, dt: np.ascontiguousarray(np.array(x, dtype=dt).reshape(-1))
+        cat = lambda xs, dt: np.ascontiguousarray(np.concatenate(xs).astype(dt)) if xs else np.zeros(1, dt)
+        keep = dict(
+            out_dm=out_dm, out_dk=out_dk, out_off=out_off, in_dm=in_dm, in_dk=in_dk, in_off=in_off,
+            k_off=A(k_off, np.int64), k_rows=A(k_rows, np.int32), k_cols=A(k_cols, np.int32),
+            k_type=A(k_type, np.int32), k_data=cat(k_data, np.float64),
+            m_rows=A(m_rows, np.int32), m_width=A(m_width, np.int32), m_ncart=A(m_ncart, np.int32),
+            m_col_off=A(m_col_off, np.int64), m_val_off=A(m_val_off, np.int64),
+            m_col=cat(m_col, np.int32), m_val=cat(m_val, np.complex128).view(np.float64),
+            mf_group=A(mf_group, np.int32), mf_part=A(mf_part, np.int32),
+            t_out=A(t_out, np.int32), t_in=A(t_in, np.int32), t_k=A(t_k, np.int32), t_mf=A(t_mf, np.int32),
+        )
+        d = _native.kr_op_desc()
+        d.nslab_out, d.nslab_in = len(slabs_out), len(slabs_in)
+        for f in ("out_dm", "out_dk", "out_off", "in_dm", "in_dk", "in_off", "k_off", "k_rows", "k_cols",
+                  "k_type", "k_data", "m_rows", "m_width", "m_ncart", "m_col_off", "m_val_off", "m_col",
+                  "m_val", "mf_group", "mf_part", "t_out", "t_in", "t_k", "t_mf"):
+            setattr(d, f, keep[f].ctypes.data)
+        d.dim_out, d.dim_in = self.dim_out, self.dim_in
+        d.nk = len(k_type)
+        d.k_data_len = keep["k_data"].size if k_data else 0
+        d.nm = len(m_rows)
+        d.m_col_len = keep["m_col"].size if m_col else 0
+        d.m_val_len = keep["m_val"].size if m_val else 0
+        d.npart = len(self.sources)
+        d.nmf = len(mf_group)
+        d.nterm = len(t_out)
+        d.maxorder = int(maxorder)
+        self.nterm = len(t_out)
+        self.maxorder = int(maxorder)
+        h = ctypes.c_void_p()
+        _native.check(L.kr_op_create(self.ctx, ctypes.byref(d), ctypes.byref(h)), self.ctx)
+        self.op = h
+        self._coef = np.zeros((_native.KR_MAXPART, _native.KR_MAXCART), np.complex128)
+        self._scale = np.zeros(_native.KR_MAXPART, np.complex128)
+        self._thresh = np.zeros(_native.KR_MAXPART, np.float64)
+
+    def __del__(self):
+        op = getattr(self, "op", None)
+        if op:
+            try:
+                _native.lib().kr_op_destroy(op)
+            except Exception:
+                pass
+            self.op = None
+
+    # ------------------------------------------------------------------
+    def set_field(self, part_states, stream=None):
+        """part_states: per part (field_prod dict cart -> value, K scale, thresh)."""
+        self._coef[:] = 0
+        for p, (prods, scale, thresh) in enumerate(part_states):
+            carts = self.part_carts[p]
+            for ci, c in enumerate(carts):
+                v = prods.get(c)
+                if v is not None:
+                    self._coef[p, ci] = v
+            self._scale[p] = scale
+            self._thresh[p] = 0.0 if thresh is None else float(thresh)
+        _native.check(_native.lib().kr_set_field(
+            self.op, self._coef.ctypes.data, self._scale.ctypes.data, self._thresh.ctypes.data,
+            stream_ptr(stream)), self.ctx)
+
+    def matvec(self, x, y, stream=None):
+        assert x.dtype == torch.complex128 and y.dtype == torch.complex128 and x.is_cuda and y.is_cuda
+        nvec = x.shape[0] if x.dim() == 2 else 1
+        _native.check(_native.lib().kr_matvec(self.op, _native.ptr(x), _native.ptr(y), nvec,
+                                              stream_ptr(stream)), self.ctx)
+
+    def step(self, states, phase, fac, tol, flags=0, korder=None, stream=None):
+        nvec = states.shape[0] if states.dim() == 2 else 1
+        kp = None
+        if korder is not None:
+            assert korder.dtype == np.int32 and korder.size >= nvec
+            kp = korder.ctypes.data
+        _native.check(_native.lib().kr_step(
+            self.op, _native.ptr(states), nvec, _native.ptr(phase), float(fac.real), float(fac.imag),
+            float(tol), int(flags), kp, stream_ptr(stream)), self.ctx)
+
+    def sync_status(self, stream=None):
+        _native.check(_native.lib().kr_sync_status(self.op, stream_ptr(stream)), self.ctx)
+
+    def launches(self):
+        return int(_native.lib().kr_op_launch_count(self.op))
+
+    def work(self):
+        f, b = ctypes.c_double(), ctypes.c_double()
+        _native.lib().kr_op_work(self.op, ctypes.byref(f), ctypes.byref(b))
+        return f.value, b.value
