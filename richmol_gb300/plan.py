@@ -18,6 +18,7 @@ import hashlib
 
 import numpy as np
 import torch
+from scipy.sparse import csr_matrix
 
 from . import _native
 from .device import context, stream_ptr
@@ -67,7 +68,9 @@ class CompiledSource:
         self.kshape = []
         self.groups = []    # (rows, width, ncart, col, val)
         self.terms = []     # (J1, s1, J2, s2, kidx, gidx)
+        self._keep = []
         gkey = {}
+        gid = {}
         for (J1, J2), kJ in src.kmat.items():
             mJ = src.mmat.get((J1, J2)) if hasattr(src.mmat, "get") else src.mmat[(J1, J2)]
             if not mJ:
@@ -90,18 +93,23 @@ class CompiledSource:
                     for cart, mm in mI.items():
                         mats[cidx[cart]] = mm
                         shape = mm.shape
-                    from scipy.sparse import csr_matrix
-                    mats = [m if m is not None else csr_matrix(shape, dtype=np.complex128) for m in mats]
-                    width, col, val = _ell(mats, shape[0], shape[1])
-                    h = hashlib.sha1()
-                    h.update(np.array([shape[0], shape[1], width], np.int64).tobytes())
-                    h.update(col.tobytes())
-                    h.update(val.tobytes())
-                    key = h.digest()
-                    if key not in gkey:
-                        gkey[key] = len(self.groups)
-                        self.groups.append((shape[0], width, len(self.carts), col, val))
-                    self.terms.append((J1, s1, J2, s2, kidx, gkey[key]))
+                    ikey = tuple(id(m) for m in mats)
+                    g = gid.get(ikey)
+                    if g is None:
+                        full = [m if m is not None else csr_matrix(shape, dtype=np.complex128) for m in mats]
+                        width, col, val = _ell(full, shape[0], shape[1])
+                        h = hashlib.sha1()
+                        h.update(np.array([shape[0], shape[1], width], np.int64).tobytes())
+                        h.update(col.tobytes())
+                        h.update(val.tobytes())
+                        key = h.digest()
+                        if key not in gkey:
+                            gkey[key] = len(self.groups)
+                            self.groups.append((shape[0], width, len(self.carts), col, val))
+                        g = gkey[key]
+                        gid[ikey] = g
+                        self._keep.append(mats)  # ids stay valid while compiled
+                    self.terms.append((J1, s1, J2, s2, kidx, g))
 
 
 def compiled(src):

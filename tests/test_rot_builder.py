@@ -1,0 +1,136 @@
+"""The in-house factor builder (richmol_gb300.rot) against the reference's own
+factors (tests/golden, produced by rot.LabTensor / rot.solve of the reference).
+
+M factors involve no eigenvectors and must agree element by element; K factors
+agree up to the sign of each eigenvector, so their magnitudes are compared;
+energies per (J, symmetry) agree to rounding. CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+
+def _mol_ocs():
+    from richmol_gb300 import rot
+    return rot.Molecule(xyz=[("C", 0, 0, 0), ("O", 0, 0, -1.16), ("S", 0, 0, 1.56)],
+                        dip=[0, 0, 0.28], pol=np.diag([35.0, 35.0, 80.0]))
+
+
+def _mol_asym():
+    from richmol_gb300 import rot
+    return rot.Molecule(B=(9.0, 5.0, 3.2), sym="D2", watson=dict(DeltaJ=1e-3, DeltaJK=1e-3, DeltaK=1e-3),
+                        dip=[0, 0, -0.73], pol=np.diag([9.1, 9.9, 9.4]))
+
+
+CASES = [
+    ("ocs_j6.npz", _mol_ocs, 6, ["dip", "pol", "cos2", "cos", "h0"]),
+    ("asym_j4.npz", _mol_asym, 4, ["dip", "pol", "cos2", "h0"]),
+]
+ARGS = {"cos2": "cos2theta", "cos": "costheta", "h0": "h0"}
+
+
+@pytest.mark.parametrize("case,mk,Jmax,names", CASES)
+def test_factors_match_reference(case, mk, Jmax, names):
+    from oracle import fixtures
+    from richmol_gb300 import rot
+    d, meta = fixtures.load(os.path.join(GOLDEN, case))
+    mol = mk()
+    sol = rot.Solution(mol, Jmax=Jmax)
+    for nm in names:
+        ref = fixtures.tensor(d, meta, nm)
+        arg = ARGS.get(nm, mol.dip if nm == "dip" else mol.pol)
+        src = rot.lab_tensor(arg, sol)._parts[0].src
+        assert src.Jlist1 == ref.Jlist1
+        assert src.symlist1 == ref.symlist1
+        assert src.dim_k1 == ref.dim_k1 and src.dim_m1 == ref.dim_m1
+        for Jp in ref.kmat:
+            for sp in ref.kmat[Jp]:
+                for i in ref.kmat[Jp][sp]:
+                    a = ref.kmat[Jp][sp][i].toarray()
+                    try:
+                        b = src.kmat[Jp][sp][i].toarray()
+                    except (KeyError, AttributeError):
+                        # the reference keeps round-off blocks above machine epsilon
+                        b = np.zeros_like(a)
+                    assert np.abs(np.abs(a) - np.abs(b)).max() < 1e-12 * max(1.0, np.abs(a).max()), (nm, Jp, sp, i)
+        for Jp in ref.mmat:
+            for sp in ref.mmat[Jp]:
+                for i in ref.mmat[Jp][sp]:
+                    for c in ref.mmat[Jp][sp][i]:
+                        a = ref.mmat[Jp][sp][i][c].toarray()
+                        b = src.mmat[Jp][sp][i][c].toarray()
+                        assert np.abs(a - b).max() < 1e-14, (nm, Jp, sp, i, c)
+
+
+def test_energies_match_reference():
+    from oracle import fixtures
+    from richmol_gb300 import rot
+    d, meta = fixtures.load(os.path.join(GOLDEN, "asym_j4.npz"))
+    sol = rot.Solution(_mol_asym(), Jmax=4)
+    i = 0
+    for J, s, n in meta["enr_keys"]:
+        e = sol.states[J][s][0]
+        assert len(e) == n
+        assert np.abs(e - d["enr"][i: i + n]).max() < 1e-10
+        i += n
+
+
+def test_ocs_rotational_constant_from_geometry():
+    import json
+    meta = json.loads(str(np.load(os.path.join(GOLDEN, "ocs_j6.npz"))["meta"]))
+    assert np.allclose(_mol_ocs().B, meta["B"], rtol=1e-14, atol=0)
+
+
+def test_three_j_against_exact_reference_stub():
+    import sys
+    sys.path.insert(0, os.path.join(GOLDEN, "refshim"))
+    try:
+        import py3nj
+    finally:
+        sys.path.pop(0)
+    from richmol_gb300 import rot
+    rng = np.random.default_rng(0)
+    for _ in range(200):
+        j1 = int(rng.integers(0, 45))
+        w = int(rng.integers(0, 3))
+        j2 = int(rng.integers(max(0, j1 - w), j1 + w + 1))
+        a = int(rng.integers(-j1, j1 + 1))
+        s = int(rng.integers(-w, w + 1))
+        if abs(a + s) > j2:
+            continue
+        ref = py3nj.wigner3j(2 * j1, 2 * w, 2 * j2, 2 * a, 2 * s, -2 * (a + s))[0]
+        assert abs(rot.three_j(j1, w, j2, a, s, -(a + s)) - ref) < 1e-15
+
+
+def test_propagation_observable_is_basis_invariant():
+    """Propagating the reference fixture's initial state with the builder's
+    factors gives the reference's <cos^2 theta> trace (the oracle runs both)."""
+    from oracle import fixtures
+    from oracle.cartens import OCarTens
+    from oracle.tdse import OTDSE
+    from richmol_gb300 import rot
+    d, meta = fixtures.load(os.path.join(GOLDEN, "ocs_j6.npz"))
+    sp = meta["split"]
+    sol = rot.Solution(_mol_ocs(), Jmax=6)
+
+    def to_oracle(T):
+        src = T._parts[0].src
+        o = OCarTens()
+        for k in ("Jlist1", "Jlist2", "symlist1", "symlist2", "dim_m1", "dim_m2", "dim_k1", "dim_k2",
+                  "dim1", "dim2", "kmat", "mmat", "rank"):
+            setattr(o, k, getattr(src, k))
+        o.cart = src.carts
+        return o
+    h0 = to_oracle(rot.lab_tensor("h0", sol))
+    Hac = to_oracle(rot.lab_tensor(_mol_ocs().pol, sol)) * sp["scale"]
+    c2 = to_oracle(rot.lab_tensor("cos2theta", sol)).tomat(form="full", cart="0")
+    td = OTDSE(t_start=sp["t_start"], t_end=sp["t_end"], dt=sp["dt"])
+    tc = td.time_grid()
+    vecs = td.init_state(h0, temp=0)
+    for i in range(len(tc)):
+        Hac.field(d["split/fields"][i])
+        vecs, _ = td.update(Hac, vecs, H0=h0)
+        c = np.vdot(vecs[0], c2.dot(vecs[0])).real + 1 / 3
+        assert abs(c - d["split/cos2"][i]) < 1e-9
