@@ -146,6 +146,11 @@ int64_t kr_op_launch_count(const kr_op* op);
  * minimum bytes moved (vector in + out + factors). */
 int kr_op_work(const kr_op* op, double* fma_per_matvec, double* bytes_per_matvec);
 
+/* Measurement helper with no counterpart in the reference: FP64 fused
+ * multiply-add throughput of the device in TFLOP/s (the roofline denominator
+ * of the FP64 path). Allocates and synchronises; not for the hot path. */
+int kr_probe_fp64(kr_ctx* ctx, double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,6 +28,7 @@ KR_STEP_SKIP_KRYLOV = 1
 EXPORTED = [
     "kr_ctx_create", "kr_ctx_destroy", "kr_last_error", "kr_op_create", "kr_op_destroy",
     "kr_set_field", "kr_matvec", "kr_step", "kr_sync_status", "kr_op_launch_count", "kr_op_work",
+    "kr_probe_fp64",
 ]
 
 
@@ -112,6 +113,8 @@ def lib():
         L.kr_op_launch_count.restype = i64
         L.kr_op_work.argtypes = [vp, ctypes.POINTER(dbl), ctypes.POINTER(dbl)]
         L.kr_op_work.restype = ctypes.c_int
+        L.kr_probe_fp64.argtypes = [vp, ctypes.POINTER(dbl)]
+        L.kr_probe_fp64.restype = ctypes.c_int
         _lib = L
         return L
 

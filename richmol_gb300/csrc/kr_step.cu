@@ -894,3 +894,40 @@ extern "C" int kr_op_work(const kr_op* op, double* fma_per_matvec, double* bytes
   if (bytes_per_matvec) *bytes_per_matvec = op->bytes_per_matvec;
   return KR_OK;
 }
+
+// ===========================================================================
+// measurement helper: FP64 FMA throughput of this device (8 independent
+// chains per thread; every thread writes one double)
+// ===========================================================================
+__global__ void kr_fp64_probe_kernel(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * (long long)blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+extern "C" int kr_probe_fp64(kr_ctx* ctx, double* tflops) {
+  if (!ctx || !tflops) return set_err(ctx, KR_ERR_ARG, "kr_probe_fp64: NULL argument");
+  KR_CUDA(ctx, cudaSetDevice(ctx->device));
+  const int blocks = ctx->nsm * 8, threads = 256, iters = 4096;
+  double* out = nullptr;
+  KR_CUDA(ctx, cudaMalloc(&out, sizeof(double) * blocks * threads));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  kr_fp64_probe_kernel<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+  cudaEventRecord(e0);
+  for (int r = 0; r < 5; ++r) kr_fp64_probe_kernel<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+  cudaEventRecord(e1);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) return set_err(ctx, KR_ERR_CUDA, cudaGetErrorString(e));
+  *tflops = 5.0 * 2.0 * 8.0 * iters * double(blocks) * threads / (ms * 1e-3) / 1e12;
+  return KR_OK;
+}

@@ -1,0 +1,69 @@
+"""Synthetic workloads of the propagation benchmark (molecules, fields, grids).
+
+No public dataset is involved: the inputs are fixed synthetic molecules and
+pulses, built with the in-house factor builder (richmol_gb300.rot).
+
+* ``linear_ocs``  linear O-C-S (C-O 1.16 A, C-S 1.56 A), mu_z = 0.28 au,
+  alpha = diag(35, 35, 80) au, J = 0..Jmax (default 20) with all M; z pulse
+  5e11 W/cm^2, FWHM 300 fs at 1 ps, cycle averaged; 0-3 ps, dt = 10 fs.
+* ``asym_top``    asymmetric top (Bx, By, Bz) = (A, B, C) = (9.0, 5.0, 3.2) cm^-1,
+  Watson A with Delta_J = Delta_JK = Delta_K = 1e-3 cm^-1, D2, mu = (0, 0, -0.73)
+  au, alpha = diag(9.1, 9.9, 9.4) au, J = 0..Jmax (default 40) with all M and k;
+  DC field 20 kV/cm along z plus a 1e12 W/cm^2 FWHM 500 fs pulse polarised at
+  35 deg to the DC field, centred at 1 ps; dt = 5 fs, 4000 steps.
+"""
+import numpy as np
+
+from . import rot
+from .convert_units import AUdip_x_Vm_to_invcm, AUpol_x_Vm_to_invcm
+
+
+class Workload:
+    """Operators, field schedule and time grid of one propagation problem."""
+
+    def __init__(self, name, mol, Jmax, t_start, t_end, dt, dc, pulse, temp=0):
+        self.name = name
+        self.mol = mol
+        self.Jmax = Jmax
+        self.t_start, self.t_end, self.dt = t_start, t_end, dt
+        self.dc = None if dc is None else np.asarray(dc, dtype=np.float64)
+        self.pulse = pulse  # (t0, fwhm, intensity, direction)
+        self.temp = temp
+        self.sol = rot.Solution(mol, Jmax=Jmax)
+        self.h0 = rot.lab_tensor("h0", self.sol)
+        self.pol = rot.lab_tensor(mol.pol, self.sol)
+        self.dip = rot.lab_tensor(mol.dip, self.sol) if mol.dip is not None and np.any(mol.dip) else None
+        self.cos2 = rot.lab_tensor("cos2theta", self.sol)
+        self.Hac = self.pol * (-0.5 * AUpol_x_Vm_to_invcm())
+        self.Hdc = None
+        if self.dc is not None and self.dip is not None:
+            self.Hdc = (self.dip * list(self.dc)) * (-1 * AUdip_x_Vm_to_invcm())
+        self.dim = sum(self.h0.dim1[J][s] for J in self.h0.Jlist1 for s in self.h0.symlist1[J])
+
+    def field(self, t):
+        t0, fwhm, inten, direction = self.pulse
+        return rot.pulse_field(t, t0, fwhm, inten, direction)
+
+    def hamiltonian(self, t):
+        """H(t) without H0: the DC term plus the pulse term at time t."""
+        self.Hac.field(self.field(t))
+        return self.Hac if self.Hdc is None else self.Hdc + self.Hac
+
+    @property
+    def nsteps(self):
+        return int((self.t_end - self.t_start) / self.dt)
+
+
+def linear_ocs(Jmax=20):
+    mol = rot.Molecule(xyz=[("C", 0, 0, 0), ("O", 0, 0, -1.16), ("S", 0, 0, 1.56)],
+                       dip=[0, 0, 0.28], pol=np.diag([35.0, 35.0, 80.0]))
+    return Workload("linear_ocs_J%d" % Jmax, mol, Jmax, 0.0, 3.0, 0.01, None,
+                    (1.0, 0.3, 5e11, [0, 0, 1]))
+
+
+def asym_top(Jmax=40, dt=0.005, nsteps=4000):
+    mol = rot.Molecule(B=(9.0, 5.0, 3.2), sym="D2", watson=dict(DeltaJ=1e-3, DeltaJK=1e-3, DeltaK=1e-3),
+                       dip=[0, 0, -0.73], pol=np.diag([9.1, 9.9, 9.4]))
+    beta = np.deg2rad(35.0)
+    return Workload("asym_top_D2_J%d" % Jmax, mol, Jmax, 0.0, nsteps * dt, dt, [0.0, 0.0, 20e3 * 1e2],
+                    (1.0, 0.5, 1e12, [np.sin(beta), 0.0, np.cos(beta)]))
