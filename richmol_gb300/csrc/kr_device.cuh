@@ -4,9 +4,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#define KR_WARPS 8                  // warps per CTA
+#define KR_WARPS 8                  // warps per CTA (2 CTAs per SM)
 #define KR_THREADS (KR_WARPS * 32)
-#define KR_QMAX 4                   // output pairs per lane (n_k1 * rows <= 128)
+#define KR_QMAX 4                   // (row, a) outputs per thread of a task
 #define KR_BARRIER_TIMEOUT_NS 2000000000ull  // 2 s per grid-barrier wait
 
 // ---------------------------------------------------------------------------
@@ -48,10 +48,11 @@ struct DevOp {
   const int* m_col; double2* mf_val;
   // terms grouped by output slab
   const int* term_ptr; const int* t_in; const int* t_k; const int* t_mf;
-  // row tasks and their static assignment to warps
+  const int* mf_type;   // per MF instance: 0 complex, 1 real, 2 imaginary (set with the field)
+  // row tasks, handed out dynamically in the order task_order
   const int* task_slab; const int* task_row0; const int* task_nrows;
-  const int* warp_task_ptr; const int* warp_tasks;
-  int zmax;  // complex entries of the per-warp Z staging buffer
+  const int* task_order; int ntask;
+  int zmax;  // complex entries of one Z staging buffer
 };
 
 // ---------------------------------------------------------------------------
@@ -134,8 +135,16 @@ __device__ double2 grid_partials_sum2(const double2* part, int n, double2* scrat
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   __syncthreads();
   if (warp == 0) {
-    double2 s = make_double2(0.0, 0.0);
-    for (int i = lane; i < n; i += 32) s = cadd(s, ldcg2(part + i));
+    double2 s0 = make_double2(0.0, 0.0), s1 = s0, s2 = s0, s3 = s0;
+    int i = lane;
+    for (; i + 96 < n; i += 128) {
+      s0 = cadd(s0, ldcg2(part + i));
+      s1 = cadd(s1, ldcg2(part + i + 32));
+      s2 = cadd(s2, ldcg2(part + i + 64));
+      s3 = cadd(s3, ldcg2(part + i + 96));
+    }
+    for (; i < n; i += 32) s0 = cadd(s0, ldcg2(part + i));
+    double2 s = cadd(cadd(s0, s1), cadd(s2, s3));
     s = warp_sum2(s);
     if (lane == 0) scratch[0] = s;
   }
@@ -146,21 +155,32 @@ __device__ double2 grid_partials_sum2(const double2* part, int n, double2* scrat
 }
 
 // ---------------------------------------------------------------------------
-// Kronecker mat-vec over the row tasks of one warp:
-//   y[s1][i, a] = sum_terms sum_b K_t[a, b] * Z_t[i, b],
-//   Z_t[i, b]   = xscale * sum_w MF_t[i, w] * x[s2][col_t(i, w), b]
+// Kronecker mat-vec over the row tasks of one CTA. A task is a block of nr
+// consecutive rows of one output slab; all threads of the CTA work on it:
+//   Z_t[r, b]   = xscale * sum_w MF_t[i0 + r, w] * x[s2][col_t(i0 + r, w), b]
+//   y[s1][i0 + r, a] = sum_terms sum_b K_t[a, b] * Z_t[r, b]
 // (field.py:1229-1243 computes the same sum as MF (K X^T)^T per term.)
-// With ALPHA the warp also accumulates sum conj(y) * (xscale * x) over its
+// Z of a term is staged in shared memory (double-buffered, one __syncthreads
+// per term); each thread owns up to KR_QMAX (row, a) outputs.
+// With ALPHA the CTA also accumulates sum conj(y) * (xscale * x) over its
 // outputs: the Lanczos coefficient vdot(w, V_k) of tdse.py:468 for a square
 // operator, where V_k = xscale * x.
 // ---------------------------------------------------------------------------
 template <bool ALPHA>
-__device__ void matvec_warp_tasks(const DevOp& op, const double2* __restrict__ x, double xscale,
-                                  double2* __restrict__ y, int gwarp, double2* zbuf, double2& alpha_acc) {
-  const int lane = threadIdx.x & 31;
-  const int t_begin = __ldg(op.warp_task_ptr + gwarp), t_end = __ldg(op.warp_task_ptr + gwarp + 1);
-  for (int t = t_begin; t < t_end; ++t) {
-    const int task = __ldg(op.warp_tasks + t);
+__device__ void matvec_cta_tasks(const DevOp& op, const double2* __restrict__ x, double xscale,
+                                 double2* __restrict__ y, unsigned* counter, double2* task_alpha,
+                                 double2* smem, double2* red) {
+  __shared__ int s_task;
+  const int tid = threadIdx.x;
+  double2* zb[2] = {smem, smem + op.zmax};
+  for (;;) {
+    // tasks are handed out in order of decreasing cost
+    if (tid == 0) s_task = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    const int t = s_task;
+    __syncthreads();
+    if (t >= op.ntask) break;
+    const int task = __ldg(op.task_order + t);
     const int s1 = __ldg(op.task_slab + task);
     const int i0 = __ldg(op.task_row0 + task);
     const int nr = __ldg(op.task_nrows + task);
@@ -172,75 +192,98 @@ __device__ void matvec_warp_tasks(const DevOp& op, const double2* __restrict__ x
 
     const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
     for (int term = tb; term < te; ++term) {
+      double2* Z = zb[(term - tb) & 1];
       const int s2 = __ldg(op.t_in + term);
-      const int kb = __ldg(op.t_k + term);
+      const int kbk = __ldg(op.t_k + term);
       const int mfi = __ldg(op.t_mf + term);
       const int nk2 = __ldg(op.in_dk + s2);
       const double2* X = x + __ldg(op.in_off + s2);
       const int W = __ldg(op.mf_width + mfi);
       const int* col = op.m_col + __ldg(op.mf_col_off + mfi);
       const double2* mf = op.mf_val + __ldg(op.mf_off + mfi);
-      // stage Z for the nr rows of this task
+      const int mtype = __ldcg(op.mf_type + mfi);
+      // stage Z (nr x nk2)
       const int nz = nr * nk2;
-      for (int p = lane; p < nz; p += 32) {
+      for (int p = tid; p < nz; p += blockDim.x) {
         const int r = p / nk2;
         const int b = p - r * nk2;
         const int base = (i0 + r) * W;
         double2 z = make_double2(0.0, 0.0);
-        for (int w = 0; w < W; ++w) {
-          const int j = __ldg(col + base + w);
-          const double2 m = __ldg(mf + base + w);
-          cfma(z, m, ldcg2(X + (long long)j * nk2 + b));
+        if (mtype == 1) {          // MF real
+          for (int w = 0; w < W; ++w) {
+            const double m = __ldcg(&mf[base + w].x);
+            const double2 xv = ldcg2(X + (long long)__ldg(col + base + w) * nk2 + b);
+            z.x = fma(m, xv.x, z.x);
+            z.y = fma(m, xv.y, z.y);
+          }
+        } else if (mtype == 2) {   // MF imaginary
+          for (int w = 0; w < W; ++w) {
+            const double m = __ldcg(&mf[base + w].y);
+            const double2 xv = ldcg2(X + (long long)__ldg(col + base + w) * nk2 + b);
+            z.x = fma(-m, xv.y, z.x);
+            z.y = fma(m, xv.x, z.y);
+          }
+        } else {
+          for (int w = 0; w < W; ++w)
+            cfma(z, ldcg2(mf + base + w), ldcg2(X + (long long)__ldg(col + base + w) * nk2 + b));
         }
-        zbuf[p] = cscale(z, xscale);
+        Z[p] = cscale(z, xscale);
       }
-      __syncwarp();
-      const double* K = op.k_data + __ldg(op.k_off + kb);
-      const int ktype = __ldg(op.k_type + kb);
+      // K is stored transposed (KT[b][a]) so that threads with consecutive a
+      // read consecutive words
+      const double* KT = op.k_data + __ldg(op.k_off + kbk);
+      const int ktype = __ldg(op.k_type + kbk);
+      __syncthreads();
 #pragma unroll
       for (int q = 0; q < KR_QMAX; ++q) {
-        const int p = lane + 32 * q;
+        const int p = tid + blockDim.x * q;
         if (p < npair) {
           const int r = p / nk1;
           const int a = p - r * nk1;
-          const double2* zr = zbuf + r * nk2;
+          const double2* zr = Z + r * nk2;
           double2 s = acc[q];
           if (ktype == 1) {  // real K
-            const double* Ka = K + (long long)a * nk2;
             for (int b = 0; b < nk2; ++b) {
-              const double kv = __ldg(Ka + b);
+              const double kv = __ldg(KT + b * nk1 + a);
               const double2 zv = zr[b];
               s.x = fma(kv, zv.x, s.x);
               s.y = fma(kv, zv.y, s.y);
             }
           } else if (ktype == 2) {  // K = i * Ki
-            const double* Ka = K + (long long)a * nk2;
             for (int b = 0; b < nk2; ++b) {
-              const double kv = __ldg(Ka + b);
+              const double kv = __ldg(KT + b * nk1 + a);
               const double2 zv = zr[b];
               s.x = fma(-kv, zv.y, s.x);
               s.y = fma(kv, zv.x, s.y);
             }
           } else {  // complex K
-            const double2* Ka = reinterpret_cast<const double2*>(K) + (long long)a * nk2;
-            for (int b = 0; b < nk2; ++b) cfma(s, __ldg(Ka + b), zr[b]);
+            const double2* KT2 = reinterpret_cast<const double2*>(KT);
+            for (int b = 0; b < nk2; ++b) cfma(s, __ldg(KT2 + b * nk1 + a), zr[b]);
           }
           acc[q] = s;
         }
       }
-      __syncwarp();
     }
     const long long obase = __ldg(op.out_off + s1) + (long long)i0 * nk1;
+    double2 al = make_double2(0.0, 0.0);
 #pragma unroll
     for (int q = 0; q < KR_QMAX; ++q) {
-      const int p = lane + 32 * q;
+      const int p = tid + blockDim.x * q;
       if (p < npair) {
         y[obase + p] = acc[q];
         if (ALPHA) {
           const double2 v = cscale(ldcg2(x + obase + p), xscale);
-          alpha_acc = cadd(alpha_acc, cconjmul(acc[q], v));
+          al = cadd(al, cconjmul(acc[q], v));
         }
       }
+    }
+    if (ALPHA) {
+      // per-task partial of vdot(w, V_k): summed later in task order, so the
+      // result does not depend on which CTA ran the task
+      al = block_sum2(al, red);
+      if (tid == 0) task_alpha[task] = al;
+    } else {
+      __syncthreads();
     }
   }
 }

@@ -23,6 +23,7 @@
 #include "kr_device.cuh"
 
 #define KR_EXPM_MAX 128  // capacity of the tridiagonal exponential (maxorder <= 128)
+#define KR_MATVEC_MAXVEC 65535  // vectors of one kr_matvec call (grid.y)
 
 // ===========================================================================
 // field contraction: MF = scale * thr(sum_c coef_c M_c)
@@ -36,6 +37,9 @@ struct FieldCoef {
 
 struct DevField {
   long long nent;
+  int nmf;
+  const signed char* m_ctype;   // [group][KR_MAXCART]: 0 mixed, 1 real, 2 imaginary, 3 all zero
+  int* mf_type;                 // out: per MF instance 0 complex, 1 real, 2 imaginary
   const int* ent_inst;          // MF instance of each entry
   const long long* inst_ptr;    // first entry of each instance
   const int* mf_group; const int* mf_part;
@@ -44,7 +48,36 @@ struct DevField {
   double2* mf_val;
 };
 
+// class of a complex number: 3 zero, 1 real, 2 imaginary, 0 general
+__device__ __forceinline__ int cclass(double2 z) {
+  if (z.x == 0.0 && z.y == 0.0) return 3;
+  if (z.y == 0.0) return 1;
+  if (z.x == 0.0) return 2;
+  return 0;
+}
+// class of a product: zero absorbs, real is neutral, imaginary * imaginary is real
+__device__ __forceinline__ int cclass_mul(int a, int b) {
+  if (a == 3 || b == 3) return 3;
+  if (a == 0 || b == 0) return 0;
+  return a == b ? 1 : 2;
+}
+
 __global__ void __launch_bounds__(256) kr_field_kernel(DevField f, FieldCoef c) {
+  // MF instance types: which components of MF = scale * sum_c coef_c M_c can be
+  // non-zero; the mat-vec skips the multiplications by exact zeros
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < f.nmf; i += gridDim.x * blockDim.x) {
+    const int g = __ldg(f.mf_group + i);
+    const int p = __ldg(f.mf_part + i);
+    const int nc = __ldg(f.m_ncart + g);
+    int t = 3;
+    for (int ci = 0; ci < nc; ++ci) {
+      const int ct = cclass_mul(cclass(c.coef[p][ci]), (int)f.m_ctype[g * KR_MAXCART + ci]);
+      if (ct == 3) continue;
+      t = (t == 3) ? ct : (t == ct ? t : 0);
+    }
+    t = cclass_mul(t, cclass(c.scale[p]));
+    f.mf_type[i] = (t == 3) ? 1 : t;
+  }
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < f.nent;
        e += (long long)gridDim.x * blockDim.x) {
     const int inst = __ldg(f.ent_inst + e);
@@ -65,14 +98,12 @@ __global__ void __launch_bounds__(256) kr_field_kernel(DevField f, FieldCoef c) 
 // ===========================================================================
 // stand-alone mat-vec (CarTens.vec): grid.y runs over vectors
 // ===========================================================================
-__global__ void __launch_bounds__(KR_THREADS) kr_matvec_kernel(DevOp op, const double2* x, double2* y) {
+__global__ void __launch_bounds__(KR_THREADS, 2) kr_matvec_kernel(DevOp op, const double2* x, double2* y,
+                                                                  unsigned* counters) {
   extern __shared__ double2 smem[];
-  const int warp = threadIdx.x >> 5;
-  double2* zbuf = smem + warp * op.zmax;
+  __shared__ double2 red[KR_WARPS];
   const long long v = blockIdx.y;
-  double2 dummy = make_double2(0.0, 0.0);
-  matvec_warp_tasks<false>(op, x + v * op.dim_in, 1.0, y + v * op.dim_out, blockIdx.x * KR_WARPS + warp, zbuf,
-                           dummy);
+  matvec_cta_tasks<false>(op, x + v * op.dim_in, 1.0, y + v * op.dim_out, counters + v, nullptr, smem, red);
 }
 
 // v <- (v * ph) * ph : the two H0 half-phases with no field term (tdse.py:375,394)
@@ -92,8 +123,8 @@ __global__ void kr_phase2_kernel(double2* v, const double2* ph, long long dim, l
 // The reference forms the dense expm (scipy Pade, tdse.py:474) and takes
 // column 0; both agree to rounding.
 // ===========================================================================
-__device__ void warp_expm_e0(const double2* alpha, const double* beta, int n, double2 fac, double2* out,
-                             double2* term, double2* tmp) {
+__device__ void warp_expm_e0_smem(const double2* alpha, const double* beta, int n, double2 fac, double2* out,
+                                  double2* term, double2* tmp) {
   const int lane = threadIdx.x & 31;
   // 1-norm of A
   double nrm = 0.0;
@@ -128,8 +159,8 @@ __device__ void warp_expm_e0(const double2* alpha, const double* beta, int n, do
       for (int i = lane; i < n; i += 32) {
         term[i] = tmp[i];
         out[i] = cadd(out[i], tmp[i]);
-        tmax = fmax(tmax, sqrt(cabs2(tmp[i])));
-        amax = fmax(amax, sqrt(cabs2(out[i])));
+        tmax = fmax(tmax, fmax(fabs(tmp[i].x), fabs(tmp[i].y)));
+        amax = fmax(amax, fmax(fabs(out[i].x), fabs(out[i].y)));
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -140,6 +171,89 @@ __device__ void warp_expm_e0(const double2* alpha, const double* beta, int n, do
       if (tmax <= 1e-18 * amax) break;
     }
   }
+}
+
+// n <= 32: one element per lane, neighbours by shuffles. When fac is purely
+// imaginary and T is real (Hermitian H: the diagonal's imaginary parts are
+// round-off), A = i tau T and each term costs 3 real x complex products.
+__device__ void warp_expm_e0_reg(const double2* alpha, const double* beta, int n, double2 fac, double2* out) {
+  const int lane = threadIdx.x & 31;
+  const bool act = lane < n;
+  const double2 al = act ? alpha[lane] : make_double2(0.0, 0.0);
+  const double bl = (lane < n - 1) ? beta[lane] : 0.0;      // couples lane and lane+1
+  double bm = __shfl_up_sync(0xffffffffu, bl, 1);            // couples lane-1 and lane
+  if (lane == 0) bm = 0.0;
+  // 1-norm of A and the realness test
+  const double fa = sqrt(fac.x * fac.x + fac.y * fac.y);
+  double cs = act ? fa * (sqrt(al.x * al.x + al.y * al.y) + fabs(bm) + fabs(bl)) : 0.0;
+  double tmagn = act ? fmax(fabs(al.x), fabs(bl)) : 0.0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    cs = fmax(cs, __shfl_xor_sync(0xffffffffu, cs, o));
+    tmagn = fmax(tmagn, __shfl_xor_sync(0xffffffffu, tmagn, o));
+  }
+  const bool real_t = (fac.x == 0.0) && __all_sync(0xffffffffu, !act || fabs(al.y) <= 1e-13 * tmagn);
+  int nsub = (int)ceil(cs);
+  if (nsub < 1) nsub = 1;
+  if (nsub > 4096) nsub = 4096;
+  const double inv_s = 1.0 / (double)nsub;
+  double2 y = make_double2(lane == 0 ? 1.0 : 0.0, 0.0);
+  if (real_t) {
+    const double tau = fac.y * inv_s;  // A / nsub = i tau T
+    for (int sub = 0; sub < nsub; ++sub) {
+      double2 t = y, acc = y;
+      for (int j = 1; j <= 40; ++j) {
+        const double2 tu = make_double2(__shfl_up_sync(0xffffffffu, t.x, 1), __shfl_up_sync(0xffffffffu, t.y, 1));
+        const double2 td = make_double2(__shfl_down_sync(0xffffffffu, t.x, 1),
+                                        __shfl_down_sync(0xffffffffu, t.y, 1));
+        double rx = al.x * t.x, ry = al.x * t.y;
+        rx = fma(bm, tu.x, rx);
+        ry = fma(bm, tu.y, ry);
+        rx = fma(bl, td.x, rx);
+        ry = fma(bl, td.y, ry);
+        const double sc = tau / (double)j;
+        t = act ? make_double2(-sc * ry, sc * rx) : make_double2(0.0, 0.0);  // i * sc * (T t)
+        acc.x += t.x;
+        acc.y += t.y;
+        const double lim = 1e-18 * fmax(1.0, fmax(fabs(acc.x), fabs(acc.y)));
+        const bool small = fabs(t.x) <= lim && fabs(t.y) <= lim;
+        if (__all_sync(0xffffffffu, small)) break;
+      }
+      y = acc;
+    }
+  } else {
+    const double2 a = cscale(cmul(fac, al), inv_s);
+    const double2 bu = cscale(fac, bm * inv_s), bd = cscale(fac, bl * inv_s);
+    for (int sub = 0; sub < nsub; ++sub) {
+      double2 t = y, acc = y;
+      for (int j = 1; j <= 40; ++j) {
+        const double2 tu = make_double2(__shfl_up_sync(0xffffffffu, t.x, 1), __shfl_up_sync(0xffffffffu, t.y, 1));
+        const double2 td = make_double2(__shfl_down_sync(0xffffffffu, t.x, 1),
+                                        __shfl_down_sync(0xffffffffu, t.y, 1));
+        double2 r = cmul(a, t);
+        cfma(r, bu, tu);
+        cfma(r, bd, td);
+        const double sc = 1.0 / (double)j;
+        t = act ? cscale(r, sc) : make_double2(0.0, 0.0);
+        acc = cadd(acc, t);
+        const double lim = 1e-18 * fmax(1.0, fmax(fabs(acc.x), fabs(acc.y)));
+        const bool small = fabs(t.x) <= lim && fabs(t.y) <= lim;
+        if (__all_sync(0xffffffffu, small)) break;
+      }
+      y = acc;
+    }
+  }
+  if (act) out[lane] = y;
+}
+
+// exp(A) e0 for A = fac * T, T (n x n) tridiagonal with diagonal alpha and
+// symmetric off-diagonal beta (tdse.py:474 takes column 0 of the same expm).
+__device__ void warp_expm_e0(const double2* alpha, const double* beta, int n, double2 fac, double2* out,
+                             double2* term, double2* tmp) {
+  if (n <= 32)
+    warp_expm_e0_reg(alpha, beta, n, fac, out);
+  else
+    warp_expm_e0_smem(alpha, beta, n, fac, out, term, tmp);
 }
 
 // ===========================================================================
@@ -154,6 +268,8 @@ struct StepArgs {
   double2* w;              // H V_k
   double2* ub[2];          // successive solutions
   double2* part_a;         // per-CTA partials
+  double2* task_alpha;     // per-task partials of vdot(w, V_k)
+  unsigned* counters;      // task counters, one per mat-vec of the step
   double* part_b;
   double* part_c;
   double2* alpha;          // T diagonal   (maxorder)
@@ -178,7 +294,7 @@ struct StepSmem {
   double scalar[4];
 };
 
-__global__ void __launch_bounds__(KR_THREADS, 1) kr_step_kernel(StepArgs a) {
+__global__ void __launch_bounds__(KR_THREADS, 2) kr_step_kernel(StepArgs a) {
   extern __shared__ double2 smem_dyn[];
   __shared__ StepSmem ss;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -186,10 +302,10 @@ __global__ void __launch_bounds__(KR_THREADS, 1) kr_step_kernel(StepArgs a) {
   const long long gtid = blockIdx.x * (long long)blockDim.x + tid;
   const long long gstride = (long long)nblk * blockDim.x;
   const long long n = a.dim;
-  double2* zbuf = smem_dyn + warp * a.op.zmax;
-  const int gwarp = blockIdx.x * KR_WARPS + warp;
 
   if (*((volatile int*)a.status) != 0) return;  // sticky error from an earlier launch
+  if (blockIdx.x == 0)
+    for (int i = tid; i < a.maxorder + 2; i += blockDim.x) a.counters[i] = 0u;
 
   // ---- V0 = phase * state (tdse.py:375) -----------------------------------
   double2* V0 = a.V;
@@ -201,15 +317,10 @@ __global__ void __launch_bounds__(KR_THREADS, 1) kr_step_kernel(StepArgs a) {
   if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
 
   // ---- k = 0: w = H V0, T00 = vdot(w, V0), W0 = w - T00 V0 (tdse.py:443-446)
-  {
-    double2 al = make_double2(0.0, 0.0);
-    matvec_warp_tasks<true>(a.op, V0, 1.0, a.w, gwarp, zbuf, al);
-    al = block_sum2(al, ss.red);
-    if (tid == 0) a.part_a[blockIdx.x] = al;
-  }
+  matvec_cta_tasks<true>(a.op, V0, 1.0, a.w, a.counters, a.task_alpha, smem_dyn, ss.red);
   if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
   {
-    const double2 a0 = grid_partials_sum2(a.part_a, nblk, ss.red);
+    const double2 a0 = grid_partials_sum2(a.task_alpha, a.op.ntask, ss.red);
     if (blockIdx.x == 0 && tid == 0) a.alpha[0] = a0;
     double bp = 0.0;
     double2* W0 = a.Wb[0];
@@ -295,16 +406,11 @@ __global__ void __launch_bounds__(KR_THREADS, 1) kr_step_kernel(StepArgs a) {
     }
 
     // w = H V_k and T_kk = vdot(w, V_k) (tdse.py:467-468)
-    {
-      double2 al = make_double2(0.0, 0.0);
-      matvec_warp_tasks<true>(a.op, xsrc, xscale, a.w, gwarp, zbuf, al);
-      al = block_sum2(al, ss.red);
-      if (tid == 0) a.part_a[blockIdx.x] = al;
-    }
+    matvec_cta_tasks<true>(a.op, xsrc, xscale, a.w, a.counters + k, a.task_alpha, smem_dyn, ss.red);
     if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
 
     // T_kk, then exp(fac T_{0..k}) e0 in every CTA (tdse.py:474)
-    const double2 ak = grid_partials_sum2(a.part_a, nblk, ss.red);
+    const double2 ak = grid_partials_sum2(a.task_alpha, a.op.ntask, ss.red);
     if (blockIdx.x == 0 && tid == 0) a.alpha[k] = ak;
     __syncthreads();
     if (warp == 0) {
@@ -416,6 +522,9 @@ struct kr_op {
   // step scratch
   double2 *V = nullptr, *Wb0 = nullptr, *Wb1 = nullptr, *w = nullptr, *ub0 = nullptr, *ub1 = nullptr;
   double2* part_a = nullptr;
+  double2* task_alpha = nullptr;
+  unsigned* counters = nullptr;
+  unsigned* mv_counters = nullptr;
   double *part_b = nullptr, *part_c = nullptr;
   double2* alpha = nullptr;
   double* beta = nullptr;
@@ -487,23 +596,26 @@ extern "C" void kr_op_destroy(kr_op* op) {
 
 namespace {
 
-// rows per warp task for an output slab with n_k1 columns: the largest useful
-// lane occupancy with at most KR_QMAX pairs per lane
-int pick_rows(int nk1, int dm1) {
-  if (nk1 <= 0) return 1;
-  int best_r = 1;
+// Splits an output slab of dm1 rows x nk1 columns into row tasks for one CTA
+// of KR_THREADS threads, each thread owning at most KR_QMAX outputs: picks
+// the task count with the best thread occupancy (finer on near-ties).
+int pick_task_rows(int nk1, int dm1) {
+  const long long P = (long long)dm1 * nk1;
+  int best_R = dm1;
   double best_eff = -1.0;
-  for (int r = 1; r <= 32 * KR_QMAX; ++r) {
-    if (r * nk1 > 32 * KR_QMAX) break;
-    if (r > dm1) break;
-    const int q = (r * nk1 + 31) / 32;
-    const double eff = double(r * nk1) / double(32 * q);
-    if (eff > best_eff + 1e-9) {
-      best_eff = eff;
-      best_r = r;
+  for (int m = 1; m <= dm1; ++m) {
+    const int R = (dm1 + m - 1) / m;
+    const int mm = (dm1 + R - 1) / R;
+    const int q = (R * nk1 + KR_THREADS - 1) / KR_THREADS;
+    if (q > KR_QMAX) continue;
+    const double eff = double(P) / (double(mm) * q * KR_THREADS);
+    if (eff > best_eff * 1.02 || (eff > best_eff * 0.98 && R < best_R && mm <= 64)) {
+      if (eff > best_eff) best_eff = eff;
+      best_R = R;
     }
+    if (q == 1 && R * nk1 <= KR_THREADS / 4) break;  // finer tasks only lose occupancy
   }
-  return best_r;
+  return best_R;
 }
 
 }  // namespace
@@ -633,30 +745,30 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   int zmax = 1;
   for (int s = 0; s < d->nslab_out; ++s) {
     const int nk1 = d->out_dk[s], dm1 = d->out_dm[s];
-    const int R = pick_rows(nk1, dm1);
-    int maxnk2 = 0;
-    double per_row = 8.0;
-    for (int t : by_out[s]) {
-      const int nk2 = d->in_dk[d->t_in[t]];
-      const int g = d->mf_group[d->t_mf[t]];
-      maxnk2 = std::max(maxnk2, nk2);
-      const double kf = d->k_type[d->t_k[t]] == KR_K_COMPLEX ? 4.0 : 2.0;
-      per_row += 4.0 * d->m_width[g] * nk2 + kf * nk1 * nk2 + 16.0;
-    }
+    const int R = pick_task_rows(nk1, dm1);
+    int maxnk2 = 1;
+    for (int t : by_out[s]) maxnk2 = std::max(maxnk2, d->in_dk[d->t_in[t]]);
     for (int i0 = 0; i0 < dm1; i0 += R) {
       const int nr = std::min(R, dm1 - i0);
+      const int q = (nr * nk1 + KR_THREADS - 1) / KR_THREADS;
+      double cost = 200.0;
+      for (int t : by_out[s]) {
+        const int nk2 = d->in_dk[d->t_in[t]];
+        const int g = d->mf_group[d->t_mf[t]];
+        const double kf = d->k_type[d->t_k[t]] == KR_K_COMPLEX ? 4.0 : 2.0;
+        const int qz = (nr * nk2 + KR_THREADS - 1) / KR_THREADS;
+        cost += 4.0 * qz * d->m_width[g] + kf * q * nk2 + 60.0;
+      }
       task_slab.push_back(s);
       task_row0.push_back(i0);
       task_nrows.push_back(nr);
-      // cost in lane-slots: pairs are processed 32 at a time
-      const int q = (nr * nk1 + 31) / 32;
-      task_cost.push_back(per_row * nr * double(32 * q) / double(std::max(1, nr * nk1)));
-      zmax = std::max(zmax, nr * std::max(1, maxnk2));
+      task_cost.push_back(cost);
+      zmax = std::max(zmax, nr * maxnk2);
     }
   }
   const int ntask = (int)task_slab.size();
-  op->smem = (size_t)KR_WARPS * zmax * sizeof(double2);
-  if (op->smem > 160 * 1024) {
+  op->smem = (size_t)2 * zmax * sizeof(double2);
+  if (op->smem > 100 * 1024) {
     kr_op_destroy(op);
     return set_err(ctx, KR_ERR_UNSUPPORTED, "Z staging buffer exceeds shared memory");
   }
@@ -668,31 +780,40 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
     kr_op_destroy(op);
     return set_err(ctx, KR_ERR_CUDA, "kr_step_kernel cannot be resident");
   }
-  int grid = ctx->nsm * std::min(occ, 1);
-  const int by_work = (ntask + KR_WARPS - 1) / KR_WARPS;
-  grid = std::max(1, std::min(grid, by_work));
+  int grid = ctx->nsm * std::min(occ, 2);
+  grid = std::max(1, std::min(grid, ntask));
   op->grid = grid;
-  const int nwarps = grid * KR_WARPS;
 
-  // longest-processing-time assignment of tasks to warps
-  std::vector<int> order(ntask);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return task_cost[x] > task_cost[y]; });
-  using Item = std::pair<double, int>;
-  std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
-  for (int w = 0; w < nwarps; ++w) heap.push({0.0, w});
-  std::vector<std::vector<int>> wl(nwarps);
-  for (int t : order) {
-    Item it = heap.top();
-    heap.pop();
-    wl[it.second].push_back(t);
-    heap.push({it.first + task_cost[t], it.second});
+  // tasks are handed out dynamically, most expensive first
+  std::vector<int> task_order(ntask);
+  std::iota(task_order.begin(), task_order.end(), 0);
+  std::stable_sort(task_order.begin(), task_order.end(),
+                   [&](int x, int y) { return task_cost[x] > task_cost[y]; });
+
+  // K blocks transposed: KT[b][a] (complex blocks keep (re, im) pairs)
+  std::vector<double> k_t(d->k_data, d->k_data + d->k_data_len);
+  for (int b = 0; b < d->nk; ++b) {
+    const int r = d->k_rows[b], c = d->k_cols[b];
+    const int words = d->k_type[b] == KR_K_COMPLEX ? 2 : 1;
+    const double* src = d->k_data + d->k_off[b];
+    double* dst = k_t.data() + d->k_off[b];
+    for (int a = 0; a < r; ++a)
+      for (int bb = 0; bb < c; ++bb)
+        for (int w = 0; w < words; ++w) dst[(bb * r + a) * words + w] = src[(a * c + bb) * words + w];
   }
-  std::vector<int> warp_task_ptr(nwarps + 1, 0), warp_tasks;
-  for (int w = 0; w < nwarps; ++w) {
-    std::sort(wl[w].begin(), wl[w].end());
-    warp_task_ptr[w + 1] = warp_task_ptr[w] + (int)wl[w].size();
-    warp_tasks.insert(warp_tasks.end(), wl[w].begin(), wl[w].end());
+  // value class of every (group, cart) of the M factors
+  std::vector<signed char> m_ctype((size_t)std::max(1, d->nm) * KR_MAXCART, 3);
+  for (int g = 0; g < d->nm; ++g) {
+    const long long ne = (long long)d->m_rows[g] * d->m_width[g];
+    for (int c = 0; c < d->m_ncart[g]; ++c) {
+      bool any_re = false, any_im = false;
+      for (long long e = 0; e < ne; ++e) {
+        const double* v = d->m_val + 2 * (d->m_val_off[g] + c * ne + e);
+        any_re |= v[0] != 0.0;
+        any_im |= v[1] != 0.0;
+      }
+      m_ctype[g * KR_MAXCART + c] = (!any_re && !any_im) ? 3 : (!any_im ? 1 : (!any_re ? 2 : 0));
+    }
   }
 
   // ---- uploads --------------------------------------------------------------
@@ -717,7 +838,7 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   UP(d->k_cols, d->nk, &p_i); D.k_cols = p_i;
   UP(d->k_type, d->nk, &p_i); D.k_type = p_i;
   double* p_d;
-  UP(d->k_data, d->k_data_len, &p_d); D.k_data = p_d;
+  UP(k_t.data(), k_t.size(), &p_d); D.k_data = p_d;
   UP((const long long*)inst_ptr.data(), d->nmf, &p_l); D.mf_off = p_l;
   UP((const long long*)mf_col_off.data(), d->nmf, &p_l); D.mf_col_off = p_l;
   UP(mf_width.data(), d->nmf, &p_i); D.mf_width = p_i;
@@ -731,8 +852,11 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   UP(task_slab.data(), ntask, &p_i); D.task_slab = p_i;
   UP(task_row0.data(), ntask, &p_i); D.task_row0 = p_i;
   UP(task_nrows.data(), ntask, &p_i); D.task_nrows = p_i;
-  UP(warp_task_ptr.data(), warp_task_ptr.size(), &p_i); D.warp_task_ptr = p_i;
-  UP(warp_tasks.data(), warp_tasks.size(), &p_i); D.warp_tasks = p_i;
+  UP(task_order.data(), task_order.size(), &p_i); D.task_order = p_i;
+  D.ntask = ntask;
+  unsigned* p_u;
+  UP((const unsigned*)nullptr, (size_t)KR_MATVEC_MAXVEC, &p_u); op->mv_counters = p_u;
+  UP((const int*)nullptr, (size_t)std::max(1, d->nmf), &p_i); D.mf_type = p_i;
   D.zmax = zmax;
 
   DevField& F = op->field;
@@ -747,6 +871,10 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   UP(d->m_width, d->nm, &p_i); F.m_width = p_i;
   UP((const double2*)d->m_val, d->m_val_len / 2, &p_c); F.m_val = p_c;
   F.mf_val = D.mf_val;
+  F.nmf = d->nmf;
+  F.mf_type = const_cast<int*>(D.mf_type);
+  signed char* p_s;
+  UP(m_ctype.data(), m_ctype.size(), &p_s); F.m_ctype = p_s;
 
   // ---- step scratch (sized once: kr_step allocates nothing) -----------------
   if (op->square) {
@@ -758,11 +886,12 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
     UP((const double2*)nullptr, (size_t)n, &p_c); op->ub0 = p_c;
     UP((const double2*)nullptr, (size_t)n, &p_c); op->ub1 = p_c;
     UP((const double2*)nullptr, (size_t)grid, &p_c); op->part_a = p_c;
+    UP((const double2*)nullptr, (size_t)ntask, &p_c); op->task_alpha = p_c;
+    UP((const unsigned*)nullptr, (size_t)d->maxorder + 2, &p_u); op->counters = p_u;
     UP((const double*)nullptr, (size_t)grid, &p_d); op->part_b = p_d;
     UP((const double*)nullptr, (size_t)grid, &p_d); op->part_c = p_d;
     UP((const double2*)nullptr, (size_t)d->maxorder + 1, &p_c); op->alpha = p_c;
     UP((const double*)nullptr, (size_t)d->maxorder + 1, &p_d); op->beta = p_d;
-    unsigned* p_u;
     UP((const unsigned*)nullptr, 2, &p_u); op->bar = p_u;
     UP((const int*)nullptr, 2, &p_i); op->status = p_i;
   }
@@ -783,9 +912,10 @@ extern "C" int kr_set_field(kr_op* op, const double* coef, const double* scale, 
     c.scale[p] = make_double2(scale[2 * p], scale[2 * p + 1]);
     c.thresh[p] = thresh[p];
   }
-  if (op->field.nent == 0) return KR_OK;
+  if (op->field.nent == 0 && op->field.nmf == 0) return KR_OK;
   const int threads = 256;
-  const int blocks = (int)std::min<long long>((op->field.nent + threads - 1) / threads, 4LL * op->ctx->nsm);
+  const long long work = std::max<long long>(op->field.nent, op->field.nmf);
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((work + threads - 1) / threads, 4LL * op->ctx->nsm));
   kr_field_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(op->field, c);
   op->launches++;
   KR_CUDA(op->ctx, cudaGetLastError());
@@ -795,9 +925,11 @@ extern "C" int kr_set_field(kr_op* op, const double* coef, const double* scale, 
 extern "C" int kr_matvec(kr_op* op, const void* x, void* y, int64_t nvec, void* stream) {
   if (!op || !x || !y || nvec < 0) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_matvec: bad argument");
   if (nvec == 0) return KR_OK;
-  if (nvec > 65535) return set_err(op->ctx, KR_ERR_ARG, "kr_matvec: nvec above 65535");
+  if (nvec > KR_MATVEC_MAXVEC) return set_err(op->ctx, KR_ERR_ARG, "kr_matvec: nvec above 65535");
+  KR_CUDA(op->ctx, cudaMemsetAsync(op->mv_counters, 0, sizeof(unsigned) * nvec, (cudaStream_t)stream));
   dim3 g(op->grid, (unsigned)nvec);
-  kr_matvec_kernel<<<g, KR_THREADS, op->smem, (cudaStream_t)stream>>>(op->dev, (const double2*)x, (double2*)y);
+  kr_matvec_kernel<<<g, KR_THREADS, op->smem, (cudaStream_t)stream>>>(op->dev, (const double2*)x, (double2*)y,
+                                                                      op->mv_counters);
   op->launches++;
   KR_CUDA(op->ctx, cudaGetLastError());
   return KR_OK;
@@ -831,6 +963,8 @@ extern "C" int kr_step(kr_op* op, void* states, int64_t nvec, const void* phase,
   a.ub[0] = op->ub0;
   a.ub[1] = op->ub1;
   a.part_a = op->part_a;
+  a.task_alpha = op->task_alpha;
+  a.counters = op->counters;
   a.part_b = op->part_b;
   a.part_c = op->part_c;
   a.alpha = op->alpha;

@@ -43,7 +43,10 @@ TMAT_S = {
                  [0, 0, -0.5, 0, 0, -0.5j, -0.5, -0.5j, 0],
                  [0.5, 0.5j, 0, 0.5j, -0.5, 0, 0, 0, 0]], dtype=np.complex128),
 }
-TMAT_X = {k: np.linalg.pinv(v) for k, v in TMAT_S.items()}
+# The reference inverts with np.linalg.pinv (rot/labtens.py:104); the maps are
+# unitary, so the exact inverse is the conjugate transpose. It agrees with pinv
+# to 2.5e-16 and keeps purely real / imaginary entries free of round-off.
+TMAT_X = {k: np.ascontiguousarray(v.conj().T) for k, v in TMAT_S.items()}
 CART_IND = {1: ["x", "y", "z"], 2: ["xx", "xy", "xz", "yx", "yy", "yz", "zx", "zy", "zz"]}
 IRREP_IND = {1: [(1, -1), (1, 0), (1, 1)], 2: [(o, s) for o in range(3) for s in range(-o, o + 1)]}
 
