@@ -136,6 +136,30 @@ int kr_step(kr_op* op, void* states, int64_t nvec, const void* phase,
             double fac_re, double fac_im, double tol, uint32_t flags,
             int32_t* korder, void* stream);
 
+/* Allocation-free variant of kr_step, no counterpart in the reference.
+ * Same arguments and results as kr_step, but the Krylov workspace lives in a
+ * fixed 64 MiB array inside the library (a file-scope __device__ array that
+ * every GPU loading the library holds until exit) instead of the workspace
+ * kr_op_create allocated. It is for callers that must not allocate device
+ * memory at step time: code recorded into CUDA graphs, or hosts whose device
+ * memory is owned by their own pool allocator. It calls no cudaMalloc,
+ * cudaFree or allocating library routine. Limits and rules:
+ *   - operators whose workspace exceeds the array (kr_static_scratch_bytes;
+ *     about dim * (maxorder + 5) * 16 bytes) are rejected with KR_ERR_ARG;
+ *   - the first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress with that device current); make that first call
+ *     before any stream capture;
+ *   - all calls share the array and it keeps the previous call's contents:
+ *     calls that overlap on the GPU (other streams, other threads) race;
+ *   - with korder == NULL a device-side error is copied into op's status and
+ *     reported by kr_sync_status. */
+int kr_step_static(kr_op* op, void* states, int64_t nvec, const void* phase,
+                   double fac_re, double fac_im, double tol, uint32_t flags,
+                   int32_t* korder, void* stream);
+
+/* Bytes of static scratch kr_step_static needs for op, and the capacity. */
+int kr_static_scratch_bytes(const kr_op* op, size_t* needed, size_t* capacity);
+
 /* Synchronises the stream and returns the pending device-side status of op. */
 int kr_sync_status(kr_op* op, void* stream);
 

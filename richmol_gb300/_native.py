@@ -28,7 +28,7 @@ KR_STEP_SKIP_KRYLOV = 1
 EXPORTED = [
     "kr_ctx_create", "kr_ctx_destroy", "kr_last_error", "kr_op_create", "kr_op_destroy",
     "kr_set_field", "kr_matvec", "kr_step", "kr_sync_status", "kr_op_launch_count", "kr_op_work",
-    "kr_probe_fp64",
+    "kr_probe_fp64", "kr_step_static", "kr_static_scratch_bytes",
 ]
 
 
@@ -113,6 +113,10 @@ def lib():
         L.kr_op_launch_count.restype = i64
         L.kr_op_work.argtypes = [vp, ctypes.POINTER(dbl), ctypes.POINTER(dbl)]
         L.kr_op_work.restype = ctypes.c_int
+        L.kr_step_static.argtypes = [vp, vp, i64, vp, dbl, dbl, dbl, ctypes.c_uint32, vp, vp]
+        L.kr_step_static.restype = ctypes.c_int
+        L.kr_static_scratch_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]
+        L.kr_static_scratch_bytes.restype = ctypes.c_int
         L.kr_probe_fp64.argtypes = [vp, ctypes.POINTER(dbl)]
         L.kr_probe_fp64.restype = ctypes.c_int
         _lib = L

@@ -1065,3 +1065,154 @@ extern "C" int kr_probe_fp64(kr_ctx* ctx, double* tflops) {
   *tflops = 5.0 * 2.0 * 8.0 * iters * double(blocks) * threads / (ms * 1e-3) / 1e12;
   return KR_OK;
 }
+
+// ===========================================================================
+// Allocation-free step: kr_step with its Krylov workspace in a fixed,
+// file-scope device array instead of the workspace kr_op_create allocated.
+// For callers that must not allocate device memory when they step: code that
+// records the step into a CUDA graph or runs inside a framework that owns all
+// device memory through its own pool. Every GPU that loads this library holds
+// the array (KR_STATIC_SCRATCH_BYTES) until the process exits.
+// ===========================================================================
+#define KR_STATIC_SCRATCH_BYTES (64ull << 20)  // 64 MiB
+
+static __device__ __align__(256) unsigned char g_kr_static_scratch[KR_STATIC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_static_mu;
+void* g_static_addr[128] = {};  // device address of g_kr_static_scratch, per device
+
+size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
+}  // namespace
+
+// copies a device-side error of the static scratch into the operator's status
+// word (kept if that one already holds an error), so kr_sync_status sees it
+__global__ void kr_status_merge_kernel(int* dst, const int* src) {
+  if (threadIdx.x == 0 && blockIdx.x == 0 && *dst == 0) *dst = *src;
+}
+
+extern "C" int kr_static_scratch_bytes(const kr_op* op, size_t* needed, size_t* capacity) {
+  if (capacity) *capacity = KR_STATIC_SCRATCH_BYTES;
+  if (!op) return KR_ERR_ARG;
+  const size_t n = (size_t)op->dev.dim_out, m = (size_t)op->maxorder;
+  size_t b = 0;
+  b += round256(sizeof(double2) * n * m);                    // V
+  b += 5 * round256(sizeof(double2) * n);                    // W[2], w, u[2]
+  b += round256(sizeof(double2) * op->grid);                 // part_a
+  b += 2 * round256(sizeof(double) * op->grid);              // part_b, part_c
+  b += round256(sizeof(double2) * op->dev.ntask);            // task_alpha
+  b += round256(sizeof(unsigned) * (m + 2));                 // counters
+  b += round256(sizeof(double2) * (m + 1));                  // alpha
+  b += round256(sizeof(double) * (m + 1));                   // beta
+  b += round256(sizeof(unsigned) * 2);                       // barrier
+  b += round256(sizeof(int) * 2);                            // status, Krylov order
+  if (needed) *needed = b;
+  return KR_OK;
+}
+
+extern "C" int kr_step_static(kr_op* op, void* states, int64_t nvec, const void* phase, double fac_re,
+                              double fac_im, double tol, uint32_t flags, int32_t* korder, void* stream) {
+  if (!op || !states || nvec < 0) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_step_static: bad argument");
+  if (!op->square) return set_err(op->ctx, KR_ERR_ARG, "kr_step_static: operator is not square");
+  if (nvec == 0) return KR_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long n = op->dev.dim_out;
+  if (flags & KR_STEP_SKIP_KRYLOV) {  // no scratch needed
+    if (phase) {
+      const int blocks = (int)std::min<long long>((n * nvec + 255) / 256, 8LL * op->ctx->nsm);
+      kr_phase2_kernel<<<blocks, 256, 0, st>>>((double2*)states, (const double2*)phase, n, nvec);
+      op->launches++;
+      KR_CUDA(op->ctx, cudaGetLastError());
+    }
+    if (korder)
+      for (int64_t v = 0; v < nvec; ++v) korder[v] = 0;
+    return KR_OK;
+  }
+  size_t need = 0;
+  kr_static_scratch_bytes(op, &need, nullptr);
+  if (need > KR_STATIC_SCRATCH_BYTES)
+    return set_err(op->ctx, KR_ERR_ARG,
+                   "kr_step_static: this operator needs " + std::to_string(need) +
+                       " bytes of Krylov workspace (dim " + std::to_string(n) + ", maxorder " +
+                       std::to_string(op->maxorder) + "), the static scratch holds " +
+                       std::to_string((unsigned long long)KR_STATIC_SCRATCH_BYTES) + " bytes; use kr_step");
+  const int dev = op->ctx->device;
+  if (dev < 0 || dev >= 128) return set_err(op->ctx, KR_ERR_UNSUPPORTED, "kr_step_static: device index above 127");
+  unsigned char* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    if (!g_static_addr[dev]) {
+      // set-up, once per device, with that device current
+      KR_CUDA(op->ctx, cudaSetDevice(dev));
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_kr_static_scratch);
+      if (e != cudaSuccess || !p)
+        return set_err(op->ctx, KR_ERR_CUDA,
+                       std::string("kr_step_static: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+      g_static_addr[dev] = p;
+    }
+    base = static_cast<unsigned char*>(g_static_addr[dev]);
+  }
+  const size_t m = (size_t)op->maxorder;
+  size_t off = 0;
+  auto carve = [&](size_t bytes) {
+    unsigned char* p = base + off;
+    off += round256(bytes);
+    return p;
+  };
+  StepArgs a;
+  a.op = op->dev;
+  a.phase = (const double2*)phase;
+  a.V = (double2*)carve(sizeof(double2) * n * m);
+  a.Wb[0] = (double2*)carve(sizeof(double2) * n);
+  a.Wb[1] = (double2*)carve(sizeof(double2) * n);
+  a.w = (double2*)carve(sizeof(double2) * n);
+  a.ub[0] = (double2*)carve(sizeof(double2) * n);
+  a.ub[1] = (double2*)carve(sizeof(double2) * n);
+  a.part_a = (double2*)carve(sizeof(double2) * op->grid);
+  a.part_b = (double*)carve(sizeof(double) * op->grid);
+  a.part_c = (double*)carve(sizeof(double) * op->grid);
+  a.task_alpha = (double2*)carve(sizeof(double2) * op->dev.ntask);
+  a.counters = (unsigned*)carve(sizeof(unsigned) * (m + 2));
+  a.alpha = (double2*)carve(sizeof(double2) * (m + 1));
+  a.beta = (double*)carve(sizeof(double) * (m + 1));
+  unsigned* bar = (unsigned*)carve(sizeof(unsigned) * 2);
+  int* status = (int*)carve(sizeof(int) * 2);
+  a.bar_count = bar;
+  a.bar_gen = bar + 1;
+  a.status = status;
+  a.kout = status + 1;
+  a.fac = make_double2(fac_re, fac_im);
+  a.tol = tol;
+  a.maxorder = op->maxorder;
+  a.dim = n;
+  // the array keeps the previous call's contents: clear the arrival count and
+  // the status word (task counters are cleared by the kernel itself)
+  KR_CUDA(op->ctx, cudaMemsetAsync(status, 0, 2 * sizeof(int), st));
+  for (int64_t v = 0; v < nvec; ++v) {
+    a.state = (double2*)states + v * n;
+    KR_CUDA(op->ctx, cudaMemsetAsync(bar, 0, sizeof(unsigned), st));
+    void* args[] = {&a};
+    KR_CUDA(op->ctx, cudaLaunchCooperativeKernel((void*)kr_step_kernel, dim3(op->grid), dim3(KR_THREADS), args,
+                                                 op->smem, st));
+    op->launches++;
+    if (korder) {
+      int hs[2] = {0, 0};
+      KR_CUDA(op->ctx, cudaMemcpyAsync(hs, status, sizeof(hs), cudaMemcpyDeviceToHost, st));
+      KR_CUDA(op->ctx, cudaStreamSynchronize(st));
+      korder[v] = hs[1];
+      if (hs[0] != 0) {
+        if (hs[0] == KR_ERR_MAXORDER)
+          return set_err(op->ctx, KR_ERR_MAXORDER,
+                         "Lanczos reached maximum order of '" + std::to_string(op->maxorder) + "' without convergence");
+        return set_err(op->ctx, hs[0], "device-side wait gave up (grid barrier timeout)");
+      }
+    }
+  }
+  if (!korder) {
+    kr_status_merge_kernel<<<1, 32, 0, st>>>(op->status, status);
+    op->launches++;
+    KR_CUDA(op->ctx, cudaGetLastError());
+  }
+  return KR_OK;
+}

@@ -1,0 +1,87 @@
+"""The allocation-free step kr_step_static against kr_step, through the C ABI.
+
+kr_step_static keeps its Krylov workspace in a fixed array inside the library,
+so callers that may not allocate device memory when they step (code recorded
+into CUDA graphs, hosts whose device memory belongs to their own pool
+allocator) can still propagate. Its results must equal kr_step's, call after
+call, although the array keeps the previous call's contents. This file is
+collected last on purpose; it passes alone in a fresh process and after the
+other tests."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+STATE_RTOL = 1e-10  # per-step state tolerance of the GPU parity tests
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def _call(entry, plan, v, phase, fac, korder):
+    from richmol_gb300 import _native
+    from richmol_gb300.device import stream_ptr
+    rc = entry(plan.op, v.data_ptr(), v.shape[0], phase.data_ptr(), float(fac.real), float(fac.imag), 1e-15, 0,
+               korder.ctypes.data, stream_ptr())
+    _native.check(rc, plan.ctx)
+
+
+def test_static_scratch_step_matches_kr_step_twice():
+    from richmol_gb300 import CarTens, TDSE, _native
+    if not os.path.exists(_native.LIB_PATH):
+        _native.build_library()
+    L = _native.lib()
+    from oracle import fixtures
+    path = os.path.join(GOLDEN, "asym_j4.npz")
+    d, meta = fixtures.load(path)
+    sc = meta["scales"]
+    h0 = CarTens(path, name="h0")
+    Hdc = (CarTens(path, name="dip") * meta["dc"]) * sc["dc"]
+    Hac = CarTens(path, name="pol") * sc["ac"]
+    td = TDSE(t_start=0.9, t_end=1.0, dt=0.005)
+    td.time_grid()
+    v0 = td.init_state(h0, temp=5, thresh=1e-3)
+    a = torch.from_numpy(v0.copy()).cuda()
+    b = torch.from_numpy(v0.copy()).cuda()
+    phase = td._h0_phase(h0, td.exp_fac, a.device)
+    for i in range(2):  # two calls in a row: the array keeps the previous call's contents
+        Hac.field(d["split/fields"][i])
+        plan = (Hdc + Hac).device_operator()
+        ka = np.zeros(a.shape[0], np.int32)
+        kb = np.zeros(b.shape[0], np.int32)
+        _call(L.kr_step, plan, a, phase, td.exp_fac, ka)
+        _call(L.kr_step_static, plan, b, phase, td.exp_fac, kb)
+        torch.cuda.synchronize()
+        assert np.array_equal(ka, kb)
+        assert _rel(b.cpu().numpy(), a.cpu().numpy()) < STATE_RTOL
+    # and it follows the reference's own propagation
+    ref = d["split/states_first2"][1]
+    assert _rel(b.cpu().numpy()[:2], ref) < STATE_RTOL
+
+
+def test_static_scratch_rejects_oversized_operator():
+    from richmol_gb300 import _native, workloads
+    L = _native.lib()
+    wl = workloads.asym_top(Jmax=32)  # dim 47,905: about 80 MB of workspace at maxorder 100
+    wl.Hac.field([0.0, 0.0, 1e9])
+    plan = wl.Hac.device_operator()
+    need, cap = ctypes.c_size_t(), ctypes.c_size_t()
+    assert L.kr_static_scratch_bytes(plan.op, ctypes.byref(need), ctypes.byref(cap)) == 0
+    assert need.value > cap.value == 64 << 20
+    v = torch.zeros((1, wl.dim), dtype=torch.complex128, device="cuda")
+    v[0, 0] = 1.0
+    before = v.clone()
+    from richmol_gb300.device import stream_ptr
+    rc = L.kr_step_static(plan.op, v.data_ptr(), 1, None, 0.0, -1e-3, 1e-15, 0, None, stream_ptr())
+    assert rc == _native.KR_ERR_ARG
+    assert "static scratch holds" in _native.last_error(plan.ctx)
+    torch.cuda.synchronize()
+    assert torch.equal(v, before)
