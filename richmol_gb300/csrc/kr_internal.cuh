@@ -1,0 +1,74 @@
+// Host/device structures shared by the translation units of the library.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/richmol_gb300.h"
+#include "kr_device.cuh"
+
+struct FieldCoef {
+  int npart;
+  double2 coef[KR_MAXPART][KR_MAXCART];
+  double2 scale[KR_MAXPART];
+  double thresh[KR_MAXPART];
+};
+
+struct DevField {
+  long long nent;
+  int nmf;
+  const signed char* m_ctype;   // [group][KR_MAXCART]: 0 mixed, 1 real, 2 imaginary, 3 all zero
+  int* mf_type;                 // out: per MF instance 0 complex, 1 real, 2 imaginary
+  const int* ent_inst;          // MF instance of each entry
+  const long long* inst_ptr;    // first entry of each instance
+  const int* mf_group; const int* mf_part;
+  const long long* m_val_off; const int* m_ncart; const int* m_rows; const int* m_width;
+  const double2* m_val;
+  double2* mf_val;
+};
+
+struct kr_ctx {
+  int device = 0;
+  int nsm = 0;
+  std::string err;
+};
+
+// records the error message of a failed call (per context and library-wide)
+int kr_set_err(kr_ctx* ctx, int code, const std::string& msg);
+#define set_err kr_set_err
+
+#define KR_CUDA(ctx, call)                                                                 \
+  do {                                                                                     \
+    cudaError_t _e = (call);                                                               \
+    if (_e != cudaSuccess)                                                                 \
+      return set_err((ctx), KR_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+struct kr_op {
+  kr_ctx* ctx = nullptr;
+  DevOp dev{};
+  DevField field{};
+  std::vector<void*> allocs;
+  int grid = 1;
+  size_t smem = 0;
+  int maxorder = 100;
+  bool square = false;
+  int npart = 0;
+  int nmf = 0;
+  long long launches = 0;
+  double fma_per_matvec = 0, bytes_per_matvec = 0;
+  // step scratch
+  double2 *V = nullptr, *Wb0 = nullptr, *Wb1 = nullptr, *w = nullptr, *ub0 = nullptr, *ub1 = nullptr;
+  double2* part_a = nullptr;
+  double2* task_alpha = nullptr;
+  unsigned* counters = nullptr;
+  unsigned* mv_counters = nullptr;
+  double *part_b = nullptr, *part_c = nullptr;
+  double2* alpha = nullptr;
+  double* beta = nullptr;
+  unsigned* bar = nullptr;  // [count, gen]
+  int* status = nullptr;    // [status, kout]
+};
+

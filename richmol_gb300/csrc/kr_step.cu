@@ -19,8 +19,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/richmol_gb300.h"
-#include "kr_device.cuh"
+#include "kr_internal.cuh"
 
 #define KR_EXPM_MAX 128  // capacity of the tridiagonal exponential (maxorder <= 128)
 #define KR_MATVEC_MAXVEC 65535  // vectors of one kr_matvec call (grid.y)
@@ -28,25 +27,7 @@
 // ===========================================================================
 // field contraction: MF = scale * thr(sum_c coef_c M_c)
 // ===========================================================================
-struct FieldCoef {
-  int npart;
-  double2 coef[KR_MAXPART][KR_MAXCART];
-  double2 scale[KR_MAXPART];
-  double thresh[KR_MAXPART];
-};
 
-struct DevField {
-  long long nent;
-  int nmf;
-  const signed char* m_ctype;   // [group][KR_MAXCART]: 0 mixed, 1 real, 2 imaginary, 3 all zero
-  int* mf_type;                 // out: per MF instance 0 complex, 1 real, 2 imaginary
-  const int* ent_inst;          // MF instance of each entry
-  const long long* inst_ptr;    // first entry of each instance
-  const int* mf_group; const int* mf_part;
-  const long long* m_val_off; const int* m_ncart; const int* m_rows; const int* m_width;
-  const double2* m_val;
-  double2* mf_val;
-};
 
 // class of a complex number: 3 zero, 1 real, 2 imaginary, 0 general
 __device__ __forceinline__ int cclass(double2 z) {
@@ -481,56 +462,19 @@ __global__ void __launch_bounds__(KR_THREADS, 2) kr_step_kernel(StepArgs a) {
 // ===========================================================================
 // host side
 // ===========================================================================
-struct kr_ctx {
-  int device = 0;
-  int nsm = 0;
-  std::string err;
-};
-
 namespace {
 std::mutex g_err_mu;
 std::string g_err;
+}  // namespace
 
-int set_err(kr_ctx* ctx, int code, const std::string& msg) {
+int kr_set_err(kr_ctx* ctx, int code, const std::string& msg) {
   if (ctx) ctx->err = msg;
   std::lock_guard<std::mutex> lk(g_err_mu);
   g_err = msg;
   return code;
 }
-}  // namespace
 
-#define KR_CUDA(ctx, call)                                                                 \
-  do {                                                                                     \
-    cudaError_t _e = (call);                                                               \
-    if (_e != cudaSuccess)                                                                 \
-      return set_err((ctx), KR_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
-  } while (0)
 
-struct kr_op {
-  kr_ctx* ctx = nullptr;
-  DevOp dev{};
-  DevField field{};
-  std::vector<void*> allocs;
-  int grid = 1;
-  size_t smem = 0;
-  int maxorder = 100;
-  bool square = false;
-  int npart = 0;
-  int nmf = 0;
-  long long launches = 0;
-  double fma_per_matvec = 0, bytes_per_matvec = 0;
-  // step scratch
-  double2 *V = nullptr, *Wb0 = nullptr, *Wb1 = nullptr, *w = nullptr, *ub0 = nullptr, *ub1 = nullptr;
-  double2* part_a = nullptr;
-  double2* task_alpha = nullptr;
-  unsigned* counters = nullptr;
-  unsigned* mv_counters = nullptr;
-  double *part_b = nullptr, *part_c = nullptr;
-  double2* alpha = nullptr;
-  double* beta = nullptr;
-  unsigned* bar = nullptr;  // [count, gen]
-  int* status = nullptr;    // [status, kout]
-};
 
 template <typename T>
 static int upload(kr_op* op, const T* host, size_t count, T** dev) {
