@@ -160,6 +160,41 @@ int kr_step_static(kr_op* op, void* states, int64_t nvec, const void* phase,
 /* Bytes of static scratch kr_step_static needs for op, and the capacity. */
 int kr_static_scratch_bytes(const kr_op* op, size_t* needed, size_t* capacity);
 
+/* ------------------------------------------------------------------------
+ * Batched mixed-precision ensembles. The reference propagates the vectors of
+ * an ensemble one by one (tdse.py:379-382 and 398-402, each through
+ * _expmv_lanczos, tdse.py:417-486); a batch propagates them together, each
+ * with its own Krylov order: complex64 mat-vec with FP32 accumulation,
+ * complex64 Krylov basis with full orthogonalisation, FP64 Lanczos scalars,
+ * tridiagonal exponential, a-posteriori error estimate and FP64 state.
+ * ------------------------------------------------------------------------ */
+typedef struct kr_batch kr_batch;
+
+/* Allocates the batch state and Krylov basis for nvec vectors of op's basis
+ * (mmax basis vectors, 2 <= mmax <= 31). */
+int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch** out);
+void kr_batch_destroy(kr_batch* b);
+/* states (nvec, dim) complex128 device <-> the batch's internal layout. */
+int kr_batch_load(kr_batch* b, const void* states, void* stream);
+int kr_batch_store(kr_batch* b, void* states, void* stream);
+/* One TDSE.update of every vector (split operator when phase != NULL):
+ * op carries H with its field set (kr_set_field); each vector stops at the
+ * first Krylov order whose error estimate is <= tol (times nothing: absolute,
+ * in the norm of the vector). *kmax_out: largest order used. Synchronises
+ * once per Krylov iteration; KR_ERR_MAXORDER if a vector needs more than mmax. */
+int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double fac_re, double fac_im,
+                  double tol, int32_t* kmax_out, void* stream);
+/* Krylov order used by each vector in the last step (host int32[nvec]). */
+int kr_batch_korder(kr_batch* b, int32_t* korder, void* stream);
+/* <v|O|v> for every vector (host complex128[nvec], interleaved), O = obs
+ * with its field set (e.g. cos^2 theta with field [0, 0, 1]); complex64
+ * mat-vec, FP64 dot products. Synchronises. */
+int kr_batch_expect(kr_batch* b, kr_op* obs, double* out, void* stream);
+/* W = op V_0 for every vector (complex64), the batched mat-vec alone
+ * (V_0 holds the normalised, phased states after a step). */
+int kr_batch_matvec(kr_batch* b, kr_op* op, void* stream);
+int64_t kr_batch_launch_count(const kr_batch* b);
+
 /* Synchronises the stream and returns the pending device-side status of op. */
 int kr_sync_status(kr_op* op, void* stream);
 

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(PKG)
 LIB_DIR = os.path.join(PKG, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "librichmol_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
-SOURCES = [os.path.join(PKG, "csrc", "kr_step.cu")]
+SOURCES = [os.path.join(PKG, "csrc", "kr_step.cu"), os.path.join(PKG, "csrc", "kr_batch.cu")]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 KR_OK, KR_ERR_ARG, KR_ERR_CUDA, KR_ERR_MAXORDER, KR_ERR_TIMEOUT, KR_ERR_UNSUPPORTED = range(6)
@@ -29,6 +29,8 @@ EXPORTED = [
     "kr_ctx_create", "kr_ctx_destroy", "kr_last_error", "kr_op_create", "kr_op_destroy",
     "kr_set_field", "kr_matvec", "kr_step", "kr_sync_status", "kr_op_launch_count", "kr_op_work",
     "kr_probe_fp64", "kr_step_static", "kr_static_scratch_bytes",
+    "kr_batch_create", "kr_batch_destroy", "kr_batch_load", "kr_batch_store", "kr_batch_step",
+    "kr_batch_korder", "kr_batch_expect", "kr_batch_launch_count", "kr_batch_matvec",
 ]
 
 
@@ -117,6 +119,24 @@ def lib():
         L.kr_step_static.restype = ctypes.c_int
         L.kr_static_scratch_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]
         L.kr_static_scratch_bytes.restype = ctypes.c_int
+        L.kr_batch_create.argtypes = [vp, i64, i32, ctypes.POINTER(vp)]
+        L.kr_batch_create.restype = ctypes.c_int
+        L.kr_batch_destroy.argtypes = [vp]
+        L.kr_batch_destroy.restype = None
+        L.kr_batch_load.argtypes = [vp, vp, vp]
+        L.kr_batch_load.restype = ctypes.c_int
+        L.kr_batch_store.argtypes = [vp, vp, vp]
+        L.kr_batch_store.restype = ctypes.c_int
+        L.kr_batch_step.argtypes = [vp, vp, vp, dbl, dbl, dbl, ctypes.POINTER(i32), vp]
+        L.kr_batch_step.restype = ctypes.c_int
+        L.kr_batch_korder.argtypes = [vp, vp, vp]
+        L.kr_batch_korder.restype = ctypes.c_int
+        L.kr_batch_expect.argtypes = [vp, vp, vp, vp]
+        L.kr_batch_expect.restype = ctypes.c_int
+        L.kr_batch_matvec.argtypes = [vp, vp, vp]
+        L.kr_batch_matvec.restype = ctypes.c_int
+        L.kr_batch_launch_count.argtypes = [vp]
+        L.kr_batch_launch_count.restype = i64
         L.kr_probe_fp64.argtypes = [vp, ctypes.POINTER(dbl)]
         L.kr_probe_fp64.restype = ctypes.c_int
         _lib = L

@@ -1,0 +1,103 @@
+"""Batched mixed-precision propagation of ensembles (thermal ensembles, many
+initial states) on the GPU.
+
+The reference propagates the vectors of an ensemble one after another
+(richmol/tdse.py:379-382) with the FP64 Lanczos of tdse.py:417-486. An
+``Ensemble`` moves all vectors at once through the C ABI (kr_batch_*): complex64
+mat-vec with FP32 accumulation, complex64 Krylov basis with full
+orthogonalisation, FP64 Lanczos scalars, tridiagonal exponential and
+a-posteriori error estimate (each vector stops at its own Krylov order), FP64
+state and H0 half-phases. Observables are weighted sums of per-vector
+expectation values, so Boltzmann weights can be applied at the end
+(equivalent, by linearity, to the sqrt(w)-weighted vectors of tdse.py:256-257).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native
+from .device import stream_ptr
+
+
+class Ensemble:
+    """nvec state vectors of one basis, propagated together.
+
+    Args:
+        tdse : richmol_gb300.TDSE   time grid, units (exp factor)
+        H0 : CarTens or None        field-free Hamiltonian for the split operator
+        nvec : int
+        tol : float                 per-vector error tolerance of the Krylov step
+        mmax : int                  maximum Krylov order (<= 31)
+    """
+
+    def __init__(self, tdse, H0, nvec, tol=1e-8, mmax=20, template=None):
+        self.tdse = tdse
+        self.H0 = H0
+        self.nvec = int(nvec)
+        self.tol = float(tol)
+        self.mmax = int(mmax)
+        self.template = template if template is not None else H0
+        self._plan0 = self.template._plan()
+        self.dim = self._plan0.dim_out
+        self.ctx = self._plan0.ctx
+        h = ctypes.c_void_p()
+        _native.check(_native.lib().kr_batch_create(self._plan0.op, self.nvec, self.mmax, ctypes.byref(h)), self.ctx)
+        self.handle = h
+        self.phase = None
+        self.last_kmax = 0
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            try:
+                _native.lib().kr_batch_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def load(self, vecs):
+        """vecs: (nvec, dim) complex128, numpy or CUDA tensor."""
+        v = vecs if torch.is_tensor(vecs) else torch.from_numpy(np.ascontiguousarray(vecs, np.complex128))
+        v = v.to("cuda", torch.complex128).contiguous()
+        assert v.shape == (self.nvec, self.dim)
+        self._keep = v
+        _native.check(_native.lib().kr_batch_load(self.handle, v.data_ptr(), stream_ptr()), self.ctx)
+
+    def store(self, out=None):
+        if out is None:
+            out = torch.empty((self.nvec, self.dim), dtype=torch.complex128, device="cuda")
+        _native.check(_native.lib().kr_batch_store(self.handle, out.data_ptr(), stream_ptr()), self.ctx)
+        return out
+
+    def step(self, H):
+        """One TDSE.update of every vector with the field-dressed H."""
+        exp_fac = self.tdse.exp_fac
+        phase = None
+        if self.H0 is not None:
+            phase = self.tdse._h0_phase(self.H0, exp_fac, torch.device("cuda", torch.cuda.current_device()))
+        plan = H.device_operator()
+        kmax = ctypes.c_int32()
+        rc = _native.lib().kr_batch_step(self.handle, plan.op, None if phase is None else phase.data_ptr(),
+                                         float(exp_fac.real), float(exp_fac.imag), self.tol, ctypes.byref(kmax),
+                                         stream_ptr())
+        _native.check(rc, self.ctx)
+        self.last_kmax = kmax.value
+
+    def korder(self):
+        out = np.zeros(self.nvec, np.int32)
+        _native.check(_native.lib().kr_batch_korder(self.handle, out.ctypes.data, stream_ptr()), self.ctx)
+        return out
+
+    def expect(self, O):
+        """<v|O|v> for every vector (complex128 numpy array). O is an H0-type
+        tensor such as cos^2(theta); its field [0, 0, 1] is set here."""
+        if not O._is_sum and O._parts[0].prods is None:
+            O.field([0, 0, 1])
+        plan = O.device_operator()
+        out = np.zeros(2 * self.nvec, np.float64)
+        _native.check(_native.lib().kr_batch_expect(self.handle, plan.op, out.ctypes.data, stream_ptr()), self.ctx)
+        return out.view(np.complex128)
+
+    def launches(self):
+        return int(_native.lib().kr_batch_launch_count(self.handle))

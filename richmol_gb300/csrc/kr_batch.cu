@@ -1,0 +1,734 @@
+// Batched mixed-precision Krylov step for ensembles of state vectors
+// (thermal ensembles, many initial states) on GB300 (sm_103a).
+//
+// The reference propagates the vectors of an ensemble one after another with
+// the FP64 Lanczos of richmol/tdse.py:379-382 / 417-486. Here all vectors move
+// together, each with its own Krylov order:
+//   * layout: every vector-valued array is vector-minor, [dim][nb] (nb = nvec
+//     rounded up to 32), so a thread owns one vector and the factors K, MF are
+//     the same for all threads of a block (broadcast reads);
+//   * mat-vec in complex64 with FP32 accumulation (the Kronecker contraction of
+//     field.py:1212-1243, term by term);
+//   * Krylov basis in complex64, full classical Gram-Schmidt orthogonalisation
+//     against every basis vector, dot products accumulated in FP64 across chunks;
+//   * FP64 per-vector scalars: alpha, beta, the tridiagonal exponential
+//     exp(fac T) e0 (Taylor series on the vector) and the a-posteriori error
+//     estimate |fac| beta_k |[exp(fac T_k)]_{k,0}| ||v|| (Saad, SIAM J. Numer.
+//     Anal. 29 (1992) 209) that stops each vector at its own order;
+//   * FP64 state and H0 half-phases.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "kr_internal.cuh"
+
+#define KB_MV_THREADS 128      // vectors per mat-vec block
+#define KB_RED_CHUNKS 256      // element chunks of the per-vector reductions
+#define KB_NK_MAX 32           // largest n_k of the batched mat-vec
+
+struct kr_batch {
+  kr_op* op = nullptr;
+  int nvec = 0, nb = 0, mmax = 0;
+  long long dim = 0;
+  std::vector<void*> allocs;
+  double2* S = nullptr;      // [dim][nb] state, FP64
+  float2* V = nullptr;       // [mmax + 1][dim][nb] Krylov basis
+  float2* W = nullptr;       // [dim][nb] H V_k
+  double* norm0 = nullptr;   // [nb]
+  double2* h = nullptr;      // [mmax + 1][nb] reduced dot products
+  double2* alpha = nullptr;  // [mmax + 1][nb]
+  double* beta = nullptr;    // [mmax + 1][nb]
+  double2* c = nullptr;      // [mmax + 1][nb] exp(fac T) e0 of the converged order
+  double* vscale = nullptr;  // [nb] 1 / beta_k of the newest basis vector
+  int* kconv = nullptr;      // [nb] converged Krylov order (0: still active)
+  int* active = nullptr;     // [nb]
+  int* grp_active = nullptr; // [nb / KB_MV_THREADS rounded up]
+  double* err = nullptr;     // [nb]
+  double2* part = nullptr;   // [KB_RED_CHUNKS][mmax + 2][nb] partial sums
+  int* counts = nullptr;     // [2]: active vectors, vectors that hit mmax
+  // mat-vec row table
+  int nrows = 0;
+  int* row_slab = nullptr;
+  int* row_i = nullptr;
+  long long launches = 0;
+};
+
+// plain-data view of a batch for kernels
+struct BatchDev {
+  int nvec, nb, mmax;
+  long long dim;
+  double2* S;
+  float2* V;
+  double* norm0;
+  double2* h;
+  double2* alpha;
+  double* beta;
+  double2* c;
+  double* vscale;
+  int* kconv;
+  int* active;
+  double* err;
+  int* counts;
+};
+
+static BatchDev dev_view(const kr_batch* b) {
+  BatchDev d;
+  d.nvec = b->nvec;
+  d.nb = b->nb;
+  d.mmax = b->mmax;
+  d.dim = b->dim;
+  d.S = b->S;
+  d.V = b->V;
+  d.norm0 = b->norm0;
+  d.h = b->h;
+  d.alpha = b->alpha;
+  d.beta = b->beta;
+  d.c = b->c;
+  d.vscale = b->vscale;
+  d.kconv = b->kconv;
+  d.active = b->active;
+  d.err = b->err;
+  d.counts = b->counts;
+  return d;
+}
+
+// ---------------------------------------------------------------------------
+// vector-minor elementwise helpers: block = (32 lanes -> vectors, 8 warps ->
+// element streams); grid = (KB_RED_CHUNKS element chunks, nb / 32 groups)
+// ---------------------------------------------------------------------------
+struct Chunk {
+  long long e0, e1;
+};
+__device__ __forceinline__ Chunk chunk_of(long long dim) {
+  const long long per = (dim + gridDim.x - 1) / gridDim.x;
+  Chunk c;
+  c.e0 = blockIdx.x * per;
+  c.e1 = min(dim, c.e0 + per);
+  return c;
+}
+
+// sum over the 8 warps of one value per (warp, lane), result in warp 0
+__device__ __forceinline__ double2 warps_sum(double2 v, double2 (*sh)[32]) {
+  sh[threadIdx.y][threadIdx.x] = v;
+  __syncthreads();
+  double2 s = make_double2(0.0, 0.0);
+  if (threadIdx.y == 0)
+    for (int w = 0; w < 8; ++w) s = cadd(s, sh[w][threadIdx.x]);
+  __syncthreads();
+  return s;
+}
+
+// S <- phase * S (optional); partial ||S_v||^2
+__global__ void kb_phase_norm(double2* S, const double2* phase, long long dim, int nb, double2* part) {
+  __shared__ double2 sh[8][32];
+  const int v = blockIdx.y * 32 + threadIdx.x;
+  const Chunk ch = chunk_of(dim);
+  double acc = 0.0;
+  for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
+    double2 s = S[e * nb + v];
+    if (phase) {
+      s = cmul(s, __ldg(phase + e));
+      S[e * nb + v] = s;
+    }
+    acc += cabs2(s);
+  }
+  const double2 t = warps_sum(make_double2(acc, 0.0), sh);
+  if (threadIdx.y == 0) part[(long long)blockIdx.x * nb + v] = t;
+}
+
+// out[j][v] = sum over chunks of part[chunk][j][v] (fixed order)
+__global__ void kb_reduce(const double2* part, int ncoef, int nb, int stride_coef, double2* out) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= ncoef * nb) return;
+  const int j = idx / nb, v = idx - j * nb;
+  double2 s = make_double2(0.0, 0.0);
+  for (int c = 0; c < KB_RED_CHUNKS; ++c) s = cadd(s, part[((long long)c * stride_coef + j) * nb + v]);
+  out[(long long)j * nb + v] = s;
+}
+
+// norm0 = ||S||, V0 = S / norm0 (complex64); resets the per-vector state
+__global__ void kb_start(const double2* S, float2* V0, const double2* nsq, double* norm0, int* active, int* kconv,
+                         double* vscale, long long dim, int nb, int nvec) {
+  const int v = blockIdx.y * 32 + threadIdx.x;
+  const double n0 = sqrt(nsq[v].x);
+  const double inv = n0 > 0.0 ? 1.0 / n0 : 0.0;
+  if (blockIdx.x == 0 && threadIdx.y == 0) {
+    norm0[v] = n0;
+    active[v] = (v < nvec && n0 > 0.0) ? 1 : 0;
+    kconv[v] = 0;
+    vscale[v] = 1.0;
+  }
+  const Chunk ch = chunk_of(dim);
+  for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
+    const double2 s = S[e * nb + v];
+    V0[e * nb + v] = make_float2((float)(s.x * inv), (float)(s.y * inv));
+  }
+}
+
+// partial dots h_j = <V_j, W> for j = 0..k: FP32 products, FP32 sums inside a
+// thread's elements, FP64 across threads and chunks
+__global__ void kb_dots(const float2* V, const float2* W, const int* active, long long dim, int nb, int k,
+                        int stride_coef, double2* part) {
+  __shared__ double2 sh[8][32];
+  const int v = blockIdx.y * 32 + threadIdx.x;
+  const Chunk ch = chunk_of(dim);
+  const bool act = active[v] != 0;
+  for (int j = 0; j <= k; ++j) {
+    float2 acc = make_float2(0.f, 0.f);
+    if (act) {
+      const float2* Vj = V + (long long)j * dim * nb;
+      for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
+        const float2 a = Vj[e * nb + v], b = W[e * nb + v];
+        acc.x = fmaf(a.x, b.x, acc.x);
+        acc.x = fmaf(a.y, b.y, acc.x);
+        acc.y = fmaf(a.x, b.y, acc.y);
+        acc.y = fmaf(-a.y, b.x, acc.y);
+      }
+    }
+    const double2 t = warps_sum(make_double2(acc.x, acc.y), sh);
+    if (threadIdx.y == 0) part[((long long)blockIdx.x * stride_coef + j) * nb + v] = t;
+  }
+}
+
+// V_{k+1} = W - sum_j h_j V_j (unnormalised), partial ||V_{k+1}||^2
+__global__ void kb_update(float2* V, const float2* W, const double2* h, const int* active, long long dim, int nb,
+                          int k, double2* part) {
+  __shared__ double2 sh[8][32];
+  const int v = blockIdx.y * 32 + threadIdx.x;
+  const Chunk ch = chunk_of(dim);
+  const bool act = active[v] != 0;
+  double nacc = 0.0;
+  if (act) {
+    float2 hv[KB_NK_MAX];
+    const int kk = min(k, KB_NK_MAX - 1);
+    for (int j = 0; j <= kk; ++j) {
+      const double2 t = h[(long long)j * nb + v];
+      hv[j] = make_float2((float)t.x, (float)t.y);
+    }
+    float2* Vn = V + (long long)(k + 1) * dim * nb;
+    for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
+      float2 r = W[e * nb + v];
+      for (int j = 0; j <= kk; ++j) {
+        const float2 a = V[((long long)j * dim + e) * nb + v];
+        r.x = fmaf(-hv[j].x, a.x, r.x);
+        r.x = fmaf(hv[j].y, a.y, r.x);
+        r.y = fmaf(-hv[j].x, a.y, r.y);
+        r.y = fmaf(-hv[j].y, a.x, r.y);
+      }
+      Vn[e * nb + v] = r;
+      nacc += (double)r.x * r.x + (double)r.y * r.y;
+    }
+  }
+  const double2 t = warps_sum(make_double2(nacc, 0.0), sh);
+  if (threadIdx.y == 0) part[(long long)blockIdx.x * nb + v] = t;
+}
+
+// per vector: T update, exp(fac T) e0, error estimate, convergence
+__global__ void kb_small(BatchDev b, int k, double2 fac, double tol, const double2* nsq) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= b.nb || !b.active[v]) return;
+  const int nb = b.nb;
+  const double2 hk = b.h[(long long)k * nb + v];
+  const double bk = sqrt(nsq[v].x);
+  b.alpha[(long long)k * nb + v] = hk;
+  b.beta[(long long)k * nb + v] = bk;
+  const int n = k + 1;
+  // Taylor series of exp(A) e0, A = fac T, sub-steps with ||A/s||_1 <= 1
+  double2 y[KB_NK_MAX], t[KB_NK_MAX], r[KB_NK_MAX];
+  double nrm = 0.0;
+  const double fa = sqrt(cabs2(fac));
+  for (int i = 0; i < n; ++i) {
+    double cs = sqrt(cabs2(cmul(fac, b.alpha[(long long)i * nb + v])));
+    if (i > 0) cs += fa * fabs(b.beta[(long long)(i - 1) * nb + v]);
+    if (i < n - 1) cs += fa * fabs(b.beta[(long long)i * nb + v]);
+    nrm = fmax(nrm, cs);
+  }
+  int nsub = max(1, (int)ceil(nrm));
+  const double inv_s = 1.0 / nsub;
+  for (int i = 0; i < n; ++i) y[i] = make_double2(i == 0 ? 1.0 : 0.0, 0.0);
+  for (int sub = 0; sub < nsub; ++sub) {
+    for (int i = 0; i < n; ++i) t[i] = y[i];
+    for (int j = 1; j <= 40; ++j) {
+      double tmax = 0.0, amax = 0.0;
+      for (int i = 0; i < n; ++i) {
+        double2 s = cmul(b.alpha[(long long)i * nb + v], t[i]);
+        if (i > 0) s = cadd(s, cscale(t[i - 1], b.beta[(long long)(i - 1) * nb + v]));
+        if (i < n - 1) s = cadd(s, cscale(t[i + 1], b.beta[(long long)i * nb + v]));
+        r[i] = cscale(cmul(fac, s), inv_s / j);
+      }
+      for (int i = 0; i < n; ++i) {
+        t[i] = r[i];
+        y[i] = cadd(y[i], r[i]);
+        tmax = fmax(tmax, fmax(fabs(r[i].x), fabs(r[i].y)));
+        amax = fmax(amax, fmax(fabs(y[i].x), fabs(y[i].y)));
+      }
+      if (tmax <= 1e-17 * amax) break;
+    }
+  }
+  const double e = b.norm0[v] * fa * bk * sqrt(cabs2(y[n - 1]));
+  b.err[v] = e;
+  const bool last = (k + 1 >= b.mmax);
+  if (e <= tol || bk == 0.0 || last) {
+    for (int i = 0; i < n; ++i) b.c[(long long)i * nb + v] = y[i];
+    b.kconv[v] = n;
+    b.active[v] = 0;
+    if (last && !(e <= tol || bk == 0.0)) atomicAdd(b.counts + 1, 1);
+  } else {
+    b.vscale[v] = 1.0 / bk;
+    atomicAdd(b.counts, 1);
+  }
+}
+
+// V_{k+1} *= 1 / beta_k for the vectors still active
+__global__ void kb_scale(float2* Vn, const double* vscale, const int* active, long long dim, int nb) {
+  const int v = blockIdx.y * 32 + threadIdx.x;
+  if (!active[v]) return;
+  const float s = (float)vscale[v];
+  const Chunk ch = chunk_of(dim);
+  for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
+    float2 a = Vn[e * nb + v];
+    Vn[e * nb + v] = make_float2(a.x * s, a.y * s);
+  }
+}
+
+// S <- phase * (c_0 S + ||v|| sum_{i>=1} c_i V_i)   (FP64)
+__global__ void kb_combine(BatchDev b, const double2* phase) {
+  const int v = blockIdx.y * 32 + threadIdx.x;
+  const int nb = b.nb;
+  const int K = b.kconv[v];
+  if (K == 0) return;  // no Krylov step (zero vector or padding)
+  double2 cc[KB_NK_MAX];
+  for (int i = 0; i < K; ++i) cc[i] = b.c[(long long)i * nb + v];
+  const double n0 = b.norm0[v];
+  const Chunk ch = chunk_of(b.dim);
+  for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
+    float2 sacc = make_float2(0.f, 0.f);
+    for (int i = 1; i < K; ++i) {
+      const float2 a = b.V[((long long)i * b.dim + e) * nb + v];
+      const float2 ci = make_float2((float)cc[i].x, (float)cc[i].y);
+      sacc.x = fmaf(ci.x, a.x, sacc.x);
+      sacc.x = fmaf(-ci.y, a.y, sacc.x);
+      sacc.y = fmaf(ci.x, a.y, sacc.y);
+      sacc.y = fmaf(ci.y, a.x, sacc.y);
+    }
+    double2 u = cmul(cc[0], b.S[e * nb + v]);
+    u.x = fma(n0, (double)sacc.x, u.x);
+    u.y = fma(n0, (double)sacc.y, u.y);
+    if (phase) u = cmul(u, __ldg(phase + e));
+    b.S[e * nb + v] = u;
+  }
+}
+
+// (nvec, dim) row-major <-> [dim][nb] vector-minor, tiled through shared memory
+__global__ void kb_transpose_in(const double2* src, double2* S, long long dim, int nvec, int nb) {
+  __shared__ double2 tile[32][33];
+  const long long e0 = blockIdx.x * 32LL;
+  const int v0 = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int v = v0 + r;
+    const long long e = e0 + threadIdx.x;
+    tile[r][threadIdx.x] = (v < nvec && e < dim) ? src[(long long)v * dim + e] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const long long e = e0 + r;
+    if (e < dim) S[e * nb + v0 + threadIdx.x] = tile[threadIdx.x][r];
+  }
+}
+__global__ void kb_transpose_out(const double2* S, double2* dst, long long dim, int nvec, int nb) {
+  __shared__ double2 tile[32][33];
+  const long long e0 = blockIdx.x * 32LL;
+  const int v0 = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const long long e = e0 + r;
+    tile[r][threadIdx.x] = (e < dim) ? S[e * nb + v0 + threadIdx.x] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int v = v0 + r;
+    const long long e = e0 + threadIdx.x;
+    if (v < nvec && e < dim) dst[(long long)v * dim + e] = tile[threadIdx.x][r];
+  }
+}
+
+// complex64 copy of the FP64 state (input of the observable mat-vec)
+__global__ void kb_to_f32(const double2* S, float2* X, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double2 s = S[i];
+    X[i] = make_float2((float)s.x, (float)s.y);
+  }
+}
+
+// partial <S_v | Y_v> with Y in complex64 (FP64 accumulation)
+__global__ void kb_expect_dots(const double2* S, const float2* Y, long long dim, int nb, double2* part) {
+  __shared__ double2 sh[8][32];
+  const int v = blockIdx.y * 32 + threadIdx.x;
+  const Chunk ch = chunk_of(dim);
+  double2 acc = make_double2(0.0, 0.0);
+  for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
+    const double2 s = S[e * nb + v];
+    const float2 y = Y[e * nb + v];
+    acc = cadd(acc, cconjmul(s, make_double2(y.x, y.y)));
+  }
+  const double2 t = warps_sum(acc, sh);
+  if (threadIdx.y == 0) part[(long long)blockIdx.x * nb + v] = t;
+}
+
+// ---------------------------------------------------------------------------
+// batched mat-vec, complex64: Y[(s1,i,a)][v] = sum_terms sum_b K[a,b] Z[b][v],
+// Z[b][v] = sum_w MF[i,w] X[(s2, col_w, b)][v]. One block = one output row i of
+// one slab x KB_MV_THREADS vectors; K^T and the MF row of each term are staged
+// in shared memory as FP32 and read as broadcasts.
+// ---------------------------------------------------------------------------
+struct BatchMV {
+  DevOp op;
+  const float2* X;
+  float2* Y;
+  int nb;
+  const int* row_slab;
+  const int* row_i;
+  const int* grp_active;  // per vector group: any vector active (null: all)
+};
+
+template <int NKP>
+__device__ void kb_row(const BatchMV& p, int s1, int i, int v, float* ks, float2* mfs, int* cols) {
+  const DevOp& op = p.op;
+  const int nk1 = __ldg(op.out_dk + s1);
+  float2 acc[NKP];
+#pragma unroll
+  for (int a = 0; a < NKP; ++a) acc[a] = make_float2(0.f, 0.f);
+  const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
+  const long long nb = p.nb;
+  for (int term = tb; term < te; ++term) {
+    const int s2 = __ldg(op.t_in + term);
+    const int kb = __ldg(op.t_k + term);
+    const int mfi = __ldg(op.t_mf + term);
+    const int nk2 = __ldg(op.in_dk + s2);
+    const int W = __ldg(op.mf_width + mfi);
+    const int ktype = __ldg(op.k_type + kb);
+    const int mtype = __ldg(op.mf_type + mfi);
+    const double* KT = op.k_data + __ldg(op.k_off + kb);
+    __syncthreads();
+    // stage K^T as [b][NKP] (complex K: [b][NKP] re then im planes) and the MF row
+    const int kwords = (ktype == 0) ? 2 : 1;
+    for (int e = threadIdx.x; e < nk2 * NKP * kwords; e += blockDim.x) {
+      const int plane = e / (nk2 * NKP);
+      const int rem = e - plane * nk2 * NKP;
+      const int bb = rem / NKP, a = rem - bb * NKP;
+      float val = 0.f;
+      if (a < nk1) val = (float)__ldg(KT + ((long long)bb * nk1 + a) * kwords + plane);
+      ks[e] = val;
+    }
+    const long long mbase = (long long)i * W;
+    for (int w = threadIdx.x; w < W; w += blockDim.x) {
+      const double2 m = __ldg(op.mf_val + __ldg(op.mf_off + mfi) + mbase + w);
+      mfs[w] = make_float2((float)m.x, (float)m.y);
+      cols[w] = __ldg(op.m_col + __ldg(op.mf_col_off + mfi) + mbase + w);
+    }
+    __syncthreads();
+    const float2* X = p.X + (long long)__ldg(op.in_off + s2) * nb + v;
+    for (int bb = 0; bb < nk2; ++bb) {
+      float2 z = make_float2(0.f, 0.f);
+      for (int w = 0; w < W; ++w) {
+        const float2 m = mfs[w];
+        const float2 x = X[((long long)cols[w] * nk2 + bb) * nb];
+        if (mtype == 1) {
+          z.x = fmaf(m.x, x.x, z.x);
+          z.y = fmaf(m.x, x.y, z.y);
+        } else if (mtype == 2) {
+          z.x = fmaf(-m.y, x.y, z.x);
+          z.y = fmaf(m.y, x.x, z.y);
+        } else {
+          z.x = fmaf(m.x, x.x, z.x);
+          z.x = fmaf(-m.y, x.y, z.x);
+          z.y = fmaf(m.x, x.y, z.y);
+          z.y = fmaf(m.y, x.x, z.y);
+        }
+      }
+      const float* kr = ks + bb * NKP;
+      if (ktype == 1) {
+#pragma unroll
+        for (int a = 0; a < NKP; a += 4) {
+          const float4 k4 = *reinterpret_cast<const float4*>(kr + a);
+          acc[a].x = fmaf(k4.x, z.x, acc[a].x); acc[a].y = fmaf(k4.x, z.y, acc[a].y);
+          acc[a + 1].x = fmaf(k4.y, z.x, acc[a + 1].x); acc[a + 1].y = fmaf(k4.y, z.y, acc[a + 1].y);
+          acc[a + 2].x = fmaf(k4.z, z.x, acc[a + 2].x); acc[a + 2].y = fmaf(k4.z, z.y, acc[a + 2].y);
+          acc[a + 3].x = fmaf(k4.w, z.x, acc[a + 3].x); acc[a + 3].y = fmaf(k4.w, z.y, acc[a + 3].y);
+        }
+      } else if (ktype == 2) {  // K = i Ki
+#pragma unroll
+        for (int a = 0; a < NKP; a += 4) {
+          const float4 k4 = *reinterpret_cast<const float4*>(kr + a);
+          acc[a].x = fmaf(-k4.x, z.y, acc[a].x); acc[a].y = fmaf(k4.x, z.x, acc[a].y);
+          acc[a + 1].x = fmaf(-k4.y, z.y, acc[a + 1].x); acc[a + 1].y = fmaf(k4.y, z.x, acc[a + 1].y);
+          acc[a + 2].x = fmaf(-k4.z, z.y, acc[a + 2].x); acc[a + 2].y = fmaf(k4.z, z.x, acc[a + 2].y);
+          acc[a + 3].x = fmaf(-k4.w, z.y, acc[a + 3].x); acc[a + 3].y = fmaf(k4.w, z.x, acc[a + 3].y);
+        }
+      } else {
+        const float* ki = ks + nk2 * NKP + bb * NKP;
+#pragma unroll
+        for (int a = 0; a < NKP; ++a) {
+          const float re = kr[a], im = ki[a];
+          acc[a].x = fmaf(re, z.x, acc[a].x);
+          acc[a].x = fmaf(-im, z.y, acc[a].x);
+          acc[a].y = fmaf(re, z.y, acc[a].y);
+          acc[a].y = fmaf(im, z.x, acc[a].y);
+        }
+      }
+    }
+  }
+  float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i * nk1) * nb + v;
+#pragma unroll
+  for (int a = 0; a < NKP; ++a)
+    if (a < nk1) Y[(long long)a * nb] = acc[a];
+}
+
+__global__ void __launch_bounds__(KB_MV_THREADS) kb_matvec(BatchMV p) {
+  extern __shared__ float kb_smem[];
+  const int row = blockIdx.x;
+  const int grp = blockIdx.y;
+  if (p.grp_active && !p.grp_active[grp]) return;
+  const int v = grp * KB_MV_THREADS + threadIdx.x;
+  const int s1 = __ldg(p.row_slab + row);
+  const int i = __ldg(p.row_i + row);
+  const int nk1 = __ldg(p.op.out_dk + s1);
+  int maxnk2 = 1;
+  const int tb = __ldg(p.op.term_ptr + s1), te = __ldg(p.op.term_ptr + s1 + 1);
+  int maxw = 1;
+  for (int t = tb; t < te; ++t) {
+    maxnk2 = max(maxnk2, __ldg(p.op.in_dk + __ldg(p.op.t_in + t)));
+    maxw = max(maxw, __ldg(p.op.mf_width + __ldg(p.op.t_mf + t)));
+  }
+  float* ks = kb_smem;
+  float2* mfs = reinterpret_cast<float2*>(kb_smem + 2 * KB_NK_MAX * KB_NK_MAX);
+  int* cols = reinterpret_cast<int*>(mfs + 64);
+  (void)maxnk2;
+  (void)maxw;
+  if (nk1 <= 4) kb_row<4>(p, s1, i, v, ks, mfs, cols);
+  else if (nk1 <= 8) kb_row<8>(p, s1, i, v, ks, mfs, cols);
+  else if (nk1 <= 12) kb_row<12>(p, s1, i, v, ks, mfs, cols);
+  else if (nk1 <= 16) kb_row<16>(p, s1, i, v, ks, mfs, cols);
+  else if (nk1 <= 24) kb_row<24>(p, s1, i, v, ks, mfs, cols);
+  else kb_row<32>(p, s1, i, v, ks, mfs, cols);
+}
+
+// any active vector per mat-vec group
+__global__ void kb_group_active(const int* active, int* grp, int nb) {
+  const int g = blockIdx.x;
+  int any = 0;
+  for (int i = threadIdx.x; i < KB_MV_THREADS; i += blockDim.x) {
+    const int v = g * KB_MV_THREADS + i;
+    if (v < nb && active[v]) any = 1;
+  }
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) grp[g] = any;
+}
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+namespace {
+template <typename T>
+int balloc(kr_batch* b, size_t count, T** p) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, sizeof(T) * std::max<size_t>(count, 1));
+  if (e != cudaSuccess) return set_err(b->op->ctx, KR_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  cudaMemset(q, 0, sizeof(T) * std::max<size_t>(count, 1));
+  b->allocs.push_back(q);
+  *p = static_cast<T*>(q);
+  return KR_OK;
+}
+int mv_groups(const kr_batch* b) { return (b->nb + KB_MV_THREADS - 1) / KB_MV_THREADS; }
+
+int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool masked, cudaStream_t st) {
+  BatchMV p;
+  p.op = op->dev;
+  p.X = X;
+  p.Y = Y;
+  p.nb = b->nb;
+  p.row_slab = b->row_slab;
+  p.row_i = b->row_i;
+  p.grp_active = masked ? b->grp_active : nullptr;
+  const size_t smem = sizeof(float) * 2 * KB_NK_MAX * KB_NK_MAX + sizeof(float2) * 64 + sizeof(int) * 64;
+  dim3 grid(b->nrows, mv_groups(b));
+  kb_matvec<<<grid, KB_MV_THREADS, smem, st>>>(p);
+  b->launches++;
+  KR_CUDA(op->ctx, cudaGetLastError());
+  return KR_OK;
+}
+}  // namespace
+
+extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch** out) {
+  if (!op || !out || nvec <= 0 || mmax < 2 || mmax > KB_NK_MAX - 1)
+    return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_batch_create: bad argument (2 <= mmax <= 31)");
+  *out = nullptr;
+  if (!op->square) return set_err(op->ctx, KR_ERR_ARG, "kr_batch_create: operator is not square");
+  // the batched mat-vec supports n_k <= 32 and ELL widths <= 64
+  std::vector<int> dk(op->dev.nslab_out), dm(op->dev.nslab_out);
+  cudaMemcpy(dk.data(), op->dev.out_dk, sizeof(int) * dk.size(), cudaMemcpyDeviceToHost);
+  cudaMemcpy(dm.data(), op->dev.out_dm, sizeof(int) * dm.size(), cudaMemcpyDeviceToHost);
+  for (int x : dk)
+    if (x > KB_NK_MAX) return set_err(op->ctx, KR_ERR_UNSUPPORTED, "kr_batch_create: n_k above 32 not supported");
+  std::vector<int> widths(std::max(1, op->nmf));
+  cudaMemcpy(widths.data(), op->dev.mf_width, sizeof(int) * op->nmf, cudaMemcpyDeviceToHost);
+  for (int i = 0; i < op->nmf; ++i)
+    if (widths[i] > 64) return set_err(op->ctx, KR_ERR_UNSUPPORTED, "kr_batch_create: M band wider than 64");
+  kr_batch* b = new kr_batch();
+  b->op = op;
+  b->nvec = (int)nvec;
+  b->nb = (int)((nvec + 127) / 128 * 128);
+  b->mmax = mmax;
+  b->dim = op->dev.dim_out;
+  const size_t nb = b->nb, dim = b->dim, m1 = mmax + 1;
+  int rc = KR_OK;
+#define BA(count, ptr) \
+  if ((rc = balloc(b, (count), (ptr))) != KR_OK) { kr_batch_destroy(b); return rc; }
+  BA(dim * nb, &b->S);
+  BA(m1 * dim * nb, &b->V);
+  BA(dim * nb, &b->W);
+  BA(nb, &b->norm0);
+  BA(m1 * nb, &b->h);
+  BA(m1 * nb, &b->alpha);
+  BA(m1 * nb, &b->beta);
+  BA(m1 * nb, &b->c);
+  BA(nb, &b->vscale);
+  BA(nb, &b->kconv);
+  BA(nb, &b->active);
+  BA((size_t)mv_groups(b), &b->grp_active);
+  BA(nb, &b->err);
+  BA((size_t)KB_RED_CHUNKS * (m1 + 1) * nb, &b->part);
+  BA(2, &b->counts);
+  std::vector<int> rs, ri;
+  for (int s = 0; s < (int)dm.size(); ++s)
+    for (int i = 0; i < dm[s]; ++i) {
+      rs.push_back(s);
+      ri.push_back(i);
+    }
+  b->nrows = (int)rs.size();
+  BA(rs.size(), &b->row_slab);
+  BA(ri.size(), &b->row_i);
+#undef BA
+  cudaMemcpy(b->row_slab, rs.data(), sizeof(int) * rs.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->row_i, ri.data(), sizeof(int) * ri.size(), cudaMemcpyHostToDevice);
+  KR_CUDA(op->ctx, cudaDeviceSynchronize());
+  *out = b;
+  return KR_OK;
+}
+
+extern "C" void kr_batch_destroy(kr_batch* b) {
+  if (!b) return;
+  for (void* p : b->allocs) cudaFree(p);
+  delete b;
+}
+
+extern "C" int kr_batch_load(kr_batch* b, const void* states, void* stream) {
+  if (!b || !states) return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_load: bad argument");
+  dim3 grid((unsigned)((b->dim + 31) / 32), b->nb / 32);
+  kb_transpose_in<<<grid, dim3(32, 8), 0, (cudaStream_t)stream>>>((const double2*)states, b->S, b->dim, b->nvec, b->nb);
+  b->launches++;
+  KR_CUDA(b->op->ctx, cudaGetLastError());
+  return KR_OK;
+}
+
+extern "C" int kr_batch_store(kr_batch* b, void* states, void* stream) {
+  if (!b || !states) return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_store: bad argument");
+  dim3 grid((unsigned)((b->dim + 31) / 32), b->nb / 32);
+  kb_transpose_out<<<grid, dim3(32, 8), 0, (cudaStream_t)stream>>>(b->S, (double2*)states, b->dim, b->nvec, b->nb);
+  b->launches++;
+  KR_CUDA(b->op->ctx, cudaGetLastError());
+  return KR_OK;
+}
+
+extern "C" int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double fac_re, double fac_im, double tol,
+                             int32_t* kmax_out, void* stream) {
+  if (!b || !op) return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_step: bad argument");
+  if (op->dev.dim_out != b->dim || !op->square)
+    return set_err(op->ctx, KR_ERR_ARG, "kr_batch_step: operator does not match the batch basis");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nb = b->nb;
+  const long long dim = b->dim;
+  const dim3 eg(KB_RED_CHUNKS, nb / 32), eb(32, 8);
+  const int stride = b->mmax + 2;
+  const double2 fac = make_double2(fac_re, fac_im);
+  kr_ctx* ctx = op->ctx;
+  // S <- phase * S, norms, V_0
+  kb_phase_norm<<<eg, eb, 0, st>>>(b->S, (const double2*)phase, dim, nb, b->part);
+  kb_reduce<<<(nb + 255) / 256, 256, 0, st>>>(b->part, 1, nb, 1, b->h);
+  kb_start<<<eg, eb, 0, st>>>(b->S, b->V, b->h, b->norm0, b->active, b->kconv, b->vscale, dim, nb, b->nvec);
+  b->launches += 3;
+  KR_CUDA(ctx, cudaGetLastError());
+  int kused = 0;
+  for (int k = 0; k < b->mmax; ++k) {
+    kb_group_active<<<mv_groups(b), 128, 0, st>>>(b->active, b->grp_active, nb);
+    int rc = launch_matvec(b, op, b->V + (long long)k * dim * nb, b->W, true, st);
+    if (rc) return rc;
+    kb_dots<<<eg, eb, 0, st>>>(b->V, b->W, b->active, dim, nb, k, stride, b->part);
+    kb_reduce<<<((k + 1) * nb + 255) / 256, 256, 0, st>>>(b->part, k + 1, nb, stride, b->h);
+    kb_update<<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->active, dim, nb, k, b->part);
+    // norms of V_{k+1} into the last coefficient slot of h (slot mmax + 1 is not a dot)
+    kb_reduce<<<(nb + 255) / 256, 256, 0, st>>>(b->part, 1, nb, 1, b->h + (long long)(b->mmax) * nb);
+    KR_CUDA(ctx, cudaMemsetAsync(b->counts, 0, 2 * sizeof(int), st));
+    kb_small<<<(nb + 127) / 128, 128, 0, st>>>(dev_view(b), k, fac, tol, b->h + (long long)(b->mmax) * nb);
+    kb_scale<<<eg, eb, 0, st>>>(b->V + (long long)(k + 1) * dim * nb, b->vscale, b->active, dim, nb);
+    b->launches += 7;
+    KR_CUDA(ctx, cudaGetLastError());
+    int counts[2] = {0, 0};
+    KR_CUDA(ctx, cudaMemcpyAsync(counts, b->counts, sizeof(counts), cudaMemcpyDeviceToHost, st));
+    KR_CUDA(ctx, cudaStreamSynchronize(st));
+    kused = k + 1;
+    if (counts[1] > 0)
+      return set_err(ctx, KR_ERR_MAXORDER,
+                     "batched Lanczos: " + std::to_string(counts[1]) + " vectors did not reach the tolerance within " +
+                         std::to_string(b->mmax) + " Krylov vectors");
+    if (counts[0] == 0) break;
+  }
+  kb_combine<<<eg, eb, 0, st>>>(dev_view(b), (const double2*)phase);
+  b->launches++;
+  KR_CUDA(ctx, cudaGetLastError());
+  if (kmax_out) *kmax_out = kused;
+  return KR_OK;
+}
+
+extern "C" int kr_batch_korder(kr_batch* b, int32_t* korder, void* stream) {
+  if (!b || !korder) return KR_ERR_ARG;
+  KR_CUDA(b->op->ctx, cudaMemcpyAsync(korder, b->kconv, sizeof(int) * b->nvec, cudaMemcpyDeviceToHost,
+                                      (cudaStream_t)stream));
+  KR_CUDA(b->op->ctx, cudaStreamSynchronize((cudaStream_t)stream));
+  return KR_OK;
+}
+
+extern "C" int kr_batch_expect(kr_batch* b, kr_op* obs, double* out, void* stream) {
+  if (!b || !obs || !out) return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_expect: bad argument");
+  if (obs->dev.dim_out != b->dim || !obs->square)
+    return set_err(obs->ctx, KR_ERR_ARG, "kr_batch_expect: observable does not match the batch basis");
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long n = b->dim * b->nb;
+  float2* X = b->V;  // basis slot 0 and W are free between steps
+  kb_to_f32<<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, st>>>(b->S, X, n);
+  int rc = launch_matvec(b, obs, X, b->W, false, st);
+  if (rc) return rc;
+  const dim3 eg(KB_RED_CHUNKS, b->nb / 32), eb(32, 8);
+  kb_expect_dots<<<eg, eb, 0, st>>>(b->S, b->W, b->dim, b->nb, b->part);
+  kb_reduce<<<(b->nb + 255) / 256, 256, 0, st>>>(b->part, 1, b->nb, 1, b->h);
+  b->launches += 3;
+  KR_CUDA(obs->ctx, cudaGetLastError());
+  std::vector<double2> h(b->nb);
+  KR_CUDA(obs->ctx, cudaMemcpyAsync(h.data(), b->h, sizeof(double2) * b->nb, cudaMemcpyDeviceToHost, st));
+  KR_CUDA(obs->ctx, cudaStreamSynchronize(st));
+  for (int v = 0; v < b->nvec; ++v) {
+    out[2 * v] = h[v].x;
+    out[2 * v + 1] = h[v].y;
+  }
+  return KR_OK;
+}
+
+extern "C" int kr_batch_matvec(kr_batch* b, kr_op* op, void* stream) {
+  if (!b || !op || op->dev.dim_out != b->dim || !op->square)
+    return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_matvec: operator does not match the batch basis");
+  return launch_matvec(b, op, b->V, b->W, false, (cudaStream_t)stream);
+}
+
+extern "C" int64_t kr_batch_launch_count(const kr_batch* b) { return b ? b->launches : -1; }

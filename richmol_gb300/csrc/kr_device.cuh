@@ -74,7 +74,7 @@ __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
 }
 
-__device__ bool grid_barrier(unsigned* count, unsigned* gen, int* status, int code_on_timeout) {
+static __device__ bool grid_barrier(unsigned* count, unsigned* gen, int* status, int code_on_timeout) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -119,7 +119,7 @@ __device__ __forceinline__ double2 warp_sum2(double2 v) {
   return v;
 }
 // Sum of one double2 per thread over the CTA; result valid in all threads.
-__device__ double2 block_sum2(double2 v, double2* scratch /* KR_WARPS */) {
+static __device__ double2 block_sum2(double2 v, double2* scratch /* KR_WARPS */) {
   v = warp_sum2(v);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   __syncthreads();
@@ -131,7 +131,7 @@ __device__ double2 block_sum2(double2 v, double2* scratch /* KR_WARPS */) {
   return s;
 }
 // Sum of n values written by the CTAs of the grid, same order in every CTA.
-__device__ double2 grid_partials_sum2(const double2* part, int n, double2* scratch) {
+static __device__ double2 grid_partials_sum2(const double2* part, int n, double2* scratch) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   __syncthreads();
   if (warp == 0) {

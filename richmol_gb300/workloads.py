@@ -67,3 +67,35 @@ def asym_top(Jmax=40, dt=0.005, nsteps=4000):
     beta = np.deg2rad(35.0)
     return Workload("asym_top_D2_J%d" % Jmax, mol, Jmax, 0.0, nsteps * dt, dt, [0.0, 0.0, 20e3 * 1e2],
                     (1.0, 0.5, 1e12, [np.sin(beta), 0.0, np.cos(beta)]))
+
+
+class Ensemble:
+    """Thermal ensemble of a workload: eigenstates of H0 (unit vectors in its
+    eigenbasis) in energy order, the Boltzmann weight of each at T, padded with
+    the next-lowest states to nvec right-hand sides."""
+
+    def __init__(self, wl, nvec, temp, wmin=1e-5):
+        import scipy.constants as const
+        wl.h0.field([0, 0, 1])
+        enr = wl.h0.tomat(form="full").diagonal().real
+        order = np.argsort(enr, kind="stable")
+        w = np.exp(-(enr[order] - enr[order[0]]) * (const.h * const.c * 100.0) / (const.k * temp))
+        w /= w.sum()
+        self.n_natural = int(np.sum(w >= wmin))
+        self.nvec = int(nvec)
+        self.index = order[: self.nvec]
+        self.weights = w[: self.nvec]
+
+    def vectors(self, dim):
+        v = np.zeros((self.nvec, dim), np.complex128)
+        v[np.arange(self.nvec), self.index] = 1.0
+        return v
+
+
+def thermal_asym_top(Jmax=30, nvec=4096, temp=5.0, dt=0.01, nsteps=3000):
+    """Batched configuration: the asymmetric top of ``asym_top`` with J = 0..30,
+    its T = 5 K ensemble (states with Boltzmann weight >= 1e-5, padded to 4096
+    vectors), same DC field and pulse, 3000 steps of 10 fs."""
+    wl = asym_top(Jmax=Jmax, dt=dt, nsteps=nsteps)
+    wl.name = "thermal_asym_top_D2_J%d_%dvec" % (Jmax, nvec)
+    return wl, Ensemble(wl, nvec, temp)
