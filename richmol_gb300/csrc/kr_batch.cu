@@ -49,10 +49,11 @@ struct kr_batch {
   double* err = nullptr;     // [nb]
   double2* part = nullptr;   // [KB_RED_CHUNKS][mmax + 2][nb] partial sums
   int* counts = nullptr;     // [2]: active vectors, vectors that hit mmax
-  // mat-vec row table
-  int nrows = 0;
-  int* row_slab = nullptr;
-  int* row_i = nullptr;
+  // mat-vec tile table
+  int ntask = 0;
+  int* task_slab = nullptr;
+  int* task_i0 = nullptr;
+  int* task_nr = nullptr;
   long long launches = 0;
 };
 
@@ -378,30 +379,101 @@ __global__ void kb_expect_dots(const double2* S, const float2* Y, long long dim,
 }
 
 // ---------------------------------------------------------------------------
-// batched mat-vec, complex64: Y[(s1,i,a)][v] = sum_terms sum_b K[a,b] Z[b][v],
-// Z[b][v] = sum_w MF[i,w] X[(s2, col_w, b)][v]. One block = one output row i of
-// one slab x KB_MV_THREADS vectors; K^T and the MF row of each term are staged
-// in shared memory as FP32 and read as broadcasts.
+// batched mat-vec, complex64, tiled. One CTA (256 threads = 8 warps) computes
+// a tile of R consecutive output rows of one slab for 32 vectors (lane =
+// vector):
+//   for each term:   T[j, a] = sum_b K[a, b] X[j, b]   for the input rows j of
+//                    the band of the tile (each computed once, kept in shared
+//                    memory), then Y[i, a] += sum_w MF[i, w] T[col(i, w), a]
+// (field.py:1212-1243 orders the same sum as MF (K X^T)^T). K^T, the MF rows
+// and their columns are staged as FP32 in shared memory per term; every thread
+// owns 16 (row, a) outputs across all terms (R * NKP = 128 per CTA).
 // ---------------------------------------------------------------------------
+#define KB_WMAX 16   // ELL width of the M band supported by the batched mat-vec
+
 struct BatchMV {
   DevOp op;
   const float2* X;
   float2* Y;
   int nb;
-  const int* row_slab;
-  const int* row_i;
-  const int* grp_active;  // per vector group: any vector active (null: all)
+  const int* task_slab;
+  const int* task_i0;
+  const int* task_nr;
+  const int* grp_active;  // per 32-vector group: any vector active (null: all)
 };
 
-template <int NKP>
-__device__ void kb_row(const BatchMV& p, int s1, int i, int v, float* ks, float2* mfs, int* cols) {
-  const DevOp& op = p.op;
-  const int nk1 = __ldg(op.out_dk + s1);
-  float2 acc[NKP];
+// complex x real/imaginary/complex K factor accumulation: t += k * x
+template <int KT>
+__device__ __forceinline__ void kacc(float2& t, float kr, float ki, float2 x) {
+  if (KT == 1) {
+    t.x = fmaf(kr, x.x, t.x);
+    t.y = fmaf(kr, x.y, t.y);
+  } else if (KT == 2) {
+    t.x = fmaf(-kr, x.y, t.x);
+    t.y = fmaf(kr, x.x, t.y);
+  } else {
+    t.x = fmaf(kr, x.x, fmaf(-ki, x.y, t.x));
+    t.y = fmaf(kr, x.y, fmaf(ki, x.x, t.y));
+  }
+}
+
+// T[jj][a] = sum_b K[a, b] X[j, b] for one input row and all a (this thread's
+// vector); X is read in groups of 4 independent loads, the next group issued
+// before the current one is used
+template <int NKP, int KT>
+__device__ __forceinline__ void kb_trow(const float2* xr, long long nb, int nk2, const float* Ks, float2* t) {
 #pragma unroll
-  for (int a = 0; a < NKP; ++a) acc[a] = make_float2(0.f, 0.f);
-  const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
+  for (int a = 0; a < NKP; ++a) t[a] = make_float2(0.f, 0.f);
+  float2 xn[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) xn[u] = (u < nk2) ? xr[(long long)u * nb] : make_float2(0.f, 0.f);
+  for (int b0 = 0; b0 < nk2; b0 += 4) {
+    float2 x[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) x[u] = xn[u];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int bn = b0 + 4 + u;
+      xn[u] = (bn < nk2) ? xr[(long long)bn * nb] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int b = b0 + u;  // Ks rows beyond nk2 hold zeros
+      const float* kr = Ks + b * NKP;
+      const float* ki = Ks + (36 + b) * NKP;
+#pragma unroll
+      for (int a = 0; a < NKP; a += 4) {
+        const float4 r4 = *reinterpret_cast<const float4*>(kr + a);
+        float4 i4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (KT == 0) i4 = *reinterpret_cast<const float4*>(ki + a);
+        kacc<KT>(t[a], r4.x, i4.x, x[u]);
+        kacc<KT>(t[a + 1], r4.y, i4.y, x[u]);
+        kacc<KT>(t[a + 2], r4.z, i4.z, x[u]);
+        kacc<KT>(t[a + 3], r4.w, i4.w, x[u]);
+      }
+    }
+  }
+}
+
+template <int NKP>
+__device__ void kb_tile(const BatchMV& p, int s1, int i0, int nr, float* smem) {
+  constexpr int R = 128 / NKP;      // rows of the tile
+  constexpr int NJ = R + 4;         // input rows of one band chunk
+  constexpr int QY = 16;            // outputs per thread: warp w owns pairs [16 w, 16 w + 16)
+  const DevOp& op = p.op;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const long long nb = p.nb;
+  const int v = blockIdx.y * 32 + lane;
+  float2* Ts = reinterpret_cast<float2*>(smem);                 // [NJ][NKP][32]
+  float* Ks = smem + 2 * NJ * NKP * 32;                          // [2][36][NKP]
+  float2* MFs = reinterpret_cast<float2*>(Ks + 2 * 36 * NKP);   // [R][KB_WMAX]
+  int* Cs = reinterpret_cast<int*>(MFs + R * KB_WMAX);           // [R][KB_WMAX]
+  int* meta = Cs + R * KB_WMAX;                                  // jmin, jmax
+  const int nk1 = __ldg(op.out_dk + s1);
+  float2 y[QY];
+#pragma unroll
+  for (int q = 0; q < QY; ++q) y[q] = make_float2(0.f, 0.f);
+  const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
   for (int term = tb; term < te; ++term) {
     const int s2 = __ldg(op.t_in + term);
     const int kb = __ldg(op.t_k + term);
@@ -409,121 +481,130 @@ __device__ void kb_row(const BatchMV& p, int s1, int i, int v, float* ks, float2
     const int nk2 = __ldg(op.in_dk + s2);
     const int W = __ldg(op.mf_width + mfi);
     const int ktype = __ldg(op.k_type + kb);
-    const int mtype = __ldg(op.mf_type + mfi);
-    const double* KT = op.k_data + __ldg(op.k_off + kb);
-    __syncthreads();
-    // stage K^T as [b][NKP] (complex K: [b][NKP] re then im planes) and the MF row
-    const int kwords = (ktype == 0) ? 2 : 1;
-    for (int e = threadIdx.x; e < nk2 * NKP * kwords; e += blockDim.x) {
-      const int plane = e / (nk2 * NKP);
-      const int rem = e - plane * nk2 * NKP;
-      const int bb = rem / NKP, a = rem - bb * NKP;
-      float val = 0.f;
-      if (a < nk1) val = (float)__ldg(KT + ((long long)bb * nk1 + a) * kwords + plane);
-      ks[e] = val;
+    const int mtype = __ldcg(op.mf_type + mfi);
+    const int kw = (ktype == 0) ? 2 : 1;
+    const float* KT = op.k_f32 + __ldg(op.k_off + kb);
+    const int* col = op.m_col + __ldg(op.mf_col_off + mfi);
+    const float2* mf = op.mf_f32 + __ldg(op.mf_off + mfi);
+    __syncthreads();  // the previous term is done with Ks, MFs, Cs, Ts
+    // K^T as [plane][b][a], zero outside nk2 x nk1 (rows up to the next multiple of 4)
+    const int nb4 = (nk2 + 3) & ~3;
+    for (int e = tid; e < kw * nb4 * NKP; e += blockDim.x) {
+      const int plane = e / (nb4 * NKP);
+      const int rem = e - plane * nb4 * NKP;
+      const int b = rem / NKP, a = rem - b * NKP;
+      Ks[(plane * 36 + b) * NKP + a] =
+          (a < nk1 && b < nk2) ? __ldg(KT + ((long long)b * nk1 + a) * kw + plane) : 0.f;
     }
-    const long long mbase = (long long)i * W;
-    for (int w = threadIdx.x; w < W; w += blockDim.x) {
-      const double2 m = __ldg(op.mf_val + __ldg(op.mf_off + mfi) + mbase + w);
-      mfs[w] = make_float2((float)m.x, (float)m.y);
-      cols[w] = __ldg(op.m_col + __ldg(op.mf_col_off + mfi) + mbase + w);
-    }
-    __syncthreads();
-    const float2* X = p.X + (long long)__ldg(op.in_off + s2) * nb + v;
-    for (int bb = 0; bb < nk2; ++bb) {
-      float2 z = make_float2(0.f, 0.f);
-      for (int w = 0; w < W; ++w) {
-        const float2 m = mfs[w];
-        const float2 x = X[((long long)cols[w] * nk2 + bb) * nb];
-        if (mtype == 1) {
-          z.x = fmaf(m.x, x.x, z.x);
-          z.y = fmaf(m.x, x.y, z.y);
-        } else if (mtype == 2) {
-          z.x = fmaf(-m.y, x.y, z.x);
-          z.y = fmaf(m.y, x.x, z.y);
-        } else {
-          z.x = fmaf(m.x, x.x, z.x);
-          z.x = fmaf(-m.y, x.y, z.x);
-          z.y = fmaf(m.x, x.y, z.y);
-          z.y = fmaf(m.y, x.x, z.y);
-        }
-      }
-      const float* kr = ks + bb * NKP;
-      if (ktype == 1) {
-#pragma unroll
-        for (int a = 0; a < NKP; a += 4) {
-          const float4 k4 = *reinterpret_cast<const float4*>(kr + a);
-          acc[a].x = fmaf(k4.x, z.x, acc[a].x); acc[a].y = fmaf(k4.x, z.y, acc[a].y);
-          acc[a + 1].x = fmaf(k4.y, z.x, acc[a + 1].x); acc[a + 1].y = fmaf(k4.y, z.y, acc[a + 1].y);
-          acc[a + 2].x = fmaf(k4.z, z.x, acc[a + 2].x); acc[a + 2].y = fmaf(k4.z, z.y, acc[a + 2].y);
-          acc[a + 3].x = fmaf(k4.w, z.x, acc[a + 3].x); acc[a + 3].y = fmaf(k4.w, z.y, acc[a + 3].y);
-        }
-      } else if (ktype == 2) {  // K = i Ki
-#pragma unroll
-        for (int a = 0; a < NKP; a += 4) {
-          const float4 k4 = *reinterpret_cast<const float4*>(kr + a);
-          acc[a].x = fmaf(-k4.x, z.y, acc[a].x); acc[a].y = fmaf(k4.x, z.x, acc[a].y);
-          acc[a + 1].x = fmaf(-k4.y, z.y, acc[a + 1].x); acc[a + 1].y = fmaf(k4.y, z.x, acc[a + 1].y);
-          acc[a + 2].x = fmaf(-k4.z, z.y, acc[a + 2].x); acc[a + 2].y = fmaf(k4.z, z.x, acc[a + 2].y);
-          acc[a + 3].x = fmaf(-k4.w, z.y, acc[a + 3].x); acc[a + 3].y = fmaf(k4.w, z.x, acc[a + 3].y);
-        }
+    for (int e = tid; e < R * W; e += blockDim.x) {
+      const int r = e / W, w = e - r * W;
+      if (r < nr) {
+        const long long src = (long long)(i0 + r) * W + w;
+        MFs[r * KB_WMAX + w] = __ldcg(mf + src);
+        Cs[r * KB_WMAX + w] = __ldg(col + src);
       } else {
-        const float* ki = ks + nk2 * NKP + bb * NKP;
+        MFs[r * KB_WMAX + w] = make_float2(0.f, 0.f);
+        Cs[r * KB_WMAX + w] = -1;
+      }
+    }
+    if (wid == 0) {
+      int lo = 0x7fffffff, hi = -1;
+      for (int e = lane; e < nr * W; e += 32) {
+        const int c = __ldg(col + (long long)(i0 + e / W) * W + (e % W));
+        lo = min(lo, c);
+        hi = max(hi, c);
+      }
 #pragma unroll
-        for (int a = 0; a < NKP; ++a) {
-          const float re = kr[a], im = ki[a];
-          acc[a].x = fmaf(re, z.x, acc[a].x);
-          acc[a].x = fmaf(-im, z.y, acc[a].x);
-          acc[a].y = fmaf(re, z.y, acc[a].y);
-          acc[a].y = fmaf(im, z.x, acc[a].y);
+      for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+      }
+      if (lane == 0) {
+        meta[0] = lo;
+        meta[1] = hi;
+      }
+    }
+    __syncthreads();
+    const int jmin = meta[0], jmax = meta[1];
+    const float2* Xs2 = p.X + (long long)__ldg(op.in_off + s2) * nb + v;
+    for (int jc = jmin; jc <= jmax; jc += NJ) {
+      const int nj = min(NJ, jmax - jc + 1);
+      if (jc != jmin) __syncthreads();  // the previous chunk's Y step is done with Ts
+      for (int jj = wid; jj < nj; jj += 8) {
+        float2 t[NKP];
+        const float2* xr = Xs2 + (long long)(jc + jj) * nk2 * nb;
+        if (ktype == 1) kb_trow<NKP, 1>(xr, nb, nk2, Ks, t);
+        else if (ktype == 2) kb_trow<NKP, 2>(xr, nb, nk2, Ks, t);
+        else kb_trow<NKP, 0>(xr, nb, nk2, Ks, t);
+        float2* tr = Ts + jj * NKP * 32 + lane;
+#pragma unroll
+        for (int a = 0; a < NKP; ++a) tr[a * 32] = t[a];
+      }
+      __syncthreads();
+      // Y[i, a] += sum_w MF[i, w] T[col, a] for this warp's 16 (i, a) pairs
+      for (int w = 0; w < W; ++w) {
+#pragma unroll
+        for (int q = 0; q < QY; ++q) {
+          const int pq = wid * QY + q;
+          const int i = pq / NKP, a = pq - (pq / NKP) * NKP;
+          const int c = Cs[i * KB_WMAX + w] - jc;
+          if (c < 0 || c >= nj) continue;
+          const float2 m = MFs[i * KB_WMAX + w];
+          const float2 tv = Ts[(c * NKP + a) * 32 + lane];
+          if (mtype == 1) {
+            y[q].x = fmaf(m.x, tv.x, y[q].x);
+            y[q].y = fmaf(m.x, tv.y, y[q].y);
+          } else if (mtype == 2) {
+            y[q].x = fmaf(-m.y, tv.y, y[q].x);
+            y[q].y = fmaf(m.y, tv.x, y[q].y);
+          } else {
+            y[q].x = fmaf(m.x, tv.x, fmaf(-m.y, tv.y, y[q].x));
+            y[q].y = fmaf(m.x, tv.y, fmaf(m.y, tv.x, y[q].y));
+          }
         }
       }
     }
   }
-  float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i * nk1) * nb + v;
+  float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * nk1) * nb + v;
 #pragma unroll
-  for (int a = 0; a < NKP; ++a)
-    if (a < nk1) Y[(long long)a * nb] = acc[a];
+  for (int q = 0; q < QY; ++q) {
+    const int pq = wid * QY + q;
+    const int i = pq / NKP, a = pq - (pq / NKP) * NKP;
+    if (i < nr && a < nk1) Y[((long long)i * nk1 + a) * nb] = y[q];
+  }
 }
 
-__global__ void __launch_bounds__(KB_MV_THREADS) kb_matvec(BatchMV p) {
+__global__ void __launch_bounds__(256, 2) kb_matvec(BatchMV p) {
   extern __shared__ float kb_smem[];
-  const int row = blockIdx.x;
-  const int grp = blockIdx.y;
-  if (p.grp_active && !p.grp_active[grp]) return;
-  const int v = grp * KB_MV_THREADS + threadIdx.x;
-  const int s1 = __ldg(p.row_slab + row);
-  const int i = __ldg(p.row_i + row);
+  const int task = blockIdx.x;
+  if (p.grp_active && !p.grp_active[blockIdx.y]) return;
+  const int s1 = __ldg(p.task_slab + task);
+  const int i0 = __ldg(p.task_i0 + task);
+  const int nr = __ldg(p.task_nr + task);
   const int nk1 = __ldg(p.op.out_dk + s1);
-  int maxnk2 = 1;
-  const int tb = __ldg(p.op.term_ptr + s1), te = __ldg(p.op.term_ptr + s1 + 1);
-  int maxw = 1;
-  for (int t = tb; t < te; ++t) {
-    maxnk2 = max(maxnk2, __ldg(p.op.in_dk + __ldg(p.op.t_in + t)));
-    maxw = max(maxw, __ldg(p.op.mf_width + __ldg(p.op.t_mf + t)));
-  }
-  float* ks = kb_smem;
-  float2* mfs = reinterpret_cast<float2*>(kb_smem + 2 * KB_NK_MAX * KB_NK_MAX);
-  int* cols = reinterpret_cast<int*>(mfs + 64);
-  (void)maxnk2;
-  (void)maxw;
-  if (nk1 <= 4) kb_row<4>(p, s1, i, v, ks, mfs, cols);
-  else if (nk1 <= 8) kb_row<8>(p, s1, i, v, ks, mfs, cols);
-  else if (nk1 <= 12) kb_row<12>(p, s1, i, v, ks, mfs, cols);
-  else if (nk1 <= 16) kb_row<16>(p, s1, i, v, ks, mfs, cols);
-  else if (nk1 <= 24) kb_row<24>(p, s1, i, v, ks, mfs, cols);
-  else kb_row<32>(p, s1, i, v, ks, mfs, cols);
+  if (nk1 <= 4) kb_tile<4>(p, s1, i0, nr, kb_smem);
+  else if (nk1 <= 8) kb_tile<8>(p, s1, i0, nr, kb_smem);
+  else if (nk1 <= 16) kb_tile<16>(p, s1, i0, nr, kb_smem);
+  else kb_tile<32>(p, s1, i0, nr, kb_smem);
 }
 
-// any active vector per mat-vec group
-__global__ void kb_group_active(const int* active, int* grp, int nb) {
-  const int g = blockIdx.x;
-  int any = 0;
-  for (int i = threadIdx.x; i < KB_MV_THREADS; i += blockDim.x) {
-    const int v = g * KB_MV_THREADS + i;
-    if (v < nb && active[v]) any = 1;
+// shared memory of kb_matvec: the largest of the four tile shapes
+static size_t kb_matvec_smem() {
+  size_t best = 0;
+  for (int nkp : {4, 8, 16, 32}) {
+    const int R = 128 / nkp, NJ = R + 4;
+    size_t b = sizeof(float2) * NJ * nkp * 32 + sizeof(float) * 2 * 36 * nkp + sizeof(float2) * R * KB_WMAX +
+               sizeof(int) * (R * KB_WMAX + 2);
+    best = std::max(best, b);
   }
-  any = __syncthreads_or(any);
+  return best;
+}
+
+// any active vector per 32-vector group
+__global__ void kb_group_active(const int* active, int* grp, int ngrp) {
+  const int g = blockIdx.x * blockDim.y + threadIdx.y;
+  if (g >= ngrp) return;
+  const int any = __any_sync(0xffffffffu, active[g * 32 + threadIdx.x] != 0);
   if (threadIdx.x == 0) grp[g] = any;
 }
 
@@ -541,7 +622,7 @@ int balloc(kr_batch* b, size_t count, T** p) {
   *p = static_cast<T*>(q);
   return KR_OK;
 }
-int mv_groups(const kr_batch* b) { return (b->nb + KB_MV_THREADS - 1) / KB_MV_THREADS; }
+int mv_groups(const kr_batch* b) { return b->nb / 32; }
 
 int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool masked, cudaStream_t st) {
   BatchMV p;
@@ -549,12 +630,18 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
   p.X = X;
   p.Y = Y;
   p.nb = b->nb;
-  p.row_slab = b->row_slab;
-  p.row_i = b->row_i;
+  p.task_slab = b->task_slab;
+  p.task_i0 = b->task_i0;
+  p.task_nr = b->task_nr;
   p.grp_active = masked ? b->grp_active : nullptr;
-  const size_t smem = sizeof(float) * 2 * KB_NK_MAX * KB_NK_MAX + sizeof(float2) * 64 + sizeof(int) * 64;
-  dim3 grid(b->nrows, mv_groups(b));
-  kb_matvec<<<grid, KB_MV_THREADS, smem, st>>>(p);
+  const size_t smem = kb_matvec_smem();
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(kb_matvec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  dim3 grid(b->ntask, mv_groups(b));
+  kb_matvec<<<grid, 256, smem, st>>>(p);
   b->launches++;
   KR_CUDA(op->ctx, cudaGetLastError());
   return KR_OK;
@@ -575,7 +662,8 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
   std::vector<int> widths(std::max(1, op->nmf));
   cudaMemcpy(widths.data(), op->dev.mf_width, sizeof(int) * op->nmf, cudaMemcpyDeviceToHost);
   for (int i = 0; i < op->nmf; ++i)
-    if (widths[i] > 64) return set_err(op->ctx, KR_ERR_UNSUPPORTED, "kr_batch_create: M band wider than 64");
+    if (widths[i] > KB_WMAX)
+      return set_err(op->ctx, KR_ERR_UNSUPPORTED, "kr_batch_create: M band wider than 16 entries per row");
   kr_batch* b = new kr_batch();
   b->op = op;
   b->nvec = (int)nvec;
@@ -601,18 +689,25 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
   BA(nb, &b->err);
   BA((size_t)KB_RED_CHUNKS * (m1 + 1) * nb, &b->part);
   BA(2, &b->counts);
-  std::vector<int> rs, ri;
-  for (int s = 0; s < (int)dm.size(); ++s)
-    for (int i = 0; i < dm[s]; ++i) {
-      rs.push_back(s);
-      ri.push_back(i);
+  // output tiles: R = 128 / NKP rows of one slab (NKP = n_k rounded up to 4, 8, 16, 32)
+  std::vector<int> ts, ti, tn;
+  for (int s = 0; s < (int)dm.size(); ++s) {
+    const int nkp = dk[s] <= 4 ? 4 : dk[s] <= 8 ? 8 : dk[s] <= 16 ? 16 : 32;
+    const int R = 128 / nkp;
+    for (int i0 = 0; i0 < dm[s]; i0 += R) {
+      ts.push_back(s);
+      ti.push_back(i0);
+      tn.push_back(std::min(R, dm[s] - i0));
     }
-  b->nrows = (int)rs.size();
-  BA(rs.size(), &b->row_slab);
-  BA(ri.size(), &b->row_i);
+  }
+  b->ntask = (int)ts.size();
+  BA(ts.size(), &b->task_slab);
+  BA(ti.size(), &b->task_i0);
+  BA(tn.size(), &b->task_nr);
 #undef BA
-  cudaMemcpy(b->row_slab, rs.data(), sizeof(int) * rs.size(), cudaMemcpyHostToDevice);
-  cudaMemcpy(b->row_i, ri.data(), sizeof(int) * ri.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->task_slab, ts.data(), sizeof(int) * ts.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->task_i0, ti.data(), sizeof(int) * ti.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->task_nr, tn.data(), sizeof(int) * tn.size(), cudaMemcpyHostToDevice);
   KR_CUDA(op->ctx, cudaDeviceSynchronize());
   *out = b;
   return KR_OK;
@@ -662,7 +757,7 @@ extern "C" int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double f
   KR_CUDA(ctx, cudaGetLastError());
   int kused = 0;
   for (int k = 0; k < b->mmax; ++k) {
-    kb_group_active<<<mv_groups(b), 128, 0, st>>>(b->active, b->grp_active, nb);
+    kb_group_active<<<(mv_groups(b) + 7) / 8, dim3(32, 8), 0, st>>>(b->active, b->grp_active, mv_groups(b));
     int rc = launch_matvec(b, op, b->V + (long long)k * dim * nb, b->W, true, st);
     if (rc) return rc;
     kb_dots<<<eg, eb, 0, st>>>(b->V, b->W, b->active, dim, nb, k, stride, b->part);

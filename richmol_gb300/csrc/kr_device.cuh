@@ -43,9 +43,11 @@ struct DevOp {
   long long dim_out, dim_in;
   // K blocks
   const long long* k_off; const int* k_rows; const int* k_cols; const int* k_type; const double* k_data;
+  const float* k_f32;   // FP32 copy of k_data (same offsets), for the batched complex64 path
   // MF instances (ELL): values at mf_val + mf_off[i], columns at m_col + mf_col_off[i]
   const long long* mf_off; const long long* mf_col_off; const int* mf_width;
   const int* m_col; double2* mf_val;
+  float2* mf_f32;       // FP32 copy of mf_val, written with it by the field kernel
   // terms grouped by output slab
   const int* term_ptr; const int* t_in; const int* t_k; const int* t_mf;
   const int* mf_type;   // per MF instance: 0 complex, 1 real, 2 imaginary (set with the field)

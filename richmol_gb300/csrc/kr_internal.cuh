@@ -27,6 +27,7 @@ struct DevField {
   const long long* m_val_off; const int* m_ncart; const int* m_rows; const int* m_width;
   const double2* m_val;
   double2* mf_val;
+  float2* mf_f32;
 };
 
 struct kr_ctx {

@@ -72,7 +72,9 @@ __global__ void __launch_bounds__(256) kr_field_kernel(DevField f, FieldCoef c) 
     for (int ci = 0; ci < nc; ++ci) cfma(v, c.coef[p][ci], __ldg(M + ci * stride));
     // field.py:1133-1137: elements below the threshold are dropped
     if (c.thresh[p] > 0.0 && sqrt(cabs2(v)) < c.thresh[p]) v = make_double2(0.0, 0.0);
-    f.mf_val[e] = cmul(c.scale[p], v);
+    const double2 mfv = cmul(c.scale[p], v);
+    f.mf_val[e] = mfv;
+    f.mf_f32[e] = make_float2((float)mfv.x, (float)mfv.y);
   }
 }
 
@@ -783,12 +785,21 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   UP(d->k_type, d->nk, &p_i); D.k_type = p_i;
   double* p_d;
   UP(k_t.data(), k_t.size(), &p_d); D.k_data = p_d;
+  {
+    std::vector<float> k32(k_t.begin(), k_t.end());
+    float* p_f;
+    UP(k32.data(), k32.size(), &p_f); D.k_f32 = p_f;
+  }
   UP((const long long*)inst_ptr.data(), d->nmf, &p_l); D.mf_off = p_l;
   UP((const long long*)mf_col_off.data(), d->nmf, &p_l); D.mf_col_off = p_l;
   UP(mf_width.data(), d->nmf, &p_i); D.mf_width = p_i;
   UP(d->m_col, d->m_col_len, &p_i); D.m_col = p_i;
   double2* p_c;
   UP((const double2*)nullptr, nent, &p_c); D.mf_val = p_c;
+  {
+    float2* p_f2;
+    UP((const float2*)nullptr, nent, &p_f2); D.mf_f32 = p_f2;
+  }
   UP(term_ptr.data(), term_ptr.size(), &p_i); D.term_ptr = p_i;
   UP(t_in.data(), t_in.size(), &p_i); D.t_in = p_i;
   UP(t_k.data(), t_k.size(), &p_i); D.t_k = p_i;
@@ -815,6 +826,7 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   UP(d->m_width, d->nm, &p_i); F.m_width = p_i;
   UP((const double2*)d->m_val, d->m_val_len / 2, &p_c); F.m_val = p_c;
   F.mf_val = D.mf_val;
+  F.mf_f32 = D.mf_f32;
   F.nmf = d->nmf;
   F.mf_type = const_cast<int*>(D.mf_type);
   signed char* p_s;
