@@ -1,15 +1,22 @@
 #!/usr/bin/env python
-"""Krylov time-propagation benchmark: state-steps/s on one GB300.
+"""Krylov time-propagation benchmark on one GB300: state-steps/s.
 
-One step is one TDSE.update of the state (H0 half-phases + the field-dressed
-Lanczos exponential). Default workload: the plain FP64 drop-in configuration,
-an asymmetric top (A, B, C = 9.0, 5.0, 3.2 cm^-1, Watson A, D2) with J = 0..40
-(dim 91,881), one state vector, DC 20 kV/cm + 1e12 W/cm^2 FWHM 500 fs pulse at
-35 deg, dt = 5 fs; synthetic molecule and fields built in-process.
+A step is one TDSE.update of a state vector (H0 half-phases + the field-dressed
+Krylov exponential); state-steps/s = vectors x steps / time.
 
-Prints ONE JSON line (rank 0). ``--impl reference`` times the CPU
-restatement of the reference algorithm (numpy/scipy, the oracle) on the host
-cores for the same workload and metric.
+Headline (``value``): the batched mixed-precision form on the thermal-ensemble
+configuration — asymmetric top (A, B, C = 9.0, 5.0, 3.2 cm^-1, Watson A,
+D2), J = 0..30 (dim 39,711), the T = 5 K ensemble (states with Boltzmann
+weight >= 1e-5, padded to 4096 vectors), DC 20 kV/cm + 1e12 W/cm^2 FWHM 500 fs
+pulse at 35 deg, dt = 10 fs, per-vector Krylov tolerance 1e-8. Beside it the
+plain FP64 path on the same workload (the ratio the metric names), the
+observable error of the batched form against FP64, and the plain FP64 drop-in
+configuration (J <= 40, dim 91,881, one vector, dt = 5 fs). Synthetic molecule
+and fields are built in-process.
+
+``--impl reference`` times the CPU restatement of the reference algorithm (the
+oracle, numpy/scipy) on the host cores, one process per core, for the same
+workload and metric.
 """
 import argparse
 import json
@@ -32,21 +39,24 @@ UNIT = "state-steps/s"
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=1000)
+    p.add_argument("--steps", type=int, default=50, help="timed steps of the batched ensemble")
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--jmax", type=int, default=40)
-    p.add_argument("--e2e-steps", type=int, default=300)
+    p.add_argument("--jmax", type=int, default=30, help="J range of the ensemble workload")
+    p.add_argument("--nvec", type=int, default=4096)
+    p.add_argument("--jmax-plain", type=int, default=40, help="J range of the plain FP64 drop-in workload")
+    p.add_argument("--plain-steps", type=int, default=400)
+    p.add_argument("--acc-steps", type=int, default=150, help="steps of the batched-vs-FP64 observable check")
+    p.add_argument("--e2e-steps", type=int, default=20)
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="bound of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true", help="headline measurement only")
     return p.parse_args()
 
 
 def dist_info():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
 
 
 # ---------------------------------------------------------------------------
@@ -67,8 +77,7 @@ class ClockSampler:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
+            threading.Thread(target=self._read, daemon=True).start()
         except (FileNotFoundError, OSError):
             self.proc = None
         return self
@@ -141,9 +150,9 @@ def to_oracle(T):
     return o
 
 
-def cpu_reference_rate(wl, seconds, max_steps=None, warmup=1):
+def cpu_reference_rate(wl, seconds, max_steps=None, warmup=1, vec=None):
     """State-steps/s of the oracle (reference algorithm in numpy/scipy, one
-    host thread) on the first steps of the workload, bounded by ``seconds``."""
+    host thread) on the first steps of the workload for one vector."""
     from oracle.cartens import add_cartens
     from oracle.tdse import OTDSE
     from richmol_gb300.convert_units import AUdip_x_Vm_to_invcm
@@ -155,10 +164,8 @@ def cpu_reference_rate(wl, seconds, max_steps=None, warmup=1):
         oHdc = oHdc * (-1 * AUdip_x_Vm_to_invcm())
     td = OTDSE(t_start=wl.t_start, t_end=wl.t_end, dt=wl.dt)
     tc = td.time_grid()
-    v = td.init_state(oh0, temp=0)
-    n = 0
-    t_run = 0.0
-    i = 0
+    v = td.init_state(oh0, temp=0) if vec is None else vec.reshape(1, -1).astype(np.complex128)
+    n, t_run, i = 0, 0.0, 0
     while True:
         oHac.field(wl.field(tc[i]))
         H = oHac if oHdc is None else add_cartens(oHdc, oHac)
@@ -174,12 +181,27 @@ def cpu_reference_rate(wl, seconds, max_steps=None, warmup=1):
     return v.shape[0] * n / t_run, n, t_run
 
 
+def _reference_worker(args):
+    """One host process: one vector of the ensemble workload (spawned)."""
+    jmax, nvec, idx, seconds, max_steps = args
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    sys.path.insert(0, ROOT)
+    from richmol_gb300 import workloads
+    wl, ens = workloads.thermal_asym_top(Jmax=jmax, nvec=nvec)
+    v = np.zeros(wl.dim, np.complex128)
+    v[ens.index[idx % nvec]] = 1.0
+    rate, n, t = cpu_reference_rate(wl, seconds, max_steps=max_steps, vec=v)
+    return n, t
+
+
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
 def run_ours(args, ws, rank, local):
+    import ctypes
     import torch
     from richmol_gb300 import TDSE, _native, workloads
+    from richmol_gb300.batch import Ensemble
     from richmol_gb300.device import context
 
     torch.cuda.set_device(local)
@@ -187,176 +209,284 @@ def run_ours(args, ws, rank, local):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    t_build = time.time()
-    wl = workloads.asym_top(Jmax=args.jmax)
-    t_build = time.time() - t_build
+    ctx = context(local)
+    fp64, fp32 = ctypes.c_double(), ctypes.c_double()
+    _native.check(_native.lib().kr_probe_fp64(ctx, ctypes.byref(fp64)), ctx)
+    _native.check(_native.lib().kr_probe_fp32(ctx, ctypes.byref(fp32)), ctx)
+    peaks, peak_kind = load_peaks()
 
+    # ---- batched ensemble: the headline --------------------------------------
+    t_build = time.time()
+    wl, ensd = workloads.thermal_asym_top(Jmax=args.jmax, nvec=args.nvec)
+    t_build = time.time() - t_build
+    nvec, dim = args.nvec, wl.dim
     td = TDSE(t_start=wl.t_start, t_end=wl.t_end, dt=wl.dt)
     tc = td.time_grid()
     nsteps = len(tc)
-    v0 = td.init_state(wl.h0, temp=0)
-    nvec = v0.shape[0]
-    v = torch.from_numpy(v0).to(dev)
-    phase = td._h0_phase(wl.h0, td.exp_fac, dev)
-    fac = td.exp_fac
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MiB > L2
-
-    def step(i):
-        H = wl.hamiltonian(tc[i % nsteps])
-        plan = H.device_operator()
-        plan.step(v, phase, fac, 1e-15)
-        return plan
-
+    ens = Ensemble(td, wl.h0, nvec, tol=1e-8)
+    ens.load(ensd.vectors(dim))
     for i in range(args.warmup):
-        plan = step(i)
+        ens.step(wl.hamiltonian(tc[i]))
     torch.cuda.synchronize()
-    plan.sync_status()
-
-    # ---- value: device-resident state, L2 flushed before every step -----------
     K = args.steps
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    ek = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    launches0 = plan.launches()
-    korders = []
+    l0 = ens.launches()
+    plan_l0 = wl.Hac._plan().launches()
+    kmax_seen = []
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         for j in range(K):
-            i = args.warmup + j
-            flush.zero_()
+            i = (args.warmup + j) % nsteps
+            H = wl.hamiltonian(tc[i])
             ev[j][0].record()
-            H = wl.hamiltonian(tc[i % nsteps])
-            plan = H.device_operator()
-            ek[j][0].record()
-            plan.step(v, phase, fac, 1e-15)
-            ek[j][1].record()
+            ens.step(H)
             ev[j][1].record()
+            kmax_seen.append(ens.last_kmax)
         torch.cuda.synchronize()
-    plan.sync_status()
-    launches = plan.launches() - launches0
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    kern_ms = [a.elapsed_time(b) for a, b in ek]
     total_s = sum(step_ms) / 1e3
+    launches = (ens.launches() - l0) + (wl.Hac._plan().launches() - plan_l0)
     if ws > 1:
         t = torch.tensor([total_s], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_s = float(t.item())
-        torch.distributed.barrier()
     value = ws * nvec * K / total_s
+    korder = np.bincount(ens.korder(), minlength=1)
 
-    # Krylov orders of the timed steps (one checked step per 50 to read them)
-    kord = np.zeros(1, np.int32)
-    ks = []
-    v_probe = v.clone()
-    for j in range(0, K, max(1, K // 20)):
-        H = wl.hamiltonian(tc[(args.warmup + j) % nsteps])
-        H.device_operator().step(v_probe, phase, fac, 1e-15, korder=kord)
-        ks.append(int(kord[0]))
-    kavg = float(np.mean(ks))
-
-    # ---- e2e: TDSE.update with host (numpy) buffers ---------------------------
-    K2 = min(args.e2e_steps, nsteps)
-    td2 = TDSE(t_start=wl.t_start, t_end=wl.t_end, dt=wl.dt)
-    tc2 = td2.time_grid()
-    vh = v0.copy()
-    Hs = wl.hamiltonian(tc2[0])
-    vh, _ = td2.update(Hs, vh, H0=wl.h0)  # warm-up (H0 phase set-up)
+    # dominant kernel (batched complex64 mat-vec) alone
+    plan = wl.hamiltonian(tc[args.warmup]).device_operator()
+    em = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
+    for a, b in em:
+        a.record()
+        _native.check(_native.lib().kr_batch_matvec(ens.handle, plan.op, ctypes.c_void_p(
+            torch.cuda.current_stream().cuda_stream)), ctx)
+        b.record()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for j in range(1, K2 + 1):
-        vh, _ = td2.update(wl.hamiltonian(tc2[j]), vh, H0=wl.h0)
-    e2e_s = time.perf_counter() - t0
-    e2e_value = ws * nvec * K2 / e2e_s
-
-    # ---- roofline of the dominant kernel (kr_step_kernel) ----------------------
+    mv_s = statistics.median(a.elapsed_time(b) for a, b in em) / 1e3
     fma_mv, bytes_mv = plan.work()
-    n = wl.dim
-    kern_s = statistics.mean(kern_ms) / 1e3
-    # FLOPs: k mat-vecs + the Lanczos vector work of each iteration
-    flops_step = 2.0 * kavg * fma_mv + n * sum(8.0 * (k + 1) + 40.0 for k in range(1, int(round(kavg))))
-    # algorithmic bytes (no re-orthogonalisation): s n (3m + 1) + factors
-    alg_bytes = 16.0 * n * (3 * kavg + 1) + (bytes_mv - 32.0 * n)
-    peaks, peak_kind = load_peaks()
-    ctx = context(local)
-    import ctypes
-    fp64 = ctypes.c_double()
-    _native.check(_native.lib().kr_probe_fp64(ctx, ctypes.byref(fp64)), ctx)
-    traffic = load_traffic().get("kr_step_kernel_per_launch_bytes")
-    achieved_gbs = alg_bytes / kern_s / 1e9
+    mv_flops = 2.0 * fma_mv * nvec
+    mv_bytes = 8.0 * 2 * dim * nvec  # complex64 X in + Y out (factors are shared by all vectors)
+    traffic = load_traffic().get("kb_matvec_per_launch_bytes_4096")
+    gbs = mv_bytes / mv_s / 1e9
     roofline = {
-        "bound": "hbm", "achieved": round(achieved_gbs, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-        "frac": round(achieved_gbs / peaks["hbm_gbs"], 5), "traffic": traffic,
-        "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
-        "kernel": "kr_step_kernel", "kernel_ms": round(kern_s * 1e3, 4),
-        "alg_bytes_per_launch": alg_bytes, "krylov_order_avg": kavg,
-        "fp64": {"achieved_tflops": round(flops_step / kern_s / 1e12, 4),
-                 "peak_tflops": round(fp64.value, 4), "frac": round(flops_step / kern_s / 1e12 / fp64.value, 4),
-                 "peak_source": "measured FMA probe (kr_probe_fp64)",
-                 "flops_per_launch": flops_step},
+        "bound": "hbm", "achieved": round(gbs, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+        "frac": round(gbs / peaks["hbm_gbs"], 4), "traffic": traffic,
+        "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+        "kernel": "kb_matvec (complex64 batched mat-vec)", "kernel_ms": round(mv_s * 1e3, 3),
+        "alg_bytes_per_launch": mv_bytes,
+        "fp32": {"achieved_tflops": round(mv_flops / mv_s / 1e12, 2), "peak_tflops": round(fp32.value, 1),
+                 "frac": round(mv_flops / mv_s / 1e12 / fp32.value, 4),
+                 "peak_source": "measured FP32 FMA probe (kr_probe_fp32)", "flops_per_launch": mv_flops},
     }
-
     out = {
-        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
-        "ms_per_step": round(total_s * 1e3 / K, 4), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
-        "config": {"workload": f"plain FP64 drop-in: asymmetric top D2 Watson-A, J=0..{args.jmax}, dim {n}, "
-                               f"{nvec} vector, DC 20 kV/cm + 1e12 W/cm^2 FWHM 500 fs pulse at 35 deg, dt 5 fs",
-                   "dim": n, "nvec": nvec, "jmax": args.jmax, "dt_fs": 5.0, "tol": 1e-15,
-                   "l2": "flushed (256 MiB write) before every timed step", "parallelism": f"replicas x{ws}",
-                   "factor_build_s": round(t_build, 2)},
-        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(v0.nbytes),
-                "d2h_bytes_per_step": int(v0.nbytes), "steps": K2,
-                "api": "richmol_gb300.TDSE.update(H, numpy vecs, H0=h0)"},
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
+        "ms_per_step": round(total_s * 1e3 / K, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64 mat-vec (FP32 accumulate) / f64 Lanczos scalars and state",
+        "data": "synthetic",
+        "config": {"workload": f"batched thermal ensemble: asymmetric top D2 Watson-A J=0..{args.jmax} "
+                               f"(dim {dim}), T=5 K ensemble of {ensd.n_natural} states with weight>=1e-5 padded "
+                               f"to {nvec} vectors, DC 20 kV/cm + 1e12 W/cm^2 FWHM 500 fs pulse at 35 deg, "
+                               f"dt 10 fs, per-vector Krylov tolerance 1e-8",
+                   "dim": dim, "nvec": nvec, "n_natural": ensd.n_natural, "jmax": args.jmax, "dt_fs": 10.0,
+                   "tol": 1e-8, "l2": "inputs larger than L2 (state 2.6 GB, basis complex64)",
+                   "parallelism": f"replicas x{ws}", "factor_build_s": round(t_build, 2),
+                   "krylov_orders": {str(k): int(c) for k, c in enumerate(korder) if c},
+                   "timed_window_ps": [float(tc[args.warmup % nsteps]), float(tc[(args.warmup + K - 1) % nsteps])]},
         "roofline": roofline,
         "gpu_launches": int(launches),
-        "step_ms_p50": round(statistics.median(step_ms), 4),
-        "step_ms_p99": round(float(np.percentile(step_ms, 99)), 4),
+        "step_ms_p50": round(statistics.median(step_ms), 3),
+        "step_ms_p99": round(float(np.percentile(step_ms, 99)), 3),
+        "peaks_probe": {"fp64_tflops": round(fp64.value, 3), "fp32_tflops": round(fp32.value, 2)},
     }
     clocks = clk.summary()
     if clocks:
         out["clocks"] = clocks
+
+    if not args.no_extras:
+        # ---- e2e: public API, per step the field in and the observable out ----
+        K2 = args.e2e_steps
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        trace = []
+        for j in range(K2):
+            H = wl.hamiltonian(tc[(args.warmup + K + j) % nsteps])
+            ens.step(H)
+            e = ens.expect(wl.cos2)                     # synchronises: result on the host
+            trace.append(float(np.dot(ensd.weights, e.real)) + 1.0 / 3.0)
+        e2e_s = time.perf_counter() - t0
+        from richmol_gb300._native import FIELD_COEF_BYTES
+        out["e2e"] = {"value": round(ws * nvec * K2 / e2e_s, 1), "unit": UNIT,
+                      "h2d_bytes_per_step": FIELD_COEF_BYTES, "d2h_bytes_per_step": 16 * nvec, "steps": K2,
+                      "api": "Ensemble.step(H(t)) + Ensemble.expect(cos^2) each step (field in, <cos^2> out)",
+                      "includes_observable": True}
+
+        # ---- batched vs plain FP64 on the natural vectors: error and plain rate ----
+        nn = min(ensd.n_natural, 32)
+        w = ensd.weights[:nn]
+        v0 = ensd.vectors(dim)[:nn]
+        tda = TDSE(t_start=wl.t_start, t_end=wl.t_end, dt=wl.dt)
+        tca = tda.time_grid()
+        ea = Ensemble(tda, wl.h0, nn, tol=1e-8)
+        ea.load(v0)
+        ref = torch.from_numpy(v0).to(dev)
+        worst_w, worst_v = 0.0, 0.0
+        plain_ms = []
+        for i in range(args.acc_steps):
+            H = wl.hamiltonian(tca[i])
+            ea.step(H)
+            a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a_.record()
+            ref, _ = tda.update(H, H0=wl.h0, vecs=ref, inplace=True, check=False)
+            b_.record()
+            if i % 5 == 4 or i == args.acc_steps - 1:
+                e = ea.expect(wl.cos2).real
+                r = ens_expect_plain(ref, wl.cos2)
+                worst_w = max(worst_w, abs(float(np.dot(w, e - r))))
+                worst_v = max(worst_v, float(np.abs(e - r).max()))
+            torch.cuda.synchronize()
+            plain_ms.append(a_.elapsed_time(b_))
+        plain_rate = nn * len(plain_ms[3:]) / (sum(plain_ms[3:]) / 1e3)
+        out["plain_fp64_same_workload"] = {
+            "value": round(plain_rate, 1), "unit": UNIT,
+            "sample": f"{nn} vectors x {args.acc_steps} steps through the pulse, CUDA events",
+            "speedup_batched_vs_plain": round(value / plain_rate, 2)}
+        out["accuracy_vs_fp64"] = {
+            "max_abs_err_weighted_cos2": worst_w, "max_abs_err_per_vector_cos2": worst_v,
+            "bound": 1e-6, "steps": args.acc_steps, "vectors": nn,
+            "reference": "plain FP64 GPU path (parity-tested against the CPU oracle)"}
+
+        # ---- plain FP64 drop-in configuration (J <= 40, one vector, dt 5 fs) ----
+        out["plain_fp64_drop_in"] = run_plain(args, dev, peaks, peak_kind, fp64.value)
+
     if rank == 0 and not args.no_cpu_baseline:
-        rate, nst, tt = cpu_reference_rate(wl, args.cpu_seconds)
+        rate, nst, tt = cpu_reference_rate(wl, args.cpu_seconds, vec=ensd.vectors(dim)[0])
         out["cpu_baseline"] = {"value": round(rate, 4), "unit": UNIT, "cores": 1, "kind": "port",
-                               "sample": f"{nst} steps x {nvec} vector of the same workload in {tt:.1f} s "
+                               "sample": f"{nst} steps of 1 vector of the ensemble workload in {tt:.1f} s "
                                          f"(oracle restatement of tdse.py/field.py, numpy/scipy, 1 thread)"}
     if ws > 1:
         torch.distributed.destroy_process_group()
     return out
 
 
+def ens_expect_plain(ref, O):
+    """<v|O|v> of FP64 states (rows of a CUDA tensor) through the FP64 mat-vec."""
+    import torch
+    plan = O.device_operator()
+    y = torch.empty_like(ref)
+    plan.matvec(ref, y)
+    return torch.sum(torch.conj(ref) * y, dim=1).real.cpu().numpy()
+
+
+def run_plain(args, dev, peaks, peak_kind, fp64_peak):
+    """The plain FP64 drop-in configuration: J <= 40 (dim 91,881), one vector,
+    dt = 5 fs, L2 flushed before every step; kernel roofline on the FP64 pipe."""
+    import torch
+    from richmol_gb300 import TDSE, workloads
+    wl = workloads.asym_top(Jmax=args.jmax_plain)
+    td = TDSE(t_start=wl.t_start, t_end=wl.t_end, dt=wl.dt)
+    tc = td.time_grid()
+    v0 = td.init_state(wl.h0, temp=0)
+    v = torch.from_numpy(v0).to(dev)
+    phase = td._h0_phase(wl.h0, td.exp_fac, dev)
+    fac = td.exp_fac
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for i in range(5):
+        wl.hamiltonian(tc[i]).device_operator().step(v, phase, fac, 1e-15)
+    K = args.plain_steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    ek = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    torch.cuda.synchronize()
+    for j in range(K):
+        flush.zero_()
+        ev[j][0].record()
+        plan = wl.hamiltonian(tc[5 + j]).device_operator()
+        ek[j][0].record()
+        plan.step(v, phase, fac, 1e-15)
+        ek[j][1].record()
+        ev[j][1].record()
+    torch.cuda.synchronize()
+    plan.sync_status()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    kern_s = statistics.mean(a.elapsed_time(b) for a, b in ek) / 1e3
+    kord = np.zeros(1, np.int32)
+    ks = []
+    vp = v.clone()
+    for j in range(0, K, max(1, K // 20)):
+        wl.hamiltonian(tc[5 + j]).device_operator().step(vp, phase, fac, 1e-15, korder=kord)
+        ks.append(int(kord[0]))
+    kavg = float(np.mean(ks))
+    fma_mv, bytes_mv = plan.work()
+    n = wl.dim
+    flops = 2.0 * kavg * fma_mv + n * sum(8.0 * (k + 1) + 40.0 for k in range(1, int(round(kavg))))
+    alg_bytes = 16.0 * n * (3 * kavg + 1) + (bytes_mv - 32.0 * n)
+    gbs = alg_bytes / kern_s / 1e9
+    # e2e through the reference-facing API with host (numpy) buffers
+    td2 = TDSE(t_start=wl.t_start, t_end=wl.t_end, dt=wl.dt)
+    tc2 = td2.time_grid()
+    vh, _ = td2.update(wl.hamiltonian(tc2[0]), v0, H0=wl.h0)
+    torch.cuda.synchronize()
+    K2 = 100
+    t0 = time.perf_counter()
+    for j in range(1, K2 + 1):
+        vh, _ = td2.update(wl.hamiltonian(tc2[j]), vh, H0=wl.h0)
+    e2e = K2 / (time.perf_counter() - t0)
+    return {
+        "value": round(K / (sum(step_ms) / 1e3), 1), "unit": UNIT, "steps": K,
+        "workload": f"asymmetric top D2 J=0..{args.jmax_plain} (dim {n}), 1 vector, dt 5 fs, L2 flushed per step",
+        "step_ms_p50": round(statistics.median(step_ms), 4), "kernel": "kr_step_kernel",
+        "kernel_ms": round(kern_s * 1e3, 4), "krylov_order_avg": kavg,
+        "roofline": {"bound": "hbm", "achieved": round(gbs, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(gbs / peaks["hbm_gbs"], 5),
+                     "traffic": load_traffic().get("kr_step_kernel_per_launch_bytes")},
+        "fp64": {"achieved_tflops": round(flops / kern_s / 1e12, 4), "peak_tflops": round(fp64_peak, 4),
+                 "frac": round(flops / kern_s / 1e12 / fp64_peak, 4), "peak_source": "kr_probe_fp64"},
+        "e2e": {"value": round(e2e, 1), "unit": UNIT, "h2d_bytes_per_step": int(v0.nbytes),
+                "d2h_bytes_per_step": int(v0.nbytes), "api": "TDSE.update(H, numpy vecs, H0=h0)"},
+    }
+
+
 def run_reference(args, ws, rank, local):
+    """CPU restatement of the reference algorithm (the reference itself does not
+    install: numpy.distutils / Fortran), one process per host core, each
+    propagating one vector of the ensemble workload."""
     if rank != 0:
         return None
-    from richmol_gb300 import workloads
-    wl = workloads.asym_top(Jmax=args.jmax)
-    budget = min(120.0, max(10.0, args.cpu_seconds * 4))
-    rate, nst, tt = cpu_reference_rate(wl, budget, max_steps=args.steps, warmup=min(args.warmup, 1))
+    import multiprocessing as mp
+    ncores = os.cpu_count() or 1
+    nproc = max(1, min(ncores, 64))
+    per_steps = max(1, min(args.steps, 20))
+    budget = 60.0
+    ctxm = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctxm.Pool(nproc) as pool:
+        res = pool.map(_reference_worker, [(args.jmax, args.nvec, i, budget, per_steps) for i in range(nproc)])
+    wall = time.perf_counter() - t0
+    steps = sum(n for n, _ in res)
+    busy = max(t for _, t in res)
+    rate = steps / busy
     return {
-        "impl": "reference", "metric": METRIC, "value": round(rate, 4), "unit": UNIT, "n_gpus": ws,
-        "steps": nst, "warmup": min(args.warmup, 1), "ms_per_step": round(tt * 1e3 / max(nst, 1), 3),
+        "impl": "reference", "metric": METRIC, "value": round(rate, 3), "unit": UNIT, "n_gpus": ws,
+        "steps": per_steps, "warmup": 1, "ms_per_step": round(busy * 1e3 / per_steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)",
         "data": "synthetic",
-        "config": {"workload": f"plain FP64 drop-in: asymmetric top D2 Watson-A, J=0..{args.jmax}, dim {wl.dim}, "
-                               f"1 vector, DC 20 kV/cm + 1e12 W/cm^2 FWHM 500 fs pulse at 35 deg, dt 5 fs",
-                   "dim": wl.dim, "nvec": 1, "jmax": args.jmax},
-        "cpu_baseline": {"value": round(rate, 4), "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": f"{nst} steps of 1 vector in {tt:.1f} s (time budget {budget:.0f} s); the "
-                                   "reference itself does not install (numpy.distutils, Fortran), its algorithm "
-                                   "runs as the numpy/scipy restatement; one vector leaves no parallel work "
-                                   "for more host threads"},
-        "e2e": {"value": round(rate, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": {"workload": f"batched thermal ensemble: asymmetric top D2 Watson-A J=0..{args.jmax}, "
+                               f"{args.nvec} vectors (sampled: {nproc} vectors x {per_steps} steps)",
+                   "jmax": args.jmax, "nvec": args.nvec},
+        "cpu_baseline": {"value": round(rate, 3), "unit": UNIT, "cores": nproc, "kind": "port",
+                         "sample": f"{nproc} processes x {per_steps} steps, one vector each, wall {wall:.0f} s "
+                                   "(incl. factor build); the reference does not install here "
+                                   "(numpy.distutils, Fortran extensions), its algorithm runs as the numpy/scipy "
+                                   "restatement"},
+        "e2e": {"value": round(rate, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
 
 def main():
     args = parse()
     ws, rank, local = dist_info()
-    if args.impl == "reference":
-        out = run_reference(args, ws, rank, local)
-    else:
-        out = run_ours(args, ws, rank, local)
+    out = run_reference(args, ws, rank, local) if args.impl == "reference" else run_ours(args, ws, rank, local)
     if out is not None and rank == 0:
         print(json.dumps(out), flush=True)
 

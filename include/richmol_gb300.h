@@ -209,6 +209,8 @@ int kr_op_work(const kr_op* op, double* fma_per_matvec, double* bytes_per_matvec
  * multiply-add throughput of the device in TFLOP/s (the roofline denominator
  * of the FP64 path). Allocates and synchronises; not for the hot path. */
 int kr_probe_fp64(kr_ctx* ctx, double* tflops);
+/* The same for FP32 fused multiply-adds (denominator of the complex64 mat-vec). */
+int kr_probe_fp32(kr_ctx* ctx, double* tflops);
 
 #ifdef __cplusplus
 }

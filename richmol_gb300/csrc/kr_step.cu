@@ -998,6 +998,39 @@ __global__ void kr_fp64_probe_kernel(double* out, int iters, double a, double b)
   out[blockIdx.x * (long long)blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+__global__ void kr_fp32_probe_kernel(float* out, int iters, float a, float b) {
+  float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+    x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+  }
+  out[blockIdx.x * (long long)blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+extern "C" int kr_probe_fp32(kr_ctx* ctx, double* tflops) {
+  if (!ctx || !tflops) return set_err(ctx, KR_ERR_ARG, "kr_probe_fp32: NULL argument");
+  KR_CUDA(ctx, cudaSetDevice(ctx->device));
+  const int blocks = ctx->nsm * 8, threads = 256, iters = 65536;
+  float* out = nullptr;
+  KR_CUDA(ctx, cudaMalloc(&out, sizeof(float) * blocks * threads));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  kr_fp32_probe_kernel<<<blocks, threads>>>(out, iters, 0.999999f, 1e-7f);
+  cudaEventRecord(e0);
+  for (int r = 0; r < 5; ++r) kr_fp32_probe_kernel<<<blocks, threads>>>(out, iters, 0.999999f, 1e-7f);
+  cudaEventRecord(e1);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) return set_err(ctx, KR_ERR_CUDA, cudaGetErrorString(e));
+  *tflops = 5.0 * 2.0 * 8.0 * iters * double(blocks) * threads / (ms * 1e-3) / 1e12;
+  return KR_OK;
+}
+
 extern "C" int kr_probe_fp64(kr_ctx* ctx, double* tflops) {
   if (!ctx || !tflops) return set_err(ctx, KR_ERR_ARG, "kr_probe_fp64: NULL argument");
   KR_CUDA(ctx, cudaSetDevice(ctx->device));
