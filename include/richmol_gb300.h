@@ -190,6 +190,10 @@ int kr_batch_korder(kr_batch* b, int32_t* korder, void* stream);
  * with its field set (e.g. cos^2 theta with field [0, 0, 1]); complex64
  * mat-vec, FP64 dot products. Synchronises. */
 int kr_batch_expect(kr_batch* b, kr_op* obs, double* out, void* stream);
+/* y = op x for nvec vectors with the batched complex64 mat-vec (CarTens.vec,
+ * field.py:1145-1245, in single precision): x, y (nvec, dim) complex128
+ * device arrays; uses the batch's basis slot 0 as scratch. Synchronises. */
+int kr_batch_apply(kr_batch* b, kr_op* op, const void* x, void* y, void* stream);
 /* W = op V_0 for every vector (complex64), the batched mat-vec alone
  * (V_0 holds the normalised, phased states after a step). */
 int kr_batch_matvec(kr_batch* b, kr_op* op, void* stream);

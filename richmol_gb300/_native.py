@@ -34,7 +34,7 @@ EXPORTED = [
     "kr_set_field", "kr_matvec", "kr_step", "kr_sync_status", "kr_op_launch_count", "kr_op_work",
     "kr_probe_fp64", "kr_probe_fp32", "kr_step_static", "kr_static_scratch_bytes",
     "kr_batch_create", "kr_batch_destroy", "kr_batch_load", "kr_batch_store", "kr_batch_step",
-    "kr_batch_korder", "kr_batch_expect", "kr_batch_launch_count", "kr_batch_matvec",
+    "kr_batch_korder", "kr_batch_expect", "kr_batch_launch_count", "kr_batch_matvec", "kr_batch_apply",
 ]
 
 
@@ -137,6 +137,8 @@ def lib():
         L.kr_batch_korder.restype = ctypes.c_int
         L.kr_batch_expect.argtypes = [vp, vp, vp, vp]
         L.kr_batch_expect.restype = ctypes.c_int
+        L.kr_batch_apply.argtypes = [vp, vp, vp, vp, vp]
+        L.kr_batch_apply.restype = ctypes.c_int
         L.kr_batch_matvec.argtypes = [vp, vp, vp]
         L.kr_batch_matvec.restype = ctypes.c_int
         L.kr_batch_launch_count.argtypes = [vp]

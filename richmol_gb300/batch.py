@@ -99,5 +99,15 @@ class Ensemble:
         _native.check(_native.lib().kr_batch_expect(self.handle, plan.op, out.ctypes.data, stream_ptr()), self.ctx)
         return out.view(np.complex128)
 
+    def apply(self, H, x):
+        """y = H x for (nvec, dim) complex128 CUDA tensors with the batched
+        complex64 mat-vec (the single-precision CarTens.vec)."""
+        plan = H.device_operator()
+        x = x.contiguous()
+        y = torch.empty_like(x)
+        _native.check(_native.lib().kr_batch_apply(self.handle, plan.op, x.data_ptr(), y.data_ptr(), stream_ptr()),
+                      self.ctx)
+        return y
+
     def launches(self):
         return int(_native.lib().kr_batch_launch_count(self.handle))

@@ -820,6 +820,57 @@ extern "C" int kr_batch_expect(kr_batch* b, kr_op* obs, double* out, void* strea
   return KR_OK;
 }
 
+// (nvec, dim) complex128 <-> [dim][nb] complex64
+__global__ void kb_transpose_in32(const double2* src, float2* X, long long dim, int nvec, int nb) {
+  __shared__ float2 tile[32][33];
+  const long long e0 = blockIdx.x * 32LL;
+  const int v0 = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int v = v0 + r;
+    const long long e = e0 + threadIdx.x;
+    const double2 x = (v < nvec && e < dim) ? src[(long long)v * dim + e] : make_double2(0.0, 0.0);
+    tile[r][threadIdx.x] = make_float2((float)x.x, (float)x.y);
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const long long e = e0 + r;
+    if (e < dim) X[e * nb + v0 + threadIdx.x] = tile[threadIdx.x][r];
+  }
+}
+__global__ void kb_transpose_out32(const float2* Y, double2* dst, long long dim, int nvec, int nb) {
+  __shared__ float2 tile[32][33];
+  const long long e0 = blockIdx.x * 32LL;
+  const int v0 = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const long long e = e0 + r;
+    tile[r][threadIdx.x] = (e < dim) ? Y[e * nb + v0 + threadIdx.x] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int v = v0 + r;
+    const long long e = e0 + threadIdx.x;
+    if (v < nvec && e < dim) {
+      const float2 y = tile[threadIdx.x][r];
+      dst[(long long)v * dim + e] = make_double2(y.x, y.y);
+    }
+  }
+}
+
+extern "C" int kr_batch_apply(kr_batch* b, kr_op* op, const void* x, void* y, void* stream) {
+  if (!b || !op || !x || !y || !op->square || op->dev.dim_out != b->dim)
+    return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_apply: bad argument or basis mismatch");
+  cudaStream_t st = (cudaStream_t)stream;
+  const dim3 grid((unsigned)((b->dim + 31) / 32), b->nb / 32);
+  kb_transpose_in32<<<grid, dim3(32, 8), 0, st>>>((const double2*)x, b->V, b->dim, b->nvec, b->nb);
+  const int rc = launch_matvec(b, op, b->V, b->W, false, st);
+  if (rc) return rc;
+  kb_transpose_out32<<<grid, dim3(32, 8), 0, st>>>(b->W, (double2*)y, b->dim, b->nvec, b->nb);
+  b->launches += 2;
+  KR_CUDA(op->ctx, cudaGetLastError());
+  KR_CUDA(op->ctx, cudaStreamSynchronize(st));
+  return KR_OK;
+}
+
 extern "C" int kr_batch_matvec(kr_batch* b, kr_op* op, void* stream) {
   if (!b || !op || op->dev.dim_out != b->dim || !op->square)
     return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_matvec: operator does not match the batch basis");
