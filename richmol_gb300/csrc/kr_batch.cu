@@ -380,14 +380,19 @@ __global__ void kb_expect_dots(const double2* S, const float2* Y, long long dim,
 
 // ---------------------------------------------------------------------------
 // batched mat-vec, complex64, tiled. One CTA (256 threads = 8 warps) computes
-// a tile of R consecutive output rows of one slab for 32 vectors (lane =
-// vector):
-//   for each term:   T[j, a] = sum_b K[a, b] X[j, b]   for the input rows j of
-//                    the band of the tile (each computed once, kept in shared
-//                    memory), then Y[i, a] += sum_w MF[i, w] T[col(i, w), a]
-// (field.py:1212-1243 orders the same sum as MF (K X^T)^T). K^T, the MF rows
-// and their columns are staged as FP32 in shared memory per term; every thread
-// owns 16 (row, a) outputs across all terms (R * NKP = 128 per CTA).
+// a tile of R = 128 / NKP consecutive output rows of one slab for 32 vectors
+// (lane = vector). Per term:
+//   T[j, a] = sum_b K[a, b] X[j, b]     for the input rows j of the band of
+//             the tile, each computed once and kept in shared memory; the
+//             work goes to the warps in (row, half-row) units
+//   Y[i, a] += sum_w MF[i, w] T[col(i, w), a]
+// (field.py:1212-1243 orders the same sum as MF (K X^T)^T). Every thread owns
+// the outputs of 4 consecutive rows x 4 consecutive k columns (16 complex
+// registers) across all terms. Diagonal M groups (slot w of row i holds column
+// i + d0 + w, detected by kr_op_create) address the band by offset: the T row
+// of (i, w) is i - i0 + w, and each T value loaded serves up to 4 rows. Other
+// groups use the stored columns, the band window taken in chunks of NJ rows.
+// K^T, the MF rows and their columns are staged as FP32 in shared memory.
 // ---------------------------------------------------------------------------
 #define KB_WMAX 16   // ELL width of the M band supported by the batched mat-vec
 
@@ -417,13 +422,28 @@ __device__ __forceinline__ void kacc(float2& t, float kr, float ki, float2 x) {
   }
 }
 
-// T[jj][a] = sum_b K[a, b] X[j, b] for one input row and all a (this thread's
-// vector); X is read in groups of 4 independent loads, the next group issued
-// before the current one is used
-template <int NKP, int KT>
+// y += m * t for a real, imaginary or complex M-band value m
+template <int MT>
+__device__ __forceinline__ void macc(float2& y, float2 m, float2 t) {
+  if (MT == 1) {
+    y.x = fmaf(m.x, t.x, y.x);
+    y.y = fmaf(m.x, t.y, y.y);
+  } else if (MT == 2) {
+    y.x = fmaf(-m.y, t.y, y.x);
+    y.y = fmaf(m.y, t.x, y.y);
+  } else {
+    y.x = fmaf(m.x, t.x, fmaf(-m.y, t.y, y.x));
+    y.y = fmaf(m.x, t.y, fmaf(m.y, t.x, y.y));
+  }
+}
+
+// t[a] = sum_b K[a, b] X[j, b] for AB consecutive k columns a (Ks points at
+// the first; rows of NKP floats) and this thread's vector; X is read in groups
+// of 4 independent loads, the next group issued before the current one is used
+template <int NKP, int AB, int KT>
 __device__ __forceinline__ void kb_trow(const float2* xr, long long nb, int nk2, const float* Ks, float2* t) {
 #pragma unroll
-  for (int a = 0; a < NKP; ++a) t[a] = make_float2(0.f, 0.f);
+  for (int a = 0; a < AB; ++a) t[a] = make_float2(0.f, 0.f);
   float2 xn[4];
 #pragma unroll
   for (int u = 0; u < 4; ++u) xn[u] = (u < nk2) ? xr[(long long)u * nb] : make_float2(0.f, 0.f);
@@ -442,7 +462,7 @@ __device__ __forceinline__ void kb_trow(const float2* xr, long long nb, int nk2,
       const float* kr = Ks + b * NKP;
       const float* ki = Ks + (36 + b) * NKP;
 #pragma unroll
-      for (int a = 0; a < NKP; a += 4) {
+      for (int a = 0; a < AB; a += 4) {
         const float4 r4 = *reinterpret_cast<const float4*>(kr + a);
         float4 i4 = make_float4(0.f, 0.f, 0.f, 0.f);
         if (KT == 0) i4 = *reinterpret_cast<const float4*>(ki + a);
@@ -455,31 +475,102 @@ __device__ __forceinline__ void kb_trow(const float2* xr, long long nb, int nk2,
   }
 }
 
+// T rows jr < nrow for the input rows j0 + jr into Ts[jr]; rows outside the
+// input slab [0, dm2) are zero. (row, half-row) units go round-robin over the
+// 8 warps.
+template <int NKP>
+__device__ __forceinline__ void kb_tstep(const float2* Xs2, long long nb, int nk2, int ktype, const float* Ks,
+                                         float2* Ts, int j0, int nrow, int dm2, int wid, int lane) {
+  constexpr int NH = NKP >= 8 ? 2 : 1;
+  constexpr int AB = NKP / NH;
+  for (int u = wid; u < nrow * NH; u += 8) {
+    const int jr = u / NH, h = u - jr * NH;
+    const int j = j0 + jr;
+    float2 t[AB];
+    if (j >= 0 && j < dm2) {
+      const float2* xr = Xs2 + (long long)j * nk2 * nb;
+      if (ktype == 1) kb_trow<NKP, AB, 1>(xr, nb, nk2, Ks + h * AB, t);
+      else if (ktype == 2) kb_trow<NKP, AB, 2>(xr, nb, nk2, Ks + h * AB, t);
+      else kb_trow<NKP, AB, 0>(xr, nb, nk2, Ks + h * AB, t);
+    } else {
+#pragma unroll
+      for (int a = 0; a < AB; ++a) t[a] = make_float2(0.f, 0.f);
+    }
+    float2* tr = Ts + (jr * NKP + h * AB) * 32 + lane;
+#pragma unroll
+    for (int a = 0; a < AB; ++a) tr[a * 32] = t[a];
+  }
+}
+
+// M step of a diagonal group for tile rows r0 .. r0 + 3 (< nr) and k columns
+// a0 .. a0 + 3: the T row of (row r, slot w) is r + w
+template <int NKP, int MT>
+__device__ __forceinline__ void kb_mdia(float2* y, const float2* Ts, const float2* MFs, int W, int r0, int a0,
+                                        int nr, int lane) {
+  for (int cw = 0; cw < W + 3; ++cw) {
+    float2 t[4];
+    const float2* tr = Ts + ((r0 + cw) * NKP + a0) * 32 + lane;
+#pragma unroll
+    for (int aa = 0; aa < 4; ++aa) t[aa] = tr[aa * 32];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int w = cw - r;
+      if (w >= 0 && w < W && r0 + r < nr) {
+        const float2 m = MFs[(r0 + r) * KB_WMAX + w];
+#pragma unroll
+        for (int aa = 0; aa < 4; ++aa) macc<MT>(y[r * 4 + aa], m, t[aa]);
+      }
+    }
+  }
+}
+
+// M step of an ELL group over one chunk of T rows [jc, jc + nj)
+template <int NKP, int MT>
+__device__ __forceinline__ void kb_mell(float2* y, const float2* Ts, const float2* MFs, const int* Cs, int W, int jc,
+                                        int nj, int r0, int a0, int nr, int lane) {
+  for (int w = 0; w < W; ++w) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      if (r0 + r >= nr) continue;
+      const int c = Cs[(r0 + r) * KB_WMAX + w] - jc;
+      if (c < 0 || c >= nj) continue;
+      const float2 m = MFs[(r0 + r) * KB_WMAX + w];
+      const float2* tr = Ts + (c * NKP + a0) * 32 + lane;
+#pragma unroll
+      for (int aa = 0; aa < 4; ++aa) macc<MT>(y[r * 4 + aa], m, tr[aa * 32]);
+    }
+  }
+}
+
 template <int NKP>
 __device__ void kb_tile(const BatchMV& p, int s1, int i0, int nr, float* smem) {
-  constexpr int R = 128 / NKP;      // rows of the tile
-  constexpr int NJ = R + 4;         // input rows of one band chunk
-  constexpr int QY = 16;            // outputs per thread: warp w owns pairs [16 w, 16 w + 16)
+  constexpr int R = 128 / NKP;            // rows of the tile
+  constexpr int NJ = R + KR_DIAG_MAX - 1; // T rows held: a diagonal band, or one ELL chunk
+  constexpr int NAB = NKP / 4;            // 4-wide k-column blocks
   const DevOp& op = p.op;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const long long nb = p.nb;
   const int v = blockIdx.y * 32 + lane;
+  const int r0 = (wid / NAB) * 4, a0 = (wid % NAB) * 4;  // this thread's outputs
   float2* Ts = reinterpret_cast<float2*>(smem);                 // [NJ][NKP][32]
   float* Ks = smem + 2 * NJ * NKP * 32;                          // [2][36][NKP]
   float2* MFs = reinterpret_cast<float2*>(Ks + 2 * 36 * NKP);   // [R][KB_WMAX]
   int* Cs = reinterpret_cast<int*>(MFs + R * KB_WMAX);           // [R][KB_WMAX]
-  int* meta = Cs + R * KB_WMAX;                                  // jmin, jmax
+  int* meta = Cs + R * KB_WMAX;                                  // ELL band window jmin, jmax
   const int nk1 = __ldg(op.out_dk + s1);
-  float2 y[QY];
+  float2 y[16];
 #pragma unroll
-  for (int q = 0; q < QY; ++q) y[q] = make_float2(0.f, 0.f);
+  for (int q = 0; q < 16; ++q) y[q] = make_float2(0.f, 0.f);
   const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
   for (int term = tb; term < te; ++term) {
     const int s2 = __ldg(op.t_in + term);
     const int kb = __ldg(op.t_k + term);
     const int mfi = __ldg(op.t_mf + term);
     const int nk2 = __ldg(op.in_dk + s2);
+    const int dm2 = __ldg(op.in_dm + s2);
     const int W = __ldg(op.mf_width + mfi);
+    const int d0 = __ldg(op.mf_diag + mfi);
+    const bool dia = d0 != KR_NO_DIAG && W <= KR_DIAG_MAX;
     const int ktype = __ldg(op.k_type + kb);
     const int mtype = __ldcg(op.mf_type + mfi);
     const int kw = (ktype == 0) ? 2 : 1;
@@ -496,18 +587,13 @@ __device__ void kb_tile(const BatchMV& p, int s1, int i0, int nr, float* smem) {
       Ks[(plane * 36 + b) * NKP + a] =
           (a < nk1 && b < nk2) ? __ldg(KT + ((long long)b * nk1 + a) * kw + plane) : 0.f;
     }
-    for (int e = tid; e < R * W; e += blockDim.x) {
+    for (int e = tid; e < nr * W; e += blockDim.x) {
       const int r = e / W, w = e - r * W;
-      if (r < nr) {
-        const long long src = (long long)(i0 + r) * W + w;
-        MFs[r * KB_WMAX + w] = __ldcg(mf + src);
-        Cs[r * KB_WMAX + w] = __ldg(col + src);
-      } else {
-        MFs[r * KB_WMAX + w] = make_float2(0.f, 0.f);
-        Cs[r * KB_WMAX + w] = -1;
-      }
+      const long long src = (long long)(i0 + r) * W + w;
+      MFs[r * KB_WMAX + w] = __ldcg(mf + src);
+      if (!dia) Cs[r * KB_WMAX + w] = __ldg(col + src);
     }
-    if (wid == 0) {
+    if (!dia && wid == 0) {
       int lo = 0x7fffffff, hi = -1;
       for (int e = lane; e < nr * W; e += 32) {
         const int c = __ldg(col + (long long)(i0 + e / W) * W + (e % W));
@@ -525,57 +611,40 @@ __device__ void kb_tile(const BatchMV& p, int s1, int i0, int nr, float* smem) {
       }
     }
     __syncthreads();
-    const int jmin = meta[0], jmax = meta[1];
     const float2* Xs2 = p.X + (long long)__ldg(op.in_off + s2) * nb + v;
-    for (int jc = jmin; jc <= jmax; jc += NJ) {
-      const int nj = min(NJ, jmax - jc + 1);
-      if (jc != jmin) __syncthreads();  // the previous chunk's Y step is done with Ts
-      for (int jj = wid; jj < nj; jj += 8) {
-        float2 t[NKP];
-        const float2* xr = Xs2 + (long long)(jc + jj) * nk2 * nb;
-        if (ktype == 1) kb_trow<NKP, 1>(xr, nb, nk2, Ks, t);
-        else if (ktype == 2) kb_trow<NKP, 2>(xr, nb, nk2, Ks, t);
-        else kb_trow<NKP, 0>(xr, nb, nk2, Ks, t);
-        float2* tr = Ts + jj * NKP * 32 + lane;
-#pragma unroll
-        for (int a = 0; a < NKP; ++a) tr[a * 32] = t[a];
-      }
+    if (dia) {
+      // T rows of the band: input rows i0 + d0 .. i0 + d0 + nr + W - 2
+      kb_tstep<NKP>(Xs2, nb, nk2, ktype, Ks, Ts, i0 + d0, nr + W - 1, dm2, wid, lane);
       __syncthreads();
-      // Y[i, a] += sum_w MF[i, w] T[col, a] for this warp's 16 (i, a) pairs
-      for (int w = 0; w < W; ++w) {
-#pragma unroll
-        for (int q = 0; q < QY; ++q) {
-          const int pq = wid * QY + q;
-          const int i = pq / NKP, a = pq - (pq / NKP) * NKP;
-          const int c = Cs[i * KB_WMAX + w] - jc;
-          if (c < 0 || c >= nj) continue;
-          const float2 m = MFs[i * KB_WMAX + w];
-          const float2 tv = Ts[(c * NKP + a) * 32 + lane];
-          if (mtype == 1) {
-            y[q].x = fmaf(m.x, tv.x, y[q].x);
-            y[q].y = fmaf(m.x, tv.y, y[q].y);
-          } else if (mtype == 2) {
-            y[q].x = fmaf(-m.y, tv.y, y[q].x);
-            y[q].y = fmaf(m.y, tv.x, y[q].y);
-          } else {
-            y[q].x = fmaf(m.x, tv.x, fmaf(-m.y, tv.y, y[q].x));
-            y[q].y = fmaf(m.x, tv.y, fmaf(m.y, tv.x, y[q].y));
-          }
-        }
+      if (mtype == 1) kb_mdia<NKP, 1>(y, Ts, MFs, W, r0, a0, nr, lane);
+      else if (mtype == 2) kb_mdia<NKP, 2>(y, Ts, MFs, W, r0, a0, nr, lane);
+      else kb_mdia<NKP, 0>(y, Ts, MFs, W, r0, a0, nr, lane);
+    } else {
+      const int jmin = meta[0], jmax = meta[1];
+      for (int jc = jmin; jc <= jmax; jc += NJ) {
+        const int nj = min(NJ, jmax - jc + 1);
+        if (jc != jmin) __syncthreads();  // the previous chunk's M step is done with Ts
+        kb_tstep<NKP>(Xs2, nb, nk2, ktype, Ks, Ts, jc, nj, dm2, wid, lane);
+        __syncthreads();
+        if (mtype == 1) kb_mell<NKP, 1>(y, Ts, MFs, Cs, W, jc, nj, r0, a0, nr, lane);
+        else if (mtype == 2) kb_mell<NKP, 2>(y, Ts, MFs, Cs, W, jc, nj, r0, a0, nr, lane);
+        else kb_mell<NKP, 0>(y, Ts, MFs, Cs, W, jc, nj, r0, a0, nr, lane);
       }
     }
   }
   float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * nk1) * nb + v;
 #pragma unroll
-  for (int q = 0; q < QY; ++q) {
-    const int pq = wid * QY + q;
-    const int i = pq / NKP, a = pq - (pq / NKP) * NKP;
-    if (i < nr && a < nk1) Y[((long long)i * nk1 + a) * nb] = y[q];
+  for (int r = 0; r < 4; ++r) {
+#pragma unroll
+    for (int aa = 0; aa < 4; ++aa) {
+      const int i = r0 + r, a = a0 + aa;
+      if (i < nr && a < nk1) Y[((long long)i * nk1 + a) * nb] = y[r * 4 + aa];
+    }
   }
 }
 
 __global__ void __launch_bounds__(256, 2) kb_matvec(BatchMV p) {
-  extern __shared__ float kb_smem[];
+  extern __shared__ __align__(16) float kb_smem[];
   const int task = blockIdx.x;
   if (p.grp_active && !p.grp_active[blockIdx.y]) return;
   const int s1 = __ldg(p.task_slab + task);
@@ -592,7 +661,7 @@ __global__ void __launch_bounds__(256, 2) kb_matvec(BatchMV p) {
 static size_t kb_matvec_smem() {
   size_t best = 0;
   for (int nkp : {4, 8, 16, 32}) {
-    const int R = 128 / nkp, NJ = R + 4;
+    const int R = 128 / nkp, NJ = R + KR_DIAG_MAX - 1;
     size_t b = sizeof(float2) * NJ * nkp * 32 + sizeof(float) * 2 * 36 * nkp + sizeof(float2) * R * KB_WMAX +
                sizeof(int) * (R * KB_WMAX + 2);
     best = std::max(best, b);

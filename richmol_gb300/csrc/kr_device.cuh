@@ -36,6 +36,9 @@ __device__ __forceinline__ double2 ldcg2(const double2* p) { return __ldcg(p); }
 // ---------------------------------------------------------------------------
 // operator tables on the device
 // ---------------------------------------------------------------------------
+#define KR_NO_DIAG (-2147483647 - 1)  // MF instance without diagonal slot order
+#define KR_DIAG_MAX 8                  // widest diagonal band the batched mat-vec takes by offset
+
 struct DevOp {
   int nslab_out, nslab_in;
   const int* out_dm; const int* out_dk; const long long* out_off;
@@ -46,6 +49,7 @@ struct DevOp {
   const float* k_f32;   // FP32 copy of k_data (same offsets), for the batched complex64 path
   // MF instances (ELL): values at mf_val + mf_off[i], columns at m_col + mf_col_off[i]
   const long long* mf_off; const long long* mf_col_off; const int* mf_width;
+  const int* mf_diag;   // per MF instance: first diagonal d0 if slot w of row i holds column i + d0 + w, else KR_NO_DIAG
   const int* m_col; double2* mf_val;
   float2* mf_f32;       // FP32 copy of mf_val, written with it by the field kernel
   // terms grouped by output slab

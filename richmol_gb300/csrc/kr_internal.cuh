@@ -58,6 +58,7 @@ struct kr_op {
   bool square = false;
   int npart = 0;
   int nmf = 0;
+  int ndiag_groups = 0;  // M groups in diagonal slot order
   long long launches = 0;
   double fma_per_matvec = 0, bytes_per_matvec = 0;
   // step scratch

@@ -655,6 +655,49 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
     mf_col_off[i] = d->m_col_off[g];
     mf_width[i] = d->m_width[g];
   }
+  // ---- diagonal slot order of the M groups --------------------------------
+  // A group is diagonal when slot w of row i holds column i + d0 + w wherever
+  // that column lies in the input slab, and zero values in every Cartesian
+  // component where it does not (the stored column is then any in-slab one).
+  // The batched mat-vec addresses such bands by offset.
+  std::vector<int> group_diag(d->nm, KR_NO_DIAG);
+  {
+    std::vector<int> gcols(d->nm, -1);  // input slab rows of the terms of each group (-2: they differ)
+    for (int t = 0; t < d->nterm; ++t) {
+      const int g = d->mf_group[d->t_mf[t]], c = d->in_dm[d->t_in[t]];
+      gcols[g] = (gcols[g] == -1 || gcols[g] == c) ? c : -2;
+    }
+    for (int g = 0; g < d->nm; ++g) {
+      const int rows = d->m_rows[g], W = d->m_width[g], ncols = gcols[g];
+      if (ncols <= 0 || W < 1 || W > KR_DIAG_MAX) continue;
+      const int* col = d->m_col + d->m_col_off[g];
+      const long long ne = (long long)rows * W;
+      const int mid = rows / 2;
+      for (int w0 = 0; w0 < W && group_diag[g] == KR_NO_DIAG; ++w0) {
+        const int cand = col[(long long)mid * W + w0] - mid - w0;
+        bool ok = true;
+        for (int i = 0; i < rows && ok; ++i)
+          for (int w = 0; w < W && ok; ++w) {
+            const long long e = (long long)i * W + w;
+            const long long c = (long long)i + cand + w;
+            if (c >= 0 && c < ncols) {
+              ok = col[e] == c;
+            } else {
+              for (int k = 0; k < d->m_ncart[g] && ok; ++k) {
+                const double* v = d->m_val + 2 * (d->m_val_off[g] + k * ne + e);
+                ok = v[0] == 0.0 && v[1] == 0.0;
+              }
+            }
+          }
+        if (ok) group_diag[g] = cand;
+      }
+    }
+  }
+  std::vector<int> mf_diag(d->nmf);
+  for (int i = 0; i < d->nmf; ++i) mf_diag[i] = group_diag[d->mf_group[i]];
+  op->ndiag_groups = 0;
+  for (int g = 0; g < d->nm; ++g) op->ndiag_groups += group_diag[g] != KR_NO_DIAG;
+
   const long long nent = inst_ptr[d->nmf];
   std::vector<int> ent_inst(nent);
   for (int i = 0; i < d->nmf; ++i)
@@ -793,6 +836,7 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   UP((const long long*)inst_ptr.data(), d->nmf, &p_l); D.mf_off = p_l;
   UP((const long long*)mf_col_off.data(), d->nmf, &p_l); D.mf_col_off = p_l;
   UP(mf_width.data(), d->nmf, &p_i); D.mf_width = p_i;
+  UP(mf_diag.data(), d->nmf, &p_i); D.mf_diag = p_i;
   UP(d->m_col, d->m_col_len, &p_i); D.m_col = p_i;
   double2* p_c;
   UP((const double2*)nullptr, nent, &p_c); D.mf_val = p_c;

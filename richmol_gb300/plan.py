@@ -36,9 +36,19 @@ def _ktype(K):
     return _native.KR_K_COMPLEX, np.ascontiguousarray(K).view(np.float64)
 
 
+DIAG_MAX = 8  # widest band stored in diagonal slot order (the batched mat-vec's limit)
+
+
 def _ell(mats, nrows, ncols):
     """Union-pattern ELL of a list of sparse matrices with equal shapes.
-    Returns (width, col[nrows*width] int32, val[ncart, nrows*width] complex)."""
+    Returns (width, col[nrows*width] int32, val[ncart, nrows*width] complex).
+
+    A band of at most DIAG_MAX diagonals (d0 .. d0 + width - 1) is stored in
+    diagonal slot order: slot w of row i holds column i + d0 + w, and where
+    that column falls outside the matrix, the nearest column with value 0.
+    Otherwise the entries of a row are packed by column, the padding slots
+    repeating the last column of the row (or of the nearest non-empty row),
+    so that a row's columns span only its own band."""
     coos = [m.tocoo() for m in mats]
     rows = np.concatenate([c.row for c in coos]).astype(np.int64) if coos else np.zeros(0, np.int64)
     cols = np.concatenate([c.col for c in coos]).astype(np.int64) if coos else np.zeros(0, np.int64)
@@ -46,11 +56,27 @@ def _ell(mats, nrows, ncols):
     urow, ucol = keys // ncols, keys % ncols
     counts = np.bincount(urow, minlength=nrows)
     width = int(counts.max()) if len(keys) else 0
-    start = np.concatenate([[0], np.cumsum(counts)[:-1]])
-    pos = np.arange(len(keys)) - start[urow]
-    slot = urow * width + pos
-    col = np.zeros(nrows * width, dtype=np.int32)
-    col[slot] = ucol
+    if width == 0:
+        return 0, np.zeros(0, np.int32), np.zeros((len(mats), 0), np.complex128)
+    off = ucol - urow
+    d0 = int(off.min())
+    wd = int(off.max()) - d0 + 1
+    if wd <= DIAG_MAX and wd <= 2 * width:
+        width = wd
+        slot = urow * width + (off - d0)
+        col = np.clip(np.arange(nrows)[:, None] + d0 + np.arange(width)[None, :], 0, ncols - 1)
+        col = np.ascontiguousarray(col.reshape(-1), dtype=np.int32)
+    else:
+        start = np.concatenate([[0], np.cumsum(counts)[:-1]])
+        pos = np.arange(len(keys)) - start[urow]
+        slot = urow * width + pos
+        last = np.full(nrows, -1, np.int64)
+        last[urow] = ucol  # keys are sorted: the last write per row is its largest column
+        src = np.where(last >= 0, np.arange(nrows), -1)
+        src = np.maximum.accumulate(src)
+        src[src < 0] = int(np.flatnonzero(last >= 0)[0])
+        col = np.repeat(last[src], width).astype(np.int32)
+        col[slot] = ucol
     val = np.zeros((len(mats), nrows * width), dtype=np.complex128)
     for ci, c in enumerate(coos):
         idx = np.searchsorted(keys, c.row.astype(np.int64) * ncols + c.col)

@@ -110,3 +110,45 @@ def test_batched_matvec_matches_fp64(jmax, nvec):
     plan.matvec(x, y64)
     err = (y32 - y64).abs().max().item() / y64.abs().max().item()
     assert err < 2e-6, err
+
+
+def _scrambled(T, seed):
+    """The tensor T with the columns of every M block permuted: the same
+    numbers of entries per row on a scattered (non-banded) pattern, which the
+    batched mat-vec takes through stored columns instead of diagonal offsets."""
+    from scipy.sparse import csr_matrix
+    from richmol_gb300 import CarTens
+    src = T._parts[0].src
+    rng = np.random.default_rng(seed)
+    perms, mmat = {}, {}
+    for JJ, mJ in src.mmat.items():
+        for ss, mS in mJ.items():
+            for irrep, mI in mS.items():
+                for cart, m in mI.items():
+                    n = m.shape[1]
+                    p = perms.setdefault(n, rng.permutation(n))
+                    d = m.toarray() if hasattr(m, "toarray") else np.asarray(m)
+                    mmat.setdefault(JJ, {}).setdefault(ss, {}).setdefault(irrep, {})[cart] = csr_matrix(d[:, p])
+    basis = {k: getattr(src, k) for k in ("Jlist1", "Jlist2", "symlist1", "symlist2",
+                                          "dim_m1", "dim_m2", "dim_k1", "dim_k2")}
+    return CarTens.from_factors(basis, src.kmat, mmat, src.rank, src.carts)
+
+
+def test_batched_matvec_scattered_m_matches_fp64():
+    from richmol_gb300 import TDSE, workloads
+    from richmol_gb300.batch import Ensemble
+    from richmol_gb300.convert_units import AUpol_x_Vm_to_invcm
+    wl = workloads.asym_top(Jmax=12)
+    H = _scrambled(wl.pol, 5) * (-0.5 * AUpol_x_Vm_to_invcm())
+    H.field(wl.field(1.0))
+    td = TDSE(t_end=1.0, dt=0.01)
+    td.time_grid()
+    nvec = 64
+    ens = Ensemble(td, wl.h0, nvec)
+    g = torch.Generator(device="cuda").manual_seed(11)
+    x = torch.randn((nvec, wl.dim), dtype=torch.complex128, device="cuda", generator=g)
+    y32 = ens.apply(H, x)
+    y64 = torch.empty_like(x)
+    H.device_operator().matvec(x, y64)
+    err = (y32 - y64).abs().max().item() / y64.abs().max().item()
+    assert err < 2e-6, err
