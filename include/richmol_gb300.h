@@ -215,6 +215,10 @@ int kr_op_work(const kr_op* op, double* fma_per_matvec, double* bytes_per_matvec
 int kr_probe_fp64(kr_ctx* ctx, double* tflops);
 /* The same for FP32 fused multiply-adds (denominator of the complex64 mat-vec). */
 int kr_probe_fp32(kr_ctx* ctx, double* tflops);
+/* Tensor-core probe (no counterpart in the reference): D = A B^T with A
+ * 128 x 16, B 16 x 16, D 128 x 16, row-major FP32 host arrays read as TF32, by
+ * one tcgen05.mma tile; checks the MMA building block of the batched mat-vec. */
+int kr_probe_mma(kr_ctx* ctx, const float* a, const float* b, float* d);
 
 #ifdef __cplusplus
 }

@@ -32,7 +32,7 @@ FIELD_COEF_BYTES = 8 + KR_MAXPART * KR_MAXCART * 16 + KR_MAXPART * 16 + KR_MAXPA
 EXPORTED = [
     "kr_ctx_create", "kr_ctx_destroy", "kr_last_error", "kr_op_create", "kr_op_destroy",
     "kr_set_field", "kr_matvec", "kr_step", "kr_sync_status", "kr_op_launch_count", "kr_op_work",
-    "kr_probe_fp64", "kr_probe_fp32", "kr_step_static", "kr_static_scratch_bytes",
+    "kr_probe_fp64", "kr_probe_fp32", "kr_probe_mma", "kr_step_static", "kr_static_scratch_bytes",
     "kr_batch_create", "kr_batch_destroy", "kr_batch_load", "kr_batch_store", "kr_batch_step",
     "kr_batch_korder", "kr_batch_expect", "kr_batch_launch_count", "kr_batch_matvec", "kr_batch_apply",
 ]
@@ -145,6 +145,8 @@ def lib():
         L.kr_batch_launch_count.restype = i64
         L.kr_probe_fp32.argtypes = [vp, ctypes.POINTER(dbl)]
         L.kr_probe_fp32.restype = ctypes.c_int
+        L.kr_probe_mma.argtypes = [vp, vp, vp, vp]
+        L.kr_probe_mma.restype = ctypes.c_int
         L.kr_probe_fp64.argtypes = [vp, ctypes.POINTER(dbl)]
         L.kr_probe_fp64.restype = ctypes.c_int
         _lib = L

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "kr_internal.cuh"
+#include "kr_tc.cuh"
 
 #define KB_MV_THREADS 128      // vectors per mat-vec block
 #define KB_RED_CHUNKS 256      // element chunks of the per-vector reductions
@@ -947,3 +948,67 @@ extern "C" int kr_batch_matvec(kr_batch* b, kr_op* op, void* stream) {
 }
 
 extern "C" int64_t kr_batch_launch_count(const kr_batch* b) { return b ? b->launches : -1; }
+
+// ---------------------------------------------------------------------------
+// tensor-core probe: D (128 x 16) = A (128 x 16) B^T (B: 16 x 16), A, B, D
+// row-major FP32 (read as TF32), one CTA: the MMA building block of the
+// batched mat-vec (operand staging, descriptors, TMEM, commit, TMEM load)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) kb_mma_probe(const float* A, const float* B, float* D, int* err) {
+  __shared__ __align__(128) float sa[128 * 16];
+  __shared__ __align__(128) float sb[16 * 16];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tbase;
+  const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+  for (int e = tid; e < 128 * 16; e += 128) sa[tc_kmajor_off(e >> 4, e & 15, 16) >> 2] = A[e];
+  for (int e = tid; e < 16 * 16; e += 128) sb[tc_kmajor_off(e >> 4, e & 15, 16) >> 2] = B[e];
+  if (wid == 0) tc_alloc(&tbase, 32);
+  if (tid == 0) tc_mbar_init(&bar, 1);
+  tc_fence_proxy();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t taddr = tbase;
+  if (tid == 0) {
+    const uint32_t idesc = tc_idesc_tf32(128, 16);
+    for (int s = 0; s < 2; ++s)  // K = 16 in two steps of 8
+      tc_mma_tf32(taddr, tc_desc(tc_smem_u32(sa) + 256u * s, 128u, 512u),
+                  tc_desc(tc_smem_u32(sb) + 256u * s, 128u, 512u), idesc, (uint32_t)s);
+    tc_commit(&bar);
+  }
+  if (!tc_mbar_wait(&bar, 0) && lane == 0) atomicExch(err, KR_ERR_TIMEOUT);
+  tc_fence_after();
+  float v[16];
+  tc_ld16(taddr + ((uint32_t)(32 * wid) << 16), v);
+#pragma unroll
+  for (int j = 0; j < 16; ++j) D[(32 * wid + lane) * 16 + j] = v[j];
+  tc_fence_before();
+  __syncthreads();
+  if (wid == 0) tc_dealloc(taddr, 32);
+}
+
+extern "C" int kr_probe_mma(kr_ctx* ctx, const float* a, const float* b, float* d) {
+  if (!ctx || !a || !b || !d) return set_err(ctx, KR_ERR_ARG, "kr_probe_mma: NULL argument");
+  KR_CUDA(ctx, cudaSetDevice(ctx->device));
+  const size_t na = 128 * 16, nbb = 16 * 16, nd = 128 * 16;
+  char* buf = nullptr;
+  KR_CUDA(ctx, cudaMalloc(&buf, sizeof(float) * (na + nbb + nd) + 16));
+  float* dA = reinterpret_cast<float*>(buf);
+  float* dB = dA + na;
+  float* dD = dB + nbb;
+  int* derr = reinterpret_cast<int*>(dD + nd);
+  int herr = 0;
+  cudaError_t e = cudaMemcpy(dA, a, sizeof(float) * na, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dB, b, sizeof(float) * nbb, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(derr, 0, sizeof(int));
+  if (e == cudaSuccess) {
+    kb_mma_probe<<<1, 128>>>(dA, dB, dD, derr);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(d, dD, sizeof(float) * nd, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(buf);
+  if (e != cudaSuccess) return set_err(ctx, KR_ERR_CUDA, std::string("kr_probe_mma: ") + cudaGetErrorString(e));
+  if (herr) return set_err(ctx, herr, "kr_probe_mma: the MMA completion wait gave up");
+  return KR_OK;
+}
