@@ -190,6 +190,12 @@ int kr_batch_korder(kr_batch* b, int32_t* korder, void* stream);
  * with its field set (e.g. cos^2 theta with field [0, 0, 1]); complex64
  * mat-vec, FP64 dot products. Synchronises. */
 int kr_batch_expect(kr_batch* b, kr_op* obs, double* out, void* stream);
+/* Mat-vec kinds of a batch: KR_MATVEC_TENSOR (default) contracts the K
+ * factors on the tensor cores (tcgen05, TF32 with split operands: about 2^-21
+ * relative per product, FP32 accumulation); KR_MATVEC_FP32 runs every
+ * product as an FP32 FMA. No counterpart in the reference (FP64 only). */
+enum { KR_MATVEC_TENSOR = 0, KR_MATVEC_FP32 = 1 };
+int kr_batch_set_matvec(kr_batch* b, int32_t kind);
 /* y = op x for nvec vectors with the batched complex64 mat-vec (CarTens.vec,
  * field.py:1145-1245, in single precision): x, y (nvec, dim) complex128
  * device arrays; uses the batch's basis slot 0 as scratch. Synchronises. */

@@ -24,6 +24,7 @@ KR_K_COMPLEX, KR_K_REAL, KR_K_IMAG = 0, 1, 2
 KR_MAXCART = 9
 KR_MAXPART = 16
 KR_STEP_SKIP_KRYLOV = 1
+KR_MATVEC_TENSOR, KR_MATVEC_FP32 = 0, 1
 # bytes of per-step field input that travel host -> device (the field
 # coefficients, scales and thresholds of kr_set_field, passed as kernel
 # parameters): int npart (padded to 8) + 16 x 9 complex + 16 complex + 16 double
@@ -34,7 +35,7 @@ EXPORTED = [
     "kr_set_field", "kr_matvec", "kr_step", "kr_sync_status", "kr_op_launch_count", "kr_op_work",
     "kr_probe_fp64", "kr_probe_fp32", "kr_probe_mma", "kr_step_static", "kr_static_scratch_bytes",
     "kr_batch_create", "kr_batch_destroy", "kr_batch_load", "kr_batch_store", "kr_batch_step",
-    "kr_batch_korder", "kr_batch_expect", "kr_batch_launch_count", "kr_batch_matvec", "kr_batch_apply",
+    "kr_batch_korder", "kr_batch_expect", "kr_batch_launch_count", "kr_batch_matvec", "kr_batch_apply", "kr_batch_set_matvec",
 ]
 
 
@@ -137,6 +138,8 @@ def lib():
         L.kr_batch_korder.restype = ctypes.c_int
         L.kr_batch_expect.argtypes = [vp, vp, vp, vp]
         L.kr_batch_expect.restype = ctypes.c_int
+        L.kr_batch_set_matvec.argtypes = [vp, i32]
+        L.kr_batch_set_matvec.restype = ctypes.c_int
         L.kr_batch_apply.argtypes = [vp, vp, vp, vp, vp]
         L.kr_batch_apply.restype = ctypes.c_int
         L.kr_batch_matvec.argtypes = [vp, vp, vp]

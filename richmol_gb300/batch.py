@@ -29,9 +29,12 @@ class Ensemble:
         nvec : int
         tol : float                 per-vector error tolerance of the Krylov step
         mmax : int                  maximum Krylov order (<= 31)
+        matvec : str                "tensor" (default): K contractions on the tensor cores
+                                    as split-TF32 MMAs (about 2^-21 relative per product);
+                                    "fp32": every product an FP32 FMA
     """
 
-    def __init__(self, tdse, H0, nvec, tol=1e-8, mmax=20, template=None):
+    def __init__(self, tdse, H0, nvec, tol=1e-8, mmax=20, template=None, matvec="tensor"):
         self.tdse = tdse
         self.H0 = H0
         self.nvec = int(nvec)
@@ -44,6 +47,11 @@ class Ensemble:
         h = ctypes.c_void_p()
         _native.check(_native.lib().kr_batch_create(self._plan0.op, self.nvec, self.mmax, ctypes.byref(h)), self.ctx)
         self.handle = h
+        kinds = {"tensor": _native.KR_MATVEC_TENSOR, "fp32": _native.KR_MATVEC_FP32}
+        if matvec not in kinds:
+            raise ValueError(f"matvec must be one of {sorted(kinds)}")
+        self.matvec = matvec
+        _native.check(_native.lib().kr_batch_set_matvec(h, kinds[matvec]), self.ctx)
         self.phase = None
         self.last_kmax = 0
 

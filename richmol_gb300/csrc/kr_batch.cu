@@ -5,10 +5,11 @@
 // the FP64 Lanczos of richmol/tdse.py:379-382 / 417-486. Here all vectors move
 // together, each with its own Krylov order:
 //   * layout: every vector-valued array is vector-minor, [dim][nb] (nb = nvec
-//     rounded up to 32), so a thread owns one vector and the factors K, MF are
+//     rounded up to 128), so a thread owns one vector and the factors K, MF are
 //     the same for all threads of a block (broadcast reads);
-//   * mat-vec in complex64 with FP32 accumulation (the Kronecker contraction of
-//     field.py:1212-1243, term by term);
+//   * mat-vec in complex64 (the Kronecker contraction of field.py:1212-1243,
+//     term by term): the K contraction on the tensor cores as split-TF32 MMAs,
+//     or every product as an FP32 FMA (kr_batch_set_matvec);
 //   * Krylov basis in complex64, full classical Gram-Schmidt orthogonalisation
 //     against every basis vector, dot products accumulated in FP64 across chunks;
 //   * FP64 per-vector scalars: alpha, beta, the tridiagonal exponential
@@ -49,12 +50,13 @@ struct kr_batch {
   int* grp_active = nullptr; // [nb / KB_MV_THREADS rounded up]
   double* err = nullptr;     // [nb]
   double2* part = nullptr;   // [KB_RED_CHUNKS][mmax + 2][nb] partial sums
-  int* counts = nullptr;     // [2]: active vectors, vectors that hit mmax
+  int* counts = nullptr;     // [3]: active vectors, vectors that hit mmax, mat-vec error word
   // mat-vec tile table
   int ntask = 0;
   int* task_slab = nullptr;
   int* task_i0 = nullptr;
   int* task_nr = nullptr;
+  int mv_kind = KR_MATVEC_TENSOR;
   long long launches = 0;
 };
 
@@ -670,6 +672,416 @@ static size_t kb_matvec_smem() {
   return best;
 }
 
+// ---------------------------------------------------------------------------
+// batched mat-vec on the tensor cores. One CTA (256 threads = 8 warps) computes
+// a tile of R consecutive output rows of one slab, all its k columns, for 128
+// vectors. Per term:
+//   Z[i][b][v]  = sum_w MF[i, w] X[col(i, w)][b][v]      SIMT, FP32 registers
+//   Y[i][a][v] += sum_b K[a, b] Z[i][b][v]               tcgen05.mma
+// (field.py:1212-1243 orders the same sum as MF (K X^T)^T). The K contraction
+// runs as 128 x NP x 8 TF32 MMAs with the vectors as the M dimension: the real
+// and imaginary parts of Z_i, each split hi + lo (3xTF32: hi*hi + hi*lo +
+// lo*hi), form the A operands; K^T, split likewise, the B operands; the real
+// and imaginary parts of Y_i accumulate in TMEM over all terms of the slab.
+// KP = n_k2 padded to 8 (largest over the slab's terms) is the MMA K extent,
+// R = 64 / KP, NP = n_k1 padded to 16 the MMA N. The SIMT part of term t + 1
+// (X loads and M-band FMAs) runs while the MMAs of term t execute; only the
+// A-tile stores wait for them.
+// Threads: warp w owns vectors 32 (w % 4) .. + 31 (= TMEM lanes) and input k
+// columns [KP/2 (w / 4), KP/2 (w / 4 + 1)).
+// ---------------------------------------------------------------------------
+struct BatchTC {
+  DevOp op;
+  const float2* X;
+  float2* Y;
+  int nb;
+  const int* task;        // [4][ntask]: slab, first row, rows, KP
+  int ntask;
+  const int* grp_active;  // per 32-vector group: any vector active (null: all)
+  int* err;
+};
+
+constexpr int TC_ABYTES = 128 * 1024;       // A tiles: R rows x 4 parts x 128 x KP FP32 (R KP = 64)
+constexpr int TC_BPART = 32 * 32 * 4;       // one B part: NP x KP FP32 at most
+constexpr int TC_BBYTES = 6 * TC_BPART;     // one B buffer: K_re, K_im, -K_im, each hi and lo
+constexpr int TC_MFBYTES = 2 * 8 * KB_WMAX * 8;
+constexpr int TC_CSBYTES = 2 * 8 * KB_WMAX * 4;
+constexpr int TC_SMEM = TC_ABYTES + 2 * TC_BBYTES + TC_MFBYTES + TC_CSBYTES + 64;
+
+// X window of one term in registers: input rows j0 + c (c < RP) for this
+// thread's vector and KP/2 input columns; RP * KP/2 = 16 loads issued back to
+// back (rows outside [0, dm2) and columns beyond n_k2 read as zero)
+template <int KP>
+struct KbtWin {
+  static constexpr int BH = KP / 2, RP = 32 / KP;
+  float2 x[RP][BH];
+  __device__ __forceinline__ void load(const float2* Xs2, long long nb, int nk2, int dm2, int j0, int nrow, int b0) {
+#pragma unroll
+    for (int c = 0; c < RP; ++c) {
+      const int j = j0 + c;
+      const bool rin = c < nrow && j >= 0 && j < dm2;
+      const float2* xr = Xs2 + (long long)j * nk2 * nb;
+#pragma unroll
+      for (int q = 0; q < BH; ++q)
+        x[c][q] = (rin && b0 + q < nk2) ? __ldg(xr + (long long)(b0 + q) * nb) : make_float2(0.f, 0.f);
+    }
+  }
+};
+
+// M step of a diagonal term for window rows cw0 .. cw0 + RP - 1 held in xw:
+// output row r takes slot w = cw - r
+template <int KP, int MT>
+__device__ __forceinline__ void kbt_mdia(float2 (&z)[64 / KP][KP / 2], const KbtWin<KP>& xw, int cw0, int nr, int W,
+                                         const float2* MFs) {
+  constexpr int R = 64 / KP, BH = KP / 2, RP = 32 / KP;
+#pragma unroll
+  for (int c = 0; c < RP; ++c) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int w = cw0 + c - r;
+      if (w >= 0 && w < W && r < nr) {
+        const float2 m = MFs[r * KB_WMAX + w];
+#pragma unroll
+        for (int q = 0; q < BH; ++q) macc<MT>(z[r][q], m, xw.x[c][q]);
+      }
+    }
+  }
+}
+
+// M step of a term with stored columns (ELL), one input row per slot
+template <int KP, int MT>
+__device__ __forceinline__ void kbt_mell(float2 (&z)[64 / KP][KP / 2], const float2* Xs2, long long nb, int nk2,
+                                         int nr, int W, int b0, const float2* MFs, const int* Cs) {
+  constexpr int R = 64 / KP, BH = KP / 2;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    if (r >= nr) continue;
+    for (int w = 0; w < W; ++w) {
+      const float2* xr = Xs2 + (long long)Cs[r * KB_WMAX + w] * nk2 * nb;
+      const float2 m = MFs[r * KB_WMAX + w];
+      float2 x[BH];
+#pragma unroll
+      for (int q = 0; q < BH; ++q) x[q] = (b0 + q < nk2) ? __ldg(xr + (long long)(b0 + q) * nb) : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int q = 0; q < BH; ++q) macc<MT>(z[r][q], m, x[q]);
+    }
+  }
+}
+
+template <int KP, int MT>
+__device__ __forceinline__ void kbt_mstep(float2 (&z)[64 / KP][KP / 2], KbtWin<KP>& xw, bool loaded,
+                                          const float2* Xs2, long long nb, int nk2, int dm2, int i0, int nr, int d0,
+                                          int W, int b0, const float2* MFs, const int* Cs, bool dia) {
+  constexpr int RP = 32 / KP;
+  if (dia) {
+    const int nwin = nr + W - 1;
+    for (int cw0 = 0; cw0 < nwin; cw0 += RP) {
+      if (cw0 > 0 || !loaded) xw.load(Xs2, nb, nk2, dm2, i0 + d0 + cw0, nwin - cw0, b0);
+      kbt_mdia<KP, MT>(z, xw, cw0, nr, W, MFs);
+    }
+  } else {
+    kbt_mell<KP, MT>(z, Xs2, nb, nk2, nr, W, b0, MFs, Cs);
+  }
+}
+
+// one term of a tensor-core tile: its tables and shared-memory staging
+struct KbtTerm {
+  int s2, nk2, dm2, W, d0, ktype, mtype;
+  bool dia, ok;
+  const float* KT;
+  const int* col;
+  const float2* mf;
+  const float2* Xs2;
+};
+
+__device__ __forceinline__ KbtTerm kbt_term(const DevOp& op, const BatchTC& p, int term, int KP, int v, long long nb) {
+  KbtTerm t;
+  t.s2 = __ldg(op.t_in + term);
+  const int kb = __ldg(op.t_k + term);
+  const int mfi = __ldg(op.t_mf + term);
+  t.nk2 = __ldg(op.in_dk + t.s2);
+  t.dm2 = __ldg(op.in_dm + t.s2);
+  t.W = __ldg(op.mf_width + mfi);
+  t.d0 = __ldg(op.mf_diag + mfi);
+  t.dia = t.d0 != KR_NO_DIAG && t.W <= KR_DIAG_MAX;
+  t.ktype = __ldg(op.k_type + kb);
+  t.mtype = __ldcg(op.mf_type + mfi);
+  t.ok = t.nk2 <= KP && t.W <= KB_WMAX;
+  t.KT = op.k_f32 + __ldg(op.k_off + kb);
+  t.col = op.m_col + __ldg(op.mf_col_off + mfi);
+  t.mf = op.mf_f32 + __ldg(op.mf_off + mfi);
+  t.Xs2 = p.X + (long long)__ldg(op.in_off + t.s2) * nb + v;
+  return t;
+}
+
+// B operands of a term: K^T (b, a) -> row a, column b; parts K_re, K_im, -K_im,
+// each hi and lo; zero outside n_k1 x n_k2. MF rows (and ELL columns).
+template <int KP>
+__device__ __forceinline__ void kbt_stage(const KbtTerm& t, int nk1, int NP, int i0, int nr, float* Bt, float2* MFs,
+                                          int* Cs, int tid) {
+  for (int e = tid; e < NP * KP; e += 256) {  // producers only
+    const int a = e / KP, b = e - (e / KP) * KP;
+    float kr = 0.f, ki = 0.f;
+    if (a < nk1 && b < t.nk2) {
+      if (t.ktype == 0) {
+        kr = __ldg(t.KT + ((long long)b * nk1 + a) * 2);
+        ki = __ldg(t.KT + ((long long)b * nk1 + a) * 2 + 1);
+      } else if (t.ktype == 1) {
+        kr = __ldg(t.KT + (long long)b * nk1 + a);
+      } else {
+        ki = __ldg(t.KT + (long long)b * nk1 + a);
+      }
+    }
+    const uint32_t o = tc_kmajor_off(a, b, KP) >> 2;
+    const float krh = tc_tf32(kr), kih = tc_tf32(ki);
+    Bt[0 * (TC_BPART / 4) + o] = krh;
+    Bt[1 * (TC_BPART / 4) + o] = kr - krh;
+    Bt[2 * (TC_BPART / 4) + o] = kih;
+    Bt[3 * (TC_BPART / 4) + o] = ki - kih;
+    Bt[4 * (TC_BPART / 4) + o] = -kih;
+    Bt[5 * (TC_BPART / 4) + o] = -(ki - kih);
+  }
+  const int W = t.W;
+  for (int e = tid; e < nr * W; e += 256) {
+    const int r = e / W, w = e - (e / W) * W;
+    const long long src = (long long)(i0 + r) * W + w;
+    MFs[r * KB_WMAX + w] = __ldcg(t.mf + src);
+    if (!t.dia) Cs[r * KB_WMAX + w] = __ldg(t.col + src);
+  }
+}
+
+template <int KP>
+__device__ __forceinline__ void kbt_zstep(float2 (&z)[64 / KP][KP / 2], KbtWin<KP>& xw, const KbtTerm& t,
+                                          long long nb, int i0, int nr, int b0, const float2* MFs, const int* Cs) {
+  constexpr int R = 64 / KP, BH = KP / 2;
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int q = 0; q < BH; ++q) z[r][q] = make_float2(0.f, 0.f);
+  if (!t.ok) return;
+  if (t.mtype == 1) kbt_mstep<KP, 1>(z, xw, true, t.Xs2, nb, t.nk2, t.dm2, i0, nr, t.d0, t.W, b0, MFs, Cs, t.dia);
+  else if (t.mtype == 2) kbt_mstep<KP, 2>(z, xw, true, t.Xs2, nb, t.nk2, t.dm2, i0, nr, t.d0, t.W, b0, MFs, Cs, t.dia);
+  else kbt_mstep<KP, 0>(z, xw, true, t.Xs2, nb, t.nk2, t.dm2, i0, nr, t.d0, t.W, b0, MFs, Cs, t.dia);
+}
+
+// producer-only barrier (warps 0-7) that leaves the MMA warp out
+__device__ __forceinline__ void kbt_producer_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+// issues the MMAs of one term (one thread): D_re += Z_re K_re - Z_im K_im,
+// D_im += Z_re K_im + Z_im K_re, each product as three TF32 MMAs per K step
+// (A hi B hi, A hi B lo, A lo B hi); zero parts of K skipped
+template <int KP>
+__device__ __forceinline__ void kbt_issue(uint32_t tmem, uint64_t adesc0, uint64_t bdesc, uint32_t idesc, int NP,
+                                          int nr, int ktype, int nk2, uint32_t& dinit) {
+  constexpr int ATILE = 128 * KP;
+  int pd[4], pa[4], pb[4];
+  int np = 0;
+  if (ktype != 2) {
+    pd[np] = 0; pa[np] = 0; pb[np] = 0; ++np;  // re <- Z_re K_re
+    pd[np] = 1; pa[np] = 2; pb[np] = 0; ++np;  // im <- Z_im K_re
+  }
+  if (ktype != 1) {
+    pd[np] = 0; pa[np] = 2; pb[np] = 4; ++np;  // re <- Z_im (-K_im)
+    pd[np] = 1; pa[np] = 0; pb[np] = 2; ++np;  // im <- Z_re K_im
+  }
+  const int nks = (nk2 + 7) >> 3;
+  // descriptor start addresses advance by (byte offset >> 4)
+  for (int r = 0; r < nr; ++r) {
+    for (int q = 0; q < np; ++q) {
+      const uint32_t dcol = tmem + (uint32_t)((2 * r + pd[q]) * NP);
+      const uint32_t dbit = 1u << (2 * r + pd[q]);
+      const uint64_t ad = adesc0 + (uint64_t)(((r * 4 + pa[q]) * ATILE * 4) >> 4);
+      const uint64_t bd = bdesc + (uint64_t)((pb[q] * TC_BPART) >> 4);
+#pragma unroll
+      for (int sp = 0; sp < 3; ++sp) {
+        const uint64_t a2 = ad + (sp == 2 ? (uint64_t)((ATILE * 4) >> 4) : 0);
+        const uint64_t b2 = bd + (sp == 1 ? (uint64_t)(TC_BPART >> 4) : 0);
+#pragma unroll
+        for (int ks = 0; ks < KP / 8; ++ks) {
+          if (ks < nks) {
+            tc_mma_tf32(dcol, a2 + 16u * ks, b2 + 16u * ks, idesc, (dinit & dbit) ? 1u : 0u);
+            dinit |= dbit;
+          }
+        }
+      }
+    }
+  }
+}
+
+// Warp-specialised pipeline over the terms of the tile. Warps 0-7 (producers)
+// compute Z and store the A tiles; warp 8 issues the MMAs. full: the A tiles
+// (and the B buffer) of a term are stored (256 arrivals); empty: the MMAs of a
+// term are done (tcgen05.commit). The X window of term t + 1 is requested
+// before the A tiles of term t are stored, and the MMAs of term t run while
+// the producers compute Z of term t + 1.
+template <int KP>
+__device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
+  constexpr int R = 64 / KP, BH = KP / 2;
+  constexpr int ATILE = 128 * KP;  // floats of one A tile
+  const DevOp& op = p.op;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const bool producer = wid < 8;
+  const int vq = wid & 3, b0 = ((wid >> 2) & 1) * BH;
+  const int vloc = vq * 32 + lane;
+  const long long nb = p.nb;
+  const int v = blockIdx.y * 128 + vloc;
+  float* As = reinterpret_cast<float*>(smem);
+  char* Bs = smem + TC_ABYTES;
+  float2* MFs0 = reinterpret_cast<float2*>(Bs + 2 * TC_BBYTES);          // [2][8][KB_WMAX]
+  int* Cs0 = reinterpret_cast<int*>(Bs + 2 * TC_BBYTES + TC_MFBYTES);   // [2][8][KB_WMAX]
+  uint64_t* full = reinterpret_cast<uint64_t*>(Bs + 2 * TC_BBYTES + TC_MFBYTES + TC_CSBYTES);
+  uint64_t* empty = full + 1;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(full + 2);
+  const int nk1 = __ldg(op.out_dk + s1);
+  const int NP = nk1 <= 16 ? 16 : 32;
+  float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * nk1) * nb + v;
+  const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
+  if (te == tb) {  // no term reaches this slab
+    if (producer)
+      for (int e = wid >> 2; e < nr * nk1; e += 2) Y[(long long)e * nb] = make_float2(0.f, 0.f);
+    return;
+  }
+  uint32_t ncols = 32;
+  while (ncols < (uint32_t)(2 * R * NP)) ncols <<= 1;
+  if (wid == 8) tc_alloc(tslot, ncols);
+  if (tid == 256) {
+    tc_mbar_init(full, 256);
+    tc_mbar_init(empty, 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  bool ok = true;
+  int ncommit = 0;  // terms whose MMAs were (or will be) committed
+
+  if (!producer) {
+    // ---- MMA warp --------------------------------------------------------
+    if (lane == 0) {
+      const uint32_t idesc = tc_idesc_tf32(128, NP);
+      const uint64_t adesc0 = tc_desc(tc_smem_u32(As), 128u, 32u * KP);
+      const uint64_t bdesc0 = tc_desc(tc_smem_u32(Bs), 128u, 32u * KP);
+      uint32_t dinit = 0;
+      for (int term = tb; term < te; ++term) {
+        const int s2 = __ldg(op.t_in + term);
+        const int nk2 = __ldg(op.in_dk + s2);
+        const int W = __ldg(op.mf_width + __ldg(op.t_mf + term));
+        if (!(nk2 <= KP && W <= KB_WMAX)) continue;
+        const int ktype = __ldg(op.k_type + __ldg(op.t_k + term));
+        if (!tc_mbar_wait(full, (uint32_t)ncommit & 1u)) ok = false;
+        tc_fence_after();
+        const uint64_t bdesc = bdesc0 + (uint64_t)((((term - tb) & 1) * TC_BBYTES) >> 4);
+        kbt_issue<KP>(tmem, adesc0, bdesc, idesc, NP, nr, ktype, nk2, dinit);
+        tc_commit(empty);
+        ++ncommit;
+      }
+      if (!ok) atomicExch(p.err, KR_ERR_TIMEOUT);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_dealloc(tmem, ncols);
+    return;
+  }
+
+  // ---- producers -----------------------------------------------------------
+  float2 z[R][BH];
+  KbtWin<KP> xw;
+  KbtTerm cur = kbt_term(op, p, tb, KP, v, nb);
+  if (cur.ok && cur.dia) xw.load(cur.Xs2, nb, cur.nk2, cur.dm2, i0 + cur.d0, nr + cur.W - 1, b0);
+  kbt_stage<KP>(cur, nk1, NP, i0, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, tid);
+  kbt_producer_sync();
+  kbt_zstep<KP>(z, xw, cur, nb, i0, nr, b0, MFs0, Cs0);
+  for (int term = tb; term < te; ++term) {
+    const int buf = (term - tb) & 1;
+    const bool has_next = term + 1 < te;
+    KbtTerm nxt;
+    if (has_next) {
+      nxt = kbt_term(op, p, term + 1, KP, v, nb);
+      if (nxt.ok && nxt.dia) xw.load(nxt.Xs2, nb, nxt.nk2, nxt.dm2, i0 + nxt.d0, nr + nxt.W - 1, b0);
+    }
+    // the MMAs of the previous committed term are done with the A tiles and its B buffer
+    if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
+    tc_fence_after();
+    if (cur.ok) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (r >= nr) continue;
+        float* At = As + r * 4 * ATILE;
+#pragma unroll
+        for (int c4 = 0; c4 < BH; c4 += 4) {
+          float4 rh, rl, ih, il;
+          float* prh = &rh.x;
+          float* prl = &rl.x;
+          float* pih = &ih.x;
+          float* pil = &il.x;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float2 zz = z[r][c4 + q];
+            prh[q] = tc_tf32(zz.x);
+            prl[q] = zz.x - prh[q];
+            pih[q] = tc_tf32(zz.y);
+            pil[q] = zz.y - pih[q];
+          }
+          const uint32_t o = tc_kmajor_off(vloc, b0 + c4, KP) >> 2;
+          *reinterpret_cast<float4*>(At + 0 * ATILE + o) = rh;
+          *reinterpret_cast<float4*>(At + 1 * ATILE + o) = rl;
+          *reinterpret_cast<float4*>(At + 2 * ATILE + o) = ih;
+          *reinterpret_cast<float4*>(At + 3 * ATILE + o) = il;
+        }
+      }
+      tc_fence_proxy();
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc_smem_u32(full)) : "memory");
+      ++ncommit;
+    } else if (tid == 0) {
+      atomicExch(p.err, KR_ERR_ARG);  // outside the tile shape: skipped
+    }
+    if (has_next) {
+      // B buffer buf ^ 1 was last read by the MMAs of term - 1 (done); MF buffer
+      // buf ^ 1 by the M step of term - 1 (every producer is past it)
+      kbt_stage<KP>(nxt, nk1, NP, i0, nr, reinterpret_cast<float*>(Bs + (buf ^ 1) * TC_BBYTES),
+                    MFs0 + (buf ^ 1) * 8 * KB_WMAX, Cs0 + (buf ^ 1) * 8 * KB_WMAX, tid);
+      kbt_producer_sync();
+      kbt_zstep<KP>(z, xw, nxt, nb, i0, nr, b0, MFs0 + (buf ^ 1) * 8 * KB_WMAX, Cs0 + (buf ^ 1) * 8 * KB_WMAX);
+      cur = nxt;
+    }
+  }
+  if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
+  tc_fence_after();
+  // epilogue: rows r = w / 4, w / 4 + 2, ... of this warp's lane quarter
+  for (int r = wid >> 2; r < nr; r += 2) {
+    for (int c0 = 0; c0 < NP; c0 += 16) {
+      float re[16], im[16];
+      const uint32_t lanebase = (uint32_t)(vq * 32) << 16;
+      tc_ld16(tmem + lanebase + (uint32_t)(2 * r * NP + c0), re);
+      tc_ld16(tmem + lanebase + (uint32_t)((2 * r + 1) * NP + c0), im);
+      const bool any = ncommit > 0;
+#pragma unroll
+      for (int q = 0; q < 16; ++q)
+        if (c0 + q < nk1)
+          Y[((long long)r * nk1 + c0 + q) * nb] = any ? make_float2(re[q], im[q]) : make_float2(0.f, 0.f);
+    }
+  }
+  if (!ok && lane == 0) atomicExch(p.err, KR_ERR_TIMEOUT);
+  tc_fence_before();
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(288, 1) kb_matvec_tc(BatchTC p) {
+  extern __shared__ __align__(1024) char kbt_smem[];
+  if (p.grp_active) {
+    const int* g = p.grp_active + 4 * blockIdx.y;
+    if (!(g[0] | g[1] | g[2] | g[3])) return;
+  }
+  const int task = blockIdx.x;
+  const int s1 = __ldg(p.task + task);
+  const int i0 = __ldg(p.task + p.ntask + task);
+  const int nr = __ldg(p.task + 2 * p.ntask + task);
+  const int kp = __ldg(p.task + 3 * p.ntask + task);
+  if (kp == 8) kbt_tile<8>(p, s1, i0, nr, kbt_smem);
+  else if (kp == 16) kbt_tile<16>(p, s1, i0, nr, kbt_smem);
+  else kbt_tile<32>(p, s1, i0, nr, kbt_smem);
+}
+
 // any active vector per 32-vector group
 __global__ void kb_group_active(const int* active, int* grp, int ngrp) {
   const int g = blockIdx.x * blockDim.y + threadIdx.y;
@@ -693,8 +1105,30 @@ int balloc(kr_batch* b, size_t count, T** p) {
   return KR_OK;
 }
 int mv_groups(const kr_batch* b) { return b->nb / 32; }
+const char* const mv_error_text =
+    "batched mat-vec: an MMA completion wait gave up or a term exceeded the tile shape";
 
 int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool masked, cudaStream_t st) {
+  if (b->mv_kind == KR_MATVEC_TENSOR && op->tc_ntask > 0) {
+    BatchTC q;
+    q.op = op->dev;
+    q.X = X;
+    q.Y = Y;
+    q.nb = b->nb;
+    q.task = op->tc_task;
+    q.ntask = op->tc_ntask;
+    q.grp_active = masked ? b->grp_active : nullptr;
+    q.err = b->counts + 2;
+    static bool tc_attr = false;
+    if (!tc_attr) {
+      KR_CUDA(op->ctx, cudaFuncSetAttribute(kb_matvec_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+      tc_attr = true;
+    }
+    kb_matvec_tc<<<dim3(op->tc_ntask, b->nb / 128), 288, TC_SMEM, st>>>(q);
+    b->launches++;
+    KR_CUDA(op->ctx, cudaGetLastError());
+    return KR_OK;
+  }
   BatchMV p;
   p.op = op->dev;
   p.X = X;
@@ -758,7 +1192,7 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
   BA((size_t)mv_groups(b), &b->grp_active);
   BA(nb, &b->err);
   BA((size_t)KB_RED_CHUNKS * (m1 + 1) * nb, &b->part);
-  BA(2, &b->counts);
+  BA(3, &b->counts);
   // output tiles: R = 128 / NKP rows of one slab (NKP = n_k rounded up to 4, 8, 16, 32)
   std::vector<int> ts, ti, tn;
   for (int s = 0; s < (int)dm.size(); ++s) {
@@ -819,6 +1253,7 @@ extern "C" int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double f
   const int stride = b->mmax + 2;
   const double2 fac = make_double2(fac_re, fac_im);
   kr_ctx* ctx = op->ctx;
+  KR_CUDA(ctx, cudaMemsetAsync(b->counts, 0, 3 * sizeof(int), st));
   // S <- phase * S, norms, V_0
   kb_phase_norm<<<eg, eb, 0, st>>>(b->S, (const double2*)phase, dim, nb, b->part);
   kb_reduce<<<(nb + 255) / 256, 256, 0, st>>>(b->part, 1, nb, 1, b->h);
@@ -840,10 +1275,11 @@ extern "C" int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double f
     kb_scale<<<eg, eb, 0, st>>>(b->V + (long long)(k + 1) * dim * nb, b->vscale, b->active, dim, nb);
     b->launches += 7;
     KR_CUDA(ctx, cudaGetLastError());
-    int counts[2] = {0, 0};
+    int counts[3] = {0, 0, 0};
     KR_CUDA(ctx, cudaMemcpyAsync(counts, b->counts, sizeof(counts), cudaMemcpyDeviceToHost, st));
     KR_CUDA(ctx, cudaStreamSynchronize(st));
     kused = k + 1;
+    if (counts[2] != 0) return set_err(ctx, counts[2], mv_error_text);
     if (counts[1] > 0)
       return set_err(ctx, KR_ERR_MAXORDER,
                      "batched Lanczos: " + std::to_string(counts[1]) + " vectors did not reach the tolerance within " +
@@ -872,6 +1308,7 @@ extern "C" int kr_batch_expect(kr_batch* b, kr_op* obs, double* out, void* strea
   cudaStream_t st = (cudaStream_t)stream;
   const long long n = b->dim * b->nb;
   float2* X = b->V;  // basis slot 0 and W are free between steps
+  KR_CUDA(obs->ctx, cudaMemsetAsync(b->counts + 2, 0, sizeof(int), st));
   kb_to_f32<<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, st>>>(b->S, X, n);
   int rc = launch_matvec(b, obs, X, b->W, false, st);
   if (rc) return rc;
@@ -881,8 +1318,11 @@ extern "C" int kr_batch_expect(kr_batch* b, kr_op* obs, double* out, void* strea
   b->launches += 3;
   KR_CUDA(obs->ctx, cudaGetLastError());
   std::vector<double2> h(b->nb);
+  int mverr = 0;
   KR_CUDA(obs->ctx, cudaMemcpyAsync(h.data(), b->h, sizeof(double2) * b->nb, cudaMemcpyDeviceToHost, st));
+  KR_CUDA(obs->ctx, cudaMemcpyAsync(&mverr, b->counts + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
   KR_CUDA(obs->ctx, cudaStreamSynchronize(st));
+  if (mverr) return set_err(obs->ctx, mverr, mv_error_text);
   for (int v = 0; v < b->nvec; ++v) {
     out[2 * v] = h[v].x;
     out[2 * v + 1] = h[v].y;
@@ -931,13 +1371,24 @@ extern "C" int kr_batch_apply(kr_batch* b, kr_op* op, const void* x, void* y, vo
     return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_apply: bad argument or basis mismatch");
   cudaStream_t st = (cudaStream_t)stream;
   const dim3 grid((unsigned)((b->dim + 31) / 32), b->nb / 32);
+  KR_CUDA(op->ctx, cudaMemsetAsync(b->counts + 2, 0, sizeof(int), st));
   kb_transpose_in32<<<grid, dim3(32, 8), 0, st>>>((const double2*)x, b->V, b->dim, b->nvec, b->nb);
   const int rc = launch_matvec(b, op, b->V, b->W, false, st);
   if (rc) return rc;
   kb_transpose_out32<<<grid, dim3(32, 8), 0, st>>>(b->W, (double2*)y, b->dim, b->nvec, b->nb);
   b->launches += 2;
   KR_CUDA(op->ctx, cudaGetLastError());
+  int mverr = 0;
+  KR_CUDA(op->ctx, cudaMemcpyAsync(&mverr, b->counts + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
   KR_CUDA(op->ctx, cudaStreamSynchronize(st));
+  if (mverr) return set_err(op->ctx, mverr, mv_error_text);
+  return KR_OK;
+}
+
+extern "C" int kr_batch_set_matvec(kr_batch* b, int32_t kind) {
+  if (!b || (kind != KR_MATVEC_TENSOR && kind != KR_MATVEC_FP32))
+    return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_set_matvec: bad argument");
+  b->mv_kind = kind;
   return KR_OK;
 }
 

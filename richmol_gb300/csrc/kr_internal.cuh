@@ -59,6 +59,9 @@ struct kr_op {
   int npart = 0;
   int nmf = 0;
   int ndiag_groups = 0;  // M groups in diagonal slot order
+  // tiles of the tensor-core batched mat-vec: [4][tc_ntask] = slab, first row, rows, KP
+  int tc_ntask = 0;
+  int* tc_task = nullptr;
   long long launches = 0;
   double fma_per_matvec = 0, bytes_per_matvec = 0;
   // step scratch

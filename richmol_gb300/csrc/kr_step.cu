@@ -779,6 +779,45 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   std::stable_sort(task_order.begin(), task_order.end(),
                    [&](int x, int y) { return task_cost[x] > task_cost[y]; });
 
+  // ---- tiles of the tensor-core batched mat-vec ---------------------------
+  // per output slab: KP = largest input n_k of its terms padded to 8 (the MMA K),
+  // R = 64 / KP rows per tile; heaviest slabs first
+  std::vector<int> tc_task;
+  {
+    std::vector<int> ts, ti, tn, tk;
+    std::vector<double> tcost;
+    for (int s = 0; s < d->nslab_out; ++s) {
+      int maxnk2 = 1;
+      for (int t : by_out[s]) maxnk2 = std::max(maxnk2, d->in_dk[d->t_in[t]]);
+      if (maxnk2 > 32 || d->out_dk[s] > 32) {
+        tc_task.clear();
+        ts.clear();
+        break;  // outside the batched mat-vec's shapes (kr_batch_create rejects such operators)
+      }
+      const int kp = maxnk2 <= 8 ? 8 : maxnk2 <= 16 ? 16 : 32;
+      const int R = 64 / kp, dm1 = d->out_dm[s];
+      for (int i0 = 0; i0 < dm1; i0 += R) {
+        ts.push_back(s);
+        ti.push_back(i0);
+        tn.push_back(std::min(R, dm1 - i0));
+        tk.push_back(kp);
+        tcost.push_back((double)by_out[s].size() * kp * std::min(R, dm1 - i0));
+      }
+    }
+    const int n = (int)ts.size();
+    std::vector<int> ord(n);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return tcost[x] > tcost[y]; });
+    tc_task.resize((size_t)4 * n);
+    for (int q = 0; q < n; ++q) {
+      tc_task[q] = ts[ord[q]];
+      tc_task[n + q] = ti[ord[q]];
+      tc_task[2 * n + q] = tn[ord[q]];
+      tc_task[3 * n + q] = tk[ord[q]];
+    }
+    op->tc_ntask = n;
+  }
+
   // K blocks transposed: KT[b][a] (complex blocks keep (re, im) pairs)
   std::vector<double> k_t(d->k_data, d->k_data + d->k_data_len);
   for (int b = 0; b < d->nk; ++b) {
@@ -852,6 +891,10 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   UP(task_row0.data(), ntask, &p_i); D.task_row0 = p_i;
   UP(task_nrows.data(), ntask, &p_i); D.task_nrows = p_i;
   UP(task_order.data(), task_order.size(), &p_i); D.task_order = p_i;
+  if (op->tc_ntask > 0) {
+    UP(tc_task.data(), tc_task.size(), &p_i);
+    op->tc_task = p_i;
+  }
   D.ntask = ntask;
   unsigned* p_u;
   UP((const unsigned*)nullptr, (size_t)KR_MATVEC_MAXVEC, &p_u); op->mv_counters = p_u;
