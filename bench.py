@@ -51,6 +51,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="bound of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="headline measurement only")
+    p.add_argument("--matvec", choices=["tensor", "fp32"], default="tensor",
+                   help="batched mat-vec kind: tensor-core K contraction (split TF32) or FP32 FMAs")
     return p.parse_args()
 
 
@@ -223,7 +225,7 @@ def run_ours(args, ws, rank, local):
     td = TDSE(t_start=wl.t_start, t_end=wl.t_end, dt=wl.dt)
     tc = td.time_grid()
     nsteps = len(tc)
-    ens = Ensemble(td, wl.h0, nvec, tol=1e-8)
+    ens = Ensemble(td, wl.h0, nvec, tol=1e-8, matvec=args.matvec)
     ens.load(ensd.vectors(dim))
     for i in range(args.warmup):
         ens.step(wl.hamiltonian(tc[i]))
@@ -257,14 +259,22 @@ def run_ours(args, ws, rank, local):
 
     # dominant kernel (batched complex64 mat-vec) alone
     plan = wl.hamiltonian(tc[args.warmup]).device_operator()
-    em = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
-    for a, b in em:
-        a.record()
-        _native.check(_native.lib().kr_batch_matvec(ens.handle, plan.op, ctypes.c_void_p(
-            torch.cuda.current_stream().cuda_stream)), ctx)
-        b.record()
-    torch.cuda.synchronize()
-    mv_s = statistics.median(a.elapsed_time(b) for a, b in em) / 1e3
+
+    def time_matvec(kind):
+        _native.check(_native.lib().kr_batch_set_matvec(ens.handle, kind), ctx)
+        em = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(6)]
+        for a, b in em:
+            a.record()
+            _native.check(_native.lib().kr_batch_matvec(ens.handle, plan.op, ctypes.c_void_p(
+                torch.cuda.current_stream().cuda_stream)), ctx)
+            b.record()
+        torch.cuda.synchronize()
+        return statistics.median(a.elapsed_time(b) for a, b in em[1:]) / 1e3
+
+    kinds = {"tensor": _native.KR_MATVEC_TENSOR, "fp32": _native.KR_MATVEC_FP32}
+    kind_s = {k: time_matvec(code) for k, code in kinds.items()}
+    _native.check(_native.lib().kr_batch_set_matvec(ens.handle, kinds[args.matvec]), ctx)
+    mv_s = kind_s[args.matvec]
     fma_mv, bytes_mv = plan.work()
     mv_flops = 2.0 * fma_mv * nvec
     mv_bytes = 8.0 * 2 * dim * nvec  # complex64 X in + Y out (factors are shared by all vectors)
@@ -274,7 +284,10 @@ def run_ours(args, ws, rank, local):
         "bound": "hbm", "achieved": round(gbs, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
         "frac": round(gbs / peaks["hbm_gbs"], 4), "traffic": traffic,
         "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
-        "kernel": "kb_matvec (complex64 batched mat-vec)", "kernel_ms": round(mv_s * 1e3, 3),
+        "kernel": ("kb_matvec_tc (complex64 batched mat-vec, K contraction on tcgen05)" if args.matvec == "tensor"
+                   else "kb_matvec (complex64 batched mat-vec, FP32 FMAs)"),
+        "kernel_ms": round(mv_s * 1e3, 3),
+        "kernel_ms_by_kind": {k: round(t * 1e3, 3) for k, t in kind_s.items()},
         "alg_bytes_per_launch": mv_bytes,
         "fp32": {"achieved_tflops": round(mv_flops / mv_s / 1e12, 2), "peak_tflops": round(fp32.value, 1),
                  "frac": round(mv_flops / mv_s / 1e12 / fp32.value, 4),
@@ -283,7 +296,8 @@ def run_ours(args, ws, rank, local):
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
         "ms_per_step": round(total_s * 1e3 / K, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c64 mat-vec (FP32 accumulate) / f64 Lanczos scalars and state",
+        "vs_baseline": None, "dtype": ("c64 mat-vec (K contraction as split-TF32 tcgen05 MMAs, FP32 accumulate)" if args.matvec == "tensor"
+                  else "c64 mat-vec (FP32 FMAs)") + " / f64 Lanczos scalars and state",
         "data": "synthetic",
         "config": {"workload": f"batched thermal ensemble: asymmetric top D2 Watson-A J=0..{args.jmax} "
                                f"(dim {dim}), T=5 K ensemble of {ensd.n_natural} states with weight>=1e-5 padded "
@@ -328,7 +342,7 @@ def run_ours(args, ws, rank, local):
         v0 = ensd.vectors(dim)[:nn]
         tda = TDSE(t_start=wl.t_start, t_end=wl.t_end, dt=wl.dt)
         tca = tda.time_grid()
-        ea = Ensemble(tda, wl.h0, nn, tol=1e-8)
+        ea = Ensemble(tda, wl.h0, nn, tol=1e-8, matvec=args.matvec)
         ea.load(v0)
         ref = torch.from_numpy(v0).to(dev)
         worst_w, worst_v = 0.0, 0.0
