@@ -99,6 +99,22 @@ typedef struct {
   int32_t maxorder;           /* Lanczos basis capacity (reference: 100)    */
 } kr_op_desc;
 
+/* x <- exp(t A) x, A = i H, for one vector (x: dim complex128 device array,
+ * overwritten; with phase != NULL, x is multiplied by phase before and after,
+ * the H0 half-phases of the split operator, tdse.py:368-394) with the Krylov scheme of EXPOKIT's ZHEXPV (Sidje 1998), which
+ * richmol calls for propag='external' (tdse.py:383-392, pyexpokit.py:55-89;
+ * m = 12, t = Im(exp_fac)): fixed Krylov dimension m (<= 30), local error
+ * control against tol, at most 500 substeps (then KR_ERR_MAXORDER, the
+ * reference's "maximum number of steps reached without convergence").
+ * anorm: 1-norm estimate of H (kr_op_norm1). stats (may be NULL): substeps,
+ * mat-vecs, rejected substeps. Synchronises the stream. */
+int kr_expv(kr_op* op, void* x, const void* phase, double t, int32_t m, double tol,
+            double anorm, int32_t* stats, void* stream);
+/* Lower-bound estimate of the 1-norm of the (Hermitian) operator with the
+ * field of the last kr_set_field: Hager-Higham power iteration (deterministic;
+ * the reference uses scipy's randomised onenormest on H.tomat(), tdse.py:387). */
+int kr_op_norm1(kr_op* op, double* norm, void* stream);
+
 /* Context on one device. Replaces nothing in the reference (which keeps no
  * device state); created once per process and device. */
 int kr_ctx_create(int device, kr_ctx** out);

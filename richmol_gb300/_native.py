@@ -16,7 +16,7 @@ ROOT = os.path.dirname(PKG)
 LIB_DIR = os.path.join(PKG, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "librichmol_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
-SOURCES = [os.path.join(PKG, "csrc", "kr_step.cu"), os.path.join(PKG, "csrc", "kr_batch.cu")]
+SOURCES = [os.path.join(PKG, "csrc", f) for f in ("kr_step.cu", "kr_batch.cu", "kr_expv.cu")]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 KR_OK, KR_ERR_ARG, KR_ERR_CUDA, KR_ERR_MAXORDER, KR_ERR_TIMEOUT, KR_ERR_UNSUPPORTED = range(6)
@@ -36,6 +36,7 @@ EXPORTED = [
     "kr_probe_fp64", "kr_probe_fp32", "kr_probe_mma", "kr_step_static", "kr_static_scratch_bytes",
     "kr_batch_create", "kr_batch_destroy", "kr_batch_load", "kr_batch_store", "kr_batch_step",
     "kr_batch_korder", "kr_batch_expect", "kr_batch_launch_count", "kr_batch_matvec", "kr_batch_apply", "kr_batch_set_matvec",
+    "kr_expv", "kr_op_norm1",
 ]
 
 
@@ -48,18 +49,31 @@ class KrylovError(RuntimeError):
 
 
 def build_library(verbose=False, nvcc="nvcc"):
-    """Compiles the CUDA sources into richmol_gb300/lib/librichmol_gb300.so."""
+    """Compiles the CUDA sources (one process per translation unit, in
+    parallel) and links richmol_gb300/lib/librichmol_gb300.so."""
     os.makedirs(LIB_DIR, exist_ok=True)
-    tmp = LIB_PATH + ".tmp"
-    cmd = [nvcc, *ARCH_FLAGS, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-           "-I", INCLUDE, "-o", tmp, *SOURCES]
+    common = [nvcc, *ARCH_FLAGS, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
     if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-    res = subprocess.run(cmd, capture_output=True, text=True)
+        common.insert(1, "-Xptxas=-v")
+    objs, procs = [], []
+    for src in SOURCES:
+        obj = os.path.join(LIB_DIR, os.path.splitext(os.path.basename(src))[0] + ".o")
+        objs.append(obj)
+        procs.append(subprocess.Popen([*common, "-c", "-o", obj, src], stdout=subprocess.PIPE,
+                                      stderr=subprocess.STDOUT, text=True))
+    out, failed = [], False
+    for pr in procs:
+        o, _ = pr.communicate()
+        out.append(o)
+        failed |= pr.returncode != 0
+    if failed:
+        raise RuntimeError("nvcc failed:\n" + "".join(out))
+    tmp = LIB_PATH + ".tmp"
+    res = subprocess.run([nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs], capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError("nvcc failed:\n" + res.stdout + res.stderr)
+        raise RuntimeError("nvcc link failed:\n" + res.stdout + res.stderr)
     os.replace(tmp, LIB_PATH)
-    return res.stdout + res.stderr
+    return "".join(out) + res.stdout + res.stderr
 
 
 class kr_op_desc(ctypes.Structure):
@@ -148,6 +162,10 @@ def lib():
         L.kr_batch_launch_count.restype = i64
         L.kr_probe_fp32.argtypes = [vp, ctypes.POINTER(dbl)]
         L.kr_probe_fp32.restype = ctypes.c_int
+        L.kr_expv.argtypes = [vp, vp, vp, dbl, i32, dbl, dbl, vp, vp]
+        L.kr_expv.restype = ctypes.c_int
+        L.kr_op_norm1.argtypes = [vp, ctypes.POINTER(dbl), vp]
+        L.kr_op_norm1.restype = ctypes.c_int
         L.kr_probe_mma.argtypes = [vp, vp, vp, vp]
         L.kr_probe_mma.restype = ctypes.c_int
         L.kr_probe_fp64.argtypes = [vp, ctypes.POINTER(dbl)]

@@ -37,6 +37,7 @@ __device__ __forceinline__ double2 ldcg2(const double2* p) { return __ldcg(p); }
 // operator tables on the device
 // ---------------------------------------------------------------------------
 #define KR_NO_DIAG (-2147483647 - 1)  // MF instance without diagonal slot order
+#define KR_EXPV_MMAX 30                // largest Krylov dimension of kr_expv
 #define KR_DIAG_MAX 8                  // widest diagonal band the batched mat-vec takes by offset
 
 struct DevOp {

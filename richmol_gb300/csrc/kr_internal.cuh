@@ -62,6 +62,9 @@ struct kr_op {
   // tiles of the tensor-core batched mat-vec: [4][tc_ntask] = slab, first row, rows, KP
   int tc_ntask = 0;
   int* tc_task = nullptr;
+  // workspace of kr_expv / kr_op_norm1 (grown on demand, freed with the operator)
+  void* expv_ws = nullptr;
+  size_t expv_bytes = 0;
   long long launches = 0;
   double fma_per_matvec = 0, bytes_per_matvec = 0;
   // step scratch

@@ -537,6 +537,7 @@ extern "C" int kr_last_error(const kr_ctx* ctx, char* buf, size_t len) {
 extern "C" void kr_op_destroy(kr_op* op) {
   if (!op) return;
   for (void* p : op->allocs) cudaFree(p);
+  if (op->expv_ws) cudaFree(op->expv_ws);
   delete op;
 }
 

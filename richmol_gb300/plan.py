@@ -297,6 +297,21 @@ class OperatorPlan:
             self.op, _native.ptr(states), nvec, _native.ptr(phase), float(fac.real), float(fac.imag),
             float(tol), int(flags), kp, stream_ptr(stream)), self.ctx)
 
+    def norm1(self, stream=None):
+        """1-norm estimate of the operator with its current field (kr_op_norm1)."""
+        out = ctypes.c_double()
+        _native.check(_native.lib().kr_op_norm1(self.op, ctypes.byref(out), stream_ptr(stream)), self.ctx)
+        return out.value
+
+    def expv(self, x, t, m, tol, anorm, phase=None, stream=None):
+        """x <- exp(t i H) x for one vector (complex128 CUDA tensor of dim elements),
+        expokit ZHEXPV scheme (kr_expv); returns (substeps, mat-vecs, rejected)."""
+        stats = np.zeros(3, np.int32)
+        _native.check(_native.lib().kr_expv(
+            self.op, _native.ptr(x), _native.ptr(phase), float(t), int(m), float(tol), float(anorm),
+            stats.ctypes.data, stream_ptr(stream)), self.ctx)
+        return tuple(int(s) for s in stats)
+
     def sync_status(self, stream=None):
         _native.check(_native.lib().kr_sync_status(self.op, stream_ptr(stream)), self.ctx)
 

@@ -20,6 +20,10 @@ from .convert_units import J_to_invcm, MHz_to_invcm
 from .field import CarTens
 
 
+class ExpokitError(Exception):
+    """Error of the external (expokit-scheme) propagator, as richmol.pyexpokit.ExpokitError."""
+
+
 def update_counter(func):
     """tdse.py:11-24: returns (vecs, t2[icall]), the end of the interval."""
     @functools.wraps(func)
@@ -176,8 +180,6 @@ class TDSE:
             propag = kwargs["propag"]
         else:
             propag = "internal"
-        if propag == "external":
-            raise NotImplementedError("propag='external' (expokit ZHEXPV) is not available on the GPU path")
         if "tol" in kwargs:
             assert type(kwargs["tol"]) in [int, float], \
                 f"tolerance `tol` has bad type: '{type(kwargs['tol'])}', (must be 'int', 'float')"
@@ -208,6 +210,20 @@ class TDSE:
             # tdse.py:377: no field term, only the two half-phases
             plan = H0._plan(maxorder)
             plan.step(v2, phase, exp_fac, tol, flags=_native.KR_STEP_SKIP_KRYLOV)
+        elif propag == "external":
+            # tdse.py:383-392 / 400-411: expokit ZHEXPV per vector, m = 12,
+            # A = i H, t = Im(exp_fac), 1-norm estimate of H
+            plan = H.device_operator(maxorder=maxorder)
+            anorm = plan.norm1()
+            for ind in range(v2.shape[0]):
+                try:
+                    self.last_expv_stats = plan.expv(v2[ind], exp_fac.imag, 12, tol, anorm, phase=phase)
+                except _native.KrylovError as e:
+                    if e.code == _native.KR_ERR_MAXORDER:  # pyexpokit.py:9-18
+                        raise ExpokitError("maximum number of steps reached without convergence") from None
+                    if e.code == _native.KR_ERR_ARG:
+                        raise ExpokitError("bad input arguments") from None
+                    raise
         else:
             plan = H.device_operator(maxorder=maxorder)
             korder = np.zeros(v2.shape[0], np.int32) if check else None
