@@ -4,10 +4,14 @@ richmol/pyexpokit.py:55-89): EXPOKIT's ZHEXPV (R. B. Sidje, ACM Trans. Math.
 Softw. 24 (1998) 130-156), vendored by the reference as expokit/expokit.f:2783-3113.
 
 The published algorithm, with the constants of that routine:
-  * fixed Krylov dimension m (richmol passes 12), three-term recurrence that
-    takes the operator as Hermitian (the projected matrix gets equal real
-    off-diagonals h_{j,j+1} = h_{j+1,j} = ||p_j||), happy breakdown at
-    ||p_j|| <= 1e-7;
+  * fixed Krylov dimension m (richmol passes 12), Hermitian three-term
+    recurrence (Lanczos) on the Hermitian operator M, happy breakdown at
+    ||p_j|| <= 1e-7; the exponent is exp(t c M) with c = 1 (ZHEXPV's own use)
+    or c = i (richmol: it passes A = i H as the operator, tdse.py:389; the
+    recurrence, written for Hermitian A, then loses orthogonality and misses
+    the breakdown of vectors with a small invariant subspace, e.g. the OCS
+    ground state under a z field; here the Lanczos runs on H and the projected
+    matrix is c T, the same exponential);
   * time stepping over [0, |t|]: first step from the a-priori bound
     (expokit.f:2946-2949), each step accepted when the local error estimate
     (two extra terms of the augmented (m+2) x (m+2) exponential,
@@ -46,9 +50,12 @@ def _round2(x):
     return math.trunc(x / p1 + 0.55) * p1
 
 
-def zhexpv(v, anorm, m, t, matvec, tol=0.0, stats=None):
-    """w = exp(t A) v with the ZHEXPV recurrence; ``matvec(x)`` returns A x.
-    Raises ExpokitError like richmol/pyexpokit.py:9-18."""
+MXREJECT = 500  # rejections per step (the routine allows any number)
+
+
+def zhexpv(v, anorm, m, t, matvec, tol=0.0, stats=None, c=1.0):
+    """w = exp(t c M) v with the ZHEXPV scheme; ``matvec(x)`` returns M x for a
+    Hermitian M, c = 1 or 1j. Raises ExpokitError like richmol/pyexpokit.py:9-18."""
     v = np.asarray(v, dtype=np.complex128).ravel()
     n = v.size
     if m >= n or m <= 0:
@@ -83,18 +90,18 @@ def zhexpv(v, anorm, m, t, matvec, tol=0.0, stats=None):
             p = matvec(V[j])
             nmult += 1
             if j > 0:
-                p = p - Hm[j - 1, j] * V[j - 1]
+                p = p - (Hm[j - 1, j] / c) * V[j - 1]
             hjj = np.vdot(V[j], p)
             p = p - hjj * V[j]
             hj1j = np.linalg.norm(p)
-            Hm[j, j] = hjj
+            Hm[j, j] = c * hjj
             if hj1j <= BREAK_TOL:
                 k1 = 0
                 mbrkdwn = j + 1
                 t_step = t_out - t_now
                 break
-            Hm[j, j + 1] = hj1j
-            Hm[j + 1, j] = hj1j
+            Hm[j, j + 1] = c * hj1j
+            Hm[j + 1, j] = c * hj1j
             V[j + 1] = p / hj1j
         if k1 != 0:
             avnorm = np.linalg.norm(matvec(V[m]))
@@ -103,7 +110,10 @@ def zhexpv(v, anorm, m, t, matvec, tol=0.0, stats=None):
         # entry above it is cleared, and a 1 at (m+2, m+1) (expokit.f:3021-3022)
         Hm[m - 1, m] = 0.0
         Hm[m + 1, m] = 1.0
+        nreject_step = 0
         while True:
+            if nreject_step > MXREJECT:
+                raise ExpokitError("requested tolerance was too high")
             mx = mbrkdwn + k1
             F = scipy.linalg.expm(sgn * t_step * Hm[:mx, :mx])
             if k1 == 0:
@@ -117,10 +127,13 @@ def zhexpv(v, anorm, m, t, matvec, tol=0.0, stats=None):
                 err_loc, xm = (p1 * p2) / (p1 - p2), 1.0 / m
             else:
                 err_loc, xm = p1, 1.0 / (m - 1)
+            if not math.isfinite(err_loc):
+                raise ExpokitError("requested tolerance was too high")
             if err_loc <= DELTA * t_step * tol:
                 break
             t_step = _round2(GAMMA * t_step * (t_step * tol / err_loc) ** xm)
             nreject += 1
+            nreject_step += 1
         mx = mbrkdwn + max(0, k1 - 1)
         w = beta * (F[:mx, 0] @ V[:mx])
         t_new = _round2(GAMMA * t_step * (t_step * tol / err_loc) ** xm)

@@ -5,11 +5,15 @@
 // (the reference passes scipy's randomised onenormest of H.tomat()).
 //
 // The step control runs on the host in FP64 exactly as the published scheme:
-// fixed Krylov dimension m, three-term recurrence that takes A as Hermitian
-// (equal real off-diagonals), happy breakdown at 1e-7, a-priori first step,
+// fixed Krylov dimension m, Hermitian Lanczos on H with the projected matrix
+// i T of A = i H (the reference hands A = i H to a recurrence written for
+// Hermitian A, which loses orthogonality and misses the breakdown of small
+// invariant subspaces; the exponential is the same), happy breakdown at 1e-7,
+// a-priori first step,
 // acceptance when the local error estimate of the augmented (m+2) x (m+2)
 // exponential is <= 1.2 t_step tol, step shrink/grow by 0.9 (t_step tol /
-// err)^(1/m), step sizes rounded to two significant digits, at most 500 steps.
+// err)^(1/m), step sizes rounded to two significant digits, at most 500 steps
+// (and 500 rejections of one step, or a non-finite error estimate: error).
 // The vector work runs on the device: the FP64 mat-vec of kr_step.cu and small
 // FP64 kernels whose reductions sum in a fixed order (bitwise reproducible).
 // The small exponential is a (6, 6) Pade approximant with scaling and squaring.
@@ -418,30 +422,31 @@ static int kr_expv_krylov(kr_op* op, void* x, double t, int32_t m, double tol, d
     std::fill(Hm.begin(), Hm.end(), cd(0.0));
     KX_TRY(kx_axpby_l(k, 1.0 / beta, w, 0.0, k.V));  // V_0 = w / beta
     int k1 = 2, mbrk = m;
-    double avnorm = 0.0;
+    double avnorm = 0.0, beta_prev = 0.0;
+    const cd iu(0.0, 1.0);
     for (int j = 0; j < m; ++j) {
       double2* vj = k.V + (size_t)j * n;
       double2* p = k.V + (size_t)(j + 1) * n;
-      KX_TRY(kx_mv(k, vj, k.P));  // P = H v_j
+      // Hermitian Lanczos on H: p = H v_j - beta_{j-1} v_{j-1} - alpha_j v_j
+      KX_TRY(kx_mv(k, vj, p));
       ++nmult;
-      // p = A v_j - h_{j-1,j} v_{j-1},  A v_j = i P
-      KX_TRY(kx_axpby_l(k, cd(0.0, 1.0), k.P, 0.0, p));
-      if (j > 0) KX_TRY(kx_axpby_l(k, -Hm[(size_t)(j - 1) * mh + j], k.V + (size_t)(j - 1) * n, 1.0, p));
+      if (j > 0) KX_TRY(kx_axpby_l(k, -beta_prev, k.V + (size_t)(j - 1) * n, 1.0, p));
       double2 hd;
       KX_TRY(kx_red(k, KX_DOT, vj, p, &hd, nullptr));
       const cd hjj(hd.x, hd.y);
       KX_TRY(kx_axpby_l(k, -hjj, vj, 1.0, p));
       double hj1j = 0.0;
       KX_TRY(kx_nrm2(k, p, &hj1j));
-      Hm[(size_t)j * mh + j] = hjj;
-      if (hj1j <= 1e-7) {  // happy breakdown
+      Hm[(size_t)j * mh + j] = iu * hjj;  // projected matrix of A = i H: i T
+      if (hj1j <= 1e-7) {                 // happy breakdown
         k1 = 0;
         mbrk = j + 1;
         t_step = t_out - t_now;
         break;
       }
-      Hm[(size_t)j * mh + j + 1] = hj1j;
-      Hm[(size_t)(j + 1) * mh + j] = hj1j;
+      Hm[(size_t)j * mh + j + 1] = iu * hj1j;
+      Hm[(size_t)(j + 1) * mh + j] = iu * hj1j;
+      beta_prev = hj1j;
       KX_TRY(kx_axpby_l(k, 0.0, nullptr, 1.0 / hj1j, p));
     }
     if (k1 != 0) {
@@ -455,7 +460,8 @@ static int kr_expv_krylov(kr_op* op, void* x, double t, int32_t m, double tol, d
     Hm[(size_t)(m + 1) * mh + m] = 1.0;
     double err_loc = 0.0;
     int mx = 0;
-    for (;;) {
+    for (int rej = 0;; ++rej) {
+      if (rej > 500) return set_err(op->ctx, KR_ERR_MAXORDER, "kr_expv: requested tolerance was too high");
       mx = mbrk + k1;
       std::vector<cd> X((size_t)mx * mx);
       for (int i = 0; i < mx; ++i)
@@ -477,6 +483,7 @@ static int kr_expv_krylov(kr_op* op, void* x, double t, int32_t m, double tol, d
         err_loc = p1;
         xm = 1.0 / (m - 1);
       }
+      if (!std::isfinite(err_loc)) return set_err(op->ctx, KR_ERR_MAXORDER, "kr_expv: requested tolerance was too high");
       if (err_loc <= 1.2 * t_step * tol) break;
       t_step = round2(0.9 * t_step * std::pow(t_step * tol / err_loc, xm));
       ++nreject;

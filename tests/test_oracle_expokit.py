@@ -22,7 +22,7 @@ def test_richmol_form_matches_expm(t):
     H, v = _herm(60, 0)
     anorm = np.abs(H).sum(axis=0).max()
     st = {}
-    w = zhexpv(v, anorm, 12, t, lambda x: 1j * (H @ x), tol=1e-15, stats=st)
+    w = zhexpv(v, anorm, 12, t, lambda x: H @ x, tol=1e-15, stats=st, c=1j)
     ref = scipy.linalg.expm(t * 1j * H) @ v
     assert np.abs(w - ref).max() / np.abs(ref).max() < 1e-12
     assert st["nstep"] >= 1 and st["nmult"] == 13 * st["nstep"]
@@ -36,11 +36,10 @@ def test_hermitian_form_matches_expm():
     assert np.abs(w - ref).max() / np.abs(ref).max() < 1e-12
 
 
-def test_happy_breakdown_is_exact():
-    """A Krylov space of dimension 3 (three distinct eigenvalues), Hermitian
-    form: breakdown at j = 3 and one step over the whole interval. (In
-    richmol's A = i H form the recurrence, which takes A as Hermitian, keeps
-    the residual above the breakdown tolerance; the result stays exact.)"""
+@pytest.mark.parametrize("c", [1.0, 1j])
+def test_happy_breakdown_is_exact(c):
+    """A Krylov space of dimension 3 (three distinct eigenvalues): breakdown at
+    j = 3 and one step over the whole interval, in both forms."""
     n = 30
     d = np.repeat([1.0, 2.5, -4.0], 10)
     rng = np.random.default_rng(2)
@@ -48,8 +47,8 @@ def test_happy_breakdown_is_exact():
     H = q @ np.diag(d) @ q.conj().T
     v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
     st = {}
-    w = zhexpv(v, np.abs(H).sum(axis=0).max(), 12, -0.7, lambda x: H @ x, tol=1e-15, stats=st)
-    ref = scipy.linalg.expm(-0.7 * H) @ v
+    w = zhexpv(v, np.abs(H).sum(axis=0).max(), 12, -0.7, lambda x: H @ x, tol=1e-15, stats=st, c=c)
+    ref = scipy.linalg.expm(-0.7 * c * H) @ v
     assert np.abs(w - ref).max() / np.abs(ref).max() < 1e-12
     assert st["nstep"] == 1
 
