@@ -36,7 +36,8 @@ struct kr_batch {
   int nvec = 0, nb = 0, mmax = 0;
   long long dim = 0;
   std::vector<void*> allocs;
-  double2* S = nullptr;      // [dim][nb] state, FP64
+  float4* S = nullptr;       // [dim][nb] state, double-float (re hi, re lo, im hi, im lo)
+  float4* phase_df = nullptr; // [dim] H0 half-phase of the current step, double-float
   float2* V = nullptr;       // [mmax + 1][dim][nb] Krylov basis
   float2* W = nullptr;       // [dim][nb] H V_k
   double* norm0 = nullptr;   // [nb]
@@ -64,7 +65,7 @@ struct kr_batch {
 struct BatchDev {
   int nvec, nb, mmax;
   long long dim;
-  double2* S;
+  float4* S;
   float2* V;
   double* norm0;
   double2* h;
@@ -125,21 +126,77 @@ __device__ __forceinline__ double2 warps_sum(double2 v, double2 (*sh)[32]) {
   return s;
 }
 
+// ---------------------------------------------------------------------------
+// double-float arithmetic for the state: value = hi + lo with |lo| <= ulp(hi)/2,
+// about 2^-48 relative. Knuth's TwoSum, the FMA TwoProduct and Dekker's
+// normalisation (published error-free transformations); the operations are
+// written with round-to-nearest intrinsics so that no FMA contraction alters
+// them. The state lives in FP32 pipes this way: GB300's FP64 rate is 1/58 of
+// its FP32 rate.
+// ---------------------------------------------------------------------------
+struct dfl {
+  float hi, lo;
+};
+struct dfc {
+  dfl re, im;
+};
+__device__ __forceinline__ dfl df_fast(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ dfl df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+  const dfl s = df_two_sum(a.hi, b.hi);
+  return df_fast(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  return df_fast(p, e);
+}
+__device__ __forceinline__ dfl df_mulf(dfl a, float b) {
+  const float p = __fmul_rn(a.hi, b);
+  return df_fast(p, fmaf(a.lo, b, fmaf(a.hi, b, -p)));
+}
+__device__ __forceinline__ dfl df_neg(dfl a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ dfc dfc_mul(dfc a, dfc b) {
+  return {df_add(df_mul(a.re, b.re), df_neg(df_mul(a.im, b.im))), df_add(df_mul(a.re, b.im), df_mul(a.im, b.re))};
+}
+__device__ __forceinline__ dfc dfc_ld(float4 q) { return {{q.x, q.y}, {q.z, q.w}}; }
+__device__ __forceinline__ float4 dfc_st(dfc a) { return make_float4(a.re.hi, a.re.lo, a.im.hi, a.im.lo); }
+__device__ __forceinline__ dfl df_from(double x) {
+  const float hi = __double2float_rn(x);
+  return {hi, __double2float_rn(x - (double)hi)};
+}
+__device__ __forceinline__ double df_to(dfl a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ dfc dfc_from(double2 x) { return {df_from(x.x), df_from(x.y)}; }
+
+// FP64 phase -> double-float (once per step, dim elements)
+__global__ void kb_phase_df(const double2* phase, float4* pdf, long long dim) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < dim; e += (long long)gridDim.x * blockDim.x)
+    pdf[e] = dfc_st(dfc_from(phase[e]));
+}
+
 // S <- phase * S (optional); partial ||S_v||^2
-__global__ void kb_phase_norm(double2* S, const double2* phase, long long dim, int nb, double2* part) {
+__global__ void kb_phase_norm(float4* S, const float4* phase, long long dim, int nb, double2* part) {
   __shared__ double2 sh[8][32];
   const int v = blockIdx.y * 32 + threadIdx.x;
   const Chunk ch = chunk_of(dim);
-  double acc = 0.0;
+  dfl acc = {0.f, 0.f};
   for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
-    double2 s = S[e * nb + v];
+    dfc s = dfc_ld(S[e * nb + v]);
     if (phase) {
-      s = cmul(s, __ldg(phase + e));
-      S[e * nb + v] = s;
+      s = dfc_mul(s, dfc_ld(__ldg(phase + e)));
+      S[e * nb + v] = dfc_st(s);
     }
-    acc += cabs2(s);
+    acc = df_add(acc, df_add(df_mul(s.re, s.re), df_mul(s.im, s.im)));
   }
-  const double2 t = warps_sum(make_double2(acc, 0.0), sh);
+  const double2 t = warps_sum(make_double2(df_to(acc), 0.0), sh);
   if (threadIdx.y == 0) part[(long long)blockIdx.x * nb + v] = t;
 }
 
@@ -154,7 +211,7 @@ __global__ void kb_reduce(const double2* part, int ncoef, int nb, int stride_coe
 }
 
 // norm0 = ||S||, V0 = S / norm0 (complex64); resets the per-vector state
-__global__ void kb_start(const double2* S, float2* V0, const double2* nsq, double* norm0, int* active, int* kconv,
+__global__ void kb_start(const float4* S, float2* V0, const double2* nsq, double* norm0, int* active, int* kconv,
                          double* vscale, long long dim, int nb, int nvec) {
   const int v = blockIdx.y * 32 + threadIdx.x;
   const double n0 = sqrt(nsq[v].x);
@@ -165,10 +222,12 @@ __global__ void kb_start(const double2* S, float2* V0, const double2* nsq, doubl
     kconv[v] = 0;
     vscale[v] = 1.0;
   }
+  const dfl invd = df_from(inv);
   const Chunk ch = chunk_of(dim);
   for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
-    const double2 s = S[e * nb + v];
-    V0[e * nb + v] = make_float2((float)(s.x * inv), (float)(s.y * inv));
+    const dfc s = dfc_ld(S[e * nb + v]);
+    const dfl re = df_mul(s.re, invd), im = df_mul(s.im, invd);
+    V0[e * nb + v] = make_float2(__fadd_rn(re.hi, re.lo), __fadd_rn(im.hi, im.lo));
   }
 }
 
@@ -298,36 +357,37 @@ __global__ void kb_scale(float2* Vn, const double* vscale, const int* active, lo
   }
 }
 
-// S <- phase * (c_0 S + ||v|| sum_{i>=1} c_i V_i)   (FP64)
-__global__ void kb_combine(BatchDev b, const double2* phase) {
+// S <- phase * (c_0 S + ||v|| sum_{i>=1} c_i V_i)   (double-float state; the
+// complex64 Krylov corrections summed in FP32)
+__global__ void kb_combine(BatchDev b, const float4* phase) {
   const int v = blockIdx.y * 32 + threadIdx.x;
   const int nb = b.nb;
   const int K = b.kconv[v];
   if (K == 0) return;  // no Krylov step (zero vector or padding)
-  double2 cc[KB_NK_MAX];
-  for (int i = 0; i < K; ++i) cc[i] = b.c[(long long)i * nb + v];
-  const double n0 = b.norm0[v];
+  float2 cf[KB_NK_MAX];
+  for (int i = 1; i < K; ++i) cf[i] = make_float2((float)b.c[(long long)i * nb + v].x, (float)b.c[(long long)i * nb + v].y);
+  const dfc c0 = dfc_from(b.c[v]);
+  const dfl n0 = df_from(b.norm0[v]);
   const Chunk ch = chunk_of(b.dim);
   for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
     float2 sacc = make_float2(0.f, 0.f);
     for (int i = 1; i < K; ++i) {
       const float2 a = b.V[((long long)i * b.dim + e) * nb + v];
-      const float2 ci = make_float2((float)cc[i].x, (float)cc[i].y);
-      sacc.x = fmaf(ci.x, a.x, sacc.x);
-      sacc.x = fmaf(-ci.y, a.y, sacc.x);
-      sacc.y = fmaf(ci.x, a.y, sacc.y);
-      sacc.y = fmaf(ci.y, a.x, sacc.y);
+      sacc.x = fmaf(cf[i].x, a.x, sacc.x);
+      sacc.x = fmaf(-cf[i].y, a.y, sacc.x);
+      sacc.y = fmaf(cf[i].x, a.y, sacc.y);
+      sacc.y = fmaf(cf[i].y, a.x, sacc.y);
     }
-    double2 u = cmul(cc[0], b.S[e * nb + v]);
-    u.x = fma(n0, (double)sacc.x, u.x);
-    u.y = fma(n0, (double)sacc.y, u.y);
-    if (phase) u = cmul(u, __ldg(phase + e));
-    b.S[e * nb + v] = u;
+    dfc u = dfc_mul(c0, dfc_ld(b.S[e * nb + v]));
+    u.re = df_add(u.re, df_mulf(n0, sacc.x));
+    u.im = df_add(u.im, df_mulf(n0, sacc.y));
+    if (phase) u = dfc_mul(u, dfc_ld(__ldg(phase + e)));
+    b.S[e * nb + v] = dfc_st(u);
   }
 }
 
 // (nvec, dim) row-major <-> [dim][nb] vector-minor, tiled through shared memory
-__global__ void kb_transpose_in(const double2* src, double2* S, long long dim, int nvec, int nb) {
+__global__ void kb_transpose_in(const double2* src, float4* S, long long dim, int nvec, int nb) {
   __shared__ double2 tile[32][33];
   const long long e0 = blockIdx.x * 32LL;
   const int v0 = blockIdx.y * 32;
@@ -339,16 +399,21 @@ __global__ void kb_transpose_in(const double2* src, double2* S, long long dim, i
   __syncthreads();
   for (int r = threadIdx.y; r < 32; r += 8) {
     const long long e = e0 + r;
-    if (e < dim) S[e * nb + v0 + threadIdx.x] = tile[threadIdx.x][r];
+    if (e < dim) S[e * nb + v0 + threadIdx.x] = dfc_st(dfc_from(tile[threadIdx.x][r]));
   }
 }
-__global__ void kb_transpose_out(const double2* S, double2* dst, long long dim, int nvec, int nb) {
+__global__ void kb_transpose_out(const float4* S, double2* dst, long long dim, int nvec, int nb) {
   __shared__ double2 tile[32][33];
   const long long e0 = blockIdx.x * 32LL;
   const int v0 = blockIdx.y * 32;
   for (int r = threadIdx.y; r < 32; r += 8) {
     const long long e = e0 + r;
-    tile[r][threadIdx.x] = (e < dim) ? S[e * nb + v0 + threadIdx.x] : make_double2(0.0, 0.0);
+    if (e < dim) {
+      const dfc s = dfc_ld(S[e * nb + v0 + threadIdx.x]);
+      tile[r][threadIdx.x] = make_double2(df_to(s.re), df_to(s.im));
+    } else {
+      tile[r][threadIdx.x] = make_double2(0.0, 0.0);
+    }
   }
   __syncthreads();
   for (int r = threadIdx.y; r < 32; r += 8) {
@@ -358,26 +423,28 @@ __global__ void kb_transpose_out(const double2* S, double2* dst, long long dim, 
   }
 }
 
-// complex64 copy of the FP64 state (input of the observable mat-vec)
-__global__ void kb_to_f32(const double2* S, float2* X, long long n) {
+// complex64 copy of the state (input of the observable mat-vec)
+__global__ void kb_to_f32(const float4* S, float2* X, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const double2 s = S[i];
-    X[i] = make_float2((float)s.x, (float)s.y);
+    const float4 s = S[i];
+    X[i] = make_float2(__fadd_rn(s.x, s.y), __fadd_rn(s.z, s.w));
   }
 }
 
-// partial <S_v | Y_v> with Y in complex64 (FP64 accumulation)
-__global__ void kb_expect_dots(const double2* S, const float2* Y, long long dim, int nb, double2* part) {
+// partial <S_v | Y_v> with Y in complex64 (double-float accumulation)
+__global__ void kb_expect_dots(const float4* S, const float2* Y, long long dim, int nb, double2* part) {
   __shared__ double2 sh[8][32];
   const int v = blockIdx.y * 32 + threadIdx.x;
   const Chunk ch = chunk_of(dim);
-  double2 acc = make_double2(0.0, 0.0);
+  dfl ar = {0.f, 0.f}, ai = {0.f, 0.f};
   for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
-    const double2 s = S[e * nb + v];
+    const dfc s = dfc_ld(S[e * nb + v]);
     const float2 y = Y[e * nb + v];
-    acc = cadd(acc, cconjmul(s, make_double2(y.x, y.y)));
+    // conj(s) y = (s.re y.x + s.im y.y) + i (s.re y.y - s.im y.x)
+    ar = df_add(ar, df_add(df_mulf(s.re, y.x), df_mulf(s.im, y.y)));
+    ai = df_add(ai, df_add(df_mulf(s.re, y.y), df_neg(df_mulf(s.im, y.x))));
   }
-  const double2 t = warps_sum(acc, sh);
+  const double2 t = warps_sum(make_double2(df_to(ar), df_to(ai)), sh);
   if (threadIdx.y == 0) part[(long long)blockIdx.x * nb + v] = t;
 }
 
@@ -1179,6 +1246,7 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
 #define BA(count, ptr) \
   if ((rc = balloc(b, (count), (ptr))) != KR_OK) { kr_batch_destroy(b); return rc; }
   BA(dim * nb, &b->S);
+  BA(dim, &b->phase_df);
   BA(m1 * dim * nb, &b->V);
   BA(dim * nb, &b->W);
   BA(nb, &b->norm0);
@@ -1255,7 +1323,14 @@ extern "C" int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double f
   kr_ctx* ctx = op->ctx;
   KR_CUDA(ctx, cudaMemsetAsync(b->counts, 0, 3 * sizeof(int), st));
   // S <- phase * S, norms, V_0
-  kb_phase_norm<<<eg, eb, 0, st>>>(b->S, (const double2*)phase, dim, nb, b->part);
+  const float4* pdf = nullptr;
+  if (phase) {
+    kb_phase_df<<<(int)std::min<long long>((dim + 255) / 256, 1024), 256, 0, st>>>((const double2*)phase, b->phase_df,
+                                                                                dim);
+    b->launches++;
+    pdf = b->phase_df;
+  }
+  kb_phase_norm<<<eg, eb, 0, st>>>(b->S, pdf, dim, nb, b->part);
   kb_reduce<<<(nb + 255) / 256, 256, 0, st>>>(b->part, 1, nb, 1, b->h);
   kb_start<<<eg, eb, 0, st>>>(b->S, b->V, b->h, b->norm0, b->active, b->kconv, b->vscale, dim, nb, b->nvec);
   b->launches += 3;
@@ -1286,7 +1361,7 @@ extern "C" int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double f
                          std::to_string(b->mmax) + " Krylov vectors");
     if (counts[0] == 0) break;
   }
-  kb_combine<<<eg, eb, 0, st>>>(dev_view(b), (const double2*)phase);
+  kb_combine<<<eg, eb, 0, st>>>(dev_view(b), pdf);
   b->launches++;
   KR_CUDA(ctx, cudaGetLastError());
   if (kmax_out) *kmax_out = kused;
