@@ -263,7 +263,7 @@ __global__ void kb_update(float2* V, const float2* W, const double2* h, const in
   const int v = blockIdx.y * 32 + threadIdx.x;
   const Chunk ch = chunk_of(dim);
   const bool act = active[v] != 0;
-  double nacc = 0.0;
+  dfl nacc = {0.f, 0.f};
   if (act) {
     float2 hv[KB_NK_MAX];
     const int kk = min(k, KB_NK_MAX - 1);
@@ -282,10 +282,10 @@ __global__ void kb_update(float2* V, const float2* W, const double2* h, const in
         r.y = fmaf(-hv[j].y, a.x, r.y);
       }
       Vn[e * nb + v] = r;
-      nacc += (double)r.x * r.x + (double)r.y * r.y;
+      nacc = df_add(nacc, df_add(df_mulf({r.x, 0.f}, r.x), df_mulf({r.y, 0.f}, r.y)));
     }
   }
-  const double2 t = warps_sum(make_double2(nacc, 0.0), sh);
+  const double2 t = warps_sum(make_double2(df_to(nacc), 0.0), sh);
   if (threadIdx.y == 0) part[(long long)blockIdx.x * nb + v] = t;
 }
 
