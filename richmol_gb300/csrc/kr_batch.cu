@@ -638,15 +638,21 @@ __device__ void kb_tile(const BatchMV& p, int s1, int i0, int nr, float* smem) {
     const int mfi = __ldg(op.t_mf + term);
     const int nk2 = __ldg(op.in_dk + s2);
     const int dm2 = __ldg(op.in_dm + s2);
-    const int W = __ldg(op.mf_width + mfi);
-    const int d0 = __ldg(op.mf_diag + mfi);
-    const bool dia = d0 != KR_NO_DIAG && W <= KR_DIAG_MAX;
+    const int Wst = __ldg(op.mf_width + mfi);  // stored width (row stride of MF)
+    const int d0s = __ldg(op.mf_diag + mfi);
+    const bool dia = d0s != KR_NO_DIAG && Wst <= KR_DIAG_MAX;
+    // slots that carry a value with the current field (the field kernel's band)
+    const int bhi = __ldcg(op.mf_band + 2 * mfi + 1);
+    if (bhi < 0) continue;  // MF is zero with this field: no contribution (uniform)
+    const int wlo = dia ? Wst - 1 - __ldcg(op.mf_band + 2 * mfi) : 0;
+    const int W = dia ? bhi - wlo + 1 : Wst;
+    const int d0 = dia ? d0s + wlo : 0;
     const int ktype = __ldg(op.k_type + kb);
     const int mtype = __ldcg(op.mf_type + mfi);
     const int kw = (ktype == 0) ? 2 : 1;
     const float* KT = op.k_f32 + __ldg(op.k_off + kb);
     const int* col = op.m_col + __ldg(op.mf_col_off + mfi);
-    const float2* mf = op.mf_f32 + __ldg(op.mf_off + mfi);
+    const float2* mf = op.mf_f32 + __ldg(op.mf_off + mfi) + wlo;
     __syncthreads();  // the previous term is done with Ks, MFs, Cs, Ts
     // K^T as [plane][b][a], zero outside nk2 x nk1 (rows up to the next multiple of 4)
     const int nb4 = (nk2 + 3) & ~3;
@@ -659,14 +665,14 @@ __device__ void kb_tile(const BatchMV& p, int s1, int i0, int nr, float* smem) {
     }
     for (int e = tid; e < nr * W; e += blockDim.x) {
       const int r = e / W, w = e - r * W;
-      const long long src = (long long)(i0 + r) * W + w;
+      const long long src = (long long)(i0 + r) * Wst + w;
       MFs[r * KB_WMAX + w] = __ldcg(mf + src);
       if (!dia) Cs[r * KB_WMAX + w] = __ldg(col + src);
     }
     if (!dia && wid == 0) {
       int lo = 0x7fffffff, hi = -1;
       for (int e = lane; e < nr * W; e += 32) {
-        const int c = __ldg(col + (long long)(i0 + e / W) * W + (e % W));
+        const int c = __ldg(col + (long long)(i0 + e / W) * Wst + (e % W));
         lo = min(lo, c);
         hi = max(hi, c);
       }
@@ -853,8 +859,8 @@ __device__ __forceinline__ void kbt_mstep(float2 (&z)[64 / KP][KP / 2], KbtWin<K
 
 // one term of a tensor-core tile: its tables and shared-memory staging
 struct KbtTerm {
-  int s2, nk2, dm2, W, d0, ktype, mtype;
-  bool dia, ok;
+  int s2, nk2, dm2, W, Wst, d0, ktype, mtype;
+  bool dia, ok, empty;
   const float* KT;
   const int* col;
   const float2* mf;
@@ -868,15 +874,21 @@ __device__ __forceinline__ KbtTerm kbt_term(const DevOp& op, const BatchTC& p, i
   const int mfi = __ldg(op.t_mf + term);
   t.nk2 = __ldg(op.in_dk + t.s2);
   t.dm2 = __ldg(op.in_dm + t.s2);
-  t.W = __ldg(op.mf_width + mfi);
-  t.d0 = __ldg(op.mf_diag + mfi);
-  t.dia = t.d0 != KR_NO_DIAG && t.W <= KR_DIAG_MAX;
+  t.Wst = __ldg(op.mf_width + mfi);
+  const int d0s = __ldg(op.mf_diag + mfi);
+  t.dia = d0s != KR_NO_DIAG && t.Wst <= KR_DIAG_MAX;
+  // slots that carry a value with the current field (the field kernel's band)
+  const int bhi = __ldcg(op.mf_band + 2 * mfi + 1);
+  t.empty = bhi < 0;
+  const int wlo = (t.dia && !t.empty) ? t.Wst - 1 - __ldcg(op.mf_band + 2 * mfi) : 0;
+  t.W = (t.dia && !t.empty) ? bhi - wlo + 1 : t.Wst;
+  t.d0 = t.dia ? d0s + wlo : 0;
   t.ktype = __ldg(op.k_type + kb);
   t.mtype = __ldcg(op.mf_type + mfi);
-  t.ok = t.nk2 <= KP && t.W <= KB_WMAX;
+  t.ok = t.nk2 <= KP && t.Wst <= KB_WMAX;
   t.KT = op.k_f32 + __ldg(op.k_off + kb);
   t.col = op.m_col + __ldg(op.mf_col_off + mfi);
-  t.mf = op.mf_f32 + __ldg(op.mf_off + mfi);
+  t.mf = op.mf_f32 + __ldg(op.mf_off + mfi) + wlo;
   t.Xs2 = p.X + (long long)__ldg(op.in_off + t.s2) * nb + v;
   return t;
 }
@@ -911,7 +923,7 @@ __device__ __forceinline__ void kbt_stage(const KbtTerm& t, int nk1, int NP, int
   const int W = t.W;
   for (int e = tid; e < nr * W; e += 256) {
     const int r = e / W, w = e - (e / W) * W;
-    const long long src = (long long)(i0 + r) * W + w;
+    const long long src = (long long)(i0 + r) * t.Wst + w;
     MFs[r * KB_WMAX + w] = __ldcg(t.mf + src);
     if (!t.dia) Cs[r * KB_WMAX + w] = __ldg(t.col + src);
   }
@@ -925,7 +937,7 @@ __device__ __forceinline__ void kbt_zstep(float2 (&z)[64 / KP][KP / 2], KbtWin<K
   for (int r = 0; r < R; ++r)
 #pragma unroll
     for (int q = 0; q < BH; ++q) z[r][q] = make_float2(0.f, 0.f);
-  if (!t.ok) return;
+  if (!t.ok || t.empty) return;
   if (t.mtype == 1) kbt_mstep<KP, 1>(z, xw, true, t.Xs2, nb, t.nk2, t.dm2, i0, nr, t.d0, t.W, b0, MFs, Cs, t.dia);
   else if (t.mtype == 2) kbt_mstep<KP, 2>(z, xw, true, t.Xs2, nb, t.nk2, t.dm2, i0, nr, t.d0, t.W, b0, MFs, Cs, t.dia);
   else kbt_mstep<KP, 0>(z, xw, true, t.Xs2, nb, t.nk2, t.dm2, i0, nr, t.d0, t.W, b0, MFs, Cs, t.dia);
@@ -1034,6 +1046,7 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
         const int nk2 = __ldg(op.in_dk + s2);
         const int W = __ldg(op.mf_width + __ldg(op.t_mf + term));
         if (!(nk2 <= KP && W <= KB_WMAX)) continue;
+        if (__ldcg(op.mf_band + 2 * __ldg(op.t_mf + term) + 1) < 0) continue;  // MF zero with this field
         const int ktype = __ldg(op.k_type + __ldg(op.t_k + term));
         if (!tc_mbar_wait(full, (uint32_t)ncommit & 1u)) ok = false;
         tc_fence_after();
@@ -1054,7 +1067,7 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
   float2 z[R][BH];
   KbtWin<KP> xw;
   KbtTerm cur = kbt_term(op, p, tb, KP, v, nb);
-  if (cur.ok && cur.dia) xw.load(cur.Xs2, nb, cur.nk2, cur.dm2, i0 + cur.d0, nr + cur.W - 1, b0);
+  if (cur.ok && !cur.empty && cur.dia) xw.load(cur.Xs2, nb, cur.nk2, cur.dm2, i0 + cur.d0, nr + cur.W - 1, b0);
   kbt_stage<KP>(cur, nk1, NP, i0, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, tid);
   kbt_producer_sync();
   kbt_zstep<KP>(z, xw, cur, nb, i0, nr, b0, MFs0, Cs0);
@@ -1064,12 +1077,12 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
     KbtTerm nxt;
     if (has_next) {
       nxt = kbt_term(op, p, term + 1, KP, v, nb);
-      if (nxt.ok && nxt.dia) xw.load(nxt.Xs2, nb, nxt.nk2, nxt.dm2, i0 + nxt.d0, nr + nxt.W - 1, b0);
+      if (nxt.ok && !nxt.empty && nxt.dia) xw.load(nxt.Xs2, nb, nxt.nk2, nxt.dm2, i0 + nxt.d0, nr + nxt.W - 1, b0);
     }
     // the MMAs of the previous committed term are done with the A tiles and its B buffer
     if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
     tc_fence_after();
-    if (cur.ok) {
+    if (cur.ok && !cur.empty) {
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         if (r >= nr) continue;
@@ -1099,7 +1112,7 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
       tc_fence_proxy();
       asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc_smem_u32(full)) : "memory");
       ++ncommit;
-    } else if (tid == 0) {
+    } else if (!cur.ok && tid == 0) {
       atomicExch(p.err, KR_ERR_ARG);  // outside the tile shape: skipped
     }
     if (has_next) {

@@ -56,6 +56,7 @@ struct DevOp {
   // terms grouped by output slab
   const int* term_ptr; const int* t_in; const int* t_k; const int* t_mf;
   const int* mf_type;   // per MF instance: 0 complex, 1 real, 2 imaginary (set with the field)
+  const int* mf_band;   // per MF instance: [W - 1 - lowest, highest] non-zero slot, -1 if none (set with the field)
   // row tasks, handed out dynamically in the order task_order
   const int* task_slab; const int* task_row0; const int* task_nrows;
   const int* task_order; int ntask;

@@ -28,6 +28,7 @@ struct DevField {
   const double2* m_val;
   double2* mf_val;
   float2* mf_f32;
+  int* mf_band;                 // out: per MF instance [W - 1 - lowest, highest] slot with a non-zero value (-1: none)
 };
 
 struct kr_ctx {

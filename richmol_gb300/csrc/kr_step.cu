@@ -75,6 +75,12 @@ __global__ void __launch_bounds__(256) kr_field_kernel(DevField f, FieldCoef c) 
     const double2 mfv = cmul(c.scale[p], v);
     f.mf_val[e] = mfv;
     f.mf_f32[e] = make_float2((float)mfv.x, (float)mfv.y);
+    if (mfv.x != 0.0 || mfv.y != 0.0) {  // band of slots that carry a value with this field
+      const int W = __ldg(f.m_width + g);
+      const int w = (int)(local % W);
+      atomicMax(f.mf_band + 2 * inst, W - 1 - w);
+      atomicMax(f.mf_band + 2 * inst + 1, w);
+    }
   }
 }
 
@@ -900,10 +906,12 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   unsigned* p_u;
   UP((const unsigned*)nullptr, (size_t)KR_MATVEC_MAXVEC, &p_u); op->mv_counters = p_u;
   UP((const int*)nullptr, (size_t)std::max(1, d->nmf), &p_i); D.mf_type = p_i;
+  UP((const int*)nullptr, (size_t)2 * std::max(1, d->nmf), &p_i); D.mf_band = p_i;
   D.zmax = zmax;
 
   DevField& F = op->field;
   F.nent = nent;
+  F.mf_band = const_cast<int*>(D.mf_band);
   UP(ent_inst.data(), nent, &p_i); F.ent_inst = p_i;
   F.inst_ptr = D.mf_off;
   UP(d->mf_group, d->nmf, &p_i); F.mf_group = p_i;
@@ -957,6 +965,8 @@ extern "C" int kr_set_field(kr_op* op, const double* coef, const double* scale, 
     c.thresh[p] = thresh[p];
   }
   if (op->field.nent == 0 && op->field.nmf == 0) return KR_OK;
+  KR_CUDA(op->ctx, cudaMemsetAsync(op->field.mf_band, 0xFF, sizeof(int) * 2 * std::max(1, op->field.nmf),
+                                   (cudaStream_t)stream));
   const int threads = 256;
   const long long work = std::max<long long>(op->field.nent, op->field.nmf);
   const int blocks = (int)std::max<long long>(1, std::min<long long>((work + threads - 1) / threads, 4LL * op->ctx->nsm));
