@@ -21,8 +21,11 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <string>
 #include <vector>
+
+#include <cuda.h>
 
 #include "kr_internal.cuh"
 #include "kr_tc.cuh"
@@ -897,7 +900,7 @@ __device__ __forceinline__ KbtTerm kbt_term(const DevOp& op, const BatchTC& p, i
 // each hi and lo; zero outside n_k1 x n_k2. MF rows (and ELL columns).
 template <int KP>
 __device__ __forceinline__ void kbt_stage(const KbtTerm& t, int nk1, int NP, int i0, int nr, float* Bt, float2* MFs,
-                                          int* Cs, int tid) {
+                                          int* Cs, int tid, int bpart = TC_BPART) {
   for (int e = tid; e < NP * KP; e += 256) {  // producers only
     const int a = e / KP, b = e - (e / KP) * KP;
     float kr = 0.f, ki = 0.f;
@@ -913,12 +916,12 @@ __device__ __forceinline__ void kbt_stage(const KbtTerm& t, int nk1, int NP, int
     }
     const uint32_t o = tc_kmajor_off(a, b, KP) >> 2;
     const float krh = tc_tf32(kr), kih = tc_tf32(ki);
-    Bt[0 * (TC_BPART / 4) + o] = krh;
-    Bt[1 * (TC_BPART / 4) + o] = kr - krh;
-    Bt[2 * (TC_BPART / 4) + o] = kih;
-    Bt[3 * (TC_BPART / 4) + o] = ki - kih;
-    Bt[4 * (TC_BPART / 4) + o] = -kih;
-    Bt[5 * (TC_BPART / 4) + o] = -(ki - kih);
+    Bt[0 * (bpart / 4) + o] = krh;
+    Bt[1 * (bpart / 4) + o] = kr - krh;
+    Bt[2 * (bpart / 4) + o] = kih;
+    Bt[3 * (bpart / 4) + o] = ki - kih;
+    Bt[4 * (bpart / 4) + o] = -kih;
+    Bt[5 * (bpart / 4) + o] = -(ki - kih);
   }
   const int W = t.W;
   for (int e = tid; e < nr * W; e += 256) {
@@ -951,7 +954,7 @@ __device__ __forceinline__ void kbt_producer_sync() { asm volatile("bar.sync 1, 
 // (A hi B hi, A hi B lo, A lo B hi); zero parts of K skipped
 template <int KP>
 __device__ __forceinline__ void kbt_issue(uint32_t tmem, uint64_t adesc0, uint64_t bdesc, uint32_t idesc, int NP,
-                                          int nr, int ktype, int nk2, uint32_t& dinit) {
+                                          int nr, int ktype, int nk2, uint32_t& dinit, int bpart = TC_BPART) {
   constexpr int ATILE = 128 * KP;
   int pd[4], pa[4], pb[4];
   int np = 0;
@@ -970,11 +973,11 @@ __device__ __forceinline__ void kbt_issue(uint32_t tmem, uint64_t adesc0, uint64
       const uint32_t dcol = tmem + (uint32_t)((2 * r + pd[q]) * NP);
       const uint32_t dbit = 1u << (2 * r + pd[q]);
       const uint64_t ad = adesc0 + (uint64_t)(((r * 4 + pa[q]) * ATILE * 4) >> 4);
-      const uint64_t bd = bdesc + (uint64_t)((pb[q] * TC_BPART) >> 4);
+      const uint64_t bd = bdesc + (uint64_t)((pb[q] * bpart) >> 4);
 #pragma unroll
       for (int sp = 0; sp < 3; ++sp) {
         const uint64_t a2 = ad + (sp == 2 ? (uint64_t)((ATILE * 4) >> 4) : 0);
-        const uint64_t b2 = bd + (sp == 1 ? (uint64_t)(TC_BPART >> 4) : 0);
+        const uint64_t b2 = bd + (sp == 1 ? (uint64_t)(bpart >> 4) : 0);
 #pragma unroll
         for (int ks = 0; ks < KP / 8; ++ks) {
           if (ks < nks) {
@@ -1035,8 +1038,8 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
   int ncommit = 0;  // terms whose MMAs were (or will be) committed
 
   if (!producer) {
-    // ---- MMA warp --------------------------------------------------------
-    if (lane == 0) {
+    // ---- MMA warp (warp 8; warp 9 idles here) ------------------------------
+    if (wid == 8 && lane == 0) {
       const uint32_t idesc = tc_idesc_tf32(128, NP);
       const uint64_t adesc0 = tc_desc(tc_smem_u32(As), 128u, 32u * KP);
       const uint64_t bdesc0 = tc_desc(tc_smem_u32(Bs), 128u, 32u * KP);
@@ -1059,7 +1062,7 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
     }
     tc_fence_before();
     __syncthreads();
-    tc_dealloc(tmem, ncols);
+    if (wid == 8) tc_dealloc(tmem, ncols);
     return;
   }
 
@@ -1146,7 +1149,267 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(288, 1) kb_matvec_tc(BatchTC p) {
+
+// ---------------------------------------------------------------------------
+// Tensor-core tile with the X windows streamed by TMA (KP = 8, 16). Warp 8
+// lane 1 walks the window rows of every diagonal term of the tile in order
+// and loads each (KP input rows x 128 vectors, KP/8 boxes of 8 rows) into a
+// ring of shared-memory slots (full: tx bytes; empty: one arrival per
+// producer warp); the producer warps read X from the ring, so no global-load
+// latency sits in their M step. Rows outside the input slab read whatever
+// lies there (finite data of other slabs, or zeros beyond the array) and meet
+// zero MF slots; columns beyond n_k2 are zeroed on read. Terms stored as ELL
+// load X directly. Everything else as in kbt_tile.
+// ---------------------------------------------------------------------------
+template <int KP>
+struct KbtRing {
+  static constexpr int NSLOT = 64 / KP;          // slots of KP rows x 128 vectors x 8 bytes
+  static constexpr int SLOT = KP * 1024;
+  static constexpr int BPART = 128 * KP;         // one B part: NP (<= 32) x KP FP32
+  static constexpr int BBUF = 6 * BPART;
+  static constexpr int OFF_B = TC_ABYTES;
+  static constexpr int OFF_RING = OFF_B + 2 * BBUF;
+  static constexpr int OFF_MF = OFF_RING + NSLOT * SLOT;
+  static constexpr int OFF_CS = OFF_MF + TC_MFBYTES;
+  static constexpr int OFF_BAR = OFF_CS + TC_CSBYTES;
+  static constexpr int TOTAL = OFF_BAR + 8 * (2 + 2 * NSLOT) + 16;
+};
+constexpr int TC_SMEM_RING = KbtRing<16>::TOTAL > KbtRing<8>::TOTAL ? KbtRing<16>::TOTAL : KbtRing<8>::TOTAL;
+
+// the ring rows of one term: count, and the first input row (diagonal terms only)
+__device__ __forceinline__ int kbt_ring_rows(const KbtTerm& t, int nr) {
+  return (t.ok && !t.empty && t.dia) ? nr + t.W - 1 : 0;
+}
+
+// M step of a diagonal term from the ring; g: ring row counter (advanced)
+template <int KP, int MT>
+__device__ __forceinline__ bool kbt_mdia_ring(float2 (&z)[64 / KP][KP / 2], const char* ring, uint64_t* rfull,
+                                              uint64_t* rempty, int& g, int nwin, int nr, int W, int nk2, int b0,
+                                              int vloc, int lane, const float2* MFs) {
+  constexpr int R = 64 / KP, BH = KP / 2, NSLOT = KbtRing<KP>::NSLOT;
+  bool ok = true;
+  for (int c = 0; c < nwin; ++c, ++g) {
+    const int slot = g % NSLOT;
+    if (!tc_mbar_wait(rfull + slot, (uint32_t)(g / NSLOT) & 1u)) ok = false;
+    const float2* xs = reinterpret_cast<const float2*>(ring + (size_t)slot * KbtRing<KP>::SLOT) + vloc;
+    float2 x[BH];
+#pragma unroll
+    for (int q = 0; q < BH; ++q) x[q] = (b0 + q < nk2) ? xs[(b0 + q) * 128] : make_float2(0.f, 0.f);
+    __syncwarp();
+    if (lane == 0) tc_mbar_arrive(rempty + slot);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int w = c - r;
+      if (w >= 0 && w < W && r < nr) {
+        const float2 m = MFs[r * KB_WMAX + w];
+#pragma unroll
+        for (int q = 0; q < BH; ++q) macc<MT>(z[r][q], m, x[q]);
+      }
+    }
+  }
+  return ok;
+}
+
+template <int KP>
+__device__ __forceinline__ bool kbt_zstep_ring(float2 (&z)[64 / KP][KP / 2], const KbtTerm& t, long long nb, int nr,
+                                               int b0, int vloc, int lane, const float2* MFs, const int* Cs,
+                                               const char* ring, uint64_t* rfull, uint64_t* rempty, int& g) {
+  constexpr int R = 64 / KP, BH = KP / 2;
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int q = 0; q < BH; ++q) z[r][q] = make_float2(0.f, 0.f);
+  if (!t.ok || t.empty) return true;
+  const int nwin = kbt_ring_rows(t, nr);
+  if (t.dia) {
+    if (t.mtype == 1) return kbt_mdia_ring<KP, 1>(z, ring, rfull, rempty, g, nwin, nr, t.W, t.nk2, b0, vloc, lane, MFs);
+    if (t.mtype == 2) return kbt_mdia_ring<KP, 2>(z, ring, rfull, rempty, g, nwin, nr, t.W, t.nk2, b0, vloc, lane, MFs);
+    return kbt_mdia_ring<KP, 0>(z, ring, rfull, rempty, g, nwin, nr, t.W, t.nk2, b0, vloc, lane, MFs);
+  }
+  if (t.mtype == 1) kbt_mell<KP, 1>(z, t.Xs2, nb, t.nk2, nr, t.W, b0, MFs, Cs);
+  else if (t.mtype == 2) kbt_mell<KP, 2>(z, t.Xs2, nb, t.nk2, nr, t.W, b0, MFs, Cs);
+  else kbt_mell<KP, 0>(z, t.Xs2, nb, t.nk2, nr, t.W, b0, MFs, Cs);
+  return true;
+}
+
+template <int KP>
+__device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1, int i0, int nr, char* smem) {
+  using L = KbtRing<KP>;
+  constexpr int R = 64 / KP, BH = KP / 2, NSLOT = L::NSLOT;
+  constexpr int ATILE = 128 * KP;  // floats of one A tile
+  const DevOp& op = p.op;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const bool producer = wid < 8;
+  const int vq = wid & 3, b0 = ((wid >> 2) & 1) * BH;
+  const int vloc = vq * 32 + lane;
+  const long long nb = p.nb;
+  const int v = blockIdx.y * 128 + vloc;
+  float* As = reinterpret_cast<float*>(smem);
+  char* Bs = smem + L::OFF_B;
+  char* ring = smem + L::OFF_RING;
+  float2* MFs0 = reinterpret_cast<float2*>(smem + L::OFF_MF);  // [2][8][KB_WMAX]
+  int* Cs0 = reinterpret_cast<int*>(smem + L::OFF_CS);         // [2][8][KB_WMAX]
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);
+  uint64_t* empty = full + 1;
+  uint64_t* rfull = full + 2;
+  uint64_t* rempty = rfull + NSLOT;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(rempty + NSLOT);
+  const int nk1 = __ldg(op.out_dk + s1);
+  const int NP = nk1 <= 16 ? 16 : 32;
+  float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * nk1) * nb + v;
+  const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
+  if (te == tb) {  // no term reaches this slab
+    if (producer)
+      for (int e = wid >> 2; e < nr * nk1; e += 2) Y[(long long)e * nb] = make_float2(0.f, 0.f);
+    return;
+  }
+  uint32_t ncols = 32;
+  while (ncols < (uint32_t)(2 * R * NP)) ncols <<= 1;
+  if (wid == 8) tc_alloc(tslot, ncols);
+  if (tid == 256) {
+    tc_mbar_init(full, 256);
+    tc_mbar_init(empty, 1);
+    for (int i = 0; i < NSLOT; ++i) {
+      tc_mbar_init(rfull + i, 1);
+      tc_mbar_init(rempty + i, 8);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  bool ok = true;
+  int ncommit = 0;  // terms whose MMAs were (or will be) committed
+
+  if (!producer) {
+    if (wid == 8 && lane == 0) {
+      // ---- MMA issue -------------------------------------------------------
+      const uint32_t idesc = tc_idesc_tf32(128, NP);
+      const uint64_t adesc0 = tc_desc(tc_smem_u32(As), 128u, 32u * KP);
+      const uint64_t bdesc0 = tc_desc(tc_smem_u32(Bs), 128u, 32u * KP);
+      uint32_t dinit = 0;
+      for (int term = tb; term < te; ++term) {
+        const int s2 = __ldg(op.t_in + term);
+        const int nk2 = __ldg(op.in_dk + s2);
+        const int W = __ldg(op.mf_width + __ldg(op.t_mf + term));
+        if (!(nk2 <= KP && W <= KB_WMAX)) continue;
+        if (__ldcg(op.mf_band + 2 * __ldg(op.t_mf + term) + 1) < 0) continue;  // MF zero with this field
+        const int ktype = __ldg(op.k_type + __ldg(op.t_k + term));
+        if (!tc_mbar_wait(full, (uint32_t)ncommit & 1u)) ok = false;
+        tc_fence_after();
+        const uint64_t bdesc = bdesc0 + (uint64_t)((((term - tb) & 1) * L::BBUF) >> 4);
+        kbt_issue<KP>(tmem, adesc0, bdesc, idesc, NP, nr, ktype, nk2, dinit, L::BPART);
+        tc_commit(empty);
+        ++ncommit;
+      }
+    } else if (wid == 9 && lane == 0) {
+      // ---- X window loads (TMA) into the ring (own warp: a waiting MMA lane
+      // would hold up a loader lane of the same warp) ------------------------
+      int g = 0;
+      for (int term = tb; term < te; ++term) {
+        const KbtTerm t = kbt_term(op, p, term, KP, v, nb);
+        const int nwin = kbt_ring_rows(t, nr);
+        const long long row0 = __ldg(op.in_off + __ldg(op.t_in + term));  // first X row of slab s2
+        for (int c = 0; c < nwin; ++c, ++g) {
+          const int slot = g % NSLOT;
+          if (g >= NSLOT && !tc_mbar_wait(rempty + slot, (uint32_t)(g / NSLOT - 1) & 1u)) ok = false;
+          tc_mbar_expect_tx(rfull + slot, (uint32_t)L::SLOT);
+          const long long y = row0 + (long long)(i0 + t.d0 + c) * t.nk2;  // first X row of the window row
+          char* dst = ring + (size_t)slot * L::SLOT;
+#pragma unroll
+          for (int h = 0; h < KP / 8; ++h)
+            tc_tma_load_2d(dst + h * 8192, xmap, blockIdx.y * 128, (int)(y + 8 * h), rfull + slot);
+        }
+      }
+    }
+    if (!ok) atomicExch(p.err, KR_ERR_TIMEOUT);
+    tc_fence_before();
+    __syncthreads();
+    if (wid == 8) tc_dealloc(tmem, ncols);
+    return;
+  }
+
+  // ---- producers -------------------------------------------------------------
+  float2 z[R][BH];
+  int g = 0;  // ring row counter
+  KbtTerm cur = kbt_term(op, p, tb, KP, v, nb);
+  kbt_stage<KP>(cur, nk1, NP, i0, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, tid, L::BPART);
+  kbt_producer_sync();
+  if (!kbt_zstep_ring<KP>(z, cur, nb, nr, b0, vloc, lane, MFs0, Cs0, ring, rfull, rempty, g)) ok = false;
+  for (int term = tb; term < te; ++term) {
+    const int buf = (term - tb) & 1;
+    const bool has_next = term + 1 < te;
+    // the MMAs of the previous committed term are done with the A tiles and its B buffer
+    if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
+    tc_fence_after();
+    if (cur.ok && !cur.empty) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (r >= nr) continue;
+        float* At = As + r * 4 * ATILE;
+#pragma unroll
+        for (int c4 = 0; c4 < BH; c4 += 4) {
+          float4 rh, rl, ih, il;
+          float* prh = &rh.x;
+          float* prl = &rl.x;
+          float* pih = &ih.x;
+          float* pil = &il.x;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float2 zz = z[r][c4 + q];
+            prh[q] = tc_tf32(zz.x);
+            prl[q] = zz.x - prh[q];
+            pih[q] = tc_tf32(zz.y);
+            pil[q] = zz.y - pih[q];
+          }
+          const uint32_t o = tc_kmajor_off(vloc, b0 + c4, KP) >> 2;
+          *reinterpret_cast<float4*>(At + 0 * ATILE + o) = rh;
+          *reinterpret_cast<float4*>(At + 1 * ATILE + o) = rl;
+          *reinterpret_cast<float4*>(At + 2 * ATILE + o) = ih;
+          *reinterpret_cast<float4*>(At + 3 * ATILE + o) = il;
+        }
+      }
+      tc_fence_proxy();
+      tc_mbar_arrive(full);
+      ++ncommit;
+    } else if (!cur.ok && tid == 0) {
+      atomicExch(p.err, KR_ERR_ARG);  // outside the tile shape: skipped
+    }
+    if (has_next) {
+      // B buffer buf ^ 1 was last read by the MMAs of term - 1 (done); MF buffer
+      // buf ^ 1 by the M step of term - 1 (every producer is past it)
+      const KbtTerm nxt = kbt_term(op, p, term + 1, KP, v, nb);
+      kbt_stage<KP>(nxt, nk1, NP, i0, nr, reinterpret_cast<float*>(Bs + (buf ^ 1) * L::BBUF),
+                    MFs0 + (buf ^ 1) * 8 * KB_WMAX, Cs0 + (buf ^ 1) * 8 * KB_WMAX, tid, L::BPART);
+      kbt_producer_sync();
+      if (!kbt_zstep_ring<KP>(z, nxt, nb, nr, b0, vloc, lane, MFs0 + (buf ^ 1) * 8 * KB_WMAX,
+                              Cs0 + (buf ^ 1) * 8 * KB_WMAX, ring, rfull, rempty, g))
+        ok = false;
+      cur = nxt;
+    }
+  }
+  if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
+  tc_fence_after();
+  // epilogue: rows r = w / 4, w / 4 + 2, ... of this warp's lane quarter
+  for (int r = wid >> 2; r < nr; r += 2) {
+    for (int c0 = 0; c0 < NP; c0 += 16) {
+      float re[16], im[16];
+      const uint32_t lanebase = (uint32_t)(vq * 32) << 16;
+      tc_ld16(tmem + lanebase + (uint32_t)(2 * r * NP + c0), re);
+      tc_ld16(tmem + lanebase + (uint32_t)((2 * r + 1) * NP + c0), im);
+      const bool any = ncommit > 0;
+#pragma unroll
+      for (int q = 0; q < 16; ++q)
+        if (c0 + q < nk1)
+          Y[((long long)r * nk1 + c0 + q) * nb] = any ? make_float2(re[q], im[q]) : make_float2(0.f, 0.f);
+    }
+  }
+  if (!ok && lane == 0) atomicExch(p.err, KR_ERR_TIMEOUT);
+  tc_fence_before();
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(320, 1) kb_matvec_tc(BatchTC p, const __grid_constant__ CUtensorMap xmap) {
   extern __shared__ __align__(1024) char kbt_smem[];
   if (p.grp_active) {
     const int* g = p.grp_active + 4 * blockIdx.y;
@@ -1157,8 +1420,8 @@ __global__ void __launch_bounds__(288, 1) kb_matvec_tc(BatchTC p) {
   const int i0 = __ldg(p.task + p.ntask + task);
   const int nr = __ldg(p.task + 2 * p.ntask + task);
   const int kp = __ldg(p.task + 3 * p.ntask + task);
-  if (kp == 8) kbt_tile<8>(p, s1, i0, nr, kbt_smem);
-  else if (kp == 16) kbt_tile<16>(p, s1, i0, nr, kbt_smem);
+  if (kp == 8) kbt_tile_ring<8>(p, &xmap, s1, i0, nr, kbt_smem);
+  else if (kp == 16) kbt_tile_ring<16>(p, &xmap, s1, i0, nr, kbt_smem);
   else kbt_tile<32>(p, s1, i0, nr, kbt_smem);
 }
 
@@ -1188,6 +1451,33 @@ int mv_groups(const kr_batch* b) { return b->nb / 32; }
 const char* const mv_error_text =
     "batched mat-vec: an MMA completion wait gave up or a term exceeded the tile shape";
 
+// TMA descriptor of an X buffer [dim][nb] (complex64 as 8-byte elements):
+// boxes of 128 vectors x 8 rows, zero fill outside the array
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+int encode_xmap(kr_ctx* ctx, const float2* X, long long dim, int nb, CUtensorMap* m) {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(f);
+  });
+  if (!fn) return set_err(ctx, KR_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  const cuuint64_t gdim[2] = {(cuuint64_t)nb, (cuuint64_t)dim};
+  const cuuint64_t gstride[1] = {(cuuint64_t)nb * sizeof(float2)};
+  const cuuint32_t box[2] = {128, 8};
+  const cuuint32_t estride[2] = {1, 1};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<float2*>(X), gdim, gstride, box, estride,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_err(ctx, KR_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return KR_OK;
+}
+
 int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool masked, cudaStream_t st) {
   if (b->mv_kind == KR_MATVEC_TENSOR && op->tc_ntask > 0) {
     BatchTC q;
@@ -1199,12 +1489,16 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
     q.ntask = op->tc_ntask;
     q.grp_active = masked ? b->grp_active : nullptr;
     q.err = b->counts + 2;
+    CUtensorMap xmap;
+    const int rc = encode_xmap(op->ctx, X, b->dim, b->nb, &xmap);
+    if (rc != KR_OK) return rc;
+    const int smem = std::max(TC_SMEM, TC_SMEM_RING);
     static bool tc_attr = false;
     if (!tc_attr) {
-      KR_CUDA(op->ctx, cudaFuncSetAttribute(kb_matvec_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+      KR_CUDA(op->ctx, cudaFuncSetAttribute(kb_matvec_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
       tc_attr = true;
     }
-    kb_matvec_tc<<<dim3(op->tc_ntask, b->nb / 128), 288, TC_SMEM, st>>>(q);
+    kb_matvec_tc<<<dim3(op->tc_ntask, b->nb / 128), 320, smem, st>>>(q, xmap);
     b->launches++;
     KR_CUDA(op->ctx, cudaGetLastError());
     return KR_OK;

@@ -113,3 +113,22 @@ __device__ __forceinline__ bool tc_mbar_wait(uint64_t* bar, uint32_t parity) {
   }
   return false;
 }
+
+// mbarrier arrival (count 1) and arrival that also expects tx bytes of async copies
+__device__ __forceinline__ void tc_mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc_smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void tc_mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc_smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+// 2-D TMA tile load (tensor map in kernel-parameter space): box at element
+// coordinates (x, y) into shared memory, completion counted on bar in bytes.
+// x times the element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tc_tma_load_2d(void* dst, const void* tmap, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          tc_smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(tc_smem_u32(bar))
+      : "memory");
+}
