@@ -1161,6 +1161,70 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
 // zero MF slots; columns beyond n_k2 are zeroed on read. Terms stored as ELL
 // load X directly. Everything else as in kbt_tile.
 // ---------------------------------------------------------------------------
+constexpr int KBT_MAXT = 64;  // terms of one output slab held in the shared-memory table
+
+// the next term's B and MF values, loaded into registers before they are staged
+struct KbtPre {
+  float kr[2], ki[2];
+  float2 mf;
+  int col;
+};
+
+template <int KP>
+__device__ __forceinline__ void kbt_preload(const KbtTerm& t, int nk1, int NP, int i0, int nr, int tid, KbtPre& q) {
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int e = tid + 256 * u;
+    const int a = e / KP, b = e - (e / KP) * KP;
+    float kr = 0.f, ki = 0.f;
+    if (e < NP * KP && a < nk1 && b < t.nk2) {
+      if (t.ktype == 0) {
+        kr = __ldg(t.KT + ((long long)b * nk1 + a) * 2);
+        ki = __ldg(t.KT + ((long long)b * nk1 + a) * 2 + 1);
+      } else if (t.ktype == 1) {
+        kr = __ldg(t.KT + (long long)b * nk1 + a);
+      } else {
+        ki = __ldg(t.KT + (long long)b * nk1 + a);
+      }
+    }
+    q.kr[u] = kr;
+    q.ki[u] = ki;
+  }
+  q.mf = make_float2(0.f, 0.f);
+  q.col = 0;
+  if (tid < nr * t.W) {
+    const int r = tid / t.W, w = tid - (tid / t.W) * t.W;
+    const long long src = (long long)(i0 + r) * t.Wst + w;
+    q.mf = __ldcg(t.mf + src);
+    if (!t.dia) q.col = __ldg(t.col + src);
+  }
+}
+
+template <int KP>
+__device__ __forceinline__ void kbt_stage_pre(const KbtTerm& t, const KbtPre& q, int NP, int nr, float* Bt,
+                                              float2* MFs, int* Cs, int tid, int bpart) {
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int e = tid + 256 * u;
+    if (e >= NP * KP) break;
+    const int a = e / KP, b = e - (e / KP) * KP;
+    const uint32_t o = tc_kmajor_off(a, b, KP) >> 2;
+    const float kr = q.kr[u], ki = q.ki[u];
+    const float krh = tc_tf32(kr), kih = tc_tf32(ki);
+    Bt[0 * (bpart / 4) + o] = krh;
+    Bt[1 * (bpart / 4) + o] = kr - krh;
+    Bt[2 * (bpart / 4) + o] = kih;
+    Bt[3 * (bpart / 4) + o] = ki - kih;
+    Bt[4 * (bpart / 4) + o] = -kih;
+    Bt[5 * (bpart / 4) + o] = -(ki - kih);
+  }
+  if (tid < nr * t.W) {
+    const int r = tid / t.W, w = tid - (tid / t.W) * t.W;
+    MFs[r * KB_WMAX + w] = q.mf;
+    if (!t.dia) Cs[r * KB_WMAX + w] = q.col;
+  }
+}
+
 template <int KP>
 struct KbtRing {
   static constexpr int NSLOT = 64 / KP;          // slots of KP rows x 128 vectors x 8 bytes
@@ -1172,7 +1236,8 @@ struct KbtRing {
   static constexpr int OFF_MF = OFF_RING + NSLOT * SLOT;
   static constexpr int OFF_CS = OFF_MF + TC_MFBYTES;
   static constexpr int OFF_BAR = OFF_CS + TC_CSBYTES;
-  static constexpr int TOTAL = OFF_BAR + 8 * (2 + 2 * NSLOT) + 16;
+  static constexpr int OFF_TAB = OFF_BAR + 8 * (2 + 2 * NSLOT) + 16;  // term table (KBT_MAXT entries)
+  static constexpr int TOTAL = OFF_TAB + KBT_MAXT * (int)sizeof(KbtTerm);
 };
 constexpr int TC_SMEM_RING = KbtRing<16>::TOTAL > KbtRing<8>::TOTAL ? KbtRing<16>::TOTAL : KbtRing<8>::TOTAL;
 
@@ -1254,6 +1319,7 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
   uint64_t* rfull = full + 2;
   uint64_t* rempty = rfull + NSLOT;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(rempty + NSLOT);
+  KbtTerm* tab = reinterpret_cast<KbtTerm*>(smem + L::OFF_TAB);
   const int nk1 = __ldg(op.out_dk + s1);
   const int NP = nk1 <= 16 ? 16 : 32;
   float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * nk1) * nb + v;
@@ -1274,6 +1340,16 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
       tc_mbar_init(rempty + i, 8);
     }
   }
+  // term table: the tables of every term of the slab, read once per tile
+  const int nt = te - tb;
+  const bool use_tab = nt <= KBT_MAXT;
+  if (use_tab)
+    for (int i = tid; i < nt; i += blockDim.x) tab[i] = kbt_term(op, p, tb + i, KP, 0, nb);
+  auto term_at = [&](int i) {
+    KbtTerm tt = use_tab ? tab[i] : kbt_term(op, p, tb + i, KP, 0, nb);
+    tt.Xs2 += v;
+    return tt;
+  };
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -1289,16 +1365,12 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
       const uint64_t bdesc0 = tc_desc(tc_smem_u32(Bs), 128u, 32u * KP);
       uint32_t dinit = 0;
       for (int term = tb; term < te; ++term) {
-        const int s2 = __ldg(op.t_in + term);
-        const int nk2 = __ldg(op.in_dk + s2);
-        const int W = __ldg(op.mf_width + __ldg(op.t_mf + term));
-        if (!(nk2 <= KP && W <= KB_WMAX)) continue;
-        if (__ldcg(op.mf_band + 2 * __ldg(op.t_mf + term) + 1) < 0) continue;  // MF zero with this field
-        const int ktype = __ldg(op.k_type + __ldg(op.t_k + term));
+        const KbtTerm tt = term_at(term - tb);
+        if (!tt.ok || tt.empty) continue;  // skipped by the producers as well
         if (!tc_mbar_wait(full, (uint32_t)ncommit & 1u)) ok = false;
         tc_fence_after();
         const uint64_t bdesc = bdesc0 + (uint64_t)((((term - tb) & 1) * L::BBUF) >> 4);
-        kbt_issue<KP>(tmem, adesc0, bdesc, idesc, NP, nr, ktype, nk2, dinit, L::BPART);
+        kbt_issue<KP>(tmem, adesc0, bdesc, idesc, NP, nr, tt.ktype, tt.nk2, dinit, L::BPART);
         tc_commit(empty);
         ++ncommit;
       }
@@ -1307,9 +1379,9 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
       // would hold up a loader lane of the same warp) ------------------------
       int g = 0;
       for (int term = tb; term < te; ++term) {
-        const KbtTerm t = kbt_term(op, p, term, KP, v, nb);
+        const KbtTerm t = term_at(term - tb);
         const int nwin = kbt_ring_rows(t, nr);
-        const long long row0 = __ldg(op.in_off + __ldg(op.t_in + term));  // first X row of slab s2
+        const long long row0 = __ldg(op.in_off + t.s2);  // first X row of slab s2
         for (int c = 0; c < nwin; ++c, ++g) {
           const int slot = g % NSLOT;
           if (g >= NSLOT && !tc_mbar_wait(rempty + slot, (uint32_t)(g / NSLOT - 1) & 1u)) ok = false;
@@ -1332,13 +1404,20 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
   // ---- producers -------------------------------------------------------------
   float2 z[R][BH];
   int g = 0;  // ring row counter
-  KbtTerm cur = kbt_term(op, p, tb, KP, v, nb);
-  kbt_stage<KP>(cur, nk1, NP, i0, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, tid, L::BPART);
+  KbtTerm cur = term_at(0);
+  KbtPre pre;
+  kbt_preload<KP>(cur, nk1, NP, i0, nr, tid, pre);
+  kbt_stage_pre<KP>(cur, pre, NP, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, tid, L::BPART);
   kbt_producer_sync();
   if (!kbt_zstep_ring<KP>(z, cur, nb, nr, b0, vloc, lane, MFs0, Cs0, ring, rfull, rempty, g)) ok = false;
   for (int term = tb; term < te; ++term) {
     const int buf = (term - tb) & 1;
     const bool has_next = term + 1 < te;
+    KbtTerm nxt;
+    if (has_next) {  // the next term's K and MF values in flight during the A-tile hand-off
+      nxt = term_at(term + 1 - tb);
+      kbt_preload<KP>(nxt, nk1, NP, i0, nr, tid, pre);
+    }
     // the MMAs of the previous committed term are done with the A tiles and its B buffer
     if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
     tc_fence_after();
@@ -1378,9 +1457,8 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
     if (has_next) {
       // B buffer buf ^ 1 was last read by the MMAs of term - 1 (done); MF buffer
       // buf ^ 1 by the M step of term - 1 (every producer is past it)
-      const KbtTerm nxt = kbt_term(op, p, term + 1, KP, v, nb);
-      kbt_stage<KP>(nxt, nk1, NP, i0, nr, reinterpret_cast<float*>(Bs + (buf ^ 1) * L::BBUF),
-                    MFs0 + (buf ^ 1) * 8 * KB_WMAX, Cs0 + (buf ^ 1) * 8 * KB_WMAX, tid, L::BPART);
+      kbt_stage_pre<KP>(nxt, pre, NP, nr, reinterpret_cast<float*>(Bs + (buf ^ 1) * L::BBUF),
+                        MFs0 + (buf ^ 1) * 8 * KB_WMAX, Cs0 + (buf ^ 1) * 8 * KB_WMAX, tid, L::BPART);
       kbt_producer_sync();
       if (!kbt_zstep_ring<KP>(z, nxt, nb, nr, b0, vloc, lane, MFs0 + (buf ^ 1) * 8 * KB_WMAX,
                               Cs0 + (buf ^ 1) * 8 * KB_WMAX, ring, rfull, rempty, g))
