@@ -24,6 +24,60 @@ class ExpokitError(Exception):
     """Error of the external (expokit-scheme) propagator, as richmol.pyexpokit.ExpokitError."""
 
 
+class BlockEigh:
+    """Eigen-decomposition of a sparse Hermitian matrix through its independent
+    blocks (connected components of the non-zero pattern): each block is
+    diagonalised densely, on the GPU (batched over blocks of equal size) when
+    one is present. Eigenvalues come sorted ascending (ties keep block order);
+    eigenvectors are formed only for the states asked for."""
+
+    def __init__(self, h):
+        from scipy.sparse.csgraph import connected_components
+        h = csr_matrix(h)
+        self.n = h.shape[0]
+        ncomp, labels = connected_components(h != 0, directed=False)
+        order = np.argsort(labels, kind="stable")
+        self.blocks = np.split(order, np.cumsum(np.bincount(labels, minlength=ncomp))[:-1])
+        self._vals, self._vecs = [None] * ncomp, [None] * ncomp
+        by_size = {}
+        for b, idx in enumerate(self.blocks):
+            by_size.setdefault(len(idx), []).append(b)
+        use_gpu = torch.cuda.is_available()
+        for size, bl in by_size.items():
+            mats = np.stack([h[self.blocks[b]][:, self.blocks[b]].toarray() for b in bl]).astype(np.complex128)
+            if use_gpu and size > 1:
+                w, v = torch.linalg.eigh(torch.from_numpy(mats).cuda())
+                w, v = w.cpu().numpy(), v.cpu().numpy()
+            else:
+                w, v = np.linalg.eigh(mats)
+            for i, b in enumerate(bl):
+                self._vals[b], self._vecs[b] = w[i], v[i]
+        vals = np.concatenate(self._vals) if ncomp else np.zeros(0)
+        owner = np.concatenate([np.full(len(self.blocks[b]), b) for b in range(ncomp)]) if ncomp else np.zeros(0, int)
+        local = np.concatenate([np.arange(len(self.blocks[b])) for b in range(ncomp)]) if ncomp else np.zeros(0, int)
+        srt = np.argsort(vals, kind="stable")
+        self.values = vals[srt]
+        self._owner, self._local = owner[srt], local[srt]
+
+    def vectors(self, states):
+        """Eigenvectors of the given sorted-state indices as rows of a CSR matrix."""
+        rows, cols, data = [], [], []
+        for r, st in enumerate(np.asarray(states, dtype=np.int64)):
+            b, j = self._owner[st], self._local[st]
+            idx = self.blocks[b]
+            rows.append(np.full(len(idx), r))
+            cols.append(idx)
+            data.append(self._vecs[b][:, j])
+        if not rows:
+            return csr_matrix((0, self.n), dtype=np.complex128)
+        return csr_matrix((np.concatenate(data), (np.concatenate(rows), np.concatenate(cols))),
+                          shape=(len(rows), self.n))
+
+    def all(self):
+        """(eigenvalues, eigenvectors as columns of a CSR matrix), like numpy's eigh."""
+        return self.values, self.vectors(np.arange(self.n)).transpose().tocsr()
+
+
 def update_counter(func):
     """tdse.py:11-24: returns (vecs, t2[icall]), the end of the interval."""
     @functools.wraps(func)
@@ -111,11 +165,20 @@ class TDSE:
             raise AttributeError("hamiltonian `H` has inappropriate type (must be Hamiltonian)") from None
         if H_is_diag:
             enrs = H.tomat(form="full", repres="csr_matrix").diagonal()
-            vecs = diags(np.ones(len(enrs)), format="csr")
+            eig = None
         else:
-            hmat = H.tomat(form="full", repres="dense")
-            enrs, vecs = np.linalg.eigh(hmat)
-            vecs = csr_matrix(vecs)
+            # tdse.py:231-233 diagonalises the dense matrix; here the
+            # independent blocks of H (with a field along z the dressed H
+            # conserves m) are diagonalised one by one, and only the
+            # eigenvectors of the states kept below are formed
+            eig = BlockEigh(H.tomat(form="full", repres="csr_matrix"))
+            enrs = eig.values
+
+        def rows(states):  # eigenvectors of the given states, as CSR rows
+            if eig is None:  # H diagonal: the basis functions, in basis order
+                return diags(np.ones(len(enrs)), format="csr")[np.asarray(states, dtype=np.int64)]
+            return eig.vectors(states)
+
         if zpe is not None:
             assert zpe <= abs(enrs[0]), \
                 f"zero-point energy `zpe` has a value that is larger than the lowest energy: " \
@@ -123,22 +186,21 @@ class TDSE:
         else:
             zpe = enrs[0]
         enrs = enrs - zpe
-        vecs = vecs.transpose()
         if temp is None:
-            pass
+            vecs = rows(np.arange(len(enrs)))
         elif temp == 0:
-            vecs = vecs.getrow(0)
+            vecs = rows([0])
         else:
             enrs = enrs * self._enr_to_J
             beta = 1.0 / (const.value("Boltzmann constant") * temp)
             weights = np.exp(-beta * enrs)
             weights /= np.sum(weights)
-            # cumulative sum in basis order, as tdse.py:254-255
+            # cumulative sum in state order, as tdse.py:254-255
             cum = np.cumsum(weights)
             inds = [i for i in range(len(weights)) if (1 - np.sum(weights[: i + 1])) > thresh] \
                 if len(weights) < 4096 else list(np.nonzero((1 - cum) > thresh)[0])
             sqrt_weights = np.sqrt(weights[inds])
-            vecs = csr_matrix(vecs)[inds].multiply(sqrt_weights[:, None])
+            vecs = rows(inds).multiply(sqrt_weights[:, None])
         if not sparse:
             vecs = csr_matrix(vecs).toarray()
         return vecs.astype(np.complex128)

@@ -98,11 +98,12 @@ def test_batch_thermal_ensemble_observable_within_1e6(matvec):
 
 
 @pytest.mark.parametrize("matvec", MATVECS)
-@pytest.mark.parametrize("jmax,nvec", [(12, 40), (30, 96), (30, 384)])
+@pytest.mark.parametrize("jmax,nvec", [(12, 40), (30, 96), (30, 384), (34, 128)])
 def test_batched_matvec_matches_fp64(jmax, nvec, matvec):
     """The complex64 batched mat-vec against the FP64 mat-vec of the same
     operator (DC + tilted pulse, all Delta J couplings) on random vectors; J<=12
-    crosses the tile shapes, J<=30 is the ensemble workload's basis."""
+    crosses the tile shapes, J<=30 is the ensemble workload's basis, J<=34 has
+    slabs with n_k = 17, 18 (the K extent 32 tiles)."""
     from richmol_gb300 import TDSE, workloads
     from richmol_gb300.batch import Ensemble
     wl = workloads.asym_top(Jmax=jmax)
