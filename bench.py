@@ -36,7 +36,7 @@ METRIC = "Krylov state-steps/s: batched FP32/FP64 vs plain FP64, 1 GB300, err<=1
 UNIT = "state-steps/s"
 
 
-def parse():
+def parse(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=50, help="timed steps of the batched ensemble")
@@ -53,12 +53,25 @@ def parse():
     p.add_argument("--no-extras", action="store_true", help="headline measurement only")
     p.add_argument("--matvec", choices=["tensor", "fp32"], default="tensor",
                    help="batched mat-vec kind: tensor-core K contraction (split TF32) or FP32 FMAs")
-    return p.parse_args()
+    return p.parse_args(argv)
 
 
 def dist_info():
     return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), \
         int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def job_throughput(local_seconds, units_per_rank, ws, device="cpu"):
+    """Whole-job rate: the units of all ranks over the slowest rank's time (max
+    over ranks, one all-reduce when ws > 1). Returns (rate, max seconds)."""
+    t = float(local_seconds)
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        x = torch.tensor([t], dtype=torch.float64, device=device)
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        t = float(x.item())
+    return ws * units_per_rank / t, t
 
 
 # ---------------------------------------------------------------------------
@@ -247,14 +260,11 @@ def run_ours(args, ws, rank, local):
             ev[j][1].record()
             kmax_seen.append(ens.last_kmax)
         torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_s = sum(step_ms) / 1e3
     launches = (ens.launches() - l0) + (wl.Hac._plan().launches() - plan_l0)
-    if ws > 1:
-        t = torch.tensor([total_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = ws * nvec * K / total_s
+    value, total_s = job_throughput(sum(step_ms) / 1e3, nvec * K, ws, dev)
     korder = np.bincount(ens.korder(), minlength=1)
 
     # dominant kernel (batched complex64 mat-vec) alone
