@@ -1571,11 +1571,8 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
     const int rc = encode_xmap(op->ctx, X, b->dim, b->nb, &xmap);
     if (rc != KR_OK) return rc;
     const int smem = std::max(TC_SMEM, TC_SMEM_RING);
-    static bool tc_attr = false;
-    if (!tc_attr) {
-      KR_CUDA(op->ctx, cudaFuncSetAttribute(kb_matvec_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-      tc_attr = true;
-    }
+    // per device (the attribute belongs to the current device's context)
+    KR_CUDA(op->ctx, cudaFuncSetAttribute(kb_matvec_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     kb_matvec_tc<<<dim3(op->tc_ntask, b->nb / 128), 320, smem, st>>>(q, xmap);
     b->launches++;
     KR_CUDA(op->ctx, cudaGetLastError());
@@ -1591,11 +1588,7 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
   p.task_nr = b->task_nr;
   p.grp_active = masked ? b->grp_active : nullptr;
   const size_t smem = kb_matvec_smem();
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(kb_matvec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
+  KR_CUDA(op->ctx, cudaFuncSetAttribute(kb_matvec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid(b->ntask, mv_groups(b));
   kb_matvec<<<grid, 256, smem, st>>>(p);
   b->launches++;
@@ -1609,14 +1602,15 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
     return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_batch_create: bad argument (2 <= mmax <= 31)");
   *out = nullptr;
   if (!op->square) return set_err(op->ctx, KR_ERR_ARG, "kr_batch_create: operator is not square");
-  // the batched mat-vec supports n_k <= 32 and ELL widths <= 64
+  KR_CUDA(op->ctx, cudaSetDevice(op->ctx->device));
+  // the batched mat-vec supports n_k <= 32 and ELL widths <= 16
   std::vector<int> dk(op->dev.nslab_out), dm(op->dev.nslab_out);
-  cudaMemcpy(dk.data(), op->dev.out_dk, sizeof(int) * dk.size(), cudaMemcpyDeviceToHost);
-  cudaMemcpy(dm.data(), op->dev.out_dm, sizeof(int) * dm.size(), cudaMemcpyDeviceToHost);
+  KR_CUDA(op->ctx, cudaMemcpy(dk.data(), op->dev.out_dk, sizeof(int) * dk.size(), cudaMemcpyDeviceToHost));
+  KR_CUDA(op->ctx, cudaMemcpy(dm.data(), op->dev.out_dm, sizeof(int) * dm.size(), cudaMemcpyDeviceToHost));
   for (int x : dk)
     if (x > KB_NK_MAX) return set_err(op->ctx, KR_ERR_UNSUPPORTED, "kr_batch_create: n_k above 32 not supported");
   std::vector<int> widths(std::max(1, op->nmf));
-  cudaMemcpy(widths.data(), op->dev.mf_width, sizeof(int) * op->nmf, cudaMemcpyDeviceToHost);
+  KR_CUDA(op->ctx, cudaMemcpy(widths.data(), op->dev.mf_width, sizeof(int) * op->nmf, cudaMemcpyDeviceToHost));
   for (int i = 0; i < op->nmf; ++i)
     if (widths[i] > KB_WMAX)
       return set_err(op->ctx, KR_ERR_UNSUPPORTED, "kr_batch_create: M band wider than 16 entries per row");
@@ -1662,10 +1656,14 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
   BA(ti.size(), &b->task_i0);
   BA(tn.size(), &b->task_nr);
 #undef BA
-  cudaMemcpy(b->task_slab, ts.data(), sizeof(int) * ts.size(), cudaMemcpyHostToDevice);
-  cudaMemcpy(b->task_i0, ti.data(), sizeof(int) * ti.size(), cudaMemcpyHostToDevice);
-  cudaMemcpy(b->task_nr, tn.data(), sizeof(int) * tn.size(), cudaMemcpyHostToDevice);
-  KR_CUDA(op->ctx, cudaDeviceSynchronize());
+  cudaError_t ce = cudaMemcpy(b->task_slab, ts.data(), sizeof(int) * ts.size(), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) ce = cudaMemcpy(b->task_i0, ti.data(), sizeof(int) * ti.size(), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) ce = cudaMemcpy(b->task_nr, tn.data(), sizeof(int) * tn.size(), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
+  if (ce != cudaSuccess) {
+    kr_batch_destroy(b);
+    return set_err(op->ctx, KR_ERR_CUDA, std::string("kr_batch_create: ") + cudaGetErrorString(ce));
+  }
   *out = b;
   return KR_OK;
 }
