@@ -162,3 +162,32 @@ def test_batched_matvec_scattered_m_matches_fp64(matvec):
     H.device_operator().matvec(x, y64)
     err = (y32 - y64).abs().max().item() / y64.abs().max().item()
     assert err < MV_RTOL[matvec], err
+
+
+@pytest.mark.parametrize("matvec", MATVECS)
+def test_batched_matvec_complex_k_c1_molecule(matvec):
+    """A C1 molecule (no symmetry) with a general dipole and polarisability in a
+    tilted DC + AC field: complex K blocks (both products of the complex
+    contraction) and n_k up to 17 (both tile K extents)."""
+    from richmol_gb300 import TDSE, rot
+    from richmol_gb300.batch import Ensemble
+    from richmol_gb300.convert_units import AUdip_x_Vm_to_invcm, AUpol_x_Vm_to_invcm
+    pol_m = np.array([[9.0, 0.5, 0.2], [0.5, 8.0, 0.1], [0.2, 0.1, 7.0]])
+    mol = rot.Molecule(B=(2.0, 1.2, 0.8), sym="C1", dip=[0.3, -0.4, 0.5], pol=pol_m)
+    sol = rot.Solution(mol, Jmax=8)
+    h0 = rot.lab_tensor("h0", sol)
+    Hdc = (rot.lab_tensor(mol.dip, sol) * [1e6, 2e6, 3e6]) * (-AUdip_x_Vm_to_invcm())
+    Hac = rot.lab_tensor(mol.pol, sol) * (-0.5 * AUpol_x_Vm_to_invcm())
+    Hac.field([4e8, -2e8, 6e8])
+    H = Hdc + Hac
+    td = TDSE(t_end=1.0, dt=0.01)
+    td.time_grid()
+    nvec = 128
+    ens = Ensemble(td, h0, nvec, matvec=matvec)
+    g = torch.Generator(device="cuda").manual_seed(17)
+    x = torch.randn((nvec, ens.dim), dtype=torch.complex128, device="cuda", generator=g)
+    y32 = ens.apply(H, x)
+    y64 = torch.empty_like(x)
+    H.device_operator().matvec(x, y64)
+    err = (y32 - y64).abs().max().item() / y64.abs().max().item()
+    assert err < MV_RTOL[matvec], err
