@@ -736,29 +736,47 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   op->bytes_per_matvec = 16.0 * (d->dim_in + d->dim_out) + kbytes + mbytes;
 
   // ---- row tasks ----------------------------------------------------------
+  // Rows per task from thread occupancy (pick_task_rows); then the slabs whose
+  // tasks would cost more than half of the mean work per CTA are cut finer
+  // (down to one output per thread), so that the dynamic queue, handed out
+  // most expensive first, ends evenly across the CTAs.
   std::vector<int> task_slab, task_row0, task_nrows;
   std::vector<double> task_cost;
   int zmax = 1;
+  auto task_cost_of = [&](int s, int nr) {
+    const int nk1 = d->out_dk[s];
+    const int q = (nr * nk1 + KR_THREADS - 1) / KR_THREADS;
+    double cost = 200.0;
+    for (int t : by_out[s]) {
+      const int nk2 = d->in_dk[d->t_in[t]];
+      const int g = d->mf_group[d->t_mf[t]];
+      const double kf = d->k_type[d->t_k[t]] == KR_K_COMPLEX ? 4.0 : 2.0;
+      const int qz = (nr * nk2 + KR_THREADS - 1) / KR_THREADS;
+      cost += 4.0 * qz * d->m_width[g] + kf * q * nk2 + 60.0;
+    }
+    return cost;
+  };
+  std::vector<int> rows_per_task(d->nslab_out);
+  double total = 0.0;
+  for (int s = 0; s < d->nslab_out; ++s) {
+    const int dm1 = d->out_dm[s];
+    rows_per_task[s] = pick_task_rows(d->out_dk[s], dm1);
+    for (int i0 = 0; i0 < dm1; i0 += rows_per_task[s]) total += task_cost_of(s, std::min(rows_per_task[s], dm1 - i0));
+  }
+  const double cap = 0.5 * total / (2.0 * ctx->nsm);  // half the mean work of one of 2 CTAs per SM
   for (int s = 0; s < d->nslab_out; ++s) {
     const int nk1 = d->out_dk[s], dm1 = d->out_dm[s];
-    const int R = pick_task_rows(nk1, dm1);
+    int R = rows_per_task[s];
+    const int rmin = std::max(1, std::min(R, KR_THREADS / nk1));  // one output per thread
+    while (R > rmin && task_cost_of(s, R) > cap) R = std::max(rmin, R / 2);
     int maxnk2 = 1;
     for (int t : by_out[s]) maxnk2 = std::max(maxnk2, d->in_dk[d->t_in[t]]);
     for (int i0 = 0; i0 < dm1; i0 += R) {
       const int nr = std::min(R, dm1 - i0);
-      const int q = (nr * nk1 + KR_THREADS - 1) / KR_THREADS;
-      double cost = 200.0;
-      for (int t : by_out[s]) {
-        const int nk2 = d->in_dk[d->t_in[t]];
-        const int g = d->mf_group[d->t_mf[t]];
-        const double kf = d->k_type[d->t_k[t]] == KR_K_COMPLEX ? 4.0 : 2.0;
-        const int qz = (nr * nk2 + KR_THREADS - 1) / KR_THREADS;
-        cost += 4.0 * qz * d->m_width[g] + kf * q * nk2 + 60.0;
-      }
       task_slab.push_back(s);
       task_row0.push_back(i0);
       task_nrows.push_back(nr);
-      task_cost.push_back(cost);
+      task_cost.push_back(task_cost_of(s, nr));
       zmax = std::max(zmax, nr * maxnk2);
     }
   }
