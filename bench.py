@@ -288,7 +288,10 @@ def run_ours(args, ws, rank, local):
     fma_mv, bytes_mv = plan.work()
     mv_flops = 2.0 * fma_mv * nvec
     mv_bytes = 8.0 * 2 * dim * nvec  # complex64 X in + Y out (factors are shared by all vectors)
-    traffic = load_traffic().get("kb_matvec_per_launch_bytes_4096")
+    # ncu DRAM bytes of one launch at 4096 vectors (profiles/traffic.json), in proportion to the vectors
+    tkey = "kb_matvec_tc_per_launch_bytes_4096" if args.matvec == "tensor" else "kb_matvec_per_launch_bytes_4096"
+    t4096 = load_traffic().get(tkey)
+    traffic = None if t4096 is None else int(round(t4096 * nvec / 4096))
     gbs = mv_bytes / mv_s / 1e9
     roofline = {
         "bound": "hbm", "achieved": round(gbs, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
