@@ -191,3 +191,78 @@ def test_batched_matvec_complex_k_c1_molecule(matvec):
     H.device_operator().matvec(x, y64)
     err = (y32 - y64).abs().max().item() / y64.abs().max().item()
     assert err < MV_RTOL[matvec], err
+
+
+def _asym_fixture_setup():
+    from oracle import fixtures
+    from richmol_gb300 import TDSE
+    d, meta = fixtures.load(os.path.join(GOLDEN, "asym_j4.npz"))
+    sc = meta["scales"]
+    h0 = _ct("asym_j4.npz", "h0")
+    Hdc = (_ct("asym_j4.npz", "dip") * meta["dc"]) * sc["dc"]
+    Hac = _ct("asym_j4.npz", "pol") * sc["ac"]
+    sp = meta["split"]
+    td = TDSE(t_start=sp["t_start"], t_end=sp["t_end"], dt=sp["dt"])
+    tc = td.time_grid()
+    return d, h0, Hdc, Hac, td, tc
+
+
+@pytest.mark.parametrize("nvec", [1, 129])
+def test_batch_ragged_ensemble_sizes_and_zero_vector(nvec):
+    """One vector (127 padding lanes) and 129 vectors (two 128-vector groups,
+    the second almost all padding), one of them zero: every vector follows the
+    plain FP64 path over 5 steps, the zero vector stays zero."""
+    from richmol_gb300.batch import Ensemble
+    d, h0, Hdc, Hac, td, tc = _asym_fixture_setup()
+    dim = sum(b[2] * b[3] for b in h0._parts[0].src.basis("1"))
+    rng = np.random.default_rng(nvec)
+    v0 = rng.standard_normal((nvec, dim)) + 1j * rng.standard_normal((nvec, dim))
+    v0 /= np.linalg.norm(v0, axis=1, keepdims=True)
+    if nvec > 1:
+        v0[nvec // 2] = 0.0
+    ens = Ensemble(td, h0, nvec, tol=1e-10)
+    ens.load(v0)
+    live = np.linalg.norm(v0, axis=1) > 0
+    vecs = v0[live].copy()  # the plain path follows the reference's Lanczos, not meant for zero vectors
+    for i in range(5):
+        Hac.field(d["split/fields"][i])
+        H = Hdc + Hac
+        ens.step(H)
+        vecs, _ = td.update(H, H0=h0, vecs=vecs, check=False)
+    got = ens.store().cpu().numpy()
+    assert np.abs(got[live] - vecs).max() < 1e-5
+    if nvec > 1:
+        assert np.count_nonzero(got[nvec // 2]) == 0
+        assert (ens.korder()[nvec // 2]) == 0
+
+
+def test_batch_zero_field_matvec_is_exactly_zero():
+    """A field that makes every MF zero leaves every term empty: the mat-vec
+    writes exact zeros (both kinds)."""
+    from richmol_gb300.batch import Ensemble
+    _, h0, _, Hac, td, _ = _asym_fixture_setup()
+    Hac.field([0.0, 0.0, 0.0])
+    nvec = 8
+    ens = Ensemble(td, h0, nvec)
+    x = torch.randn((nvec, ens.dim), dtype=torch.complex128, device="cuda")
+    for kind in ("tensor", "fp32"):
+        from richmol_gb300 import _native
+        _native.check(_native.lib().kr_batch_set_matvec(
+            ens.handle, {"tensor": _native.KR_MATVEC_TENSOR, "fp32": _native.KR_MATVEC_FP32}[kind]), ens.ctx)
+        y = ens.apply(Hac, x)
+        assert torch.count_nonzero(y).item() == 0, kind
+
+
+def test_batch_maxorder_raises():
+    """A step that needs more Krylov vectors than the batch holds is an error
+    (the reference's ValueError at maxorder, tdse.py:480-484)."""
+    from richmol_gb300 import _native
+    from richmol_gb300.batch import Ensemble
+    d, h0, Hdc, Hac, td, tc = _asym_fixture_setup()
+    Hac.field(np.asarray(d["split/fields"][0]) * 30.0)
+    v0 = td.init_state(h0, temp=5, thresh=1e-3)
+    ens = Ensemble(td, h0, v0.shape[0], tol=1e-12, mmax=2)
+    ens.load(v0)
+    with pytest.raises(_native.KrylovError) as e:
+        ens.step(Hdc + Hac)
+    assert e.value.code == _native.KR_ERR_MAXORDER
