@@ -206,6 +206,11 @@ int kr_batch_korder(kr_batch* b, int32_t* korder, void* stream);
  * with its field set (e.g. cos^2 theta with field [0, 0, 1]); complex64
  * mat-vec, FP64 dot products. Synchronises. */
 int kr_batch_expect(kr_batch* b, kr_op* obs, double* out, void* stream);
+/* Populations of every slab (the (J, sym) blocks of the flat vector order) for
+ * every vector: out[slab * nvec + v] = sum over the slab of |S_v|^2 (host array,
+ * nslab x nvec doubles); summed over the symmetries of a J they are the
+ * J-populations of the reference's observables (tests/test_tdse.py:63-67). */
+int kr_batch_populations(kr_batch* b, double* out, void* stream);
 /* Mat-vec kinds of a batch: KR_MATVEC_TENSOR (default) contracts the K
  * factors on the tensor cores (tcgen05, TF32 with split operands: about 2^-21
  * relative per product, FP32 accumulation); KR_MATVEC_FP32 runs every

@@ -36,6 +36,7 @@ EXPORTED = [
     "kr_probe_fp64", "kr_probe_fp32", "kr_probe_mma", "kr_step_static", "kr_static_scratch_bytes",
     "kr_batch_create", "kr_batch_destroy", "kr_batch_load", "kr_batch_store", "kr_batch_step",
     "kr_batch_korder", "kr_batch_expect", "kr_batch_launch_count", "kr_batch_matvec", "kr_batch_apply", "kr_batch_set_matvec",
+    "kr_batch_populations",
     "kr_expv", "kr_op_norm1",
 ]
 
@@ -152,6 +153,8 @@ def lib():
         L.kr_batch_korder.restype = ctypes.c_int
         L.kr_batch_expect.argtypes = [vp, vp, vp, vp]
         L.kr_batch_expect.restype = ctypes.c_int
+        L.kr_batch_populations.argtypes = [vp, vp, vp]
+        L.kr_batch_populations.restype = ctypes.c_int
         L.kr_batch_set_matvec.argtypes = [vp, i32]
         L.kr_batch_set_matvec.restype = ctypes.c_int
         L.kr_batch_apply.argtypes = [vp, vp, vp, vp, vp]

@@ -107,6 +107,18 @@ class Ensemble:
         _native.check(_native.lib().kr_batch_expect(self.handle, plan.op, out.ctypes.data, stream_ptr()), self.ctx)
         return out.view(np.complex128)
 
+    def populations(self):
+        """{J: (nvec,) array} J-populations of every vector (sum of |v|^2 over the
+        slabs of each J), as the reference's observables (tests/test_tdse.py:63-67)."""
+        basis = self.template._parts[0].src.basis("1")
+        out = np.zeros(len(basis) * self.nvec, np.float64)
+        _native.check(_native.lib().kr_batch_populations(self.handle, out.ctypes.data, stream_ptr()), self.ctx)
+        out = out.reshape(len(basis), self.nvec)
+        pops = {}
+        for (J, _sym, _dm, _dk), row in zip(basis, out):
+            pops[J] = pops.get(J, 0.0) + row
+        return pops
+
     def apply(self, H, x):
         """y = H x for (nvec, dim) complex128 CUDA tensors with the batched
         complex64 mat-vec (the single-precision CarTens.vec)."""

@@ -266,3 +266,30 @@ def test_batch_maxorder_raises():
     with pytest.raises(_native.KrylovError) as e:
         ens.step(Hdc + Hac)
     assert e.value.code == _native.KR_ERR_MAXORDER
+
+
+def test_batch_populations_match_plain_fp64():
+    """J-populations of the 22-vector fixture ensemble after 5 steps against the
+    same sums over the plain FP64 vectors."""
+    from richmol_gb300.batch import Ensemble
+    d, h0, Hdc, Hac, td, tc = _asym_fixture_setup()
+    v0 = td.init_state(h0, temp=5, thresh=1e-3)
+    ens = Ensemble(td, h0, v0.shape[0], tol=1e-10)
+    ens.load(v0)
+    vecs = v0
+    for i in range(5):
+        Hac.field(d["split/fields"][i])
+        H = Hdc + Hac
+        ens.step(H)
+        vecs, _ = td.update(H, H0=h0, vecs=vecs)
+    pops = ens.populations()
+    off = 0
+    ref = {}
+    for J, _s, dm, dk in h0._parts[0].src.basis("1"):
+        ref[J] = ref.get(J, 0.0) + (np.abs(vecs[:, off:off + dm * dk]) ** 2).sum(axis=1)
+        off += dm * dk
+    assert sorted(pops) == sorted(ref)
+    for J in ref:
+        assert np.abs(pops[J] - ref[J]).max() < 1e-6, J
+    total = sum(pops.values())
+    assert np.abs(total - (np.abs(vecs) ** 2).sum(axis=1)).max() < 1e-6
