@@ -16,7 +16,8 @@ ROOT = os.path.dirname(PKG)
 LIB_DIR = os.path.join(PKG, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "librichmol_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
-SOURCES = [os.path.join(PKG, "csrc", f) for f in ("kr_step.cu", "kr_batch.cu", "kr_expv.cu")]
+SOURCES = [os.path.join(PKG, "csrc", f) for f in ("kr_step.cu", "kr_batch.cu", "kr_batch_simt.cu", "kr_batch_tc.cu",
+                                                        "kr_expv.cu")]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 KR_OK, KR_ERR_ARG, KR_ERR_CUDA, KR_ERR_MAXORDER, KR_ERR_TIMEOUT, KR_ERR_UNSUPPORTED = range(6)

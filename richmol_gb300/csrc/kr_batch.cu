@@ -16,19 +16,17 @@
 //     exp(fac T) e0 (Taylor series on the vector) and the a-posteriori error
 //     estimate |fac| beta_k |[exp(fac T_k)]_{k,0}| ||v|| (Saad, SIAM J. Numer.
 //     Anal. 29 (1992) 209) that stops each vector at its own order;
-//   * FP64 state and H0 half-phases.
+//   * state in double-float (an FP32 pair, about 2^-48 relative), H0 half-phases
+//     converted from FP64 to double-float once per step.
+// The two mat-vec kinds live in kr_batch_simt.cu and kr_batch_tc.cu.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
-#include <mutex>
 #include <string>
 #include <vector>
 
-#include <cuda.h>
-
-#include "kr_internal.cuh"
-#include "kr_tc.cuh"
+#include "kr_batch_mv.cuh"
 
 #define KB_MV_THREADS 128      // vectors per mat-vec block
 #define KB_RED_CHUNKS 256      // element chunks of the per-vector reductions
@@ -472,1057 +470,6 @@ __global__ void kb_slab_pop(const float4* S, const long long* slab_off, const lo
   if (threadIdx.y == 0) out[(long long)blockIdx.x * nb + v] = t.x;
 }
 
-// ---------------------------------------------------------------------------
-// batched mat-vec, complex64, tiled. One CTA (256 threads = 8 warps) computes
-// a tile of R = 128 / NKP consecutive output rows of one slab for 32 vectors
-// (lane = vector). Per term:
-//   T[j, a] = sum_b K[a, b] X[j, b]     for the input rows j of the band of
-//             the tile, each computed once and kept in shared memory; the
-//             work goes to the warps in (row, half-row) units
-//   Y[i, a] += sum_w MF[i, w] T[col(i, w), a]
-// (field.py:1212-1243 orders the same sum as MF (K X^T)^T). Every thread owns
-// the outputs of 4 consecutive rows x 4 consecutive k columns (16 complex
-// registers) across all terms. Diagonal M groups (slot w of row i holds column
-// i + d0 + w, detected by kr_op_create) address the band by offset: the T row
-// of (i, w) is i - i0 + w, and each T value loaded serves up to 4 rows. Other
-// groups use the stored columns, the band window taken in chunks of NJ rows.
-// K^T, the MF rows and their columns are staged as FP32 in shared memory.
-// ---------------------------------------------------------------------------
-#define KB_WMAX 16   // ELL width of the M band supported by the batched mat-vec
-
-struct BatchMV {
-  DevOp op;
-  const float2* X;
-  float2* Y;
-  int nb;
-  const int* task_slab;
-  const int* task_i0;
-  const int* task_nr;
-  const int* grp_active;  // per 32-vector group: any vector active (null: all)
-};
-
-// complex x real/imaginary/complex K factor accumulation: t += k * x
-template <int KT>
-__device__ __forceinline__ void kacc(float2& t, float kr, float ki, float2 x) {
-  if (KT == 1) {
-    t.x = fmaf(kr, x.x, t.x);
-    t.y = fmaf(kr, x.y, t.y);
-  } else if (KT == 2) {
-    t.x = fmaf(-kr, x.y, t.x);
-    t.y = fmaf(kr, x.x, t.y);
-  } else {
-    t.x = fmaf(kr, x.x, fmaf(-ki, x.y, t.x));
-    t.y = fmaf(kr, x.y, fmaf(ki, x.x, t.y));
-  }
-}
-
-// y += m * t for a real, imaginary or complex M-band value m
-template <int MT>
-__device__ __forceinline__ void macc(float2& y, float2 m, float2 t) {
-  if (MT == 1) {
-    y.x = fmaf(m.x, t.x, y.x);
-    y.y = fmaf(m.x, t.y, y.y);
-  } else if (MT == 2) {
-    y.x = fmaf(-m.y, t.y, y.x);
-    y.y = fmaf(m.y, t.x, y.y);
-  } else {
-    y.x = fmaf(m.x, t.x, fmaf(-m.y, t.y, y.x));
-    y.y = fmaf(m.x, t.y, fmaf(m.y, t.x, y.y));
-  }
-}
-
-// t[a] = sum_b K[a, b] X[j, b] for AB consecutive k columns a (Ks points at
-// the first; rows of NKP floats) and this thread's vector; X is read in groups
-// of 4 independent loads, the next group issued before the current one is used
-template <int NKP, int AB, int KT>
-__device__ __forceinline__ void kb_trow(const float2* xr, long long nb, int nk2, const float* Ks, float2* t) {
-#pragma unroll
-  for (int a = 0; a < AB; ++a) t[a] = make_float2(0.f, 0.f);
-  float2 xn[4];
-#pragma unroll
-  for (int u = 0; u < 4; ++u) xn[u] = (u < nk2) ? xr[(long long)u * nb] : make_float2(0.f, 0.f);
-  for (int b0 = 0; b0 < nk2; b0 += 4) {
-    float2 x[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) x[u] = xn[u];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int bn = b0 + 4 + u;
-      xn[u] = (bn < nk2) ? xr[(long long)bn * nb] : make_float2(0.f, 0.f);
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int b = b0 + u;  // Ks rows beyond nk2 hold zeros
-      const float* kr = Ks + b * NKP;
-      const float* ki = Ks + (36 + b) * NKP;
-#pragma unroll
-      for (int a = 0; a < AB; a += 4) {
-        const float4 r4 = *reinterpret_cast<const float4*>(kr + a);
-        float4 i4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (KT == 0) i4 = *reinterpret_cast<const float4*>(ki + a);
-        kacc<KT>(t[a], r4.x, i4.x, x[u]);
-        kacc<KT>(t[a + 1], r4.y, i4.y, x[u]);
-        kacc<KT>(t[a + 2], r4.z, i4.z, x[u]);
-        kacc<KT>(t[a + 3], r4.w, i4.w, x[u]);
-      }
-    }
-  }
-}
-
-// T rows jr < nrow for the input rows j0 + jr into Ts[jr]; rows outside the
-// input slab [0, dm2) are zero. (row, half-row) units go round-robin over the
-// 8 warps.
-template <int NKP>
-__device__ __forceinline__ void kb_tstep(const float2* Xs2, long long nb, int nk2, int ktype, const float* Ks,
-                                         float2* Ts, int j0, int nrow, int dm2, int wid, int lane) {
-  constexpr int NH = NKP >= 8 ? 2 : 1;
-  constexpr int AB = NKP / NH;
-  for (int u = wid; u < nrow * NH; u += 8) {
-    const int jr = u / NH, h = u - jr * NH;
-    const int j = j0 + jr;
-    float2 t[AB];
-    if (j >= 0 && j < dm2) {
-      const float2* xr = Xs2 + (long long)j * nk2 * nb;
-      if (ktype == 1) kb_trow<NKP, AB, 1>(xr, nb, nk2, Ks + h * AB, t);
-      else if (ktype == 2) kb_trow<NKP, AB, 2>(xr, nb, nk2, Ks + h * AB, t);
-      else kb_trow<NKP, AB, 0>(xr, nb, nk2, Ks + h * AB, t);
-    } else {
-#pragma unroll
-      for (int a = 0; a < AB; ++a) t[a] = make_float2(0.f, 0.f);
-    }
-    float2* tr = Ts + (jr * NKP + h * AB) * 32 + lane;
-#pragma unroll
-    for (int a = 0; a < AB; ++a) tr[a * 32] = t[a];
-  }
-}
-
-// M step of a diagonal group for tile rows r0 .. r0 + 3 (< nr) and k columns
-// a0 .. a0 + 3: the T row of (row r, slot w) is r + w
-template <int NKP, int MT>
-__device__ __forceinline__ void kb_mdia(float2* y, const float2* Ts, const float2* MFs, int W, int r0, int a0,
-                                        int nr, int lane) {
-  for (int cw = 0; cw < W + 3; ++cw) {
-    float2 t[4];
-    const float2* tr = Ts + ((r0 + cw) * NKP + a0) * 32 + lane;
-#pragma unroll
-    for (int aa = 0; aa < 4; ++aa) t[aa] = tr[aa * 32];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const int w = cw - r;
-      if (w >= 0 && w < W && r0 + r < nr) {
-        const float2 m = MFs[(r0 + r) * KB_WMAX + w];
-#pragma unroll
-        for (int aa = 0; aa < 4; ++aa) macc<MT>(y[r * 4 + aa], m, t[aa]);
-      }
-    }
-  }
-}
-
-// M step of an ELL group over one chunk of T rows [jc, jc + nj)
-template <int NKP, int MT>
-__device__ __forceinline__ void kb_mell(float2* y, const float2* Ts, const float2* MFs, const int* Cs, int W, int jc,
-                                        int nj, int r0, int a0, int nr, int lane) {
-  for (int w = 0; w < W; ++w) {
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      if (r0 + r >= nr) continue;
-      const int c = Cs[(r0 + r) * KB_WMAX + w] - jc;
-      if (c < 0 || c >= nj) continue;
-      const float2 m = MFs[(r0 + r) * KB_WMAX + w];
-      const float2* tr = Ts + (c * NKP + a0) * 32 + lane;
-#pragma unroll
-      for (int aa = 0; aa < 4; ++aa) macc<MT>(y[r * 4 + aa], m, tr[aa * 32]);
-    }
-  }
-}
-
-template <int NKP>
-__device__ void kb_tile(const BatchMV& p, int s1, int i0, int nr, float* smem) {
-  constexpr int R = 128 / NKP;            // rows of the tile
-  constexpr int NJ = R + KR_DIAG_MAX - 1; // T rows held: a diagonal band, or one ELL chunk
-  constexpr int NAB = NKP / 4;            // 4-wide k-column blocks
-  const DevOp& op = p.op;
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const long long nb = p.nb;
-  const int v = blockIdx.y * 32 + lane;
-  const int r0 = (wid / NAB) * 4, a0 = (wid % NAB) * 4;  // this thread's outputs
-  float2* Ts = reinterpret_cast<float2*>(smem);                 // [NJ][NKP][32]
-  float* Ks = smem + 2 * NJ * NKP * 32;                          // [2][36][NKP]
-  float2* MFs = reinterpret_cast<float2*>(Ks + 2 * 36 * NKP);   // [R][KB_WMAX]
-  int* Cs = reinterpret_cast<int*>(MFs + R * KB_WMAX);           // [R][KB_WMAX]
-  int* meta = Cs + R * KB_WMAX;                                  // ELL band window jmin, jmax
-  const int nk1 = __ldg(op.out_dk + s1);
-  float2 y[16];
-#pragma unroll
-  for (int q = 0; q < 16; ++q) y[q] = make_float2(0.f, 0.f);
-  const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
-  for (int term = tb; term < te; ++term) {
-    const int s2 = __ldg(op.t_in + term);
-    const int kb = __ldg(op.t_k + term);
-    const int mfi = __ldg(op.t_mf + term);
-    const int nk2 = __ldg(op.in_dk + s2);
-    const int dm2 = __ldg(op.in_dm + s2);
-    const int Wst = __ldg(op.mf_width + mfi);  // stored width (row stride of MF)
-    const int d0s = __ldg(op.mf_diag + mfi);
-    const bool dia = d0s != KR_NO_DIAG && Wst <= KR_DIAG_MAX;
-    // slots that carry a value with the current field (the field kernel's band)
-    const int bhi = __ldcg(op.mf_band + 2 * mfi + 1);
-    if (bhi < 0) continue;  // MF is zero with this field: no contribution (uniform)
-    const int wlo = dia ? Wst - 1 - __ldcg(op.mf_band + 2 * mfi) : 0;
-    const int W = dia ? bhi - wlo + 1 : Wst;
-    const int d0 = dia ? d0s + wlo : 0;
-    const int ktype = __ldg(op.k_type + kb);
-    const int mtype = __ldcg(op.mf_type + mfi);
-    const int kw = (ktype == 0) ? 2 : 1;
-    const float* KT = op.k_f32 + __ldg(op.k_off + kb);
-    const int* col = op.m_col + __ldg(op.mf_col_off + mfi);
-    const float2* mf = op.mf_f32 + __ldg(op.mf_off + mfi) + wlo;
-    __syncthreads();  // the previous term is done with Ks, MFs, Cs, Ts
-    // K^T as [plane][b][a], zero outside nk2 x nk1 (rows up to the next multiple of 4)
-    const int nb4 = (nk2 + 3) & ~3;
-    for (int e = tid; e < kw * nb4 * NKP; e += blockDim.x) {
-      const int plane = e / (nb4 * NKP);
-      const int rem = e - plane * nb4 * NKP;
-      const int b = rem / NKP, a = rem - b * NKP;
-      Ks[(plane * 36 + b) * NKP + a] =
-          (a < nk1 && b < nk2) ? __ldg(KT + ((long long)b * nk1 + a) * kw + plane) : 0.f;
-    }
-    for (int e = tid; e < nr * W; e += blockDim.x) {
-      const int r = e / W, w = e - r * W;
-      const long long src = (long long)(i0 + r) * Wst + w;
-      MFs[r * KB_WMAX + w] = __ldcg(mf + src);
-      if (!dia) Cs[r * KB_WMAX + w] = __ldg(col + src);
-    }
-    if (!dia && wid == 0) {
-      int lo = 0x7fffffff, hi = -1;
-      for (int e = lane; e < nr * W; e += 32) {
-        const int c = __ldg(col + (long long)(i0 + e / W) * Wst + (e % W));
-        lo = min(lo, c);
-        hi = max(hi, c);
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-      }
-      if (lane == 0) {
-        meta[0] = lo;
-        meta[1] = hi;
-      }
-    }
-    __syncthreads();
-    const float2* Xs2 = p.X + (long long)__ldg(op.in_off + s2) * nb + v;
-    if (dia) {
-      // T rows of the band: input rows i0 + d0 .. i0 + d0 + nr + W - 2
-      kb_tstep<NKP>(Xs2, nb, nk2, ktype, Ks, Ts, i0 + d0, nr + W - 1, dm2, wid, lane);
-      __syncthreads();
-      if (mtype == 1) kb_mdia<NKP, 1>(y, Ts, MFs, W, r0, a0, nr, lane);
-      else if (mtype == 2) kb_mdia<NKP, 2>(y, Ts, MFs, W, r0, a0, nr, lane);
-      else kb_mdia<NKP, 0>(y, Ts, MFs, W, r0, a0, nr, lane);
-    } else {
-      const int jmin = meta[0], jmax = meta[1];
-      for (int jc = jmin; jc <= jmax; jc += NJ) {
-        const int nj = min(NJ, jmax - jc + 1);
-        if (jc != jmin) __syncthreads();  // the previous chunk's M step is done with Ts
-        kb_tstep<NKP>(Xs2, nb, nk2, ktype, Ks, Ts, jc, nj, dm2, wid, lane);
-        __syncthreads();
-        if (mtype == 1) kb_mell<NKP, 1>(y, Ts, MFs, Cs, W, jc, nj, r0, a0, nr, lane);
-        else if (mtype == 2) kb_mell<NKP, 2>(y, Ts, MFs, Cs, W, jc, nj, r0, a0, nr, lane);
-        else kb_mell<NKP, 0>(y, Ts, MFs, Cs, W, jc, nj, r0, a0, nr, lane);
-      }
-    }
-  }
-  float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * nk1) * nb + v;
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-#pragma unroll
-    for (int aa = 0; aa < 4; ++aa) {
-      const int i = r0 + r, a = a0 + aa;
-      if (i < nr && a < nk1) Y[((long long)i * nk1 + a) * nb] = y[r * 4 + aa];
-    }
-  }
-}
-
-__global__ void __launch_bounds__(256, 2) kb_matvec(BatchMV p) {
-  extern __shared__ __align__(16) float kb_smem[];
-  const int task = blockIdx.x;
-  if (p.grp_active && !p.grp_active[blockIdx.y]) return;
-  const int s1 = __ldg(p.task_slab + task);
-  const int i0 = __ldg(p.task_i0 + task);
-  const int nr = __ldg(p.task_nr + task);
-  const int nk1 = __ldg(p.op.out_dk + s1);
-  if (nk1 <= 4) kb_tile<4>(p, s1, i0, nr, kb_smem);
-  else if (nk1 <= 8) kb_tile<8>(p, s1, i0, nr, kb_smem);
-  else if (nk1 <= 16) kb_tile<16>(p, s1, i0, nr, kb_smem);
-  else kb_tile<32>(p, s1, i0, nr, kb_smem);
-}
-
-// shared memory of kb_matvec: the largest of the four tile shapes
-static size_t kb_matvec_smem() {
-  size_t best = 0;
-  for (int nkp : {4, 8, 16, 32}) {
-    const int R = 128 / nkp, NJ = R + KR_DIAG_MAX - 1;
-    size_t b = sizeof(float2) * NJ * nkp * 32 + sizeof(float) * 2 * 36 * nkp + sizeof(float2) * R * KB_WMAX +
-               sizeof(int) * (R * KB_WMAX + 2);
-    best = std::max(best, b);
-  }
-  return best;
-}
-
-// ---------------------------------------------------------------------------
-// batched mat-vec on the tensor cores. One CTA (256 threads = 8 warps) computes
-// a tile of R consecutive output rows of one slab, all its k columns, for 128
-// vectors. Per term:
-//   Z[i][b][v]  = sum_w MF[i, w] X[col(i, w)][b][v]      SIMT, FP32 registers
-//   Y[i][a][v] += sum_b K[a, b] Z[i][b][v]               tcgen05.mma
-// (field.py:1212-1243 orders the same sum as MF (K X^T)^T). The K contraction
-// runs as 128 x NP x 8 TF32 MMAs with the vectors as the M dimension: the real
-// and imaginary parts of Z_i, each split hi + lo (3xTF32: hi*hi + hi*lo +
-// lo*hi), form the A operands; K^T, split likewise, the B operands; the real
-// and imaginary parts of Y_i accumulate in TMEM over all terms of the slab.
-// KP = n_k2 padded to 8 (largest over the slab's terms) is the MMA K extent,
-// R = 64 / KP, NP = n_k1 padded to 16 the MMA N. The SIMT part of term t + 1
-// (X loads and M-band FMAs) runs while the MMAs of term t execute; only the
-// A-tile stores wait for them.
-// Threads: warp w owns vectors 32 (w % 4) .. + 31 (= TMEM lanes) and input k
-// columns [KP/2 (w / 4), KP/2 (w / 4 + 1)).
-// ---------------------------------------------------------------------------
-struct BatchTC {
-  DevOp op;
-  const float2* X;
-  float2* Y;
-  int nb;
-  const int* task;        // [4][ntask]: slab, first row, rows, KP
-  int ntask;
-  const int* grp_active;  // per 32-vector group: any vector active (null: all)
-  int* err;
-};
-
-constexpr int TC_ABYTES = 128 * 1024;       // A tiles: R rows x 4 parts x 128 x KP FP32 (R KP = 64)
-constexpr int TC_BPART = 32 * 32 * 4;       // one B part: NP x KP FP32 at most
-constexpr int TC_BBYTES = 6 * TC_BPART;     // one B buffer: K_re, K_im, -K_im, each hi and lo
-constexpr int TC_MFBYTES = 2 * 8 * KB_WMAX * 8;
-constexpr int TC_CSBYTES = 2 * 8 * KB_WMAX * 4;
-constexpr int TC_SMEM = TC_ABYTES + 2 * TC_BBYTES + TC_MFBYTES + TC_CSBYTES + 64;
-
-// X window of one term in registers: input rows j0 + c (c < RP) for this
-// thread's vector and KP/2 input columns; RP * KP/2 = 16 loads issued back to
-// back (rows outside [0, dm2) and columns beyond n_k2 read as zero)
-template <int KP>
-struct KbtWin {
-  static constexpr int BH = KP / 2, RP = 32 / KP;
-  float2 x[RP][BH];
-  __device__ __forceinline__ void load(const float2* Xs2, long long nb, int nk2, int dm2, int j0, int nrow, int b0) {
-#pragma unroll
-    for (int c = 0; c < RP; ++c) {
-      const int j = j0 + c;
-      const bool rin = c < nrow && j >= 0 && j < dm2;
-      const float2* xr = Xs2 + (long long)j * nk2 * nb;
-#pragma unroll
-      for (int q = 0; q < BH; ++q)
-        x[c][q] = (rin && b0 + q < nk2) ? __ldg(xr + (long long)(b0 + q) * nb) : make_float2(0.f, 0.f);
-    }
-  }
-};
-
-// M step of a diagonal term for window rows cw0 .. cw0 + RP - 1 held in xw:
-// output row r takes slot w = cw - r
-template <int KP, int MT>
-__device__ __forceinline__ void kbt_mdia(float2 (&z)[64 / KP][KP / 2], const KbtWin<KP>& xw, int cw0, int nr, int W,
-                                         const float2* MFs) {
-  constexpr int R = 64 / KP, BH = KP / 2, RP = 32 / KP;
-#pragma unroll
-  for (int c = 0; c < RP; ++c) {
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int w = cw0 + c - r;
-      if (w >= 0 && w < W && r < nr) {
-        const float2 m = MFs[r * KB_WMAX + w];
-#pragma unroll
-        for (int q = 0; q < BH; ++q) macc<MT>(z[r][q], m, xw.x[c][q]);
-      }
-    }
-  }
-}
-
-// M step of a term with stored columns (ELL), one input row per slot
-template <int KP, int MT>
-__device__ __forceinline__ void kbt_mell(float2 (&z)[64 / KP][KP / 2], const float2* Xs2, long long nb, int nk2,
-                                         int nr, int W, int b0, const float2* MFs, const int* Cs) {
-  constexpr int R = 64 / KP, BH = KP / 2;
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    if (r >= nr) continue;
-    for (int w = 0; w < W; ++w) {
-      const float2* xr = Xs2 + (long long)Cs[r * KB_WMAX + w] * nk2 * nb;
-      const float2 m = MFs[r * KB_WMAX + w];
-      float2 x[BH];
-#pragma unroll
-      for (int q = 0; q < BH; ++q) x[q] = (b0 + q < nk2) ? __ldg(xr + (long long)(b0 + q) * nb) : make_float2(0.f, 0.f);
-#pragma unroll
-      for (int q = 0; q < BH; ++q) macc<MT>(z[r][q], m, x[q]);
-    }
-  }
-}
-
-template <int KP, int MT>
-__device__ __forceinline__ void kbt_mstep(float2 (&z)[64 / KP][KP / 2], KbtWin<KP>& xw, bool loaded,
-                                          const float2* Xs2, long long nb, int nk2, int dm2, int i0, int nr, int d0,
-                                          int W, int b0, const float2* MFs, const int* Cs, bool dia) {
-  constexpr int RP = 32 / KP;
-  if (dia) {
-    const int nwin = nr + W - 1;
-    for (int cw0 = 0; cw0 < nwin; cw0 += RP) {
-      if (cw0 > 0 || !loaded) xw.load(Xs2, nb, nk2, dm2, i0 + d0 + cw0, nwin - cw0, b0);
-      kbt_mdia<KP, MT>(z, xw, cw0, nr, W, MFs);
-    }
-  } else {
-    kbt_mell<KP, MT>(z, Xs2, nb, nk2, nr, W, b0, MFs, Cs);
-  }
-}
-
-// one term of a tensor-core tile: its tables and shared-memory staging
-struct KbtTerm {
-  int s2, nk2, dm2, W, Wst, d0, ktype, mtype;
-  bool dia, ok, empty;
-  const float* KT;
-  const int* col;
-  const float2* mf;
-  const float2* Xs2;
-};
-
-__device__ __forceinline__ KbtTerm kbt_term(const DevOp& op, const BatchTC& p, int term, int KP, int v, long long nb) {
-  KbtTerm t;
-  t.s2 = __ldg(op.t_in + term);
-  const int kb = __ldg(op.t_k + term);
-  const int mfi = __ldg(op.t_mf + term);
-  t.nk2 = __ldg(op.in_dk + t.s2);
-  t.dm2 = __ldg(op.in_dm + t.s2);
-  t.Wst = __ldg(op.mf_width + mfi);
-  const int d0s = __ldg(op.mf_diag + mfi);
-  t.dia = d0s != KR_NO_DIAG && t.Wst <= KR_DIAG_MAX;
-  // slots that carry a value with the current field (the field kernel's band)
-  const int bhi = __ldcg(op.mf_band + 2 * mfi + 1);
-  t.empty = bhi < 0;
-  const int wlo = (t.dia && !t.empty) ? t.Wst - 1 - __ldcg(op.mf_band + 2 * mfi) : 0;
-  t.W = (t.dia && !t.empty) ? bhi - wlo + 1 : t.Wst;
-  t.d0 = t.dia ? d0s + wlo : 0;
-  t.ktype = __ldg(op.k_type + kb);
-  t.mtype = __ldcg(op.mf_type + mfi);
-  t.ok = t.nk2 <= KP && t.Wst <= KB_WMAX;
-  t.KT = op.k_f32 + __ldg(op.k_off + kb);
-  t.col = op.m_col + __ldg(op.mf_col_off + mfi);
-  t.mf = op.mf_f32 + __ldg(op.mf_off + mfi) + wlo;
-  t.Xs2 = p.X + (long long)__ldg(op.in_off + t.s2) * nb + v;
-  return t;
-}
-
-// B operands of a term: K^T (b, a) -> row a, column b; parts K_re, K_im, -K_im,
-// each hi and lo; zero outside n_k1 x n_k2. MF rows (and ELL columns).
-template <int KP>
-__device__ __forceinline__ void kbt_stage(const KbtTerm& t, int nk1, int NP, int i0, int nr, float* Bt, float2* MFs,
-                                          int* Cs, int tid, int bpart = TC_BPART) {
-  for (int e = tid; e < NP * KP; e += 256) {  // producers only
-    const int a = e / KP, b = e - (e / KP) * KP;
-    float kr = 0.f, ki = 0.f;
-    if (a < nk1 && b < t.nk2) {
-      if (t.ktype == 0) {
-        kr = __ldg(t.KT + ((long long)b * nk1 + a) * 2);
-        ki = __ldg(t.KT + ((long long)b * nk1 + a) * 2 + 1);
-      } else if (t.ktype == 1) {
-        kr = __ldg(t.KT + (long long)b * nk1 + a);
-      } else {
-        ki = __ldg(t.KT + (long long)b * nk1 + a);
-      }
-    }
-    const uint32_t o = tc_kmajor_off(a, b, KP) >> 2;
-    const float krh = tc_tf32(kr), kih = tc_tf32(ki);
-    Bt[0 * (bpart / 4) + o] = krh;
-    Bt[1 * (bpart / 4) + o] = kr - krh;
-    Bt[2 * (bpart / 4) + o] = kih;
-    Bt[3 * (bpart / 4) + o] = ki - kih;
-    Bt[4 * (bpart / 4) + o] = -kih;
-    Bt[5 * (bpart / 4) + o] = -(ki - kih);
-  }
-  const int W = t.W;
-  for (int e = tid; e < nr * W; e += 256) {
-    const int r = e / W, w = e - (e / W) * W;
-    const long long src = (long long)(i0 + r) * t.Wst + w;
-    MFs[r * KB_WMAX + w] = __ldcg(t.mf + src);
-    if (!t.dia) Cs[r * KB_WMAX + w] = __ldg(t.col + src);
-  }
-}
-
-template <int KP>
-__device__ __forceinline__ void kbt_zstep(float2 (&z)[64 / KP][KP / 2], KbtWin<KP>& xw, const KbtTerm& t,
-                                          long long nb, int i0, int nr, int b0, const float2* MFs, const int* Cs) {
-  constexpr int R = 64 / KP, BH = KP / 2;
-#pragma unroll
-  for (int r = 0; r < R; ++r)
-#pragma unroll
-    for (int q = 0; q < BH; ++q) z[r][q] = make_float2(0.f, 0.f);
-  if (!t.ok || t.empty) return;
-  if (t.mtype == 1) kbt_mstep<KP, 1>(z, xw, true, t.Xs2, nb, t.nk2, t.dm2, i0, nr, t.d0, t.W, b0, MFs, Cs, t.dia);
-  else if (t.mtype == 2) kbt_mstep<KP, 2>(z, xw, true, t.Xs2, nb, t.nk2, t.dm2, i0, nr, t.d0, t.W, b0, MFs, Cs, t.dia);
-  else kbt_mstep<KP, 0>(z, xw, true, t.Xs2, nb, t.nk2, t.dm2, i0, nr, t.d0, t.W, b0, MFs, Cs, t.dia);
-}
-
-// producer-only barrier (warps 0-7) that leaves the MMA warp out
-__device__ __forceinline__ void kbt_producer_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
-
-// issues the MMAs of one term (one thread): D_re += Z_re K_re - Z_im K_im,
-// D_im += Z_re K_im + Z_im K_re, each product as three TF32 MMAs per K step
-// (A hi B hi, A hi B lo, A lo B hi); zero parts of K skipped
-template <int KP>
-__device__ __forceinline__ void kbt_issue(uint32_t tmem, uint64_t adesc0, uint64_t bdesc, uint32_t idesc, int NP,
-                                          int nr, int ktype, int nk2, uint32_t& dinit, int bpart = TC_BPART) {
-  constexpr int ATILE = 128 * KP;
-  int pd[4], pa[4], pb[4];
-  int np = 0;
-  if (ktype != 2) {
-    pd[np] = 0; pa[np] = 0; pb[np] = 0; ++np;  // re <- Z_re K_re
-    pd[np] = 1; pa[np] = 2; pb[np] = 0; ++np;  // im <- Z_im K_re
-  }
-  if (ktype != 1) {
-    pd[np] = 0; pa[np] = 2; pb[np] = 4; ++np;  // re <- Z_im (-K_im)
-    pd[np] = 1; pa[np] = 0; pb[np] = 2; ++np;  // im <- Z_re K_im
-  }
-  const int nks = (nk2 + 7) >> 3;
-  // descriptor start addresses advance by (byte offset >> 4)
-  for (int r = 0; r < nr; ++r) {
-    for (int q = 0; q < np; ++q) {
-      const uint32_t dcol = tmem + (uint32_t)((2 * r + pd[q]) * NP);
-      const uint32_t dbit = 1u << (2 * r + pd[q]);
-      const uint64_t ad = adesc0 + (uint64_t)(((r * 4 + pa[q]) * ATILE * 4) >> 4);
-      const uint64_t bd = bdesc + (uint64_t)((pb[q] * bpart) >> 4);
-#pragma unroll
-      for (int sp = 0; sp < 3; ++sp) {
-        const uint64_t a2 = ad + (sp == 2 ? (uint64_t)((ATILE * 4) >> 4) : 0);
-        const uint64_t b2 = bd + (sp == 1 ? (uint64_t)(bpart >> 4) : 0);
-#pragma unroll
-        for (int ks = 0; ks < KP / 8; ++ks) {
-          if (ks < nks) {
-            tc_mma_tf32(dcol, a2 + 16u * ks, b2 + 16u * ks, idesc, (dinit & dbit) ? 1u : 0u);
-            dinit |= dbit;
-          }
-        }
-      }
-    }
-  }
-}
-
-// Warp-specialised pipeline over the terms of the tile. Warps 0-7 (producers)
-// compute Z and store the A tiles; warp 8 issues the MMAs. full: the A tiles
-// (and the B buffer) of a term are stored (256 arrivals); empty: the MMAs of a
-// term are done (tcgen05.commit). The X window of term t + 1 is requested
-// before the A tiles of term t are stored, and the MMAs of term t run while
-// the producers compute Z of term t + 1.
-template <int KP>
-__device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
-  constexpr int R = 64 / KP, BH = KP / 2;
-  constexpr int ATILE = 128 * KP;  // floats of one A tile
-  const DevOp& op = p.op;
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const bool producer = wid < 8;
-  const int vq = wid & 3, b0 = ((wid >> 2) & 1) * BH;
-  const int vloc = vq * 32 + lane;
-  const long long nb = p.nb;
-  const int v = blockIdx.y * 128 + vloc;
-  float* As = reinterpret_cast<float*>(smem);
-  char* Bs = smem + TC_ABYTES;
-  float2* MFs0 = reinterpret_cast<float2*>(Bs + 2 * TC_BBYTES);          // [2][8][KB_WMAX]
-  int* Cs0 = reinterpret_cast<int*>(Bs + 2 * TC_BBYTES + TC_MFBYTES);   // [2][8][KB_WMAX]
-  uint64_t* full = reinterpret_cast<uint64_t*>(Bs + 2 * TC_BBYTES + TC_MFBYTES + TC_CSBYTES);
-  uint64_t* empty = full + 1;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(full + 2);
-  const int nk1 = __ldg(op.out_dk + s1);
-  const int NP = nk1 <= 16 ? 16 : 32;
-  float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * nk1) * nb + v;
-  const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
-  if (te == tb) {  // no term reaches this slab
-    if (producer)
-      for (int e = wid >> 2; e < nr * nk1; e += 2) Y[(long long)e * nb] = make_float2(0.f, 0.f);
-    return;
-  }
-  uint32_t ncols = 32;
-  while (ncols < (uint32_t)(2 * R * NP)) ncols <<= 1;
-  if (wid == 8) tc_alloc(tslot, ncols);
-  if (tid == 256) {
-    tc_mbar_init(full, 256);
-    tc_mbar_init(empty, 1);
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = *tslot;
-  bool ok = true;
-  int ncommit = 0;  // terms whose MMAs were (or will be) committed
-
-  if (!producer) {
-    // ---- MMA warp (warp 8; warp 9 idles here) ------------------------------
-    if (wid == 8 && lane == 0) {
-      const uint32_t idesc = tc_idesc_tf32(128, NP);
-      const uint64_t adesc0 = tc_desc(tc_smem_u32(As), 128u, 32u * KP);
-      const uint64_t bdesc0 = tc_desc(tc_smem_u32(Bs), 128u, 32u * KP);
-      uint32_t dinit = 0;
-      for (int term = tb; term < te; ++term) {
-        const int s2 = __ldg(op.t_in + term);
-        const int nk2 = __ldg(op.in_dk + s2);
-        const int W = __ldg(op.mf_width + __ldg(op.t_mf + term));
-        if (!(nk2 <= KP && W <= KB_WMAX)) continue;
-        if (__ldcg(op.mf_band + 2 * __ldg(op.t_mf + term) + 1) < 0) continue;  // MF zero with this field
-        const int ktype = __ldg(op.k_type + __ldg(op.t_k + term));
-        if (!tc_mbar_wait(full, (uint32_t)ncommit & 1u)) ok = false;
-        tc_fence_after();
-        const uint64_t bdesc = bdesc0 + (uint64_t)((((term - tb) & 1) * TC_BBYTES) >> 4);
-        kbt_issue<KP>(tmem, adesc0, bdesc, idesc, NP, nr, ktype, nk2, dinit);
-        tc_commit(empty);
-        ++ncommit;
-      }
-      if (!ok) atomicExch(p.err, KR_ERR_TIMEOUT);
-    }
-    tc_fence_before();
-    __syncthreads();
-    if (wid == 8) tc_dealloc(tmem, ncols);
-    return;
-  }
-
-  // ---- producers -----------------------------------------------------------
-  float2 z[R][BH];
-  KbtWin<KP> xw;
-  KbtTerm cur = kbt_term(op, p, tb, KP, v, nb);
-  if (cur.ok && !cur.empty && cur.dia) xw.load(cur.Xs2, nb, cur.nk2, cur.dm2, i0 + cur.d0, nr + cur.W - 1, b0);
-  kbt_stage<KP>(cur, nk1, NP, i0, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, tid);
-  kbt_producer_sync();
-  kbt_zstep<KP>(z, xw, cur, nb, i0, nr, b0, MFs0, Cs0);
-  for (int term = tb; term < te; ++term) {
-    const int buf = (term - tb) & 1;
-    const bool has_next = term + 1 < te;
-    KbtTerm nxt;
-    if (has_next) {
-      nxt = kbt_term(op, p, term + 1, KP, v, nb);
-      if (nxt.ok && !nxt.empty && nxt.dia) xw.load(nxt.Xs2, nb, nxt.nk2, nxt.dm2, i0 + nxt.d0, nr + nxt.W - 1, b0);
-    }
-    // the MMAs of the previous committed term are done with the A tiles and its B buffer
-    if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
-    tc_fence_after();
-    if (cur.ok && !cur.empty) {
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        if (r >= nr) continue;
-        float* At = As + r * 4 * ATILE;
-#pragma unroll
-        for (int c4 = 0; c4 < BH; c4 += 4) {
-          float4 rh, rl, ih, il;
-          float* prh = &rh.x;
-          float* prl = &rl.x;
-          float* pih = &ih.x;
-          float* pil = &il.x;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float2 zz = z[r][c4 + q];
-            prh[q] = tc_tf32(zz.x);
-            prl[q] = zz.x - prh[q];
-            pih[q] = tc_tf32(zz.y);
-            pil[q] = zz.y - pih[q];
-          }
-          const uint32_t o = tc_kmajor_off(vloc, b0 + c4, KP) >> 2;
-          *reinterpret_cast<float4*>(At + 0 * ATILE + o) = rh;
-          *reinterpret_cast<float4*>(At + 1 * ATILE + o) = rl;
-          *reinterpret_cast<float4*>(At + 2 * ATILE + o) = ih;
-          *reinterpret_cast<float4*>(At + 3 * ATILE + o) = il;
-        }
-      }
-      tc_fence_proxy();
-      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc_smem_u32(full)) : "memory");
-      ++ncommit;
-    } else if (!cur.ok && tid == 0) {
-      atomicExch(p.err, KR_ERR_ARG);  // outside the tile shape: skipped
-    }
-    if (has_next) {
-      // B buffer buf ^ 1 was last read by the MMAs of term - 1 (done); MF buffer
-      // buf ^ 1 by the M step of term - 1 (every producer is past it)
-      kbt_stage<KP>(nxt, nk1, NP, i0, nr, reinterpret_cast<float*>(Bs + (buf ^ 1) * TC_BBYTES),
-                    MFs0 + (buf ^ 1) * 8 * KB_WMAX, Cs0 + (buf ^ 1) * 8 * KB_WMAX, tid);
-      kbt_producer_sync();
-      kbt_zstep<KP>(z, xw, nxt, nb, i0, nr, b0, MFs0 + (buf ^ 1) * 8 * KB_WMAX, Cs0 + (buf ^ 1) * 8 * KB_WMAX);
-      cur = nxt;
-    }
-  }
-  if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
-  tc_fence_after();
-  // epilogue: rows r = w / 4, w / 4 + 2, ... of this warp's lane quarter
-  for (int r = wid >> 2; r < nr; r += 2) {
-    for (int c0 = 0; c0 < NP; c0 += 16) {
-      float re[16], im[16];
-      const uint32_t lanebase = (uint32_t)(vq * 32) << 16;
-      tc_ld16(tmem + lanebase + (uint32_t)(2 * r * NP + c0), re);
-      tc_ld16(tmem + lanebase + (uint32_t)((2 * r + 1) * NP + c0), im);
-      const bool any = ncommit > 0;
-#pragma unroll
-      for (int q = 0; q < 16; ++q)
-        if (c0 + q < nk1)
-          Y[((long long)r * nk1 + c0 + q) * nb] = any ? make_float2(re[q], im[q]) : make_float2(0.f, 0.f);
-    }
-  }
-  if (!ok && lane == 0) atomicExch(p.err, KR_ERR_TIMEOUT);
-  tc_fence_before();
-  __syncthreads();
-}
-
-
-// ---------------------------------------------------------------------------
-// Tensor-core tile with the X windows streamed by TMA (KP = 8, 16). Warp 8
-// lane 1 walks the window rows of every diagonal term of the tile in order
-// and loads each (KP input rows x 128 vectors, KP/8 boxes of 8 rows) into a
-// ring of shared-memory slots (full: tx bytes; empty: one arrival per
-// producer warp); the producer warps read X from the ring, so no global-load
-// latency sits in their M step. Rows outside the input slab read whatever
-// lies there (finite data of other slabs, or zeros beyond the array) and meet
-// zero MF slots; columns beyond n_k2 are zeroed on read. Terms stored as ELL
-// load X directly. Everything else as in kbt_tile.
-// ---------------------------------------------------------------------------
-constexpr int KBT_MAXT = 64;  // terms of one output slab held in the shared-memory table
-
-// the next term's B and MF values, loaded into registers before they are staged
-struct KbtPre {
-  float kr[2], ki[2];
-  float2 mf;
-  int col;
-};
-
-template <int KP>
-__device__ __forceinline__ void kbt_preload(const KbtTerm& t, int nk1, int NP, int i0, int nr, int tid, KbtPre& q) {
-#pragma unroll
-  for (int u = 0; u < 2; ++u) {
-    const int e = tid + 256 * u;
-    const int a = e / KP, b = e - (e / KP) * KP;
-    float kr = 0.f, ki = 0.f;
-    if (e < NP * KP && a < nk1 && b < t.nk2) {
-      if (t.ktype == 0) {
-        kr = __ldg(t.KT + ((long long)b * nk1 + a) * 2);
-        ki = __ldg(t.KT + ((long long)b * nk1 + a) * 2 + 1);
-      } else if (t.ktype == 1) {
-        kr = __ldg(t.KT + (long long)b * nk1 + a);
-      } else {
-        ki = __ldg(t.KT + (long long)b * nk1 + a);
-      }
-    }
-    q.kr[u] = kr;
-    q.ki[u] = ki;
-  }
-  q.mf = make_float2(0.f, 0.f);
-  q.col = 0;
-  if (tid < nr * t.W) {
-    const int r = tid / t.W, w = tid - (tid / t.W) * t.W;
-    const long long src = (long long)(i0 + r) * t.Wst + w;
-    q.mf = __ldcg(t.mf + src);
-    if (!t.dia) q.col = __ldg(t.col + src);
-  }
-}
-
-template <int KP>
-__device__ __forceinline__ void kbt_stage_pre(const KbtTerm& t, const KbtPre& q, int NP, int nr, float* Bt,
-                                              float2* MFs, int* Cs, int tid, int bpart) {
-#pragma unroll
-  for (int u = 0; u < 2; ++u) {
-    const int e = tid + 256 * u;
-    if (e >= NP * KP) break;
-    const int a = e / KP, b = e - (e / KP) * KP;
-    const uint32_t o = tc_kmajor_off(a, b, KP) >> 2;
-    const float kr = q.kr[u], ki = q.ki[u];
-    const float krh = tc_tf32(kr), kih = tc_tf32(ki);
-    Bt[0 * (bpart / 4) + o] = krh;
-    Bt[1 * (bpart / 4) + o] = kr - krh;
-    Bt[2 * (bpart / 4) + o] = kih;
-    Bt[3 * (bpart / 4) + o] = ki - kih;
-    Bt[4 * (bpart / 4) + o] = -kih;
-    Bt[5 * (bpart / 4) + o] = -(ki - kih);
-  }
-  if (tid < nr * t.W) {
-    const int r = tid / t.W, w = tid - (tid / t.W) * t.W;
-    MFs[r * KB_WMAX + w] = q.mf;
-    if (!t.dia) Cs[r * KB_WMAX + w] = q.col;
-  }
-}
-
-template <int KP>
-struct KbtRing {
-  static constexpr int NSLOT = 64 / KP;          // slots of KP rows x 128 vectors x 8 bytes
-  static constexpr int SLOT = KP * 1024;
-  static constexpr int BPART = 128 * KP;         // one B part: NP (<= 32) x KP FP32
-  static constexpr int BBUF = 6 * BPART;
-  static constexpr int OFF_B = TC_ABYTES;
-  static constexpr int OFF_RING = OFF_B + 2 * BBUF;
-  static constexpr int OFF_MF = OFF_RING + NSLOT * SLOT;
-  static constexpr int OFF_CS = OFF_MF + TC_MFBYTES;
-  static constexpr int OFF_BAR = OFF_CS + TC_CSBYTES;
-  static constexpr int OFF_TAB = OFF_BAR + 8 * (2 + 2 * NSLOT) + 16;  // term table (KBT_MAXT entries)
-  static constexpr int TOTAL = OFF_TAB + KBT_MAXT * (int)sizeof(KbtTerm);
-};
-constexpr int TC_SMEM_RING = KbtRing<16>::TOTAL > KbtRing<8>::TOTAL ? KbtRing<16>::TOTAL : KbtRing<8>::TOTAL;
-
-// the ring rows of one term: count, and the first input row (diagonal terms only)
-__device__ __forceinline__ int kbt_ring_rows(const KbtTerm& t, int nr) {
-  return (t.ok && !t.empty && t.dia) ? nr + t.W - 1 : 0;
-}
-
-// M step of a diagonal term from the ring; g: ring row counter (advanced)
-template <int KP, int MT>
-__device__ __forceinline__ bool kbt_mdia_ring(float2 (&z)[64 / KP][KP / 2], const char* ring, uint64_t* rfull,
-                                              uint64_t* rempty, int& g, int nwin, int nr, int W, int nk2, int b0,
-                                              int vloc, int lane, const float2* MFs) {
-  constexpr int R = 64 / KP, BH = KP / 2, NSLOT = KbtRing<KP>::NSLOT;
-  bool ok = true;
-  for (int c = 0; c < nwin; ++c, ++g) {
-    const int slot = g % NSLOT;
-    if (!tc_mbar_wait(rfull + slot, (uint32_t)(g / NSLOT) & 1u)) ok = false;
-    const float2* xs = reinterpret_cast<const float2*>(ring + (size_t)slot * KbtRing<KP>::SLOT) + vloc;
-    float2 x[BH];
-#pragma unroll
-    for (int q = 0; q < BH; ++q) x[q] = (b0 + q < nk2) ? xs[(b0 + q) * 128] : make_float2(0.f, 0.f);
-    __syncwarp();
-    if (lane == 0) tc_mbar_arrive(rempty + slot);
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int w = c - r;
-      if (w >= 0 && w < W && r < nr) {
-        const float2 m = MFs[r * KB_WMAX + w];
-#pragma unroll
-        for (int q = 0; q < BH; ++q) macc<MT>(z[r][q], m, x[q]);
-      }
-    }
-  }
-  return ok;
-}
-
-template <int KP>
-__device__ __forceinline__ bool kbt_zstep_ring(float2 (&z)[64 / KP][KP / 2], const KbtTerm& t, long long nb, int nr,
-                                               int b0, int vloc, int lane, const float2* MFs, const int* Cs,
-                                               const char* ring, uint64_t* rfull, uint64_t* rempty, int& g) {
-  constexpr int R = 64 / KP, BH = KP / 2;
-#pragma unroll
-  for (int r = 0; r < R; ++r)
-#pragma unroll
-    for (int q = 0; q < BH; ++q) z[r][q] = make_float2(0.f, 0.f);
-  if (!t.ok || t.empty) return true;
-  const int nwin = kbt_ring_rows(t, nr);
-  if (t.dia) {
-    if (t.mtype == 1) return kbt_mdia_ring<KP, 1>(z, ring, rfull, rempty, g, nwin, nr, t.W, t.nk2, b0, vloc, lane, MFs);
-    if (t.mtype == 2) return kbt_mdia_ring<KP, 2>(z, ring, rfull, rempty, g, nwin, nr, t.W, t.nk2, b0, vloc, lane, MFs);
-    return kbt_mdia_ring<KP, 0>(z, ring, rfull, rempty, g, nwin, nr, t.W, t.nk2, b0, vloc, lane, MFs);
-  }
-  if (t.mtype == 1) kbt_mell<KP, 1>(z, t.Xs2, nb, t.nk2, nr, t.W, b0, MFs, Cs);
-  else if (t.mtype == 2) kbt_mell<KP, 2>(z, t.Xs2, nb, t.nk2, nr, t.W, b0, MFs, Cs);
-  else kbt_mell<KP, 0>(z, t.Xs2, nb, t.nk2, nr, t.W, b0, MFs, Cs);
-  return true;
-}
-
-template <int KP>
-__device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1, int i0, int nr, char* smem) {
-  using L = KbtRing<KP>;
-  constexpr int R = 64 / KP, BH = KP / 2, NSLOT = L::NSLOT;
-  constexpr int ATILE = 128 * KP;  // floats of one A tile
-  const DevOp& op = p.op;
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const bool producer = wid < 8;
-  const int vq = wid & 3, b0 = ((wid >> 2) & 1) * BH;
-  const int vloc = vq * 32 + lane;
-  const long long nb = p.nb;
-  const int v = blockIdx.y * 128 + vloc;
-  float* As = reinterpret_cast<float*>(smem);
-  char* Bs = smem + L::OFF_B;
-  char* ring = smem + L::OFF_RING;
-  float2* MFs0 = reinterpret_cast<float2*>(smem + L::OFF_MF);  // [2][8][KB_WMAX]
-  int* Cs0 = reinterpret_cast<int*>(smem + L::OFF_CS);         // [2][8][KB_WMAX]
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);
-  uint64_t* empty = full + 1;
-  uint64_t* rfull = full + 2;
-  uint64_t* rempty = rfull + NSLOT;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(rempty + NSLOT);
-  KbtTerm* tab = reinterpret_cast<KbtTerm*>(smem + L::OFF_TAB);
-  const int nk1 = __ldg(op.out_dk + s1);
-  const int NP = nk1 <= 16 ? 16 : 32;
-  float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * nk1) * nb + v;
-  const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
-  if (te == tb) {  // no term reaches this slab
-    if (producer)
-      for (int e = wid >> 2; e < nr * nk1; e += 2) Y[(long long)e * nb] = make_float2(0.f, 0.f);
-    return;
-  }
-  uint32_t ncols = 32;
-  while (ncols < (uint32_t)(2 * R * NP)) ncols <<= 1;
-  if (wid == 8) tc_alloc(tslot, ncols);
-  if (tid == 256) {
-    tc_mbar_init(full, 256);
-    tc_mbar_init(empty, 1);
-    for (int i = 0; i < NSLOT; ++i) {
-      tc_mbar_init(rfull + i, 1);
-      tc_mbar_init(rempty + i, 8);
-    }
-  }
-  // term table: the tables of every term of the slab, read once per tile
-  const int nt = te - tb;
-  const bool use_tab = nt <= KBT_MAXT;
-  if (use_tab)
-    for (int i = tid; i < nt; i += blockDim.x) tab[i] = kbt_term(op, p, tb + i, KP, 0, nb);
-  auto term_at = [&](int i) {
-    KbtTerm tt = use_tab ? tab[i] : kbt_term(op, p, tb + i, KP, 0, nb);
-    tt.Xs2 += v;
-    return tt;
-  };
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = *tslot;
-  bool ok = true;
-  int ncommit = 0;  // terms whose MMAs were (or will be) committed
-
-  if (!producer) {
-    if (wid == 8 && lane == 0) {
-      // ---- MMA issue -------------------------------------------------------
-      const uint32_t idesc = tc_idesc_tf32(128, NP);
-      const uint64_t adesc0 = tc_desc(tc_smem_u32(As), 128u, 32u * KP);
-      const uint64_t bdesc0 = tc_desc(tc_smem_u32(Bs), 128u, 32u * KP);
-      uint32_t dinit = 0;
-      for (int term = tb; term < te; ++term) {
-        const KbtTerm tt = term_at(term - tb);
-        if (!tt.ok || tt.empty) continue;  // skipped by the producers as well
-        if (!tc_mbar_wait(full, (uint32_t)ncommit & 1u)) ok = false;
-        tc_fence_after();
-        const uint64_t bdesc = bdesc0 + (uint64_t)((((term - tb) & 1) * L::BBUF) >> 4);
-        kbt_issue<KP>(tmem, adesc0, bdesc, idesc, NP, nr, tt.ktype, tt.nk2, dinit, L::BPART);
-        tc_commit(empty);
-        ++ncommit;
-      }
-    } else if (wid == 9 && lane == 0) {
-      // ---- X window loads (TMA) into the ring (own warp: a waiting MMA lane
-      // would hold up a loader lane of the same warp) ------------------------
-      int g = 0;
-      for (int term = tb; term < te; ++term) {
-        const KbtTerm t = term_at(term - tb);
-        const int nwin = kbt_ring_rows(t, nr);
-        const long long row0 = __ldg(op.in_off + t.s2);  // first X row of slab s2
-        for (int c = 0; c < nwin; ++c, ++g) {
-          const int slot = g % NSLOT;
-          if (g >= NSLOT && !tc_mbar_wait(rempty + slot, (uint32_t)(g / NSLOT - 1) & 1u)) ok = false;
-          tc_mbar_expect_tx(rfull + slot, (uint32_t)L::SLOT);
-          const long long y = row0 + (long long)(i0 + t.d0 + c) * t.nk2;  // first X row of the window row
-          char* dst = ring + (size_t)slot * L::SLOT;
-#pragma unroll
-          for (int h = 0; h < KP / 8; ++h)
-            tc_tma_load_2d(dst + h * 8192, xmap, blockIdx.y * 128, (int)(y + 8 * h), rfull + slot);
-        }
-      }
-    }
-    if (!ok) atomicExch(p.err, KR_ERR_TIMEOUT);
-    tc_fence_before();
-    __syncthreads();
-    if (wid == 8) tc_dealloc(tmem, ncols);
-    return;
-  }
-
-  // ---- producers -------------------------------------------------------------
-  float2 z[R][BH];
-  int g = 0;  // ring row counter
-  KbtTerm cur = term_at(0);
-  KbtPre pre;
-  kbt_preload<KP>(cur, nk1, NP, i0, nr, tid, pre);
-  kbt_stage_pre<KP>(cur, pre, NP, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, tid, L::BPART);
-  kbt_producer_sync();
-  if (!kbt_zstep_ring<KP>(z, cur, nb, nr, b0, vloc, lane, MFs0, Cs0, ring, rfull, rempty, g)) ok = false;
-  for (int term = tb; term < te; ++term) {
-    const int buf = (term - tb) & 1;
-    const bool has_next = term + 1 < te;
-    KbtTerm nxt;
-    if (has_next) {  // the next term's K and MF values in flight during the A-tile hand-off
-      nxt = term_at(term + 1 - tb);
-      kbt_preload<KP>(nxt, nk1, NP, i0, nr, tid, pre);
-    }
-    // the MMAs of the previous committed term are done with the A tiles and its B buffer
-    if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
-    tc_fence_after();
-    if (cur.ok && !cur.empty) {
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        if (r >= nr) continue;
-        float* At = As + r * 4 * ATILE;
-#pragma unroll
-        for (int c4 = 0; c4 < BH; c4 += 4) {
-          float4 rh, rl, ih, il;
-          float* prh = &rh.x;
-          float* prl = &rl.x;
-          float* pih = &ih.x;
-          float* pil = &il.x;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float2 zz = z[r][c4 + q];
-            prh[q] = tc_tf32(zz.x);
-            prl[q] = zz.x - prh[q];
-            pih[q] = tc_tf32(zz.y);
-            pil[q] = zz.y - pih[q];
-          }
-          const uint32_t o = tc_kmajor_off(vloc, b0 + c4, KP) >> 2;
-          *reinterpret_cast<float4*>(At + 0 * ATILE + o) = rh;
-          *reinterpret_cast<float4*>(At + 1 * ATILE + o) = rl;
-          *reinterpret_cast<float4*>(At + 2 * ATILE + o) = ih;
-          *reinterpret_cast<float4*>(At + 3 * ATILE + o) = il;
-        }
-      }
-      tc_fence_proxy();
-      tc_mbar_arrive(full);
-      ++ncommit;
-    } else if (!cur.ok && tid == 0) {
-      atomicExch(p.err, KR_ERR_ARG);  // outside the tile shape: skipped
-    }
-    if (has_next) {
-      // B buffer buf ^ 1 was last read by the MMAs of term - 1 (done); MF buffer
-      // buf ^ 1 by the M step of term - 1 (every producer is past it)
-      kbt_stage_pre<KP>(nxt, pre, NP, nr, reinterpret_cast<float*>(Bs + (buf ^ 1) * L::BBUF),
-                        MFs0 + (buf ^ 1) * 8 * KB_WMAX, Cs0 + (buf ^ 1) * 8 * KB_WMAX, tid, L::BPART);
-      kbt_producer_sync();
-      if (!kbt_zstep_ring<KP>(z, nxt, nb, nr, b0, vloc, lane, MFs0 + (buf ^ 1) * 8 * KB_WMAX,
-                              Cs0 + (buf ^ 1) * 8 * KB_WMAX, ring, rfull, rempty, g))
-        ok = false;
-      cur = nxt;
-    }
-  }
-  if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
-  tc_fence_after();
-  // epilogue: rows r = w / 4, w / 4 + 2, ... of this warp's lane quarter
-  for (int r = wid >> 2; r < nr; r += 2) {
-    for (int c0 = 0; c0 < NP; c0 += 16) {
-      float re[16], im[16];
-      const uint32_t lanebase = (uint32_t)(vq * 32) << 16;
-      tc_ld16(tmem + lanebase + (uint32_t)(2 * r * NP + c0), re);
-      tc_ld16(tmem + lanebase + (uint32_t)((2 * r + 1) * NP + c0), im);
-      const bool any = ncommit > 0;
-#pragma unroll
-      for (int q = 0; q < 16; ++q)
-        if (c0 + q < nk1)
-          Y[((long long)r * nk1 + c0 + q) * nb] = any ? make_float2(re[q], im[q]) : make_float2(0.f, 0.f);
-    }
-  }
-  if (!ok && lane == 0) atomicExch(p.err, KR_ERR_TIMEOUT);
-  tc_fence_before();
-  __syncthreads();
-}
-
-__global__ void __launch_bounds__(320, 1) kb_matvec_tc(BatchTC p, const __grid_constant__ CUtensorMap xmap) {
-  extern __shared__ __align__(1024) char kbt_smem[];
-  if (p.grp_active) {
-    const int* g = p.grp_active + 4 * blockIdx.y;
-    if (!(g[0] | g[1] | g[2] | g[3])) return;
-  }
-  const int task = blockIdx.x;
-  const int s1 = __ldg(p.task + task);
-  const int i0 = __ldg(p.task + p.ntask + task);
-  const int nr = __ldg(p.task + 2 * p.ntask + task);
-  const int kp = __ldg(p.task + 3 * p.ntask + task);
-  if (kp == 8) kbt_tile_ring<8>(p, &xmap, s1, i0, nr, kbt_smem);
-  else if (kp == 16) kbt_tile_ring<16>(p, &xmap, s1, i0, nr, kbt_smem);
-  else kbt_tile<32>(p, s1, i0, nr, kbt_smem);
-}
 
 // any active vector per 32-vector group
 __global__ void kb_group_active(const int* active, int* grp, int ngrp) {
@@ -1550,33 +497,6 @@ int mv_groups(const kr_batch* b) { return b->nb / 32; }
 const char* const mv_error_text =
     "batched mat-vec: an MMA completion wait gave up or a term exceeded the tile shape";
 
-// TMA descriptor of an X buffer [dim][nb] (complex64 as 8-byte elements):
-// boxes of 128 vectors x 8 rows, zero fill outside the array
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-int encode_xmap(kr_ctx* ctx, const float2* X, long long dim, int nb, CUtensorMap* m) {
-  static EncodeTiledFn fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* f = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(f);
-  });
-  if (!fn) return set_err(ctx, KR_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-  const cuuint64_t gdim[2] = {(cuuint64_t)nb, (cuuint64_t)dim};
-  const cuuint64_t gstride[1] = {(cuuint64_t)nb * sizeof(float2)};
-  const cuuint32_t box[2] = {128, 8};
-  const cuuint32_t estride[2] = {1, 1};
-  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<float2*>(X), gdim, gstride, box, estride,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return set_err(ctx, KR_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
-  return KR_OK;
-}
-
 int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool masked, cudaStream_t st) {
   if (b->mv_kind == KR_MATVEC_TENSOR && op->tc_ntask > 0) {
     BatchTC q;
@@ -1588,16 +508,9 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
     q.ntask = op->tc_ntask;
     q.grp_active = masked ? b->grp_active : nullptr;
     q.err = b->counts + 2;
-    CUtensorMap xmap;
-    const int rc = encode_xmap(op->ctx, X, b->dim, b->nb, &xmap);
-    if (rc != KR_OK) return rc;
-    const int smem = std::max(TC_SMEM, TC_SMEM_RING);
-    // per device (the attribute belongs to the current device's context)
-    KR_CUDA(op->ctx, cudaFuncSetAttribute(kb_matvec_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    kb_matvec_tc<<<dim3(op->tc_ntask, b->nb / 128), 320, smem, st>>>(q, xmap);
-    b->launches++;
-    KR_CUDA(op->ctx, cudaGetLastError());
-    return KR_OK;
+    const int rc = kb_launch_tc(op->ctx, q, b->dim, st);
+    if (rc == KR_OK) b->launches++;
+    return rc;
   }
   BatchMV p;
   p.op = op->dev;
@@ -1608,13 +521,9 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
   p.task_i0 = b->task_i0;
   p.task_nr = b->task_nr;
   p.grp_active = masked ? b->grp_active : nullptr;
-  const size_t smem = kb_matvec_smem();
-  KR_CUDA(op->ctx, cudaFuncSetAttribute(kb_matvec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid(b->ntask, mv_groups(b));
-  kb_matvec<<<grid, 256, smem, st>>>(p);
-  b->launches++;
-  KR_CUDA(op->ctx, cudaGetLastError());
-  return KR_OK;
+  const int rc = kb_launch_simt(op->ctx, p, b->ntask, mv_groups(b), st);
+  if (rc == KR_OK) b->launches++;
+  return rc;
 }
 }  // namespace
 
@@ -1907,67 +816,3 @@ extern "C" int kr_batch_matvec(kr_batch* b, kr_op* op, void* stream) {
 }
 
 extern "C" int64_t kr_batch_launch_count(const kr_batch* b) { return b ? b->launches : -1; }
-
-// ---------------------------------------------------------------------------
-// tensor-core probe: D (128 x 16) = A (128 x 16) B^T (B: 16 x 16), A, B, D
-// row-major FP32 (read as TF32), one CTA: the MMA building block of the
-// batched mat-vec (operand staging, descriptors, TMEM, commit, TMEM load)
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) kb_mma_probe(const float* A, const float* B, float* D, int* err) {
-  __shared__ __align__(128) float sa[128 * 16];
-  __shared__ __align__(128) float sb[16 * 16];
-  __shared__ __align__(8) uint64_t bar;
-  __shared__ uint32_t tbase;
-  const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
-  for (int e = tid; e < 128 * 16; e += 128) sa[tc_kmajor_off(e >> 4, e & 15, 16) >> 2] = A[e];
-  for (int e = tid; e < 16 * 16; e += 128) sb[tc_kmajor_off(e >> 4, e & 15, 16) >> 2] = B[e];
-  if (wid == 0) tc_alloc(&tbase, 32);
-  if (tid == 0) tc_mbar_init(&bar, 1);
-  tc_fence_proxy();
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t taddr = tbase;
-  if (tid == 0) {
-    const uint32_t idesc = tc_idesc_tf32(128, 16);
-    for (int s = 0; s < 2; ++s)  // K = 16 in two steps of 8
-      tc_mma_tf32(taddr, tc_desc(tc_smem_u32(sa) + 256u * s, 128u, 512u),
-                  tc_desc(tc_smem_u32(sb) + 256u * s, 128u, 512u), idesc, (uint32_t)s);
-    tc_commit(&bar);
-  }
-  if (!tc_mbar_wait(&bar, 0) && lane == 0) atomicExch(err, KR_ERR_TIMEOUT);
-  tc_fence_after();
-  float v[16];
-  tc_ld16(taddr + ((uint32_t)(32 * wid) << 16), v);
-#pragma unroll
-  for (int j = 0; j < 16; ++j) D[(32 * wid + lane) * 16 + j] = v[j];
-  tc_fence_before();
-  __syncthreads();
-  if (wid == 0) tc_dealloc(taddr, 32);
-}
-
-extern "C" int kr_probe_mma(kr_ctx* ctx, const float* a, const float* b, float* d) {
-  if (!ctx || !a || !b || !d) return set_err(ctx, KR_ERR_ARG, "kr_probe_mma: NULL argument");
-  KR_CUDA(ctx, cudaSetDevice(ctx->device));
-  const size_t na = 128 * 16, nbb = 16 * 16, nd = 128 * 16;
-  char* buf = nullptr;
-  KR_CUDA(ctx, cudaMalloc(&buf, sizeof(float) * (na + nbb + nd) + 16));
-  float* dA = reinterpret_cast<float*>(buf);
-  float* dB = dA + na;
-  float* dD = dB + nbb;
-  int* derr = reinterpret_cast<int*>(dD + nd);
-  int herr = 0;
-  cudaError_t e = cudaMemcpy(dA, a, sizeof(float) * na, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(dB, b, sizeof(float) * nbb, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemset(derr, 0, sizeof(int));
-  if (e == cudaSuccess) {
-    kb_mma_probe<<<1, 128>>>(dA, dB, dD, derr);
-    e = cudaGetLastError();
-  }
-  if (e == cudaSuccess) e = cudaMemcpy(d, dD, sizeof(float) * nd, cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess) e = cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost);
-  cudaFree(buf);
-  if (e != cudaSuccess) return set_err(ctx, KR_ERR_CUDA, std::string("kr_probe_mma: ") + cudaGetErrorString(e));
-  if (herr) return set_err(ctx, herr, "kr_probe_mma: the MMA completion wait gave up");
-  return KR_OK;
-}

@@ -1,0 +1,55 @@
+// Batched mat-vec Y = H X over vector-minor [dim][nb] complex64 arrays: the
+// argument blocks and launchers of its two implementations, the SIMT FP32 one
+// (kr_batch_simt.cu) and the tensor-core one (kr_batch_tc.cu), used by the
+// batch driver (kr_batch.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "kr_internal.cuh"
+
+#define KB_WMAX 16   // ELL width of the M band supported by the batched mat-vec
+
+// arguments of the SIMT mat-vec kb_matvec (kr_batch_simt.cu)
+struct BatchMV {
+  DevOp op;
+  const float2* X;
+  float2* Y;
+  int nb;
+  const int* task_slab;
+  const int* task_i0;
+  const int* task_nr;
+  const int* grp_active;  // per 32-vector group: any vector active (null: all)
+};
+
+// arguments of the tensor-core mat-vec kb_matvec_tc (kr_batch_tc.cu)
+struct BatchTC {
+  DevOp op;
+  const float2* X;
+  float2* Y;
+  int nb;
+  const int* task;        // [4][ntask]: slab, first row, rows, KP
+  int ntask;
+  const int* grp_active;  // per 32-vector group: any vector active (null: all)
+  int* err;
+};
+
+// y += m * t for a real, imaginary or complex M-band value m
+template <int MT>
+__device__ __forceinline__ void macc(float2& y, float2 m, float2 t) {
+  if (MT == 1) {
+    y.x = fmaf(m.x, t.x, y.x);
+    y.y = fmaf(m.x, t.y, y.y);
+  } else if (MT == 2) {
+    y.x = fmaf(-m.y, t.y, y.x);
+    y.y = fmaf(m.y, t.x, y.y);
+  } else {
+    y.x = fmaf(m.x, t.x, fmaf(-m.y, t.y, y.x));
+    y.y = fmaf(m.x, t.y, fmaf(m.y, t.x, y.y));
+  }
+}
+
+// launch kb_matvec over the tile table (ntask tiles x ngrp 32-vector groups)
+int kb_launch_simt(kr_ctx* ctx, const BatchMV& p, int ntask, int ngrp, cudaStream_t st);
+// launch kb_matvec_tc over its tile table (p.ntask tiles x nb / 128 vector
+// blocks); encodes the TMA descriptor of p.X ([dim][nb] complex64)
+int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, cudaStream_t st);
