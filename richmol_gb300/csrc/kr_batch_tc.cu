@@ -203,12 +203,13 @@ __device__ __forceinline__ void kbt_zstep(float2 (&z)[64 / KP][KP / 2], KbtWin<K
 // producer-only barrier (warps 0-7) that leaves the MMA warp out
 __device__ __forceinline__ void kbt_producer_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
 
-// issues the MMAs of one term (one thread): D_re += Z_re K_re - Z_im K_im,
-// D_im += Z_re K_im + Z_im K_re, each product as three TF32 MMAs per K step
-// (A hi B hi, A hi B lo, A lo B hi); zero parts of K skipped
+// issues the MMAs of tile row r of one term (one thread): D_re += Z_re K_re -
+// Z_im K_im, D_im += Z_re K_im + Z_im K_re, each product as three TF32 MMAs per
+// K step (A hi B hi, A hi B lo, A lo B hi); zero parts of K skipped
 template <int KP>
-__device__ __forceinline__ void kbt_issue(uint32_t tmem, uint64_t adesc0, uint64_t bdesc, uint32_t idesc, int NP,
-                                          int nr, int ktype, int nk2, uint32_t& dinit, int bpart = TC_BPART) {
+__device__ __forceinline__ void kbt_issue_row(uint32_t tmem, uint64_t adesc0, uint64_t bdesc, uint32_t idesc,
+                                              int NP, int r, int ktype, int nk2, uint32_t& dinit,
+                                              int bpart = TC_BPART) {
   constexpr int ATILE = 128 * KP;
   int pd[4], pa[4], pb[4];
   int np = 0;
@@ -222,25 +223,98 @@ __device__ __forceinline__ void kbt_issue(uint32_t tmem, uint64_t adesc0, uint64
   }
   const int nks = (nk2 + 7) >> 3;
   // descriptor start addresses advance by (byte offset >> 4)
-  for (int r = 0; r < nr; ++r) {
-    for (int q = 0; q < np; ++q) {
-      const uint32_t dcol = tmem + (uint32_t)((2 * r + pd[q]) * NP);
-      const uint32_t dbit = 1u << (2 * r + pd[q]);
-      const uint64_t ad = adesc0 + (uint64_t)(((r * 4 + pa[q]) * ATILE * 4) >> 4);
-      const uint64_t bd = bdesc + (uint64_t)((pb[q] * bpart) >> 4);
+  for (int q = 0; q < np; ++q) {
+    const uint32_t dcol = tmem + (uint32_t)((2 * r + pd[q]) * NP);
+    const uint32_t dbit = 1u << (2 * r + pd[q]);
+    const uint64_t ad = adesc0 + (uint64_t)(((r * 4 + pa[q]) * ATILE * 4) >> 4);
+    const uint64_t bd = bdesc + (uint64_t)((pb[q] * bpart) >> 4);
 #pragma unroll
-      for (int sp = 0; sp < 3; ++sp) {
-        const uint64_t a2 = ad + (sp == 2 ? (uint64_t)((ATILE * 4) >> 4) : 0);
-        const uint64_t b2 = bd + (sp == 1 ? (uint64_t)(bpart >> 4) : 0);
+    for (int sp = 0; sp < 3; ++sp) {
+      const uint64_t a2 = ad + (sp == 2 ? (uint64_t)((ATILE * 4) >> 4) : 0);
+      const uint64_t b2 = bd + (sp == 1 ? (uint64_t)(bpart >> 4) : 0);
 #pragma unroll
-        for (int ks = 0; ks < KP / 8; ++ks) {
-          if (ks < nks) {
-            tc_mma_tf32(dcol, a2 + 16u * ks, b2 + 16u * ks, idesc, (dinit & dbit) ? 1u : 0u);
-            dinit |= dbit;
-          }
+      for (int ks = 0; ks < KP / 8; ++ks) {
+        if (ks < nks) {
+          tc_mma_tf32(dcol, a2 + 16u * ks, b2 + 16u * ks, idesc, (dinit & dbit) ? 1u : 0u);
+          dinit |= dbit;
         }
       }
     }
+  }
+}
+
+template <int KP>
+__device__ __forceinline__ void kbt_issue(uint32_t tmem, uint64_t adesc0, uint64_t bdesc, uint32_t idesc, int NP,
+                                          int nr, int ktype, int nk2, uint32_t& dinit, int bpart = TC_BPART) {
+  for (int r = 0; r < nr; ++r) kbt_issue_row<KP>(tmem, adesc0, bdesc, idesc, NP, r, ktype, nk2, dinit, bpart);
+}
+
+// MMAs of one term with K_hi and K_lo merged along N (one thread): per row r
+// and K step, Z_hi [K_hi; K_lo] (N = 2 NP) and Z_lo K_hi (N = NP) into a D
+// region of 2 NP columns whose halves the epilogue adds: D_re at column
+// 4 r NP, D_im at 4 r NP + 2 NP. KT: K real (1), imaginary (2) or complex (0).
+// B parts (bpart bytes each, NP rows): K_re hi, lo; K_im hi, lo; -K_im hi, lo.
+// acc0: 0 for the first committed term of the tile (fresh accumulators).
+template <int KP, int KT>
+__device__ __forceinline__ void kbt_issue_merged(uint32_t tmem, uint64_t adesc0, uint64_t bdesc, uint32_t id1,
+                                                 uint32_t id2, int NP, int nr, int nk2, uint32_t acc0, int bpart) {
+  constexpr uint64_t AP = (uint64_t)((128 * KP * 4) >> 4);  // descriptor step of one A part
+  const uint64_t BP = (uint64_t)(bpart >> 4);               // of one B part
+  const int nks = (nk2 + 7) >> 3;
+  for (int r = 0; r < nr; ++r) {
+    const uint32_t dre = tmem + (uint32_t)(4 * r * NP), dim = dre + (uint32_t)(2 * NP);
+    const uint64_t a = adesc0 + (uint64_t)(4 * r) * AP;
+#pragma unroll
+    for (int ks = 0; ks < KP / 8; ++ks) {
+      if (ks >= nks) break;
+      const uint32_t f = ks == 0 ? acc0 : 1u;
+      const uint64_t ak = a + 16u * ks, bk = bdesc + 16u * ks;  // 8 K columns = 256 bytes
+      if (KT != 2) {
+        tc_mma_tf32(dre, ak + 0 * AP, bk + 0 * BP, id2, f);   // Z_re_hi [K_re_hi; K_re_lo]
+        tc_mma_tf32(dre, ak + 1 * AP, bk + 0 * BP, id1, 1u);  // Z_re_lo K_re_hi
+        tc_mma_tf32(dim, ak + 2 * AP, bk + 0 * BP, id2, f);   // Z_im_hi [K_re_hi; K_re_lo]
+        tc_mma_tf32(dim, ak + 3 * AP, bk + 0 * BP, id1, 1u);  // Z_im_lo K_re_hi
+      }
+      if (KT != 1) {
+        const uint32_t g = KT == 2 ? f : 1u;
+        tc_mma_tf32(dre, ak + 2 * AP, bk + 4 * BP, id2, g);   // Z_im_hi [-K_im_hi; -K_im_lo]
+        tc_mma_tf32(dre, ak + 3 * AP, bk + 4 * BP, id1, 1u);  // Z_im_lo (-K_im_hi)
+        tc_mma_tf32(dim, ak + 0 * AP, bk + 2 * BP, id2, g);   // Z_re_hi [K_im_hi; K_im_lo]
+        tc_mma_tf32(dim, ak + 1 * AP, bk + 2 * BP, id1, 1u);  // Z_re_lo K_im_hi
+      }
+    }
+  }
+}
+
+// A tiles of tile row r: the real and imaginary parts of Z_r, each split into
+// TF32 hi (rounded to nearest, ties away, by integer arithmetic on the bit
+// pattern: finite values) and lo = value - hi, at K-major positions
+template <int KP>
+__device__ __forceinline__ void kbt_store_row(float* At, const float2 (&zr)[KP / 2], int vloc, int b0) {
+  constexpr int ATILE = 128 * KP, BH = KP / 2;
+#pragma unroll
+  for (int c4 = 0; c4 < BH; c4 += 4) {
+    float4 rh, rl, ih, il;
+    float* prh = &rh.x;
+    float* prl = &rl.x;
+    float* pih = &ih.x;
+    float* pil = &il.x;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float2 zz = zr[c4 + q];
+      const float2 hi = make_float2(__uint_as_float((__float_as_uint(zz.x) + 0x1000u) & 0xFFFFE000u),
+                                    __uint_as_float((__float_as_uint(zz.y) + 0x1000u) & 0xFFFFE000u));
+      const float2 lo = tc_fsub2(zz, hi);
+      prh[q] = hi.x;
+      prl[q] = lo.x;
+      pih[q] = hi.y;
+      pil[q] = lo.y;
+    }
+    const uint32_t o = tc_kmajor_off(vloc, b0 + c4, KP) >> 2;
+    *reinterpret_cast<float4*>(At + 0 * ATILE + o) = rh;
+    *reinterpret_cast<float4*>(At + 1 * ATILE + o) = rl;
+    *reinterpret_cast<float4*>(At + 2 * ATILE + o) = ih;
+    *reinterpret_cast<float4*>(At + 3 * ATILE + o) = il;
   }
 }
 
@@ -417,6 +491,30 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
 // ---------------------------------------------------------------------------
 constexpr int KBT_MAXT = 64;  // terms of one output slab held in the shared-memory table
 
+template <int KP>
+struct KbtRing {
+  static constexpr int NSLOT = 64 / KP;          // slots of KP rows x 128 vectors x 8 bytes
+  static constexpr int SLOT = KP * 1024;
+  static constexpr int BPART = 128 * KP;         // one B part: NP (<= 32) x KP FP32
+  static constexpr int BBUF = 6 * BPART;
+  static constexpr int OFF_B = TC_ABYTES;
+  static constexpr int OFF_RING = OFF_B + 2 * BBUF;
+  static constexpr int OFF_MF = OFF_RING + NSLOT * SLOT;
+  static constexpr int OFF_CS = OFF_MF + TC_MFBYTES;
+  // dense band of a diagonal term: [window row c][tile row r] float4
+  // (m_re, m_re, -m_im, m_im) of MF[r, c - r], zero outside the band; two buffers
+  static constexpr int R = 64 / KP;
+  static constexpr int NWIN = R + KR_DIAG_MAX - 1;  // window rows of the widest band
+  static constexpr int OFF_MFD = OFF_CS + TC_CSBYTES;
+  static constexpr int MFD = NWIN * R;             // float4 entries of one buffer
+  static constexpr int OFF_BAR = OFF_MFD + 2 * MFD * 16;
+  static constexpr int OFF_TAB = OFF_BAR + 8 * (2 + 2 * NSLOT) + 16;  // term table (KBT_MAXT entries)
+  static constexpr int TOTAL = OFF_TAB + KBT_MAXT * (int)sizeof(KbtTerm);
+};
+constexpr int TC_SMEM_RING = KbtRing<16>::TOTAL > KbtRing<8>::TOTAL ? KbtRing<16>::TOTAL : KbtRing<8>::TOTAL;
+static_assert(TC_SMEM_RING <= 232448, "ring tile exceeds the shared memory of one CTA");
+static_assert(KbtRing<8>::MFD <= 256 && KbtRing<16>::MFD <= 256, "one dense-band entry per producer thread");
+
 // the next term's B and MF values, loaded into registers before they are staged
 struct KbtPre {
   float kr[2], ki[2];
@@ -446,17 +544,22 @@ __device__ __forceinline__ void kbt_preload(const KbtTerm& t, int nk1, int NP, i
   }
   q.mf = make_float2(0.f, 0.f);
   q.col = 0;
-  if (tid < nr * t.W) {
+  if (t.dia) {  // dense band entry (c, r) = (tid / R, tid % R): MF[r, c - r]
+    constexpr int R = 64 / KP;
+    const int c = tid / R, r = tid - (tid / R) * R, w = c - r;
+    if (tid < KbtRing<KP>::MFD && r < nr && w >= 0 && w < t.W)
+      q.mf = __ldcg(t.mf + (long long)(i0 + r) * t.Wst + w);
+  } else if (tid < nr * t.W) {
     const int r = tid / t.W, w = tid - (tid / t.W) * t.W;
     const long long src = (long long)(i0 + r) * t.Wst + w;
     q.mf = __ldcg(t.mf + src);
-    if (!t.dia) q.col = __ldg(t.col + src);
+    q.col = __ldg(t.col + src);
   }
 }
 
 template <int KP>
 __device__ __forceinline__ void kbt_stage_pre(const KbtTerm& t, const KbtPre& q, int NP, int nr, float* Bt,
-                                              float2* MFs, int* Cs, int tid, int bpart) {
+                                              float2* MFs, int* Cs, float4* MFd, int tid, int bpart) {
 #pragma unroll
   for (int u = 0; u < 2; ++u) {
     const int e = tid + 256 * u;
@@ -472,40 +575,40 @@ __device__ __forceinline__ void kbt_stage_pre(const KbtTerm& t, const KbtPre& q,
     Bt[4 * (bpart / 4) + o] = -kih;
     Bt[5 * (bpart / 4) + o] = -(ki - kih);
   }
-  if (tid < nr * t.W) {
+  if (t.dia) {
+    if (tid < KbtRing<KP>::MFD) MFd[tid] = make_float4(q.mf.x, q.mf.x, -q.mf.y, q.mf.y);
+  } else if (tid < nr * t.W) {
     const int r = tid / t.W, w = tid - (tid / t.W) * t.W;
     MFs[r * KB_WMAX + w] = q.mf;
-    if (!t.dia) Cs[r * KB_WMAX + w] = q.col;
+    Cs[r * KB_WMAX + w] = q.col;
   }
 }
 
-template <int KP>
-struct KbtRing {
-  static constexpr int NSLOT = 64 / KP;          // slots of KP rows x 128 vectors x 8 bytes
-  static constexpr int SLOT = KP * 1024;
-  static constexpr int BPART = 128 * KP;         // one B part: NP (<= 32) x KP FP32
-  static constexpr int BBUF = 6 * BPART;
-  static constexpr int OFF_B = TC_ABYTES;
-  static constexpr int OFF_RING = OFF_B + 2 * BBUF;
-  static constexpr int OFF_MF = OFF_RING + NSLOT * SLOT;
-  static constexpr int OFF_CS = OFF_MF + TC_MFBYTES;
-  static constexpr int OFF_BAR = OFF_CS + TC_CSBYTES;
-  static constexpr int OFF_TAB = OFF_BAR + 8 * (2 + 2 * NSLOT) + 16;  // term table (KBT_MAXT entries)
-  static constexpr int TOTAL = OFF_TAB + KBT_MAXT * (int)sizeof(KbtTerm);
-};
-constexpr int TC_SMEM_RING = KbtRing<16>::TOTAL > KbtRing<8>::TOTAL ? KbtRing<16>::TOTAL : KbtRing<8>::TOTAL;
 
 // the ring rows of one term: count, and the first input row (diagonal terms only)
 __device__ __forceinline__ int kbt_ring_rows(const KbtTerm& t, int nr) {
   return (t.ok && !t.empty && t.dia) ? nr + t.W - 1 : 0;
 }
 
-// M step of a diagonal term from the ring; g: ring row counter (advanced)
+// z += m x for one complex x and the band value m = (m_re, m_re, -m_im, m_im)
+// of a real (MT 1), imaginary (2) or complex (0) M factor, as f32x2 FMAs
+template <int MT>
+__device__ __forceinline__ void macc2(float2& z, const float4& m, float2 x) {
+  if (MT != 2) z = tc_ffma2(make_float2(m.x, m.y), x, z);
+  if (MT != 1) z = tc_ffma2(make_float2(m.z, m.w), make_float2(x.y, x.x), z);
+}
+
+// M step of a diagonal term from the ring; g: ring row counter (advanced).
+// Window row c feeds tile rows r = c - W + 1 .. c through the dense band
+// MFd[c][r] (zero outside the band); rows go in groups of G, a group skipped
+// (warp-uniform) when the band misses it. Input columns at or beyond n_k2 hold
+// finite data of the neighbouring rows and meet zero rows of K^T in the MMA.
 template <int KP, int MT>
 __device__ __forceinline__ bool kbt_mdia_ring(float2 (&z)[64 / KP][KP / 2], const char* ring, uint64_t* rfull,
-                                              uint64_t* rempty, int& g, int nwin, int nr, int W, int nk2, int b0,
-                                              int vloc, int lane, const float2* MFs) {
+                                              uint64_t* rempty, int& g, int nwin, int nr, int W, int b0,
+                                              int vloc, int lane, const float4* MFd) {
   constexpr int R = 64 / KP, BH = KP / 2, NSLOT = KbtRing<KP>::NSLOT;
+  constexpr int G = R >= 8 ? 2 : 1;
   bool ok = true;
   for (int c = 0; c < nwin; ++c, ++g) {
     const int slot = g % NSLOT;
@@ -513,16 +616,20 @@ __device__ __forceinline__ bool kbt_mdia_ring(float2 (&z)[64 / KP][KP / 2], cons
     const float2* xs = reinterpret_cast<const float2*>(ring + (size_t)slot * KbtRing<KP>::SLOT) + vloc;
     float2 x[BH];
 #pragma unroll
-    for (int q = 0; q < BH; ++q) x[q] = (b0 + q < nk2) ? xs[(b0 + q) * 128] : make_float2(0.f, 0.f);
+    for (int q = 0; q < BH; ++q) x[q] = xs[(b0 + q) * 128];
     __syncwarp();
     if (lane == 0) tc_mbar_arrive(rempty + slot);
+    const float4* mrow = MFd + c * R;
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int w = c - r;
-      if (w >= 0 && w < W && r < nr) {
-        const float2 m = MFs[r * KB_WMAX + w];
+    for (int gr = 0; gr < R / G; ++gr) {
+      if (c >= gr * G && c < gr * G + G - 1 + W && gr * G < nr) {
 #pragma unroll
-        for (int q = 0; q < BH; ++q) macc<MT>(z[r][q], m, x[q]);
+        for (int rr = 0; rr < G; ++rr) {
+          const int r = gr * G + rr;
+          const float4 m = mrow[r];
+#pragma unroll
+          for (int q = 0; q < BH; ++q) macc2<MT>(z[r][q], m, x[q]);
+        }
       }
     }
   }
@@ -532,7 +639,8 @@ __device__ __forceinline__ bool kbt_mdia_ring(float2 (&z)[64 / KP][KP / 2], cons
 template <int KP>
 __device__ __forceinline__ bool kbt_zstep_ring(float2 (&z)[64 / KP][KP / 2], const KbtTerm& t, long long nb, int nr,
                                                int b0, int vloc, int lane, const float2* MFs, const int* Cs,
-                                               const char* ring, uint64_t* rfull, uint64_t* rempty, int& g) {
+                                               const float4* MFd, const char* ring, uint64_t* rfull,
+                                               uint64_t* rempty, int& g) {
   constexpr int R = 64 / KP, BH = KP / 2;
 #pragma unroll
   for (int r = 0; r < R; ++r)
@@ -541,9 +649,9 @@ __device__ __forceinline__ bool kbt_zstep_ring(float2 (&z)[64 / KP][KP / 2], con
   if (!t.ok || t.empty) return true;
   const int nwin = kbt_ring_rows(t, nr);
   if (t.dia) {
-    if (t.mtype == 1) return kbt_mdia_ring<KP, 1>(z, ring, rfull, rempty, g, nwin, nr, t.W, t.nk2, b0, vloc, lane, MFs);
-    if (t.mtype == 2) return kbt_mdia_ring<KP, 2>(z, ring, rfull, rempty, g, nwin, nr, t.W, t.nk2, b0, vloc, lane, MFs);
-    return kbt_mdia_ring<KP, 0>(z, ring, rfull, rempty, g, nwin, nr, t.W, t.nk2, b0, vloc, lane, MFs);
+    if (t.mtype == 1) return kbt_mdia_ring<KP, 1>(z, ring, rfull, rempty, g, nwin, nr, t.W, b0, vloc, lane, MFd);
+    if (t.mtype == 2) return kbt_mdia_ring<KP, 2>(z, ring, rfull, rempty, g, nwin, nr, t.W, b0, vloc, lane, MFd);
+    return kbt_mdia_ring<KP, 0>(z, ring, rfull, rempty, g, nwin, nr, t.W, b0, vloc, lane, MFd);
   }
   if (t.mtype == 1) kbt_mell<KP, 1>(z, t.Xs2, nb, t.nk2, nr, t.W, b0, MFs, Cs);
   else if (t.mtype == 2) kbt_mell<KP, 2>(z, t.Xs2, nb, t.nk2, nr, t.W, b0, MFs, Cs);
@@ -568,14 +676,18 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
   char* ring = smem + L::OFF_RING;
   float2* MFs0 = reinterpret_cast<float2*>(smem + L::OFF_MF);  // [2][8][KB_WMAX]
   int* Cs0 = reinterpret_cast<int*>(smem + L::OFF_CS);         // [2][8][KB_WMAX]
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);
-  uint64_t* empty = full + 1;
+  float4* MFd0 = reinterpret_cast<float4*>(smem + L::OFF_MFD);  // [2][L::MFD]
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);  // A tiles of a term stored (8 warps)
+  uint64_t* empty = full + 1;                                         // MMAs of a term done
   uint64_t* rfull = full + 2;
   uint64_t* rempty = rfull + NSLOT;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(rempty + NSLOT);
   KbtTerm* tab = reinterpret_cast<KbtTerm*>(smem + L::OFF_TAB);
   const int nk1 = __ldg(op.out_dk + s1);
   const int NP = nk1 <= 16 ? 16 : 32;
+  // K_hi and K_lo merged along N when the split D regions fit the TMEM
+  const bool merged = 4 * R * NP <= 512;
+  const int bpart = merged ? NP * KP * 4 : L::BPART;  // merged: parts adjacent along N
   float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * nk1) * nb + v;
   const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
   if (te == tb) {  // no term reaches this slab
@@ -584,10 +696,10 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
     return;
   }
   uint32_t ncols = 32;
-  while (ncols < (uint32_t)(2 * R * NP)) ncols <<= 1;
+  while (ncols < (uint32_t)((merged ? 4 : 2) * R * NP)) ncols <<= 1;
   if (wid == 8) tc_alloc(tslot, ncols);
   if (tid == 256) {
-    tc_mbar_init(full, 256);
+    tc_mbar_init(full, 8);
     tc_mbar_init(empty, 1);
     for (int i = 0; i < NSLOT; ++i) {
       tc_mbar_init(rfull + i, 1);
@@ -615,16 +727,24 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
     if (wid == 8 && lane == 0) {
       // ---- MMA issue -------------------------------------------------------
       const uint32_t idesc = tc_idesc_tf32(128, NP);
+      const uint32_t idesc2 = tc_idesc_tf32(128, 2 * NP);
       const uint64_t adesc0 = tc_desc(tc_smem_u32(As), 128u, 32u * KP);
       const uint64_t bdesc0 = tc_desc(tc_smem_u32(Bs), 128u, 32u * KP);
       uint32_t dinit = 0;
       for (int term = tb; term < te; ++term) {
         const KbtTerm tt = term_at(term - tb);
         if (!tt.ok || tt.empty) continue;  // skipped by the producers as well
+        const uint64_t bdesc = bdesc0 + (uint64_t)((((term - tb) & 1) * L::BBUF) >> 4);
         if (!tc_mbar_wait(full, (uint32_t)ncommit & 1u)) ok = false;
         tc_fence_after();
-        const uint64_t bdesc = bdesc0 + (uint64_t)((((term - tb) & 1) * L::BBUF) >> 4);
-        kbt_issue<KP>(tmem, adesc0, bdesc, idesc, NP, nr, tt.ktype, tt.nk2, dinit, L::BPART);
+        if (merged) {
+          const uint32_t acc0 = ncommit > 0 ? 1u : 0u;
+          if (tt.ktype == 1) kbt_issue_merged<KP, 1>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
+          else if (tt.ktype == 2) kbt_issue_merged<KP, 2>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
+          else kbt_issue_merged<KP, 0>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
+        } else {
+          kbt_issue<KP>(tmem, adesc0, bdesc, idesc, NP, nr, tt.ktype, tt.nk2, dinit, L::BPART);
+        }
         tc_commit(empty);
         ++ncommit;
       }
@@ -661,9 +781,9 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
   KbtTerm cur = term_at(0);
   KbtPre pre;
   kbt_preload<KP>(cur, nk1, NP, i0, nr, tid, pre);
-  kbt_stage_pre<KP>(cur, pre, NP, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, tid, L::BPART);
+  kbt_stage_pre<KP>(cur, pre, NP, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, MFd0, tid, bpart);
   kbt_producer_sync();
-  if (!kbt_zstep_ring<KP>(z, cur, nb, nr, b0, vloc, lane, MFs0, Cs0, ring, rfull, rempty, g)) ok = false;
+  if (!kbt_zstep_ring<KP>(z, cur, nb, nr, b0, vloc, lane, MFs0, Cs0, MFd0, ring, rfull, rempty, g)) ok = false;
   for (int term = tb; term < te; ++term) {
     const int buf = (term - tb) & 1;
     const bool has_next = term + 1 < te;
@@ -677,33 +797,11 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
     tc_fence_after();
     if (cur.ok && !cur.empty) {
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        if (r >= nr) continue;
-        float* At = As + r * 4 * ATILE;
-#pragma unroll
-        for (int c4 = 0; c4 < BH; c4 += 4) {
-          float4 rh, rl, ih, il;
-          float* prh = &rh.x;
-          float* prl = &rl.x;
-          float* pih = &ih.x;
-          float* pil = &il.x;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float2 zz = z[r][c4 + q];
-            prh[q] = tc_tf32(zz.x);
-            prl[q] = zz.x - prh[q];
-            pih[q] = tc_tf32(zz.y);
-            pil[q] = zz.y - pih[q];
-          }
-          const uint32_t o = tc_kmajor_off(vloc, b0 + c4, KP) >> 2;
-          *reinterpret_cast<float4*>(At + 0 * ATILE + o) = rh;
-          *reinterpret_cast<float4*>(At + 1 * ATILE + o) = rl;
-          *reinterpret_cast<float4*>(At + 2 * ATILE + o) = ih;
-          *reinterpret_cast<float4*>(At + 3 * ATILE + o) = il;
-        }
-      }
+      for (int r = 0; r < R; ++r)
+        if (r < nr) kbt_store_row<KP>(As + r * 4 * ATILE, z[r], vloc, b0);
       tc_fence_proxy();
-      tc_mbar_arrive(full);
+      __syncwarp();  // one arrival per warp, after every lane's stores and proxy fence
+      if (lane == 0) tc_mbar_arrive(full);
       ++ncommit;
     } else if (!cur.ok && tid == 0) {
       atomicExch(p.err, KR_ERR_ARG);  // outside the tile shape: skipped
@@ -712,10 +810,11 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
       // B buffer buf ^ 1 was last read by the MMAs of term - 1 (done); MF buffer
       // buf ^ 1 by the M step of term - 1 (every producer is past it)
       kbt_stage_pre<KP>(nxt, pre, NP, nr, reinterpret_cast<float*>(Bs + (buf ^ 1) * L::BBUF),
-                        MFs0 + (buf ^ 1) * 8 * KB_WMAX, Cs0 + (buf ^ 1) * 8 * KB_WMAX, tid, L::BPART);
+                        MFs0 + (buf ^ 1) * 8 * KB_WMAX, Cs0 + (buf ^ 1) * 8 * KB_WMAX, MFd0 + (buf ^ 1) * L::MFD,
+                        tid, bpart);
       kbt_producer_sync();
       if (!kbt_zstep_ring<KP>(z, nxt, nb, nr, b0, vloc, lane, MFs0 + (buf ^ 1) * 8 * KB_WMAX,
-                              Cs0 + (buf ^ 1) * 8 * KB_WMAX, ring, rfull, rempty, g))
+                              Cs0 + (buf ^ 1) * 8 * KB_WMAX, MFd0 + (buf ^ 1) * L::MFD, ring, rfull, rempty, g))
         ok = false;
       cur = nxt;
     }
@@ -727,8 +826,21 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
     for (int c0 = 0; c0 < NP; c0 += 16) {
       float re[16], im[16];
       const uint32_t lanebase = (uint32_t)(vq * 32) << 16;
-      tc_ld16(tmem + lanebase + (uint32_t)(2 * r * NP + c0), re);
-      tc_ld16(tmem + lanebase + (uint32_t)((2 * r + 1) * NP + c0), im);
+      if (merged) {  // D_re, D_im: halves hi [K_hi] + lo [K_hi] and hi [K_lo]
+        float re2[16], im2[16];
+        tc_ld16(tmem + lanebase + (uint32_t)(4 * r * NP + c0), re);
+        tc_ld16(tmem + lanebase + (uint32_t)(4 * r * NP + NP + c0), re2);
+        tc_ld16(tmem + lanebase + (uint32_t)(4 * r * NP + 2 * NP + c0), im);
+        tc_ld16(tmem + lanebase + (uint32_t)(4 * r * NP + 3 * NP + c0), im2);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          re[q] += re2[q];
+          im[q] += im2[q];
+        }
+      } else {
+        tc_ld16(tmem + lanebase + (uint32_t)(2 * r * NP + c0), re);
+        tc_ld16(tmem + lanebase + (uint32_t)((2 * r + 1) * NP + c0), im);
+      }
       const bool any = ncommit > 0;
 #pragma unroll
       for (int q = 0; q < 16; ++q)

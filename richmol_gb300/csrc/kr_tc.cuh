@@ -1,6 +1,7 @@
 // Blackwell (sm_103a) tensor-core helpers in inline PTX: shared-memory matrix
 // descriptors, TMEM allocation, tcgen05.mma issue and commit, TMEM loads and
-// bounded mbarrier waits. Used by the batched mat-vec (kr_batch.cu).
+// bounded mbarrier waits, paired FP32 FMAs. Used by the batched mat-vec
+// (kr_batch_tc.cu).
 //
 // Operand layout used throughout: no swizzle, K-major, canonical core matrices
 // of 8 rows x 16 bytes (4 TF32 values along K) stored as 128 contiguous bytes.
@@ -84,6 +85,25 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// d = a * b + c on both FP32 lanes (PTX fma.rn.f32x2, one instruction)
+__device__ __forceinline__ float2 tc_ffma2(float2 a, float2 b, float2 c) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;"
+      : "=l"(d)
+      : "l"(*reinterpret_cast<const uint64_t*>(&a)), "l"(*reinterpret_cast<const uint64_t*>(&b)),
+        "l"(*reinterpret_cast<const uint64_t*>(&c)));
+  return *reinterpret_cast<const float2*>(&d);
+}
+
+// d = a - b on both FP32 lanes (PTX sub.rn.f32x2)
+__device__ __forceinline__ float2 tc_fsub2(float2 a, float2 b) {
+  uint64_t d;
+  asm("sub.rn.f32x2 %0, %1, %2;"
+      : "=l"(d)
+      : "l"(*reinterpret_cast<const uint64_t*>(&a)), "l"(*reinterpret_cast<const uint64_t*>(&b)));
+  return *reinterpret_cast<const float2*>(&d);
 }
 
 // TF32 rounding (round to nearest, ties away) of an FP32 value, as FP32 bits
