@@ -97,6 +97,15 @@ typedef struct {
   const int32_t* t_out; const int32_t* t_in; const int32_t* t_k; const int32_t* t_mf;
 
   int32_t maxorder;           /* Lanczos basis capacity (reference: 100)    */
+
+  /* Row strides of the slabs (NULL: dim_k, the contiguous row-major slabs
+   * above). A slab with stride > dim_k is a column chunk of a wider row-major
+   * block: element (i, a) sits at off + i * stride + a. The chunks of an
+   * operator must cover each vector element exactly once. Operators with
+   * chunks are taken by the batched path only (kr_batch_*), where they carry
+   * n_k above 32 as chunks of at most 32 columns; kr_step, kr_matvec,
+   * kr_expv and kr_op_norm1 return KR_ERR_UNSUPPORTED for them. */
+  const int32_t* out_stride; const int32_t* in_stride;
 } kr_op_desc;
 
 /* x <- exp(t A) x, A = i H, for one vector (x: dim complex128 device array,

@@ -96,6 +96,7 @@ class kr_op_desc(ctypes.Structure):
         ("nmf", ctypes.c_int32), ("mf_group", P), ("mf_part", P),
         ("nterm", ctypes.c_int32), ("t_out", P), ("t_in", P), ("t_k", P), ("t_mf", P),
         ("maxorder", ctypes.c_int32),
+        ("out_stride", P), ("in_stride", P),
     ]
 
 

@@ -41,7 +41,10 @@ class Ensemble:
         self.tol = float(tol)
         self.mmax = int(mmax)
         self.template = template if template is not None else H0
-        self._plan0 = self.template._plan()
+        # n_k above 32: slabs go to the batched mat-vec as column chunks of 32
+        basis = self.template._parts[0].src.basis("1")
+        self.split = 32 if max(b[3] for b in basis) > 32 else None
+        self._plan0 = self.template._plan(split=self.split)
         self.dim = self._plan0.dim_out
         self.ctx = self._plan0.ctx
         h = ctypes.c_void_p()
@@ -84,7 +87,7 @@ class Ensemble:
         phase = None
         if self.H0 is not None:
             phase = self.tdse._h0_phase(self.H0, exp_fac, torch.device("cuda", torch.cuda.current_device()))
-        plan = H.device_operator()
+        plan = H.device_operator(split=self.split)
         kmax = ctypes.c_int32()
         rc = _native.lib().kr_batch_step(self.handle, plan.op, None if phase is None else phase.data_ptr(),
                                          float(exp_fac.real), float(exp_fac.imag), self.tol, ctypes.byref(kmax),
@@ -102,7 +105,7 @@ class Ensemble:
         tensor such as cos^2(theta); its field [0, 0, 1] is set here."""
         if not O._is_sum and O._parts[0].prods is None:
             O.field([0, 0, 1])
-        plan = O.device_operator()
+        plan = O.device_operator(split=self.split)
         out = np.zeros(2 * self.nvec, np.float64)
         _native.check(_native.lib().kr_batch_expect(self.handle, plan.op, out.ctypes.data, stream_ptr()), self.ctx)
         return out.view(np.complex128)
@@ -111,18 +114,20 @@ class Ensemble:
         """{J: (nvec,) array} J-populations of every vector (sum of |v|^2 over the
         slabs of each J), as the reference's observables (tests/test_tdse.py:63-67)."""
         basis = self.template._parts[0].src.basis("1")
-        out = np.zeros(len(basis) * self.nvec, np.float64)
+        parent = self._plan0.slab_parent  # slab (or column chunk) -> basis slab
+        out = np.zeros(len(parent) * self.nvec, np.float64)
         _native.check(_native.lib().kr_batch_populations(self.handle, out.ctypes.data, stream_ptr()), self.ctx)
-        out = out.reshape(len(basis), self.nvec)
+        out = out.reshape(len(parent), self.nvec)
         pops = {}
-        for (J, _sym, _dm, _dk), row in zip(basis, out):
+        for p, row in zip(parent, out):
+            J = basis[p][0]
             pops[J] = pops.get(J, 0.0) + row
         return pops
 
     def apply(self, H, x):
         """y = H x for (nvec, dim) complex128 CUDA tensors with the batched
         complex64 mat-vec (the single-precision CarTens.vec)."""
-        plan = H.device_operator()
+        plan = H.device_operator(split=self.split)
         x = x.contiguous()
         y = torch.empty_like(x)
         _native.check(_native.lib().kr_batch_apply(self.handle, plan.op, x.data_ptr(), y.data_ptr(), stream_ptr()),

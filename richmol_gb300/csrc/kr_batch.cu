@@ -55,10 +55,8 @@ struct kr_batch {
   int* counts = nullptr;     // [3]: active vectors, vectors that hit mmax, mat-vec error word
   // mat-vec tile table
   int ntask = 0;
-  // slab element ranges (populations)
+  // per-slab populations (slabs of the operator the batch was created with)
   int nslab = 0;
-  long long* slab_off = nullptr;
-  long long* slab_len = nullptr;
   double* pop = nullptr;     // [nslab][nb]
   int* task_slab = nullptr;
   int* task_i0 = nullptr;
@@ -455,14 +453,18 @@ __global__ void kb_expect_dots(const float4* S, const float2* Y, long long dim, 
 }
 
 // per slab (blockIdx.x) and vector: sum of |S|^2 over the slab's elements
-// (double-float accumulation, fixed order); out[slab][nb]
-__global__ void kb_slab_pop(const float4* S, const long long* slab_off, const long long* slab_len, int nb,
-                            double* out) {
+// (double-float accumulation, fixed order); out[slab][nb]. Element q of a slab
+// (row q / dk, column q % dk) sits at off + row * stride + column.
+__global__ void kb_slab_pop(const float4* S, const long long* slab_off, const int* slab_dm, const int* slab_dk,
+                            const int* slab_stride, int nb, double* out) {
   __shared__ double2 sh[8][32];
   const int v = blockIdx.y * 32 + threadIdx.x;
-  const long long e0 = slab_off[blockIdx.x], e1 = e0 + slab_len[blockIdx.x];
+  const long long off = slab_off[blockIdx.x];
+  const int dk = slab_dk[blockIdx.x], ld = slab_stride[blockIdx.x];
+  const long long n = (long long)slab_dm[blockIdx.x] * dk;
   dfl acc = {0.f, 0.f};
-  for (long long e = e0 + threadIdx.y; e < e1; e += 8) {
+  for (long long q = threadIdx.y; q < n; q += 8) {
+    const long long e = off + (q / dk) * ld + q % dk;
     const dfc s = dfc_ld(S[e * nb + v]);
     acc = df_add(acc, df_add(df_mul(s.re, s.re), df_mul(s.im, s.im)));
   }
@@ -583,25 +585,12 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
   }
   b->ntask = (int)ts.size();
   b->nslab = (int)dk.size();
-  std::vector<long long> soff(b->nslab), slen(b->nslab);
-  {
-    long long o = 0;
-    for (int s = 0; s < b->nslab; ++s) {
-      soff[s] = o;
-      slen[s] = (long long)dk[s] * dm[s];
-      o += slen[s];
-    }
-  }
-  BA(b->nslab, &b->slab_off);
-  BA(b->nslab, &b->slab_len);
   BA((size_t)b->nslab * nb, &b->pop);
   BA(ts.size(), &b->task_slab);
   BA(ti.size(), &b->task_i0);
   BA(tn.size(), &b->task_nr);
 #undef BA
   cudaError_t ce = cudaMemcpy(b->task_slab, ts.data(), sizeof(int) * ts.size(), cudaMemcpyHostToDevice);
-  if (ce == cudaSuccess) ce = cudaMemcpy(b->slab_off, soff.data(), sizeof(long long) * soff.size(), cudaMemcpyHostToDevice);
-  if (ce == cudaSuccess) ce = cudaMemcpy(b->slab_len, slen.data(), sizeof(long long) * slen.size(), cudaMemcpyHostToDevice);
   if (ce == cudaSuccess) ce = cudaMemcpy(b->task_i0, ti.data(), sizeof(int) * ti.size(), cudaMemcpyHostToDevice);
   if (ce == cudaSuccess) ce = cudaMemcpy(b->task_nr, tn.data(), sizeof(int) * tn.size(), cudaMemcpyHostToDevice);
   if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
@@ -791,7 +780,9 @@ extern "C" int kr_batch_apply(kr_batch* b, kr_op* op, const void* x, void* y, vo
 extern "C" int kr_batch_populations(kr_batch* b, double* out, void* stream) {
   if (!b || !out) return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_populations: bad argument");
   cudaStream_t st = (cudaStream_t)stream;
-  kb_slab_pop<<<dim3(b->nslab, b->nb / 32), dim3(32, 8), 0, st>>>(b->S, b->slab_off, b->slab_len, b->nb, b->pop);
+  const DevOp& o = b->op->dev;
+  kb_slab_pop<<<dim3(b->nslab, b->nb / 32), dim3(32, 8), 0, st>>>(b->S, o.out_off, o.out_dm, o.out_dk, o.out_stride,
+                                                                  b->nb, b->pop);
   b->launches++;
   KR_CUDA(b->op->ctx, cudaGetLastError());
   std::vector<double> h((size_t)b->nslab * b->nb);

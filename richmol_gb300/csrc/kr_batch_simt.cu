@@ -77,12 +77,12 @@ __device__ __forceinline__ void kb_trow(const float2* xr, long long nb, int nk2,
   }
 }
 
-// T rows jr < nrow for the input rows j0 + jr into Ts[jr]; rows outside the
-// input slab [0, dm2) are zero. (row, half-row) units go round-robin over the
-// 8 warps.
+// T rows jr < nrow for the input rows j0 + jr into Ts[jr] (rows ld2 elements
+// apart); rows outside the input slab [0, dm2) are zero. (row, half-row) units
+// go round-robin over the 8 warps.
 template <int NKP>
-__device__ __forceinline__ void kb_tstep(const float2* Xs2, long long nb, int nk2, int ktype, const float* Ks,
-                                         float2* Ts, int j0, int nrow, int dm2, int wid, int lane) {
+__device__ __forceinline__ void kb_tstep(const float2* Xs2, long long nb, int nk2, int ld2, int ktype,
+                                         const float* Ks, float2* Ts, int j0, int nrow, int dm2, int wid, int lane) {
   constexpr int NH = NKP >= 8 ? 2 : 1;
   constexpr int AB = NKP / NH;
   for (int u = wid; u < nrow * NH; u += 8) {
@@ -90,7 +90,7 @@ __device__ __forceinline__ void kb_tstep(const float2* Xs2, long long nb, int nk
     const int j = j0 + jr;
     float2 t[AB];
     if (j >= 0 && j < dm2) {
-      const float2* xr = Xs2 + (long long)j * nk2 * nb;
+      const float2* xr = Xs2 + (long long)j * ld2 * nb;
       if (ktype == 1) kb_trow<NKP, AB, 1>(xr, nb, nk2, Ks + h * AB, t);
       else if (ktype == 2) kb_trow<NKP, AB, 2>(xr, nb, nk2, Ks + h * AB, t);
       else kb_trow<NKP, AB, 0>(xr, nb, nk2, Ks + h * AB, t);
@@ -160,6 +160,7 @@ __device__ void kb_tile(const BatchMV& p, int s1, int i0, int nr, float* smem) {
   int* Cs = reinterpret_cast<int*>(MFs + R * KB_WMAX);           // [R][KB_WMAX]
   int* meta = Cs + R * KB_WMAX;                                  // ELL band window jmin, jmax
   const int nk1 = __ldg(op.out_dk + s1);
+  const int ld1 = __ldg(op.out_stride + s1);  // output row stride
   float2 y[16];
 #pragma unroll
   for (int q = 0; q < 16; ++q) y[q] = make_float2(0.f, 0.f);
@@ -169,6 +170,7 @@ __device__ void kb_tile(const BatchMV& p, int s1, int i0, int nr, float* smem) {
     const int kb = __ldg(op.t_k + term);
     const int mfi = __ldg(op.t_mf + term);
     const int nk2 = __ldg(op.in_dk + s2);
+    const int ld2 = __ldg(op.in_stride + s2);
     const int dm2 = __ldg(op.in_dm + s2);
     const int Wst = __ldg(op.mf_width + mfi);  // stored width (row stride of MF)
     const int d0s = __ldg(op.mf_diag + mfi);
@@ -222,7 +224,7 @@ __device__ void kb_tile(const BatchMV& p, int s1, int i0, int nr, float* smem) {
     const float2* Xs2 = p.X + (long long)__ldg(op.in_off + s2) * nb + v;
     if (dia) {
       // T rows of the band: input rows i0 + d0 .. i0 + d0 + nr + W - 2
-      kb_tstep<NKP>(Xs2, nb, nk2, ktype, Ks, Ts, i0 + d0, nr + W - 1, dm2, wid, lane);
+      kb_tstep<NKP>(Xs2, nb, nk2, ld2, ktype, Ks, Ts, i0 + d0, nr + W - 1, dm2, wid, lane);
       __syncthreads();
       if (mtype == 1) kb_mdia<NKP, 1>(y, Ts, MFs, W, r0, a0, nr, lane);
       else if (mtype == 2) kb_mdia<NKP, 2>(y, Ts, MFs, W, r0, a0, nr, lane);
@@ -232,7 +234,7 @@ __device__ void kb_tile(const BatchMV& p, int s1, int i0, int nr, float* smem) {
       for (int jc = jmin; jc <= jmax; jc += NJ) {
         const int nj = min(NJ, jmax - jc + 1);
         if (jc != jmin) __syncthreads();  // the previous chunk's M step is done with Ts
-        kb_tstep<NKP>(Xs2, nb, nk2, ktype, Ks, Ts, jc, nj, dm2, wid, lane);
+        kb_tstep<NKP>(Xs2, nb, nk2, ld2, ktype, Ks, Ts, jc, nj, dm2, wid, lane);
         __syncthreads();
         if (mtype == 1) kb_mell<NKP, 1>(y, Ts, MFs, Cs, W, jc, nj, r0, a0, nr, lane);
         else if (mtype == 2) kb_mell<NKP, 2>(y, Ts, MFs, Cs, W, jc, nj, r0, a0, nr, lane);
@@ -240,13 +242,13 @@ __device__ void kb_tile(const BatchMV& p, int s1, int i0, int nr, float* smem) {
       }
     }
   }
-  float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * nk1) * nb + v;
+  float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * ld1) * nb + v;
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
 #pragma unroll
     for (int aa = 0; aa < 4; ++aa) {
       const int i = r0 + r, a = a0 + aa;
-      if (i < nr && a < nk1) Y[((long long)i * nk1 + a) * nb] = y[r * 4 + aa];
+      if (i < nr && a < nk1) Y[((long long)i * ld1 + a) * nb] = y[r * 4 + aa];
     }
   }
 }

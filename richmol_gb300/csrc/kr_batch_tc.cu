@@ -45,12 +45,13 @@ template <int KP>
 struct KbtWin {
   static constexpr int BH = KP / 2, RP = 32 / KP;
   float2 x[RP][BH];
-  __device__ __forceinline__ void load(const float2* Xs2, long long nb, int nk2, int dm2, int j0, int nrow, int b0) {
+  __device__ __forceinline__ void load(const float2* Xs2, long long nb, int nk2, int ld2, int dm2, int j0, int nrow,
+                                       int b0) {
 #pragma unroll
     for (int c = 0; c < RP; ++c) {
       const int j = j0 + c;
       const bool rin = c < nrow && j >= 0 && j < dm2;
-      const float2* xr = Xs2 + (long long)j * nk2 * nb;
+      const float2* xr = Xs2 + (long long)j * ld2 * nb;
 #pragma unroll
       for (int q = 0; q < BH; ++q)
         x[c][q] = (rin && b0 + q < nk2) ? __ldg(xr + (long long)(b0 + q) * nb) : make_float2(0.f, 0.f);
@@ -81,13 +82,13 @@ __device__ __forceinline__ void kbt_mdia(float2 (&z)[64 / KP][KP / 2], const Kbt
 // M step of a term with stored columns (ELL), one input row per slot
 template <int KP, int MT>
 __device__ __forceinline__ void kbt_mell(float2 (&z)[64 / KP][KP / 2], const float2* Xs2, long long nb, int nk2,
-                                         int nr, int W, int b0, const float2* MFs, const int* Cs) {
+                                         int ld2, int nr, int W, int b0, const float2* MFs, const int* Cs) {
   constexpr int R = 64 / KP, BH = KP / 2;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     if (r >= nr) continue;
     for (int w = 0; w < W; ++w) {
-      const float2* xr = Xs2 + (long long)Cs[r * KB_WMAX + w] * nk2 * nb;
+      const float2* xr = Xs2 + (long long)Cs[r * KB_WMAX + w] * ld2 * nb;
       const float2 m = MFs[r * KB_WMAX + w];
       float2 x[BH];
 #pragma unroll
@@ -100,23 +101,23 @@ __device__ __forceinline__ void kbt_mell(float2 (&z)[64 / KP][KP / 2], const flo
 
 template <int KP, int MT>
 __device__ __forceinline__ void kbt_mstep(float2 (&z)[64 / KP][KP / 2], KbtWin<KP>& xw, bool loaded,
-                                          const float2* Xs2, long long nb, int nk2, int dm2, int i0, int nr, int d0,
-                                          int W, int b0, const float2* MFs, const int* Cs, bool dia) {
+                                          const float2* Xs2, long long nb, int nk2, int ld2, int dm2, int i0, int nr,
+                                          int d0, int W, int b0, const float2* MFs, const int* Cs, bool dia) {
   constexpr int RP = 32 / KP;
   if (dia) {
     const int nwin = nr + W - 1;
     for (int cw0 = 0; cw0 < nwin; cw0 += RP) {
-      if (cw0 > 0 || !loaded) xw.load(Xs2, nb, nk2, dm2, i0 + d0 + cw0, nwin - cw0, b0);
+      if (cw0 > 0 || !loaded) xw.load(Xs2, nb, nk2, ld2, dm2, i0 + d0 + cw0, nwin - cw0, b0);
       kbt_mdia<KP, MT>(z, xw, cw0, nr, W, MFs);
     }
   } else {
-    kbt_mell<KP, MT>(z, Xs2, nb, nk2, nr, W, b0, MFs, Cs);
+    kbt_mell<KP, MT>(z, Xs2, nb, nk2, ld2, nr, W, b0, MFs, Cs);
   }
 }
 
 // one term of a tensor-core tile: its tables and shared-memory staging
 struct KbtTerm {
-  int s2, nk2, dm2, W, Wst, d0, ktype, mtype;
+  int s2, nk2, ld2, dm2, W, Wst, d0, ktype, mtype;  // ld2: input row stride
   bool dia, ok, empty;
   const float* KT;
   const int* col;
@@ -130,6 +131,7 @@ __device__ __forceinline__ KbtTerm kbt_term(const DevOp& op, const BatchTC& p, i
   const int kb = __ldg(op.t_k + term);
   const int mfi = __ldg(op.t_mf + term);
   t.nk2 = __ldg(op.in_dk + t.s2);
+  t.ld2 = __ldg(op.in_stride + t.s2);
   t.dm2 = __ldg(op.in_dm + t.s2);
   t.Wst = __ldg(op.mf_width + mfi);
   const int d0s = __ldg(op.mf_diag + mfi);
@@ -195,9 +197,9 @@ __device__ __forceinline__ void kbt_zstep(float2 (&z)[64 / KP][KP / 2], KbtWin<K
 #pragma unroll
     for (int q = 0; q < BH; ++q) z[r][q] = make_float2(0.f, 0.f);
   if (!t.ok || t.empty) return;
-  if (t.mtype == 1) kbt_mstep<KP, 1>(z, xw, true, t.Xs2, nb, t.nk2, t.dm2, i0, nr, t.d0, t.W, b0, MFs, Cs, t.dia);
-  else if (t.mtype == 2) kbt_mstep<KP, 2>(z, xw, true, t.Xs2, nb, t.nk2, t.dm2, i0, nr, t.d0, t.W, b0, MFs, Cs, t.dia);
-  else kbt_mstep<KP, 0>(z, xw, true, t.Xs2, nb, t.nk2, t.dm2, i0, nr, t.d0, t.W, b0, MFs, Cs, t.dia);
+  if (t.mtype == 1) kbt_mstep<KP, 1>(z, xw, true, t.Xs2, nb, t.nk2, t.ld2, t.dm2, i0, nr, t.d0, t.W, b0, MFs, Cs, t.dia);
+  else if (t.mtype == 2) kbt_mstep<KP, 2>(z, xw, true, t.Xs2, nb, t.nk2, t.ld2, t.dm2, i0, nr, t.d0, t.W, b0, MFs, Cs, t.dia);
+  else kbt_mstep<KP, 0>(z, xw, true, t.Xs2, nb, t.nk2, t.ld2, t.dm2, i0, nr, t.d0, t.W, b0, MFs, Cs, t.dia);
 }
 
 // producer-only barrier (warps 0-7) that leaves the MMA warp out
@@ -344,11 +346,19 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
   uint32_t* tslot = reinterpret_cast<uint32_t*>(full + 2);
   const int nk1 = __ldg(op.out_dk + s1);
   const int NP = nk1 <= 16 ? 16 : 32;
-  float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * nk1) * nb + v;
+  // output rows ld1 elements apart; the pointer is formed where it is used
+  auto y_rows = [&](int& ld1) {
+    ld1 = __ldg(op.out_stride + s1);
+    return p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * ld1) * nb + v;
+  };
   const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
   if (te == tb) {  // no term reaches this slab
-    if (producer)
-      for (int e = wid >> 2; e < nr * nk1; e += 2) Y[(long long)e * nb] = make_float2(0.f, 0.f);
+    if (producer) {
+      int ld1;
+      float2* Y = y_rows(ld1);
+      for (int e = wid >> 2; e < nr * nk1; e += 2)
+        Y[((long long)(e / nk1) * ld1 + e % nk1) * nb] = make_float2(0.f, 0.f);
+    }
     return;
   }
   uint32_t ncols = 32;
@@ -398,7 +408,7 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
   float2 z[R][BH];
   KbtWin<KP> xw;
   KbtTerm cur = kbt_term(op, p, tb, KP, v, nb);
-  if (cur.ok && !cur.empty && cur.dia) xw.load(cur.Xs2, nb, cur.nk2, cur.dm2, i0 + cur.d0, nr + cur.W - 1, b0);
+  if (cur.ok && !cur.empty && cur.dia) xw.load(cur.Xs2, nb, cur.nk2, cur.ld2, cur.dm2, i0 + cur.d0, nr + cur.W - 1, b0);
   kbt_stage<KP>(cur, nk1, NP, i0, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, tid);
   kbt_producer_sync();
   kbt_zstep<KP>(z, xw, cur, nb, i0, nr, b0, MFs0, Cs0);
@@ -408,7 +418,7 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
     KbtTerm nxt;
     if (has_next) {
       nxt = kbt_term(op, p, term + 1, KP, v, nb);
-      if (nxt.ok && !nxt.empty && nxt.dia) xw.load(nxt.Xs2, nb, nxt.nk2, nxt.dm2, i0 + nxt.d0, nr + nxt.W - 1, b0);
+      if (nxt.ok && !nxt.empty && nxt.dia) xw.load(nxt.Xs2, nb, nxt.nk2, nxt.ld2, nxt.dm2, i0 + nxt.d0, nr + nxt.W - 1, b0);
     }
     // the MMAs of the previous committed term are done with the A tiles and its B buffer
     if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
@@ -459,6 +469,8 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
   if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
   tc_fence_after();
   // epilogue: rows r = w / 4, w / 4 + 2, ... of this warp's lane quarter
+  int ld1;
+  float2* Y = y_rows(ld1);
   for (int r = wid >> 2; r < nr; r += 2) {
     for (int c0 = 0; c0 < NP; c0 += 16) {
       float re[16], im[16];
@@ -469,7 +481,7 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
 #pragma unroll
       for (int q = 0; q < 16; ++q)
         if (c0 + q < nk1)
-          Y[((long long)r * nk1 + c0 + q) * nb] = any ? make_float2(re[q], im[q]) : make_float2(0.f, 0.f);
+          Y[((long long)r * ld1 + c0 + q) * nb] = any ? make_float2(re[q], im[q]) : make_float2(0.f, 0.f);
     }
   }
   if (!ok && lane == 0) atomicExch(p.err, KR_ERR_TIMEOUT);
@@ -653,9 +665,9 @@ __device__ __forceinline__ bool kbt_zstep_ring(float2 (&z)[64 / KP][KP / 2], con
     if (t.mtype == 2) return kbt_mdia_ring<KP, 2>(z, ring, rfull, rempty, g, nwin, nr, t.W, b0, vloc, lane, MFd);
     return kbt_mdia_ring<KP, 0>(z, ring, rfull, rempty, g, nwin, nr, t.W, b0, vloc, lane, MFd);
   }
-  if (t.mtype == 1) kbt_mell<KP, 1>(z, t.Xs2, nb, t.nk2, nr, t.W, b0, MFs, Cs);
-  else if (t.mtype == 2) kbt_mell<KP, 2>(z, t.Xs2, nb, t.nk2, nr, t.W, b0, MFs, Cs);
-  else kbt_mell<KP, 0>(z, t.Xs2, nb, t.nk2, nr, t.W, b0, MFs, Cs);
+  if (t.mtype == 1) kbt_mell<KP, 1>(z, t.Xs2, nb, t.nk2, t.ld2, nr, t.W, b0, MFs, Cs);
+  else if (t.mtype == 2) kbt_mell<KP, 2>(z, t.Xs2, nb, t.nk2, t.ld2, nr, t.W, b0, MFs, Cs);
+  else kbt_mell<KP, 0>(z, t.Xs2, nb, t.nk2, t.ld2, nr, t.W, b0, MFs, Cs);
   return true;
 }
 
@@ -688,11 +700,19 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
   // K_hi and K_lo merged along N when the split D regions fit the TMEM
   const bool merged = 4 * R * NP <= 512;
   const int bpart = merged ? NP * KP * 4 : L::BPART;  // merged: parts adjacent along N
-  float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * nk1) * nb + v;
+  // output rows ld1 elements apart; the pointer is formed where it is used
+  auto y_rows = [&](int& ld1) {
+    ld1 = __ldg(op.out_stride + s1);
+    return p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * ld1) * nb + v;
+  };
   const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
   if (te == tb) {  // no term reaches this slab
-    if (producer)
-      for (int e = wid >> 2; e < nr * nk1; e += 2) Y[(long long)e * nb] = make_float2(0.f, 0.f);
+    if (producer) {
+      int ld1;
+      float2* Y = y_rows(ld1);
+      for (int e = wid >> 2; e < nr * nk1; e += 2)
+        Y[((long long)(e / nk1) * ld1 + e % nk1) * nb] = make_float2(0.f, 0.f);
+    }
     return;
   }
   uint32_t ncols = 32;
@@ -760,7 +780,7 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
           const int slot = g % NSLOT;
           if (g >= NSLOT && !tc_mbar_wait(rempty + slot, (uint32_t)(g / NSLOT - 1) & 1u)) ok = false;
           tc_mbar_expect_tx(rfull + slot, (uint32_t)L::SLOT);
-          const long long y = row0 + (long long)(i0 + t.d0 + c) * t.nk2;  // first X row of the window row
+          const long long y = row0 + (long long)(i0 + t.d0 + c) * t.ld2;  // first X row of the window row
           char* dst = ring + (size_t)slot * L::SLOT;
 #pragma unroll
           for (int h = 0; h < KP / 8; ++h)
@@ -822,6 +842,8 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
   if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
   tc_fence_after();
   // epilogue: rows r = w / 4, w / 4 + 2, ... of this warp's lane quarter
+  int ld1;
+  float2* Y = y_rows(ld1);
   for (int r = wid >> 2; r < nr; r += 2) {
     for (int c0 = 0; c0 < NP; c0 += 16) {
       float re[16], im[16];
@@ -845,7 +867,7 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
 #pragma unroll
       for (int q = 0; q < 16; ++q)
         if (c0 + q < nk1)
-          Y[((long long)r * nk1 + c0 + q) * nb] = any ? make_float2(re[q], im[q]) : make_float2(0.f, 0.f);
+          Y[((long long)r * ld1 + c0 + q) * nb] = any ? make_float2(re[q], im[q]) : make_float2(0.f, 0.f);
     }
   }
   if (!ok && lane == 0) atomicExch(p.err, KR_ERR_TIMEOUT);

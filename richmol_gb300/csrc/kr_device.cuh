@@ -44,6 +44,7 @@ struct DevOp {
   int nslab_out, nslab_in;
   const int* out_dm; const int* out_dk; const long long* out_off;
   const int* in_dm;  const int* in_dk;  const long long* in_off;
+  const int* out_stride; const int* in_stride;  // slab row strides (= dk unless split into column chunks)
   long long dim_out, dim_in;
   // K blocks
   const long long* k_off; const int* k_rows; const int* k_cols; const int* k_type; const double* k_data;

@@ -318,6 +318,7 @@ int kx_mv(Kx& k, const double2* x, double2* y) { return kr_matvec(k.op, x, y, 1,
 extern "C" int kr_op_norm1(kr_op* op, double* norm, void* stream) {
   if (!op || !norm) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_op_norm1: bad argument");
   if (!op->square) return set_err(op->ctx, KR_ERR_ARG, "kr_op_norm1: operator is not square");
+  if (op->split) return set_err(op->ctx, KR_ERR_UNSUPPORTED, "kr_op_norm1: operator with column chunks");
   const long long n = op->dev.dim_out;
   Kx k;
   k.st = (cudaStream_t)stream;
@@ -367,6 +368,7 @@ static int kr_expv_krylov(kr_op* op, void* x, double t, int32_t m, double tol, d
 extern "C" int kr_expv(kr_op* op, void* x, const void* phase, double t, int32_t m, double tol, double anorm,
                        int32_t* stats, void* stream) {
   if (!op || !x) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_expv: bad argument");
+  if (op->split) return set_err(op->ctx, KR_ERR_UNSUPPORTED, "kr_expv: operator with column chunks");
   const long long n = op->dev.dim_out;
   const int grid = std::max(1, std::min(8 * op->ctx->nsm, (int)((n + KX_THREADS - 1) / KX_THREADS)));
   cudaStream_t st = (cudaStream_t)stream;

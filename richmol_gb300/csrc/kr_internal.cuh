@@ -57,6 +57,7 @@ struct kr_op {
   size_t smem = 0;
   int maxorder = 100;
   bool square = false;
+  bool split = false;    // slabs are column chunks (row stride > dk): batched path only
   int npart = 0;
   int nmf = 0;
   int ndiag_groups = 0;  // M groups in diagonal slot order

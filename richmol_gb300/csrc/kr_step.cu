@@ -581,13 +581,17 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   if (d->nslab_out <= 0 || d->nslab_in <= 0) return set_err(ctx, KR_ERR_ARG, "empty basis");
   if (d->npart < 0 || d->npart > KR_MAXPART) return set_err(ctx, KR_ERR_ARG, "npart out of range");
   if (d->maxorder < 2 || d->maxorder > KR_EXPM_MAX) return set_err(ctx, KR_ERR_ARG, "maxorder out of range [2, 128]");
-  {
+  bool split = false;
+  std::vector<int> out_stride(d->nslab_out), in_stride(d->nslab_in);
+  if (!d->out_stride != !d->in_stride) return set_err(ctx, KR_ERR_ARG, "slab strides given on one side only");
+  if (!d->out_stride) {
     long long off = 0;
     for (int s = 0; s < d->nslab_out; ++s) {
       if (d->out_off[s] != off || d->out_dm[s] <= 0 || d->out_dk[s] <= 0)
         return set_err(ctx, KR_ERR_ARG, "malformed output slab table");
       if (d->out_dk[s] > 32 * KR_QMAX) return set_err(ctx, KR_ERR_UNSUPPORTED, "n_k above 128 not supported");
       off += (long long)d->out_dm[s] * d->out_dk[s];
+      out_stride[s] = d->out_dk[s];
     }
     if (off != d->dim_out) return set_err(ctx, KR_ERR_ARG, "dim_out does not match the slab table");
     off = 0;
@@ -595,8 +599,35 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
       if (d->in_off[s] != off || d->in_dm[s] <= 0 || d->in_dk[s] <= 0)
         return set_err(ctx, KR_ERR_ARG, "malformed input slab table");
       off += (long long)d->in_dm[s] * d->in_dk[s];
+      in_stride[s] = d->in_dk[s];
     }
     if (off != d->dim_in) return set_err(ctx, KR_ERR_ARG, "dim_in does not match the slab table");
+  } else {
+    // column chunks: every element of the vector in exactly one chunk
+    for (int side = 0; side < 2; ++side) {
+      const int ns = side ? d->nslab_in : d->nslab_out;
+      const int32_t *dm = side ? d->in_dm : d->out_dm, *dk = side ? d->in_dk : d->out_dk;
+      const int32_t* st = side ? d->in_stride : d->out_stride;
+      const int64_t* off = side ? d->in_off : d->out_off;
+      const long long dim = side ? d->dim_in : d->dim_out;
+      std::vector<unsigned char> seen((size_t)std::max(dim, 1LL), 0);
+      for (int s = 0; s < ns; ++s) {
+        if (dm[s] <= 0 || dk[s] <= 0 || st[s] < dk[s] || off[s] < 0 ||
+            off[s] + (long long)(dm[s] - 1) * st[s] + dk[s] > dim)
+          return set_err(ctx, KR_ERR_ARG, "malformed slab chunk table");
+        if (dk[s] > 32 * KR_QMAX) return set_err(ctx, KR_ERR_UNSUPPORTED, "n_k above 128 not supported");
+        for (int i = 0; i < dm[s]; ++i)
+          for (int a = 0; a < dk[s]; ++a) {
+            unsigned char& c = seen[(size_t)(off[s] + (long long)i * st[s] + a)];
+            if (c) return set_err(ctx, KR_ERR_ARG, "slab chunks overlap");
+            c = 1;
+          }
+        (side ? in_stride : out_stride)[s] = st[s];
+        split = split || st[s] != dk[s];
+      }
+      for (long long e = 0; e < dim; ++e)
+        if (!seen[(size_t)e]) return set_err(ctx, KR_ERR_ARG, "slab chunks do not cover the vector");
+    }
   }
   for (int g = 0; g < d->nm; ++g) {
     if (d->m_rows[g] <= 0 || d->m_width[g] < 0 || d->m_ncart[g] < 1 || d->m_ncart[g] > KR_MAXCART)
@@ -638,10 +669,13 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   op->maxorder = d->maxorder;
   op->npart = d->npart;
   op->nmf = d->nmf;
+  op->split = split;
   op->square = (d->nslab_out == d->nslab_in) && (d->dim_out == d->dim_in);
   if (op->square)
     for (int s = 0; s < d->nslab_out; ++s)
-      if (d->out_dm[s] != d->in_dm[s] || d->out_dk[s] != d->in_dk[s]) op->square = false;
+      if (d->out_dm[s] != d->in_dm[s] || d->out_dk[s] != d->in_dk[s] || d->out_off[s] != d->in_off[s] ||
+          out_stride[s] != in_stride[s])
+        op->square = false;
 
   // ---- terms grouped by output slab ---------------------------------------
   std::vector<int> term_ptr(d->nslab_out + 1, 0), t_in, t_k, t_mf;
@@ -886,6 +920,8 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   UP(d->in_dm, d->nslab_in, &p_i); D.in_dm = p_i;
   UP(d->in_dk, d->nslab_in, &p_i); D.in_dk = p_i;
   UP((const long long*)d->in_off, d->nslab_in, &p_l); D.in_off = p_l;
+  UP(out_stride.data(), d->nslab_out, &p_i); D.out_stride = p_i;
+  UP(in_stride.data(), d->nslab_in, &p_i); D.in_stride = p_i;
   UP((const long long*)d->k_off, d->nk, &p_l); D.k_off = p_l;
   UP(d->k_rows, d->nk, &p_i); D.k_rows = p_i;
   UP(d->k_cols, d->nk, &p_i); D.k_cols = p_i;
@@ -996,6 +1032,7 @@ extern "C" int kr_set_field(kr_op* op, const double* coef, const double* scale, 
 
 extern "C" int kr_matvec(kr_op* op, const void* x, void* y, int64_t nvec, void* stream) {
   if (!op || !x || !y || nvec < 0) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_matvec: bad argument");
+  if (op->split) return set_err(op->ctx, KR_ERR_UNSUPPORTED, "kr_matvec: operator with column chunks (batched path only)");
   if (nvec == 0) return KR_OK;
   if (nvec > KR_MATVEC_MAXVEC) return set_err(op->ctx, KR_ERR_ARG, "kr_matvec: nvec above 65535");
   KR_CUDA(op->ctx, cudaMemsetAsync(op->mv_counters, 0, sizeof(unsigned) * nvec, (cudaStream_t)stream));
@@ -1011,6 +1048,7 @@ extern "C" int kr_step(kr_op* op, void* states, int64_t nvec, const void* phase,
                        double tol, uint32_t flags, int32_t* korder, void* stream) {
   if (!op || !states || nvec < 0) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_step: bad argument");
   if (!op->square) return set_err(op->ctx, KR_ERR_ARG, "kr_step: operator is not square (bra basis != ket basis)");
+  if (op->split) return set_err(op->ctx, KR_ERR_UNSUPPORTED, "kr_step: operator with column chunks (batched path only)");
   if (nvec == 0) return KR_OK;
   cudaStream_t st = (cudaStream_t)stream;
   const long long n = op->dev.dim_out;
@@ -1219,6 +1257,7 @@ extern "C" int kr_step_static(kr_op* op, void* states, int64_t nvec, const void*
                               double fac_im, double tol, uint32_t flags, int32_t* korder, void* stream) {
   if (!op || !states || nvec < 0) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_step_static: bad argument");
   if (!op->square) return set_err(op->ctx, KR_ERR_ARG, "kr_step_static: operator is not square");
+  if (op->split) return set_err(op->ctx, KR_ERR_UNSUPPORTED, "kr_step_static: operator with column chunks");
   if (nvec == 0) return KR_OK;
   cudaStream_t st = (cudaStream_t)stream;
   const long long n = op->dev.dim_out;

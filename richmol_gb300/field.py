@@ -271,24 +271,26 @@ class CarTens:
     # ------------------------------------------------------------------
     # GPU operator
     # ------------------------------------------------------------------
-    def _plan(self, maxorder=100):
+    def _plan(self, maxorder=100, split=None):
         from .plan import OperatorPlan
-        key = (tuple(id(p.src) for p in self._parts), int(maxorder))
+        key = (tuple(id(p.src) for p in self._parts), int(maxorder), split)
         plan = _PLANS.get(key)
         if plan is None:
             src0 = self._parts[0].src
-            plan = OperatorPlan([p.src for p in self._parts], src0.basis("1"), src0.basis("2"), maxorder=maxorder)
+            plan = OperatorPlan([p.src for p in self._parts], src0.basis("1"), src0.basis("2"), maxorder=maxorder,
+                                split=split)
             _PLANS[key] = plan
         return plan
 
     def _part_states(self):
         return [((p.prods or {}), p.kscale, p.thresh) for p in self._parts]
 
-    def device_operator(self, maxorder=100, stream=None):
-        """The OperatorPlan of this tensor with the current field applied."""
+    def device_operator(self, maxorder=100, stream=None, split=None):
+        """The OperatorPlan of this tensor with the current field applied
+        (split: column chunks of the batched path, see OperatorPlan)."""
         if not self._is_sum and self._parts[0].prods is None:
             raise AttributeError("you need to multiply tensor with field before applying it to a vector")
-        plan = self._plan(maxorder)
+        plan = self._plan(maxorder, split)
         plan.set_field(self._part_states(), stream)
         return plan
 

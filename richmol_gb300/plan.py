@@ -28,6 +28,25 @@ def _dense(m):
     return np.asarray(m.toarray() if hasattr(m, "toarray") else m, dtype=np.complex128)
 
 
+def _kdense(kt, kd, shape):
+    """The complex dense K block back from its stored kind and data."""
+    if kt == _native.KR_K_REAL:
+        return np.asarray(kd, np.float64).reshape(shape).astype(np.complex128)
+    if kt == _native.KR_K_IMAG:
+        return 1j * np.asarray(kd, np.float64).reshape(shape)
+    return np.ascontiguousarray(kd).view(np.complex128).reshape(shape)
+
+
+def _chunks(dm, dk, off, width):
+    """Column chunks of at most ``width`` of row-major (dm, dk) slabs at ``off``:
+    per chunk (parent slab, first column, columns, rows, offset, row stride)."""
+    out = []
+    for i in range(len(dm)):
+        for c0 in range(0, int(dk[i]), width):
+            out.append((i, c0, min(width, int(dk[i]) - c0), int(dm[i]), int(off[i]) + c0, int(dk[i])))
+    return out
+
+
 def _ktype(K):
     if not np.any(K.imag):
         return _native.KR_K_REAL, np.ascontiguousarray(K.real)
@@ -149,7 +168,10 @@ def compiled(src):
 class OperatorPlan:
     """One kr_op: the device tables for a tuple of factor sources."""
 
-    def __init__(self, sources, basis_out, basis_in, maxorder=100, device=None):
+    def __init__(self, sources, basis_out, basis_in, maxorder=100, device=None, split=None):
+        """split: None, or a width (32): slabs wider than it become column chunks
+        of at most that many columns with the K blocks cut to match (the batched
+        path's form for n_k above 32; the plain FP64 path refuses such operators)."""
         if len(sources) > _native.KR_MAXPART:
             raise ValueError(f"at most {_native.KR_MAXPART} operator parts are supported")
         self.ctx = context(device)
@@ -167,6 +189,19 @@ class OperatorPlan:
         in_off = np.concatenate([[0], np.cumsum(in_dm.astype(np.int64) * in_dk)[:-1]]).astype(np.int64)
         self.dim_out = int((out_dm.astype(np.int64) * out_dk).sum())
         self.dim_in = int((in_dm.astype(np.int64) * in_dk).sum())
+        self.split = int(split) if split else None
+        if self.split:
+            ch_out = _chunks(out_dm, out_dk, out_off, self.split)
+            ch_in = _chunks(in_dm, in_dk, in_off, self.split)
+            vout = [[] for _ in range(len(out_dm))]
+            vin = [[] for _ in range(len(in_dm))]
+            for v, c in enumerate(ch_out):
+                vout[c[0]].append(v)
+            for v, c in enumerate(ch_in):
+                vin[c[0]].append(v)
+            self.slab_parent = [c[0] for c in ch_out]
+        else:
+            self.slab_parent = list(range(len(out_dm)))
 
         k_off, k_rows, k_cols, k_type, k_data = [], [], [], [], []
         m_rows, m_width, m_ncart, m_col_off, m_val_off, m_col, m_val = [], [], [], [], [], [], []
@@ -176,23 +211,31 @@ class OperatorPlan:
         coff = 0
         voff = 0
         src_base = {}
+        full_k, sub_k = [], {}
+
+        def add_k(kt, kd, r, c, koff):
+            if kt == _native.KR_K_COMPLEX and koff % 2:
+                k_data.append(np.zeros(1))
+                koff += 1
+            k_off.append(koff)
+            k_rows.append(r)
+            k_cols.append(c)
+            k_type.append(kt)
+            flat = np.ascontiguousarray(kd, dtype=np.float64).reshape(-1)
+            k_data.append(flat)
+            return koff + flat.size
+
         self.part_carts = []
         for p, src in enumerate(self.sources):
             cs = compiled(src)
             self.part_carts.append(cs.carts)
             if id(src) not in src_base:
-                kb0, g0 = len(k_type), len(m_rows)
+                kb0, g0 = (len(full_k) if self.split else len(k_type)), len(m_rows)
                 for (kt, kd), (r, c) in zip(cs.kblocks, cs.kshape):
-                    if kt == _native.KR_K_COMPLEX and koff % 2:
-                        k_data.append(np.zeros(1))
-                        koff += 1
-                    k_off.append(koff)
-                    k_rows.append(r)
-                    k_cols.append(c)
-                    k_type.append(kt)
-                    flat = np.ascontiguousarray(kd, dtype=np.float64).reshape(-1)
-                    k_data.append(flat)
-                    koff += flat.size
+                    if self.split:
+                        full_k.append((kt, kd, (r, c)))
+                    else:
+                        koff = add_k(kt, kd, r, c, koff)
                 for rows, width, ncart, col, val in cs.groups:
                     m_rows.append(rows)
                     m_width.append(width)
@@ -214,13 +257,45 @@ class OperatorPlan:
                     inst[g] = len(mf_group)
                     mf_group.append(g)
                     mf_part.append(p)
-                t_out.append(sidx_out[(J1, s1)])
-                t_in.append(sidx_in[(J2, s2)])
-                t_k.append(kb0 + kidx)
-                t_mf.append(inst[g])
+                so, si = sidx_out[(J1, s1)], sidx_in[(J2, s2)]
+                if not self.split:
+                    t_out.append(so)
+                    t_in.append(si)
+                    t_k.append(kb0 + kidx)
+                    t_mf.append(inst[g])
+                    continue
+                for vo in vout[so]:
+                    for vi in vin[si]:
+                        key = (kb0 + kidx, ch_out[vo][1], ch_in[vi][1])
+                        kb = sub_k.get(key, -2)
+                        if kb == -2:
+                            kt, kd, shp = full_k[kb0 + kidx]
+                            a0, w1, b0_, w2 = ch_out[vo][1], ch_out[vo][2], ch_in[vi][1], ch_in[vi][2]
+                            sub = _kdense(kt, kd, shp)[a0:a0 + w1, b0_:b0_ + w2]
+                            kb = -1
+                            if np.any(sub):
+                                skt, skd = _ktype(np.ascontiguousarray(sub))
+                                kb = len(k_type)
+                                koff = add_k(skt, skd, w1, w2, koff)
+                            sub_k[key] = kb
+                        if kb < 0:
+                            continue  # a zero K sub-block: no term
+                        t_out.append(vo)
+                        t_in.append(vi)
+                        t_k.append(kb)
+                        t_mf.append(inst[g])
 
         A = lambda x, dt: np.ascontiguousarray(np.array(x, dtype=dt).reshape(-1))
         cat = lambda xs, dt: np.ascontiguousarray(np.concatenate(xs).astype(dt)) if xs else np.zeros(1, dt)
+        if self.split:
+            out_dm = np.array([c[3] for c in ch_out], np.int32)
+            out_dk = np.array([c[2] for c in ch_out], np.int32)
+            out_off = np.array([c[4] for c in ch_out], np.int64)
+            out_st = np.array([c[5] for c in ch_out], np.int32)
+            in_dm = np.array([c[3] for c in ch_in], np.int32)
+            in_dk = np.array([c[2] for c in ch_in], np.int32)
+            in_off = np.array([c[4] for c in ch_in], np.int64)
+            in_st = np.array([c[5] for c in ch_in], np.int32)
         keep = dict(
             out_dm=out_dm, out_dk=out_dk, out_off=out_off, in_dm=in_dm, in_dk=in_dk, in_off=in_off,
             k_off=A(k_off, np.int64), k_rows=A(k_rows, np.int32), k_cols=A(k_cols, np.int32),
@@ -232,7 +307,10 @@ class OperatorPlan:
             t_out=A(t_out, np.int32), t_in=A(t_in, np.int32), t_k=A(t_k, np.int32), t_mf=A(t_mf, np.int32),
         )
         d = _native.kr_op_desc()
-        d.nslab_out, d.nslab_in = len(slabs_out), len(slabs_in)
+        d.nslab_out, d.nslab_in = len(out_dm), len(in_dm)
+        if self.split:
+            keep["out_st"], keep["in_st"] = out_st, in_st
+            d.out_stride, d.in_stride = out_st.ctypes.data, in_st.ctypes.data
         for f in ("out_dm", "out_dk", "out_off", "in_dm", "in_dk", "in_off", "k_off", "k_rows", "k_cols",
                   "k_type", "k_data", "m_rows", "m_width", "m_ncart", "m_col_off", "m_val_off", "m_col",
                   "m_val", "mf_group", "mf_part", "t_out", "t_in", "t_k", "t_mf"):

@@ -293,3 +293,76 @@ def test_batch_populations_match_plain_fp64():
         assert np.abs(pops[J] - ref[J]).max() < 1e-6, J
     total = sum(pops.values())
     assert np.abs(total - (np.abs(vecs) ** 2).sum(axis=1)).max() < 1e-6
+
+
+def _c1_workload(jmax, seed=4):
+    """An asymmetric top without symmetry (n_k = 2J + 1, up to 2 jmax + 1),
+    random polarizability, pulse polarised off the axes."""
+    from richmol_gb300 import rot, workloads
+    rng = np.random.default_rng(seed)
+    q, r = np.linalg.qr(rng.normal(size=(3, 3)))
+    pol = (q * np.sign(np.diag(r))) @ np.diag([12.0, 40.0, 75.0]) @ (q * np.sign(np.diag(r))).T
+    mol = rot.Molecule(B=(0.9, 0.5, 0.31), sym="C1", pol=0.5 * (pol + pol.T))
+    d = np.array([0.3, -0.5, 0.81])
+    return workloads.Workload("c1_j%d" % jmax, mol, jmax, 0.0, 0.2, 0.01, None,
+                              (0.1, 0.08, 5e12, d / np.linalg.norm(d)))
+
+
+@pytest.mark.parametrize("matvec", MATVECS)
+def test_batch_wide_k_column_chunks_match_fp64(matvec):
+    """n_k up to 37 (J <= 18, C1): the batched path splits every slab wider
+    than 32 into column chunks with K sub-blocks (row stride = n_k); single
+    mat-vecs, states, <cos^2> and J-populations against the plain FP64 path,
+    which takes the slabs whole."""
+    from richmol_gb300 import TDSE
+    from richmol_gb300.batch import Ensemble
+    wl = _c1_workload(18)
+    basis = wl.h0._parts[0].src.basis("1")
+    assert max(b[3] for b in basis) == 37
+    td = TDSE(t_start=0.0, t_end=0.12, dt=0.01)
+    tc = td.time_grid()
+    nvec = 40
+    wl.h0.field([0, 0, 1])
+    order = np.argsort(wl.h0.tomat(form="full").diagonal().real, kind="stable")
+    v0 = np.zeros((nvec, wl.dim), np.complex128)
+    v0[np.arange(nvec), order[:nvec]] = 1.0
+    ens = Ensemble(td, wl.h0, nvec, tol=1e-10, matvec=matvec)
+    assert ens.split == 32 and ens._plan0.split == 32
+    ens.load(v0)
+    # one mat-vec with the pulse on: chunked complex64 against whole-slab FP64
+    H = wl.hamiltonian(0.1)
+    x = torch.randn(nvec, wl.dim, dtype=torch.complex128, device="cuda")
+    y = ens.apply(H, x)
+    y64 = torch.empty_like(x)
+    H.device_operator().matvec(x, y64)
+    assert float((y - y64).abs().max() / y64.abs().max()) < MV_RTOL[matvec]
+    # the plain FP64 path refuses the chunked operator
+    from richmol_gb300 import _native
+    with pytest.raises(_native.KrylovError) as ei:
+        H.device_operator(split=32).matvec(x, torch.empty_like(x))
+    assert ei.value.code == _native.KR_ERR_UNSUPPORTED
+    c2 = wl.cos2
+    ref = torch.from_numpy(v0).cuda()
+    for i in range(len(tc)):
+        H = wl.hamiltonian(tc[i])
+        ens.step(H)
+        ref, _ = td.update(H, H0=wl.h0, vecs=ref, inplace=True, check=False)
+    e = ens.expect(c2).real
+    plan = c2.device_operator()
+    yy = torch.empty_like(ref)
+    plan.matvec(ref, yy)
+    r = torch.sum(torch.conj(ref) * yy, dim=1).real.cpu().numpy()
+    assert np.abs(e - r).max() < OBS_ATOL
+    got = ens.store()
+    assert float((got - ref).abs().max() / ref.abs().max()) < 1e-5
+    pops = ens.populations()
+    tot = sum(pops.values())
+    assert np.allclose(tot, 1.0, atol=1e-9)
+    refn = ref.cpu().numpy()
+    off = 0
+    for J, s, dm, dk in basis:
+        blk = refn[:, off:off + dm * dk]
+        off += dm * dk
+        pops_ref = np.sum(np.abs(blk) ** 2, axis=1)
+        pops[J] = pops[J] - pops_ref
+    assert max(np.abs(p).max() for p in pops.values()) < 1e-6
