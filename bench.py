@@ -58,6 +58,9 @@ def parse(argv=None):
     p.add_argument("--serve-jmax", type=int, nargs=2, default=[10, 50], help="Jmax range of the requests")
     p.add_argument("--serve-tend", type=float, default=0.1, help="ps propagated per request (dt 10 fs)")
     p.add_argument("--serve-budget-gb", type=float, default=150.0)
+    p.add_argument("--uneven-n", type=int, default=32, help="molecules of the uneven-size batch sample")
+    p.add_argument("--uneven-jmax", type=int, nargs=2, default=[10, 50])
+    p.add_argument("--uneven-steps", type=int, default=5)
     return p.parse_args(argv)
 
 
@@ -397,6 +400,7 @@ def run_ours(args, ws, rank, local):
             del ens, ea
             torch.cuda.empty_cache()
             out["serving"] = run_serving(args)
+            out["uneven_batch"] = run_uneven(args)
 
     if rank == 0 and not args.no_cpu_baseline:
         rate, nst, tt = cpu_reference_rate(wl, args.cpu_seconds, vec=ensd.vectors(dim)[0])
@@ -454,6 +458,73 @@ def run_serving(args):
                    "latency = arrival to finished trace, incl. factor build"),
         "fp64_check": {"rid": small.rid, "jmax": small.jmax, "vectors": job.nvec,
                        "max_abs_err_cos2": worst, "bound": 1e-6},
+    }
+
+
+def run_uneven(args):
+    """The uneven-size batch: molecules drawn from the seeded distributions (C1,
+    Jmax uniform in the range, own pulse each) joined in one block-diagonal
+    operator; a time step is one field launch and one persistent FP64 step
+    launch over the ragged block table of all molecules. Timed through the
+    pulse maximum; the first three molecules are checked against their own
+    TDSE.update propagation."""
+    import torch
+    from richmol_gb300 import TDSE, workloads
+    from richmol_gb300.molecules import MoleculeSet
+    t0 = time.time()
+    wls = workloads.uneven_molecules(args.uneven_n, seed=2025, jmax_range=tuple(args.uneven_jmax), t_end=20.0)
+    build_s = time.time() - t0
+    td = TDSE(t_start=0.0, t_end=20.0, dt=0.01)
+    tc = td.time_grid()
+    ms = MoleculeSet(td, [w.h0 for w in wls], [w.Hac for w in wls])
+    v0 = [workloads.ground_state(w) for w in wls]
+    state = ms.join(v0)
+    i0 = len(tc) // 2 - 2
+    for i in range(i0, i0 + 2):  # warm-up
+        for w in wls:
+            w.hamiltonian(tc[i])
+        ms.step(state)
+    torch.cuda.synchronize()
+    ev = []
+    korders = []
+    l0 = ms.launches()
+    for i in range(i0 + 2, i0 + 2 + args.uneven_steps):
+        for w in wls:
+            w.hamiltonian(tc[i])
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        ms.step(state)
+        b.record()
+        ev.append((a, b))
+        korders.append([int(ms.last_korder.min()), int(ms.last_korder.max())])
+    torch.cuda.synchronize()
+    launches = ms.launches() - l0
+    ms_step = statistics.median(a.elapsed_time(b) for a, b in ev)
+    # the first three molecules alone, same steps from the same start
+    chk = wls[:3]
+    ms2 = MoleculeSet(td, [w.h0 for w in chk], [w.Hac for w in chk])
+    st2 = ms2.join(v0[:3])
+    alone = [torch.from_numpy(v).cuda().reshape(1, -1) for v in v0[:3]]
+    tds = [TDSE(t_start=0.0, t_end=20.0, dt=0.01) for _ in chk]
+    for t_ in tds:
+        t_.time_grid()
+    for i in range(i0, i0 + 2 + args.uneven_steps):
+        for w in chk:
+            w.hamiltonian(tc[i])
+        ms2.step(st2)
+        for m, w in enumerate(chk):
+            alone[m], _ = tds[m].update(w.hamiltonian(tc[i]), H0=w.h0, vecs=alone[m], inplace=True, check=False)
+    worst = max(float((v - alone[m].reshape(-1)).abs().max()) for m, v in enumerate(ms2.split(st2)))
+    return {
+        "value": round(len(wls) / (ms_step / 1e3), 1), "unit": "molecule-steps/s",
+        "ms_per_step": round(ms_step, 3), "molecules": len(wls), "total_dim": ms.dim,
+        "dims_min_max": [int(min(ms.dims)), int(max(ms.dims))], "krylov_order_min_max_per_step": korders,
+        "gpu_launches_per_step": launches / max(1, args.uneven_steps),
+        "dtype": "f64 (segmented step: mat-vec, per-molecule Lanczos, state)",
+        "sample": (f"{len(wls)} molecules (C1, Jmax {args.uneven_jmax[0]}-{args.uneven_jmax[1]}, seed 2025), "
+                   f"{args.uneven_steps} steps of 10 fs through the pulse maxima; factor build {build_s:.1f} s"),
+        "check_vs_alone": {"molecules": 3, "steps": 2 + args.uneven_steps, "max_abs_err_state": worst,
+                           "bound": 1e-10},
     }
 
 

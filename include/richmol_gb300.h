@@ -47,7 +47,10 @@ enum {
 enum { KR_K_COMPLEX = 0, KR_K_REAL = 1, KR_K_IMAG = 2 };
 
 #define KR_MAXCART 9   /* Cartesian components of a rank-2 tensor         */
-#define KR_MAXPART 16  /* operator parts of one sum (A + B + ...)         */
+#define KR_MAXPART 4096 /* operator parts of one sum (A + B + ...); each
+                           part has its own field (kr_set_field), so a
+                           set of molecules is one part per tensor of
+                           each molecule                                 */
 
 /* Flags of kr_step. */
 #define KR_STEP_SKIP_KRYLOV 1u /* H carries no field term (tdse.py:377): apply
@@ -123,6 +126,25 @@ int kr_expv(kr_op* op, void* x, const void* phase, double t, int32_t m, double t
  * field of the last kr_set_field: Hager-Higham power iteration (deterministic;
  * the reference uses scipy's randomised onenormest on H.tomat(), tdse.py:387). */
 int kr_op_norm1(kr_op* op, double* norm, void* stream);
+
+/* Segments of a square operator: independent problems (molecules) whose
+ * vectors lie one after the other (a block-diagonal operator, e.g. several
+ * molecules' slabs in one table). slab_seg[s] is the segment of output slab s:
+ * 0, 1, ..., nseg - 1 in slab order, every segment a non-empty slab range, no
+ * term coupling two segments. Replaces the per-molecule TDSE.update calls of
+ * the reference (tdse.py:265-414) for a set of molecules. */
+typedef struct kr_seg kr_seg;
+int kr_seg_create(kr_op* op, int32_t nseg, const int32_t* slab_seg, kr_seg** out);
+void kr_seg_destroy(kr_seg* seg);
+/* One TDSE.update of every segment's vector in one persistent launch (states:
+ * dim complex128, in place; phase: H0 half-phases or NULL): the Lanczos
+ * recurrence of kr_step per segment, with the segment's own scalars, stopping
+ * test (tol) and Krylov order (korder[nseg], host, may be NULL). The operator's
+ * kr_step scratch is used: not concurrently with kr_step on the same operator.
+ * Synchronises the stream; KR_ERR_MAXORDER if a segment reached maxorder. */
+int kr_seg_step(kr_seg* seg, void* states, const void* phase, double fac_re, double fac_im, double tol,
+                int32_t* korder, void* stream);
+int64_t kr_seg_launch_count(const kr_seg* seg);
 
 /* Context on one device. Replaces nothing in the reference (which keeps no
  * device state); created once per process and device. */

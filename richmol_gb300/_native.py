@@ -23,13 +23,14 @@ ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 KR_OK, KR_ERR_ARG, KR_ERR_CUDA, KR_ERR_MAXORDER, KR_ERR_TIMEOUT, KR_ERR_UNSUPPORTED = range(6)
 KR_K_COMPLEX, KR_K_REAL, KR_K_IMAG = 0, 1, 2
 KR_MAXCART = 9
-KR_MAXPART = 16
+KR_MAXPART = 4096
+KR_PART_INLINE = 16  # parts whose field coefficients go as kernel parameters
 KR_STEP_SKIP_KRYLOV = 1
 KR_MATVEC_TENSOR, KR_MATVEC_FP32 = 0, 1
 # bytes of per-step field input that travel host -> device (the field
 # coefficients, scales and thresholds of kr_set_field, passed as kernel
 # parameters): int npart (padded to 8) + 16 x 9 complex + 16 complex + 16 double
-FIELD_COEF_BYTES = 8 + KR_MAXPART * KR_MAXCART * 16 + KR_MAXPART * 16 + KR_MAXPART * 8
+FIELD_COEF_BYTES = 8 + KR_PART_INLINE * KR_MAXCART * 16 + KR_PART_INLINE * 16 + KR_PART_INLINE * 8
 
 EXPORTED = [
     "kr_ctx_create", "kr_ctx_destroy", "kr_last_error", "kr_op_create", "kr_op_destroy",
@@ -39,6 +40,7 @@ EXPORTED = [
     "kr_batch_korder", "kr_batch_expect", "kr_batch_launch_count", "kr_batch_matvec", "kr_batch_apply", "kr_batch_set_matvec",
     "kr_batch_populations",
     "kr_expv", "kr_op_norm1",
+    "kr_seg_create", "kr_seg_destroy", "kr_seg_step", "kr_seg_launch_count",
 ]
 
 
@@ -161,6 +163,14 @@ def lib():
         L.kr_batch_set_matvec.restype = ctypes.c_int
         L.kr_batch_apply.argtypes = [vp, vp, vp, vp, vp]
         L.kr_batch_apply.restype = ctypes.c_int
+        L.kr_seg_create.argtypes = [vp, i32, vp, ctypes.POINTER(vp)]
+        L.kr_seg_create.restype = ctypes.c_int
+        L.kr_seg_destroy.argtypes = [vp]
+        L.kr_seg_destroy.restype = None
+        L.kr_seg_step.argtypes = [vp, vp, vp, dbl, dbl, dbl, vp, vp]
+        L.kr_seg_step.restype = ctypes.c_int
+        L.kr_seg_launch_count.argtypes = [vp]
+        L.kr_seg_launch_count.restype = i64
         L.kr_batch_matvec.argtypes = [vp, vp, vp]
         L.kr_batch_matvec.restype = ctypes.c_int
         L.kr_batch_launch_count.argtypes = [vp]

@@ -175,10 +175,13 @@ static __device__ double2 grid_partials_sum2(const double2* part, int n, double2
 // outputs: the Lanczos coefficient vdot(w, V_k) of tdse.py:468 for a square
 // operator, where V_k = xscale * x.
 // ---------------------------------------------------------------------------
+// seg_done / slab_seg (optional): tasks of an output slab whose segment is
+// done are skipped (their alpha partial is zero), for the segmented step.
 template <bool ALPHA>
 __device__ void matvec_cta_tasks(const DevOp& op, const double2* __restrict__ x, double xscale,
                                  double2* __restrict__ y, unsigned* counter, double2* task_alpha,
-                                 double2* smem, double2* red) {
+                                 double2* smem, double2* red, const int* seg_done = nullptr,
+                                 const int* slab_seg = nullptr) {
   __shared__ int s_task;
   const int tid = threadIdx.x;
   double2* zb[2] = {smem, smem + op.zmax};
@@ -191,6 +194,10 @@ __device__ void matvec_cta_tasks(const DevOp& op, const double2* __restrict__ x,
     if (t >= op.ntask) break;
     const int task = __ldg(op.task_order + t);
     const int s1 = __ldg(op.task_slab + task);
+    if (seg_done && __ldcg(seg_done + __ldg(slab_seg + s1))) {  // uniform over the CTA
+      if (ALPHA && tid == 0) task_alpha[task] = make_double2(0.0, 0.0);
+      continue;
+    }
     const int i0 = __ldg(op.task_row0 + task);
     const int nr = __ldg(op.task_nrows + task);
     const int nk1 = __ldg(op.out_dk + s1);

@@ -9,11 +9,25 @@
 #include "../../include/richmol_gb300.h"
 #include "kr_device.cuh"
 
+// field coefficients of up to KR_PART_INLINE parts, passed as kernel parameters
+#define KR_PART_INLINE 16
 struct FieldCoef {
   int npart;
-  double2 coef[KR_MAXPART][KR_MAXCART];
-  double2 scale[KR_MAXPART];
-  double thresh[KR_MAXPART];
+  double2 coef[KR_PART_INLINE][KR_MAXCART];
+  double2 scale[KR_PART_INLINE];
+  double thresh[KR_PART_INLINE];
+  __device__ __forceinline__ double2 c(int p, int ci) const { return coef[p][ci]; }
+  __device__ __forceinline__ double2 s(int p) const { return scale[p]; }
+  __device__ __forceinline__ double t(int p) const { return thresh[p]; }
+};
+// the same for more parts, from device memory: [npart][KR_MAXCART], [npart], [npart]
+struct FieldCoefDev {
+  const double2* coef;
+  const double2* scale;
+  const double* thresh;
+  __device__ __forceinline__ double2 c(int p, int ci) const { return __ldg(coef + p * KR_MAXCART + ci); }
+  __device__ __forceinline__ double2 s(int p) const { return __ldg(scale + p); }
+  __device__ __forceinline__ double t(int p) const { return __ldg(thresh + p); }
 };
 
 struct DevField {
@@ -61,6 +75,11 @@ struct kr_op {
   int npart = 0;
   int nmf = 0;
   int ndiag_groups = 0;  // M groups in diagonal slot order
+  // field coefficients in device memory when npart > KR_PART_INLINE
+  double2* fc_coef = nullptr;
+  double2* fc_scale = nullptr;
+  double* fc_thresh = nullptr;
+  std::vector<double> fc_host;  // staging: coef, scale, thresh
   // tiles of the tensor-core batched mat-vec: [4][tc_ntask] = slab, first row, rows, KP
   int tc_ntask = 0;
   int* tc_task = nullptr;

@@ -43,7 +43,8 @@ __device__ __forceinline__ int cclass_mul(int a, int b) {
   return a == b ? 1 : 2;
 }
 
-__global__ void __launch_bounds__(256) kr_field_kernel(DevField f, FieldCoef c) {
+template <class Coef>
+__global__ void __launch_bounds__(256) kr_field_kernel(DevField f, Coef c) {
   // MF instance types: which components of MF = scale * sum_c coef_c M_c can be
   // non-zero; the mat-vec skips the multiplications by exact zeros
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < f.nmf; i += gridDim.x * blockDim.x) {
@@ -52,11 +53,11 @@ __global__ void __launch_bounds__(256) kr_field_kernel(DevField f, FieldCoef c) 
     const int nc = __ldg(f.m_ncart + g);
     int t = 3;
     for (int ci = 0; ci < nc; ++ci) {
-      const int ct = cclass_mul(cclass(c.coef[p][ci]), (int)f.m_ctype[g * KR_MAXCART + ci]);
+      const int ct = cclass_mul(cclass(c.c(p, ci)), (int)f.m_ctype[g * KR_MAXCART + ci]);
       if (ct == 3) continue;
       t = (t == 3) ? ct : (t == ct ? t : 0);
     }
-    t = cclass_mul(t, cclass(c.scale[p]));
+    t = cclass_mul(t, cclass(c.s(p)));
     f.mf_type[i] = (t == 3) ? 1 : t;
   }
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < f.nent;
@@ -69,10 +70,10 @@ __global__ void __launch_bounds__(256) kr_field_kernel(DevField f, FieldCoef c) 
     const double2* M = f.m_val + __ldg(f.m_val_off + g) + local;
     const int nc = __ldg(f.m_ncart + g);
     double2 v = make_double2(0.0, 0.0);
-    for (int ci = 0; ci < nc; ++ci) cfma(v, c.coef[p][ci], __ldg(M + ci * stride));
+    for (int ci = 0; ci < nc; ++ci) cfma(v, c.c(p, ci), __ldg(M + ci * stride));
     // field.py:1133-1137: elements below the threshold are dropped
-    if (c.thresh[p] > 0.0 && sqrt(cabs2(v)) < c.thresh[p]) v = make_double2(0.0, 0.0);
-    const double2 mfv = cmul(c.scale[p], v);
+    if (c.t(p) > 0.0 && sqrt(cabs2(v)) < c.t(p)) v = make_double2(0.0, 0.0);
+    const double2 mfv = cmul(c.s(p), v);
     f.mf_val[e] = mfv;
     f.mf_f32[e] = make_float2((float)mfv.x, (float)mfv.y);
     if (mfv.x != 0.0 || mfv.y != 0.0) {  // band of slots that carry a value with this field
@@ -468,6 +469,244 @@ __global__ void __launch_bounds__(KR_THREADS, 2) kr_step_kernel(StepArgs a) {
 }
 
 // ===========================================================================
+// Segmented step: independent problems (molecules) whose vectors lie one after
+// the other in one vector, under one block-diagonal operator. One persistent
+// launch runs the Lanczos recurrence of kr_step_kernel for every segment at
+// once, each with its own scalars (alpha, beta, exp(fac T) e0), its own
+// stopping test (squared distance of successive solutions, tdse.py:476) and
+// Krylov order: the mat-vec tasks of the whole ragged block table are shared,
+// the per-element work goes in chunks that lie inside one segment, and every
+// per-segment sum is taken over that segment's chunk (or task) partials in a
+// fixed order. A segment whose Krylov space closes (beta = 0) ends with the
+// exact solution of that space. Segments that have converged are skipped.
+// ===========================================================================
+struct SegArgs {
+  DevOp op;
+  double2* state;
+  const double2* phase;
+  double2* V;
+  double2* Wb[2];
+  double2* w;
+  double2* ub[2];
+  double2* task_alpha;
+  unsigned* counters;
+  unsigned* bar_count;
+  unsigned* bar_gen;
+  int* status;
+  int nseg, nchunk;
+  const int* slab_seg;       // [nslab] segment of each slab
+  const int* chunk_seg;      // [nchunk]
+  const long long* chunk_e0; // [nchunk] element range of each chunk
+  const long long* chunk_e1;
+  const int* seg_chunk_ptr;  // [nseg + 1] chunks of each segment
+  const int* seg_task_ptr;   // [nseg + 1] mat-vec tasks of each segment ...
+  const int* seg_tasks;      // ... their indices, ascending
+  double2* alpha;            // [nseg][maxorder + 1]
+  double* beta;              // [nseg][maxorder + 1]
+  double2* coef;             // [nseg][maxorder + 1] exp(fac T) e0 of the last order
+  int* done;                 // [nseg]
+  int* kout;                 // [nseg] Krylov order used
+  int* ufin;                 // [nseg] final solution: ub[ufin], or coef[0] V0 if -1
+  double* chunk_b;           // [nchunk] partial sums
+  double* chunk_c;
+  int* nactive;              // [2] segments still running, by iteration parity
+  double2 fac;
+  double tol;
+  int maxorder;
+  long long dim;
+};
+
+// sum of the doubles part[p[0] .. p[1]) by one warp in a fixed order (all lanes)
+__device__ __forceinline__ double seg_warp_sum(const double* part, int b, int e, int lane) {
+  double s = 0.0;
+  for (int i = b + lane; i < e; i += 32) s += __ldcg(part + i);
+  return warp_sum(s);
+}
+
+__global__ void __launch_bounds__(KR_THREADS, 2) kr_seg_step_kernel(SegArgs a) {
+  extern __shared__ double2 smem_dyn[];
+  __shared__ StepSmem ss;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nblk = gridDim.x;
+  const int M1 = a.maxorder + 1;
+  const long long n = a.dim;
+#define SEG_BARRIER() \
+  if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return
+
+  if (*((volatile int*)a.status) != 0) return;  // sticky error from an earlier launch
+  if (blockIdx.x == 0) {
+    for (int i = tid; i < a.maxorder + 2; i += blockDim.x) a.counters[i] = 0u;
+    if (tid < 2) a.nactive[tid] = 0;
+  }
+  for (int sg = blockIdx.x * blockDim.x + tid; sg < a.nseg; sg += nblk * blockDim.x) {
+    a.done[sg] = 0;
+    a.kout[sg] = 0;
+    a.ufin[sg] = -1;
+  }
+  double2* V0 = a.V;
+  for (int ch = blockIdx.x; ch < a.nchunk; ch += nblk)
+    for (long long e = a.chunk_e0[ch] + tid; e < a.chunk_e1[ch]; e += blockDim.x) {
+      double2 v = a.state[e];
+      if (a.phase) v = cmul(v, a.phase[e]);
+      V0[e] = v;
+    }
+  SEG_BARRIER();
+
+  // w = H V0, alpha_0 = vdot(w, V0), W0 = w - alpha_0 V0 (tdse.py:443-446)
+  matvec_cta_tasks<true>(a.op, V0, 1.0, a.w, a.counters, a.task_alpha, smem_dyn, ss.red, a.done, a.slab_seg);
+  SEG_BARRIER();
+  if (warp == 0)
+    for (int sg = blockIdx.x; sg < a.nseg; sg += nblk) {
+      double2 t = make_double2(0.0, 0.0);
+      for (int i = a.seg_task_ptr[sg] + lane; i < a.seg_task_ptr[sg + 1]; i += 32) t = cadd(t, ldcg2(a.task_alpha + a.seg_tasks[i]));
+      t = warp_sum2(t);
+      if (lane == 0) a.alpha[(long long)sg * M1] = t;
+    }
+  SEG_BARRIER();
+  for (int ch = blockIdx.x; ch < a.nchunk; ch += nblk) {
+    const int sg = a.chunk_seg[ch];
+    const double2 a0 = ldcg2(a.alpha + (long long)sg * M1);
+    double bp = 0.0;
+    for (long long e = a.chunk_e0[ch] + tid; e < a.chunk_e1[ch]; e += blockDim.x) {
+      const double2 r = csub(ldcg2(a.w + e), cmul(a0, ldcg2(V0 + e)));
+      a.Wb[0][e] = r;
+      bp += cabs2(r);
+    }
+    const double2 sb = block_sum2(make_double2(bp, 0.0), ss.red);
+    if (tid == 0) a.chunk_b[ch] = sb.x;
+  }
+  SEG_BARRIER();
+
+  int k = 1;
+  for (;;) {
+    // beta_{k-1} = ||W_{k-1}|| per segment; a closed Krylov space ends the segment
+    if (warp == 0)
+      for (int sg = blockIdx.x; sg < a.nseg; sg += nblk) {
+        if (__ldcg(a.done + sg)) continue;
+        const double b2 = seg_warp_sum(a.chunk_b, a.seg_chunk_ptr[sg], a.seg_chunk_ptr[sg + 1], lane);
+        if (lane == 0) {
+          const double b = sqrt(b2);
+          a.beta[(long long)sg * M1 + k - 1] = b;
+          if (b == 0.0) {
+            if (k == 1) {  // V0 spans the space: u = exp(fac alpha_0) V0
+              const double2 z = cmul(a.fac, ldcg2(a.alpha + (long long)sg * M1));
+              const double m = exp(z.x);
+              a.coef[(long long)sg * M1] = make_double2(m * cos(z.y), m * sin(z.y));
+              a.ufin[sg] = -1;
+            } else {
+              a.ufin[sg] = (k - 1) & 1;  // u_{k-1} is exact
+            }
+            a.kout[sg] = k;
+            a.done[sg] = 1;
+          }
+        }
+      }
+    SEG_BARRIER();
+    double2* Vk = a.V + (long long)k * n;
+    const double2* Vkm1 = a.V + (long long)(k - 1) * n;
+    const double2* Wprev = a.Wb[(k - 1) & 1];
+    for (int ch = blockIdx.x; ch < a.nchunk; ch += nblk) {
+      const int sg = a.chunk_seg[ch];
+      if (__ldcg(a.done + sg)) continue;
+      const double inv = 1.0 / __ldcg(a.beta + (long long)sg * M1 + k - 1);
+      for (long long e = a.chunk_e0[ch] + tid; e < a.chunk_e1[ch]; e += blockDim.x) Vk[e] = cscale(ldcg2(Wprev + e), inv);
+    }
+    SEG_BARRIER();
+    // w = H V_k (tdse.py:467-468)
+    matvec_cta_tasks<true>(a.op, Vk, 1.0, a.w, a.counters + k, a.task_alpha, smem_dyn, ss.red, a.done, a.slab_seg);
+    SEG_BARRIER();
+    // alpha_k and exp(fac T_{0..k}) e0 per segment (tdse.py:474)
+    if (warp == 0)
+      for (int sg = blockIdx.x; sg < a.nseg; sg += nblk) {
+        if (__ldcg(a.done + sg)) continue;
+        double2 t = make_double2(0.0, 0.0);
+        for (int i = a.seg_task_ptr[sg] + lane; i < a.seg_task_ptr[sg + 1]; i += 32)
+          t = cadd(t, ldcg2(a.task_alpha + a.seg_tasks[i]));
+        const double2 ak = warp_sum2(t);
+        for (int i = lane; i <= k; i += 32) {
+          ss.ta[i] = (i == k) ? ak : ldcg2(a.alpha + (long long)sg * M1 + i);
+          if (i < k) ss.tb[i] = __ldcg(a.beta + (long long)sg * M1 + i);
+        }
+        __syncwarp();
+        warp_expm_e0(ss.ta, ss.tb, k + 1, a.fac, ss.c, ss.term, ss.tmp);
+        __syncwarp();
+        for (int i = lane; i <= k; i += 32) a.coef[(long long)sg * M1 + i] = ss.c[i];
+        if (lane == 0) a.alpha[(long long)sg * M1 + k] = ak;
+        __syncwarp();
+      }
+    SEG_BARRIER();
+    // W_k = w - alpha_k V_k - beta_{k-1} V_{k-1} (tdse.py:469); u_k = sum_i c_i V_i,
+    // distance to u_{k-1} (tdse.py:475-476)
+    {
+      const double2* uprev = (k == 1) ? V0 : a.ub[(k - 1) & 1];
+      double2* unext = a.ub[k & 1];
+      double2* Wk = a.Wb[k & 1];
+      for (int ch = blockIdx.x; ch < a.nchunk; ch += nblk) {
+        const int sg = a.chunk_seg[ch];
+        if (__ldcg(a.done + sg)) continue;
+        __syncthreads();  // ss.c of the previous chunk is no longer read
+        for (int i = tid; i <= k; i += blockDim.x) ss.c[i] = ldcg2(a.coef + (long long)sg * M1 + i);
+        __syncthreads();
+        const double2 ak = ldcg2(a.alpha + (long long)sg * M1 + k);
+        const double bk = __ldcg(a.beta + (long long)sg * M1 + k - 1);
+        double bp = 0.0, cp = 0.0;
+        for (long long e = a.chunk_e0[ch] + tid; e < a.chunk_e1[ch]; e += blockDim.x) {
+          const double2 vk = ldcg2(Vk + e);
+          double2 r = csub(ldcg2(a.w + e), cmul(ak, vk));
+          r = csub(r, cscale(ldcg2(Vkm1 + e), bk));
+          Wk[e] = r;
+          bp += cabs2(r);
+          double2 u = make_double2(0.0, 0.0);
+          for (int i = 0; i <= k; ++i) cfma(u, ss.c[i], ldcg2(a.V + (long long)i * n + e));
+          cp += cabs2(csub(u, ldcg2(uprev + e)));
+          unext[e] = u;
+        }
+        const double2 sc = block_sum2(make_double2(bp, cp), ss.red);
+        if (tid == 0) {
+          a.chunk_b[ch] = sc.x;
+          a.chunk_c[ch] = sc.y;
+        }
+      }
+    }
+    SEG_BARRIER();
+    // stopping test per segment
+    if (warp == 0)
+      for (int sg = blockIdx.x; sg < a.nseg; sg += nblk) {
+        if (__ldcg(a.done + sg)) continue;
+        const double conv = seg_warp_sum(a.chunk_c, a.seg_chunk_ptr[sg], a.seg_chunk_ptr[sg + 1], lane);
+        if (lane == 0) {
+          if (!(conv > a.tol) || k + 1 >= a.maxorder) {
+            if (conv > a.tol) atomicCAS(a.status, 0, KR_ERR_MAXORDER);  // tdse.py:480-484
+            a.ufin[sg] = k & 1;
+            a.kout[sg] = k + 1;
+            a.done[sg] = 1;
+          } else {
+            atomicAdd(a.nactive + (k & 1), 1);
+          }
+        }
+      }
+    SEG_BARRIER();
+    const int act = __ldcg(a.nactive + (k & 1));
+    if (blockIdx.x == 0 && tid == 0) a.nactive[(k + 1) & 1] = 0;  // counted again two barriers later
+    if (act == 0) break;
+    k += 1;
+  }
+  SEG_BARRIER();
+  // state = phase * u (tdse.py:394)
+  for (int ch = blockIdx.x; ch < a.nchunk; ch += nblk) {
+    const int sg = a.chunk_seg[ch];
+    const int f = __ldcg(a.ufin + sg);
+    const double2 c0 = (f < 0) ? ldcg2(a.coef + (long long)sg * M1) : make_double2(0.0, 0.0);
+    for (long long e = a.chunk_e0[ch] + tid; e < a.chunk_e1[ch]; e += blockDim.x) {
+      double2 u = (f < 0) ? cmul(c0, ldcg2(V0 + e)) : ldcg2(a.ub[f] + e);
+      if (a.phase) u = cmul(u, a.phase[e]);
+      a.state[e] = u;
+    }
+  }
+#undef SEG_BARRIER
+}
+
+// ===========================================================================
 // host side
 // ===========================================================================
 namespace {
@@ -572,6 +811,24 @@ int pick_task_rows(int nk1, int dm1) {
 }
 
 }  // namespace
+
+// The dynamic shared memory attribute of the plain kernels is a property of
+// the kernel, not of an operator: it only ever grows (to the largest operator
+// seen), so a launch of any operator stays within it, whatever operators were
+// created since, by this thread or another.
+static std::mutex g_smem_mu;
+static size_t g_smem_max = 0;
+static cudaError_t ensure_step_smem(size_t smem) {
+  std::lock_guard<std::mutex> lk(g_smem_mu);
+  if (smem <= g_smem_max) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(kr_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(kr_matvec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(kr_seg_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) g_smem_max = smem;
+  return e;
+}
 
 extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   if (!ctx || !d || !out) return set_err(ctx, KR_ERR_ARG, "kr_op_create: NULL argument");
@@ -820,8 +1077,10 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
     kr_op_destroy(op);
     return set_err(ctx, KR_ERR_UNSUPPORTED, "Z staging buffer exceeds shared memory");
   }
-  cudaFuncSetAttribute(kr_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)op->smem);
-  cudaFuncSetAttribute(kr_matvec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)op->smem);
+  if (ensure_step_smem(op->smem) != cudaSuccess) {
+    kr_op_destroy(op);
+    return set_err(ctx, KR_ERR_CUDA, "cannot raise the dynamic shared memory of the step kernels");
+  }
   int occ = 0;
   cudaError_t ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kr_step_kernel, KR_THREADS, op->smem);
   if (ce != cudaSuccess || occ < 1) {
@@ -981,6 +1240,12 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   F.mf_type = const_cast<int*>(D.mf_type);
   signed char* p_s;
   UP(m_ctype.data(), m_ctype.size(), &p_s); F.m_ctype = p_s;
+  if (d->npart > KR_PART_INLINE) {  // one block: coef, scale, thresh (see kr_set_field)
+    UP((const double*)nullptr, (size_t)d->npart * (KR_MAXCART * 2 + 2 + 1), &p_d);
+    op->fc_coef = reinterpret_cast<double2*>(p_d);
+    op->fc_scale = op->fc_coef + (size_t)d->npart * KR_MAXCART;
+    op->fc_thresh = reinterpret_cast<double*>(op->fc_scale + d->npart);
+  }
 
   // ---- step scratch (sized once: kr_step allocates nothing) -----------------
   if (op->square) {
@@ -1009,22 +1274,38 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
 
 extern "C" int kr_set_field(kr_op* op, const double* coef, const double* scale, const double* thresh, void* stream) {
   if (!op || !coef || !scale || !thresh) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_set_field: NULL argument");
-  FieldCoef c;
-  std::memset(&c, 0, sizeof(c));
-  c.npart = op->npart;
-  for (int p = 0; p < op->npart; ++p) {
-    for (int ci = 0; ci < KR_MAXCART; ++ci)
-      c.coef[p][ci] = make_double2(coef[2 * (p * KR_MAXCART + ci)], coef[2 * (p * KR_MAXCART + ci) + 1]);
-    c.scale[p] = make_double2(scale[2 * p], scale[2 * p + 1]);
-    c.thresh[p] = thresh[p];
-  }
   if (op->field.nent == 0 && op->field.nmf == 0) return KR_OK;
-  KR_CUDA(op->ctx, cudaMemsetAsync(op->field.mf_band, 0xFF, sizeof(int) * 2 * std::max(1, op->field.nmf),
-                                   (cudaStream_t)stream));
+  cudaStream_t st = (cudaStream_t)stream;
+  KR_CUDA(op->ctx, cudaMemsetAsync(op->field.mf_band, 0xFF, sizeof(int) * 2 * std::max(1, op->field.nmf), st));
   const int threads = 256;
   const long long work = std::max<long long>(op->field.nent, op->field.nmf);
   const int blocks = (int)std::max<long long>(1, std::min<long long>((work + threads - 1) / threads, 4LL * op->ctx->nsm));
-  kr_field_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(op->field, c);
+  if (op->npart <= KR_PART_INLINE) {
+    FieldCoef c;
+    std::memset(&c, 0, sizeof(c));
+    c.npart = op->npart;
+    for (int p = 0; p < op->npart; ++p) {
+      for (int ci = 0; ci < KR_MAXCART; ++ci)
+        c.coef[p][ci] = make_double2(coef[2 * (p * KR_MAXCART + ci)], coef[2 * (p * KR_MAXCART + ci) + 1]);
+      c.scale[p] = make_double2(scale[2 * p], scale[2 * p + 1]);
+      c.thresh[p] = thresh[p];
+    }
+    kr_field_kernel<<<blocks, threads, 0, st>>>(op->field, c);
+  } else {
+    // stage coef [npart][9] complex, scale [npart] complex, thresh [npart] into
+    // one host block, then one copy to the operator's device buffers (the
+    // copy completes before the host block is written again: the staging
+    // vector is reused only after the stream has passed it)
+    const size_t nc = (size_t)op->npart * KR_MAXCART * 2, ns = (size_t)op->npart * 2, nt = op->npart;
+    KR_CUDA(op->ctx, cudaStreamSynchronize(st));
+    op->fc_host.assign(coef, coef + nc);
+    op->fc_host.insert(op->fc_host.end(), scale, scale + ns);
+    op->fc_host.insert(op->fc_host.end(), thresh, thresh + nt);
+    KR_CUDA(op->ctx, cudaMemcpyAsync(op->fc_coef, op->fc_host.data(), sizeof(double) * op->fc_host.size(),
+                                     cudaMemcpyHostToDevice, st));
+    FieldCoefDev c{op->fc_coef, op->fc_scale, op->fc_thresh};
+    kr_field_kernel<<<blocks, threads, 0, st>>>(op->field, c);
+  }
   op->launches++;
   KR_CUDA(op->ctx, cudaGetLastError());
   return KR_OK;
@@ -1037,6 +1318,7 @@ extern "C" int kr_matvec(kr_op* op, const void* x, void* y, int64_t nvec, void* 
   if (nvec > KR_MATVEC_MAXVEC) return set_err(op->ctx, KR_ERR_ARG, "kr_matvec: nvec above 65535");
   KR_CUDA(op->ctx, cudaMemsetAsync(op->mv_counters, 0, sizeof(unsigned) * nvec, (cudaStream_t)stream));
   dim3 g(op->grid, (unsigned)nvec);
+  KR_CUDA(op->ctx, ensure_step_smem(op->smem));
   kr_matvec_kernel<<<g, KR_THREADS, op->smem, (cudaStream_t)stream>>>(op->dev, (const double2*)x, (double2*)y,
                                                                       op->mv_counters);
   op->launches++;
@@ -1091,6 +1373,7 @@ extern "C" int kr_step(kr_op* op, void* states, int64_t nvec, const void* phase,
     a.state = (double2*)states + v * n;
     KR_CUDA(op->ctx, cudaMemsetAsync(op->bar, 0, sizeof(unsigned), st));  // arrival count only
     void* args[] = {&a};
+    KR_CUDA(op->ctx, ensure_step_smem(op->smem));
     KR_CUDA(op->ctx, cudaLaunchCooperativeKernel((void*)kr_step_kernel, dim3(op->grid), dim3(KR_THREADS), args,
                                                  op->smem, st));
     op->launches++;
@@ -1337,6 +1620,7 @@ extern "C" int kr_step_static(kr_op* op, void* states, int64_t nvec, const void*
     a.state = (double2*)states + v * n;
     KR_CUDA(op->ctx, cudaMemsetAsync(bar, 0, sizeof(unsigned), st));
     void* args[] = {&a};
+    KR_CUDA(op->ctx, ensure_step_smem(op->smem));
     KR_CUDA(op->ctx, cudaLaunchCooperativeKernel((void*)kr_step_kernel, dim3(op->grid), dim3(KR_THREADS), args,
                                                  op->smem, st));
     op->launches++;
@@ -1360,3 +1644,199 @@ extern "C" int kr_step_static(kr_op* op, void* states, int64_t nvec, const void*
   }
   return KR_OK;
 }
+
+
+// ===========================================================================
+// segmented step (C ABI)
+// ===========================================================================
+struct kr_seg {
+  kr_op* op = nullptr;
+  int nseg = 0, nchunk = 0, grid = 1;
+  std::vector<void*> allocs;
+  int *slab_seg = nullptr, *chunk_seg = nullptr, *seg_chunk_ptr = nullptr, *seg_task_ptr = nullptr,
+      *seg_tasks = nullptr;
+  long long *chunk_e0 = nullptr, *chunk_e1 = nullptr;
+  double2 *alpha = nullptr, *coef = nullptr;
+  double* beta = nullptr;
+  int *done = nullptr, *kout = nullptr, *ufin = nullptr, *nactive = nullptr;
+  double *chunk_b = nullptr, *chunk_c = nullptr;
+  long long launches = 0;
+};
+
+extern "C" void kr_seg_destroy(kr_seg* g) {
+  if (!g) return;
+  for (void* p : g->allocs) cudaFree(p);
+  delete g;
+}
+
+namespace {
+template <typename T>
+int seg_upload(kr_seg* g, const T* host, size_t count, T** dev) {
+  void* p = nullptr;
+  const size_t bytes = sizeof(T) * std::max<size_t>(count, 1);
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e == cudaSuccess) e = host ? cudaMemcpy(p, host, sizeof(T) * count, cudaMemcpyHostToDevice) : cudaMemset(p, 0, bytes);
+  if (e != cudaSuccess) {
+    if (p) cudaFree(p);
+    return set_err(g->op->ctx, KR_ERR_CUDA, std::string("kr_seg_create: ") + cudaGetErrorString(e));
+  }
+  g->allocs.push_back(p);
+  *dev = static_cast<T*>(p);
+  return KR_OK;
+}
+}  // namespace
+
+extern "C" int kr_seg_create(kr_op* op, int32_t nseg, const int32_t* slab_seg, kr_seg** out) {
+  if (!op || !slab_seg || !out || nseg <= 0) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_seg_create: bad argument");
+  *out = nullptr;
+  if (!op->square || op->split) return set_err(op->ctx, KR_ERR_ARG, "kr_seg_create: operator is not square or has column chunks");
+  KR_CUDA(op->ctx, cudaSetDevice(op->ctx->device));
+  const DevOp& D = op->dev;
+  const int ns = D.nslab_out;
+  std::vector<long long> off(ns);
+  std::vector<int> dm(ns), dk(ns), term_ptr(ns + 1), t_in(1), tslab(std::max(1, D.ntask));
+  KR_CUDA(op->ctx, cudaMemcpy(off.data(), D.out_off, sizeof(long long) * ns, cudaMemcpyDeviceToHost));
+  KR_CUDA(op->ctx, cudaMemcpy(dm.data(), D.out_dm, sizeof(int) * ns, cudaMemcpyDeviceToHost));
+  KR_CUDA(op->ctx, cudaMemcpy(dk.data(), D.out_dk, sizeof(int) * ns, cudaMemcpyDeviceToHost));
+  KR_CUDA(op->ctx, cudaMemcpy(term_ptr.data(), D.term_ptr, sizeof(int) * (ns + 1), cudaMemcpyDeviceToHost));
+  t_in.resize(std::max(1, term_ptr[ns]));
+  if (term_ptr[ns] > 0)
+    KR_CUDA(op->ctx, cudaMemcpy(t_in.data(), D.t_in, sizeof(int) * term_ptr[ns], cudaMemcpyDeviceToHost));
+  if (D.ntask > 0) KR_CUDA(op->ctx, cudaMemcpy(tslab.data(), D.task_slab, sizeof(int) * D.ntask, cudaMemcpyDeviceToHost));
+  // segments: contiguous, non-empty slab ranges in order; terms inside segments
+  std::vector<long long> seg_off(nseg + 1, -1);
+  for (int s = 0; s < ns; ++s) {
+    const int g = slab_seg[s];
+    if (g < 0 || g >= nseg || (s > 0 && g != slab_seg[s - 1] && g != slab_seg[s - 1] + 1) || (s == 0 && g != 0))
+      return set_err(op->ctx, KR_ERR_ARG, "kr_seg_create: slab segments must be 0, 1, ... in slab order");
+    if (seg_off[g] < 0) seg_off[g] = off[s];
+    for (int t = term_ptr[s]; t < term_ptr[s + 1]; ++t)
+      if (slab_seg[t_in[t]] != g) return set_err(op->ctx, KR_ERR_ARG, "kr_seg_create: a term couples two segments");
+  }
+  if (slab_seg[ns - 1] != nseg - 1) return set_err(op->ctx, KR_ERR_ARG, "kr_seg_create: a segment has no slab");
+  seg_off[nseg] = D.dim_out;
+  // chunks of at most 4096 elements inside segments; tasks grouped by segment
+  std::vector<int> chunk_seg, seg_chunk_ptr(nseg + 1, 0), seg_task_ptr(nseg + 1, 0), seg_tasks;
+  std::vector<long long> ce0, ce1;
+  for (int g = 0; g < nseg; ++g) {
+    seg_chunk_ptr[g] = (int)chunk_seg.size();
+    for (long long e = seg_off[g]; e < seg_off[g + 1]; e += 4096) {
+      chunk_seg.push_back(g);
+      ce0.push_back(e);
+      ce1.push_back(std::min(seg_off[g + 1], e + 4096));
+    }
+  }
+  seg_chunk_ptr[nseg] = (int)chunk_seg.size();
+  std::vector<std::vector<int>> by_seg(nseg);
+  for (int t = 0; t < D.ntask; ++t) by_seg[slab_seg[tslab[t]]].push_back(t);
+  for (int g = 0; g < nseg; ++g) {
+    seg_task_ptr[g] = (int)seg_tasks.size();
+    seg_tasks.insert(seg_tasks.end(), by_seg[g].begin(), by_seg[g].end());
+  }
+  seg_task_ptr[nseg] = (int)seg_tasks.size();
+
+  kr_seg* g = new kr_seg();
+  g->op = op;
+  g->nseg = nseg;
+  g->nchunk = (int)chunk_seg.size();
+  const size_t M1 = (size_t)op->maxorder + 1;
+  int rc = KR_OK;
+#define SU(host, count, dst) \
+  if ((rc = seg_upload(g, host, count, dst)) != KR_OK) { kr_seg_destroy(g); return rc; }
+  SU(slab_seg, (size_t)ns, &g->slab_seg);
+  SU(chunk_seg.data(), chunk_seg.size(), &g->chunk_seg);
+  SU(ce0.data(), ce0.size(), &g->chunk_e0);
+  SU(ce1.data(), ce1.size(), &g->chunk_e1);
+  SU(seg_chunk_ptr.data(), seg_chunk_ptr.size(), &g->seg_chunk_ptr);
+  SU(seg_task_ptr.data(), seg_task_ptr.size(), &g->seg_task_ptr);
+  SU(seg_tasks.data(), seg_tasks.size(), &g->seg_tasks);
+  SU((const double2*)nullptr, nseg * M1, &g->alpha);
+  SU((const double*)nullptr, nseg * M1, &g->beta);
+  SU((const double2*)nullptr, nseg * M1, &g->coef);
+  SU((const int*)nullptr, (size_t)nseg, &g->done);
+  SU((const int*)nullptr, (size_t)nseg, &g->kout);
+  SU((const int*)nullptr, (size_t)nseg, &g->ufin);
+  SU((const int*)nullptr, (size_t)2, &g->nactive);
+  SU((const double*)nullptr, (size_t)g->nchunk, &g->chunk_b);
+  SU((const double*)nullptr, (size_t)g->nchunk, &g->chunk_c);
+#undef SU
+  // persistent grid: every CTA resident (cooperative launch)
+  if (ensure_step_smem(op->smem) != cudaSuccess) {
+    kr_seg_destroy(g);
+    return set_err(op->ctx, KR_ERR_CUDA, "kr_seg_create: cannot raise the dynamic shared memory");
+  }
+  int occ = 0;
+  cudaError_t ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kr_seg_step_kernel, KR_THREADS, op->smem);
+  if (ce != cudaSuccess || occ < 1) {
+    kr_seg_destroy(g);
+    return set_err(op->ctx, KR_ERR_CUDA, "kr_seg_step_kernel cannot be resident");
+  }
+  g->grid = std::max(1, op->ctx->nsm * std::min(occ, 2));
+  *out = g;
+  return KR_OK;
+}
+
+extern "C" int kr_seg_step(kr_seg* g, void* states, const void* phase, double fac_re, double fac_im, double tol,
+                           int32_t* korder, void* stream) {
+  if (!g || !states) return set_err(g ? g->op->ctx : nullptr, KR_ERR_ARG, "kr_seg_step: bad argument");
+  kr_op* op = g->op;
+  cudaStream_t st = (cudaStream_t)stream;
+  SegArgs a;
+  a.op = op->dev;
+  a.state = (double2*)states;
+  a.phase = (const double2*)phase;
+  a.V = op->V;
+  a.Wb[0] = op->Wb0;
+  a.Wb[1] = op->Wb1;
+  a.w = op->w;
+  a.ub[0] = op->ub0;
+  a.ub[1] = op->ub1;
+  a.task_alpha = op->task_alpha;
+  a.counters = op->counters;
+  a.bar_count = op->bar;
+  a.bar_gen = op->bar + 1;
+  a.status = op->status;
+  a.nseg = g->nseg;
+  a.nchunk = g->nchunk;
+  a.slab_seg = g->slab_seg;
+  a.chunk_seg = g->chunk_seg;
+  a.chunk_e0 = g->chunk_e0;
+  a.chunk_e1 = g->chunk_e1;
+  a.seg_chunk_ptr = g->seg_chunk_ptr;
+  a.seg_task_ptr = g->seg_task_ptr;
+  a.seg_tasks = g->seg_tasks;
+  a.alpha = g->alpha;
+  a.beta = g->beta;
+  a.coef = g->coef;
+  a.done = g->done;
+  a.kout = g->kout;
+  a.ufin = g->ufin;
+  a.chunk_b = g->chunk_b;
+  a.chunk_c = g->chunk_c;
+  a.nactive = g->nactive;
+  a.fac = make_double2(fac_re, fac_im);
+  a.tol = tol;
+  a.maxorder = op->maxorder;
+  a.dim = op->dev.dim_out;
+  KR_CUDA(op->ctx, cudaMemsetAsync(op->bar, 0, sizeof(unsigned), st));  // arrival count only
+  KR_CUDA(op->ctx, ensure_step_smem(op->smem));
+  void* args[] = {&a};
+  KR_CUDA(op->ctx, cudaLaunchCooperativeKernel((void*)kr_seg_step_kernel, dim3(g->grid), dim3(KR_THREADS), args,
+                                               op->smem, st));
+  g->launches++;
+  int hs = 0;
+  KR_CUDA(op->ctx, cudaMemcpyAsync(&hs, op->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  if (korder) KR_CUDA(op->ctx, cudaMemcpyAsync(korder, g->kout, sizeof(int) * g->nseg, cudaMemcpyDeviceToHost, st));
+  KR_CUDA(op->ctx, cudaStreamSynchronize(st));
+  if (hs != 0) {
+    cudaMemsetAsync(op->status, 0, sizeof(int), st);
+    cudaStreamSynchronize(st);
+    if (hs == KR_ERR_MAXORDER)
+      return set_err(op->ctx, KR_ERR_MAXORDER,
+                     "Lanczos reached maximum order of '" + std::to_string(op->maxorder) + "' without convergence");
+    return set_err(op->ctx, hs, "device-side wait gave up (grid barrier timeout)");
+  }
+  return KR_OK;
+}
+
+extern "C" int64_t kr_seg_launch_count(const kr_seg* g) { return g ? g->launches : -1; }

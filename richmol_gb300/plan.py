@@ -168,17 +168,31 @@ def compiled(src):
 class OperatorPlan:
     """One kr_op: the device tables for a tuple of factor sources."""
 
-    def __init__(self, sources, basis_out, basis_in, maxorder=100, device=None, split=None):
+    def __init__(self, sources, basis_out, basis_in, maxorder=100, device=None, split=None, blocks=None,
+                 source_block=None):
         """split: None, or a width (32): slabs wider than it become column chunks
         of at most that many columns with the K blocks cut to match (the batched
-        path's form for n_k above 32; the plain FP64 path refuses such operators)."""
+        path's form for n_k above 32; the plain FP64 path refuses such operators).
+
+        blocks: a block-diagonal operator over several bases (one molecule each),
+        given as [(basis_out, basis_in), ...] in place of basis_out / basis_in;
+        source_block[p] is the block of source p. The vector is the blocks'
+        vectors one after the other, and every source is a part of its own
+        (its own field coefficients in set_field)."""
         if len(sources) > _native.KR_MAXPART:
             raise ValueError(f"at most {_native.KR_MAXPART} operator parts are supported")
         self.ctx = context(device)
         self.sources = list(sources)
         L = _native.lib()
-        slabs_out = [(J, s) for J, s, _, _ in basis_out]
-        slabs_in = [(J, s) for J, s, _, _ in basis_in]
+        if blocks is None:
+            blocks = [(basis_out, basis_in)]
+            source_block = [0] * len(self.sources)
+        assert len(source_block) == len(self.sources)
+        self.nblock = len(blocks)
+        basis_out = [b for bo, _ in blocks for b in bo]
+        basis_in = [b for _, bi in blocks for b in bi]
+        slabs_out = [(k, J, s) for k, (bo, _) in enumerate(blocks) for J, s, _, _ in bo]
+        slabs_in = [(k, J, s) for k, (_, bi) in enumerate(blocks) for J, s, _, _ in bi]
         sidx_out = {k: i for i, k in enumerate(slabs_out)}
         sidx_in = {k: i for i, k in enumerate(slabs_in)}
         out_dm = np.array([b[2] for b in basis_out], np.int32)
@@ -250,14 +264,15 @@ class OperatorPlan:
             kb0, g0 = src_base[id(src)]
             inst = {}
             for J1, s1, J2, s2, kidx, gidx in cs.terms:
-                if (J1, s1) not in sidx_out or (J2, s2) not in sidx_in:
+                blk = source_block[p]
+                if (blk, J1, s1) not in sidx_out or (blk, J2, s2) not in sidx_in:
                     continue
                 g = g0 + gidx
                 if g not in inst:
                     inst[g] = len(mf_group)
                     mf_group.append(g)
                     mf_part.append(p)
-                so, si = sidx_out[(J1, s1)], sidx_in[(J2, s2)]
+                so, si = sidx_out[(blk, J1, s1)], sidx_in[(blk, J2, s2)]
                 if not self.split:
                     t_out.append(so)
                     t_in.append(si)
@@ -330,9 +345,10 @@ class OperatorPlan:
         h = ctypes.c_void_p()
         _native.check(L.kr_op_create(self.ctx, ctypes.byref(d), ctypes.byref(h)), self.ctx)
         self.op = h
-        self._coef = np.zeros((_native.KR_MAXPART, _native.KR_MAXCART), np.complex128)
-        self._scale = np.zeros(_native.KR_MAXPART, np.complex128)
-        self._thresh = np.zeros(_native.KR_MAXPART, np.float64)
+        npart = max(1, len(self.sources))
+        self._coef = np.zeros((npart, _native.KR_MAXCART), np.complex128)
+        self._scale = np.zeros(npart, np.complex128)
+        self._thresh = np.zeros(npart, np.float64)
 
     def __del__(self):
         op = getattr(self, "op", None)

@@ -99,3 +99,27 @@ def thermal_asym_top(Jmax=30, nvec=4096, temp=5.0, dt=0.01, nsteps=3000):
     wl = asym_top(Jmax=Jmax, dt=dt, nsteps=nsteps)
     wl.name = "thermal_asym_top_D2_J%d_%dvec" % (Jmax, nvec)
     return wl, Ensemble(wl, nvec, temp)
+
+
+def uneven_molecules(n, seed=0, jmax_range=(10, 50), t_end=20.0, dt=0.01):
+    """The uneven-size batch: n asymmetric tops without symmetry (C1), each
+    drawn as a propagation request is (richmol_gb300.serve.draw_request: A >= B
+    >= C log-uniform in 0.05-5 cm^-1, Jmax uniform in ``jmax_range``, random
+    polarizability, its own pulse centred at t_end / 2), 0 - t_end ps at dt."""
+    from .serve import draw_request
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        r = draw_request(rng, i, 0.0, jmax_range=jmax_range, t_end=t_end, dt=dt)
+        mol = rot.Molecule(B=r.abc, sym="C1", pol=r.pol)
+        out.append(Workload("molecule_%d_J%d" % (i, r.jmax), mol, r.jmax, 0.0, t_end, dt, None, r.pulse))
+    return out
+
+
+def ground_state(wl):
+    """Unit vector of the lowest eigenstate of the workload's H0."""
+    wl.h0.field([0, 0, 1])
+    e = wl.h0.tomat(form="full").diagonal().real
+    v = np.zeros(wl.dim, np.complex128)
+    v[int(np.argmin(e))] = 1.0
+    return v
