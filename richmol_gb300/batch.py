@@ -20,6 +20,9 @@ from . import _native
 from .device import stream_ptr
 
 
+_KINDS = {"tensor": _native.KR_MATVEC_TENSOR, "fp32": _native.KR_MATVEC_FP32}
+
+
 class Ensemble:
     """nvec state vectors of one basis, propagated together.
 
@@ -31,7 +34,11 @@ class Ensemble:
         mmax : int                  maximum Krylov order (<= 31)
         matvec : str                "tensor" (default): K contractions on the tensor cores
                                     as split-TF32 MMAs (about 2^-21 relative per product);
-                                    "fp32": every product an FP32 FMA
+                                    "fp32": every product an FP32 FMA; "auto": at the first
+                                    step both kernels (tensor-core tiles of 64/KP rows x 128
+                                    vectors, SIMT tiles of 128/NKP rows x 32 vectors) are
+                                    timed on that step's operator and the faster one is
+                                    kept (``self.tuned``: ms per mat-vec of each)
     """
 
     def __init__(self, tdse, H0, nvec, tol=1e-8, mmax=20, template=None, matvec="tensor"):
@@ -50,11 +57,12 @@ class Ensemble:
         h = ctypes.c_void_p()
         _native.check(_native.lib().kr_batch_create(self._plan0.op, self.nvec, self.mmax, ctypes.byref(h)), self.ctx)
         self.handle = h
-        kinds = {"tensor": _native.KR_MATVEC_TENSOR, "fp32": _native.KR_MATVEC_FP32}
-        if matvec not in kinds:
-            raise ValueError(f"matvec must be one of {sorted(kinds)}")
+        if matvec not in ("tensor", "fp32", "auto"):
+            raise ValueError("matvec must be one of ['auto', 'fp32', 'tensor']")
         self.matvec = matvec
-        _native.check(_native.lib().kr_batch_set_matvec(h, kinds[matvec]), self.ctx)
+        self.tuned = None
+        _native.check(_native.lib().kr_batch_set_matvec(h, _KINDS["tensor" if matvec == "auto" else matvec]),
+                      self.ctx)
         self.phase = None
         self.last_kmax = 0
 
@@ -88,12 +96,34 @@ class Ensemble:
         if self.H0 is not None:
             phase = self.tdse._h0_phase(self.H0, exp_fac, torch.device("cuda", torch.cuda.current_device()))
         plan = H.device_operator(split=self.split)
+        if self.matvec == "auto":
+            self._tune(plan)
         kmax = ctypes.c_int32()
         rc = _native.lib().kr_batch_step(self.handle, plan.op, None if phase is None else phase.data_ptr(),
                                          float(exp_fac.real), float(exp_fac.imag), self.tol, ctypes.byref(kmax),
                                          stream_ptr())
         _native.check(rc, self.ctx)
         self.last_kmax = kmax.value
+
+    def _tune(self, plan, reps=3):
+        """Times one mat-vec of each kind on ``plan`` (CUDA events, after one
+        untimed launch each) and keeps the faster kind."""
+        L = _native.lib()
+        times = {}
+        for name, code in _KINDS.items():
+            _native.check(L.kr_batch_set_matvec(self.handle, code), self.ctx)
+            _native.check(L.kr_batch_matvec(self.handle, plan.op, stream_ptr()), self.ctx)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(reps):
+                _native.check(L.kr_batch_matvec(self.handle, plan.op, stream_ptr()), self.ctx)
+            b.record()
+            b.synchronize()
+            times[name] = a.elapsed_time(b) / reps
+        best = min(times, key=times.get)
+        _native.check(L.kr_batch_set_matvec(self.handle, _KINDS[best]), self.ctx)
+        self.tuned = times
+        self.matvec = best
 
     def korder(self):
         out = np.zeros(self.nvec, np.int32)

@@ -1,0 +1,66 @@
+"""Time-step loops recorded once as a CUDA graph and replayed with one launch.
+
+A user loop over the reference's ``TDSE.update`` (richmol/tdse.py:265-414,
+examples/ocs_alignment.py:70-100) sets the field, then steps, every time step.
+``StepGraph`` records a run of such steps for the plain FP64 path: per step the
+field launch (kr_set_field, the step's coefficients as kernel parameters, so
+each recorded step carries its own field) and the persistent step launch
+(kr_step, one per vector) on one stream; ``replay()`` then runs all of them with
+no host work in between. The library allocates nothing while stepping, so the
+recording holds only these launches and two small memsets per step.
+
+Limits: up to 16 operator parts (their field coefficients travel as kernel
+parameters; beyond that they are copied from host memory per call, which a
+recording cannot repeat); no Krylov orders are read back per step (a Lanczos
+error is sticky on the device and raised by ``replay`` through kr_sync_status).
+"""
+import torch
+
+from . import _native
+
+
+class StepGraph:
+    """Args:
+        tdse : richmol_gb300.TDSE      time grid and units
+        H0 : CarTens or None           field-free Hamiltonian (split operator)
+        vecs : (nvec, dim) complex128 CUDA tensor, propagated in place by replay()
+        hamiltonian : callable t -> CarTens with the field of time t set
+        times : the times of the recorded steps (e.g. a slice of time_grid())
+        tol, maxorder : as TDSE.update
+        before_step : optional callable recorded ahead of every step (e.g. an
+                      L2 flush for timing)
+    """
+
+    def __init__(self, tdse, H0, vecs, hamiltonian, times, tol=1e-15, maxorder=100, before_step=None):
+        assert torch.is_tensor(vecs) and vecs.is_cuda and vecs.dtype == torch.complex128
+        self.vecs = vecs if vecs.dim() == 2 else vecs.reshape(1, -1)
+        self.times = list(times)
+        fac = tdse.exp_fac
+        phase = tdse._h0_phase(H0, fac, vecs.device) if H0 is not None else None
+        # operators are created (and uploaded) outside the recording
+        plans = [hamiltonian(t).device_operator(maxorder=maxorder) for t in self.times[:1]]
+        if len(plans[0].sources) > _native.KR_PART_INLINE:
+            raise ValueError(f"a recorded step takes at most {_native.KR_PART_INLINE} operator parts")
+        self.plan = plans[0]
+        self.graph = torch.cuda.CUDAGraph()
+        stream = torch.cuda.Stream()
+        stream.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.graph(self.graph, stream=stream):
+            for t in self.times:
+                if before_step is not None:
+                    before_step()
+                plan = hamiltonian(t).device_operator(maxorder=maxorder)  # field launch of this step
+                plan.step(self.vecs, phase, fac, tol, flags=0, korder=None)
+        torch.cuda.current_stream().wait_stream(stream)
+
+    def replay(self):
+        """Runs the recorded steps on the current stream's device and checks
+        the Lanczos status afterwards (ValueError at maxorder, as tdse.py:480-484)."""
+        self.graph.replay()
+        try:
+            self.plan.sync_status()
+        except _native.KrylovError as e:
+            if e.code == _native.KR_ERR_MAXORDER:
+                raise ValueError("Lanczos reached maximum order without convergence") from None
+            raise
+        return self.vecs

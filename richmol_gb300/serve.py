@@ -103,7 +103,7 @@ class Job:
     C1 basis size and ``max_vectors``); ``run`` builds the molecule's factors on
     the host, then propagates."""
 
-    def __init__(self, req, mmax=20, tol=1e-8, matvec="tensor"):
+    def __init__(self, req, mmax=20, tol=1e-8, matvec="auto"):
         self.req = req
         self.mmax, self.tol, self.matvec = mmax, tol, matvec
         self.state_steps = 0
