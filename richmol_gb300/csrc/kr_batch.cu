@@ -53,6 +53,7 @@ struct kr_batch {
   double* err = nullptr;     // [nb]
   double2* part = nullptr;   // [KB_RED_CHUNKS][mmax + 2][nb] partial sums
   int* counts = nullptr;     // [3]: active vectors, vectors that hit mmax, mat-vec error word
+  int* tc_work = nullptr;    // [2] work-item counters of the persistent tensor-core launches
   // mat-vec tile table
   int ntask = 0;
   // per-slab populations (slabs of the operator the batch was created with)
@@ -237,6 +238,10 @@ __global__ void kb_start(const float4* S, float2* V0, const double2* nsq, double
 
 // partial dots h_j = <V_j, W> for j = 0..k: FP32 products, FP32 sums inside a
 // thread's elements, FP64 across threads and chunks
+// vdot(V_j, W) for j = 0 .. k, one pass per j: the chunk of W a CTA reads
+// stays in cache from pass to pass, so DRAM sees W once (one pass over all V_j
+// with W read once measured 45 % slower at C3); per chunk and vector,
+// part[chunk][j][nb]
 __global__ void kb_dots(const float2* V, const float2* W, const int* active, long long dim, int nb, int k,
                         int stride_coef, double2* part) {
   __shared__ double2 sh[8][32];
@@ -260,7 +265,8 @@ __global__ void kb_dots(const float2* V, const float2* W, const int* active, lon
   }
 }
 
-// V_{k+1} = W - sum_j h_j V_j (unnormalised), partial ||V_{k+1}||^2
+// V_{k+1} = W - sum_j h_j V_j (unnormalised), partial ||V_{k+1}||^2; k < KM
+template <int KM>
 __global__ void kb_update(float2* V, const float2* W, const double2* h, const int* active, long long dim, int nb,
                           int k, double2* part) {
   __shared__ double2 sh[8][32];
@@ -269,21 +275,24 @@ __global__ void kb_update(float2* V, const float2* W, const double2* h, const in
   const bool act = active[v] != 0;
   dfl nacc = {0.f, 0.f};
   if (act) {
-    float2 hv[KB_NK_MAX];
-    const int kk = min(k, KB_NK_MAX - 1);
-    for (int j = 0; j <= kk; ++j) {
-      const double2 t = h[(long long)j * nb + v];
+    float2 hv[KM];
+#pragma unroll
+    for (int j = 0; j < KM; ++j) {
+      const double2 t = j <= k ? h[(long long)j * nb + v] : make_double2(0.0, 0.0);
       hv[j] = make_float2((float)t.x, (float)t.y);
     }
     float2* Vn = V + (long long)(k + 1) * dim * nb;
     for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
       float2 r = W[e * nb + v];
-      for (int j = 0; j <= kk; ++j) {
-        const float2 a = V[((long long)j * dim + e) * nb + v];
-        r.x = fmaf(-hv[j].x, a.x, r.x);
-        r.x = fmaf(hv[j].y, a.y, r.x);
-        r.y = fmaf(-hv[j].x, a.y, r.y);
-        r.y = fmaf(-hv[j].y, a.x, r.y);
+#pragma unroll
+      for (int j = 0; j < KM; ++j) {
+        if (j <= k) {
+          const float2 a = V[((long long)j * dim + e) * nb + v];
+          r.x = fmaf(-hv[j].x, a.x, r.x);
+          r.x = fmaf(hv[j].y, a.y, r.x);
+          r.y = fmaf(-hv[j].x, a.y, r.y);
+          r.y = fmaf(-hv[j].y, a.x, r.y);
+        }
       }
       Vn[e * nb + v] = r;
       nacc = df_add(nacc, df_add(df_mulf({r.x, 0.f}, r.x), df_mulf({r.y, 0.f}, r.y)));
@@ -363,24 +372,32 @@ __global__ void kb_scale(float2* Vn, const double* vscale, const int* active, lo
 
 // S <- phase * (c_0 S + ||v|| sum_{i>=1} c_i V_i)   (double-float state; the
 // complex64 Krylov corrections summed in FP32)
+// S <- P (c_0 S + ||S|| sum_{1 <= i < K} c_i V_i), K < KM + 1 per vector
+template <int KM>
 __global__ void kb_combine(BatchDev b, const float4* phase) {
   const int v = blockIdx.y * 32 + threadIdx.x;
   const int nb = b.nb;
   const int K = b.kconv[v];
   if (K == 0) return;  // no Krylov step (zero vector or padding)
-  float2 cf[KB_NK_MAX];
-  for (int i = 1; i < K; ++i) cf[i] = make_float2((float)b.c[(long long)i * nb + v].x, (float)b.c[(long long)i * nb + v].y);
+  float2 cf[KM];
+#pragma unroll
+  for (int i = 1; i < KM; ++i)
+    cf[i] = i < K ? make_float2((float)b.c[(long long)i * nb + v].x, (float)b.c[(long long)i * nb + v].y)
+                  : make_float2(0.f, 0.f);
   const dfc c0 = dfc_from(b.c[v]);
   const dfl n0 = df_from(b.norm0[v]);
   const Chunk ch = chunk_of(b.dim);
   for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
     float2 sacc = make_float2(0.f, 0.f);
-    for (int i = 1; i < K; ++i) {
-      const float2 a = b.V[((long long)i * b.dim + e) * nb + v];
-      sacc.x = fmaf(cf[i].x, a.x, sacc.x);
-      sacc.x = fmaf(-cf[i].y, a.y, sacc.x);
-      sacc.y = fmaf(cf[i].x, a.y, sacc.y);
-      sacc.y = fmaf(cf[i].y, a.x, sacc.y);
+#pragma unroll
+    for (int i = 1; i < KM; ++i) {
+      if (i < K) {
+        const float2 a = b.V[((long long)i * b.dim + e) * nb + v];
+        sacc.x = fmaf(cf[i].x, a.x, sacc.x);
+        sacc.x = fmaf(-cf[i].y, a.y, sacc.x);
+        sacc.y = fmaf(cf[i].x, a.y, sacc.y);
+        sacc.y = fmaf(cf[i].y, a.x, sacc.y);
+      }
     }
     dfc u = dfc_mul(c0, dfc_ld(b.S[e * nb + v]));
     u.re = df_add(u.re, df_mulf(n0, sacc.x));
@@ -510,8 +527,14 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
     q.ntask = op->tc_ntask;
     q.grp_active = masked ? b->grp_active : nullptr;
     q.err = b->counts + 2;
-    const int rc = kb_launch_tc(op->ctx, q, b->dim, st);
-    if (rc == KR_OK) b->launches++;
+    q.tfirst = 0;
+    q.tend = op->tc_ntask;
+    q.nvb = b->nb / 128;
+    q.work = b->tc_work;
+    const int rc = kb_launch_tc(op->ctx, q, b->dim, op->tc_class, b->tc_work, st);
+    if (rc == KR_OK)
+      b->launches += (op->tc_class[1] > op->tc_class[0]) + (op->tc_class[2] > op->tc_class[1]) +
+                     (op->tc_class[3] > op->tc_class[2]);
     return rc;
   }
   BatchMV p;
@@ -572,6 +595,7 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
   BA(nb, &b->err);
   BA((size_t)KB_RED_CHUNKS * (m1 + 1) * nb, &b->part);
   BA(3, &b->counts);
+  BA(2, &b->tc_work);
   // output tiles: R = 128 / NKP rows of one slab (NKP = n_k rounded up to 4, 8, 16, 32)
   std::vector<int> ts, ti, tn;
   for (int s = 0; s < (int)dm.size(); ++s) {
@@ -659,7 +683,10 @@ extern "C" int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double f
     if (rc) return rc;
     kb_dots<<<eg, eb, 0, st>>>(b->V, b->W, b->active, dim, nb, k, stride, b->part);
     kb_reduce<<<((k + 1) * nb + 255) / 256, 256, 0, st>>>(b->part, k + 1, nb, stride, b->h);
-    kb_update<<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->active, dim, nb, k, b->part);
+    if (k < 4) kb_update<4><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->active, dim, nb, k, b->part);
+    else if (k < 8) kb_update<8><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->active, dim, nb, k, b->part);
+    else if (k < 16) kb_update<16><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->active, dim, nb, k, b->part);
+    else kb_update<32><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->active, dim, nb, k, b->part);
     // norms of V_{k+1} into the last coefficient slot of h (slot mmax + 1 is not a dot)
     kb_reduce<<<(nb + 255) / 256, 256, 0, st>>>(b->part, 1, nb, 1, b->h + (long long)(b->mmax) * nb);
     KR_CUDA(ctx, cudaMemsetAsync(b->counts, 0, 2 * sizeof(int), st));
@@ -678,7 +705,11 @@ extern "C" int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double f
                          std::to_string(b->mmax) + " Krylov vectors");
     if (counts[0] == 0) break;
   }
-  kb_combine<<<eg, eb, 0, st>>>(dev_view(b), pdf);
+  // every vector's order is at most kused + 1 (kconv)
+  if (kused < 4) kb_combine<4><<<eg, eb, 0, st>>>(dev_view(b), pdf);
+  else if (kused < 8) kb_combine<8><<<eg, eb, 0, st>>>(dev_view(b), pdf);
+  else if (kused < 16) kb_combine<16><<<eg, eb, 0, st>>>(dev_view(b), pdf);
+  else kb_combine<32><<<eg, eb, 0, st>>>(dev_view(b), pdf);
   b->launches++;
   KR_CUDA(ctx, cudaGetLastError());
   if (kmax_out) *kmax_out = kused;

@@ -29,6 +29,10 @@ struct BatchTC {
   int nb;
   const int* task;        // [4][ntask]: slab, first row, rows, KP
   int ntask;
+  int tfirst;             // first tile of this launch in task (per-tile kernel: tile tfirst + blockIdx.x)
+  int tend;               // persistent kernel: tiles [tfirst, tend) x vector blocks
+  int nvb;                // vector blocks of 128
+  int* work;              // persistent kernel: work-item counter (zero at launch)
   const int* grp_active;  // per 32-vector group: any vector active (null: all)
   int* err;
 };
@@ -50,6 +54,8 @@ __device__ __forceinline__ void macc(float2& y, float2 m, float2 t) {
 
 // launch kb_matvec over the tile table (ntask tiles x ngrp 32-vector groups)
 int kb_launch_simt(kr_ctx* ctx, const BatchMV& p, int ntask, int ngrp, cudaStream_t st);
-// launch kb_matvec_tc over its tile table (p.ntask tiles x nb / 128 vector
-// blocks); encodes the TMA descriptor of p.X ([dim][nb] complex64)
-int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, cudaStream_t st);
+// launch the tensor-core mat-vec over its tile table: the tiles of KP = 8 and
+// 16 (cls[0] .. cls[2]) as one persistent launch per class (work counters
+// work[0], work[1], zeroed here), the KP = 32 tiles (cls[2] .. cls[3]) one CTA
+// per tile and vector block; encodes the TMA descriptor of p.X ([dim][nb] complex64)
+int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, const int* cls, int* work, cudaStream_t st);

@@ -875,13 +875,310 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
   __syncthreads();
 }
 
+// ---------------------------------------------------------------------------
+// Persistent form of the ring tile (KP = 8, 16): one CTA per SM loops over the
+// work items (tile, block of 128 vectors) of one KP class, taken from a global
+// counter in order (heaviest tiles first). Warp 9 takes the next item, writes
+// its header and term table into one of two shared-memory buffers (ready: one
+// arrival; free: the 8 producer warps and the MMA warp, once done with the
+// tile) and streams the item's X window rows into the ring, running ahead of
+// the producers across tiles. TMEM, barriers and the ring persist over the
+// items; the commit count and the ring row counter run on. The first MMA of a
+// tile starts its accumulators afresh. Everything else as in kbt_tile_ring.
+// ---------------------------------------------------------------------------
+constexpr int KBT_MAXT_P = 32;  // term table entries per buffer
+
+template <int KP>
+struct KbtPers {
+  using Rg = KbtRing<KP>;
+  static constexpr int NSLOT = Rg::NSLOT;
+  static constexpr int OFF_BAR = Rg::OFF_MFD + 2 * Rg::MFD * 16;
+  // full, empty, rfull[NSLOT], rempty[NSLOT], ready[2], free[2], TMEM slot
+  static constexpr int OFF_HDR = OFF_BAR + 8 * (2 + 2 * NSLOT + 4) + 16;
+  static constexpr int OFF_TAB = OFF_HDR + 2 * 8 * 4;
+  static constexpr int TOTAL = OFF_TAB + 2 * KBT_MAXT_P * (int)sizeof(KbtTerm);
+};
+static_assert(KbtPers<8>::TOTAL <= 232448 && KbtPers<16>::TOTAL <= 232448, "persistent tile exceeds shared memory");
+
+template <int KP>
+__device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* smem) {
+  using L = KbtPers<KP>;
+  using Rg = KbtRing<KP>;
+  constexpr int R = 64 / KP, BH = KP / 2, NSLOT = L::NSLOT;
+  constexpr int ATILE = 128 * KP;
+  const DevOp& op = p.op;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int vq = wid & 3, b0 = ((wid >> 2) & 1) * BH;
+  const int vloc = vq * 32 + lane;
+  const long long nb = p.nb;
+  float* As = reinterpret_cast<float*>(smem);
+  char* Bs = smem + Rg::OFF_B;
+  char* ring = smem + Rg::OFF_RING;
+  float2* MFs0 = reinterpret_cast<float2*>(smem + Rg::OFF_MF);
+  int* Cs0 = reinterpret_cast<int*>(smem + Rg::OFF_CS);
+  float4* MFd0 = reinterpret_cast<float4*>(smem + Rg::OFF_MFD);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);
+  uint64_t* empty = full + 1;
+  uint64_t* rfull = full + 2;
+  uint64_t* rempty = rfull + NSLOT;
+  uint64_t* tready = rempty + NSLOT;
+  uint64_t* tfree = tready + 2;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(tfree + 2);
+  int* hdr0 = reinterpret_cast<int*>(smem + L::OFF_HDR);  // [2][8]: item (-1: none), s1, i0, nr, vb, tb, te
+  KbtTerm* tab0 = reinterpret_cast<KbtTerm*>(smem + L::OFF_TAB);
+  constexpr uint32_t NCOLS = 512;  // the largest D of a tile: 4 R NP <= 512 (merged) or 2 R NP
+  if (wid == 8) tc_alloc(tslot, NCOLS);
+  if (tid == 256) {
+    tc_mbar_init(full, 8);
+    tc_mbar_init(empty, 1);
+    for (int i = 0; i < NSLOT; ++i) {
+      tc_mbar_init(rfull + i, 1);
+      tc_mbar_init(rempty + i, 8);
+    }
+    for (int b = 0; b < 2; ++b) {
+      tc_mbar_init(tready + b, 1);
+      tc_mbar_init(tfree + b, 9);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  bool ok = true;
+  const int nct = p.tend - p.tfirst;
+  const int nwork = nct * p.nvb;
+
+  if (wid == 9) {
+    // ---- work items, term tables and X window loads -------------------------
+    int g = 0;
+    for (int it = 0;; ++it) {
+      const int b = it & 1;
+      if (it >= 2 && !tc_mbar_wait(tfree + b, (uint32_t)((it - 2) >> 1) & 1u)) ok = false;
+      int w = 0;
+      for (;;) {  // next item whose vector block has an active vector
+        if (lane == 0) w = (int)atomicAdd(reinterpret_cast<unsigned*>(p.work), 1u);
+        w = __shfl_sync(0xffffffffu, w, 0);
+        if (w >= nwork || !p.grp_active) break;
+        const int* gq = p.grp_active + 4 * (w / nct);
+        if (gq[0] | gq[1] | gq[2] | gq[3]) break;
+      }
+      int* hdr = hdr0 + 8 * b;
+      KbtTerm* tab = tab0 + KBT_MAXT_P * b;
+      if (w >= nwork) {
+        if (lane == 0) {
+          hdr[0] = -1;
+          tc_mbar_arrive(tready + b);
+        }
+        break;
+      }
+      const int task = p.tfirst + w % nct, vb = w / nct;
+      const int s1 = __ldg(p.task + task);
+      const int i0 = __ldg(p.task + p.ntask + task);
+      const int nr = __ldg(p.task + 2 * p.ntask + task);
+      const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
+      for (int j = lane; j < te - tb && j < KBT_MAXT_P; j += 32) tab[j] = kbt_term(op, p, tb + j, KP, 0, nb);
+      if (lane == 0) {
+        hdr[0] = w;
+        hdr[1] = s1;
+        hdr[2] = i0;
+        hdr[3] = nr;
+        hdr[4] = vb;
+        hdr[5] = tb;
+        hdr[6] = te;
+      }
+      __syncwarp();
+      if (lane == 0) {
+        tc_mbar_arrive(tready + b);  // release: the header and table above
+        for (int term = tb; term < te; ++term) {
+          const KbtTerm t = (term - tb < KBT_MAXT_P) ? tab[term - tb] : kbt_term(op, p, term, KP, 0, nb);
+          const int nwin = kbt_ring_rows(t, nr);
+          const long long row0 = __ldg(op.in_off + t.s2);
+          for (int c = 0; c < nwin; ++c, ++g) {
+            const int slot = g % NSLOT;
+            if (g >= NSLOT && !tc_mbar_wait(rempty + slot, (uint32_t)(g / NSLOT - 1) & 1u)) ok = false;
+            tc_mbar_expect_tx(rfull + slot, (uint32_t)Rg::SLOT);
+            const long long y = row0 + (long long)(i0 + t.d0 + c) * t.ld2;
+            char* dst = ring + (size_t)slot * Rg::SLOT;
+#pragma unroll
+            for (int h = 0; h < KP / 8; ++h)
+              tc_tma_load_2d(dst + h * 8192, xmap, vb * 128, (int)(y + 8 * h), rfull + slot);
+          }
+        }
+      }
+      __syncwarp();
+    }
+  } else if (wid == 8) {
+    // ---- MMA issue -------------------------------------------------------------
+    int ncommit = 0;
+    const uint64_t adesc0 = tc_desc(tc_smem_u32(As), 128u, 32u * KP);
+    const uint64_t bdesc0 = tc_desc(tc_smem_u32(Bs), 128u, 32u * KP);
+    for (int it = 0;; ++it) {
+      const int b = it & 1;
+      if (!tc_mbar_wait(tready + b, (uint32_t)(it >> 1) & 1u)) {
+        ok = false;
+        break;
+      }
+      const int* hdr = hdr0 + 8 * b;
+      if (hdr[0] < 0) break;
+      const int s1 = hdr[1], nr = hdr[3], tb = hdr[5], te = hdr[6];
+      const KbtTerm* tab = tab0 + KBT_MAXT_P * b;
+      if (lane == 0) {
+        const int nk1 = __ldg(op.out_dk + s1);
+        const int NP = nk1 <= 16 ? 16 : 32;
+        const bool merged = 4 * R * NP <= 512;
+        const int bpart = merged ? NP * KP * 4 : Rg::BPART;
+        const uint32_t idesc = tc_idesc_tf32(128, NP), idesc2 = tc_idesc_tf32(128, 2 * NP);
+        const int c0 = ncommit;
+        uint32_t dinit = 0;
+        for (int term = tb; term < te; ++term) {
+          const KbtTerm tt = (term - tb < KBT_MAXT_P) ? tab[term - tb] : kbt_term(op, p, term, KP, 0, nb);
+          if (!tt.ok || tt.empty) continue;  // skipped by the producers as well
+          if (!tc_mbar_wait(full, (uint32_t)ncommit & 1u)) ok = false;
+          tc_fence_after();
+          const uint64_t bdesc = bdesc0 + (uint64_t)((((term - tb) & 1) * Rg::BBUF) >> 4);
+          if (merged) {
+            const uint32_t acc0 = ncommit > c0 ? 1u : 0u;
+            if (tt.ktype == 1) kbt_issue_merged<KP, 1>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
+            else if (tt.ktype == 2) kbt_issue_merged<KP, 2>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
+            else kbt_issue_merged<KP, 0>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
+          } else {
+            kbt_issue<KP>(tmem, adesc0, bdesc, idesc, NP, nr, tt.ktype, tt.nk2, dinit, Rg::BPART);
+          }
+          tc_commit(empty);
+          ++ncommit;
+        }
+      }
+      ncommit = __shfl_sync(0xffffffffu, ncommit, 0);
+      __syncwarp();
+      if (lane == 0) tc_mbar_arrive(tfree + b);
+    }
+  } else {
+    // ---- producers ---------------------------------------------------------------
+    int g = 0, ncommit = 0;
+    float2 z[R][BH];
+    for (int it = 0;; ++it) {
+      const int b = it & 1;
+      if (!tc_mbar_wait(tready + b, (uint32_t)(it >> 1) & 1u)) {
+        ok = false;
+        break;
+      }
+      const int* hdr = hdr0 + 8 * b;
+      if (hdr[0] < 0) break;
+      const int s1 = hdr[1], i0 = hdr[2], nr = hdr[3], vb = hdr[4], tb = hdr[5], te = hdr[6];
+      const KbtTerm* tab = tab0 + KBT_MAXT_P * b;
+      const int v = vb * 128 + vloc;
+      auto term_at = [&](int i) {
+        KbtTerm tt = (i < KBT_MAXT_P) ? tab[i] : kbt_term(op, p, tb + i, KP, 0, nb);
+        tt.Xs2 += v;
+        return tt;
+      };
+      const int nk1 = __ldg(op.out_dk + s1);
+      const int ld1 = __ldg(op.out_stride + s1);
+      float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * ld1) * nb + v;
+      const int NP = nk1 <= 16 ? 16 : 32;
+      const bool merged = 4 * R * NP <= 512;
+      const int bpart = merged ? NP * KP * 4 : Rg::BPART;
+      if (te == tb) {  // no term reaches this slab
+        for (int e = wid >> 2; e < nr * nk1; e += 2)
+          Y[((long long)(e / nk1) * ld1 + e % nk1) * nb] = make_float2(0.f, 0.f);
+        __syncwarp();
+        if (lane == 0) tc_mbar_arrive(tfree + b);
+        continue;
+      }
+      const int c0 = ncommit;
+      KbtTerm cur = term_at(0);
+      KbtPre pre;
+      // every producer is past the previous tile's use of the B / MF buffers
+      // (its epilogue waited for the last MMAs); the staging below reuses them
+      kbt_preload<KP>(cur, nk1, NP, i0, nr, tid, pre);
+      kbt_producer_sync();
+      kbt_stage_pre<KP>(cur, pre, NP, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, MFd0, tid, bpart);
+      kbt_producer_sync();
+      if (!kbt_zstep_ring<KP>(z, cur, nb, nr, b0, vloc, lane, MFs0, Cs0, MFd0, ring, rfull, rempty, g)) ok = false;
+      for (int term = tb; term < te; ++term) {
+        const int buf = (term - tb) & 1;
+        const bool has_next = term + 1 < te;
+        KbtTerm nxt;
+        if (has_next) {
+          nxt = term_at(term + 1 - tb);
+          kbt_preload<KP>(nxt, nk1, NP, i0, nr, tid, pre);
+        }
+        if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
+        tc_fence_after();
+        if (cur.ok && !cur.empty) {
+#pragma unroll
+          for (int r = 0; r < R; ++r)
+            if (r < nr) kbt_store_row<KP>(As + r * 4 * ATILE, z[r], vloc, b0);
+          tc_fence_proxy();
+          __syncwarp();
+          if (lane == 0) tc_mbar_arrive(full);
+          ++ncommit;
+        } else if (!cur.ok && tid == 0) {
+          atomicExch(p.err, KR_ERR_ARG);  // outside the tile shape: skipped
+        }
+        if (has_next) {
+          kbt_stage_pre<KP>(nxt, pre, NP, nr, reinterpret_cast<float*>(Bs + (buf ^ 1) * Rg::BBUF),
+                            MFs0 + (buf ^ 1) * 8 * KB_WMAX, Cs0 + (buf ^ 1) * 8 * KB_WMAX,
+                            MFd0 + (buf ^ 1) * Rg::MFD, tid, bpart);
+          kbt_producer_sync();
+          if (!kbt_zstep_ring<KP>(z, nxt, nb, nr, b0, vloc, lane, MFs0 + (buf ^ 1) * 8 * KB_WMAX,
+                                  Cs0 + (buf ^ 1) * 8 * KB_WMAX, MFd0 + (buf ^ 1) * Rg::MFD, ring, rfull, rempty, g))
+            ok = false;
+          cur = nxt;
+        }
+      }
+      if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
+      tc_fence_after();
+      const bool any = ncommit > c0;
+      for (int r = wid >> 2; r < nr; r += 2) {
+        for (int cc = 0; cc < NP; cc += 16) {
+          float re[16], im[16];
+          const uint32_t lanebase = (uint32_t)(vq * 32) << 16;
+          if (merged) {
+            float re2[16], im2[16];
+            tc_ld16(tmem + lanebase + (uint32_t)(4 * r * NP + cc), re);
+            tc_ld16(tmem + lanebase + (uint32_t)(4 * r * NP + NP + cc), re2);
+            tc_ld16(tmem + lanebase + (uint32_t)(4 * r * NP + 2 * NP + cc), im);
+            tc_ld16(tmem + lanebase + (uint32_t)(4 * r * NP + 3 * NP + cc), im2);
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              re[q] += re2[q];
+              im[q] += im2[q];
+            }
+          } else {
+            tc_ld16(tmem + lanebase + (uint32_t)(2 * r * NP + cc), re);
+            tc_ld16(tmem + lanebase + (uint32_t)((2 * r + 1) * NP + cc), im);
+          }
+#pragma unroll
+          for (int q = 0; q < 16; ++q)
+            if (cc + q < nk1)
+              Y[((long long)r * ld1 + cc + q) * nb] = any ? make_float2(re[q], im[q]) : make_float2(0.f, 0.f);
+        }
+      }
+      tc_fence_before();  // the TMEM reads above come before the next tile's MMAs
+      __syncwarp();
+      if (lane == 0) tc_mbar_arrive(tfree + b);
+    }
+  }
+  if (!ok && lane == 0) atomicExch(p.err, KR_ERR_TIMEOUT);
+  tc_fence_before();
+  __syncthreads();
+  if (wid == 8) tc_dealloc(tmem, NCOLS);
+}
+
+template <int KP>
+__global__ void __launch_bounds__(320, 1) kb_matvec_tcp(BatchTC p, const __grid_constant__ CUtensorMap xmap) {
+  extern __shared__ __align__(1024) char kbt_smem[];
+  kbt_persist<KP>(p, &xmap, kbt_smem);
+}
+
 __global__ void __launch_bounds__(320, 1) kb_matvec_tc(BatchTC p, const __grid_constant__ CUtensorMap xmap) {
   extern __shared__ __align__(1024) char kbt_smem[];
   if (p.grp_active) {
     const int* g = p.grp_active + 4 * blockIdx.y;
     if (!(g[0] | g[1] | g[2] | g[3])) return;
   }
-  const int task = blockIdx.x;
+  const int task = p.tfirst + blockIdx.x;
   const int s1 = __ldg(p.task + task);
   const int i0 = __ldg(p.task + p.ntask + task);
   const int nr = __ldg(p.task + 2 * p.ntask + task);
@@ -918,15 +1215,45 @@ static int encode_xmap(kr_ctx* ctx, const float2* X, long long dim, int nb, CUte
   return KR_OK;
 }
 
-int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, cudaStream_t st) {
+int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, const int* cls, int* work, cudaStream_t st) {
   CUtensorMap xmap;
   const int rc = encode_xmap(ctx, p.X, dim, p.nb, &xmap);
   if (rc != KR_OK) return rc;
-  const int smem = std::max(TC_SMEM, TC_SMEM_RING);
-  // per device (the attribute belongs to the current device's context)
-  KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  kb_matvec_tc<<<dim3(p.ntask, p.nb / 128), 320, smem, st>>>(p, xmap);
-  KR_CUDA(ctx, cudaGetLastError());
+  const int nvb = p.nb / 128;
+  KR_CUDA(ctx, cudaMemsetAsync(work, 0, 2 * sizeof(int), st));
+  // persistent launches, one per KP class (8, 16): one CTA per SM at most
+  for (int c = 0; c < 2; ++c) {
+    const int n = cls[c + 1] - cls[c];
+    if (n <= 0) continue;
+    BatchTC q = p;
+    q.tfirst = cls[c];
+    q.tend = cls[c + 1];
+    q.nvb = nvb;
+    q.work = work + c;
+    const int grid = (int)std::min<long long>((long long)n * nvb, ctx->nsm);
+    if (c == 0) {
+      KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tcp<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        KbtPers<8>::TOTAL));
+      kb_matvec_tcp<8><<<grid, 320, KbtPers<8>::TOTAL, st>>>(q, xmap);
+    } else {
+      KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tcp<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        KbtPers<16>::TOTAL));
+      kb_matvec_tcp<16><<<grid, 320, KbtPers<16>::TOTAL, st>>>(q, xmap);
+    }
+    KR_CUDA(ctx, cudaGetLastError());
+  }
+  // KP = 32: one CTA per tile and vector block
+  const int n32 = cls[3] - cls[2];
+  if (n32 > 0) {
+    BatchTC q = p;
+    q.tfirst = cls[2];
+    q.tend = cls[3];
+    q.nvb = nvb;
+    const int smem = std::max(TC_SMEM, TC_SMEM_RING);
+    KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    kb_matvec_tc<<<dim3(n32, nvb), 320, smem, st>>>(q, xmap);
+    KR_CUDA(ctx, cudaGetLastError());
+  }
   return KR_OK;
 }
 

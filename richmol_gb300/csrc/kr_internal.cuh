@@ -83,6 +83,7 @@ struct kr_op {
   // tiles of the tensor-core batched mat-vec: [4][tc_ntask] = slab, first row, rows, KP
   int tc_ntask = 0;
   int* tc_task = nullptr;
+  int tc_class[4] = {0, 0, 0, 0};  // first tile of KP = 8, 16, 32 in tc_task, and the end
   // workspace of kr_expv / kr_op_norm1 (grown on demand, freed with the operator)
   void* expv_ws = nullptr;
   size_t expv_bytes = 0;

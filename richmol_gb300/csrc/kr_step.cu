@@ -1125,7 +1125,15 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
     const int n = (int)ts.size();
     std::vector<int> ord(n);
     std::iota(ord.begin(), ord.end(), 0);
-    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return tcost[x] > tcost[y]; });
+    // classes of KP together (8, 16, 32: one persistent launch per class), heaviest first
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int x, int y) { return tk[x] != tk[y] ? tk[x] < tk[y] : tcost[x] > tcost[y]; });
+    for (int c = 0; c < 3; ++c) {
+      const int kpc = 8 << c;
+      op->tc_class[c] = (int)(std::lower_bound(ord.begin(), ord.end(), kpc,
+                                               [&](int x, int kv) { return tk[x] < kv; }) - ord.begin());
+    }
+    op->tc_class[3] = n;
     tc_task.resize((size_t)4 * n);
     for (int q = 0; q < n; ++q) {
       tc_task[q] = ts[ord[q]];
