@@ -103,7 +103,9 @@ class Job:
     C1 basis size and ``max_vectors``); ``run`` builds the molecule's factors on
     the host, then propagates."""
 
-    def __init__(self, req, mmax=20, tol=1e-8, matvec="auto"):
+    def __init__(self, req, mmax=20, tol=1e-8, matvec="tensor"):
+        # a fixed kernel kind: a timed choice (matvec="auto") could differ between a
+        # job alone and the same job among others, and so could its last digits
         self.req = req
         self.mmax, self.tol, self.matvec = mmax, tol, matvec
         self.state_steps = 0
