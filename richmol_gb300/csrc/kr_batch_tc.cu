@@ -491,17 +491,15 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
 
 
 // ---------------------------------------------------------------------------
-// Tensor-core tile with the X windows streamed by TMA (KP = 8, 16). Warp 8
-// lane 1 walks the window rows of every diagonal term of the tile in order
-// and loads each (KP input rows x 128 vectors, KP/8 boxes of 8 rows) into a
-// ring of shared-memory slots (full: tx bytes; empty: one arrival per
-// producer warp); the producer warps read X from the ring, so no global-load
-// latency sits in their M step. Rows outside the input slab read whatever
-// lies there (finite data of other slabs, or zeros beyond the array) and meet
-// zero MF slots; columns beyond n_k2 are zeroed on read. Terms stored as ELL
-// load X directly. Everything else as in kbt_tile.
+// X windows streamed by TMA (KP = 8, 16): the loader warp walks the window
+// rows of every diagonal term in order and loads each (KP input rows x 128
+// vectors, KP/8 boxes of 8 rows) into a ring of shared-memory slots (full: tx
+// bytes; empty: one arrival per producer warp); the producer warps read X from
+// the ring, so no global-load latency sits in their M step. Rows outside the
+// input slab read whatever lies there (finite data of other slabs, or zeros
+// beyond the array) and meet zero MF slots. Terms stored as ELL load X
+// directly. The layout below is shared by the persistent kernel (KbtPers).
 // ---------------------------------------------------------------------------
-constexpr int KBT_MAXT = 64;  // terms of one output slab held in the shared-memory table
 
 template <int KP>
 struct KbtRing {
@@ -519,12 +517,7 @@ struct KbtRing {
   static constexpr int NWIN = R + KR_DIAG_MAX - 1;  // window rows of the widest band
   static constexpr int OFF_MFD = OFF_CS + TC_CSBYTES;
   static constexpr int MFD = NWIN * R;             // float4 entries of one buffer
-  static constexpr int OFF_BAR = OFF_MFD + 2 * MFD * 16;
-  static constexpr int OFF_TAB = OFF_BAR + 8 * (2 + 2 * NSLOT) + 16;  // term table (KBT_MAXT entries)
-  static constexpr int TOTAL = OFF_TAB + KBT_MAXT * (int)sizeof(KbtTerm);
 };
-constexpr int TC_SMEM_RING = KbtRing<16>::TOTAL > KbtRing<8>::TOTAL ? KbtRing<16>::TOTAL : KbtRing<8>::TOTAL;
-static_assert(TC_SMEM_RING <= 232448, "ring tile exceeds the shared memory of one CTA");
 static_assert(KbtRing<8>::MFD <= 256 && KbtRing<16>::MFD <= 256, "one dense-band entry per producer thread");
 
 // the next term's B and MF values, loaded into registers before they are staged
@@ -671,209 +664,6 @@ __device__ __forceinline__ bool kbt_zstep_ring(float2 (&z)[64 / KP][KP / 2], con
   return true;
 }
 
-template <int KP>
-__device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1, int i0, int nr, char* smem) {
-  using L = KbtRing<KP>;
-  constexpr int R = 64 / KP, BH = KP / 2, NSLOT = L::NSLOT;
-  constexpr int ATILE = 128 * KP;  // floats of one A tile
-  const DevOp& op = p.op;
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const bool producer = wid < 8;
-  const int vq = wid & 3, b0 = ((wid >> 2) & 1) * BH;
-  const int vloc = vq * 32 + lane;
-  const long long nb = p.nb;
-  const int v = blockIdx.y * 128 + vloc;
-  float* As = reinterpret_cast<float*>(smem);
-  char* Bs = smem + L::OFF_B;
-  char* ring = smem + L::OFF_RING;
-  float2* MFs0 = reinterpret_cast<float2*>(smem + L::OFF_MF);  // [2][8][KB_WMAX]
-  int* Cs0 = reinterpret_cast<int*>(smem + L::OFF_CS);         // [2][8][KB_WMAX]
-  float4* MFd0 = reinterpret_cast<float4*>(smem + L::OFF_MFD);  // [2][L::MFD]
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);  // A tiles of a term stored (8 warps)
-  uint64_t* empty = full + 1;                                         // MMAs of a term done
-  uint64_t* rfull = full + 2;
-  uint64_t* rempty = rfull + NSLOT;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(rempty + NSLOT);
-  KbtTerm* tab = reinterpret_cast<KbtTerm*>(smem + L::OFF_TAB);
-  const int nk1 = __ldg(op.out_dk + s1);
-  const int NP = nk1 <= 16 ? 16 : 32;
-  // K_hi and K_lo merged along N when the split D regions fit the TMEM
-  const bool merged = 4 * R * NP <= 512;
-  const int bpart = merged ? NP * KP * 4 : L::BPART;  // merged: parts adjacent along N
-  // output rows ld1 elements apart; the pointer is formed where it is used
-  auto y_rows = [&](int& ld1) {
-    ld1 = __ldg(op.out_stride + s1);
-    return p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * ld1) * nb + v;
-  };
-  const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
-  if (te == tb) {  // no term reaches this slab
-    if (producer) {
-      int ld1;
-      float2* Y = y_rows(ld1);
-      for (int e = wid >> 2; e < nr * nk1; e += 2)
-        Y[((long long)(e / nk1) * ld1 + e % nk1) * nb] = make_float2(0.f, 0.f);
-    }
-    return;
-  }
-  uint32_t ncols = 32;
-  while (ncols < (uint32_t)((merged ? 4 : 2) * R * NP)) ncols <<= 1;
-  if (wid == 8) tc_alloc(tslot, ncols);
-  if (tid == 256) {
-    tc_mbar_init(full, 8);
-    tc_mbar_init(empty, 1);
-    for (int i = 0; i < NSLOT; ++i) {
-      tc_mbar_init(rfull + i, 1);
-      tc_mbar_init(rempty + i, 8);
-    }
-  }
-  // term table: the tables of every term of the slab, read once per tile
-  const int nt = te - tb;
-  const bool use_tab = nt <= KBT_MAXT;
-  if (use_tab)
-    for (int i = tid; i < nt; i += blockDim.x) tab[i] = kbt_term(op, p, tb + i, KP, 0, nb);
-  auto term_at = [&](int i) {
-    KbtTerm tt = use_tab ? tab[i] : kbt_term(op, p, tb + i, KP, 0, nb);
-    tt.Xs2 += v;
-    return tt;
-  };
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = *tslot;
-  bool ok = true;
-  int ncommit = 0;  // terms whose MMAs were (or will be) committed
-
-  if (!producer) {
-    if (wid == 8 && lane == 0) {
-      // ---- MMA issue -------------------------------------------------------
-      const uint32_t idesc = tc_idesc_tf32(128, NP);
-      const uint32_t idesc2 = tc_idesc_tf32(128, 2 * NP);
-      const uint64_t adesc0 = tc_desc(tc_smem_u32(As), 128u, 32u * KP);
-      const uint64_t bdesc0 = tc_desc(tc_smem_u32(Bs), 128u, 32u * KP);
-      uint32_t dinit = 0;
-      for (int term = tb; term < te; ++term) {
-        const KbtTerm tt = term_at(term - tb);
-        if (!tt.ok || tt.empty) continue;  // skipped by the producers as well
-        const uint64_t bdesc = bdesc0 + (uint64_t)((((term - tb) & 1) * L::BBUF) >> 4);
-        if (!tc_mbar_wait(full, (uint32_t)ncommit & 1u)) ok = false;
-        tc_fence_after();
-        if (merged) {
-          const uint32_t acc0 = ncommit > 0 ? 1u : 0u;
-          if (tt.ktype == 1) kbt_issue_merged<KP, 1>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
-          else if (tt.ktype == 2) kbt_issue_merged<KP, 2>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
-          else kbt_issue_merged<KP, 0>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
-        } else {
-          kbt_issue<KP>(tmem, adesc0, bdesc, idesc, NP, nr, tt.ktype, tt.nk2, dinit, L::BPART);
-        }
-        tc_commit(empty);
-        ++ncommit;
-      }
-    } else if (wid == 9 && lane == 0) {
-      // ---- X window loads (TMA) into the ring (own warp: a waiting MMA lane
-      // would hold up a loader lane of the same warp) ------------------------
-      int g = 0;
-      for (int term = tb; term < te; ++term) {
-        const KbtTerm t = term_at(term - tb);
-        const int nwin = kbt_ring_rows(t, nr);
-        const long long row0 = __ldg(op.in_off + t.s2);  // first X row of slab s2
-        for (int c = 0; c < nwin; ++c, ++g) {
-          const int slot = g % NSLOT;
-          if (g >= NSLOT && !tc_mbar_wait(rempty + slot, (uint32_t)(g / NSLOT - 1) & 1u)) ok = false;
-          tc_mbar_expect_tx(rfull + slot, (uint32_t)L::SLOT);
-          const long long y = row0 + (long long)(i0 + t.d0 + c) * t.ld2;  // first X row of the window row
-          char* dst = ring + (size_t)slot * L::SLOT;
-#pragma unroll
-          for (int h = 0; h < KP / 8; ++h)
-            tc_tma_load_2d(dst + h * 8192, xmap, blockIdx.y * 128, (int)(y + 8 * h), rfull + slot);
-        }
-      }
-    }
-    if (!ok) atomicExch(p.err, KR_ERR_TIMEOUT);
-    tc_fence_before();
-    __syncthreads();
-    if (wid == 8) tc_dealloc(tmem, ncols);
-    return;
-  }
-
-  // ---- producers -------------------------------------------------------------
-  float2 z[R][BH];
-  int g = 0;  // ring row counter
-  KbtTerm cur = term_at(0);
-  KbtPre pre;
-  kbt_preload<KP>(cur, nk1, NP, i0, nr, tid, pre);
-  kbt_stage_pre<KP>(cur, pre, NP, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, MFd0, tid, bpart);
-  kbt_producer_sync();
-  if (!kbt_zstep_ring<KP>(z, cur, nb, nr, b0, vloc, lane, MFs0, Cs0, MFd0, ring, rfull, rempty, g)) ok = false;
-  for (int term = tb; term < te; ++term) {
-    const int buf = (term - tb) & 1;
-    const bool has_next = term + 1 < te;
-    KbtTerm nxt;
-    if (has_next) {  // the next term's K and MF values in flight during the A-tile hand-off
-      nxt = term_at(term + 1 - tb);
-      kbt_preload<KP>(nxt, nk1, NP, i0, nr, tid, pre);
-    }
-    // the MMAs of the previous committed term are done with the A tiles and its B buffer
-    if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
-    tc_fence_after();
-    if (cur.ok && !cur.empty) {
-#pragma unroll
-      for (int r = 0; r < R; ++r)
-        if (r < nr) kbt_store_row<KP>(As + r * 4 * ATILE, z[r], vloc, b0);
-      tc_fence_proxy();
-      __syncwarp();  // one arrival per warp, after every lane's stores and proxy fence
-      if (lane == 0) tc_mbar_arrive(full);
-      ++ncommit;
-    } else if (!cur.ok && tid == 0) {
-      atomicExch(p.err, KR_ERR_ARG);  // outside the tile shape: skipped
-    }
-    if (has_next) {
-      // B buffer buf ^ 1 was last read by the MMAs of term - 1 (done); MF buffer
-      // buf ^ 1 by the M step of term - 1 (every producer is past it)
-      kbt_stage_pre<KP>(nxt, pre, NP, nr, reinterpret_cast<float*>(Bs + (buf ^ 1) * L::BBUF),
-                        MFs0 + (buf ^ 1) * 8 * KB_WMAX, Cs0 + (buf ^ 1) * 8 * KB_WMAX, MFd0 + (buf ^ 1) * L::MFD,
-                        tid, bpart);
-      kbt_producer_sync();
-      if (!kbt_zstep_ring<KP>(z, nxt, nb, nr, b0, vloc, lane, MFs0 + (buf ^ 1) * 8 * KB_WMAX,
-                              Cs0 + (buf ^ 1) * 8 * KB_WMAX, MFd0 + (buf ^ 1) * L::MFD, ring, rfull, rempty, g))
-        ok = false;
-      cur = nxt;
-    }
-  }
-  if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
-  tc_fence_after();
-  // epilogue: rows r = w / 4, w / 4 + 2, ... of this warp's lane quarter
-  int ld1;
-  float2* Y = y_rows(ld1);
-  for (int r = wid >> 2; r < nr; r += 2) {
-    for (int c0 = 0; c0 < NP; c0 += 16) {
-      float re[16], im[16];
-      const uint32_t lanebase = (uint32_t)(vq * 32) << 16;
-      if (merged) {  // D_re, D_im: halves hi [K_hi] + lo [K_hi] and hi [K_lo]
-        float re2[16], im2[16];
-        tc_ld16(tmem + lanebase + (uint32_t)(4 * r * NP + c0), re);
-        tc_ld16(tmem + lanebase + (uint32_t)(4 * r * NP + NP + c0), re2);
-        tc_ld16(tmem + lanebase + (uint32_t)(4 * r * NP + 2 * NP + c0), im);
-        tc_ld16(tmem + lanebase + (uint32_t)(4 * r * NP + 3 * NP + c0), im2);
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          re[q] += re2[q];
-          im[q] += im2[q];
-        }
-      } else {
-        tc_ld16(tmem + lanebase + (uint32_t)(2 * r * NP + c0), re);
-        tc_ld16(tmem + lanebase + (uint32_t)((2 * r + 1) * NP + c0), im);
-      }
-      const bool any = ncommit > 0;
-#pragma unroll
-      for (int q = 0; q < 16; ++q)
-        if (c0 + q < nk1)
-          Y[((long long)r * ld1 + c0 + q) * nb] = any ? make_float2(re[q], im[q]) : make_float2(0.f, 0.f);
-    }
-  }
-  if (!ok && lane == 0) atomicExch(p.err, KR_ERR_TIMEOUT);
-  tc_fence_before();
-  __syncthreads();
-}
 
 // ---------------------------------------------------------------------------
 // Persistent form of the ring tile (KP = 8, 16): one CTA per SM loops over the
@@ -884,7 +674,7 @@ __device__ void kbt_tile_ring(const BatchTC& p, const CUtensorMap* xmap, int s1,
 // tile) and streams the item's X window rows into the ring, running ahead of
 // the producers across tiles. TMEM, barriers and the ring persist over the
 // items; the commit count and the ring row counter run on. The first MMA of a
-// tile starts its accumulators afresh. Everything else as in kbt_tile_ring.
+// tile starts its accumulators afresh.
 // ---------------------------------------------------------------------------
 constexpr int KBT_MAXT_P = 32;  // term table entries per buffer
 
@@ -1183,9 +973,8 @@ __global__ void __launch_bounds__(320, 1) kb_matvec_tc(BatchTC p, const __grid_c
   const int i0 = __ldg(p.task + p.ntask + task);
   const int nr = __ldg(p.task + 2 * p.ntask + task);
   const int kp = __ldg(p.task + 3 * p.ntask + task);
-  if (kp == 8) kbt_tile_ring<8>(p, &xmap, s1, i0, nr, kbt_smem);
-  else if (kp == 16) kbt_tile_ring<16>(p, &xmap, s1, i0, nr, kbt_smem);
-  else kbt_tile<32>(p, s1, i0, nr, kbt_smem);
+  if (kp == 32) kbt_tile<32>(p, s1, i0, nr, kbt_smem);
+  else if (threadIdx.x == 0) atomicExch(p.err, KR_ERR_ARG);  // KP = 8, 16 tiles go to kb_matvec_tcp
 }
 
 // TMA descriptor of an X buffer [dim][nb] (complex64 as 8-byte elements):
@@ -1249,7 +1038,7 @@ int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, const int* cls, i
     q.tfirst = cls[2];
     q.tend = cls[3];
     q.nvb = nvb;
-    const int smem = std::max(TC_SMEM, TC_SMEM_RING);
+    const int smem = TC_SMEM;
     KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     kb_matvec_tc<<<dim3(n32, nvb), 320, smem, st>>>(q, xmap);
     KR_CUDA(ctx, cudaGetLastError());
