@@ -46,7 +46,7 @@ struct kr_batch {
   double2* alpha = nullptr;  // [mmax + 1][nb]
   double* beta = nullptr;    // [mmax + 1][nb]
   double2* c = nullptr;      // [mmax + 1][nb] exp(fac T) e0 of the converged order
-  double* vscale = nullptr;  // [nb] 1 / beta_k of the newest basis vector
+  double* vscale = nullptr;  // [mmax + 1][nb] scale of each stored basis vector (V_j = vscale_j x stored)
   int* kconv = nullptr;      // [nb] converged Krylov order (0: still active)
   int* active = nullptr;     // [nb]
   int* grp_active = nullptr; // [nb / KB_MV_THREADS rounded up]
@@ -225,7 +225,7 @@ __global__ void kb_start(const float4* S, float2* V0, const double2* nsq, double
     norm0[v] = n0;
     active[v] = (v < nvec && n0 > 0.0) ? 1 : 0;
     kconv[v] = 0;
-    vscale[v] = 1.0;
+    vscale[v] = 1.0;  // V_0 is stored normalised
   }
   const dfl invd = df_from(inv);
   const Chunk ch = chunk_of(dim);
@@ -242,8 +242,8 @@ __global__ void kb_start(const float4* S, float2* V0, const double2* nsq, double
 // stays in cache from pass to pass, so DRAM sees W once (one pass over all V_j
 // with W read once measured 45 % slower at C3); per chunk and vector,
 // part[chunk][j][nb]
-__global__ void kb_dots(const float2* V, const float2* W, const int* active, long long dim, int nb, int k,
-                        int stride_coef, double2* part) {
+__global__ void kb_dots(const float2* V, const float2* W, const int* active, const double* vscale, long long dim,
+                        int nb, int k, int stride_coef, double2* part) {
   __shared__ double2 sh[8][32];
   const int v = blockIdx.y * 32 + threadIdx.x;
   const Chunk ch = chunk_of(dim);
@@ -261,14 +261,14 @@ __global__ void kb_dots(const float2* V, const float2* W, const int* active, lon
       }
     }
     const double2 t = warps_sum(make_double2(acc.x, acc.y), sh);
-    if (threadIdx.y == 0) part[((long long)blockIdx.x * stride_coef + j) * nb + v] = t;
+    if (threadIdx.y == 0) part[((long long)blockIdx.x * stride_coef + j) * nb + v] = cscale(t, vscale[(long long)j * nb + v]);
   }
 }
 
 // V_{k+1} = W - sum_j h_j V_j (unnormalised), partial ||V_{k+1}||^2; k < KM
 template <int KM>
-__global__ void kb_update(float2* V, const float2* W, const double2* h, const int* active, long long dim, int nb,
-                          int k, double2* part) {
+__global__ void kb_update(float2* V, const float2* W, const double2* h, const double* vscale, const int* active,
+                          long long dim, int nb, int k, double2* part) {
   __shared__ double2 sh[8][32];
   const int v = blockIdx.y * 32 + threadIdx.x;
   const Chunk ch = chunk_of(dim);
@@ -278,7 +278,7 @@ __global__ void kb_update(float2* V, const float2* W, const double2* h, const in
     float2 hv[KM];
 #pragma unroll
     for (int j = 0; j < KM; ++j) {
-      const double2 t = j <= k ? h[(long long)j * nb + v] : make_double2(0.0, 0.0);
+      const double2 t = j <= k ? cscale(h[(long long)j * nb + v], vscale[(long long)j * nb + v]) : make_double2(0.0, 0.0);
       hv[j] = make_float2((float)t.x, (float)t.y);
     }
     float2* Vn = V + (long long)(k + 1) * dim * nb;
@@ -353,22 +353,12 @@ __global__ void kb_small(BatchDev b, int k, double2 fac, double tol, const doubl
     b.active[v] = 0;
     if (last && !(e <= tol || bk == 0.0)) atomicAdd(b.counts + 1, 1);
   } else {
-    b.vscale[v] = 1.0 / bk;
+    b.vscale[(long long)(k + 1) * nb + v] = 1.0 / bk;  // V_{k+1} stays stored unnormalised
     atomicAdd(b.counts, 1);
   }
 }
 
 // V_{k+1} *= 1 / beta_k for the vectors still active
-__global__ void kb_scale(float2* Vn, const double* vscale, const int* active, long long dim, int nb) {
-  const int v = blockIdx.y * 32 + threadIdx.x;
-  if (!active[v]) return;
-  const float s = (float)vscale[v];
-  const Chunk ch = chunk_of(dim);
-  for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
-    float2 a = Vn[e * nb + v];
-    Vn[e * nb + v] = make_float2(a.x * s, a.y * s);
-  }
-}
 
 // S <- phase * (c_0 S + ||v|| sum_{i>=1} c_i V_i)   (double-float state; the
 // complex64 Krylov corrections summed in FP32)
@@ -382,7 +372,8 @@ __global__ void kb_combine(BatchDev b, const float4* phase) {
   float2 cf[KM];
 #pragma unroll
   for (int i = 1; i < KM; ++i)
-    cf[i] = i < K ? make_float2((float)b.c[(long long)i * nb + v].x, (float)b.c[(long long)i * nb + v].y)
+    cf[i] = i < K ? make_float2((float)(b.c[(long long)i * nb + v].x * b.vscale[(long long)i * nb + v]),
+                                (float)(b.c[(long long)i * nb + v].y * b.vscale[(long long)i * nb + v]))
                   : make_float2(0.f, 0.f);
   const dfc c0 = dfc_from(b.c[v]);
   const dfl n0 = df_from(b.norm0[v]);
@@ -516,7 +507,10 @@ int mv_groups(const kr_batch* b) { return b->nb / 32; }
 const char* const mv_error_text =
     "batched mat-vec: an MMA completion wait gave up or a term exceeded the tile shape";
 
-int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool masked, cudaStream_t st) {
+// Y = H X, each vector's output times yscale[v] when yscale is given (the
+// scale of a basis vector stored unnormalised)
+int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool masked, const double* yscale,
+                  cudaStream_t st) {
   if (b->mv_kind == KR_MATVEC_TENSOR && op->tc_ntask > 0) {
     BatchTC q;
     q.op = op->dev;
@@ -526,6 +520,7 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
     q.task = op->tc_task;
     q.ntask = op->tc_ntask;
     q.grp_active = masked ? b->grp_active : nullptr;
+    q.yscale = yscale;
     q.err = b->counts + 2;
     q.tfirst = 0;
     q.tend = op->tc_ntask;
@@ -546,6 +541,7 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
   p.task_i0 = b->task_i0;
   p.task_nr = b->task_nr;
   p.grp_active = masked ? b->grp_active : nullptr;
+  p.yscale = yscale;
   const int rc = kb_launch_simt(op->ctx, p, b->ntask, mv_groups(b), st);
   if (rc == KR_OK) b->launches++;
   return rc;
@@ -588,7 +584,7 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
   BA(m1 * nb, &b->alpha);
   BA(m1 * nb, &b->beta);
   BA(m1 * nb, &b->c);
-  BA(nb, &b->vscale);
+  BA(m1 * nb, &b->vscale);
   BA(nb, &b->kconv);
   BA(nb, &b->active);
   BA((size_t)mv_groups(b), &b->grp_active);
@@ -679,20 +675,19 @@ extern "C" int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double f
   int kused = 0;
   for (int k = 0; k < b->mmax; ++k) {
     kb_group_active<<<(mv_groups(b) + 7) / 8, dim3(32, 8), 0, st>>>(b->active, b->grp_active, mv_groups(b));
-    int rc = launch_matvec(b, op, b->V + (long long)k * dim * nb, b->W, true, st);
+    int rc = launch_matvec(b, op, b->V + (long long)k * dim * nb, b->W, true, b->vscale + (long long)k * nb, st);
     if (rc) return rc;
-    kb_dots<<<eg, eb, 0, st>>>(b->V, b->W, b->active, dim, nb, k, stride, b->part);
+    kb_dots<<<eg, eb, 0, st>>>(b->V, b->W, b->active, b->vscale, dim, nb, k, stride, b->part);
     kb_reduce<<<((k + 1) * nb + 255) / 256, 256, 0, st>>>(b->part, k + 1, nb, stride, b->h);
-    if (k < 4) kb_update<4><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->active, dim, nb, k, b->part);
-    else if (k < 8) kb_update<8><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->active, dim, nb, k, b->part);
-    else if (k < 16) kb_update<16><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->active, dim, nb, k, b->part);
-    else kb_update<32><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->active, dim, nb, k, b->part);
+    if (k < 4) kb_update<4><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->vscale, b->active, dim, nb, k, b->part);
+    else if (k < 8) kb_update<8><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->vscale, b->active, dim, nb, k, b->part);
+    else if (k < 16) kb_update<16><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->vscale, b->active, dim, nb, k, b->part);
+    else kb_update<32><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->vscale, b->active, dim, nb, k, b->part);
     // norms of V_{k+1} into the last coefficient slot of h (slot mmax + 1 is not a dot)
     kb_reduce<<<(nb + 255) / 256, 256, 0, st>>>(b->part, 1, nb, 1, b->h + (long long)(b->mmax) * nb);
     KR_CUDA(ctx, cudaMemsetAsync(b->counts, 0, 2 * sizeof(int), st));
     kb_small<<<(nb + 127) / 128, 128, 0, st>>>(dev_view(b), k, fac, tol, b->h + (long long)(b->mmax) * nb);
-    kb_scale<<<eg, eb, 0, st>>>(b->V + (long long)(k + 1) * dim * nb, b->vscale, b->active, dim, nb);
-    b->launches += 7;
+    b->launches += 6;
     KR_CUDA(ctx, cudaGetLastError());
     int counts[3] = {0, 0, 0};
     KR_CUDA(ctx, cudaMemcpyAsync(counts, b->counts, sizeof(counts), cudaMemcpyDeviceToHost, st));
@@ -733,7 +728,7 @@ extern "C" int kr_batch_expect(kr_batch* b, kr_op* obs, double* out, void* strea
   float2* X = b->V;  // basis slot 0 and W are free between steps
   KR_CUDA(obs->ctx, cudaMemsetAsync(b->counts + 2, 0, sizeof(int), st));
   kb_to_f32<<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, st>>>(b->S, X, n);
-  int rc = launch_matvec(b, obs, X, b->W, false, st);
+  int rc = launch_matvec(b, obs, X, b->W, false, nullptr, st);
   if (rc) return rc;
   const dim3 eg(KB_RED_CHUNKS, b->nb / 32), eb(32, 8);
   kb_expect_dots<<<eg, eb, 0, st>>>(b->S, b->W, b->dim, b->nb, b->part);
@@ -796,7 +791,7 @@ extern "C" int kr_batch_apply(kr_batch* b, kr_op* op, const void* x, void* y, vo
   const dim3 grid((unsigned)((b->dim + 31) / 32), b->nb / 32);
   KR_CUDA(op->ctx, cudaMemsetAsync(b->counts + 2, 0, sizeof(int), st));
   kb_transpose_in32<<<grid, dim3(32, 8), 0, st>>>((const double2*)x, b->V, b->dim, b->nvec, b->nb);
-  const int rc = launch_matvec(b, op, b->V, b->W, false, st);
+  const int rc = launch_matvec(b, op, b->V, b->W, false, nullptr, st);
   if (rc) return rc;
   kb_transpose_out32<<<grid, dim3(32, 8), 0, st>>>(b->W, (double2*)y, b->dim, b->nvec, b->nb);
   b->launches += 2;
@@ -834,7 +829,7 @@ extern "C" int kr_batch_set_matvec(kr_batch* b, int32_t kind) {
 extern "C" int kr_batch_matvec(kr_batch* b, kr_op* op, void* stream) {
   if (!b || !op || op->dev.dim_out != b->dim || !op->square)
     return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_matvec: operator does not match the batch basis");
-  return launch_matvec(b, op, b->V, b->W, false, (cudaStream_t)stream);
+  return launch_matvec(b, op, b->V, b->W, false, nullptr, (cudaStream_t)stream);
 }
 
 extern "C" int64_t kr_batch_launch_count(const kr_batch* b) { return b ? b->launches : -1; }

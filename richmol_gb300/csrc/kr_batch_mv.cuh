@@ -19,6 +19,7 @@ struct BatchMV {
   const int* task_i0;
   const int* task_nr;
   const int* grp_active;  // per 32-vector group: any vector active (null: all)
+  const double* yscale;   // per vector: output scale (null: 1)
 };
 
 // arguments of the tensor-core mat-vec kb_matvec_tc (kr_batch_tc.cu)
@@ -34,6 +35,7 @@ struct BatchTC {
   int nvb;                // vector blocks of 128
   int* work;              // persistent kernel: work-item counter (zero at launch)
   const int* grp_active;  // per 32-vector group: any vector active (null: all)
+  const double* yscale;   // per vector: output scale (null: 1)
   int* err;
 };
 

@@ -243,12 +243,13 @@ __device__ void kb_tile(const BatchMV& p, int s1, int i0, int nr, float* smem) {
     }
   }
   float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * ld1) * nb + v;
+  const float sc = p.yscale ? (float)p.yscale[v] : 1.f;
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
 #pragma unroll
     for (int aa = 0; aa < 4; ++aa) {
       const int i = r0 + r, a = a0 + aa;
-      if (i < nr && a < nk1) Y[((long long)i * ld1 + a) * nb] = y[r * 4 + aa];
+      if (i < nr && a < nk1) Y[((long long)i * ld1 + a) * nb] = make_float2(y[r * 4 + aa].x * sc, y[r * 4 + aa].y * sc);
     }
   }
 }

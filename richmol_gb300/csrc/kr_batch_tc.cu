@@ -471,6 +471,7 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
   // epilogue: rows r = w / 4, w / 4 + 2, ... of this warp's lane quarter
   int ld1;
   float2* Y = y_rows(ld1);
+  const float sc = p.yscale ? (float)p.yscale[v] : 1.f;
   for (int r = wid >> 2; r < nr; r += 2) {
     for (int c0 = 0; c0 < NP; c0 += 16) {
       float re[16], im[16];
@@ -481,7 +482,7 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
 #pragma unroll
       for (int q = 0; q < 16; ++q)
         if (c0 + q < nk1)
-          Y[((long long)r * ld1 + c0 + q) * nb] = any ? make_float2(re[q], im[q]) : make_float2(0.f, 0.f);
+          Y[((long long)r * ld1 + c0 + q) * nb] = any ? make_float2(re[q] * sc, im[q] * sc) : make_float2(0.f, 0.f);
     }
   }
   if (!ok && lane == 0) atomicExch(p.err, KR_ERR_TIMEOUT);
@@ -865,6 +866,7 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
       const int nk1 = __ldg(op.out_dk + s1);
       const int ld1 = __ldg(op.out_stride + s1);
       float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * ld1) * nb + v;
+      const float sc = p.yscale ? (float)p.yscale[v] : 1.f;
       const int NP = nk1 <= 16 ? 16 : 32;
       const bool merged = 4 * R * NP <= 512;
       const int bpart = merged ? NP * KP * 4 : Rg::BPART;
@@ -942,7 +944,7 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
 #pragma unroll
           for (int q = 0; q < 16; ++q)
             if (cc + q < nk1)
-              Y[((long long)r * ld1 + cc + q) * nb] = any ? make_float2(re[q], im[q]) : make_float2(0.f, 0.f);
+              Y[((long long)r * ld1 + cc + q) * nb] = any ? make_float2(re[q] * sc, im[q] * sc) : make_float2(0.f, 0.f);
         }
       }
       tc_fence_before();  // the TMEM reads above come before the next tile's MMAs
