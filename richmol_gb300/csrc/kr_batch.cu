@@ -187,8 +187,8 @@ __global__ void kb_phase_df(const double2* phase, float4* pdf, long long dim) {
     pdf[e] = dfc_st(dfc_from(phase[e]));
 }
 
-// S <- phase * S (optional); partial ||S_v||^2
-__global__ void kb_phase_norm(float4* S, const float4* phase, long long dim, int nb, double2* part) {
+// S <- phase * S (optional); V_0 = S in complex64 (unnormalised); partial ||S_v||^2
+__global__ void kb_phase_norm(float4* S, const float4* phase, float2* V0, long long dim, int nb, double2* part) {
   __shared__ double2 sh[8][32];
   const int v = blockIdx.y * 32 + threadIdx.x;
   const Chunk ch = chunk_of(dim);
@@ -199,6 +199,8 @@ __global__ void kb_phase_norm(float4* S, const float4* phase, long long dim, int
       s = dfc_mul(s, dfc_ld(__ldg(phase + e)));
       S[e * nb + v] = dfc_st(s);
     }
+    // the first basis vector, stored unnormalised (its scale 1 / ||S|| is set by kb_start)
+    V0[e * nb + v] = make_float2(__fadd_rn(s.re.hi, s.re.lo), __fadd_rn(s.im.hi, s.im.lo));
     acc = df_add(acc, df_add(df_mul(s.re, s.re), df_mul(s.im, s.im)));
   }
   const double2 t = warps_sum(make_double2(df_to(acc), 0.0), sh);
@@ -215,33 +217,23 @@ __global__ void kb_reduce(const double2* part, int ncoef, int nb, int stride_coe
   out[(long long)j * nb + v] = s;
 }
 
-// norm0 = ||S||, V0 = S / norm0 (complex64); resets the per-vector state
-__global__ void kb_start(const float4* S, float2* V0, const double2* nsq, double* norm0, int* active, int* kconv,
-                         double* vscale, long long dim, int nb, int nvec) {
-  const int v = blockIdx.y * 32 + threadIdx.x;
+// per vector: ||S||, active flag, the scale of V_0 (phase * S stored by kb_phase_norm)
+__global__ void kb_start(const double2* nsq, double* norm0, int* active, int* kconv, double* vscale, int nb,
+                         int nvec) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nb) return;
   const double n0 = sqrt(nsq[v].x);
-  const double inv = n0 > 0.0 ? 1.0 / n0 : 0.0;
-  if (blockIdx.x == 0 && threadIdx.y == 0) {
-    norm0[v] = n0;
-    active[v] = (v < nvec && n0 > 0.0) ? 1 : 0;
-    kconv[v] = 0;
-    vscale[v] = 1.0;  // V_0 is stored normalised
-  }
-  const dfl invd = df_from(inv);
-  const Chunk ch = chunk_of(dim);
-  for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
-    const dfc s = dfc_ld(S[e * nb + v]);
-    const dfl re = df_mul(s.re, invd), im = df_mul(s.im, invd);
-    V0[e * nb + v] = make_float2(__fadd_rn(re.hi, re.lo), __fadd_rn(im.hi, im.lo));
-  }
+  norm0[v] = n0;
+  active[v] = (v < nvec && n0 > 0.0) ? 1 : 0;
+  kconv[v] = 0;
+  vscale[v] = n0 > 0.0 ? 1.0 / n0 : 0.0;
 }
 
-// partial dots h_j = <V_j, W> for j = 0..k: FP32 products, FP32 sums inside a
-// thread's elements, FP64 across threads and chunks
-// vdot(V_j, W) for j = 0 .. k, one pass per j: the chunk of W a CTA reads
-// stays in cache from pass to pass, so DRAM sees W once (one pass over all V_j
-// with W read once measured 45 % slower at C3); per chunk and vector,
-// part[chunk][j][nb]
+// partial dots h_j = <V_j, W> for j = 0..k (V_j as stored, times its scale):
+// FP32 products, FP32 sums inside a thread's elements, FP64 across threads and
+// chunks; per chunk and vector, part[chunk][j][nb]. One pass per j: the chunk
+// of W a CTA reads stays in cache from pass to pass, so DRAM sees W once (one
+// pass over all V_j with W read once measured 45 % slower at C3).
 __global__ void kb_dots(const float2* V, const float2* W, const int* active, const double* vscale, long long dim,
                         int nb, int k, int stride_coef, double2* part) {
   __shared__ double2 sh[8][32];
@@ -303,12 +295,14 @@ __global__ void kb_update(float2* V, const float2* W, const double2* h, const do
 }
 
 // per vector: T update, exp(fac T) e0, error estimate, convergence
-__global__ void kb_small(BatchDev b, int k, double2 fac, double tol, const double2* nsq) {
+__global__ void kb_small(BatchDev b, int k, double2 fac, double tol, const double2* npart) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= b.nb || !b.active[v]) return;
   const int nb = b.nb;
   const double2 hk = b.h[(long long)k * nb + v];
-  const double bk = sqrt(nsq[v].x);
+  double2 nsq = make_double2(0.0, 0.0);  // ||V_{k+1}||^2 from the chunk partials, in chunk order
+  for (int c = 0; c < KB_RED_CHUNKS; ++c) nsq = cadd(nsq, npart[(long long)c * nb + v]);
+  const double bk = sqrt(nsq.x);
   b.alpha[(long long)k * nb + v] = hk;
   b.beta[(long long)k * nb + v] = bk;
   const int n = k + 1;
@@ -667,9 +661,9 @@ extern "C" int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double f
     b->launches++;
     pdf = b->phase_df;
   }
-  kb_phase_norm<<<eg, eb, 0, st>>>(b->S, pdf, dim, nb, b->part);
+  kb_phase_norm<<<eg, eb, 0, st>>>(b->S, pdf, b->V, dim, nb, b->part);
   kb_reduce<<<(nb + 255) / 256, 256, 0, st>>>(b->part, 1, nb, 1, b->h);
-  kb_start<<<eg, eb, 0, st>>>(b->S, b->V, b->h, b->norm0, b->active, b->kconv, b->vscale, dim, nb, b->nvec);
+  kb_start<<<(nb + 255) / 256, 256, 0, st>>>(b->h, b->norm0, b->active, b->kconv, b->vscale, nb, b->nvec);
   b->launches += 3;
   KR_CUDA(ctx, cudaGetLastError());
   int kused = 0;
@@ -683,11 +677,10 @@ extern "C" int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double f
     else if (k < 8) kb_update<8><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->vscale, b->active, dim, nb, k, b->part);
     else if (k < 16) kb_update<16><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->vscale, b->active, dim, nb, k, b->part);
     else kb_update<32><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->vscale, b->active, dim, nb, k, b->part);
-    // norms of V_{k+1} into the last coefficient slot of h (slot mmax + 1 is not a dot)
-    kb_reduce<<<(nb + 255) / 256, 256, 0, st>>>(b->part, 1, nb, 1, b->h + (long long)(b->mmax) * nb);
+    // kb_small sums the chunk partials of ||V_{k+1}||^2 itself (as kb_reduce would)
     KR_CUDA(ctx, cudaMemsetAsync(b->counts, 0, 2 * sizeof(int), st));
-    kb_small<<<(nb + 127) / 128, 128, 0, st>>>(dev_view(b), k, fac, tol, b->h + (long long)(b->mmax) * nb);
-    b->launches += 6;
+    kb_small<<<(nb + 127) / 128, 128, 0, st>>>(dev_view(b), k, fac, tol, b->part);
+    b->launches += 5;
     KR_CUDA(ctx, cudaGetLastError());
     int counts[3] = {0, 0, 0};
     KR_CUDA(ctx, cudaMemcpyAsync(counts, b->counts, sizeof(counts), cudaMemcpyDeviceToHost, st));
