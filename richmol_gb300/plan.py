@@ -16,6 +16,8 @@ and, per part, one MF instance for each group it uses. Terms are the
 import ctypes
 import hashlib
 
+from types import SimpleNamespace
+
 import numpy as np
 import torch
 from scipy.sparse import csr_matrix
@@ -165,6 +167,157 @@ def compiled(src):
     return c
 
 
+def build_tables(sources, basis_out, basis_in, split=None, blocks=None, source_block=None):
+    """Host tables of one operator (the kr_op_desc arrays) from its factor
+    sources; no device work. Returns a SimpleNamespace: ``arrays`` (name -> numpy
+    array, the descriptor fields), ``dim_out``, ``dim_in``, ``slab_parent``,
+    ``part_carts``, ``nblock``, ``split``, ``nterm`` and the counts ``nk``,
+    ``nm``, ``nmf``. Arguments as OperatorPlan."""
+    sources = list(sources)
+    split = int(split) if split else None
+    if blocks is None:
+        blocks = [(basis_out, basis_in)]
+        source_block = [0] * len(sources)
+    assert len(source_block) == len(sources)
+    nblock = len(blocks)
+    basis_out = [b for bo, _ in blocks for b in bo]
+    basis_in = [b for _, bi in blocks for b in bi]
+    slabs_out = [(k, J, s) for k, (bo, _) in enumerate(blocks) for J, s, _, _ in bo]
+    slabs_in = [(k, J, s) for k, (_, bi) in enumerate(blocks) for J, s, _, _ in bi]
+    sidx_out = {k: i for i, k in enumerate(slabs_out)}
+    sidx_in = {k: i for i, k in enumerate(slabs_in)}
+    out_dm = np.array([b[2] for b in basis_out], np.int32)
+    out_dk = np.array([b[3] for b in basis_out], np.int32)
+    in_dm = np.array([b[2] for b in basis_in], np.int32)
+    in_dk = np.array([b[3] for b in basis_in], np.int32)
+    out_off = np.concatenate([[0], np.cumsum(out_dm.astype(np.int64) * out_dk)[:-1]]).astype(np.int64)
+    in_off = np.concatenate([[0], np.cumsum(in_dm.astype(np.int64) * in_dk)[:-1]]).astype(np.int64)
+    dim_out = int((out_dm.astype(np.int64) * out_dk).sum())
+    dim_in = int((in_dm.astype(np.int64) * in_dk).sum())
+    if split:
+        ch_out = _chunks(out_dm, out_dk, out_off, split)
+        ch_in = _chunks(in_dm, in_dk, in_off, split)
+        vout = [[] for _ in range(len(out_dm))]
+        vin = [[] for _ in range(len(in_dm))]
+        for v, c in enumerate(ch_out):
+            vout[c[0]].append(v)
+        for v, c in enumerate(ch_in):
+            vin[c[0]].append(v)
+        slab_parent = [c[0] for c in ch_out]
+    else:
+        slab_parent = list(range(len(out_dm)))
+
+    k_off, k_rows, k_cols, k_type, k_data = [], [], [], [], []
+    m_rows, m_width, m_ncart, m_col_off, m_val_off, m_col, m_val = [], [], [], [], [], [], []
+    mf_group, mf_part = [], []
+    t_out, t_in, t_k, t_mf = [], [], [], []
+    koff = 0
+    coff = 0
+    voff = 0
+    src_base = {}
+    full_k, sub_k = [], {}
+
+    def add_k(kt, kd, r, c, koff):
+        if kt == _native.KR_K_COMPLEX and koff % 2:
+            k_data.append(np.zeros(1))
+            koff += 1
+        k_off.append(koff)
+        k_rows.append(r)
+        k_cols.append(c)
+        k_type.append(kt)
+        flat = np.ascontiguousarray(kd, dtype=np.float64).reshape(-1)
+        k_data.append(flat)
+        return koff + flat.size
+
+    part_carts = []
+    for p, src in enumerate(sources):
+        cs = compiled(src)
+        part_carts.append(cs.carts)
+        if id(src) not in src_base:
+            kb0, g0 = (len(full_k) if split else len(k_type)), len(m_rows)
+            for (kt, kd), (r, c) in zip(cs.kblocks, cs.kshape):
+                if split:
+                    full_k.append((kt, kd, (r, c)))
+                else:
+                    koff = add_k(kt, kd, r, c, koff)
+            for rows, width, ncart, col, val in cs.groups:
+                m_rows.append(rows)
+                m_width.append(width)
+                m_ncart.append(ncart)
+                m_col_off.append(coff)
+                m_val_off.append(voff)
+                m_col.append(col)
+                m_val.append(val.reshape(-1))
+                coff += col.size
+                voff += val.size
+            src_base[id(src)] = (kb0, g0)
+        kb0, g0 = src_base[id(src)]
+        inst = {}
+        for J1, s1, J2, s2, kidx, gidx in cs.terms:
+            blk = source_block[p]
+            if (blk, J1, s1) not in sidx_out or (blk, J2, s2) not in sidx_in:
+                continue
+            g = g0 + gidx
+            if g not in inst:
+                inst[g] = len(mf_group)
+                mf_group.append(g)
+                mf_part.append(p)
+            so, si = sidx_out[(blk, J1, s1)], sidx_in[(blk, J2, s2)]
+            if not split:
+                t_out.append(so)
+                t_in.append(si)
+                t_k.append(kb0 + kidx)
+                t_mf.append(inst[g])
+                continue
+            for vo in vout[so]:
+                for vi in vin[si]:
+                    key = (kb0 + kidx, ch_out[vo][1], ch_in[vi][1])
+                    kb = sub_k.get(key, -2)
+                    if kb == -2:
+                        kt, kd, shp = full_k[kb0 + kidx]
+                        a0, w1, b0_, w2 = ch_out[vo][1], ch_out[vo][2], ch_in[vi][1], ch_in[vi][2]
+                        sub = _kdense(kt, kd, shp)[a0:a0 + w1, b0_:b0_ + w2]
+                        kb = -1
+                        if np.any(sub):
+                            skt, skd = _ktype(np.ascontiguousarray(sub))
+                            kb = len(k_type)
+                            koff = add_k(skt, skd, w1, w2, koff)
+                        sub_k[key] = kb
+                    if kb < 0:
+                        continue  # a zero K sub-block: no term
+                    t_out.append(vo)
+                    t_in.append(vi)
+                    t_k.append(kb)
+                    t_mf.append(inst[g])
+
+    A = lambda x, dt: np.ascontiguousarray(np.array(x, dtype=dt).reshape(-1))
+    cat = lambda xs, dt: np.ascontiguousarray(np.concatenate(xs).astype(dt)) if xs else np.zeros(1, dt)
+    if split:
+        out_dm = np.array([c[3] for c in ch_out], np.int32)
+        out_dk = np.array([c[2] for c in ch_out], np.int32)
+        out_off = np.array([c[4] for c in ch_out], np.int64)
+        out_st = np.array([c[5] for c in ch_out], np.int32)
+        in_dm = np.array([c[3] for c in ch_in], np.int32)
+        in_dk = np.array([c[2] for c in ch_in], np.int32)
+        in_off = np.array([c[4] for c in ch_in], np.int64)
+        in_st = np.array([c[5] for c in ch_in], np.int32)
+    keep = dict(
+        out_dm=out_dm, out_dk=out_dk, out_off=out_off, in_dm=in_dm, in_dk=in_dk, in_off=in_off,
+        k_off=A(k_off, np.int64), k_rows=A(k_rows, np.int32), k_cols=A(k_cols, np.int32),
+        k_type=A(k_type, np.int32), k_data=cat(k_data, np.float64),
+        m_rows=A(m_rows, np.int32), m_width=A(m_width, np.int32), m_ncart=A(m_ncart, np.int32),
+        m_col_off=A(m_col_off, np.int64), m_val_off=A(m_val_off, np.int64),
+        m_col=cat(m_col, np.int32), m_val=cat(m_val, np.complex128).view(np.float64),
+        mf_group=A(mf_group, np.int32), mf_part=A(mf_part, np.int32),
+        t_out=A(t_out, np.int32), t_in=A(t_in, np.int32), t_k=A(t_k, np.int32), t_mf=A(t_mf, np.int32),
+    )
+    if split:
+        keep["out_stride"], keep["in_stride"] = out_st, in_st
+    return SimpleNamespace(arrays=keep, dim_out=dim_out, dim_in=dim_in, slab_parent=slab_parent,
+                           part_carts=part_carts, nblock=nblock, split=split, nterm=len(t_out),
+                           nk=len(k_type), nm=len(m_rows), nmf=len(mf_group))
+
+
 class OperatorPlan:
     """One kr_op: the device tables for a tuple of factor sources."""
 
@@ -184,163 +337,31 @@ class OperatorPlan:
         self.ctx = context(device)
         self.sources = list(sources)
         L = _native.lib()
-        if blocks is None:
-            blocks = [(basis_out, basis_in)]
-            source_block = [0] * len(self.sources)
-        assert len(source_block) == len(self.sources)
-        self.nblock = len(blocks)
-        basis_out = [b for bo, _ in blocks for b in bo]
-        basis_in = [b for _, bi in blocks for b in bi]
-        slabs_out = [(k, J, s) for k, (bo, _) in enumerate(blocks) for J, s, _, _ in bo]
-        slabs_in = [(k, J, s) for k, (_, bi) in enumerate(blocks) for J, s, _, _ in bi]
-        sidx_out = {k: i for i, k in enumerate(slabs_out)}
-        sidx_in = {k: i for i, k in enumerate(slabs_in)}
-        out_dm = np.array([b[2] for b in basis_out], np.int32)
-        out_dk = np.array([b[3] for b in basis_out], np.int32)
-        in_dm = np.array([b[2] for b in basis_in], np.int32)
-        in_dk = np.array([b[3] for b in basis_in], np.int32)
-        out_off = np.concatenate([[0], np.cumsum(out_dm.astype(np.int64) * out_dk)[:-1]]).astype(np.int64)
-        in_off = np.concatenate([[0], np.cumsum(in_dm.astype(np.int64) * in_dk)[:-1]]).astype(np.int64)
-        self.dim_out = int((out_dm.astype(np.int64) * out_dk).sum())
-        self.dim_in = int((in_dm.astype(np.int64) * in_dk).sum())
-        self.split = int(split) if split else None
-        if self.split:
-            ch_out = _chunks(out_dm, out_dk, out_off, self.split)
-            ch_in = _chunks(in_dm, in_dk, in_off, self.split)
-            vout = [[] for _ in range(len(out_dm))]
-            vin = [[] for _ in range(len(in_dm))]
-            for v, c in enumerate(ch_out):
-                vout[c[0]].append(v)
-            for v, c in enumerate(ch_in):
-                vin[c[0]].append(v)
-            self.slab_parent = [c[0] for c in ch_out]
-        else:
-            self.slab_parent = list(range(len(out_dm)))
-
-        k_off, k_rows, k_cols, k_type, k_data = [], [], [], [], []
-        m_rows, m_width, m_ncart, m_col_off, m_val_off, m_col, m_val = [], [], [], [], [], [], []
-        mf_group, mf_part = [], []
-        t_out, t_in, t_k, t_mf = [], [], [], []
-        koff = 0
-        coff = 0
-        voff = 0
-        src_base = {}
-        full_k, sub_k = [], {}
-
-        def add_k(kt, kd, r, c, koff):
-            if kt == _native.KR_K_COMPLEX and koff % 2:
-                k_data.append(np.zeros(1))
-                koff += 1
-            k_off.append(koff)
-            k_rows.append(r)
-            k_cols.append(c)
-            k_type.append(kt)
-            flat = np.ascontiguousarray(kd, dtype=np.float64).reshape(-1)
-            k_data.append(flat)
-            return koff + flat.size
-
-        self.part_carts = []
-        for p, src in enumerate(self.sources):
-            cs = compiled(src)
-            self.part_carts.append(cs.carts)
-            if id(src) not in src_base:
-                kb0, g0 = (len(full_k) if self.split else len(k_type)), len(m_rows)
-                for (kt, kd), (r, c) in zip(cs.kblocks, cs.kshape):
-                    if self.split:
-                        full_k.append((kt, kd, (r, c)))
-                    else:
-                        koff = add_k(kt, kd, r, c, koff)
-                for rows, width, ncart, col, val in cs.groups:
-                    m_rows.append(rows)
-                    m_width.append(width)
-                    m_ncart.append(ncart)
-                    m_col_off.append(coff)
-                    m_val_off.append(voff)
-                    m_col.append(col)
-                    m_val.append(val.reshape(-1))
-                    coff += col.size
-                    voff += val.size
-                src_base[id(src)] = (kb0, g0)
-            kb0, g0 = src_base[id(src)]
-            inst = {}
-            for J1, s1, J2, s2, kidx, gidx in cs.terms:
-                blk = source_block[p]
-                if (blk, J1, s1) not in sidx_out or (blk, J2, s2) not in sidx_in:
-                    continue
-                g = g0 + gidx
-                if g not in inst:
-                    inst[g] = len(mf_group)
-                    mf_group.append(g)
-                    mf_part.append(p)
-                so, si = sidx_out[(blk, J1, s1)], sidx_in[(blk, J2, s2)]
-                if not self.split:
-                    t_out.append(so)
-                    t_in.append(si)
-                    t_k.append(kb0 + kidx)
-                    t_mf.append(inst[g])
-                    continue
-                for vo in vout[so]:
-                    for vi in vin[si]:
-                        key = (kb0 + kidx, ch_out[vo][1], ch_in[vi][1])
-                        kb = sub_k.get(key, -2)
-                        if kb == -2:
-                            kt, kd, shp = full_k[kb0 + kidx]
-                            a0, w1, b0_, w2 = ch_out[vo][1], ch_out[vo][2], ch_in[vi][1], ch_in[vi][2]
-                            sub = _kdense(kt, kd, shp)[a0:a0 + w1, b0_:b0_ + w2]
-                            kb = -1
-                            if np.any(sub):
-                                skt, skd = _ktype(np.ascontiguousarray(sub))
-                                kb = len(k_type)
-                                koff = add_k(skt, skd, w1, w2, koff)
-                            sub_k[key] = kb
-                        if kb < 0:
-                            continue  # a zero K sub-block: no term
-                        t_out.append(vo)
-                        t_in.append(vi)
-                        t_k.append(kb)
-                        t_mf.append(inst[g])
-
-        A = lambda x, dt: np.ascontiguousarray(np.array(x, dtype=dt).reshape(-1))
-        cat = lambda xs, dt: np.ascontiguousarray(np.concatenate(xs).astype(dt)) if xs else np.zeros(1, dt)
-        if self.split:
-            out_dm = np.array([c[3] for c in ch_out], np.int32)
-            out_dk = np.array([c[2] for c in ch_out], np.int32)
-            out_off = np.array([c[4] for c in ch_out], np.int64)
-            out_st = np.array([c[5] for c in ch_out], np.int32)
-            in_dm = np.array([c[3] for c in ch_in], np.int32)
-            in_dk = np.array([c[2] for c in ch_in], np.int32)
-            in_off = np.array([c[4] for c in ch_in], np.int64)
-            in_st = np.array([c[5] for c in ch_in], np.int32)
-        keep = dict(
-            out_dm=out_dm, out_dk=out_dk, out_off=out_off, in_dm=in_dm, in_dk=in_dk, in_off=in_off,
-            k_off=A(k_off, np.int64), k_rows=A(k_rows, np.int32), k_cols=A(k_cols, np.int32),
-            k_type=A(k_type, np.int32), k_data=cat(k_data, np.float64),
-            m_rows=A(m_rows, np.int32), m_width=A(m_width, np.int32), m_ncart=A(m_ncart, np.int32),
-            m_col_off=A(m_col_off, np.int64), m_val_off=A(m_val_off, np.int64),
-            m_col=cat(m_col, np.int32), m_val=cat(m_val, np.complex128).view(np.float64),
-            mf_group=A(mf_group, np.int32), mf_part=A(mf_part, np.int32),
-            t_out=A(t_out, np.int32), t_in=A(t_in, np.int32), t_k=A(t_k, np.int32), t_mf=A(t_mf, np.int32),
-        )
+        T = build_tables(self.sources, basis_out, basis_in, split, blocks, source_block)
+        self.tables = T
+        self.nblock, self.dim_out, self.dim_in = T.nblock, T.dim_out, T.dim_in
+        self.split, self.slab_parent, self.part_carts = T.split, T.slab_parent, T.part_carts
+        keep = T.arrays
+        out_dm, in_dm = keep["out_dm"], keep["in_dm"]
         d = _native.kr_op_desc()
         d.nslab_out, d.nslab_in = len(out_dm), len(in_dm)
         if self.split:
-            keep["out_st"], keep["in_st"] = out_st, in_st
-            d.out_stride, d.in_stride = out_st.ctypes.data, in_st.ctypes.data
+            d.out_stride, d.in_stride = keep["out_stride"].ctypes.data, keep["in_stride"].ctypes.data
         for f in ("out_dm", "out_dk", "out_off", "in_dm", "in_dk", "in_off", "k_off", "k_rows", "k_cols",
                   "k_type", "k_data", "m_rows", "m_width", "m_ncart", "m_col_off", "m_val_off", "m_col",
                   "m_val", "mf_group", "mf_part", "t_out", "t_in", "t_k", "t_mf"):
             setattr(d, f, keep[f].ctypes.data)
         d.dim_out, d.dim_in = self.dim_out, self.dim_in
-        d.nk = len(k_type)
-        d.k_data_len = keep["k_data"].size if k_data else 0
-        d.nm = len(m_rows)
-        d.m_col_len = keep["m_col"].size if m_col else 0
-        d.m_val_len = keep["m_val"].size if m_val else 0
+        d.nk = T.nk
+        d.k_data_len = keep["k_data"].size if T.nk else 0
+        d.nm = T.nm
+        d.m_col_len = keep["m_col"].size if T.nm else 0
+        d.m_val_len = keep["m_val"].size if T.nm else 0
         d.npart = len(self.sources)
-        d.nmf = len(mf_group)
-        d.nterm = len(t_out)
+        d.nmf = T.nmf
+        d.nterm = T.nterm
         d.maxorder = int(maxorder)
-        self.nterm = len(t_out)
+        self.nterm = T.nterm
         self.maxorder = int(maxorder)
         h = ctypes.c_void_p()
         _native.check(L.kr_op_create(self.ctx, ctypes.byref(d), ctypes.byref(h)), self.ctx)
