@@ -127,6 +127,18 @@ int kr_expv(kr_op* op, void* x, const void* phase, double t, int32_t m, double t
  * the reference uses scipy's randomised onenormest on H.tomat(), tdse.py:387). */
 int kr_op_norm1(kr_op* op, double* norm, void* stream);
 
+/* Expectation values of an observable for FP64 states: out[i] = <v_i|O|v_i>
+ * (host complex128[nvec], interleaved) for the rows v_i of states (device,
+ * (nvec, dim) complex128), O = obs with its field set (e.g. cos^2 theta - 1/3
+ * with field [0, 0, 1]); FP64 mat-vec and fixed-order FP64 sums, so the values
+ * are reproducible bit for bit. If wsum != NULL, *wsum = sum_i w_i Re out[i]
+ * with w = weights (host double[nvec]; NULL: all 1), the Boltzmann-weighted
+ * ensemble value. Replaces the observable evaluation of the reference's
+ * callers (examples/ocs_alignment.py:70,99-100: v^H (cos^2 theta) v per vector
+ * through CarTens.tomat; tests/test_tdse.py:63-67). Synchronises the stream. */
+int kr_observables(kr_op* obs, const void* states, int64_t nvec, const double* weights,
+                   double* out, double* wsum, void* stream);
+
 /* Segments of a square operator: independent problems (molecules) whose
  * vectors lie one after the other (a block-diagonal operator, e.g. several
  * molecules' slabs in one table). slab_seg[s] is the segment of output slab s:
@@ -164,6 +176,22 @@ void kr_op_destroy(kr_op* op);
  * thresh: npart doubles (<= 0: no element threshold). Host pointers. */
 int kr_set_field(kr_op* op, const double* coef, const double* scale,
                  const double* thresh, void* stream);
+
+/* Field schedule: the coefficients of nsteps time steps uploaded at once, for
+ * loops whose field is known ahead (the pulse of examples/ocs_alignment.py:
+ * 70-100 evaluated on the time grid). coef: nsteps x npart x KR_MAXCART
+ * complex, scale: nsteps x npart complex, thresh: nsteps x npart doubles,
+ * step-major, each step laid out as for kr_set_field. Host pointers; the call
+ * returns once the copy is complete. Replaces a previous schedule (waiting for
+ * the device first) and frees its memory: a CUDA graph that recorded
+ * kr_set_field_step of the old schedule must not be replayed afterwards. */
+int kr_set_field_schedule(kr_op* op, int32_t nsteps, const double* coef,
+                          const double* scale, const double* thresh,
+                          void* stream);
+/* kr_set_field with the coefficients of step `step` of the schedule: no host
+ * data travels, so it can be recorded into a CUDA graph for any part count.
+ * KR_ERR_ARG if there is no schedule or step is outside [0, nsteps). */
+int kr_set_field_step(kr_op* op, int32_t step, void* stream);
 
 /* y = H x for nvec vectors (field.py:1145-1245). x: (nvec, dim_in),
  * y: (nvec, dim_out), device pointers, complex128. */

@@ -34,12 +34,13 @@ FIELD_COEF_BYTES = 8 + KR_PART_INLINE * KR_MAXCART * 16 + KR_PART_INLINE * 16 + 
 
 EXPORTED = [
     "kr_ctx_create", "kr_ctx_destroy", "kr_last_error", "kr_op_create", "kr_op_destroy",
-    "kr_set_field", "kr_matvec", "kr_step", "kr_sync_status", "kr_op_launch_count", "kr_op_work",
+    "kr_set_field", "kr_set_field_schedule", "kr_set_field_step",
+    "kr_matvec", "kr_step", "kr_sync_status", "kr_op_launch_count", "kr_op_work",
     "kr_probe_fp64", "kr_probe_fp32", "kr_probe_mma", "kr_step_static", "kr_static_scratch_bytes",
     "kr_batch_create", "kr_batch_destroy", "kr_batch_load", "kr_batch_store", "kr_batch_step",
     "kr_batch_korder", "kr_batch_expect", "kr_batch_launch_count", "kr_batch_matvec", "kr_batch_apply", "kr_batch_set_matvec",
     "kr_batch_populations",
-    "kr_expv", "kr_op_norm1",
+    "kr_expv", "kr_op_norm1", "kr_observables",
     "kr_seg_create", "kr_seg_destroy", "kr_seg_step", "kr_seg_launch_count",
 ]
 
@@ -129,6 +130,10 @@ def lib():
         L.kr_op_destroy.restype = None
         L.kr_set_field.argtypes = [vp, vp, vp, vp, vp]
         L.kr_set_field.restype = ctypes.c_int
+        L.kr_set_field_schedule.argtypes = [vp, i32, vp, vp, vp, vp]
+        L.kr_set_field_schedule.restype = ctypes.c_int
+        L.kr_set_field_step.argtypes = [vp, i32, vp]
+        L.kr_set_field_step.restype = ctypes.c_int
         L.kr_matvec.argtypes = [vp, vp, vp, i64, vp]
         L.kr_matvec.restype = ctypes.c_int
         L.kr_step.argtypes = [vp, vp, i64, vp, dbl, dbl, dbl, ctypes.c_uint32, vp, vp]
@@ -181,6 +186,8 @@ def lib():
         L.kr_expv.restype = ctypes.c_int
         L.kr_op_norm1.argtypes = [vp, ctypes.POINTER(dbl), vp]
         L.kr_op_norm1.restype = ctypes.c_int
+        L.kr_observables.argtypes = [vp, vp, i64, vp, vp, ctypes.POINTER(dbl), vp]
+        L.kr_observables.restype = ctypes.c_int
         L.kr_probe_mma.argtypes = [vp, vp, vp, vp]
         L.kr_probe_mma.restype = ctypes.c_int
         L.kr_probe_fp64.argtypes = [vp, ctypes.POINTER(dbl)]

@@ -257,8 +257,9 @@ struct Kx {
   int grid;
 };
 
-int kx_workspace(kr_op* op, long long n, int m, Kx& k) {
-  const size_t need = sizeof(double2) * ((size_t)(m + 2) * n + KX_BLOCKS + 1) + sizeof(long long) * (KX_BLOCKS + 1);
+// grows the operator's workspace of kr_expv / kr_op_norm1 / kr_observables
+// (each of them synchronises its stream before it returns)
+int kx_grow(kr_op* op, size_t need) {
   if (op->expv_bytes < need) {
     void* q = nullptr;
     cudaError_t e = cudaMalloc(&q, need);
@@ -267,6 +268,13 @@ int kx_workspace(kr_op* op, long long n, int m, Kx& k) {
     op->expv_ws = q;
     op->expv_bytes = need;
   }
+  return KR_OK;
+}
+
+int kx_workspace(kr_op* op, long long n, int m, Kx& k) {
+  const size_t need = sizeof(double2) * ((size_t)(m + 2) * n + KX_BLOCKS + 1) + sizeof(long long) * (KX_BLOCKS + 1);
+  const int rc = kx_grow(op, need);
+  if (rc != KR_OK) return rc;
   char* b = static_cast<char*>(op->expv_ws);
   k.V = reinterpret_cast<double2*>(b);
   k.P = k.V + (size_t)(m + 1) * n;
@@ -359,6 +367,46 @@ extern "C" int kr_op_norm1(kr_op* op, double* norm, void* stream) {
   est = std::max(est, 2.0 * r.x / (3.0 * (double)n));
   *norm = est;
   KR_CUDA(op->ctx, cudaGetLastError());
+  return KR_OK;
+}
+
+extern "C" int kr_observables(kr_op* obs, const void* states, int64_t nvec, const double* weights, double* out,
+                              double* wsum, void* stream) {
+  if (!obs || (!states && nvec > 0) || nvec < 0 || (!out && nvec > 0))
+    return set_err(obs ? obs->ctx : nullptr, KR_ERR_ARG, "kr_observables: bad argument");
+  if (!obs->square) return set_err(obs->ctx, KR_ERR_ARG, "kr_observables: operator is not square");
+  if (obs->split) return set_err(obs->ctx, KR_ERR_UNSUPPORTED, "kr_observables: operator with column chunks");
+  const long long n = obs->dev.dim_out;
+  cudaStream_t st = (cudaStream_t)stream;
+  // vectors in chunks whose products O v fit 256 MiB: [chunk][n] products,
+  // per-block partials, one result per vector
+  const long long chunk = std::max(1LL, std::min<long long>(nvec, (256LL << 20) / (16LL * std::max(1LL, n))));
+  const size_t need = sizeof(double2) * ((size_t)chunk * n + KX_BLOCKS + (size_t)nvec) +
+                      sizeof(long long) * (KX_BLOCKS + (size_t)nvec);
+  KX_TRY(kx_grow(obs, need));
+  double2* y = static_cast<double2*>(obs->expv_ws);
+  double2* part = y + (size_t)chunk * n;
+  double2* res = part + KX_BLOCKS;
+  long long* ipart = reinterpret_cast<long long*>(res + nvec);
+  long long* ires = ipart + KX_BLOCKS;
+  const double2* S = static_cast<const double2*>(states);
+  for (long long v0 = 0; v0 < nvec; v0 += chunk) {
+    const long long c = std::min(chunk, nvec - v0);
+    KX_TRY(kr_matvec(obs, S + v0 * n, y, c, st));
+    for (long long i = 0; i < c; ++i) {  // <v|O v> = conj(v) . (O v), fixed summation order
+      kx_reduce<<<KX_BLOCKS, KX_THREADS, 0, st>>>(KX_DOT, S + (v0 + i) * n, y + i * n, n, part, ipart);
+      kx_final<<<1, 32, 0, st>>>(KX_DOT, part, ipart, KX_BLOCKS, res + v0 + i, ires + v0 + i);
+    }
+    obs->launches += 2 * c;
+    KR_CUDA(obs->ctx, cudaGetLastError());
+  }
+  if (nvec > 0) KR_CUDA(obs->ctx, cudaMemcpyAsync(out, res, sizeof(double2) * nvec, cudaMemcpyDeviceToHost, st));
+  KR_CUDA(obs->ctx, cudaStreamSynchronize(st));
+  if (wsum) {
+    double s = 0.0;
+    for (long long i = 0; i < nvec; ++i) s += (weights ? weights[i] : 1.0) * out[2 * i];
+    *wsum = s;
+  }
   return KR_OK;
 }
 

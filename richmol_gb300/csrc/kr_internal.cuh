@@ -80,6 +80,12 @@ struct kr_op {
   double2* fc_scale = nullptr;
   double* fc_thresh = nullptr;
   std::vector<double> fc_host;  // staging: coef, scale, thresh
+  // field schedule (kr_set_field_schedule): [nsteps][npart][KR_MAXCART], [nsteps][npart] x2
+  void* fs_buf = nullptr;
+  int fs_nsteps = 0;
+  double2* fs_coef = nullptr;
+  double2* fs_scale = nullptr;
+  double* fs_thresh = nullptr;
   // tiles of the tensor-core batched mat-vec: [4][tc_ntask] = slab, first row, rows, KP
   int tc_ntask = 0;
   int* tc_task = nullptr;

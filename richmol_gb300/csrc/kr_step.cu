@@ -783,6 +783,7 @@ extern "C" void kr_op_destroy(kr_op* op) {
   if (!op) return;
   for (void* p : op->allocs) cudaFree(p);
   if (op->expv_ws) cudaFree(op->expv_ws);
+  if (op->fs_buf) cudaFree(op->fs_buf);
   delete op;
 }
 
@@ -1280,14 +1281,25 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   return KR_OK;
 }
 
-extern "C" int kr_set_field(kr_op* op, const double* coef, const double* scale, const double* thresh, void* stream) {
-  if (!op || !coef || !scale || !thresh) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_set_field: NULL argument");
-  if (op->field.nent == 0 && op->field.nmf == 0) return KR_OK;
-  cudaStream_t st = (cudaStream_t)stream;
+namespace {
+// the field launch of one step: band bounds reset, then MF = field products
+template <class Coef>
+int launch_field(kr_op* op, const Coef& c, cudaStream_t st) {
   KR_CUDA(op->ctx, cudaMemsetAsync(op->field.mf_band, 0xFF, sizeof(int) * 2 * std::max(1, op->field.nmf), st));
   const int threads = 256;
   const long long work = std::max<long long>(op->field.nent, op->field.nmf);
   const int blocks = (int)std::max<long long>(1, std::min<long long>((work + threads - 1) / threads, 4LL * op->ctx->nsm));
+  kr_field_kernel<<<blocks, threads, 0, st>>>(op->field, c);
+  op->launches++;
+  KR_CUDA(op->ctx, cudaGetLastError());
+  return KR_OK;
+}
+}  // namespace
+
+extern "C" int kr_set_field(kr_op* op, const double* coef, const double* scale, const double* thresh, void* stream) {
+  if (!op || !coef || !scale || !thresh) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_set_field: NULL argument");
+  if (op->field.nent == 0 && op->field.nmf == 0) return KR_OK;
+  cudaStream_t st = (cudaStream_t)stream;
   if (op->npart <= KR_PART_INLINE) {
     FieldCoef c;
     std::memset(&c, 0, sizeof(c));
@@ -1298,7 +1310,7 @@ extern "C" int kr_set_field(kr_op* op, const double* coef, const double* scale, 
       c.scale[p] = make_double2(scale[2 * p], scale[2 * p + 1]);
       c.thresh[p] = thresh[p];
     }
-    kr_field_kernel<<<blocks, threads, 0, st>>>(op->field, c);
+    return launch_field(op, c, st);
   } else {
     // stage coef [npart][9] complex, scale [npart] complex, thresh [npart] into
     // one host block, then one copy to the operator's device buffers (the
@@ -1312,11 +1324,46 @@ extern "C" int kr_set_field(kr_op* op, const double* coef, const double* scale, 
     KR_CUDA(op->ctx, cudaMemcpyAsync(op->fc_coef, op->fc_host.data(), sizeof(double) * op->fc_host.size(),
                                      cudaMemcpyHostToDevice, st));
     FieldCoefDev c{op->fc_coef, op->fc_scale, op->fc_thresh};
-    kr_field_kernel<<<blocks, threads, 0, st>>>(op->field, c);
+    return launch_field(op, c, st);
   }
-  op->launches++;
-  KR_CUDA(op->ctx, cudaGetLastError());
+}
+
+extern "C" int kr_set_field_schedule(kr_op* op, int32_t nsteps, const double* coef, const double* scale,
+                                     const double* thresh, void* stream) {
+  if (!op || nsteps <= 0 || !coef || !scale || !thresh)
+    return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_set_field_schedule: bad argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (op->fs_buf) {  // the old schedule may still be read by queued field launches
+    KR_CUDA(op->ctx, cudaDeviceSynchronize());
+    KR_CUDA(op->ctx, cudaFree(op->fs_buf));
+    op->fs_buf = nullptr;
+    op->fs_nsteps = 0;
+  }
+  const size_t np = (size_t)op->npart, ns = (size_t)nsteps * np;
+  if (ns > 0) {
+    const size_t bc = sizeof(double2) * ns * KR_MAXCART, bs = sizeof(double2) * ns, bt = sizeof(double) * ns;
+    KR_CUDA(op->ctx, cudaMalloc(&op->fs_buf, bc + bs + bt));
+    op->fs_coef = reinterpret_cast<double2*>(op->fs_buf);
+    op->fs_scale = op->fs_coef + ns * KR_MAXCART;
+    op->fs_thresh = reinterpret_cast<double*>(op->fs_scale + ns);
+    KR_CUDA(op->ctx, cudaMemcpyAsync(op->fs_coef, coef, bc, cudaMemcpyHostToDevice, st));
+    KR_CUDA(op->ctx, cudaMemcpyAsync(op->fs_scale, scale, bs, cudaMemcpyHostToDevice, st));
+    KR_CUDA(op->ctx, cudaMemcpyAsync(op->fs_thresh, thresh, bt, cudaMemcpyHostToDevice, st));
+    KR_CUDA(op->ctx, cudaStreamSynchronize(st));
+  }
+  op->fs_nsteps = nsteps;
   return KR_OK;
+}
+
+extern "C" int kr_set_field_step(kr_op* op, int32_t step, void* stream) {
+  if (!op) return set_err(nullptr, KR_ERR_ARG, "kr_set_field_step: NULL operator");
+  if (step < 0 || step >= op->fs_nsteps)
+    return set_err(op->ctx, KR_ERR_ARG, "kr_set_field_step: step " + std::to_string(step) + " outside the schedule of " +
+                                            std::to_string(op->fs_nsteps) + " steps");
+  if (op->field.nent == 0 && op->field.nmf == 0) return KR_OK;
+  const size_t np = (size_t)op->npart, s = (size_t)step;
+  FieldCoefDev c{op->fs_coef + s * np * KR_MAXCART, op->fs_scale + s * np, op->fs_thresh + s * np};
+  return launch_field(op, c, (cudaStream_t)stream);
 }
 
 extern "C" int kr_matvec(kr_op* op, const void* x, void* y, int64_t nvec, void* stream) {

@@ -9,10 +9,13 @@ each recorded step carries its own field) and the persistent step launch
 no host work in between. The library allocates nothing while stepping, so the
 recording holds only these launches and two small memsets per step.
 
-Limits: up to 16 operator parts (their field coefficients travel as kernel
-parameters; beyond that they are copied from host memory per call, which a
-recording cannot repeat); no Krylov orders are read back per step (a Lanczos
-error is sticky on the device and raised by ``replay`` through kr_sync_status).
+Operators of up to 16 parts record their field coefficients as kernel
+parameters. Above that (or with ``schedule=True``) the fields of all recorded
+steps are uploaded once before recording (kr_set_field_schedule) and each
+recorded step sets its own from device memory (kr_set_field_step), since a
+per-call copy from host memory cannot be repeated by a replay. No Krylov
+orders are read back per step (a Lanczos error is sticky on the device and
+raised by ``replay`` through kr_sync_status).
 """
 import torch
 
@@ -29,33 +32,53 @@ class StepGraph:
         tol, maxorder : as TDSE.update
         before_step : optional callable recorded ahead of every step (e.g. an
                       L2 flush for timing)
+        schedule : None (fields from device memory above 16 parts), or True /
+                   False to force either form
     """
 
-    def __init__(self, tdse, H0, vecs, hamiltonian, times, tol=1e-15, maxorder=100, before_step=None):
+    def __init__(self, tdse, H0, vecs, hamiltonian, times, tol=1e-15, maxorder=100, before_step=None,
+                 schedule=None):
         assert torch.is_tensor(vecs) and vecs.is_cuda and vecs.dtype == torch.complex128
         self.vecs = vecs if vecs.dim() == 2 else vecs.reshape(1, -1)
         self.times = list(times)
         fac = tdse.exp_fac
         phase = tdse._h0_phase(H0, fac, vecs.device) if H0 is not None else None
         # operators are created (and uploaded) outside the recording
-        plans = [hamiltonian(t).device_operator(maxorder=maxorder) for t in self.times[:1]]
-        if len(plans[0].sources) > _native.KR_PART_INLINE:
-            raise ValueError(f"a recorded step takes at most {_native.KR_PART_INLINE} operator parts")
-        self.plan = plans[0]
+        self.plan = hamiltonian(self.times[0]).device_operator(maxorder=maxorder)
+        if schedule is None:
+            schedule = len(self.plan.sources) > _native.KR_PART_INLINE
+        elif not schedule and len(self.plan.sources) > _native.KR_PART_INLINE:
+            raise ValueError(f"above {_native.KR_PART_INLINE} operator parts a recorded step needs the field schedule")
+        self.schedule = bool(schedule)
+        if self.schedule:
+            steps = []
+            for t in self.times:
+                H = hamiltonian(t)
+                if H._plan(maxorder) is not self.plan:
+                    raise ValueError("the recorded steps must share one operator (the same factor sources)")
+                steps.append(H._part_states())
+            self.plan.set_field_schedule(steps)
+            self._schedule_gen = self.plan.schedule_gen
         self.graph = torch.cuda.CUDAGraph()
         stream = torch.cuda.Stream()
         stream.wait_stream(torch.cuda.current_stream())
         with torch.cuda.graph(self.graph, stream=stream):
-            for t in self.times:
+            for i, t in enumerate(self.times):
                 if before_step is not None:
                     before_step()
-                plan = hamiltonian(t).device_operator(maxorder=maxorder)  # field launch of this step
+                if self.schedule:
+                    plan = self.plan
+                    plan.set_field_step(i)  # field launch of this step, from the schedule
+                else:
+                    plan = hamiltonian(t).device_operator(maxorder=maxorder)  # field launch of this step
                 plan.step(self.vecs, phase, fac, tol, flags=0, korder=None)
         torch.cuda.current_stream().wait_stream(stream)
 
     def replay(self):
         """Runs the recorded steps on the current stream's device and checks
         the Lanczos status afterwards (ValueError at maxorder, as tdse.py:480-484)."""
+        if self.schedule and self.plan.schedule_gen != self._schedule_gen:
+            raise RuntimeError("the operator's field schedule was replaced after this recording")
         self.graph.replay()
         try:
             self.plan.sync_status()

@@ -98,12 +98,28 @@ class MoleculeSet:
                 pass
             self.handle = None
 
-    def step(self, state):
+    def set_field_schedule(self, set_fields, nsteps):
+        """Uploads the fields of ``nsteps`` steps at once (kr_set_field_schedule):
+        ``set_fields(i)`` sets step i's field on the tensors, as a caller does
+        before ``step``. ``step(state, field_step=i)`` then takes step i's field
+        from device memory: no host copy and no stream synchronisation per step
+        (a set of more than 16 parts otherwise stages its coefficients through
+        host memory every step)."""
+        steps = []
+        for i in range(nsteps):
+            set_fields(i)
+            steps.append([ps for T in self.tensors for ps in T._part_states()])
+        self.plan.set_field_schedule(steps)
+
+    def step(self, state, field_step=None):
         """One TDSE.update of every molecule, in place on the joint vector
         ``state`` ((dim,) complex128 CUDA tensor), each molecule with the field
-        its tensor carries. ``last_korder``: the Krylov order of each molecule."""
-        part_states = [ps for T in self.tensors for ps in T._part_states()]
-        self.plan.set_field(part_states)
+        its tensor carries (or with step ``field_step`` of the uploaded field
+        schedule). ``last_korder``: the Krylov order of each molecule."""
+        if field_step is None:
+            self.plan.set_field([ps for T in self.tensors for ps in T._part_states()])
+        else:
+            self.plan.set_field_step(field_step)
         korder = np.zeros(len(self.dims), np.int32)
         fac = self.tdse.exp_fac
         rc = _native.lib().kr_seg_step(self.handle, _native.ptr(state), _native.ptr(self._phase_dev()),
@@ -116,15 +132,14 @@ class MoleculeSet:
 
     def expect(self, ops, state):
         """<v_m|O_m|v_m> per molecule (numpy array) for per-molecule H0-type
-        tensors ``ops`` (e.g. cos^2 theta), through the FP64 mat-vec of each."""
+        tensors ``ops`` (e.g. cos^2 theta), through kr_observables (the FP64
+        mat-vec of each and a fixed-order FP64 dot product)."""
         out = np.zeros(len(ops))
         for m, (O, v) in enumerate(zip(ops, self.split(state))):
             if not O._is_sum and O._parts[0].prods is None:
                 O.field([0, 0, 1])
-            plan = O.device_operator()
-            y = torch.empty_like(v)
-            plan.matvec(v.reshape(1, -1), y.reshape(1, -1))
-            out[m] = float(torch.vdot(v, y).real)
+            vals, _ = O.device_operator().observables(v.reshape(1, -1))
+            out[m] = vals[0].real
         return out
 
     def launches(self):

@@ -381,20 +381,51 @@ class OperatorPlan:
             self.op = None
 
     # ------------------------------------------------------------------
-    def set_field(self, part_states, stream=None):
-        """part_states: per part (field_prod dict cart -> value, K scale, thresh)."""
-        self._coef[:] = 0
-        for p, (prods, scale, thresh) in enumerate(part_states):
-            carts = self.part_carts[p]
-            for ci, c in enumerate(carts):
+    def field_coefficients(self, part_states, coef=None, scale=None, thresh=None):
+        """The kr_set_field arrays of one step. part_states: per part (field_prod
+        dict cart -> value, K scale, thresh), as CarTens._part_states() gives."""
+        coef = np.zeros_like(self._coef) if coef is None else coef
+        scale = np.zeros_like(self._scale) if scale is None else scale
+        thresh = np.zeros_like(self._thresh) if thresh is None else thresh
+        coef[:] = 0
+        for p, (prods, sc, th) in enumerate(part_states):
+            for ci, c in enumerate(self.part_carts[p]):
                 v = prods.get(c)
                 if v is not None:
-                    self._coef[p, ci] = v
-            self._scale[p] = scale
-            self._thresh[p] = 0.0 if thresh is None else float(thresh)
+                    coef[p, ci] = v
+            scale[p] = sc
+            thresh[p] = 0.0 if th is None else float(th)
+        return coef, scale, thresh
+
+    def set_field(self, part_states, stream=None):
+        """part_states: per part (field_prod dict cart -> value, K scale, thresh)."""
+        self.field_coefficients(part_states, self._coef, self._scale, self._thresh)
         _native.check(_native.lib().kr_set_field(
             self.op, self._coef.ctypes.data, self._scale.ctypes.data, self._thresh.ctypes.data,
             stream_ptr(stream)), self.ctx)
+
+    def set_field_schedule(self, steps, stream=None):
+        """Uploads the field of many steps at once (kr_set_field_schedule);
+        steps: per step the part_states of set_field. set_field_step(i) then
+        sets step i's field with no host data (recordable at any part count)."""
+        n = len(steps)
+        if n == 0:
+            raise ValueError("empty field schedule")
+        coef = np.zeros((n,) + self._coef.shape, np.complex128)
+        scale = np.zeros((n,) + self._scale.shape, np.complex128)
+        thresh = np.zeros((n,) + self._thresh.shape, np.float64)
+        for i, ps in enumerate(steps):
+            self.field_coefficients(ps, coef[i], scale[i], thresh[i])
+        _native.check(_native.lib().kr_set_field_schedule(
+            self.op, n, coef.ctypes.data, scale.ctypes.data, thresh.ctypes.data, stream_ptr(stream)), self.ctx)
+        self.schedule_steps = n
+        # a replaced schedule's memory is freed: recordings of set_field_step
+        # keep the generation they were made with and refuse another
+        self.schedule_gen = getattr(self, "schedule_gen", 0) + 1
+
+    def set_field_step(self, step, stream=None):
+        """The field of step `step` of the uploaded schedule (kr_set_field_step)."""
+        _native.check(_native.lib().kr_set_field_step(self.op, int(step), stream_ptr(stream)), self.ctx)
 
     def matvec(self, x, y, stream=None):
         assert x.dtype == torch.complex128 and y.dtype == torch.complex128 and x.is_cuda and y.is_cuda
@@ -411,6 +442,22 @@ class OperatorPlan:
         _native.check(_native.lib().kr_step(
             self.op, _native.ptr(states), nvec, _native.ptr(phase), float(fac.real), float(fac.imag),
             float(tol), int(flags), kp, stream_ptr(stream)), self.ctx)
+
+    def observables(self, states, weights=None, stream=None):
+        """<v_i|O|v_i> of the rows of ``states`` ((nvec, dim) or (dim,) complex128
+        CUDA tensor) with this operator as O (kr_observables): a complex numpy
+        array, and sum_i w_i Re <v_i|O|v_i> (weights: None = all 1)."""
+        nvec = states.shape[0] if states.dim() == 2 else 1
+        out = np.zeros(nvec, np.complex128)
+        w = None
+        if weights is not None:
+            w = np.ascontiguousarray(weights, np.float64)
+            assert w.size == nvec
+        ws = ctypes.c_double()
+        _native.check(_native.lib().kr_observables(
+            self.op, _native.ptr(states), nvec, None if w is None else w.ctypes.data, out.ctypes.data,
+            ctypes.byref(ws), stream_ptr(stream)), self.ctx)
+        return out, ws.value
 
     def norm1(self, stream=None):
         """1-norm estimate of the operator with its current field (kr_op_norm1)."""
