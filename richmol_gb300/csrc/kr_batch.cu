@@ -235,7 +235,7 @@ __global__ void kb_start(const double2* nsq, double* norm0, int* active, int* kc
 // of W a CTA reads stays in cache from pass to pass, so DRAM sees W once (one
 // pass over all V_j with W read once measured 45 % slower at C3). The loads of
 // four elements go out before their FMAs (summed in element order, so the
-// result is the one-at-a-time sum), at 6 CTAs per SM: 12 % faster at C3.
+// result is the one-at-a-time sum), at 6 CTAs per SM: 14 % faster at C3.
 __global__ void __launch_bounds__(256, 6) kb_dots(const float2* V, const float2* W, const int* active,
                                                   const double* vscale, long long dim, int nb, int k,
                                                   int stride_coef, double2* part) {
@@ -278,8 +278,9 @@ __global__ void __launch_bounds__(256, 6) kb_dots(const float2* V, const float2*
 }
 
 // V_{k+1} = W - sum_j h_j V_j (unnormalised), partial ||V_{k+1}||^2; k < KM.
-// KM = 4 at 5 CTAs per SM (48 registers, no spills): 11 % faster at C3 than
-// the 63-register form at 4.
+// KM = 4 with the register budget of 5 CTAs per SM: 48 registers (40 without
+// the bound), which lets the loads of W and every basis vector go out ahead of
+// their FMAs; 15 % faster at C3.
 template <int KM>
 __global__ void __launch_bounds__(256, KM == 4 ? 5 : 1) kb_update(float2* V, const float2* W, const double2* h, const double* vscale, const int* active,
                           long long dim, int nb, int k, double2* part) {
@@ -377,9 +378,8 @@ __global__ void kb_small(BatchDev b, int k, double2 fac, double tol, const doubl
 // S <- phase * (c_0 S + ||v|| sum_{i>=1} c_i V_i)   (double-float state; the
 // complex64 Krylov corrections summed in FP32)
 // S <- P (c_0 S + ||S|| sum_{1 <= i < K} c_i V_i), K < KM + 1 per vector
-// KM = 4 at 5 CTAs per SM: 19 % faster at C3 than the 69-register form at 3
 template <int KM>
-__global__ void __launch_bounds__(256, KM == 4 ? 5 : 1) kb_combine(BatchDev b, const float4* phase) {
+__global__ void kb_combine(BatchDev b, const float4* phase) {
   const int v = blockIdx.y * 32 + threadIdx.x;
   const int nb = b.nb;
   const int K = b.kconv[v];
