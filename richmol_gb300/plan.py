@@ -318,6 +318,31 @@ def build_tables(sources, basis_out, basis_in, split=None, blocks=None, source_b
                            nk=len(k_type), nm=len(m_rows), nmf=len(mf_group))
 
 
+def field_arrays(part_carts, part_states, coef=None, scale=None, thresh=None):
+    """The field input of kr_set_field (and of one step of a field schedule):
+    coef[p, c] = the field product of part p's Cartesian component c (in the
+    part's component order, part_carts[p]; zero where the field has none),
+    scale[p] = the part's K scale, thresh[p] = its element threshold (None: 0,
+    no threshold). part_states: per part (field_prod dict cart -> value, K
+    scale, thresh), as CarTens._part_states() gives (field.py:1094-1139 forms
+    the same products)."""
+    n = max(1, len(part_carts))
+    coef = np.zeros((n, _native.KR_MAXCART), np.complex128) if coef is None else coef
+    scale = np.zeros(n, np.complex128) if scale is None else scale
+    thresh = np.zeros(n, np.float64) if thresh is None else thresh
+    if len(part_states) != len(part_carts):
+        raise ValueError(f"{len(part_states)} part states for an operator of {len(part_carts)} parts")
+    coef[:] = 0
+    for p, (prods, sc, th) in enumerate(part_states):
+        for ci, c in enumerate(part_carts[p]):
+            v = prods.get(c)
+            if v is not None:
+                coef[p, ci] = v
+        scale[p] = sc
+        thresh[p] = 0.0 if th is None else float(th)
+    return coef, scale, thresh
+
+
 class OperatorPlan:
     """One kr_op: the device tables for a tuple of factor sources."""
 
@@ -382,20 +407,10 @@ class OperatorPlan:
 
     # ------------------------------------------------------------------
     def field_coefficients(self, part_states, coef=None, scale=None, thresh=None):
-        """The kr_set_field arrays of one step. part_states: per part (field_prod
-        dict cart -> value, K scale, thresh), as CarTens._part_states() gives."""
-        coef = np.zeros_like(self._coef) if coef is None else coef
-        scale = np.zeros_like(self._scale) if scale is None else scale
-        thresh = np.zeros_like(self._thresh) if thresh is None else thresh
-        coef[:] = 0
-        for p, (prods, sc, th) in enumerate(part_states):
-            for ci, c in enumerate(self.part_carts[p]):
-                v = prods.get(c)
-                if v is not None:
-                    coef[p, ci] = v
-            scale[p] = sc
-            thresh[p] = 0.0 if th is None else float(th)
-        return coef, scale, thresh
+        """The kr_set_field arrays of one step (see field_arrays)."""
+        if coef is None:
+            coef, scale, thresh = np.zeros_like(self._coef), np.zeros_like(self._scale), np.zeros_like(self._thresh)
+        return field_arrays(self.part_carts, part_states, coef, scale, thresh)
 
     def set_field(self, part_states, stream=None):
         """part_states: per part (field_prod dict cart -> value, K scale, thresh)."""

@@ -8,12 +8,13 @@ strided slabs) applied to random vectors.
 * a block-diagonal operator over several molecules (blocks=..., the
   uneven-size batch) is the molecules' operators side by side, each part
   with its own field coefficients;
-* the reading itself agrees with the host assembly CarTens.tomat."""
+* the reading itself agrees with the host assembly CarTens.tomat, fed with
+  the field input as kr_set_field receives it (plan.field_arrays)."""
 import numpy as np
 import pytest
 
 from richmol_gb300 import _native, workloads
-from richmol_gb300.plan import build_tables
+from richmol_gb300.plan import build_tables, field_arrays
 
 RTOL = 1e-12
 
@@ -148,12 +149,26 @@ def test_emulation_matches_the_host_matrix(c1_molecule):
     H.field(np.array([0.3, -0.7, 0.55]) * 1e7)
     srcs = [p.src for p in H._parts]
     T = build_tables(srcs, srcs[0].basis("1"), srcs[0].basis("2"))
-    coef, scale = [], []
-    for (prods, kscale, _thresh), carts in zip(H._part_states(), T.part_carts):
-        coef.append(np.array([prods.get(c, 0.0) for c in carts], np.complex128))
-        scale.append(kscale)
+    # the field input exactly as kr_set_field and the field schedule receive it
+    coef, scale, thresh = field_arrays(T.part_carts, H._part_states())
+    assert np.all(thresh == 0.0)
     rng = np.random.default_rng(3)
     x = rng.normal(size=T.dim_in) + 1j * rng.normal(size=T.dim_in)
-    y = emulate(T, coef, np.array(scale, np.complex128), x)
+    y = emulate(T, coef, scale, x)
     ref = H.tomat(form="full") @ x
     assert np.abs(y - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
+def test_field_arrays_layout():
+    """Per part: coefficients in the part's own Cartesian order (zero where the
+    field has no product), K scale, threshold (None: 0); the part count must
+    match the operator's."""
+    carts = [["x", "y", "z"], ["xx", "xy", "xz", "yy", "yz", "zz"]]
+    states = [({"z": 2.0, "x": 1j}, 0.5, None), ({"zz": -3.0, "xy": 0.25}, 1 + 1j, 1e-12)]
+    coef, scale, thresh = field_arrays(carts, states)
+    assert coef.shape == (2, 9)
+    assert coef[0].tolist() == [1j, 0, 2.0] + [0] * 6
+    assert coef[1].tolist() == [0, 0.25, 0, 0, 0, -3.0] + [0] * 3
+    assert scale.tolist() == [0.5, 1 + 1j] and thresh.tolist() == [0.0, 1e-12]
+    with pytest.raises(ValueError):
+        field_arrays(carts, states[:1])
