@@ -24,7 +24,7 @@ import numpy as np
 import scipy.constants as const
 from scipy.sparse import csr_matrix
 
-from .field import CarTens, FactorSource
+from .field import CarTens
 
 # Cartesian-to-spherical transformation of rank-1 and rank-2 tensors
 # (rot/labtens.py:89-100); rows follow IRREP_IND, columns CART_IND.

@@ -5,7 +5,6 @@ import os
 import socket
 import sys
 
-import pytest
 
 from conftest import ROOT
 

@@ -5,7 +5,6 @@ import threading
 import time
 
 import numpy as np
-import pytest
 
 from richmol_gb300 import serve
 
