@@ -206,14 +206,14 @@ def cpu_reference_rate(wl, seconds, max_steps=None, warmup=1, vec=None):
 
 def _reference_worker(args):
     """One host process: one vector of the ensemble workload (spawned)."""
-    jmax, nvec, idx, seconds, max_steps = args
+    jmax, nvec, idx, seconds, max_steps, warmup = args
     os.environ.setdefault("OMP_NUM_THREADS", "1")
     sys.path.insert(0, ROOT)
     from richmol_gb300 import workloads
     wl, ens = workloads.thermal_asym_top(Jmax=jmax, nvec=nvec)
     v = np.zeros(wl.dim, np.complex128)
     v[ens.index[idx % nvec]] = 1.0
-    rate, n, t = cpu_reference_rate(wl, seconds, max_steps=max_steps, vec=v)
+    rate, n, t = cpu_reference_rate(wl, seconds, max_steps=max_steps, warmup=warmup, vec=v)
     return n, t
 
 
@@ -638,18 +638,19 @@ def run_reference(args, ws, rank, local):
     ncores = os.cpu_count() or 1
     nproc = max(1, min(ncores, 64))
     per_steps = max(1, min(args.steps, 20))
+    warm = max(1, min(args.warmup, 10))  # untimed steps per process (bounded: each is ~0.5 s of CPU)
     budget = 60.0
     ctxm = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctxm.Pool(nproc) as pool:
-        res = pool.map(_reference_worker, [(args.jmax, args.nvec, i, budget, per_steps) for i in range(nproc)])
+        res = pool.map(_reference_worker, [(args.jmax, args.nvec, i, budget, per_steps, warm) for i in range(nproc)])
     wall = time.perf_counter() - t0
     steps = sum(n for n, _ in res)
     busy = max(t for _, t in res)
     rate = steps / busy
     return {
         "impl": "reference", "metric": METRIC, "value": round(rate, 3), "unit": UNIT, "n_gpus": ws,
-        "steps": per_steps, "warmup": 1, "ms_per_step": round(busy * 1e3 / per_steps, 1),
+        "steps": per_steps, "warmup": warm, "ms_per_step": round(busy * 1e3 / per_steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)",
         "data": "synthetic",
         "config": {"workload": f"batched thermal ensemble: asymmetric top D2 Watson-A J=0..{args.jmax}, "
