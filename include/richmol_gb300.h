@@ -305,6 +305,14 @@ int kr_probe_fp32(kr_ctx* ctx, double* tflops);
  * 128 x 16, B 16 x 16, D 128 x 16, row-major FP32 host arrays read as TF32, by
  * one tcgen05.mma tile; checks the MMA building block of the batched mat-vec. */
 int kr_probe_mma(kr_ctx* ctx, const float* a, const float* b, float* d);
+/* Failure-detection probe (no counterpart in the reference): the bounded grid
+ * barrier of the step kernels in a launch of two CTAs of which one never
+ * arrives (a rank that never joins). The other's wait gives up after its limit
+ * (2 s), records KR_ERR_TIMEOUT and returns instead of hanging; *status gets
+ * the status the barrier recorded (KR_ERR_TIMEOUT, or KR_OK had it completed),
+ * *waited_s how long it waited. The call itself returns KR_OK and the context
+ * stays usable. Synchronises the device. */
+int kr_probe_wait(kr_ctx* ctx, int32_t* status, double* waited_s);
 
 #ifdef __cplusplus
 }

@@ -36,7 +36,7 @@ EXPORTED = [
     "kr_ctx_create", "kr_ctx_destroy", "kr_last_error", "kr_op_create", "kr_op_destroy",
     "kr_set_field", "kr_set_field_schedule", "kr_set_field_step",
     "kr_matvec", "kr_step", "kr_sync_status", "kr_op_launch_count", "kr_op_work",
-    "kr_probe_fp64", "kr_probe_fp32", "kr_probe_mma", "kr_step_static", "kr_static_scratch_bytes",
+    "kr_probe_fp64", "kr_probe_fp32", "kr_probe_mma", "kr_probe_wait", "kr_step_static", "kr_static_scratch_bytes",
     "kr_batch_create", "kr_batch_destroy", "kr_batch_load", "kr_batch_store", "kr_batch_step",
     "kr_batch_korder", "kr_batch_expect", "kr_batch_launch_count", "kr_batch_matvec", "kr_batch_apply", "kr_batch_set_matvec",
     "kr_batch_populations",
@@ -190,6 +190,8 @@ def lib():
         L.kr_observables.restype = ctypes.c_int
         L.kr_probe_mma.argtypes = [vp, vp, vp, vp]
         L.kr_probe_mma.restype = ctypes.c_int
+        L.kr_probe_wait.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(dbl)]
+        L.kr_probe_wait.restype = ctypes.c_int
         L.kr_probe_fp64.argtypes = [vp, ctypes.POINTER(dbl)]
         L.kr_probe_fp64.restype = ctypes.c_int
         _lib = L

@@ -8,6 +8,7 @@
 #define KR_THREADS (KR_WARPS * 32)
 #define KR_QMAX 4                   // (row, a) outputs per thread of a task
 #define KR_BARRIER_TIMEOUT_NS 2000000000ull  // 2 s per grid-barrier wait
+#define KR_BARRIER_MAX_SPINS (1u << 24)      // spins per wait (>= 5 s at 0.3 us each)
 
 // ---------------------------------------------------------------------------
 // complex helpers (double2 = re, im)
@@ -97,8 +98,10 @@ static __device__ bool grid_barrier(unsigned* count, unsigned* gen, int* status,
       st_release_u32(gen, my_gen + 1u);
     } else {
       unsigned long long t0 = globaltimer_ns();
-      while (ld_acquire_u32(gen) == my_gen) {
-        if (globaltimer_ns() - t0 > KR_BARRIER_TIMEOUT_NS) {
+      // bounded twice: by time, and by a spin count that takes longer than the
+      // time limit at any iteration time (an acquire load of L2 takes ~0.3 us)
+      for (unsigned spins = 0; ld_acquire_u32(gen) == my_gen; ++spins) {
+        if (globaltimer_ns() - t0 > KR_BARRIER_TIMEOUT_NS || spins >= KR_BARRIER_MAX_SPINS) {
           atomicCAS(status, 0, code_on_timeout);
           ok = 0;
           break;

@@ -1547,6 +1547,46 @@ extern "C" int kr_probe_fp64(kr_ctx* ctx, double* tflops) {
   return KR_OK;
 }
 
+// The grid barrier of the step kernels with a CTA that never arrives (CTA 1
+// returns at once, as a rank that never joins): CTA 0's bounded wait gives up
+// after KR_BARRIER_TIMEOUT_NS, records KR_ERR_TIMEOUT in status and returns.
+// out[0]: 1 if the barrier reported failure, out[1]: ns CTA 0 waited.
+__global__ void kr_wait_probe_kernel(unsigned* bar, int* status, unsigned long long* out) {
+  if (blockIdx.x != 0) return;
+  const unsigned long long t0 = globaltimer_ns();
+  const bool ok = grid_barrier(bar, bar + 1, status, KR_ERR_TIMEOUT);
+  if (threadIdx.x == 0) {
+    out[0] = ok ? 0ull : 1ull;
+    out[1] = globaltimer_ns() - t0;
+  }
+}
+
+extern "C" int kr_probe_wait(kr_ctx* ctx, int32_t* status, double* waited_s) {
+  if (!ctx || !status || !waited_s) return set_err(ctx, KR_ERR_ARG, "kr_probe_wait: NULL argument");
+  KR_CUDA(ctx, cudaSetDevice(ctx->device));
+  // bar[2] (count, generation), status, pad, out[2]
+  void* buf = nullptr;
+  KR_CUDA(ctx, cudaMalloc(&buf, 32));
+  cudaError_t e = cudaMemset(buf, 0, 32);
+  unsigned* bar = static_cast<unsigned*>(buf);
+  int* st = reinterpret_cast<int*>(bar + 2);
+  unsigned long long* out = reinterpret_cast<unsigned long long*>(static_cast<char*>(buf) + 16);
+  if (e == cudaSuccess) {
+    kr_wait_probe_kernel<<<2, 32>>>(bar, st, out);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  int h_st = 0;
+  unsigned long long h_out[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(&h_st, st, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(h_out, out, sizeof(h_out), cudaMemcpyDeviceToHost);
+  cudaFree(buf);
+  if (e != cudaSuccess) return set_err(ctx, KR_ERR_CUDA, std::string("kr_probe_wait: ") + cudaGetErrorString(e));
+  *status = h_out[0] ? h_st : KR_OK;
+  *waited_s = 1e-9 * (double)h_out[1];
+  return KR_OK;
+}
+
 // ===========================================================================
 // Allocation-free step: kr_step with its Krylov workspace in a fixed,
 // file-scope device array instead of the workspace kr_op_create allocated.
