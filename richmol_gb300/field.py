@@ -316,6 +316,8 @@ class CarTens:
             np.asarray(vec[J][s], dtype=np.complex128).reshape(-1) if (J in vec and s in vec[J])
             else np.zeros(src.dim2[J][s], np.complex128)
             for J in src.Jlist2 for s in src.symlist2[J]])
+        from .device import require_cuda
+        require_cuda()  # the product runs on the GPU only: no CPU fallback
         xd = torch.from_numpy(x).cuda()
         y = self.vec_device(xd).cpu().numpy()
         out, ind = {}, 0

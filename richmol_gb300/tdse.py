@@ -17,6 +17,7 @@ from scipy.sparse import csr_matrix, diags
 
 from . import _native
 from .convert_units import J_to_invcm, MHz_to_invcm
+from .device import require_cuda
 from .field import CarTens
 
 
@@ -253,6 +254,7 @@ class TDSE:
         check = bool(kwargs.get("check", True))
         exp_fac = self.exp_fac
 
+        require_cuda()  # the step runs on the GPU only: no CPU fallback
         as_numpy = isinstance(vecs, np.ndarray)
         if as_numpy:
             v = torch.from_numpy(np.ascontiguousarray(vecs, dtype=np.complex128)).cuda()
