@@ -104,6 +104,10 @@ def test_recorded_steps_from_schedule_below_16_parts():
         eager, _ = td_e.update(wl.hamiltonian(t), H0=wl.h0, vecs=eager, inplace=True, check=False)
     torch.cuda.synchronize()
     assert float((rec - eager).abs().max()) <= STATE_TOL
+    # a new schedule frees the one the recording reads: its replay is refused
+    g.plan.set_field_schedule([wl.hamiltonian(t)._part_states() for t in times])
+    with pytest.raises(RuntimeError, match="replaced"):
+        g.replay()
 
 
 def test_molecule_set_with_field_schedule():
