@@ -1,10 +1,10 @@
 """Multi-process host logic of bench.py on CPU (gloo, world size 2): the
 whole-job rate takes the slowest rank's time (max over ranks) and counts the
 units of every rank; the reference arm runs on rank 0 only."""
+import json
 import os
 import socket
 import sys
-
 
 from conftest import ROOT
 
@@ -55,3 +55,20 @@ def test_reference_arm_runs_on_rank_0_only():
     import bench
     args = bench.parse([])
     assert bench.run_reference(args, 2, 1, 1) is None
+
+
+def test_reference_arm_line_keeps_the_contract():
+    """The reference arm end to end on the host cores at a small size (J <= 8):
+    one JSON-ready dict with the keys the bench contract names."""
+    sys.path.insert(0, ROOT)
+    import bench
+    args = bench.parse(["--impl", "reference", "--steps", "2", "--warmup", "3", "--jmax", "8", "--nvec", "256"])
+    out = bench.run_reference(args, 1, 0, 0)
+    for key in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in out, key
+    assert out["impl"] == "reference" and out["value"] > 0 and out["warmup"] == 3 and out["steps"] == 2
+    assert out["e2e"]["value"] == out["value"]
+    assert out["e2e"]["h2d_bytes_per_step"] == 0 and out["e2e"]["d2h_bytes_per_step"] == 0
+    assert out["cpu_baseline"]["kind"] == "port" and out["cpu_baseline"]["cores"] >= 1
+    json.dumps(out)
