@@ -169,6 +169,12 @@ int kr_last_error(const kr_ctx* ctx, char* buf, size_t len);
  * Replaces the data held by CarTens.kmat / CarTens.mmat (field.py:58-170). */
 int kr_op_create(kr_ctx* ctx, const kr_op_desc* desc, kr_op** out);
 void kr_op_destroy(kr_op* op);
+/* Validates a descriptor on the host, with no device and no context: the
+ * checks kr_op_create applies before it uploads anything (slab tables, row
+ * strides and coverage of column chunks, M groups, MF instances, K blocks,
+ * terms). KR_OK, or the status kr_op_create would return, with its message in
+ * buf (len bytes, may be NULL) and in kr_last_error(NULL, ...). */
+int kr_op_check(const kr_op_desc* desc, char* buf, size_t len);
 
 /* Field contraction, one call per time step (field.py:1073-1142):
  * MF = scale_p * (|x| < thresh_p ? 0 : x),  x = sum_c coef[p][c] M_c.

@@ -33,7 +33,7 @@ KR_MATVEC_TENSOR, KR_MATVEC_FP32 = 0, 1
 FIELD_COEF_BYTES = 8 + KR_PART_INLINE * KR_MAXCART * 16 + KR_PART_INLINE * 16 + KR_PART_INLINE * 8
 
 EXPORTED = [
-    "kr_ctx_create", "kr_ctx_destroy", "kr_last_error", "kr_op_create", "kr_op_destroy",
+    "kr_ctx_create", "kr_ctx_destroy", "kr_last_error", "kr_op_create", "kr_op_destroy", "kr_op_check",
     "kr_set_field", "kr_set_field_schedule", "kr_set_field_step",
     "kr_matvec", "kr_step", "kr_sync_status", "kr_op_launch_count", "kr_op_work",
     "kr_probe_fp64", "kr_probe_fp32", "kr_probe_mma", "kr_probe_wait", "kr_step_static", "kr_static_scratch_bytes",
@@ -128,6 +128,8 @@ def lib():
         L.kr_op_create.restype = ctypes.c_int
         L.kr_op_destroy.argtypes = [vp]
         L.kr_op_destroy.restype = None
+        L.kr_op_check.argtypes = [ctypes.POINTER(kr_op_desc), ctypes.c_char_p, ctypes.c_size_t]
+        L.kr_op_check.restype = ctypes.c_int
         L.kr_set_field.argtypes = [vp, vp, vp, vp, vp]
         L.kr_set_field.restype = ctypes.c_int
         L.kr_set_field_schedule.argtypes = [vp, i32, vp, vp, vp, vp]

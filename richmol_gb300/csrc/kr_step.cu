@@ -831,35 +831,50 @@ static cudaError_t ensure_step_smem(size_t smem) {
   return e;
 }
 
-extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
-  if (!ctx || !d || !out) return set_err(ctx, KR_ERR_ARG, "kr_op_create: NULL argument");
-  *out = nullptr;
-  KR_CUDA(ctx, cudaSetDevice(ctx->device));
-  // ---- validation -------------------------------------------------------
-  if (d->nslab_out <= 0 || d->nslab_in <= 0) return set_err(ctx, KR_ERR_ARG, "empty basis");
-  if (d->npart < 0 || d->npart > KR_MAXPART) return set_err(ctx, KR_ERR_ARG, "npart out of range");
-  if (d->maxorder < 2 || d->maxorder > KR_EXPM_MAX) return set_err(ctx, KR_ERR_ARG, "maxorder out of range [2, 128]");
+namespace {
+// What the validation of a descriptor derives: column chunks present, row
+// strides of every slab, and the terms of every output slab.
+struct DescCheck {
   bool split = false;
-  std::vector<int> out_stride(d->nslab_out), in_stride(d->nslab_in);
-  if (!d->out_stride != !d->in_stride) return set_err(ctx, KR_ERR_ARG, "slab strides given on one side only");
+  std::vector<int> out_stride, in_stride;
+  std::vector<std::vector<int>> by_out;
+};
+
+// Validates a descriptor on the host (no device work): KR_OK, or the status
+// and message of the first problem found.
+int check_desc(const kr_op_desc* d, DescCheck& c, std::string& err) {
+  auto fail = [&err](int code, const std::string& msg) {
+    err = msg;
+    return code;
+  };
+  if (d->nslab_out <= 0 || d->nslab_in <= 0) return fail(KR_ERR_ARG, "empty basis");
+  if (d->npart < 0 || d->npart > KR_MAXPART) return fail(KR_ERR_ARG, "npart out of range");
+  if (d->maxorder < 2 || d->maxorder > KR_EXPM_MAX) return fail(KR_ERR_ARG, "maxorder out of range [2, 128]");
+  bool& split = c.split;
+  std::vector<int>& out_stride = c.out_stride;
+  std::vector<int>& in_stride = c.in_stride;
+  split = false;
+  out_stride.assign(d->nslab_out, 0);
+  in_stride.assign(d->nslab_in, 0);
+  if (!d->out_stride != !d->in_stride) return fail(KR_ERR_ARG, "slab strides given on one side only");
   if (!d->out_stride) {
     long long off = 0;
     for (int s = 0; s < d->nslab_out; ++s) {
       if (d->out_off[s] != off || d->out_dm[s] <= 0 || d->out_dk[s] <= 0)
-        return set_err(ctx, KR_ERR_ARG, "malformed output slab table");
-      if (d->out_dk[s] > 32 * KR_QMAX) return set_err(ctx, KR_ERR_UNSUPPORTED, "n_k above 128 not supported");
+        return fail(KR_ERR_ARG, "malformed output slab table");
+      if (d->out_dk[s] > 32 * KR_QMAX) return fail(KR_ERR_UNSUPPORTED, "n_k above 128 not supported");
       off += (long long)d->out_dm[s] * d->out_dk[s];
       out_stride[s] = d->out_dk[s];
     }
-    if (off != d->dim_out) return set_err(ctx, KR_ERR_ARG, "dim_out does not match the slab table");
+    if (off != d->dim_out) return fail(KR_ERR_ARG, "dim_out does not match the slab table");
     off = 0;
     for (int s = 0; s < d->nslab_in; ++s) {
       if (d->in_off[s] != off || d->in_dm[s] <= 0 || d->in_dk[s] <= 0)
-        return set_err(ctx, KR_ERR_ARG, "malformed input slab table");
+        return fail(KR_ERR_ARG, "malformed input slab table");
       off += (long long)d->in_dm[s] * d->in_dk[s];
       in_stride[s] = d->in_dk[s];
     }
-    if (off != d->dim_in) return set_err(ctx, KR_ERR_ARG, "dim_in does not match the slab table");
+    if (off != d->dim_in) return fail(KR_ERR_ARG, "dim_in does not match the slab table");
   } else {
     // column chunks: every element of the vector in exactly one chunk
     for (int side = 0; side < 2; ++side) {
@@ -872,55 +887,92 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
       for (int s = 0; s < ns; ++s) {
         if (dm[s] <= 0 || dk[s] <= 0 || st[s] < dk[s] || off[s] < 0 ||
             off[s] + (long long)(dm[s] - 1) * st[s] + dk[s] > dim)
-          return set_err(ctx, KR_ERR_ARG, "malformed slab chunk table");
-        if (dk[s] > 32 * KR_QMAX) return set_err(ctx, KR_ERR_UNSUPPORTED, "n_k above 128 not supported");
+          return fail(KR_ERR_ARG, "malformed slab chunk table");
+        if (dk[s] > 32 * KR_QMAX) return fail(KR_ERR_UNSUPPORTED, "n_k above 128 not supported");
         for (int i = 0; i < dm[s]; ++i)
           for (int a = 0; a < dk[s]; ++a) {
             unsigned char& c = seen[(size_t)(off[s] + (long long)i * st[s] + a)];
-            if (c) return set_err(ctx, KR_ERR_ARG, "slab chunks overlap");
+            if (c) return fail(KR_ERR_ARG, "slab chunks overlap");
             c = 1;
           }
         (side ? in_stride : out_stride)[s] = st[s];
         split = split || st[s] != dk[s];
       }
       for (long long e = 0; e < dim; ++e)
-        if (!seen[(size_t)e]) return set_err(ctx, KR_ERR_ARG, "slab chunks do not cover the vector");
+        if (!seen[(size_t)e]) return fail(KR_ERR_ARG, "slab chunks do not cover the vector");
     }
   }
   for (int g = 0; g < d->nm; ++g) {
     if (d->m_rows[g] <= 0 || d->m_width[g] < 0 || d->m_ncart[g] < 1 || d->m_ncart[g] > KR_MAXCART)
-      return set_err(ctx, KR_ERR_ARG, "malformed M group");
+      return fail(KR_ERR_ARG, "malformed M group");
     const long long ne = (long long)d->m_rows[g] * d->m_width[g];
-    if (d->m_col_off[g] < 0 || d->m_col_off[g] + ne > d->m_col_len) return set_err(ctx, KR_ERR_ARG, "M columns out of range");
+    if (d->m_col_off[g] < 0 || d->m_col_off[g] + ne > d->m_col_len) return fail(KR_ERR_ARG, "M columns out of range");
     if (d->m_val_off[g] < 0 || d->m_val_off[g] + ne * d->m_ncart[g] > d->m_val_len / 2)
-      return set_err(ctx, KR_ERR_ARG, "M values out of range");
+      return fail(KR_ERR_ARG, "M values out of range");
   }
   for (int i = 0; i < d->nmf; ++i)
     if (d->mf_group[i] < 0 || d->mf_group[i] >= d->nm || d->mf_part[i] < 0 || d->mf_part[i] >= d->npart)
-      return set_err(ctx, KR_ERR_ARG, "malformed MF instance");
+      return fail(KR_ERR_ARG, "malformed MF instance");
   for (int b = 0; b < d->nk; ++b) {
     const int words = d->k_type[b] == KR_K_COMPLEX ? 2 : 1;
-    if (d->k_type[b] < 0 || d->k_type[b] > 2) return set_err(ctx, KR_ERR_ARG, "bad K type");
+    if (d->k_type[b] < 0 || d->k_type[b] > 2) return fail(KR_ERR_ARG, "bad K type");
     if (d->k_off[b] < 0 || d->k_off[b] + (long long)d->k_rows[b] * d->k_cols[b] * words > d->k_data_len)
-      return set_err(ctx, KR_ERR_ARG, "K block out of range");
-    if (d->k_type[b] == KR_K_COMPLEX && (d->k_off[b] & 1)) return set_err(ctx, KR_ERR_ARG, "complex K block misaligned");
+      return fail(KR_ERR_ARG, "K block out of range");
+    if (d->k_type[b] == KR_K_COMPLEX && (d->k_off[b] & 1)) return fail(KR_ERR_ARG, "complex K block misaligned");
   }
-  std::vector<std::vector<int>> by_out(d->nslab_out);
+  std::vector<std::vector<int>>& by_out = c.by_out;
+  by_out.assign(d->nslab_out, {});
   for (int t = 0; t < d->nterm; ++t) {
     const int s1 = d->t_out[t], s2 = d->t_in[t], kb = d->t_k[t], mi = d->t_mf[t];
     if (s1 < 0 || s1 >= d->nslab_out || s2 < 0 || s2 >= d->nslab_in || kb < 0 || kb >= d->nk || mi < 0 || mi >= d->nmf)
-      return set_err(ctx, KR_ERR_ARG, "term index out of range");
+      return fail(KR_ERR_ARG, "term index out of range");
     const int g = d->mf_group[mi];
     if (d->k_rows[kb] != d->out_dk[s1] || d->k_cols[kb] != d->in_dk[s2])
-      return set_err(ctx, KR_ERR_ARG, "K block shape does not match its slabs");
-    if (d->m_rows[g] != d->out_dm[s1]) return set_err(ctx, KR_ERR_ARG, "M group rows do not match the output slab");
+      return fail(KR_ERR_ARG, "K block shape does not match its slabs");
+    if (d->m_rows[g] != d->out_dm[s1]) return fail(KR_ERR_ARG, "M group rows do not match the output slab");
     const long long ne = (long long)d->m_rows[g] * d->m_width[g];
     for (long long e = 0; e < ne; ++e) {
       const int c = d->m_col[d->m_col_off[g] + e];
-      if (c < 0 || c >= d->in_dm[s2]) return set_err(ctx, KR_ERR_ARG, "M column outside the input slab");
+      if (c < 0 || c >= d->in_dm[s2]) return fail(KR_ERR_ARG, "M column outside the input slab");
     }
     by_out[s1].push_back(t);
   }
+
+  return KR_OK;
+}
+}  // namespace
+
+extern "C" int kr_op_check(const kr_op_desc* d, char* buf, size_t len) {
+  if (buf && len) buf[0] = 0;
+  if (!d) return set_err(nullptr, KR_ERR_ARG, "kr_op_check: NULL descriptor");
+  DescCheck c;
+  std::string msg;
+  const int rc = check_desc(d, c, msg);
+  if (rc != KR_OK) {
+    if (buf && len) {
+      std::strncpy(buf, msg.c_str(), len - 1);
+      buf[len - 1] = 0;
+    }
+    return set_err(nullptr, rc, msg);
+  }
+  return KR_OK;
+}
+
+extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
+  if (!ctx || !d || !out) return set_err(ctx, KR_ERR_ARG, "kr_op_create: NULL argument");
+  *out = nullptr;
+  KR_CUDA(ctx, cudaSetDevice(ctx->device));
+  // ---- validation (check_desc) -----------------------------------------------
+  DescCheck dchk;
+  {
+    std::string msg;
+    const int rc = check_desc(d, dchk, msg);
+    if (rc != KR_OK) return set_err(ctx, rc, msg);
+  }
+  const bool split = dchk.split;
+  const std::vector<int>& out_stride = dchk.out_stride;
+  const std::vector<int>& in_stride = dchk.in_stride;
+  const std::vector<std::vector<int>>& by_out = dchk.by_out;
 
   kr_op* op = new kr_op();
   op->ctx = ctx;

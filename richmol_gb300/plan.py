@@ -318,6 +318,41 @@ def build_tables(sources, basis_out, basis_in, split=None, blocks=None, source_b
                            nk=len(k_type), nm=len(m_rows), nmf=len(mf_group))
 
 
+def make_desc(T, npart, maxorder=100):
+    """The kr_op_desc of host tables T (build_tables): pointers into T.arrays,
+    which must stay alive while the descriptor is used."""
+    keep = T.arrays
+    d = _native.kr_op_desc()
+    d.nslab_out, d.nslab_in = len(keep["out_dm"]), len(keep["in_dm"])
+    if T.split:
+        d.out_stride, d.in_stride = keep["out_stride"].ctypes.data, keep["in_stride"].ctypes.data
+    for f in ("out_dm", "out_dk", "out_off", "in_dm", "in_dk", "in_off", "k_off", "k_rows", "k_cols",
+              "k_type", "k_data", "m_rows", "m_width", "m_ncart", "m_col_off", "m_val_off", "m_col",
+              "m_val", "mf_group", "mf_part", "t_out", "t_in", "t_k", "t_mf"):
+        setattr(d, f, keep[f].ctypes.data)
+    d.dim_out, d.dim_in = T.dim_out, T.dim_in
+    d.nk = T.nk
+    d.k_data_len = keep["k_data"].size if T.nk else 0
+    d.nm = T.nm
+    d.m_col_len = keep["m_col"].size if T.nm else 0
+    d.m_val_len = keep["m_val"].size if T.nm else 0
+    d.npart = int(npart)
+    d.nmf = T.nmf
+    d.nterm = T.nterm
+    d.maxorder = int(maxorder)
+    return d
+
+
+def check_desc(T, npart, maxorder=100):
+    """kr_op_check of the descriptor of T on the host (no device): raises
+    KrylovError with the library's message if kr_op_create would refuse it."""
+    d = make_desc(T, npart, maxorder)
+    buf = ctypes.create_string_buffer(256)
+    rc = _native.lib().kr_op_check(ctypes.byref(d), buf, len(buf))
+    if rc != _native.KR_OK:
+        raise _native.KrylovError(rc, buf.value.decode(errors="replace"))
+
+
 def field_arrays(part_carts, part_states, coef=None, scale=None, thresh=None):
     """The field input of kr_set_field (and of one step of a field schedule):
     coef[p, c] = the field product of part p's Cartesian component c (in the
@@ -366,26 +401,7 @@ class OperatorPlan:
         self.tables = T
         self.nblock, self.dim_out, self.dim_in = T.nblock, T.dim_out, T.dim_in
         self.split, self.slab_parent, self.part_carts = T.split, T.slab_parent, T.part_carts
-        keep = T.arrays
-        out_dm, in_dm = keep["out_dm"], keep["in_dm"]
-        d = _native.kr_op_desc()
-        d.nslab_out, d.nslab_in = len(out_dm), len(in_dm)
-        if self.split:
-            d.out_stride, d.in_stride = keep["out_stride"].ctypes.data, keep["in_stride"].ctypes.data
-        for f in ("out_dm", "out_dk", "out_off", "in_dm", "in_dk", "in_off", "k_off", "k_rows", "k_cols",
-                  "k_type", "k_data", "m_rows", "m_width", "m_ncart", "m_col_off", "m_val_off", "m_col",
-                  "m_val", "mf_group", "mf_part", "t_out", "t_in", "t_k", "t_mf"):
-            setattr(d, f, keep[f].ctypes.data)
-        d.dim_out, d.dim_in = self.dim_out, self.dim_in
-        d.nk = T.nk
-        d.k_data_len = keep["k_data"].size if T.nk else 0
-        d.nm = T.nm
-        d.m_col_len = keep["m_col"].size if T.nm else 0
-        d.m_val_len = keep["m_val"].size if T.nm else 0
-        d.npart = len(self.sources)
-        d.nmf = T.nmf
-        d.nterm = T.nterm
-        d.maxorder = int(maxorder)
+        d = make_desc(T, len(self.sources), maxorder)
         self.nterm = T.nterm
         self.maxorder = int(maxorder)
         h = ctypes.c_void_p()
