@@ -32,5 +32,8 @@ def test_wait_nothing_ends_gives_up_with_timeout_status():
         v, _ = td.update(wl.hamiltonian(t), H0=wl.h0, vecs=v, inplace=True, check=False)
     torch.cuda.synchronize()
     nrm = torch.linalg.vector_norm(v, dim=1).cpu().numpy()
-    assert np.allclose(nrm, np.linalg.norm(v0, axis=1), rtol=0, atol=1e-12)
+    # the Lanczos stopping test (squared distance of successive solutions below
+    # tol = 1e-15, tdse.py:476) leaves each step's last correction up to
+    # sqrt(1e-15) ~ 3.2e-8, so five steps keep the norms to about 1.6e-7
+    assert np.allclose(nrm, np.linalg.norm(v0, axis=1), rtol=0, atol=1e-7)
     assert float((v - torch.from_numpy(v0).cuda()).abs().max()) > 1e-6  # the steps moved the states
