@@ -72,3 +72,13 @@ def test_reference_arm_line_keeps_the_contract():
     assert out["e2e"]["h2d_bytes_per_step"] == 0 and out["e2e"]["d2h_bytes_per_step"] == 0
     assert out["cpu_baseline"]["kind"] == "port" and out["cpu_baseline"]["cores"] >= 1
     json.dumps(out)
+
+
+def test_bench_defaults_keep_the_timing_rules():
+    """With no flags: one GPU, at least 3 warm-up steps, a bounded number of
+    timed steps (50 steps of about 26 ms: the timed work stays near a second)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    args = bench.parse([])
+    assert args.gpus == 1 and args.impl == "ours"
+    assert args.warmup >= 3 and 1 <= args.steps <= 200
