@@ -204,17 +204,23 @@ def cpu_reference_rate(wl, seconds, max_steps=None, warmup=1, vec=None):
     return v.shape[0] * n / t_run, n, t_run
 
 
+SINGLE_THREAD_ENV = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS", "BLIS_NUM_THREADS",
+                     "VECLIB_MAXIMUM_THREADS", "NUMEXPR_NUM_THREADS")
+
+
 def _reference_worker(args):
-    """One host process: one vector of the ensemble workload (spawned)."""
+    """One host process: one vector of the ensemble workload (spawned; its
+    BLAS thread pools are limited to one thread by the environment the parent
+    set before starting the pool, which a spawned child reads when it imports
+    numpy)."""
     jmax, nvec, idx, seconds, max_steps, warmup = args
-    os.environ.setdefault("OMP_NUM_THREADS", "1")
     sys.path.insert(0, ROOT)
     from richmol_gb300 import workloads
     wl, ens = workloads.thermal_asym_top(Jmax=jmax, nvec=nvec)
     v = np.zeros(wl.dim, np.complex128)
     v[ens.index[idx % nvec]] = 1.0
     rate, n, t = cpu_reference_rate(wl, seconds, max_steps=max_steps, warmup=warmup, vec=v)
-    return n, t
+    return n, t, {k: os.environ.get(k) for k in SINGLE_THREAD_ENV}
 
 
 # ---------------------------------------------------------------------------
@@ -641,13 +647,27 @@ def run_reference(args, ws, rank, local):
     warm = max(1, min(args.warmup, 10))  # untimed steps per process (bounded: each is ~0.5 s of CPU)
     budget = 60.0
     ctxm = mp.get_context("spawn")
+    # one thread per process: the children import numpy (and its BLAS) at
+    # start-up, before any code of theirs runs, so the limit goes into the
+    # environment they inherit
+    saved = {k: os.environ.get(k) for k in SINGLE_THREAD_ENV}
+    os.environ.update({k: "1" for k in SINGLE_THREAD_ENV})
     t0 = time.perf_counter()
-    with ctxm.Pool(nproc) as pool:
-        res = pool.map(_reference_worker, [(args.jmax, args.nvec, i, budget, per_steps, warm) for i in range(nproc)])
+    try:
+        with ctxm.Pool(nproc) as pool:
+            res = pool.map(_reference_worker,
+                           [(args.jmax, args.nvec, i, budget, per_steps, warm) for i in range(nproc)])
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
     wall = time.perf_counter() - t0
-    steps = sum(n for n, _ in res)
-    busy = max(t for _, t in res)
+    steps = sum(r[0] for r in res)
+    busy = max(r[1] for r in res)
     rate = steps / busy
+    threads = sorted({str(r[2].get("OMP_NUM_THREADS")) for r in res})
     return {
         "impl": "reference", "metric": METRIC, "value": round(rate, 3), "unit": UNIT, "n_gpus": ws,
         "steps": per_steps, "warmup": warm, "ms_per_step": round(busy * 1e3 / per_steps, 1),
@@ -657,7 +677,9 @@ def run_reference(args, ws, rank, local):
                                f"{args.nvec} vectors (sampled: {nproc} vectors x {per_steps} steps)",
                    "jmax": args.jmax, "nvec": args.nvec},
         "cpu_baseline": {"value": round(rate, 3), "unit": UNIT, "cores": nproc, "kind": "port",
-                         "sample": f"{nproc} processes x {per_steps} steps, one vector each, wall {wall:.0f} s "
+                         "threads_per_process": threads,
+                         "sample": f"{nproc} processes x {per_steps} steps, one vector each, one BLAS/OpenMP "
+                                   f"thread per process, wall {wall:.0f} s "
                                    "(incl. factor build); the reference does not install here "
                                    "(numpy.distutils, Fortran extensions), its algorithm runs as the numpy/scipy "
                                    "restatement"},

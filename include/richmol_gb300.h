@@ -10,8 +10,8 @@
  *   richmol/field.py:1145-1245 CarTens.vec     (Kronecker mat-vec)
  *
  * The reference has no FFI for this path (it is pure Python over scipy); the
- * entry points below are what its Python layer binds through ctypes, see
- * INTEGRATION.md. Conventions:
+ * entry points below are what its Python layer binds through ctypes
+ * (richmol_gb300/_native.py is such a binding). Conventions:
  *
  *   - every function returns an int status (KR_OK == 0); no exception or C++
  *     type crosses the boundary; kr_last_error() gives the message;
@@ -233,7 +233,10 @@ int kr_step(kr_op* op, void* states, int64_t nvec, const void* phase,
  *   - all calls share the array and it keeps the previous call's contents:
  *     calls that overlap on the GPU (other streams, other threads) race;
  *   - with korder == NULL a device-side error is copied into op's status and
- *     reported by kr_sync_status. */
+ *     reported by kr_sync_status;
+ *   - an error still pending in op's status (an earlier call with
+ *     korder == NULL) makes the call skip its work, as kr_step does;
+ *   - the caller's current device is the same after the call as before. */
 int kr_step_static(kr_op* op, void* states, int64_t nvec, const void* phase,
                    double fac_re, double fac_im, double tol, uint32_t flags,
                    int32_t* korder, void* stream);

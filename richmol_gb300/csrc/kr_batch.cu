@@ -568,7 +568,7 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
     return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_batch_create: bad argument (2 <= mmax <= 31)");
   *out = nullptr;
   if (!op->square) return set_err(op->ctx, KR_ERR_ARG, "kr_batch_create: operator is not square");
-  KR_CUDA(op->ctx, cudaSetDevice(op->ctx->device));
+  KR_DEVICE_SCOPE(op->ctx, op->ctx->device);
   // the batched mat-vec supports n_k <= 32 and ELL widths <= 16
   std::vector<int> dk(op->dev.nslab_out), dm(op->dev.nslab_out);
   KR_CUDA(op->ctx, cudaMemcpy(dk.data(), op->dev.out_dk, sizeof(int) * dk.size(), cudaMemcpyDeviceToHost));

@@ -1088,7 +1088,7 @@ __global__ void __launch_bounds__(128) kb_mma_probe(const float* A, const float*
 
 extern "C" int kr_probe_mma(kr_ctx* ctx, const float* a, const float* b, float* d) {
   if (!ctx || !a || !b || !d) return set_err(ctx, KR_ERR_ARG, "kr_probe_mma: NULL argument");
-  KR_CUDA(ctx, cudaSetDevice(ctx->device));
+  KR_DEVICE_SCOPE(ctx, ctx->device);
   const size_t na = 128 * 16, nbb = 16 * 16, nd = 128 * 16;
   char* buf = nullptr;
   KR_CUDA(ctx, cudaMalloc(&buf, sizeof(float) * (na + nbb + nd) + 16));

@@ -62,6 +62,26 @@ int kr_set_err(kr_ctx* ctx, int code, const std::string& msg);
       return set_err((ctx), KR_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
   } while (0)
 
+// Makes a device current for the rest of a call and gives the caller's current
+// device back when the call returns (on every path), so no entry point leaves
+// a side effect on the calling thread's device.
+struct DeviceScope {
+  int prev = -1;
+  cudaError_t err = cudaSuccess;
+  explicit DeviceScope(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) err = cudaSetDevice(dev);
+  }
+  ~DeviceScope() {
+    if (prev >= 0 && err == cudaSuccess) cudaSetDevice(prev);
+  }
+  DeviceScope(const DeviceScope&) = delete;
+  DeviceScope& operator=(const DeviceScope&) = delete;
+};
+#define KR_DEVICE_SCOPE(ctx, dev) \
+  DeviceScope _kr_dev_scope(dev); \
+  KR_CUDA(ctx, _kr_dev_scope.err)
+
 struct kr_op {
   kr_ctx* ctx = nullptr;
   DevOp dev{};

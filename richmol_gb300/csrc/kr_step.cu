@@ -749,8 +749,9 @@ extern "C" int kr_ctx_create(int device, kr_ctx** out) {
   if (e != cudaSuccess || ndev == 0)
     return set_err(nullptr, KR_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
   if (device < 0 || device >= ndev) return set_err(nullptr, KR_ERR_ARG, "kr_ctx_create: bad device index");
-  e = cudaSetDevice(device);
-  if (e != cudaSuccess) return set_err(nullptr, KR_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+  DeviceScope scope(device);
+  if (scope.err != cudaSuccess)
+    return set_err(nullptr, KR_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(scope.err));
   kr_ctx* c = new kr_ctx();
   c->device = device;
   cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
@@ -961,7 +962,7 @@ extern "C" int kr_op_check(const kr_op_desc* d, char* buf, size_t len) {
 extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   if (!ctx || !d || !out) return set_err(ctx, KR_ERR_ARG, "kr_op_create: NULL argument");
   *out = nullptr;
-  KR_CUDA(ctx, cudaSetDevice(ctx->device));
+  KR_DEVICE_SCOPE(ctx, ctx->device);
   // ---- validation (check_desc) -----------------------------------------------
   DescCheck dchk;
   {
@@ -1553,7 +1554,7 @@ __global__ void kr_fp32_probe_kernel(float* out, int iters, float a, float b) {
 
 extern "C" int kr_probe_fp32(kr_ctx* ctx, double* tflops) {
   if (!ctx || !tflops) return set_err(ctx, KR_ERR_ARG, "kr_probe_fp32: NULL argument");
-  KR_CUDA(ctx, cudaSetDevice(ctx->device));
+  KR_DEVICE_SCOPE(ctx, ctx->device);
   const int blocks = ctx->nsm * 8, threads = 256, iters = 65536;
   float* out = nullptr;
   KR_CUDA(ctx, cudaMalloc(&out, sizeof(float) * blocks * threads));
@@ -1577,7 +1578,7 @@ extern "C" int kr_probe_fp32(kr_ctx* ctx, double* tflops) {
 
 extern "C" int kr_probe_fp64(kr_ctx* ctx, double* tflops) {
   if (!ctx || !tflops) return set_err(ctx, KR_ERR_ARG, "kr_probe_fp64: NULL argument");
-  KR_CUDA(ctx, cudaSetDevice(ctx->device));
+  KR_DEVICE_SCOPE(ctx, ctx->device);
   const int blocks = ctx->nsm * 8, threads = 256, iters = 4096;
   double* out = nullptr;
   KR_CUDA(ctx, cudaMalloc(&out, sizeof(double) * blocks * threads));
@@ -1615,7 +1616,7 @@ __global__ void kr_wait_probe_kernel(unsigned* bar, int* status, unsigned long l
 
 extern "C" int kr_probe_wait(kr_ctx* ctx, int32_t* status, double* waited_s) {
   if (!ctx || !status || !waited_s) return set_err(ctx, KR_ERR_ARG, "kr_probe_wait: NULL argument");
-  KR_CUDA(ctx, cudaSetDevice(ctx->device));
+  KR_DEVICE_SCOPE(ctx, ctx->device);
   // bar[2] (count, generation), status, pad, out[2]
   void* buf = nullptr;
   KR_CUDA(ctx, cudaMalloc(&buf, 32));
@@ -1716,8 +1717,9 @@ extern "C" int kr_step_static(kr_op* op, void* states, int64_t nvec, const void*
   {
     std::lock_guard<std::mutex> lk(g_static_mu);
     if (!g_static_addr[dev]) {
-      // set-up, once per device, with that device current
-      KR_CUDA(op->ctx, cudaSetDevice(dev));
+      // set-up, once per device, with that device current (the caller's
+      // current device is given back when the scope ends)
+      KR_DEVICE_SCOPE(op->ctx, dev);
       void* p = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&p, g_kr_static_scratch);
       if (e != cudaSuccess || !p)
@@ -1761,8 +1763,12 @@ extern "C" int kr_step_static(kr_op* op, void* states, int64_t nvec, const void*
   a.maxorder = op->maxorder;
   a.dim = n;
   // the array keeps the previous call's contents: clear the arrival count and
-  // the status word (task counters are cleared by the kernel itself)
+  // the status word (task counters are cleared by the kernel itself), then
+  // take over an error still pending in the operator's own status word, so
+  // that, as kr_step does, the call skips its work until kr_sync_status has
+  // reported that error
   KR_CUDA(op->ctx, cudaMemsetAsync(status, 0, 2 * sizeof(int), st));
+  KR_CUDA(op->ctx, cudaMemcpyAsync(status, op->status, sizeof(int), cudaMemcpyDeviceToDevice, st));
   for (int64_t v = 0; v < nvec; ++v) {
     a.state = (double2*)states + v * n;
     KR_CUDA(op->ctx, cudaMemsetAsync(bar, 0, sizeof(unsigned), st));
@@ -1777,6 +1783,9 @@ extern "C" int kr_step_static(kr_op* op, void* states, int64_t nvec, const void*
       KR_CUDA(op->ctx, cudaStreamSynchronize(st));
       korder[v] = hs[1];
       if (hs[0] != 0) {
+        // reported here: the operator's status word no longer holds it (as kr_step)
+        cudaMemsetAsync(op->status, 0, sizeof(int), st);
+        cudaStreamSynchronize(st);
         if (hs[0] == KR_ERR_MAXORDER)
           return set_err(op->ctx, KR_ERR_MAXORDER,
                          "Lanczos reached maximum order of '" + std::to_string(op->maxorder) + "' without convergence");
@@ -1837,7 +1846,7 @@ extern "C" int kr_seg_create(kr_op* op, int32_t nseg, const int32_t* slab_seg, k
   if (!op || !slab_seg || !out || nseg <= 0) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_seg_create: bad argument");
   *out = nullptr;
   if (!op->square || op->split) return set_err(op->ctx, KR_ERR_ARG, "kr_seg_create: operator is not square or has column chunks");
-  KR_CUDA(op->ctx, cudaSetDevice(op->ctx->device));
+  KR_DEVICE_SCOPE(op->ctx, op->ctx->device);
   const DevOp& D = op->dev;
   const int ns = D.nslab_out;
   std::vector<long long> off(ns);

@@ -71,6 +71,8 @@ def test_reference_arm_line_keeps_the_contract():
     assert out["e2e"]["value"] == out["value"]
     assert out["e2e"]["h2d_bytes_per_step"] == 0 and out["e2e"]["d2h_bytes_per_step"] == 0
     assert out["cpu_baseline"]["kind"] == "port" and out["cpu_baseline"]["cores"] >= 1
+    # every spawned process ran its BLAS with one thread (one process per core)
+    assert out["cpu_baseline"]["threads_per_process"] == ["1"]
     json.dumps(out)
 
 
