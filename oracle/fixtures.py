@@ -81,3 +81,22 @@ def init_rows(d, lab):
     v = np.zeros(shape, dtype=np.complex128)
     v[d[lab + "/rows"], d[lab + "/cols"]] = d[lab + "/vals"]
     return v
+
+
+def from_cartens(T):
+    """Oracle copy of a tensor made by the in-house factor builder
+    (richmol_gb300.CarTens with one factor source): the same K and M blocks in
+    an OCarTens, the part's scale applied as the reference's mul() would
+    (field.py:932-1070). Test infrastructure: lets the oracle propagate the
+    builder's operators at sizes the reference cannot build here."""
+    src = T._parts[0].src
+    o = OCarTens()
+    for k in ("Jlist1", "Jlist2", "symlist1", "symlist2", "dim_m1", "dim_m2", "dim_k1", "dim_k2", "dim1", "dim2",
+              "mmat", "rank"):
+        setattr(o, k, getattr(src, k))
+    # own copy of the K dictionaries: mul() replaces their entries
+    o.kmat = {Jp: {sp: dict(kS) for sp, kS in kJ.items()} for Jp, kJ in src.kmat.items()}
+    o.cart = src.carts
+    if T._parts[0].kscale != 1:
+        o.mul(T._parts[0].kscale)
+    return o

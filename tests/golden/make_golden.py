@@ -469,7 +469,199 @@ def case_trunc_pulse(nsteps=3000):
     save("trunc_pulse_j10", out, meta)
 
 
+def slab_populations(T, vecs):
+    """J-populations of each row of vecs: sum of |v|^2 over the slabs of each J
+    (the observable of tests/test_tdse.py:63-67), as an (nvec, nJ) array."""
+    out = np.zeros((vecs.shape[0], len(T.Jlist1)))
+    for v in range(vecs.shape[0]):
+        d = split(T, vecs[v], "1")
+        for iJ, J in enumerate(T.Jlist1):
+            out[v, iJ] = sum(float(np.sum(np.abs(d[J][s]) ** 2)) for s in T.symlist1[J])
+    return out
+
+
+def expect_rows(mat, vecs):
+    """<v|O|v> of each row (complex)."""
+    return np.array([np.vdot(v, mat.dot(v)) for v in vecs])
+
+
+def case_ocs_c1(nsteps=300):
+    """The CPU-runnable configuration as configured: linear OCS (C-O 1.16 A,
+    C-S 1.56 A), mu_z 0.28 au, alpha diag(35, 35, 80) au, J = 0..20 with all M
+    (dim 441), |J=0,M=0>, z-polarised cycle-averaged Gaussian pulse 5e11 W/cm^2,
+    FWHM 300 fs at 1 ps, 0-3 ps at dt = 10 fs (300 steps), split operator with
+    the reference's internal Lanczos (its expokit path, whose Krylov dimension
+    is 12, needs the Fortran extension). Per step: <cos^2>, <cos> and the
+    J-populations; states every 10 steps."""
+    out, meta = {}, {"Jmax": 20}
+    mol = ocs_molecule()
+    sol = solve(mol, Jmax=20)
+    h0 = LabTensor(mol, sol)
+    pol = LabTensor(mol.pol, sol)
+    cos2 = LabTensor("cos2theta", sol)
+    cos = LabTensor("costheta", sol)
+    for nm, T in (("h0", h0), ("pol", pol), ("cos2", cos2), ("cos", cos)):
+        export_cartens(T, nm, out, meta, with_mfmat=False)
+    scale = -0.5 * AUpol_x_Vm_to_invcm()
+    meta["scale"] = scale
+    Hac = pol * scale
+    tdse = TDSE(t_start=0.0, t_end=nsteps * 0.01, dt=0.01, t_units="ps", enr_units="invcm")
+    tgrid = tdse.time_grid()
+    vecs = tdse.init_state(h0, temp=0)
+    out["vec0"] = vecs.copy()
+    c2 = cos2.tomat(form="full", cart="0")
+    c1 = cos.tomat(form="full", cart="0")
+    fields, saved, saved_steps, cos2_t, cos_t, pops, times = [], [], [], [], [], [], []
+    t0 = time.time()
+    for i, t in enumerate(tgrid):
+        f = gaussian_field(t, 1.0, 0.3, 5e11, [0, 0, 1])
+        Hac.field(f)
+        vecs, t2 = tdse.update(Hac, H0=h0, vecs=vecs)
+        fields.append(f)
+        times.append(t2)
+        cos2_t.append(expect_rows(c2, vecs).real.sum() + 1 / 3)
+        cos_t.append(expect_rows(c1, vecs).real.sum())
+        pops.append(slab_populations(h0, vecs).sum(axis=0))
+        if i % 10 == 9 or i < 3:
+            saved.append(vecs[0].copy())
+            saved_steps.append(i)
+    print("ocs c1 replay", time.time() - t0, "s")
+    out["fields"] = np.array(fields)
+    out["times"] = np.array(times)
+    out["tc"] = np.asarray(tgrid)
+    out["cos2"] = np.array(cos2_t)
+    out["cos"] = np.array(cos_t)
+    out["pops"] = np.array(pops)
+    out["states"] = np.array(saved)
+    out["state_steps"] = np.array(saved_steps)
+    meta["tdse"] = dict(t_start=0.0, t_end=nsteps * 0.01, dt=0.01)
+    meta["pulse"] = dict(t0=1.0, fwhm=0.3, intensity=5e11, direction=[0, 0, 1])
+    save("ocs_c1_j20", out, meta)
+
+
+def case_asym_j10(nsteps=50):
+    """The asymmetric top of the larger configurations (A, B, C = 9.0, 5.0,
+    3.2 cm^-1, Watson A, D2, mu (0, 0, -0.73) au, alpha diag(9.1, 9.9, 9.4) au) at
+    J = 0..10 (dim 1,771): DC 20 kV/cm along z plus the 1e12 W/cm^2 FWHM 500 fs
+    pulse at 35 deg, dt = 5 fs, 50 steps through the pulse maximum at 1 ps, from
+    the T = 5 K ensemble (thresh 1e-3). Per step and vector: <cos^2>, <cos>,
+    J-populations; states of two vectors every 10 steps, all vectors at the end."""
+    out, meta = {}, {"Jmax": 10}
+    mol = asym_molecule()
+    sol = solve(mol, Jmax=10)
+    t0 = time.time()
+    h0 = LabTensor(mol, sol, thresh=1e-9)
+    dip = LabTensor(mol.dip, sol)
+    pol = LabTensor(mol.pol, sol)
+    cos2 = LabTensor("cos2theta", sol)
+    cos = LabTensor("costheta", sol)
+    print("asym j10 factors", time.time() - t0, "s")
+    for nm, T in (("h0", h0), ("dip", dip), ("pol", pol), ("cos2", cos2), ("cos", cos)):
+        export_cartens(T, nm, out, meta, with_mfmat=False)
+    out["enr"] = np.concatenate([np.asarray(sol[J][s].enr) for J in sol.keys() for s in sol[J].keys()])
+    meta["enr_keys"] = [[int(J), str(s), len(sol[J][s].enr)] for J in sol.keys() for s in sol[J].keys()]
+    dc = [0.0, 0.0, 20e3 * 1e2]
+    beta = np.deg2rad(35.0)
+    direction = [np.sin(beta), 0, np.cos(beta)]
+    Hdc = -1 * dip * dc * AUdip_x_Vm_to_invcm()
+    Hac = -0.5 * pol * AUpol_x_Vm_to_invcm()
+    meta["dc"] = dc
+    meta["scales"] = dict(dc=-1 * AUdip_x_Vm_to_invcm(), ac=-0.5 * AUpol_x_Vm_to_invcm())
+    t_start = 1.0 - nsteps * 0.005 / 2
+    tdse = TDSE(t_start=t_start, t_end=t_start + nsteps * 0.005, dt=0.005, t_units="ps", enr_units="invcm")
+    tgrid = tdse.time_grid()
+    vecs = tdse.init_state(h0, temp=5, thresh=1e-3)
+    out["vec0"] = vecs.copy()
+    c2 = cos2.tomat(form="full", cart="0")
+    c1 = cos.tomat(form="full", cart="0")
+    fields, saved, saved_steps, cos2_t, cos_t, pops = [], [], [], [], [], []
+    t0 = time.time()
+    for i, t in enumerate(tgrid):
+        f = gaussian_field(t, 1.0, 0.5, 1e12, direction)
+        Hac.field(f)
+        vecs, _ = tdse.update(Hdc + Hac, H0=h0, vecs=vecs)
+        fields.append(f)
+        cos2_t.append(expect_rows(c2, vecs).real)
+        cos_t.append(expect_rows(c1, vecs).real)
+        pops.append(slab_populations(h0, vecs))
+        if i % 10 == 9:
+            saved.append(vecs[:2].copy())
+            saved_steps.append(i)
+    print("asym j10 replay", time.time() - t0, "s,", vecs.shape[0], "vectors")
+    out["fields"] = np.array(fields)
+    out["tc"] = np.asarray(tgrid)
+    out["cos2"] = np.array(cos2_t)        # (nsteps, nvec), without the 1/3
+    out["cos"] = np.array(cos_t)          # (nsteps, nvec)
+    out["pops"] = np.array(pops)          # (nsteps, nvec, nJ)
+    out["states"] = np.array(saved)       # (nsaved, 2, dim)
+    out["state_steps"] = np.array(saved_steps)
+    out["final"] = vecs.copy()
+    meta["tdse"] = dict(t_start=t_start, t_end=t_start + nsteps * 0.005, dt=0.005)
+    meta["pulse"] = dict(t0=1.0, fwhm=0.5, intensity=1e12, direction=direction)
+    save("asym_j10", out, meta)
+
+
+def c1_molecule():
+    """An asymmetric top without symmetry (C1), drawn like the uneven-size
+    batch's molecules: rotational constants (Bx, By, Bz) = (2.3, 0.71, 0.38)
+    cm^-1, dipole (0.31, -0.52, 0.17) au, a non-diagonal symmetric positive
+    definite polarizability (eigenvalues 12, 37, 81 au)."""
+    m = Molecule()
+    m.B = (2.3, 0.71, 0.38)
+    m.sym = "C1"
+    m.dip = [0.31, -0.52, 0.17]
+    q, _ = np.linalg.qr(np.random.default_rng(11).standard_normal((3, 3)))
+    p = q @ np.diag([12.0, 37.0, 81.0]) @ q.T
+    m.pol = ((p + p.T) / 2).tolist()
+    return m
+
+
+def case_c1_j10(nsteps=10):
+    """Factors of a C1 molecule at J = 0..10 (dim 1,771; n_k = 2J + 1) for the
+    factor builder, and a short propagation from its T = 2 K ensemble under a
+    tilted pulse (the C1 propagation of the uneven-size and serving workloads)."""
+    out, meta = {}, {"Jmax": 10}
+    mol = c1_molecule()
+    sol = solve(mol, Jmax=10)
+    t0 = time.time()
+    h0 = LabTensor(mol, sol, thresh=1e-9)
+    dip = LabTensor(mol.dip, sol)
+    pol = LabTensor(mol.pol, sol)
+    cos2 = LabTensor("cos2theta", sol)
+    print("c1 j10 factors", time.time() - t0, "s")
+    for nm, T in (("h0", h0), ("dip", dip), ("pol", pol), ("cos2", cos2)):
+        export_cartens(T, nm, out, meta, with_mfmat=False)
+    out["enr"] = np.concatenate([np.asarray(sol[J][s].enr) for J in sol.keys() for s in sol[J].keys()])
+    meta["enr_keys"] = [[int(J), str(s), len(sol[J][s].enr)] for J in sol.keys() for s in sol[J].keys()]
+    meta["mol"] = dict(B=list(mol.B), dip=list(map(float, mol.dip)), pol=np.asarray(mol.pol).tolist())
+    direction = [0.48, -0.36, 0.8]
+    Hac = -0.5 * pol * AUpol_x_Vm_to_invcm()
+    meta["scale"] = -0.5 * AUpol_x_Vm_to_invcm()
+    tdse = TDSE(t_start=0.45, t_end=0.45 + nsteps * 0.01, dt=0.01, t_units="ps", enr_units="invcm")
+    tgrid = tdse.time_grid()
+    vecs = tdse.init_state(h0, temp=2, thresh=1e-2)
+    out["vec0"] = vecs.copy()
+    c2 = cos2.tomat(form="full", cart="0")
+    fields, cos2_t = [], []
+    for t in tgrid:
+        f = gaussian_field(t, 0.5, 0.2, 3e12, direction)
+        Hac.field(f)
+        vecs, _ = tdse.update(Hac, H0=h0, vecs=vecs)
+        fields.append(f)
+        cos2_t.append(expect_rows(c2, vecs).real)
+    out["fields"] = np.array(fields)
+    out["tc"] = np.asarray(tgrid)
+    out["cos2"] = np.array(cos2_t)        # (nsteps, nvec), without the 1/3
+    out["final"] = vecs[:4].copy()        # the first four vectors (the file stays small)
+    meta["tdse"] = dict(t_start=0.45, t_end=0.45 + nsteps * 0.01, dt=0.01)
+    meta["pulse"] = dict(t0=0.5, fwhm=0.2, intensity=3e12, direction=direction)
+    save("c1_j10", out, meta)
+
+
 CASES = {
+    "ocs_c1": case_ocs_c1,
+    "asym_j10": case_asym_j10,
+    "c1_j10": case_c1_j10,
     "ocs_small": case_ocs_small,
     "asym_small": case_asym_small,
     "lanczos": case_lanczos,

@@ -24,11 +24,59 @@ def _mol_asym():
                         dip=[0, 0, -0.73], pol=np.diag([9.1, 9.9, 9.4]))
 
 
+def _mol_c1():
+    """The C1 molecule of tests/golden/c1_j10.npz (its parameters are in the
+    fixture's meta, written by make_golden.py's c1_molecule)."""
+    import json
+    from richmol_gb300 import rot
+    m = json.loads(str(np.load(os.path.join(GOLDEN, "c1_j10.npz"))["meta"]))["mol"]
+    return rot.Molecule(B=tuple(m["B"]), sym="C1", dip=m["dip"], pol=np.array(m["pol"]))
+
+
 CASES = [
     ("ocs_j6.npz", _mol_ocs, 6, ["dip", "pol", "cos2", "cos", "h0"]),
     ("asym_j4.npz", _mol_asym, 4, ["dip", "pol", "cos2", "h0"]),
+    ("asym_j10.npz", _mol_asym, 10, ["dip", "pol", "cos2", "cos", "h0"]),
+    ("c1_j10.npz", _mol_c1, 10, ["dip", "pol", "cos2", "h0"]),
 ]
 ARGS = {"cos2": "cos2theta", "cos": "costheta", "h0": "h0"}
+
+
+# Eigenvalues of one (J, sym) closer than this (cm^-1) form a cluster: inside
+# it the eigenvectors are fixed only up to a unitary mixing whose size is the
+# eigensolver's round-off over the gap (near-prolate C1 tops have K doublets
+# split by 1e-10 cm^-1 at J = 10), so K factors are compared there through
+# invariants of that mixing (singular values of each cluster-pair sub-block).
+CLUSTER_GAP = 1e-2
+
+
+def _clusters(e):
+    order = np.argsort(e, kind="stable")
+    out, cur = [], [int(order[0])]
+    for a, b in zip(order[:-1], order[1:]):
+        if e[b] - e[a] < CLUSTER_GAP:
+            cur.append(int(b))
+        else:
+            out.append(cur)
+            cur = [int(b)]
+    out.append(cur)
+    return out
+
+
+def _k_equivalent(a, b, ca, cb, tol):
+    """|a| == |b| element by element outside multi-state clusters (signs and
+    phases of single eigenvectors are free); singular values of the
+    sub-blocks of clusters with more than one state."""
+    for ia in ca:
+        for ib in cb:
+            sa, sb = a[np.ix_(ia, ib)], b[np.ix_(ia, ib)]
+            if len(ia) == 1 and len(ib) == 1:
+                if abs(abs(sa[0, 0]) - abs(sb[0, 0])) > tol:
+                    return False
+            else:
+                if np.abs(np.linalg.svd(sa, compute_uv=False) - np.linalg.svd(sb, compute_uv=False)).max() > tol:
+                    return False
+    return True
 
 
 @pytest.mark.parametrize("case,mk,Jmax,names", CASES)
@@ -38,6 +86,14 @@ def test_factors_match_reference(case, mk, Jmax, names):
     d, meta = fixtures.load(os.path.join(GOLDEN, case))
     mol = mk()
     sol = rot.Solution(mol, Jmax=Jmax)
+    # reference energies per (J, sym), when the fixture holds them
+    enr, clus = {}, {}
+    if "enr_keys" in meta:
+        i = 0
+        for J, s, n in meta["enr_keys"]:
+            enr[(float(J), s)] = d["enr"][i: i + n]
+            i += n
+        clus = {k: _clusters(e) for k, e in enr.items()}
     for nm in names:
         ref = fixtures.tensor(d, meta, nm)
         arg = ARGS.get(nm, mol.dip if nm == "dip" else mol.pol)
@@ -54,7 +110,13 @@ def test_factors_match_reference(case, mk, Jmax, names):
                     except (KeyError, AttributeError):
                         # the reference keeps round-off blocks above machine epsilon
                         b = np.zeros_like(a)
-                    assert np.abs(np.abs(a) - np.abs(b)).max() < 1e-12 * max(1.0, np.abs(a).max()), (nm, Jp, sp, i)
+                    tol = 1e-12 * max(1.0, np.abs(a).max())
+                    k1, k2 = (float(Jp[0]), sp[0]), (float(Jp[1]), sp[1])
+                    if k1 in clus and k2 in clus and a.shape == (len(enr[k1]), len(enr[k2])):
+                        assert _k_equivalent(a, b, clus[k1], clus[k2], 1e-10 * max(1.0, np.abs(a).max())), \
+                            (nm, Jp, sp, i)
+                    else:
+                        assert np.abs(np.abs(a) - np.abs(b)).max() < tol, (nm, Jp, sp, i)
         for Jp in ref.mmat:
             for sp in ref.mmat[Jp]:
                 for i in ref.mmat[Jp][sp]:
@@ -64,11 +126,13 @@ def test_factors_match_reference(case, mk, Jmax, names):
                         assert np.abs(a - b).max() < 1e-14, (nm, Jp, sp, i, c)
 
 
-def test_energies_match_reference():
+@pytest.mark.parametrize("case,mk,Jmax", [("asym_j4.npz", _mol_asym, 4), ("asym_j10.npz", _mol_asym, 10),
+                                          ("c1_j10.npz", _mol_c1, 10)])
+def test_energies_match_reference(case, mk, Jmax):
     from oracle import fixtures
     from richmol_gb300 import rot
-    d, meta = fixtures.load(os.path.join(GOLDEN, "asym_j4.npz"))
-    sol = rot.Solution(_mol_asym(), Jmax=4)
+    d, meta = fixtures.load(os.path.join(GOLDEN, case))
+    sol = rot.Solution(mk(), Jmax=Jmax)
     i = 0
     for J, s, n in meta["enr_keys"]:
         e = sol.states[J][s][0]
