@@ -156,6 +156,13 @@ void kr_seg_destroy(kr_seg* seg);
  * Synchronises the stream; KR_ERR_MAXORDER if a segment reached maxorder. */
 int kr_seg_step(kr_seg* seg, void* states, const void* phase, double fac_re, double fac_im, double tol,
                 int32_t* korder, void* stream);
+/* Arithmetic of kr_seg_step's mat-vecs (no counterpart in the reference, which
+ * is FP64 throughout): KR_SEG_F64 (default), or KR_SEG_F32_MATVEC, the products
+ * in FP32 on the FP32 pipes from FP32 copies of the factors (complex64
+ * accuracy, about 1e-7 relative per mat-vec) with the states, Krylov vectors,
+ * Lanczos scalars, exponential and stopping test in FP64. */
+enum { KR_SEG_F64 = 0, KR_SEG_F32_MATVEC = 1 };
+int kr_seg_set_precision(kr_seg* seg, int32_t mode);
 int64_t kr_seg_launch_count(const kr_seg* seg);
 
 /* Context on one device. Replaces nothing in the reference (which keeps no
@@ -264,10 +271,25 @@ int kr_batch_store(kr_batch* b, void* states, void* stream);
 /* One TDSE.update of every vector (split operator when phase != NULL):
  * op carries H with its field set (kr_set_field); each vector stops at the
  * first Krylov order whose error estimate is <= tol (times nothing: absolute,
- * in the norm of the vector). *kmax_out: largest order used. Synchronises
- * once per Krylov iteration; KR_ERR_MAXORDER if a vector needs more than mmax. */
+ * in the norm of the vector). The Krylov loop runs on the device (a CUDA graph
+ * with a conditional WHILE node; the Krylov index lives in device memory), so
+ * the host takes no part between iterations:
+ *   - on a stream that is not capturing, the step is recorded once per
+ *     (op, phase, fac, tol, mat-vec kind) and launched as one graph;
+ *     kmax_out != NULL synchronises the stream, writes the largest order used
+ *     and returns a step error (KR_ERR_MAXORDER if a vector needs more than
+ *     mmax); kmax_out == NULL returns at once, errors wait for kr_batch_sync;
+ *   - on a capturing stream (the caller records its time loop into a CUDA
+ *     graph) the step's nodes go into the caller's graph; kmax_out must be
+ *     NULL and errors are read by kr_batch_sync after the replay.
+ * A pending error makes later steps leave the states unchanged until it has
+ * been read. */
 int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double fac_re, double fac_im,
                   double tol, int32_t* kmax_out, void* stream);
+/* Synchronises the stream and reports (and clears) the error of an earlier
+ * kr_batch_step; *kmax_out (optional): largest Krylov order of the last step.
+ * No counterpart in the reference (its steps are synchronous). */
+int kr_batch_sync(kr_batch* b, int32_t* kmax_out, void* stream);
 /* Krylov order used by each vector in the last step (host int32[nvec]). */
 int kr_batch_korder(kr_batch* b, int32_t* korder, void* stream);
 /* <v|O|v> for every vector (host complex128[nvec], interleaved), O = obs
@@ -281,9 +303,12 @@ int kr_batch_expect(kr_batch* b, kr_op* obs, double* out, void* stream);
 int kr_batch_populations(kr_batch* b, double* out, void* stream);
 /* Mat-vec kinds of a batch: KR_MATVEC_TENSOR (default) contracts the K
  * factors on the tensor cores (tcgen05, TF32 with split operands: about 2^-21
- * relative per product, FP32 accumulation); KR_MATVEC_FP32 runs every
- * product as an FP32 FMA. No counterpart in the reference (FP64 only). */
-enum { KR_MATVEC_TENSOR = 0, KR_MATVEC_FP32 = 1 };
+ * relative per product, FP32 accumulation), the A operands staged in shared
+ * memory; KR_MATVEC_TENSOR_TMEM the same products with the A operands written
+ * to tensor memory (tcgen05.st) and a deeper TMA ring of input rows in the
+ * shared memory this frees; KR_MATVEC_FP32 runs every product as an FP32
+ * FMA. No counterpart in the reference (FP64 only). */
+enum { KR_MATVEC_TENSOR = 0, KR_MATVEC_FP32 = 1, KR_MATVEC_TENSOR_TMEM = 2 };
 int kr_batch_set_matvec(kr_batch* b, int32_t kind);
 /* y = op x for nvec vectors with the batched complex64 mat-vec (CarTens.vec,
  * field.py:1145-1245, in single precision): x, y (nvec, dim) complex128
@@ -314,6 +339,9 @@ int kr_probe_fp32(kr_ctx* ctx, double* tflops);
  * 128 x 16, B 16 x 16, D 128 x 16, row-major FP32 host arrays read as TF32, by
  * one tcgen05.mma tile; checks the MMA building block of the batched mat-vec. */
 int kr_probe_mma(kr_ctx* ctx, const float* a, const float* b, float* d);
+/* The same product with A held in tensor memory (row m in TMEM lane m, written
+ * by tcgen05.st) instead of shared memory; no counterpart in the reference. */
+int kr_probe_mma_ta(kr_ctx* ctx, const float* a, const float* b, float* d);
 /* Failure-detection probe (no counterpart in the reference): the bounded grid
  * barrier of the step kernels in a launch of two CTAs of which one never
  * arrives (a rank that never joins). The other's wait gives up after its limit

@@ -26,7 +26,8 @@ KR_MAXCART = 9
 KR_MAXPART = 4096
 KR_PART_INLINE = 16  # parts whose field coefficients go as kernel parameters
 KR_STEP_SKIP_KRYLOV = 1
-KR_MATVEC_TENSOR, KR_MATVEC_FP32 = 0, 1
+KR_MATVEC_TENSOR, KR_MATVEC_FP32, KR_MATVEC_TENSOR_TMEM = 0, 1, 2
+KR_SEG_F64, KR_SEG_F32_MATVEC = 0, 1
 # bytes of per-step field input that travel host -> device (the field
 # coefficients, scales and thresholds of kr_set_field, passed as kernel
 # parameters): int npart (padded to 8) + 16 x 9 complex + 16 complex + 16 double
@@ -36,12 +37,12 @@ EXPORTED = [
     "kr_ctx_create", "kr_ctx_destroy", "kr_last_error", "kr_op_create", "kr_op_destroy", "kr_op_check",
     "kr_set_field", "kr_set_field_schedule", "kr_set_field_step",
     "kr_matvec", "kr_step", "kr_sync_status", "kr_op_launch_count", "kr_op_work",
-    "kr_probe_fp64", "kr_probe_fp32", "kr_probe_mma", "kr_probe_wait", "kr_step_static", "kr_static_scratch_bytes",
-    "kr_batch_create", "kr_batch_destroy", "kr_batch_load", "kr_batch_store", "kr_batch_step",
+    "kr_probe_fp64", "kr_probe_fp32", "kr_probe_mma", "kr_probe_mma_ta", "kr_probe_wait", "kr_step_static", "kr_static_scratch_bytes",
+    "kr_batch_create", "kr_batch_destroy", "kr_batch_load", "kr_batch_store", "kr_batch_step", "kr_batch_sync",
     "kr_batch_korder", "kr_batch_expect", "kr_batch_launch_count", "kr_batch_matvec", "kr_batch_apply", "kr_batch_set_matvec",
     "kr_batch_populations",
     "kr_expv", "kr_op_norm1", "kr_observables",
-    "kr_seg_create", "kr_seg_destroy", "kr_seg_step", "kr_seg_launch_count",
+    "kr_seg_create", "kr_seg_destroy", "kr_seg_step", "kr_seg_launch_count", "kr_seg_set_precision",
 ]
 
 
@@ -160,6 +161,8 @@ def lib():
         L.kr_batch_store.restype = ctypes.c_int
         L.kr_batch_step.argtypes = [vp, vp, vp, dbl, dbl, dbl, ctypes.POINTER(i32), vp]
         L.kr_batch_step.restype = ctypes.c_int
+        L.kr_batch_sync.argtypes = [vp, ctypes.POINTER(i32), vp]
+        L.kr_batch_sync.restype = ctypes.c_int
         L.kr_batch_korder.argtypes = [vp, vp, vp]
         L.kr_batch_korder.restype = ctypes.c_int
         L.kr_batch_expect.argtypes = [vp, vp, vp, vp]
@@ -178,6 +181,8 @@ def lib():
         L.kr_seg_step.restype = ctypes.c_int
         L.kr_seg_launch_count.argtypes = [vp]
         L.kr_seg_launch_count.restype = i64
+        L.kr_seg_set_precision.argtypes = [vp, i32]
+        L.kr_seg_set_precision.restype = ctypes.c_int
         L.kr_batch_matvec.argtypes = [vp, vp, vp]
         L.kr_batch_matvec.restype = ctypes.c_int
         L.kr_batch_launch_count.argtypes = [vp]
@@ -192,6 +197,8 @@ def lib():
         L.kr_observables.restype = ctypes.c_int
         L.kr_probe_mma.argtypes = [vp, vp, vp, vp]
         L.kr_probe_mma.restype = ctypes.c_int
+        L.kr_probe_mma_ta.argtypes = [vp, vp, vp, vp]
+        L.kr_probe_mma_ta.restype = ctypes.c_int
         L.kr_probe_wait.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(dbl)]
         L.kr_probe_wait.restype = ctypes.c_int
         L.kr_probe_fp64.argtypes = [vp, ctypes.POINTER(dbl)]

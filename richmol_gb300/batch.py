@@ -20,7 +20,8 @@ from . import _native
 from .device import stream_ptr
 
 
-_KINDS = {"tensor": _native.KR_MATVEC_TENSOR, "fp32": _native.KR_MATVEC_FP32}
+_KINDS = {"tensor": _native.KR_MATVEC_TENSOR, "fp32": _native.KR_MATVEC_FP32,
+          "tensor_tmem": _native.KR_MATVEC_TENSOR_TMEM}
 
 
 class Ensemble:
@@ -34,14 +35,17 @@ class Ensemble:
         mmax : int                  maximum Krylov order (<= 31)
         matvec : str                "tensor" (default): K contractions on the tensor cores
                                     as split-TF32 MMAs (about 2^-21 relative per product);
-                                    "fp32": every product an FP32 FMA; "auto": at the first
-                                    step both kernels (tensor-core tiles of 64/KP rows x 128
-                                    vectors, SIMT tiles of 128/NKP rows x 32 vectors) are
-                                    timed on that step's operator and the faster one is
-                                    kept (``self.tuned``: ms per mat-vec of each)
+                                    "tensor_tmem": the same with the A operands in tensor
+                                    memory; "fp32": every product an FP32 FMA; "auto": at
+                                    the first step the kind is picked by richmol_gb300.tune
+                                    (the cached choice for this operator shape and vector
+                                    count, else every kind timed on that step's operator and
+                                    the fastest kept and cached; ``self.tuned``: ms per
+                                    mat-vec of each)
+        tune_cache : bool           "auto" reads and writes the tuning cache file
     """
 
-    def __init__(self, tdse, H0, nvec, tol=1e-8, mmax=20, template=None, matvec="tensor"):
+    def __init__(self, tdse, H0, nvec, tol=1e-8, mmax=20, template=None, matvec="tensor", tune_cache=True):
         self.tdse = tdse
         self.H0 = H0
         self.nvec = int(nvec)
@@ -57,10 +61,12 @@ class Ensemble:
         h = ctypes.c_void_p()
         _native.check(_native.lib().kr_batch_create(self._plan0.op, self.nvec, self.mmax, ctypes.byref(h)), self.ctx)
         self.handle = h
-        if matvec not in ("tensor", "fp32", "auto"):
-            raise ValueError("matvec must be one of ['auto', 'fp32', 'tensor']")
+        if matvec not in ("tensor", "tensor_tmem", "fp32", "auto"):
+            raise ValueError("matvec must be one of ['auto', 'fp32', 'tensor', 'tensor_tmem']")
         self.matvec = matvec
         self.tuned = None
+        self.tuned_from_cache = False
+        self.tune_cache = bool(tune_cache)
         _native.check(_native.lib().kr_batch_set_matvec(h, _KINDS["tensor" if matvec == "auto" else matvec]),
                       self.ctx)
         self.phase = None
@@ -89,8 +95,16 @@ class Ensemble:
         _native.check(_native.lib().kr_batch_store(self.handle, out.data_ptr(), stream_ptr()), self.ctx)
         return out
 
-    def step(self, H):
-        """One TDSE.update of every vector with the field-dressed H."""
+    def step(self, H, sync=True):
+        """One TDSE.update of every vector with the field-dressed H.
+
+        The Krylov loop runs on the device (the step is one CUDA graph). With
+        ``sync=True`` the call waits for the step, sets ``last_kmax`` and raises
+        on a step error (KrylovError with code KR_ERR_MAXORDER when a vector
+        needs more than mmax Krylov vectors, the reference's maxorder error of
+        tdse.py:480-484); with ``sync=False`` it returns at once and
+        ``sync()`` reports errors later. Inside a CUDA-graph recording (a
+        capturing stream) the step's nodes join the recording; use sync=False."""
         exp_fac = self.tdse.exp_fac
         phase = None
         if self.H0 is not None:
@@ -98,31 +112,47 @@ class Ensemble:
         plan = H.device_operator(split=self.split)
         if self.matvec == "auto":
             self._tune(plan)
+        self._step_plan(plan, phase, sync)
+
+    def _step_plan(self, plan, phase, sync):
+        """kr_batch_step on an operator plan whose field is set."""
+        exp_fac = self.tdse.exp_fac
         kmax = ctypes.c_int32()
         rc = _native.lib().kr_batch_step(self.handle, plan.op, None if phase is None else phase.data_ptr(),
-                                         float(exp_fac.real), float(exp_fac.imag), self.tol, ctypes.byref(kmax),
-                                         stream_ptr())
-        _native.check(rc, self.ctx)
+                                         float(exp_fac.real), float(exp_fac.imag), self.tol,
+                                         ctypes.byref(kmax) if sync else None, stream_ptr())
+        self._raise(rc)
+        if sync:
+            self.last_kmax = kmax.value
+
+    def _raise(self, rc):
+        _native.check(rc, self.ctx)  # KrylovError; code KR_ERR_MAXORDER when mmax was not enough
+
+    def sync(self):
+        """Waits for the steps launched so far and raises a pending step error;
+        sets ``last_kmax`` (largest Krylov order of the last step)."""
+        kmax = ctypes.c_int32()
+        self._raise(_native.lib().kr_batch_sync(self.handle, ctypes.byref(kmax), stream_ptr()))
         self.last_kmax = kmax.value
 
     def _tune(self, plan, reps=3):
-        """Times one mat-vec of each kind on ``plan`` (CUDA events, after one
-        untimed launch each) and keeps the faster kind."""
+        """Picks the mat-vec kind for this operator shape and vector count
+        (richmol_gb300.tune: from the cache file when the shape was tuned
+        before, else every kind timed with CUDA events and the fastest kept
+        and stored) and keeps it."""
+        from . import tune
         L = _native.lib()
-        times = {}
-        for name, code in _KINDS.items():
-            _native.check(L.kr_batch_set_matvec(self.handle, code), self.ctx)
+
+        def run(kind):
+            _native.check(L.kr_batch_set_matvec(self.handle, _KINDS[kind]), self.ctx)
             _native.check(L.kr_batch_matvec(self.handle, plan.op, stream_ptr()), self.ctx)
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record()
-            for _ in range(reps):
-                _native.check(L.kr_batch_matvec(self.handle, plan.op, stream_ptr()), self.ctx)
-            b.record()
-            b.synchronize()
-            times[name] = a.elapsed_time(b) / reps
-        best = min(times, key=times.get)
+
+        name = torch.cuda.get_device_name(torch.cuda.current_device())
+        best, times, cached = tune.choose(plan, self.nvec, list(_KINDS), run, name, use_cache=self.tune_cache,
+                                          reps=reps)
         _native.check(L.kr_batch_set_matvec(self.handle, _KINDS[best]), self.ctx)
         self.tuned = times
+        self.tuned_from_cache = cached
         self.matvec = best
 
     def korder(self):

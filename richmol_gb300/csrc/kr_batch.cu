@@ -54,6 +54,18 @@ struct kr_batch {
   double2* part = nullptr;   // [KB_RED_CHUNKS][mmax + 2][nb] partial sums
   int* counts = nullptr;     // [3]: active vectors, vectors that hit mmax, mat-vec error word
   int* tc_work = nullptr;    // [2] work-item counters of the persistent tensor-core launches
+  int* kdev = nullptr;       // [2]: Krylov index of the running iteration, orders used by the last step
+  int* status = nullptr;     // [1] sticky error of a step (0: none), read by kr_batch_sync / kr_batch_step
+  // the step as a CUDA graph (prologue, a WHILE node over the Krylov
+  // iterations, the state combination), instantiated once per step key
+  cudaGraphExec_t gexec = nullptr;
+  cudaStream_t cap = nullptr, side0 = nullptr, side1 = nullptr;
+  const kr_op* g_op = nullptr;
+  unsigned long long g_uid = 0;
+  const void* g_phase = nullptr;
+  double g_fac[2] = {0, 0}, g_tol = 0;
+  int g_kind = -1;
+  int nodes_fixed = 0, nodes_iter = 0;  // kernel launches of a step outside / per Krylov iteration
   // mat-vec tile table
   int ntask = 0;
   // per-slab populations (slabs of the operator the batch was created with)
@@ -82,6 +94,8 @@ struct BatchDev {
   int* active;
   double* err;
   int* counts;
+  const int* kdev;  // device Krylov index (null: the k argument of the kernel)
+  int* status;
 };
 
 static BatchDev dev_view(const kr_batch* b) {
@@ -102,6 +116,8 @@ static BatchDev dev_view(const kr_batch* b) {
   d.active = b->active;
   d.err = b->err;
   d.counts = b->counts;
+  d.kdev = b->kdev;
+  d.status = b->status;
   return d;
 }
 
@@ -188,8 +204,10 @@ __global__ void kb_phase_df(const double2* phase, float4* pdf, long long dim) {
 }
 
 // S <- phase * S (optional); V_0 = S in complex64 (unnormalised); partial ||S_v||^2
-__global__ void kb_phase_norm(float4* S, const float4* phase, float2* V0, long long dim, int nb, double2* part) {
+__global__ void kb_phase_norm(float4* S, const float4* phase, float2* V0, long long dim, int nb, double2* part,
+                              const int* status) {
   __shared__ double2 sh[8][32];
+  if (status && *((volatile const int*)status) != 0) return;  // an error is pending: the step does nothing
   const int v = blockIdx.y * 32 + threadIdx.x;
   const Chunk ch = chunk_of(dim);
   dfl acc = {0.f, 0.f};
@@ -207,8 +225,10 @@ __global__ void kb_phase_norm(float4* S, const float4* phase, float2* V0, long l
   if (threadIdx.y == 0) part[(long long)blockIdx.x * nb + v] = t;
 }
 
-// out[j][v] = sum over chunks of part[chunk][j][v] (fixed order)
-__global__ void kb_reduce(const double2* part, int ncoef, int nb, int stride_coef, double2* out) {
+// out[j][v] = sum over chunks of part[chunk][j][v] (fixed order); with kdev
+// the coefficients are j = 0 .. *kdev (the dots of the running iteration)
+__global__ void kb_reduce(const double2* part, int ncoef, int nb, int stride_coef, double2* out, const int* kdev) {
+  if (kdev) ncoef = *kdev + 1;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= ncoef * nb) return;
   const int j = idx / nb, v = idx - j * nb;
@@ -217,16 +237,21 @@ __global__ void kb_reduce(const double2* part, int ncoef, int nb, int stride_coe
   out[(long long)j * nb + v] = s;
 }
 
-// per vector: ||S||, active flag, the scale of V_0 (phase * S stored by kb_phase_norm)
+// per vector: ||S||, active flag, the scale of V_0 (phase * S stored by
+// kb_phase_norm); counts[0] = active vectors. With an error pending no vector
+// is active, so the step leaves the state as it is.
 __global__ void kb_start(const double2* nsq, double* norm0, int* active, int* kconv, double* vscale, int nb,
-                         int nvec) {
+                         int nvec, int* counts, const int* status) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nb) return;
-  const double n0 = sqrt(nsq[v].x);
+  const bool ok = status == nullptr || *((volatile const int*)status) == 0;
+  const double n0 = ok ? sqrt(nsq[v].x) : 0.0;
   norm0[v] = n0;
-  active[v] = (v < nvec && n0 > 0.0) ? 1 : 0;
+  const int act = (ok && v < nvec && n0 > 0.0) ? 1 : 0;
+  active[v] = act;
   kconv[v] = 0;
   vscale[v] = n0 > 0.0 ? 1.0 / n0 : 0.0;
+  if (act && counts) atomicAdd(counts, 1);
 }
 
 // partial dots h_j = <V_j, W> for j = 0..k (V_j as stored, times its scale):
@@ -238,9 +263,10 @@ __global__ void kb_start(const double2* nsq, double* norm0, int* active, int* kc
 // result is the one-at-a-time sum), at 6 CTAs per SM: 14 % faster at C3.
 __global__ void __launch_bounds__(256, 6) kb_dots(const float2* V, const float2* W, const int* active,
                                                   const double* vscale, long long dim, int nb, int k,
-                                                  int stride_coef, double2* part) {
+                                                  int stride_coef, double2* part, const int* kdev) {
   constexpr int U = 4;
   __shared__ double2 sh[8][32];
+  if (kdev) k = *kdev;
   const int v = blockIdx.y * 32 + threadIdx.x;
   const Chunk ch = chunk_of(dim);
   const bool act = active[v] != 0;
@@ -283,8 +309,9 @@ __global__ void __launch_bounds__(256, 6) kb_dots(const float2* V, const float2*
 // their FMAs; 15 % faster at C3.
 template <int KM>
 __global__ void __launch_bounds__(256, KM == 4 ? 5 : 1) kb_update(float2* V, const float2* W, const double2* h, const double* vscale, const int* active,
-                          long long dim, int nb, int k, double2* part) {
+                          long long dim, int nb, int k, double2* part, const int* kdev) {
   __shared__ double2 sh[8][32];
+  if (kdev) k = *kdev;
   const int v = blockIdx.y * 32 + threadIdx.x;
   const Chunk ch = chunk_of(dim);
   const bool act = active[v] != 0;
@@ -319,6 +346,7 @@ __global__ void __launch_bounds__(256, KM == 4 ? 5 : 1) kb_update(float2* V, con
 
 // per vector: T update, exp(fac T) e0, error estimate, convergence
 __global__ void kb_small(BatchDev b, int k, double2 fac, double tol, const double2* npart) {
+  if (b.kdev) k = *b.kdev;
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= b.nb || !b.active[v]) return;
   const int nb = b.nb;
@@ -496,12 +524,51 @@ __global__ void kb_slab_pop(const float4* S, const long long* slab_off, const in
 }
 
 
-// any active vector per 32-vector group
-__global__ void kb_group_active(const int* active, int* grp, int ngrp) {
+// any active vector per 32-vector group; in a recorded step, thread 0 also
+// selects the Gram-Schmidt kernel of the running iteration (its Krylov-index
+// bound 4, 8, 16, 32) for the switch node that follows
+__device__ __forceinline__ unsigned kb_bound_class(int k) { return k < 4 ? 0u : k < 8 ? 1u : k < 16 ? 2u : 3u; }
+__global__ void kb_group_active(const int* active, int* grp, int ngrp, const int* kdev,
+                                cudaGraphConditionalHandle hupd) {
+  if (kdev && blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+    cudaGraphSetConditional(hupd, kb_bound_class(*kdev));
   const int g = blockIdx.x * blockDim.y + threadIdx.y;
   if (g >= ngrp) return;
   const int any = __any_sync(0xffffffffu, active[g * 32 + threadIdx.x] != 0);
   if (threadIdx.x == 0) grp[g] = any;
+}
+
+// ---------------------------------------------------------------------------
+// loop control of a recorded step (one thread each)
+// ---------------------------------------------------------------------------
+// after the prologue: iteration 0 runs if any vector is active and no error is pending
+__global__ void kb_ctl_init(int* counts, int* kdev, const int* status, cudaGraphConditionalHandle hloop) {
+  const int go = counts[0] > 0 && *((volatile const int*)status) == 0;
+  kdev[0] = 0;
+  kdev[1] = 0;
+  counts[0] = 0;
+  counts[1] = 0;
+  cudaGraphSetConditional(hloop, go ? 1u : 0u);
+}
+// after iteration k: errors into the sticky status (mat-vec error word, then
+// vectors that reached mmax), k + 1, and whether iteration k + 1 runs
+__global__ void kb_ctl(int* counts, int* kdev, int* status, int mmax, cudaGraphConditionalHandle hloop) {
+  const int k = kdev[0];
+  int e = 0;
+  if (counts[2] != 0) e = counts[2];
+  else if (counts[1] != 0) e = KR_ERR_MAXORDER;
+  if (e != 0 && *status == 0) *status = e;
+  const int more = counts[0] > 0 && e == 0 && k + 1 < mmax;
+  kdev[0] = k + 1;
+  kdev[1] = k + 1;
+  counts[0] = 0;
+  counts[1] = 0;
+  counts[2] = 0;
+  cudaGraphSetConditional(hloop, more ? 1u : 0u);
+}
+// after the loop: the state combination kernel for the orders used (bound class)
+__global__ void kb_combine_select(const int* kdev, cudaGraphConditionalHandle hcomb) {
+  cudaGraphSetConditional(hcomb, kb_bound_class(kdev[1]));
 }
 
 // ===========================================================================
@@ -523,15 +590,21 @@ const char* const mv_error_text =
     "batched mat-vec: an MMA completion wait gave up or a term exceeded the tile shape";
 
 // Y = H X, each vector's output times yscale[v] when yscale is given (the
-// scale of a basis vector stored unnormalised)
+// scale of a basis vector stored unnormalised). X (and yscale) is the basis
+// array b->V (b->vscale); with kslot its slot is the device-side Krylov index
+// *kslot, else slot 0.
 int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool masked, const double* yscale,
-                  cudaStream_t st) {
-  if (b->mv_kind == KR_MATVEC_TENSOR && op->tc_ntask > 0) {
+                  const int* kslot, cudaStream_t st) {
+  const long long slot_elems = b->dim * (long long)b->nb;
+  if ((b->mv_kind == KR_MATVEC_TENSOR || b->mv_kind == KR_MATVEC_TENSOR_TMEM) && op->tc_ntask > 0) {
     BatchTC q;
     q.op = op->dev;
     q.X = X;
     q.Y = Y;
     q.nb = b->nb;
+    q.kslot = kslot;
+    q.slot_elems = slot_elems;
+    q.nslots = kslot ? b->mmax + 1 : 1;
     q.task = op->tc_task;
     q.ntask = op->tc_ntask;
     q.grp_active = masked ? b->grp_active : nullptr;
@@ -541,7 +614,7 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
     q.tend = op->tc_ntask;
     q.nvb = b->nb / 128;
     q.work = b->tc_work;
-    const int rc = kb_launch_tc(op->ctx, q, b->dim, op->tc_class, b->tc_work, st);
+    const int rc = kb_launch_tc(op->ctx, q, b->dim, op->tc_class, b->tc_work, b->mv_kind == KR_MATVEC_TENSOR_TMEM, st);
     if (rc == KR_OK)
       b->launches += (op->tc_class[1] > op->tc_class[0]) + (op->tc_class[2] > op->tc_class[1]) +
                      (op->tc_class[3] > op->tc_class[2]);
@@ -552,6 +625,8 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
   p.X = X;
   p.Y = Y;
   p.nb = b->nb;
+  p.kslot = kslot;
+  p.slot_elems = slot_elems;
   p.task_slab = b->task_slab;
   p.task_i0 = b->task_i0;
   p.task_nr = b->task_nr;
@@ -607,6 +682,8 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
   BA((size_t)KB_RED_CHUNKS * (m1 + 1) * nb, &b->part);
   BA(3, &b->counts);
   BA(2, &b->tc_work);
+  BA(2, &b->kdev);
+  BA(1, &b->status);
   // output tiles: R = 128 / NKP rows of one slab (NKP = n_k rounded up to 4, 8, 16, 32)
   std::vector<int> ts, ti, tn;
   for (int s = 0; s < (int)dm.size(); ++s) {
@@ -628,6 +705,9 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
   cudaError_t ce = cudaMemcpy(b->task_slab, ts.data(), sizeof(int) * ts.size(), cudaMemcpyHostToDevice);
   if (ce == cudaSuccess) ce = cudaMemcpy(b->task_i0, ti.data(), sizeof(int) * ti.size(), cudaMemcpyHostToDevice);
   if (ce == cudaSuccess) ce = cudaMemcpy(b->task_nr, tn.data(), sizeof(int) * tn.size(), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&b->side0, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&b->side1, cudaStreamNonBlocking);
   if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
   if (ce != cudaSuccess) {
     kr_batch_destroy(b);
@@ -639,6 +719,9 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
 
 extern "C" void kr_batch_destroy(kr_batch* b) {
   if (!b) return;
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  for (cudaStream_t s : {b->cap, b->side0, b->side1})
+    if (s) cudaStreamDestroy(s);
   for (void* p : b->allocs) cudaFree(p);
   delete b;
 }
@@ -661,68 +744,217 @@ extern "C" int kr_batch_store(kr_batch* b, void* states, void* stream) {
   return KR_OK;
 }
 
+namespace {
+// adds a conditional node (WHILE or SWITCH) at the current end of stream s's
+// capture and makes it the new end; its body graphs are returned in body
+int add_conditional(kr_ctx* ctx, cudaStream_t s, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                    unsigned size, cudaGraph_t* body) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  KR_CUDA(ctx, cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+  if (cs != cudaStreamCaptureStatusActive) return set_err(ctx, KR_ERR_CUDA, "batched step: stream is not capturing");
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = type;
+  np.conditional.size = size;
+  cudaGraphNode_t node;
+  KR_CUDA(ctx, cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np));
+  for (unsigned i = 0; i < size; ++i) body[i] = np.conditional.phGraph_out[i];
+  KR_CUDA(ctx, cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  return KR_OK;
+}
+
+// records one Gram-Schmidt kernel or state combination per Krylov-index bound
+// class (4, 8, 16, 32) into the four bodies of a switch node, on stream s
+template <typename F>
+int record_switch(kr_ctx* ctx, cudaStream_t s, cudaGraph_t* bodies, F launch) {
+  for (int c = 0; c < 4; ++c) {
+    KR_CUDA(ctx, cudaStreamBeginCaptureToGraph(s, bodies[c], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    launch(c, s);
+    cudaGraph_t done = nullptr;
+    const cudaError_t e1 = cudaGetLastError();
+    KR_CUDA(ctx, cudaStreamEndCapture(s, &done));
+    KR_CUDA(ctx, e1);
+  }
+  return KR_OK;
+}
+
+// Records one batched step into the graph that stream s is capturing into:
+//   prologue   counts = 0; H0 half-phase to double-float; S <- P S, V_0, ||S||^2;
+//              per-vector start; loop control (iteration 0 runs?)
+//   WHILE      mask of active vector groups (+ Gram-Schmidt kernel class);
+//              W = H V_k (mat-vec of the device-side slot k); dots <V_j, W>;
+//              their sums; SWITCH: V_{k+1} = W - sum h_j V_j (bound class of k);
+//              per-vector T, exp(fac T) e0, error estimate, convergence;
+//              loop control (k + 1, errors, iteration k + 1 runs?)
+//   SWITCH     state combination S <- P (c_0 S + ||S|| sum c_i V_i) (class of the orders used)
+// The Krylov index lives in device memory (b->kdev), so nothing of the loop
+// depends on the host: a recorded step replays as it is.
+int record_step(kr_batch* b, kr_op* op, const double2* phase, double2 fac, double tol, cudaStream_t s) {
+  kr_ctx* ctx = op->ctx;
+  const int nb = b->nb;
+  const long long dim = b->dim;
+  const dim3 eg(KB_RED_CHUNKS, nb / 32), eb(32, 8);
+  const int stride = b->mmax + 2;
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  KR_CUDA(ctx, cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+  if (cs != cudaStreamCaptureStatusActive) return set_err(ctx, KR_ERR_CUDA, "batched step: stream is not capturing");
+  cudaGraphConditionalHandle hloop, hupd, hcomb;
+  KR_CUDA(ctx, cudaGraphConditionalHandleCreate(&hloop, g, 0, cudaGraphCondAssignDefault));
+  KR_CUDA(ctx, cudaGraphConditionalHandleCreate(&hupd, g, 0, 0));
+  KR_CUDA(ctx, cudaGraphConditionalHandleCreate(&hcomb, g, 0, 0));
+  int fixed = 0, iter = 0;
+  // ---- prologue
+  KR_CUDA(ctx, cudaMemsetAsync(b->counts, 0, 3 * sizeof(int), s));
+  const float4* pdf = nullptr;
+  if (phase) {
+    kb_phase_df<<<(int)std::min<long long>((dim + 255) / 256, 1024), 256, 0, s>>>(phase, b->phase_df, dim);
+    pdf = b->phase_df;
+    ++fixed;
+  }
+  kb_phase_norm<<<eg, eb, 0, s>>>(b->S, pdf, b->V, dim, nb, b->part, b->status);
+  kb_reduce<<<(nb + 255) / 256, 256, 0, s>>>(b->part, 1, nb, 1, b->h, nullptr);
+  kb_start<<<(nb + 255) / 256, 256, 0, s>>>(b->h, b->norm0, b->active, b->kconv, b->vscale, nb, b->nvec, b->counts,
+                                            b->status);
+  kb_ctl_init<<<1, 1, 0, s>>>(b->counts, b->kdev, b->status, hloop);
+  fixed += 4;
+  KR_CUDA(ctx, cudaGetLastError());
+  // ---- the Krylov iterations
+  cudaGraph_t body;
+  int rc = add_conditional(ctx, s, hloop, cudaGraphCondTypeWhile, 1, &body);
+  if (rc) return rc;
+  cudaStream_t s0 = b->side0;
+  KR_CUDA(ctx, cudaStreamBeginCaptureToGraph(s0, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  {
+    kb_group_active<<<(mv_groups(b) + 7) / 8, dim3(32, 8), 0, s0>>>(b->active, b->grp_active, mv_groups(b), b->kdev,
+                                                                     hupd);
+    const long long l0 = b->launches;
+    rc = launch_matvec(b, op, b->V, b->W, true, b->vscale, b->kdev, s0);
+    const int mv_launches = (int)(b->launches - l0);
+    b->launches = l0;
+    kb_dots<<<eg, eb, 0, s0>>>(b->V, b->W, b->active, b->vscale, dim, nb, 0, stride, b->part, b->kdev);
+    kb_reduce<<<((b->mmax + 1) * nb + 255) / 256, 256, 0, s0>>>(b->part, 1, nb, stride, b->h, b->kdev);
+    iter += 3 + mv_launches;
+    cudaGraph_t ub[4];
+    if (rc == KR_OK) rc = add_conditional(ctx, s0, hupd, cudaGraphCondTypeSwitch, 4, ub);
+    if (rc == KR_OK)
+      rc = record_switch(ctx, b->side1, ub, [&](int c, cudaStream_t t) {
+        if (c == 0) kb_update<4><<<eg, eb, 0, t>>>(b->V, b->W, b->h, b->vscale, b->active, dim, nb, 0, b->part, b->kdev);
+        else if (c == 1) kb_update<8><<<eg, eb, 0, t>>>(b->V, b->W, b->h, b->vscale, b->active, dim, nb, 0, b->part, b->kdev);
+        else if (c == 2) kb_update<16><<<eg, eb, 0, t>>>(b->V, b->W, b->h, b->vscale, b->active, dim, nb, 0, b->part, b->kdev);
+        else kb_update<32><<<eg, eb, 0, t>>>(b->V, b->W, b->h, b->vscale, b->active, dim, nb, 0, b->part, b->kdev);
+      });
+    kb_small<<<(nb + 127) / 128, 128, 0, s0>>>(dev_view(b), 0, fac, tol, b->part);
+    kb_ctl<<<1, 1, 0, s0>>>(b->counts, b->kdev, b->status, b->mmax, hloop);
+    iter += 3;
+  }
+  const cudaError_t le = cudaGetLastError();
+  cudaGraph_t done = nullptr;
+  const cudaError_t ee = cudaStreamEndCapture(s0, &done);
+  if (rc) return rc;
+  KR_CUDA(ctx, le);
+  KR_CUDA(ctx, ee);
+  // ---- the state combination
+  kb_combine_select<<<1, 1, 0, s>>>(b->kdev, hcomb);
+  cudaGraph_t cb[4];
+  rc = add_conditional(ctx, s, hcomb, cudaGraphCondTypeSwitch, 4, cb);
+  if (rc) return rc;
+  const BatchDev bd = dev_view(b);
+  rc = record_switch(ctx, b->side1, cb, [&](int c, cudaStream_t t) {
+    if (c == 0) kb_combine<4><<<eg, eb, 0, t>>>(bd, pdf);
+    else if (c == 1) kb_combine<8><<<eg, eb, 0, t>>>(bd, pdf);
+    else if (c == 2) kb_combine<16><<<eg, eb, 0, t>>>(bd, pdf);
+    else kb_combine<32><<<eg, eb, 0, t>>>(bd, pdf);
+  });
+  if (rc) return rc;
+  fixed += 2;
+  KR_CUDA(ctx, cudaGetLastError());
+  b->nodes_fixed = fixed;
+  b->nodes_iter = iter;
+  return KR_OK;
+}
+
+// the sticky step status: 0, or the error of a step (cleared when read)
+int take_status(kr_batch* b, cudaStream_t st, int* kused) {
+  int h[3] = {0, 0, 0};
+  KR_CUDA(b->op->ctx, cudaMemcpyAsync(h, b->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  KR_CUDA(b->op->ctx, cudaMemcpyAsync(h + 1, b->kdev, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  KR_CUDA(b->op->ctx, cudaStreamSynchronize(st));
+  if (kused) *kused = h[2];
+  if (h[0] == 0) return KR_OK;
+  KR_CUDA(b->op->ctx, cudaMemsetAsync(b->status, 0, sizeof(int), st));
+  KR_CUDA(b->op->ctx, cudaStreamSynchronize(st));
+  if (h[0] == KR_ERR_MAXORDER)
+    return set_err(b->op->ctx, KR_ERR_MAXORDER,
+                   "batched Lanczos: vectors did not reach the tolerance within " + std::to_string(b->mmax) +
+                       " Krylov vectors");
+  return set_err(b->op->ctx, h[0], mv_error_text);
+}
+}  // namespace
+
 extern "C" int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double fac_re, double fac_im, double tol,
                              int32_t* kmax_out, void* stream) {
   if (!b || !op) return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_step: bad argument");
   if (op->dev.dim_out != b->dim || !op->square)
     return set_err(op->ctx, KR_ERR_ARG, "kr_batch_step: operator does not match the batch basis");
   cudaStream_t st = (cudaStream_t)stream;
-  const int nb = b->nb;
-  const long long dim = b->dim;
-  const dim3 eg(KB_RED_CHUNKS, nb / 32), eb(32, 8);
-  const int stride = b->mmax + 2;
-  const double2 fac = make_double2(fac_re, fac_im);
   kr_ctx* ctx = op->ctx;
-  KR_CUDA(ctx, cudaMemsetAsync(b->counts, 0, 3 * sizeof(int), st));
-  // S <- phase * S, norms, V_0
-  const float4* pdf = nullptr;
-  if (phase) {
-    kb_phase_df<<<(int)std::min<long long>((dim + 255) / 256, 1024), 256, 0, st>>>((const double2*)phase, b->phase_df,
-                                                                                dim);
-    b->launches++;
-    pdf = b->phase_df;
+  const double2 fac = make_double2(fac_re, fac_im);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  KR_CUDA(ctx, cudaStreamIsCapturing(st, &cs));
+  if (cs == cudaStreamCaptureStatusActive) {
+    // the caller records: the step's nodes go into the caller's graph
+    if (kmax_out) return set_err(ctx, KR_ERR_ARG, "kr_batch_step: kmax_out must be NULL while the stream captures");
+    return record_step(b, op, (const double2*)phase, fac, tol, st);
   }
-  kb_phase_norm<<<eg, eb, 0, st>>>(b->S, pdf, b->V, dim, nb, b->part);
-  kb_reduce<<<(nb + 255) / 256, 256, 0, st>>>(b->part, 1, nb, 1, b->h);
-  kb_start<<<(nb + 255) / 256, 256, 0, st>>>(b->h, b->norm0, b->active, b->kconv, b->vscale, nb, b->nvec);
-  b->launches += 3;
-  KR_CUDA(ctx, cudaGetLastError());
+  // a call: the step recorded once per (operator, phase, factor, tolerance,
+  // mat-vec kind) and launched as one graph
+  if (!b->gexec || b->g_op != op || b->g_uid != op->uid || b->g_phase != phase || b->g_fac[0] != fac_re ||
+      b->g_fac[1] != fac_im || b->g_tol != tol || b->g_kind != b->mv_kind) {
+    if (b->gexec) {
+      KR_CUDA(ctx, cudaGraphExecDestroy(b->gexec));
+      b->gexec = nullptr;
+    }
+    KR_CUDA(ctx, cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeRelaxed));
+    const int rc = record_step(b, op, (const double2*)phase, fac, tol, b->cap);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(b->cap, &g);
+    if (rc != KR_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    KR_CUDA(ctx, e);
+    const cudaError_t ie = cudaGraphInstantiate(&b->gexec, g, 0);
+    cudaGraphDestroy(g);
+    KR_CUDA(ctx, ie);
+    b->g_op = op;
+    b->g_uid = op->uid;
+    b->g_phase = phase;
+    b->g_fac[0] = fac_re;
+    b->g_fac[1] = fac_im;
+    b->g_tol = tol;
+    b->g_kind = b->mv_kind;
+  }
+  KR_CUDA(ctx, cudaGraphLaunch(b->gexec, st));
+  b->launches += b->nodes_fixed;
+  if (!kmax_out) return KR_OK;
   int kused = 0;
-  for (int k = 0; k < b->mmax; ++k) {
-    kb_group_active<<<(mv_groups(b) + 7) / 8, dim3(32, 8), 0, st>>>(b->active, b->grp_active, mv_groups(b));
-    int rc = launch_matvec(b, op, b->V + (long long)k * dim * nb, b->W, true, b->vscale + (long long)k * nb, st);
-    if (rc) return rc;
-    kb_dots<<<eg, eb, 0, st>>>(b->V, b->W, b->active, b->vscale, dim, nb, k, stride, b->part);
-    kb_reduce<<<((k + 1) * nb + 255) / 256, 256, 0, st>>>(b->part, k + 1, nb, stride, b->h);
-    if (k < 4) kb_update<4><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->vscale, b->active, dim, nb, k, b->part);
-    else if (k < 8) kb_update<8><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->vscale, b->active, dim, nb, k, b->part);
-    else if (k < 16) kb_update<16><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->vscale, b->active, dim, nb, k, b->part);
-    else kb_update<32><<<eg, eb, 0, st>>>(b->V, b->W, b->h, b->vscale, b->active, dim, nb, k, b->part);
-    // kb_small sums the chunk partials of ||V_{k+1}||^2 itself (as kb_reduce would)
-    KR_CUDA(ctx, cudaMemsetAsync(b->counts, 0, 2 * sizeof(int), st));
-    kb_small<<<(nb + 127) / 128, 128, 0, st>>>(dev_view(b), k, fac, tol, b->part);
-    b->launches += 5;
-    KR_CUDA(ctx, cudaGetLastError());
-    int counts[3] = {0, 0, 0};
-    KR_CUDA(ctx, cudaMemcpyAsync(counts, b->counts, sizeof(counts), cudaMemcpyDeviceToHost, st));
-    KR_CUDA(ctx, cudaStreamSynchronize(st));
-    kused = k + 1;
-    if (counts[2] != 0) return set_err(ctx, counts[2], mv_error_text);
-    if (counts[1] > 0)
-      return set_err(ctx, KR_ERR_MAXORDER,
-                     "batched Lanczos: " + std::to_string(counts[1]) + " vectors did not reach the tolerance within " +
-                         std::to_string(b->mmax) + " Krylov vectors");
-    if (counts[0] == 0) break;
-  }
-  // every vector's order is at most kused + 1 (kconv)
-  if (kused < 4) kb_combine<4><<<eg, eb, 0, st>>>(dev_view(b), pdf);
-  else if (kused < 8) kb_combine<8><<<eg, eb, 0, st>>>(dev_view(b), pdf);
-  else if (kused < 16) kb_combine<16><<<eg, eb, 0, st>>>(dev_view(b), pdf);
-  else kb_combine<32><<<eg, eb, 0, st>>>(dev_view(b), pdf);
-  b->launches++;
-  KR_CUDA(ctx, cudaGetLastError());
+  const int rc = take_status(b, st, &kused);
+  b->launches += (long long)kused * b->nodes_iter;
+  *kmax_out = kused;
+  return rc;
+}
+
+extern "C" int kr_batch_sync(kr_batch* b, int32_t* kmax_out, void* stream) {
+  if (!b) return set_err(nullptr, KR_ERR_ARG, "kr_batch_sync: NULL batch");
+  int kused = 0;
+  const int rc = take_status(b, (cudaStream_t)stream, &kused);
   if (kmax_out) *kmax_out = kused;
-  return KR_OK;
+  return rc;
 }
 
 extern "C" int kr_batch_korder(kr_batch* b, int32_t* korder, void* stream) {
@@ -742,11 +974,11 @@ extern "C" int kr_batch_expect(kr_batch* b, kr_op* obs, double* out, void* strea
   float2* X = b->V;  // basis slot 0 and W are free between steps
   KR_CUDA(obs->ctx, cudaMemsetAsync(b->counts + 2, 0, sizeof(int), st));
   kb_to_f32<<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, st>>>(b->S, X, n);
-  int rc = launch_matvec(b, obs, X, b->W, false, nullptr, st);
+  int rc = launch_matvec(b, obs, X, b->W, false, nullptr, nullptr, st);
   if (rc) return rc;
   const dim3 eg(KB_RED_CHUNKS, b->nb / 32), eb(32, 8);
   kb_expect_dots<<<eg, eb, 0, st>>>(b->S, b->W, b->dim, b->nb, b->part);
-  kb_reduce<<<(b->nb + 255) / 256, 256, 0, st>>>(b->part, 1, b->nb, 1, b->h);
+  kb_reduce<<<(b->nb + 255) / 256, 256, 0, st>>>(b->part, 1, b->nb, 1, b->h, nullptr);
   b->launches += 3;
   KR_CUDA(obs->ctx, cudaGetLastError());
   std::vector<double2> h(b->nb);
@@ -805,7 +1037,7 @@ extern "C" int kr_batch_apply(kr_batch* b, kr_op* op, const void* x, void* y, vo
   const dim3 grid((unsigned)((b->dim + 31) / 32), b->nb / 32);
   KR_CUDA(op->ctx, cudaMemsetAsync(b->counts + 2, 0, sizeof(int), st));
   kb_transpose_in32<<<grid, dim3(32, 8), 0, st>>>((const double2*)x, b->V, b->dim, b->nvec, b->nb);
-  const int rc = launch_matvec(b, op, b->V, b->W, false, nullptr, st);
+  const int rc = launch_matvec(b, op, b->V, b->W, false, nullptr, nullptr, st);
   if (rc) return rc;
   kb_transpose_out32<<<grid, dim3(32, 8), 0, st>>>(b->W, (double2*)y, b->dim, b->nvec, b->nb);
   b->launches += 2;
@@ -834,7 +1066,7 @@ extern "C" int kr_batch_populations(kr_batch* b, double* out, void* stream) {
 }
 
 extern "C" int kr_batch_set_matvec(kr_batch* b, int32_t kind) {
-  if (!b || (kind != KR_MATVEC_TENSOR && kind != KR_MATVEC_FP32))
+  if (!b || (kind != KR_MATVEC_TENSOR && kind != KR_MATVEC_FP32 && kind != KR_MATVEC_TENSOR_TMEM))
     return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_set_matvec: bad argument");
   b->mv_kind = kind;
   return KR_OK;
@@ -843,7 +1075,7 @@ extern "C" int kr_batch_set_matvec(kr_batch* b, int32_t kind) {
 extern "C" int kr_batch_matvec(kr_batch* b, kr_op* op, void* stream) {
   if (!b || !op || op->dev.dim_out != b->dim || !op->square)
     return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_matvec: operator does not match the batch basis");
-  return launch_matvec(b, op, b->V, b->W, false, nullptr, (cudaStream_t)stream);
+  return launch_matvec(b, op, b->V, b->W, false, nullptr, nullptr, (cudaStream_t)stream);
 }
 
 extern "C" int64_t kr_batch_launch_count(const kr_batch* b) { return b ? b->launches : -1; }

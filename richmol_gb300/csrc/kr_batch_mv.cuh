@@ -9,12 +9,20 @@
 
 #define KB_WMAX 16   // ELL width of the M band supported by the batched mat-vec
 
+// Basis slot a mat-vec reads: X (and yscale) are the base of an array of
+// basis slots of slot_elems elements (nb per row); with kslot non-null the
+// slot is the device-side Krylov index *kslot (read at launch, so a recorded
+// step needs no host-side index), else slot 0.
+__device__ __forceinline__ int kb_slot(const int* kslot) { return kslot ? __ldg(kslot) : 0; }
+
 // arguments of the SIMT mat-vec kb_matvec (kr_batch_simt.cu)
 struct BatchMV {
   DevOp op;
   const float2* X;
   float2* Y;
   int nb;
+  const int* kslot;       // device Krylov index: basis slot of X and yscale (null: slot 0)
+  long long slot_elems;   // elements of one basis slot (dim * nb)
   const int* task_slab;
   const int* task_i0;
   const int* task_nr;
@@ -28,6 +36,9 @@ struct BatchTC {
   const float2* X;
   float2* Y;
   int nb;
+  const int* kslot;       // device Krylov index: basis slot of X and yscale (null: slot 0)
+  long long slot_elems;   // elements of one basis slot (dim * nb)
+  int nslots;             // basis slots behind X (extent of the TMA descriptor)
   const int* task;        // [4][ntask]: slab, first row, rows, KP
   int ntask;
   int tfirst;             // first tile of this launch in task (per-tile kernel: tile tfirst + blockIdx.x)
@@ -59,5 +70,9 @@ int kb_launch_simt(kr_ctx* ctx, const BatchMV& p, int ntask, int ngrp, cudaStrea
 // launch the tensor-core mat-vec over its tile table: the tiles of KP = 8 and
 // 16 (cls[0] .. cls[2]) as one persistent launch per class (work counters
 // work[0], work[1], zeroed here), the KP = 32 tiles (cls[2] .. cls[3]) one CTA
-// per tile and vector block; encodes the TMA descriptor of p.X ([dim][nb] complex64)
-int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, const int* cls, int* work, cudaStream_t st);
+// per tile and vector block; encodes the TMA descriptor of p.X (p.nslots
+// slots of [dim][nb] complex64)
+// tmem_a: the persistent launches keep their A tiles in tensor memory (written by
+// tcgen05.st; the shared memory holds a deeper TMA ring), else in shared memory
+int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, const int* cls, int* work, bool tmem_a,
+                 cudaStream_t st);

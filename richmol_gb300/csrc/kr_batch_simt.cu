@@ -221,7 +221,7 @@ __device__ void kb_tile(const BatchMV& p, int s1, int i0, int nr, float* smem) {
       }
     }
     __syncthreads();
-    const float2* Xs2 = p.X + (long long)__ldg(op.in_off + s2) * nb + v;
+    const float2* Xs2 = p.X + (long long)kb_slot(p.kslot) * p.slot_elems + (long long)__ldg(op.in_off + s2) * nb + v;
     if (dia) {
       // T rows of the band: input rows i0 + d0 .. i0 + d0 + nr + W - 2
       kb_tstep<NKP>(Xs2, nb, nk2, ld2, ktype, Ks, Ts, i0 + d0, nr + W - 1, dm2, wid, lane);
@@ -243,7 +243,7 @@ __device__ void kb_tile(const BatchMV& p, int s1, int i0, int nr, float* smem) {
     }
   }
   float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * ld1) * nb + v;
-  const float sc = p.yscale ? (float)p.yscale[v] : 1.f;
+  const float sc = p.yscale ? (float)p.yscale[(long long)kb_slot(p.kslot) * nb + v] : 1.f;
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
 #pragma unroll

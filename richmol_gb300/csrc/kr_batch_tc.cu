@@ -148,7 +148,7 @@ __device__ __forceinline__ KbtTerm kbt_term(const DevOp& op, const BatchTC& p, i
   t.KT = op.k_f32 + __ldg(op.k_off + kb);
   t.col = op.m_col + __ldg(op.mf_col_off + mfi);
   t.mf = op.mf_f32 + __ldg(op.mf_off + mfi) + wlo;
-  t.Xs2 = p.X + (long long)__ldg(op.in_off + t.s2) * nb + v;
+  t.Xs2 = p.X + (long long)kb_slot(p.kslot) * p.slot_elems + (long long)__ldg(op.in_off + t.s2) * nb + v;
   return t;
 }
 
@@ -471,7 +471,7 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
   // epilogue: rows r = w / 4, w / 4 + 2, ... of this warp's lane quarter
   int ld1;
   float2* Y = y_rows(ld1);
-  const float sc = p.yscale ? (float)p.yscale[v] : 1.f;
+  const float sc = p.yscale ? (float)p.yscale[(long long)kb_slot(p.kslot) * nb + v] : 1.f;
   for (int r = wid >> 2; r < nr; r += 2) {
     for (int c0 = 0; c0 < NP; c0 += 16) {
       float re[16], im[16];
@@ -502,13 +502,15 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
 // directly. The layout below is shared by the persistent kernel (KbtPers).
 // ---------------------------------------------------------------------------
 
-template <int KP>
+template <int KP, bool TA = false>
 struct KbtRing {
-  static constexpr int NSLOT = 64 / KP;          // slots of KP rows x 128 vectors x 8 bytes
+  // slots of KP rows x 128 vectors x 8 bytes: with the A tiles in TMEM (TA) the
+  // shared memory they took holds a ring about three times as deep
+  static constexpr int NSLOT = TA ? (KP == 16 ? 11 : 22) : 64 / KP;
   static constexpr int SLOT = KP * 1024;
   static constexpr int BPART = 128 * KP;         // one B part: NP (<= 32) x KP FP32
   static constexpr int BBUF = 6 * BPART;
-  static constexpr int OFF_B = TC_ABYTES;
+  static constexpr int OFF_B = TA ? 0 : TC_ABYTES;
   static constexpr int OFF_RING = OFF_B + 2 * BBUF;
   static constexpr int OFF_MF = OFF_RING + NSLOT * SLOT;
   static constexpr int OFF_CS = OFF_MF + TC_MFBYTES;
@@ -609,11 +611,11 @@ __device__ __forceinline__ void macc2(float2& z, const float4& m, float2 x) {
 // MFd[c][r] (zero outside the band); rows go in groups of G, a group skipped
 // (warp-uniform) when the band misses it. Input columns at or beyond n_k2 hold
 // finite data of the neighbouring rows and meet zero rows of K^T in the MMA.
-template <int KP, int MT>
+template <int KP, int MT, int NSLOT>
 __device__ __forceinline__ bool kbt_mdia_ring(float2 (&z)[64 / KP][KP / 2], const char* ring, uint64_t* rfull,
                                               uint64_t* rempty, int& g, int nwin, int nr, int W, int b0,
                                               int vloc, int lane, const float4* MFd) {
-  constexpr int R = 64 / KP, BH = KP / 2, NSLOT = KbtRing<KP>::NSLOT;
+  constexpr int R = 64 / KP, BH = KP / 2;
   constexpr int G = R >= 8 ? 2 : 1;
   bool ok = true;
   for (int c = 0; c < nwin; ++c, ++g) {
@@ -642,7 +644,7 @@ __device__ __forceinline__ bool kbt_mdia_ring(float2 (&z)[64 / KP][KP / 2], cons
   return ok;
 }
 
-template <int KP>
+template <int KP, int NSLOT>
 __device__ __forceinline__ bool kbt_zstep_ring(float2 (&z)[64 / KP][KP / 2], const KbtTerm& t, long long nb, int nr,
                                                int b0, int vloc, int lane, const float2* MFs, const int* Cs,
                                                const float4* MFd, const char* ring, uint64_t* rfull,
@@ -655,9 +657,9 @@ __device__ __forceinline__ bool kbt_zstep_ring(float2 (&z)[64 / KP][KP / 2], con
   if (!t.ok || t.empty) return true;
   const int nwin = kbt_ring_rows(t, nr);
   if (t.dia) {
-    if (t.mtype == 1) return kbt_mdia_ring<KP, 1>(z, ring, rfull, rempty, g, nwin, nr, t.W, b0, vloc, lane, MFd);
-    if (t.mtype == 2) return kbt_mdia_ring<KP, 2>(z, ring, rfull, rempty, g, nwin, nr, t.W, b0, vloc, lane, MFd);
-    return kbt_mdia_ring<KP, 0>(z, ring, rfull, rempty, g, nwin, nr, t.W, b0, vloc, lane, MFd);
+    if (t.mtype == 1) return kbt_mdia_ring<KP, 1, NSLOT>(z, ring, rfull, rempty, g, nwin, nr, t.W, b0, vloc, lane, MFd);
+    if (t.mtype == 2) return kbt_mdia_ring<KP, 2, NSLOT>(z, ring, rfull, rempty, g, nwin, nr, t.W, b0, vloc, lane, MFd);
+    return kbt_mdia_ring<KP, 0, NSLOT>(z, ring, rfull, rempty, g, nwin, nr, t.W, b0, vloc, lane, MFd);
   }
   if (t.mtype == 1) kbt_mell<KP, 1>(z, t.Xs2, nb, t.nk2, t.ld2, nr, t.W, b0, MFs, Cs);
   else if (t.mtype == 2) kbt_mell<KP, 2>(z, t.Xs2, nb, t.nk2, t.ld2, nr, t.W, b0, MFs, Cs);
@@ -679,9 +681,9 @@ __device__ __forceinline__ bool kbt_zstep_ring(float2 (&z)[64 / KP][KP / 2], con
 // ---------------------------------------------------------------------------
 constexpr int KBT_MAXT_P = 32;  // term table entries per buffer
 
-template <int KP>
+template <int KP, bool TA = false>
 struct KbtPers {
-  using Rg = KbtRing<KP>;
+  using Rg = KbtRing<KP, TA>;
   static constexpr int NSLOT = Rg::NSLOT;
   static constexpr int OFF_BAR = Rg::OFF_MFD + 2 * Rg::MFD * 16;
   // full, empty, rfull[NSLOT], rempty[NSLOT], ready[2], free[2], TMEM slot
@@ -690,11 +692,116 @@ struct KbtPers {
   static constexpr int TOTAL = OFF_TAB + 2 * KBT_MAXT_P * (int)sizeof(KbtTerm);
 };
 static_assert(KbtPers<8>::TOTAL <= 232448 && KbtPers<16>::TOTAL <= 232448, "persistent tile exceeds shared memory");
+static_assert(KbtPers<8, true>::TOTAL <= 232448 && KbtPers<16, true>::TOTAL <= 232448,
+              "persistent tile (A in TMEM) exceeds shared memory");
 
+// A tiles of tile row r in TMEM (the TA form): parts Z_re hi, lo, Z_im hi, lo,
+// KP columns each, from column abase + 4 r KP; this thread's lane, its half of
+// the K columns (b0 .. b0 + KP/2). The TF32 split is the one of kbt_store_row.
 template <int KP>
+__device__ __forceinline__ void kbt_store_row_tmem(uint32_t arow, const float2 (&zr)[KP / 2], int b0) {
+  constexpr int BH = KP / 2;
+  float rh[BH], rl[BH], ih[BH], il[BH];
+#pragma unroll
+  for (int q = 0; q < BH; ++q) {
+    const float2 zz = zr[q];
+    const float2 hi = make_float2(__uint_as_float((__float_as_uint(zz.x) + 0x1000u) & 0xFFFFE000u),
+                                  __uint_as_float((__float_as_uint(zz.y) + 0x1000u) & 0xFFFFE000u));
+    const float2 lo = tc_fsub2(zz, hi);
+    rh[q] = hi.x;
+    rl[q] = lo.x;
+    ih[q] = hi.y;
+    il[q] = lo.y;
+  }
+  const uint32_t c = arow + (uint32_t)b0;
+  if constexpr (BH == 8) {
+    tc_st8(c + 0 * KP, rh);
+    tc_st8(c + 1 * KP, rl);
+    tc_st8(c + 2 * KP, ih);
+    tc_st8(c + 3 * KP, il);
+  } else {
+    tc_st4(c + 0 * KP, rh);
+    tc_st4(c + 1 * KP, rl);
+    tc_st4(c + 2 * KP, ih);
+    tc_st4(c + 3 * KP, il);
+  }
+}
+
+// kbt_issue_merged with the A tiles in TMEM (column atm + 4 r KP + part KP)
+template <int KP, int KT>
+__device__ __forceinline__ void kbt_issue_merged_ta(uint32_t tmem, uint32_t atm, uint64_t bdesc, uint32_t id1,
+                                                    uint32_t id2, int NP, int nr, int nk2, uint32_t acc0,
+                                                    int bpart) {
+  const uint64_t BP = (uint64_t)(bpart >> 4);
+  const int nks = (nk2 + 7) >> 3;
+  for (int r = 0; r < nr; ++r) {
+    const uint32_t dre = tmem + (uint32_t)(4 * r * NP), dim = dre + (uint32_t)(2 * NP);
+    const uint32_t a = atm + (uint32_t)(4 * r * KP);
+#pragma unroll
+    for (int ks = 0; ks < KP / 8; ++ks) {
+      if (ks >= nks) break;
+      const uint32_t f = ks == 0 ? acc0 : 1u;
+      const uint32_t ak = a + 8u * ks;
+      const uint64_t bk = bdesc + 16u * ks;
+      if (KT != 2) {
+        tc_mma_tf32_ta(dre, ak + 0 * KP, bk + 0 * BP, id2, f);
+        tc_mma_tf32_ta(dre, ak + 1 * KP, bk + 0 * BP, id1, 1u);
+        tc_mma_tf32_ta(dim, ak + 2 * KP, bk + 0 * BP, id2, f);
+        tc_mma_tf32_ta(dim, ak + 3 * KP, bk + 0 * BP, id1, 1u);
+      }
+      if (KT != 1) {
+        const uint32_t g = KT == 2 ? f : 1u;
+        tc_mma_tf32_ta(dre, ak + 2 * KP, bk + 4 * BP, id2, g);
+        tc_mma_tf32_ta(dre, ak + 3 * KP, bk + 4 * BP, id1, 1u);
+        tc_mma_tf32_ta(dim, ak + 0 * KP, bk + 2 * BP, id2, g);
+        tc_mma_tf32_ta(dim, ak + 1 * KP, bk + 2 * BP, id1, 1u);
+      }
+    }
+  }
+}
+
+// kbt_issue (three MMAs per part and K step, D regions 2 r NP) with the A
+// tiles in TMEM
+template <int KP>
+__device__ __forceinline__ void kbt_issue_ta(uint32_t tmem, uint32_t atm, uint64_t bdesc, uint32_t idesc, int NP,
+                                             int nr, int ktype, int nk2, uint32_t& dinit, int bpart) {
+  const int nks = (nk2 + 7) >> 3;
+  for (int r = 0; r < nr; ++r) {
+    int pd[4], pa[4], pb[4];
+    int np = 0;
+    if (ktype != 2) {
+      pd[np] = 0; pa[np] = 0; pb[np] = 0; ++np;
+      pd[np] = 1; pa[np] = 2; pb[np] = 0; ++np;
+    }
+    if (ktype != 1) {
+      pd[np] = 0; pa[np] = 2; pb[np] = 4; ++np;
+      pd[np] = 1; pa[np] = 0; pb[np] = 2; ++np;
+    }
+    for (int q = 0; q < np; ++q) {
+      const uint32_t dcol = tmem + (uint32_t)((2 * r + pd[q]) * NP);
+      const uint32_t dbit = 1u << (2 * r + pd[q]);
+      const uint32_t ad = atm + (uint32_t)((r * 4 + pa[q]) * KP);
+      const uint64_t bd = bdesc + (uint64_t)((pb[q] * bpart) >> 4);
+#pragma unroll
+      for (int sp = 0; sp < 3; ++sp) {
+        const uint32_t a2 = ad + (sp == 2 ? (uint32_t)KP : 0u);
+        const uint64_t b2 = bd + (sp == 1 ? (uint64_t)(bpart >> 4) : 0);
+#pragma unroll
+        for (int ks = 0; ks < KP / 8; ++ks) {
+          if (ks < nks) {
+            tc_mma_tf32_ta(dcol, a2 + 8u * ks, b2 + 16u * ks, idesc, (dinit & dbit) ? 1u : 0u);
+            dinit |= dbit;
+          }
+        }
+      }
+    }
+  }
+}
+
+template <int KP, bool TA>
 __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* smem) {
-  using L = KbtPers<KP>;
-  using Rg = KbtRing<KP>;
+  using L = KbtPers<KP, TA>;
+  using Rg = KbtRing<KP, TA>;
   constexpr int R = 64 / KP, BH = KP / 2, NSLOT = L::NSLOT;
   constexpr int ATILE = 128 * KP;
   const DevOp& op = p.op;
@@ -717,7 +824,12 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
   uint32_t* tslot = reinterpret_cast<uint32_t*>(tfree + 2);
   int* hdr0 = reinterpret_cast<int*>(smem + L::OFF_HDR);  // [2][8]: item (-1: none), s1, i0, nr, vb, tb, te
   KbtTerm* tab0 = reinterpret_cast<KbtTerm*>(smem + L::OFF_TAB);
-  constexpr uint32_t NCOLS = 512;  // the largest D of a tile: 4 R NP <= 512 (merged) or 2 R NP
+  // TMEM: the D regions of a tile (4 R NP <= 512 columns merged, else 2 R NP);
+  // with TA, D in columns 0-255 (merged when 4 R NP <= 256) and the A tiles
+  // (R rows x 4 parts x KP = 256 columns) from column TA_ACOL on
+  constexpr uint32_t NCOLS = 512;
+  constexpr uint32_t TA_ACOL = 256;
+  constexpr int DMAX = TA ? 256 : 512;
   if (wid == 8) tc_alloc(tslot, NCOLS);
   if (tid == 256) {
     tc_mbar_init(full, 8);
@@ -741,6 +853,7 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
 
   if (wid == 9) {
     // ---- work items, term tables and X window loads -------------------------
+    const int zslot = kb_slot(p.kslot);  // basis slot of X (third TMA coordinate)
     int g = 0;
     for (int it = 0;; ++it) {
       const int b = it & 1;
@@ -792,7 +905,7 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
             char* dst = ring + (size_t)slot * Rg::SLOT;
 #pragma unroll
             for (int h = 0; h < KP / 8; ++h)
-              tc_tma_load_2d(dst + h * 8192, xmap, vb * 128, (int)(y + 8 * h), rfull + slot);
+              tc_tma_load_3d(dst + h * 8192, xmap, vb * 128, (int)(y + 8 * h), zslot, rfull + slot);
           }
         }
       }
@@ -816,7 +929,7 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
       if (lane == 0) {
         const int nk1 = __ldg(op.out_dk + s1);
         const int NP = nk1 <= 16 ? 16 : 32;
-        const bool merged = 4 * R * NP <= 512;
+        const bool merged = 4 * R * NP <= DMAX;
         const int bpart = merged ? NP * KP * 4 : Rg::BPART;
         const uint32_t idesc = tc_idesc_tf32(128, NP), idesc2 = tc_idesc_tf32(128, 2 * NP);
         const int c0 = ncommit;
@@ -827,7 +940,17 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
           if (!tc_mbar_wait(full, (uint32_t)ncommit & 1u)) ok = false;
           tc_fence_after();
           const uint64_t bdesc = bdesc0 + (uint64_t)((((term - tb) & 1) * Rg::BBUF) >> 4);
-          if (merged) {
+          if constexpr (TA) {
+            const uint32_t atm = tmem + TA_ACOL;
+            if (merged) {
+              const uint32_t acc0 = ncommit > c0 ? 1u : 0u;
+              if (tt.ktype == 1) kbt_issue_merged_ta<KP, 1>(tmem, atm, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
+              else if (tt.ktype == 2) kbt_issue_merged_ta<KP, 2>(tmem, atm, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
+              else kbt_issue_merged_ta<KP, 0>(tmem, atm, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
+            } else {
+              kbt_issue_ta<KP>(tmem, atm, bdesc, idesc, NP, nr, tt.ktype, tt.nk2, dinit, Rg::BPART);
+            }
+          } else if (merged) {
             const uint32_t acc0 = ncommit > c0 ? 1u : 0u;
             if (tt.ktype == 1) kbt_issue_merged<KP, 1>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
             else if (tt.ktype == 2) kbt_issue_merged<KP, 2>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
@@ -866,9 +989,9 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
       const int nk1 = __ldg(op.out_dk + s1);
       const int ld1 = __ldg(op.out_stride + s1);
       float2* Y = p.Y + ((long long)__ldg(op.out_off + s1) + (long long)i0 * ld1) * nb + v;
-      const float sc = p.yscale ? (float)p.yscale[v] : 1.f;
+      const float sc = p.yscale ? (float)p.yscale[(long long)kb_slot(p.kslot) * nb + v] : 1.f;
       const int NP = nk1 <= 16 ? 16 : 32;
-      const bool merged = 4 * R * NP <= 512;
+      const bool merged = 4 * R * NP <= DMAX;
       const int bpart = merged ? NP * KP * 4 : Rg::BPART;
       if (te == tb) {  // no term reaches this slab
         for (int e = wid >> 2; e < nr * nk1; e += 2)
@@ -886,7 +1009,8 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
       kbt_producer_sync();
       kbt_stage_pre<KP>(cur, pre, NP, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, MFd0, tid, bpart);
       kbt_producer_sync();
-      if (!kbt_zstep_ring<KP>(z, cur, nb, nr, b0, vloc, lane, MFs0, Cs0, MFd0, ring, rfull, rempty, g)) ok = false;
+      if (!kbt_zstep_ring<KP, L::NSLOT>(z, cur, nb, nr, b0, vloc, lane, MFs0, Cs0, MFd0, ring, rfull, rempty, g))
+        ok = false;
       for (int term = tb; term < te; ++term) {
         const int buf = (term - tb) & 1;
         const bool has_next = term + 1 < te;
@@ -898,10 +1022,19 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
         if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
         tc_fence_after();
         if (cur.ok && !cur.empty) {
+          if constexpr (TA) {
+            const uint32_t arow = tmem + TA_ACOL + ((uint32_t)(vq * 32) << 16);
 #pragma unroll
-          for (int r = 0; r < R; ++r)
-            if (r < nr) kbt_store_row<KP>(As + r * 4 * ATILE, z[r], vloc, b0);
-          tc_fence_proxy();
+            for (int r = 0; r < R; ++r)
+              if (r < nr) kbt_store_row_tmem<KP>(arow + (uint32_t)(4 * r * KP), z[r], b0);
+            tc_wait_st();
+            tc_fence_before();
+          } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+              if (r < nr) kbt_store_row<KP>(As + r * 4 * ATILE, z[r], vloc, b0);
+          }
+          tc_fence_proxy();  // the B tiles staged by generic stores, and the A tiles
           __syncwarp();
           if (lane == 0) tc_mbar_arrive(full);
           ++ncommit;
@@ -913,7 +1046,7 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
                             MFs0 + (buf ^ 1) * 8 * KB_WMAX, Cs0 + (buf ^ 1) * 8 * KB_WMAX,
                             MFd0 + (buf ^ 1) * Rg::MFD, tid, bpart);
           kbt_producer_sync();
-          if (!kbt_zstep_ring<KP>(z, nxt, nb, nr, b0, vloc, lane, MFs0 + (buf ^ 1) * 8 * KB_WMAX,
+          if (!kbt_zstep_ring<KP, L::NSLOT>(z, nxt, nb, nr, b0, vloc, lane, MFs0 + (buf ^ 1) * 8 * KB_WMAX,
                                   Cs0 + (buf ^ 1) * 8 * KB_WMAX, MFd0 + (buf ^ 1) * Rg::MFD, ring, rfull, rempty, g))
             ok = false;
           cur = nxt;
@@ -958,10 +1091,10 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
   if (wid == 8) tc_dealloc(tmem, NCOLS);
 }
 
-template <int KP>
+template <int KP, bool TA>
 __global__ void __launch_bounds__(320, 1) kb_matvec_tcp(BatchTC p, const __grid_constant__ CUtensorMap xmap) {
   extern __shared__ __align__(1024) char kbt_smem[];
-  kbt_persist<KP>(p, &xmap, kbt_smem);
+  kbt_persist<KP, TA>(p, &xmap, kbt_smem);
 }
 
 __global__ void __launch_bounds__(320, 1) kb_matvec_tc(BatchTC p, const __grid_constant__ CUtensorMap xmap) {
@@ -979,12 +1112,13 @@ __global__ void __launch_bounds__(320, 1) kb_matvec_tc(BatchTC p, const __grid_c
   else if (threadIdx.x == 0) atomicExch(p.err, KR_ERR_ARG);  // KP = 8, 16 tiles go to kb_matvec_tcp
 }
 
-// TMA descriptor of an X buffer [dim][nb] (complex64 as 8-byte elements):
-// boxes of 128 vectors x 8 rows, zero fill outside the array
+// TMA descriptor of the basis slots behind X, [nslots][dim][nb] (complex64 as
+// 8-byte elements): boxes of 128 vectors x 8 rows of one slot, zero fill
+// outside the slot's rows (a window never reads into the next slot)
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-static int encode_xmap(kr_ctx* ctx, const float2* X, long long dim, int nb, CUtensorMap* m) {
+static int encode_xmap(kr_ctx* ctx, const float2* X, long long dim, int nb, int nslots, CUtensorMap* m) {
   static EncodeTiledFn fn = nullptr;
   static std::once_flag once;
   std::call_once(once, [] {
@@ -995,20 +1129,21 @@ static int encode_xmap(kr_ctx* ctx, const float2* X, long long dim, int nb, CUte
       fn = reinterpret_cast<EncodeTiledFn>(f);
   });
   if (!fn) return set_err(ctx, KR_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-  const cuuint64_t gdim[2] = {(cuuint64_t)nb, (cuuint64_t)dim};
-  const cuuint64_t gstride[1] = {(cuuint64_t)nb * sizeof(float2)};
-  const cuuint32_t box[2] = {128, 8};
-  const cuuint32_t estride[2] = {1, 1};
-  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<float2*>(X), gdim, gstride, box, estride,
+  const cuuint64_t gdim[3] = {(cuuint64_t)nb, (cuuint64_t)dim, (cuuint64_t)std::max(1, nslots)};
+  const cuuint64_t gstride[2] = {(cuuint64_t)nb * sizeof(float2), (cuuint64_t)dim * nb * sizeof(float2)};
+  const cuuint32_t box[3] = {128, 8, 1};
+  const cuuint32_t estride[3] = {1, 1, 1};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<float2*>(X), gdim, gstride, box, estride,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return set_err(ctx, KR_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
   return KR_OK;
 }
 
-int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, const int* cls, int* work, cudaStream_t st) {
+int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, const int* cls, int* work, bool tmem_a,
+                 cudaStream_t st) {
   CUtensorMap xmap;
-  const int rc = encode_xmap(ctx, p.X, dim, p.nb, &xmap);
+  const int rc = encode_xmap(ctx, p.X, dim, p.nb, p.nslots, &xmap);
   if (rc != KR_OK) return rc;
   const int nvb = p.nb / 128;
   KR_CUDA(ctx, cudaMemsetAsync(work, 0, 2 * sizeof(int), st));
@@ -1022,14 +1157,24 @@ int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, const int* cls, i
     q.nvb = nvb;
     q.work = work + c;
     const int grid = (int)std::min<long long>((long long)n * nvb, ctx->nsm);
-    if (c == 0) {
-      KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tcp<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (tmem_a) {
+      if (c == 0) {
+        KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tcp<8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          KbtPers<8, true>::TOTAL));
+        kb_matvec_tcp<8, true><<<grid, 320, KbtPers<8, true>::TOTAL, st>>>(q, xmap);
+      } else {
+        KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tcp<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          KbtPers<16, true>::TOTAL));
+        kb_matvec_tcp<16, true><<<grid, 320, KbtPers<16, true>::TOTAL, st>>>(q, xmap);
+      }
+    } else if (c == 0) {
+      KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tcp<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         KbtPers<8>::TOTAL));
-      kb_matvec_tcp<8><<<grid, 320, KbtPers<8>::TOTAL, st>>>(q, xmap);
+      kb_matvec_tcp<8, false><<<grid, 320, KbtPers<8>::TOTAL, st>>>(q, xmap);
     } else {
-      KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tcp<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tcp<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         KbtPers<16>::TOTAL));
-      kb_matvec_tcp<16><<<grid, 320, KbtPers<16>::TOTAL, st>>>(q, xmap);
+      kb_matvec_tcp<16, false><<<grid, 320, KbtPers<16>::TOTAL, st>>>(q, xmap);
     }
     KR_CUDA(ctx, cudaGetLastError());
   }
@@ -1084,6 +1229,76 @@ __global__ void __launch_bounds__(128) kb_mma_probe(const float* A, const float*
   tc_fence_before();
   __syncthreads();
   if (wid == 0) tc_dealloc(taddr, 32);
+}
+
+// the same product with A in TMEM (written by tcgen05.st, row m in lane m):
+// the operand path of MMAs whose A comes from registers of the lane's thread
+__global__ void __launch_bounds__(128) kb_mma_probe_ta(const float* A, const float* B, float* D, int* err) {
+  __shared__ __align__(128) float sb[16 * 16];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tbase;
+  const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+  for (int e = tid; e < 16 * 16; e += 128) sb[tc_kmajor_off(e >> 4, e & 15, 16) >> 2] = B[e];
+  if (wid == 0) tc_alloc(&tbase, 64);
+  if (tid == 0) tc_mbar_init(&bar, 1);
+  tc_fence_proxy();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t taddr = tbase;
+  const uint32_t lanebase = (uint32_t)(32 * wid) << 16;
+  float a[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) a[j] = A[(32 * wid + lane) * 16 + j];
+  tc_st8(taddr + lanebase + 32u, a);
+  tc_st8(taddr + lanebase + 40u, a + 8);
+  tc_wait_st();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (tid == 0) {
+    const uint32_t idesc = tc_idesc_tf32(128, 16);
+    for (int s = 0; s < 2; ++s)  // K = 16 in two steps of 8
+      tc_mma_tf32_ta(taddr, taddr + 32u + 8u * s, tc_desc(tc_smem_u32(sb) + 256u * s, 128u, 512u), idesc,
+                     (uint32_t)s);
+    tc_commit(&bar);
+  }
+  if (!tc_mbar_wait(&bar, 0) && lane == 0) atomicExch(err, KR_ERR_TIMEOUT);
+  tc_fence_after();
+  float v[16];
+  tc_ld16(taddr + lanebase, v);
+#pragma unroll
+  for (int j = 0; j < 16; ++j) D[(32 * wid + lane) * 16 + j] = v[j];
+  tc_fence_before();
+  __syncthreads();
+  if (wid == 0) tc_dealloc(taddr, 64);
+}
+
+extern "C" int kr_probe_mma_ta(kr_ctx* ctx, const float* a, const float* b, float* d) {
+  if (!ctx || !a || !b || !d) return set_err(ctx, KR_ERR_ARG, "kr_probe_mma_ta: NULL argument");
+  KR_DEVICE_SCOPE(ctx, ctx->device);
+  const size_t na = 128 * 16, nbb = 16 * 16, nd = 128 * 16;
+  char* buf = nullptr;
+  KR_CUDA(ctx, cudaMalloc(&buf, sizeof(float) * (na + nbb + nd) + 16));
+  float* dA = reinterpret_cast<float*>(buf);
+  float* dB = dA + na;
+  float* dD = dB + nbb;
+  int* derr = reinterpret_cast<int*>(dD + nd);
+  int herr = 0;
+  cudaError_t e = cudaMemcpy(dA, a, sizeof(float) * na, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dB, b, sizeof(float) * nbb, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(derr, 0, sizeof(int));
+  if (e == cudaSuccess) {
+    kb_mma_probe_ta<<<1, 128>>>(dA, dB, dD, derr);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(d, dD, sizeof(float) * nd, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(buf);
+  KR_CUDA(ctx, e);
+  if (herr) return set_err(ctx, herr, "kr_probe_mma_ta: MMA completion wait gave up");
+  return KR_OK;
 }
 
 extern "C" int kr_probe_mma(kr_ctx* ctx, const float* a, const float* b, float* d) {

@@ -167,6 +167,131 @@ static __device__ double2 grid_partials_sum2(const double2* part, int n, double2
 }
 
 // ---------------------------------------------------------------------------
+// The row-task mat-vec below (matvec_cta_tasks) with its products in FP32:
+// same tasks, terms and staging; see its F32 argument.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cfmaf(float2& s, float2 a, float2 b) {
+  s.x = fmaf(a.x, b.x, fmaf(-a.y, b.y, s.x));
+  s.y = fmaf(a.x, b.y, fmaf(a.y, b.x, s.y));
+}
+template <bool ALPHA>
+__device__ void matvec_cta_tasks_f32(const DevOp& op, const double2* __restrict__ x, double xscale,
+                                     double2* __restrict__ y, unsigned* counter, double2* task_alpha,
+                                     double2* smem, double2* red, const int* seg_done, const int* slab_seg) {
+  __shared__ int s_task;
+  const int tid = threadIdx.x;
+  float2* zb[2] = {reinterpret_cast<float2*>(smem), reinterpret_cast<float2*>(smem) + op.zmax};
+  const float xs = (float)xscale;
+  for (;;) {
+    if (tid == 0) s_task = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    const int t = s_task;
+    __syncthreads();
+    if (t >= op.ntask) break;
+    const int task = __ldg(op.task_order + t);
+    const int s1 = __ldg(op.task_slab + task);
+    if (seg_done && __ldcg(seg_done + __ldg(slab_seg + s1))) {
+      if (ALPHA && tid == 0) task_alpha[task] = make_double2(0.0, 0.0);
+      continue;
+    }
+    const int i0 = __ldg(op.task_row0 + task);
+    const int nr = __ldg(op.task_nrows + task);
+    const int nk1 = __ldg(op.out_dk + s1);
+    const int npair = nr * nk1;
+    float2 acc[KR_QMAX];
+#pragma unroll
+    for (int q = 0; q < KR_QMAX; ++q) acc[q] = make_float2(0.f, 0.f);
+    const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
+    for (int term = tb; term < te; ++term) {
+      float2* Z = zb[(term - tb) & 1];
+      const int s2 = __ldg(op.t_in + term);
+      const int kbk = __ldg(op.t_k + term);
+      const int mfi = __ldg(op.t_mf + term);
+      const int nk2 = __ldg(op.in_dk + s2);
+      const double2* X = x + __ldg(op.in_off + s2);
+      const int W = __ldg(op.mf_width + mfi);
+      const int* col = op.m_col + __ldg(op.mf_col_off + mfi);
+      const float2* mf = op.mf_f32 + __ldg(op.mf_off + mfi);
+      const int mtype = __ldcg(op.mf_type + mfi);
+      const int nz = nr * nk2;
+      for (int p = tid; p < nz; p += blockDim.x) {
+        const int r = p / nk2;
+        const int b = p - r * nk2;
+        const int base = (i0 + r) * W;
+        float2 z = make_float2(0.f, 0.f);
+        for (int w = 0; w < W; ++w) {
+          const float2 m = __ldcg(mf + base + w);
+          const double2 xd = ldcg2(X + (long long)__ldg(col + base + w) * nk2 + b);
+          const float2 xv = make_float2((float)xd.x, (float)xd.y);
+          if (mtype == 1) {
+            z.x = fmaf(m.x, xv.x, z.x);
+            z.y = fmaf(m.x, xv.y, z.y);
+          } else if (mtype == 2) {
+            z.x = fmaf(-m.y, xv.y, z.x);
+            z.y = fmaf(m.y, xv.x, z.y);
+          } else {
+            cfmaf(z, m, xv);
+          }
+        }
+        Z[p] = make_float2(z.x * xs, z.y * xs);
+      }
+      const float* KT = op.k_f32 + __ldg(op.k_off + kbk);
+      const int ktype = __ldg(op.k_type + kbk);
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < KR_QMAX; ++q) {
+        const int p = tid + blockDim.x * q;
+        if (p < npair) {
+          const int r = p / nk1;
+          const int a = p - r * nk1;
+          const float2* zr = Z + r * nk2;
+          float2 s = acc[q];
+          if (ktype == 1) {
+            for (int b = 0; b < nk2; ++b) {
+              const float kv = __ldg(KT + b * nk1 + a);
+              const float2 zv = zr[b];
+              s.x = fmaf(kv, zv.x, s.x);
+              s.y = fmaf(kv, zv.y, s.y);
+            }
+          } else if (ktype == 2) {
+            for (int b = 0; b < nk2; ++b) {
+              const float kv = __ldg(KT + b * nk1 + a);
+              const float2 zv = zr[b];
+              s.x = fmaf(-kv, zv.y, s.x);
+              s.y = fmaf(kv, zv.x, s.y);
+            }
+          } else {
+            const float2* KT2 = reinterpret_cast<const float2*>(KT);
+            for (int b = 0; b < nk2; ++b) cfmaf(s, __ldg(KT2 + b * nk1 + a), zr[b]);
+          }
+          acc[q] = s;
+        }
+      }
+    }
+    const long long obase = __ldg(op.out_off + s1) + (long long)i0 * nk1;
+    double2 al = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int q = 0; q < KR_QMAX; ++q) {
+      const int p = tid + blockDim.x * q;
+      if (p < npair) {
+        const double2 yv = make_double2((double)acc[q].x, (double)acc[q].y);
+        y[obase + p] = yv;
+        if (ALPHA) {
+          const double2 v = cscale(ldcg2(x + obase + p), xscale);
+          al = cadd(al, cconjmul(yv, v));
+        }
+      }
+    }
+    if (ALPHA) {
+      al = block_sum2(al, red);
+      if (tid == 0) task_alpha[task] = al;
+    } else {
+      __syncthreads();
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Kronecker mat-vec over the row tasks of one CTA. A task is a block of nr
 // consecutive rows of one output slab; all threads of the CTA work on it:
 //   Z_t[r, b]   = xscale * sum_w MF_t[i0 + r, w] * x[s2][col_t(i0 + r, w), b]
@@ -180,11 +305,19 @@ static __device__ double2 grid_partials_sum2(const double2* part, int n, double2
 // ---------------------------------------------------------------------------
 // seg_done / slab_seg (optional): tasks of an output slab whose segment is
 // done are skipped (their alpha partial is zero), for the segmented step.
-template <bool ALPHA>
+// F32: the products in single precision on the FP32 pipes (GB300's FP64 rate
+// is 1/58 of its FP32 rate): x read in FP64 and rounded, the FP32 copies of K
+// and MF (k_f32, mf_f32), Z and the sums in FP32, y and the alpha partial in
+// FP64 (the Lanczos scalars stay FP64).
+template <bool ALPHA, bool F32 = false>
 __device__ void matvec_cta_tasks(const DevOp& op, const double2* __restrict__ x, double xscale,
                                  double2* __restrict__ y, unsigned* counter, double2* task_alpha,
                                  double2* smem, double2* red, const int* seg_done = nullptr,
                                  const int* slab_seg = nullptr) {
+  if constexpr (F32) {
+    matvec_cta_tasks_f32<ALPHA>(op, x, xscale, y, counter, task_alpha, smem, red, seg_done, slab_seg);
+    return;
+  }
   __shared__ int s_task;
   const int tid = threadIdx.x;
   double2* zb[2] = {smem, smem + op.zmax};

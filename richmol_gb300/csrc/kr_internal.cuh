@@ -84,6 +84,7 @@ struct DeviceScope {
 
 struct kr_op {
   kr_ctx* ctx = nullptr;
+  unsigned long long uid = 0;  // creation number, unique in the process (keys of recorded steps)
   DevOp dev{};
   DevField field{};
   std::vector<void*> allocs;

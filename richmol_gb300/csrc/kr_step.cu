@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -523,6 +524,7 @@ __device__ __forceinline__ double seg_warp_sum(const double* part, int b, int e,
   return warp_sum(s);
 }
 
+template <bool F32>
 __global__ void __launch_bounds__(KR_THREADS, 2) kr_seg_step_kernel(SegArgs a) {
   extern __shared__ double2 smem_dyn[];
   __shared__ StepSmem ss;
@@ -553,7 +555,7 @@ __global__ void __launch_bounds__(KR_THREADS, 2) kr_seg_step_kernel(SegArgs a) {
   SEG_BARRIER();
 
   // w = H V0, alpha_0 = vdot(w, V0), W0 = w - alpha_0 V0 (tdse.py:443-446)
-  matvec_cta_tasks<true>(a.op, V0, 1.0, a.w, a.counters, a.task_alpha, smem_dyn, ss.red, a.done, a.slab_seg);
+  matvec_cta_tasks<true, F32>(a.op, V0, 1.0, a.w, a.counters, a.task_alpha, smem_dyn, ss.red, a.done, a.slab_seg);
   SEG_BARRIER();
   if (warp == 0)
     for (int sg = blockIdx.x; sg < a.nseg; sg += nblk) {
@@ -613,7 +615,8 @@ __global__ void __launch_bounds__(KR_THREADS, 2) kr_seg_step_kernel(SegArgs a) {
     }
     SEG_BARRIER();
     // w = H V_k (tdse.py:467-468)
-    matvec_cta_tasks<true>(a.op, Vk, 1.0, a.w, a.counters + k, a.task_alpha, smem_dyn, ss.red, a.done, a.slab_seg);
+    matvec_cta_tasks<true, F32>(a.op, Vk, 1.0, a.w, a.counters + k, a.task_alpha, smem_dyn, ss.red, a.done,
+                                a.slab_seg);
     SEG_BARRIER();
     // alpha_k and exp(fac T_{0..k}) e0 per segment (tdse.py:474)
     if (warp == 0)
@@ -827,7 +830,9 @@ static cudaError_t ensure_step_smem(size_t smem) {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(kr_matvec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(kr_seg_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(kr_seg_step_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(kr_seg_step_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess) g_smem_max = smem;
   return e;
 }
@@ -975,7 +980,9 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   const std::vector<int>& in_stride = dchk.in_stride;
   const std::vector<std::vector<int>>& by_out = dchk.by_out;
 
+  static std::atomic<unsigned long long> next_uid{1};
   kr_op* op = new kr_op();
+  op->uid = next_uid.fetch_add(1);
   op->ctx = ctx;
   op->maxorder = d->maxorder;
   op->npart = d->npart;
@@ -1166,7 +1173,10 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
         ts.clear();
         break;  // outside the batched mat-vec's shapes (kr_batch_create rejects such operators)
       }
-      const int kp = maxnk2 <= 8 ? 8 : maxnk2 <= 16 ? 16 : 32;
+      // an output slab wider than 16 columns takes tiles of at most 4 rows
+      // (KP >= 16), so that its accumulators (2 R NP TMEM columns, NP = 32)
+      // leave half of the tensor memory to the A tiles of the TMEM form
+      const int kp = (maxnk2 <= 8 && d->out_dk[s] <= 16) ? 8 : maxnk2 <= 16 ? 16 : 32;
       const int R = 64 / kp, dm1 = d->out_dm[s];
       for (int i0 = 0; i0 < dm1; i0 += R) {
         ts.push_back(s);
@@ -1817,7 +1827,15 @@ struct kr_seg {
   int *done = nullptr, *kout = nullptr, *ufin = nullptr, *nactive = nullptr;
   double *chunk_b = nullptr, *chunk_c = nullptr;
   long long launches = 0;
+  bool f32 = false;  // mat-vec products in FP32 (kr_seg_set_precision)
 };
+
+extern "C" int kr_seg_set_precision(kr_seg* g, int32_t mode) {
+  if (!g || (mode != KR_SEG_F64 && mode != KR_SEG_F32_MATVEC))
+    return set_err(g ? g->op->ctx : nullptr, KR_ERR_ARG, "kr_seg_set_precision: bad argument");
+  g->f32 = mode == KR_SEG_F32_MATVEC;
+  return KR_OK;
+}
 
 extern "C" void kr_seg_destroy(kr_seg* g) {
   if (!g) return;
@@ -1922,7 +1940,11 @@ extern "C" int kr_seg_create(kr_op* op, int32_t nseg, const int32_t* slab_seg, k
     return set_err(op->ctx, KR_ERR_CUDA, "kr_seg_create: cannot raise the dynamic shared memory");
   }
   int occ = 0;
-  cudaError_t ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kr_seg_step_kernel, KR_THREADS, op->smem);
+  int occ32 = 0;
+  cudaError_t ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kr_seg_step_kernel<false>, KR_THREADS, op->smem);
+  if (ce == cudaSuccess)
+    ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ32, kr_seg_step_kernel<true>, KR_THREADS, op->smem);
+  occ = std::min(occ, occ32);
   if (ce != cudaSuccess || occ < 1) {
     kr_seg_destroy(g);
     return set_err(op->ctx, KR_ERR_CUDA, "kr_seg_step_kernel cannot be resident");
@@ -1977,8 +1999,8 @@ extern "C" int kr_seg_step(kr_seg* g, void* states, const void* phase, double fa
   KR_CUDA(op->ctx, cudaMemsetAsync(op->bar, 0, sizeof(unsigned), st));  // arrival count only
   KR_CUDA(op->ctx, ensure_step_smem(op->smem));
   void* args[] = {&a};
-  KR_CUDA(op->ctx, cudaLaunchCooperativeKernel((void*)kr_seg_step_kernel, dim3(g->grid), dim3(KR_THREADS), args,
-                                               op->smem, st));
+  KR_CUDA(op->ctx, cudaLaunchCooperativeKernel(g->f32 ? (void*)kr_seg_step_kernel<true> : (void*)kr_seg_step_kernel<false>,
+                                               dim3(g->grid), dim3(KR_THREADS), args, op->smem, st));
   g->launches++;
   int hs = 0;
   KR_CUDA(op->ctx, cudaMemcpyAsync(&hs, op->status, sizeof(int), cudaMemcpyDeviceToHost, st));

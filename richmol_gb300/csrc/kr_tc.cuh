@@ -60,6 +60,17 @@ __device__ __forceinline__ void tc_mma_tf32(uint32_t dtmem, uint64_t adesc, uint
       : "memory");
 }
 
+// D (TMEM) = A * B^T (+ D if acc) with A in TMEM: lane m holds row m of A, its
+// K values in consecutive 32-bit columns from atmem on; issued by one thread
+__device__ __forceinline__ void tc_mma_tf32_ta(uint32_t dtmem, uint32_t atmem, uint64_t bdesc, uint32_t idesc,
+                                               uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(dtmem),
+      "r"(atmem), "l"(bdesc), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
 // arrive on the mbarrier once every MMA issued so far by this thread is done
 __device__ __forceinline__ void tc_commit(uint64_t* mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -86,6 +97,23 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
 #pragma unroll
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
+
+// 8 consecutive 32-bit TMEM columns of this thread's lane from v (the lane
+// rule of tc_ld16); tc_wait_st() before the values are used by an MMA
+__device__ __forceinline__ void tc_st8(uint32_t taddr, const float* v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
+               "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+               "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+               "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+               : "memory");
+}
+__device__ __forceinline__ void tc_st4(uint32_t taddr, const float* v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(taddr),
+               "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+               "r"(__float_as_uint(v[3]))
+               : "memory");
+}
+__device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // d = a * b + c on both FP32 lanes (PTX fma.rn.f32x2, one instruction)
 __device__ __forceinline__ float2 tc_ffma2(float2 a, float2 b, float2 c) {
@@ -150,5 +178,13 @@ __device__ __forceinline__ void tc_tma_load_2d(void* dst, const void* tmap, int 
       "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
           tc_smem_u32(dst)),
       "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(tc_smem_u32(bar))
+      : "memory");
+}
+// 3-D TMA tile load: box at element coordinates (x, y, z); the same rules
+__device__ __forceinline__ void tc_tma_load_3d(void* dst, const void* tmap, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+          "r"(tc_smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(z), "r"(tc_smem_u32(bar))
       : "memory");
 }

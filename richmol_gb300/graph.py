@@ -9,6 +9,11 @@ each recorded step carries its own field) and the persistent step launch
 no host work in between. The library allocates nothing while stepping, so the
 recording holds only these launches and two small memsets per step.
 
+``EnsembleGraph`` does the same for the batched ensemble path: per step the
+field launch and the batched step's own nodes (its Krylov loop is a
+conditional WHILE node on the device, so a recorded step needs no host
+decision between iterations).
+
 Operators of up to 16 parts record their field coefficients as kernel
 parameters. Above that (or with ``schedule=True``) the fields of all recorded
 steps are uploaded once before recording (kr_set_field_schedule) and each
@@ -87,3 +92,58 @@ class StepGraph:
                 raise ValueError("Lanczos reached maximum order without convergence") from None
             raise
         return self.vecs
+
+
+class EnsembleGraph:
+    """A run of batched ensemble steps (batch.Ensemble.step) recorded once as
+    a CUDA graph and replayed with one launch.
+
+    Args:
+        ens : batch.Ensemble         the ensemble (its states are propagated in place)
+        hamiltonian : callable t -> CarTens with the field of time t set
+        times : the times of the recorded steps
+        schedule : None (fields from device memory above 16 parts), or True /
+                   False to force either form
+    """
+
+    def __init__(self, ens, hamiltonian, times, schedule=None):
+        if ens.matvec == "auto":
+            raise ValueError("tune the ensemble's mat-vec kind (one step) before recording")
+        self.ens = ens
+        self.times = list(times)
+        dev = torch.device("cuda", torch.cuda.current_device())
+        phase = ens.tdse._h0_phase(ens.H0, ens.tdse.exp_fac, dev) if ens.H0 is not None else None
+        self.plan = hamiltonian(self.times[0]).device_operator(split=ens.split)
+        if schedule is None:
+            schedule = len(self.plan.sources) > _native.KR_PART_INLINE
+        elif not schedule and len(self.plan.sources) > _native.KR_PART_INLINE:
+            raise ValueError(f"above {_native.KR_PART_INLINE} operator parts a recorded step needs the field schedule")
+        self.schedule = bool(schedule)
+        if self.schedule:
+            steps = []
+            for t in self.times:
+                H = hamiltonian(t)
+                if H._plan(split=ens.split) is not self.plan:
+                    raise ValueError("the recorded steps must share one operator (the same factor sources)")
+                steps.append(H._part_states())
+            self.plan.set_field_schedule(steps)
+            self._schedule_gen = self.plan.schedule_gen
+        self.graph = torch.cuda.CUDAGraph()
+        stream = torch.cuda.Stream()
+        stream.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.graph(self.graph, stream=stream):
+            for i, t in enumerate(self.times):
+                if self.schedule:
+                    self.plan.set_field_step(i)
+                    ens._step_plan(self.plan, phase, sync=False)
+                else:
+                    ens.step(hamiltonian(t), sync=False)
+        torch.cuda.current_stream().wait_stream(stream)
+
+    def replay(self):
+        """Runs the recorded steps and reports a step error afterwards
+        (KrylovError, code KR_ERR_MAXORDER when mmax was not enough)."""
+        if self.schedule and self.plan.schedule_gen != self._schedule_gen:
+            raise RuntimeError("the operator's field schedule was replaced after this recording")
+        self.graph.replay()
+        self.ens.sync()

@@ -33,9 +33,14 @@ class MoleculeSet:
                                       (``tensors[m].field(E_m(t))``) before each step
         maxorder : int                Lanczos basis capacity (tdse.py default 100)
         tol : float                   stopping tolerance (tdse.py default 1e-15)
+        precision : str               "f64" (default): every product in FP64, as the
+                                      reference; "mixed": the mat-vec products in FP32
+                                      on the FP32 pipes (complex64 accuracy, about 1e-7
+                                      relative per mat-vec) with states, Krylov vectors,
+                                      Lanczos scalars and the stopping test in FP64
     """
 
-    def __init__(self, tdse, h0s, tensors, maxorder=100, tol=1e-15):
+    def __init__(self, tdse, h0s, tensors, maxorder=100, tol=1e-15, precision="f64"):
         assert len(h0s) == len(tensors) and len(h0s) > 0
         self.tdse = tdse
         self.h0s, self.tensors = list(h0s), list(tensors)
@@ -55,6 +60,11 @@ class MoleculeSet:
         _native.check(_native.lib().kr_seg_create(self.plan.op, len(blocks), self._slab_seg.ctypes.data,
                                                   ctypes.byref(h)), self.plan.ctx)
         self.handle = h
+        if precision not in ("f64", "mixed"):
+            raise ValueError("precision must be 'f64' or 'mixed'")
+        self.precision = precision
+        _native.check(_native.lib().kr_seg_set_precision(
+            h, _native.KR_SEG_F32_MATVEC if precision == "mixed" else _native.KR_SEG_F64), self.plan.ctx)
         self.dims = [sum(dm * dk for _, _, dm, dk in b[0]) for b in blocks]
         self.offsets = np.concatenate([[0], np.cumsum(self.dims)[:-1]]).astype(np.int64)
         self.dim = int(sum(self.dims))

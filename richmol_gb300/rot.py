@@ -284,6 +284,28 @@ def _tensor_spherical(arg):
     return rank, carts, irreps, Us, Ux, flat
 
 
+@lru_cache(maxsize=None)
+def _m_factors(carts, uxo_bytes, sigmas, J1, J2, o, thr):
+    """M factors of one (J1, J2, omega) block: sqrt((2J1+1)(2J2+1)) (-1)^|b|
+    sum_sigma Ux[c, sigma] (J2 omega J1; a sigma -b) per Cartesian component c,
+    as CSR matrices. They depend on the tensor's rank and lab-frame
+    transformation only, not on the molecule, so every molecule with the same
+    J pair shares them (a set of molecules builds each once)."""
+    Uxo = np.frombuffer(uxo_bytes, dtype=np.complex128).reshape(len(carts), len(sigmas))
+    T = three_j_rows(J2, o, J1)
+    mfull = np.zeros((len(carts), 2 * J1 + 1, 2 * J2 + 1), dtype=np.complex128)
+    fac_m = math.sqrt((2 * J1 + 1) * (2 * J2 + 1))
+    a = np.arange(-J2, J2 + 1)
+    for si, sg in enumerate(sigmas):
+        b = a + sg
+        ok = np.abs(b) <= J1
+        aa, bb = a[ok], b[ok]
+        v = T[sg + o, aa + J2] * np.where(bb % 2, -1.0, 1.0)
+        mfull[:, bb + J1, aa + J2] += fac_m * v[None, :] * Uxo[:, si][:, None]
+    mfull[np.abs(mfull) < thr] = 0
+    return {cart: csr_matrix(mfull[ci]) for ci, cart in enumerate(carts) if np.any(mfull[ci])}
+
+
 def lab_tensor(arg, sol, thresh=None):
     """LabTensor equivalent: the K and M factors of a lab-frame tensor, a named
     observable ('costheta', 'cos2theta'), or the field-free Hamiltonian
@@ -313,13 +335,11 @@ def lab_tensor(arg, sol, thresh=None):
                 if abs(J1 - J2) > o:
                     continue
                 T = three_j_rows(J2, o, J1)  # (J2 o J1; a sigma -(a+sigma))
-                sigmas = [irreps[i][1] for i in sig[o]]
+                sigmas = tuple(irreps[i][1] for i in sig[o])
                 # primitive matrix elements <J1,b| . |J2,a>, b = a + sigma:
                 # K: (-1)^|b| sum_s 3j * UsT[s]; M: sqrt((2J1+1)(2J2+1)) (-1)^|b| sum_s Ux[c,s] 3j
                 lin = sol.mol.linear
                 kfull = np.zeros((2 * J1 + 1, 2 * J2 + 1), dtype=np.complex128)
-                mfull = np.zeros((len(carts), 2 * J1 + 1, 2 * J2 + 1), dtype=np.complex128)
-                fac_m = math.sqrt((2 * J1 + 1) * (2 * J2 + 1))
                 a = np.arange(-J2, J2 + 1)
                 for si, sg in enumerate(sigmas):
                     b = a + sg
@@ -327,10 +347,8 @@ def lab_tensor(arg, sol, thresh=None):
                     aa, bb = a[ok], b[ok]
                     v = T[sg + o, aa + J2] * np.where(bb % 2, -1.0, 1.0)
                     kfull[bb + J1, aa + J2] += v * UsT[o][si]
-                    mfull[:, bb + J1, aa + J2] += fac_m * v[None, :] * Uxo[o][:, si][:, None]
                 kprim = kfull[J1:J1 + 1, J2:J2 + 1] if lin else kfull
-                mfull[np.abs(mfull) < thr] = 0
-                mcsr = {cart: csr_matrix(mfull[ci]) for ci, cart in enumerate(carts) if np.any(mfull[ci])}
+                mcsr = _m_factors(tuple(carts), Uxo[o].tobytes(), sigmas, J1, J2, o, float(thr))
                 for s2, (_, C2) in sol.states[J2].items():
                     for s1, (_, C1) in sol.states[J1].items():
                         K = np.conj(C1.T) @ kprim @ C2

@@ -9,7 +9,9 @@ state). This is the loop a user of the reference writes around
 run for many requests at once:
 
 * requests arrive over time (a Poisson stream in ``poisson_requests``);
-* a request is admitted as soon as it has arrived and its device memory
+* a job's host set-up (its molecule's factors) starts when its request
+  arrives, on a builder thread, while admitted jobs run (``prebuild``);
+* a request is admitted as soon as it has arrived, is built, and its device memory
   (``Job.device_bytes``: state, Krylov basis, operator) fits the HBM budget
   beside the jobs already running, first fit in arrival order;
 * every admitted job owns its operator plans (private factor sources, so no
@@ -118,6 +120,8 @@ class Job:
         return batch_device_bytes(dim, nvec, self.mmax, 2 * (self.req.jmax + 1)) + 16 * dim * (nvec + 1) + (64 << 20)
 
     def build(self):
+        if hasattr(self, "wl"):
+            return
         req = self.req
         mol = rot.Molecule(B=req.abc, sym="C1", pol=req.pol)
         self.wl = workloads.Workload("request_%d" % req.rid, mol, req.jmax, 0.0, req.t_end, req.dt, None, req.pulse)
@@ -178,11 +182,12 @@ class Server:
                  of the scheduling on the host)
     """
 
-    def __init__(self, budget_bytes=150e9, max_active=16, make_job=None, device=0):
+    def __init__(self, budget_bytes=150e9, max_active=16, make_job=None, device=0, prebuild=True):
         self.budget = int(budget_bytes)
         self.max_active = int(max_active)
         self.make_job = make_job if make_job is not None else Job
         self.device = device
+        self.prebuild = bool(prebuild)
 
     def serve(self, requests, realtime=True):
         """Serves ``requests`` (their ``arrival`` seconds after the start; with
@@ -221,6 +226,30 @@ class Server:
                 lock.notify_all()
 
         jobs = {}
+        built = {}  # rid -> True once the job's host set-up (factor build) is done
+        if self.prebuild:
+            # host set-up off the latency path: one builder thread prepares the
+            # jobs in arrival order as they arrive, while admitted jobs run
+            for req in pending:
+                jobs[req.rid] = self.make_job(req)
+
+            def builder():
+                for req in list(pending):
+                    if realtime:
+                        wait = req.arrival - now()
+                        if wait > 0:
+                            time.sleep(wait)
+                    job = jobs[req.rid]
+                    try:
+                        if hasattr(job, "build"):
+                            job.build()
+                    except Exception:
+                        pass  # run() repeats the build and reports the error
+                    with lock:
+                        built[req.rid] = True
+                        lock.notify_all()
+            bth = threading.Thread(target=builder, daemon=True)
+            bth.start()
         with lock:
             while pending or state["active"] > 0:
                 t = now()
@@ -230,6 +259,8 @@ class Server:
                         break
                     if state["active"] >= self.max_active:
                         break
+                    if self.prebuild and not built.get(req.rid):
+                        continue  # its build is still running
                     job = jobs.get(req.rid)
                     if job is None:
                         job = jobs[req.rid] = self.make_job(req)
@@ -253,11 +284,12 @@ class Server:
                     admitted = True
                 if admitted:
                     continue
-                # wait for a job to finish or the next arrival
+                # wait for a job to finish, a build to end or the next arrival
                 timeout = None
                 if realtime and pending and pending[0].arrival > t:
                     timeout = pending[0].arrival - t
-                if state["active"] > 0 or timeout is not None:
+                waiting_build = self.prebuild and any(not built.get(r.rid) for r in pending)
+                if state["active"] > 0 or timeout is not None or waiting_build:
                     lock.wait(timeout=timeout if timeout is not None else 1.0)
         for th in threads:
             th.join()

@@ -34,6 +34,7 @@ class Workload:
         self.pol = rot.lab_tensor(mol.pol, self.sol)
         self.dip = rot.lab_tensor(mol.dip, self.sol) if mol.dip is not None and np.any(mol.dip) else None
         self.cos2 = rot.lab_tensor("cos2theta", self.sol)
+        self.cos = rot.lab_tensor("costheta", self.sol)
         self.Hac = self.pol * (-0.5 * AUpol_x_Vm_to_invcm())
         self.Hdc = None
         if self.dc is not None and self.dip is not None:

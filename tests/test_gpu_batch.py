@@ -18,8 +18,8 @@ OBS_ATOL = 1e-6
 # relative max-norm error of one batched mat-vec against the FP64 mat-vec, per
 # kind: FP32 products (2^-24 rounding) and split-TF32 tensor-core products
 # (about 2^-21 per product)
-MV_RTOL = {"fp32": 2e-6, "tensor": 1e-5}
-MATVECS = ["tensor", "fp32"]
+MV_RTOL = {"fp32": 2e-6, "tensor": 1e-5, "tensor_tmem": 1e-5}
+MATVECS = ["tensor", "tensor_tmem", "fp32"]
 
 
 def _ct(case, name):
@@ -245,10 +245,11 @@ def test_batch_zero_field_matvec_is_exactly_zero():
     nvec = 8
     ens = Ensemble(td, h0, nvec)
     x = torch.randn((nvec, ens.dim), dtype=torch.complex128, device="cuda")
-    for kind in ("tensor", "fp32"):
+    from richmol_gb300.batch import _KINDS
+    for kind in _KINDS:
         from richmol_gb300 import _native
         _native.check(_native.lib().kr_batch_set_matvec(
-            ens.handle, {"tensor": _native.KR_MATVEC_TENSOR, "fp32": _native.KR_MATVEC_FP32}[kind]), ens.ctx)
+            ens.handle, _KINDS[kind]), ens.ctx)
         y = ens.apply(Hac, x)
         assert torch.count_nonzero(y).item() == 0, kind
 

@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 
-def _probe(a, b):
+def _probe(a, b, entry="kr_probe_mma"):
     from richmol_gb300 import _native
     from richmol_gb300.device import context
     if not os.path.exists(_native.LIB_PATH):
@@ -22,7 +22,7 @@ def _probe(a, b):
     a = np.ascontiguousarray(a, np.float32)
     b = np.ascontiguousarray(b, np.float32)
     d = np.zeros((128, 16), np.float32)
-    _native.check(_native.lib().kr_probe_mma(ctx, a.ctypes.data, b.ctypes.data, d.ctypes.data), ctx)
+    _native.check(getattr(_native.lib(), entry)(ctx, a.ctypes.data, b.ctypes.data, d.ctypes.data), ctx)
     return d
 
 
@@ -43,3 +43,15 @@ def test_mma_tf32_precision():
     ref = a.astype(np.float64) @ b.astype(np.float64).T
     scale = np.abs(a).astype(np.float64) @ np.abs(b).astype(np.float64).T
     assert np.all(np.abs(d - ref) <= 2.0 ** -9 * scale + 1e-6)
+
+
+def test_mma_with_a_in_tensor_memory():
+    """A in TMEM (lane m = row m, K along the columns), B in shared memory: the
+    same products as the shared-memory form, bit for bit."""
+    rng = np.random.default_rng(3)
+    a = rng.integers(-4, 5, (128, 16)).astype(np.float32)
+    b = rng.integers(-4, 5, (16, 16)).astype(np.float32)
+    assert np.array_equal(_probe(a, b, "kr_probe_mma_ta"), a @ b.T)
+    a = rng.standard_normal((128, 16)).astype(np.float32)
+    b = rng.standard_normal((16, 16)).astype(np.float32)
+    assert np.array_equal(_probe(a, b, "kr_probe_mma_ta"), _probe(a, b))

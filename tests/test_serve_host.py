@@ -136,3 +136,37 @@ def test_device_bytes_bound_the_batch_allocation():
     assert dim == sum((2 * J + 1) ** 2 for J in range(13))
     nvec = min(512, dim)
     assert serve.Job(r).device_bytes() > serve.batch_device_bytes(dim, nvec, 20)
+
+
+class BuildJob(FakeJob):
+    """A job with a host set-up (build) of ``abc[2]`` seconds; records when its
+    build ran and when it was admitted (run started)."""
+    events = []
+
+    def build(self):
+        t0 = time.perf_counter()
+        time.sleep(float(self.req.abc[2]))
+        BuildJob.events.append(("built", self.req.rid, t0, time.perf_counter()))
+
+    def run(self):
+        BuildJob.events.append(("run", self.req.rid, time.perf_counter(), None))
+        return super().run()
+
+
+def test_builds_start_at_arrival_and_overlap_running_jobs():
+    """Host set-up off the latency path: the builder thread starts each build
+    as its request arrives, while earlier jobs run; a job is admitted only
+    once built."""
+    reset()
+    BuildJob.events = []
+    reqs = [serve.Request(i, 0.05 * i, (10, 0.3, 0.1), 10, np.eye(3), (0, 0, 0, np.array([0, 0, 1.0])), 1.0)
+            for i in range(4)]
+    srv = serve.Server(budget_bytes=100, max_active=8, make_job=BuildJob, device=None)
+    results, stats = srv.serve(reqs, realtime=True)
+    assert all(results[i] == ("done", i) for i in range(4))
+    built = {rid: (t0, t1) for kind, rid, t0, t1 in BuildJob.events if kind == "built"}
+    run = {rid: t0 for kind, rid, t0, _ in BuildJob.events if kind == "run"}
+    for rid in range(4):
+        assert run[rid] >= built[rid][1]          # admitted once built
+    # the second build ran while the first job was running (not after it)
+    assert built[1][0] < run[0] + 0.3
