@@ -55,13 +55,13 @@ def parse(argv=None):
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="bound of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="headline measurement only")
-    p.add_argument("--matvec", choices=["tensor", "tensor_tmem", "fp32"], default="tensor",
+    p.add_argument("--matvec", choices=["tensor", "tensor_tmem", "fp32", "fp32_reg"], default="tensor",
                    help="batched mat-vec kind: tensor-core K contraction (split TF32; A operands in shared "
                         "or tensor memory) or FP32 FMAs")
-    p.add_argument("--serve-rate", type=float, default=8.0, help="requests per second of the serving sample")
-    p.add_argument("--serve-duration", type=float, default=2.0, help="seconds of arrivals of the serving sample")
+    p.add_argument("--serve-rate", type=float, default=2.0, help="requests per second of the serving sample")
+    p.add_argument("--serve-duration", type=float, default=3.0, help="seconds of arrivals of the serving sample")
     p.add_argument("--serve-jmax", type=int, nargs=2, default=[10, 50], help="Jmax range of the requests")
-    p.add_argument("--serve-tend", type=float, default=0.1, help="ps propagated per request (dt 10 fs)")
+    p.add_argument("--serve-tend", type=float, default=5.0, help="ps propagated per request (dt 10 fs)")
     p.add_argument("--serve-budget-gb", type=float, default=150.0)
     p.add_argument("--uneven-n", type=int, default=256, help="molecules of the uneven-size batch")
     p.add_argument("--uneven-jmax", type=int, nargs=2, default=[10, 50])
@@ -240,6 +240,7 @@ def run_ours(args, ws, rank, local):
     peaks, peak_kind = load_peaks()
 
     # ---- batched ensemble: the headline --------------------------------------
+    note("headline")
     t_build = time.time()
     wl, ensd = workloads.thermal_asym_top(Jmax=args.jmax, nvec=args.nvec)
     t_build = time.time() - t_build
@@ -279,6 +280,8 @@ def run_ours(args, ws, rank, local):
     # dominant kernel (batched complex64 mat-vec) alone
     plan = wl.hamiltonian(tc[args.warmup]).device_operator()
 
+    note("mat-vec kinds")
+
     def time_matvec(kind):
         _native.check(_native.lib().kr_batch_set_matvec(ens.handle, kind), ctx)
         em = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(6)]
@@ -291,7 +294,7 @@ def run_ours(args, ws, rank, local):
         return statistics.median(a.elapsed_time(b) for a, b in em[1:]) / 1e3
 
     kinds = {"tensor": _native.KR_MATVEC_TENSOR, "tensor_tmem": _native.KR_MATVEC_TENSOR_TMEM,
-             "fp32": _native.KR_MATVEC_FP32}
+             "fp32": _native.KR_MATVEC_FP32, "fp32_reg": _native.KR_MATVEC_FP32_REG}
     kind_s = {k: time_matvec(code) for k, code in kinds.items()}
     _native.check(_native.lib().kr_batch_set_matvec(ens.handle, kinds[args.matvec]), ctx)
     mv_s = kind_s[args.matvec]
@@ -299,7 +302,8 @@ def run_ours(args, ws, rank, local):
     mv_flops = 2.0 * fma_mv * nvec
     mv_bytes = 8.0 * 2 * dim * nvec  # complex64 X in + Y out (factors are shared by all vectors)
     # ncu DRAM bytes of one launch at 4096 vectors (profiles/traffic.json), in proportion to the vectors
-    tkey = "kb_matvec_per_launch_bytes_4096" if args.matvec == "fp32" else "kb_matvec_tc_per_launch_bytes_4096"
+    tkey = {"fp32": "kb_matvec_per_launch_bytes_4096", "fp32_reg": "kb_matvec_zr_per_launch_bytes_4096"}.get(
+        args.matvec, "kb_matvec_tc_per_launch_bytes_4096")
     t4096 = load_traffic().get(tkey)
     traffic = None if t4096 is None else int(round(t4096 * nvec / 4096))
     gbs = mv_bytes / mv_s / 1e9
@@ -309,7 +313,8 @@ def run_ours(args, ws, rank, local):
         "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
         "kernel": {"tensor": "kb_matvec_tcp (complex64 batched mat-vec, K contraction on tcgen05, A in shared memory)",
                    "tensor_tmem": "kb_matvec_tcp (complex64 batched mat-vec, K contraction on tcgen05, A in TMEM)",
-                   "fp32": "kb_matvec (complex64 batched mat-vec, FP32 FMAs)"}[args.matvec],
+                   "fp32": "kb_matvec (complex64 batched mat-vec, FP32 FMAs)",
+                   "fp32_reg": "kb_matvec_zr (complex64 batched mat-vec, FP32 FMAs, register-tiled)"}[args.matvec],
         "kernel_ms": round(mv_s * 1e3, 3),
         "kernel_ms_by_kind": {k: round(t * 1e3, 3) for k, t in kind_s.items()},
         "alg_bytes_per_launch": mv_bytes,
@@ -320,7 +325,7 @@ def run_ours(args, ws, rank, local):
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
         "ms_per_step": round(total_s * 1e3 / K, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": ("c64 mat-vec (FP32 FMAs)" if args.matvec == "fp32" else
+        "vs_baseline": None, "dtype": ("c64 mat-vec (FP32 FMAs)" if args.matvec.startswith("fp32") else
                                        "c64 mat-vec (K contraction as split-TF32 tcgen05 MMAs, FP32 accumulate)")
         + " / f64 Lanczos scalars, double-float state",
         "data": "synthetic",
@@ -344,6 +349,7 @@ def run_ours(args, ws, rank, local):
         out["clocks"] = clocks
 
     # ---- the same K steps through the pulse maximum (where the Krylov orders rise)
+    note("pulse window")
     ip = int(np.argmin(np.abs(np.asarray(tc) - wl.pulse[0])))
     i_lo = max(args.warmup, ip - K // 2)
     ens.load(ensd.vectors(dim))
@@ -370,6 +376,7 @@ def run_ours(args, ws, rank, local):
 
     if not args.no_extras:
         # ---- e2e: public API, per step the field in and the observable out ----
+        note("e2e")
         K2 = args.e2e_steps
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -387,18 +394,22 @@ def run_ours(args, ws, rank, local):
                       "includes_observable": True}
 
         # ---- the configured run: every step, batched beside plain FP64 ----
+        note("configured run")
         full = run_full(args, wl, ensd, ens, dev)
         out["full_run"] = full.pop("rates")
         out["accuracy_vs_fp64"] = full.pop("accuracy")
 
         # ---- plain FP64 drop-in configuration (J <= 40, one vector, dt 5 fs) ----
+        note("plain drop-in")
         out["plain_fp64_drop_in"] = run_plain(args, dev, peaks, peak_kind, fp64.value)
 
         # ---- serving: a Poisson stream of requests, continuous batching ----
+        note("serving")
         if ws == 1:
             del ens
             torch.cuda.empty_cache()
             out["serving"] = run_serving(args)
+            note("uneven batch")
             out["uneven_batch"] = run_uneven(args)
 
     if rank == 0 and not args.no_cpu_baseline:
@@ -544,8 +555,9 @@ def run_serving(args):
     ref = torch.from_numpy(v).cuda()
     worst = 0.0
     trace = results.get(small.rid)
+    ncheck = min(len(tc), 100)  # the first 1 ps of the trace (the FP64 path runs vector by vector)
     if trace is not None and not isinstance(trace, Exception):
-        for i, t in enumerate(tc):
+        for i, t in enumerate(tc[:ncheck]):
             ref, _ = td.update(job.wl.hamiltonian(t), H0=job.wl.h0, vecs=ref, inplace=True, check=False)
             if not job.wl.cos2._parts[0].prods:
                 job.wl.cos2.field([0, 0, 1])
@@ -561,8 +573,9 @@ def run_serving(args):
         "sample": (f"Poisson {args.serve_rate}/s for {args.serve_duration} s, Jmax {args.serve_jmax[0]}-"
                    f"{args.serve_jmax[1]} (C1, n_k up to {2 * args.serve_jmax[1] + 1}), <=512 vectors per "
                    f"request, {args.serve_tend} ps at 10 fs each, HBM budget {args.serve_budget_gb:.0f} GB; "
-                   "latency = arrival to finished trace, incl. factor build"),
-        "fp64_check": {"rid": small.rid, "jmax": small.jmax, "vectors": job.nvec,
+                   "latency = arrival to finished trace, incl. queueing and the factor build (started at "
+                   "arrival on the builder thread)"),
+        "fp64_check": {"rid": small.rid, "jmax": small.jmax, "vectors": job.nvec, "steps": ncheck,
                        "max_abs_err_cos2": worst, "bound": 1e-6},
     }
 
@@ -802,7 +815,14 @@ def run_reference(args, ws, rank, local):
     }
 
 
+def note(msg):
+    """Progress of the run on stderr (stdout carries the JSON line only)."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
 def main():
+    import faulthandler
+    faulthandler.enable()  # a crash prints the Python stacks of all threads on stderr
     args = parse()
     ws, rank, local = dist_info()
     out = run_reference(args, ws, rank, local) if args.impl == "reference" else run_ours(args, ws, rank, local)

@@ -307,8 +307,11 @@ int kr_batch_populations(kr_batch* b, double* out, void* stream);
  * memory; KR_MATVEC_TENSOR_TMEM the same products with the A operands written
  * to tensor memory (tcgen05.st) and a deeper TMA ring of input rows in the
  * shared memory this frees; KR_MATVEC_FP32 runs every product as an FP32
- * FMA. No counterpart in the reference (FP64 only). */
-enum { KR_MATVEC_TENSOR = 0, KR_MATVEC_FP32 = 1, KR_MATVEC_TENSOR_TMEM = 2 };
+ * FMA (tiles staged through shared memory); KR_MATVEC_FP32_REG the same
+ * products register-tiled (each thread a few output rows of one vector,
+ * all terms of the tile's slab summed in registers). No counterpart in the
+ * reference (FP64 only). */
+enum { KR_MATVEC_TENSOR = 0, KR_MATVEC_FP32 = 1, KR_MATVEC_TENSOR_TMEM = 2, KR_MATVEC_FP32_REG = 3 };
 int kr_batch_set_matvec(kr_batch* b, int32_t kind);
 /* y = op x for nvec vectors with the batched complex64 mat-vec (CarTens.vec,
  * field.py:1145-1245, in single precision): x, y (nvec, dim) complex128

@@ -17,7 +17,7 @@ LIB_DIR = os.path.join(PKG, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "librichmol_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 SOURCES = [os.path.join(PKG, "csrc", f) for f in ("kr_step.cu", "kr_batch.cu", "kr_batch_simt.cu", "kr_batch_tc.cu",
-                                                        "kr_expv.cu")]
+                                                        "kr_batch_zr.cu", "kr_expv.cu")]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 KR_OK, KR_ERR_ARG, KR_ERR_CUDA, KR_ERR_MAXORDER, KR_ERR_TIMEOUT, KR_ERR_UNSUPPORTED = range(6)
@@ -26,7 +26,7 @@ KR_MAXCART = 9
 KR_MAXPART = 4096
 KR_PART_INLINE = 16  # parts whose field coefficients go as kernel parameters
 KR_STEP_SKIP_KRYLOV = 1
-KR_MATVEC_TENSOR, KR_MATVEC_FP32, KR_MATVEC_TENSOR_TMEM = 0, 1, 2
+KR_MATVEC_TENSOR, KR_MATVEC_FP32, KR_MATVEC_TENSOR_TMEM, KR_MATVEC_FP32_REG = 0, 1, 2, 3
 KR_SEG_F64, KR_SEG_F32_MATVEC = 0, 1
 # bytes of per-step field input that travel host -> device (the field
 # coefficients, scales and thresholds of kr_set_field, passed as kernel

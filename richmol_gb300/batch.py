@@ -21,7 +21,7 @@ from .device import stream_ptr
 
 
 _KINDS = {"tensor": _native.KR_MATVEC_TENSOR, "fp32": _native.KR_MATVEC_FP32,
-          "tensor_tmem": _native.KR_MATVEC_TENSOR_TMEM}
+          "tensor_tmem": _native.KR_MATVEC_TENSOR_TMEM, "fp32_reg": _native.KR_MATVEC_FP32_REG}
 
 
 class Ensemble:
@@ -36,7 +36,9 @@ class Ensemble:
         matvec : str                "tensor" (default): K contractions on the tensor cores
                                     as split-TF32 MMAs (about 2^-21 relative per product);
                                     "tensor_tmem": the same with the A operands in tensor
-                                    memory; "fp32": every product an FP32 FMA; "auto": at
+                                    memory; "fp32": every product an FP32 FMA; "fp32_reg":
+                                    the same register-tiled (all terms of a tile
+                                    summed in registers); "auto": at
                                     the first step the kind is picked by richmol_gb300.tune
                                     (the cached choice for this operator shape and vector
                                     count, else every kind timed on that step's operator and
@@ -61,8 +63,8 @@ class Ensemble:
         h = ctypes.c_void_p()
         _native.check(_native.lib().kr_batch_create(self._plan0.op, self.nvec, self.mmax, ctypes.byref(h)), self.ctx)
         self.handle = h
-        if matvec not in ("tensor", "tensor_tmem", "fp32", "auto"):
-            raise ValueError("matvec must be one of ['auto', 'fp32', 'tensor', 'tensor_tmem']")
+        if matvec not in tuple(_KINDS) + ("auto",):
+            raise ValueError(f"matvec must be one of {sorted(_KINDS) + ['auto']}")
         self.matvec = matvec
         self.tuned = None
         self.tuned_from_cache = False

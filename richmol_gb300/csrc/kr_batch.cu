@@ -627,11 +627,19 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
   p.nb = b->nb;
   p.kslot = kslot;
   p.slot_elems = slot_elems;
+  p.err = b->counts + 2;
   p.task_slab = b->task_slab;
   p.task_i0 = b->task_i0;
   p.task_nr = b->task_nr;
   p.grp_active = masked ? b->grp_active : nullptr;
   p.yscale = yscale;
+  if (b->mv_kind == KR_MATVEC_FP32_REG && op->zr_ntask > 0) {
+    const int rc = kb_launch_zr(op->ctx, p, op->zr_task, op->zr_ntask, op->zr_class, mv_groups(b), st);
+    if (rc == KR_OK)
+      b->launches += (op->zr_class[1] > op->zr_class[0]) + (op->zr_class[2] > op->zr_class[1]) +
+                     (op->zr_class[3] > op->zr_class[2]);
+    return rc;
+  }
   const int rc = kb_launch_simt(op->ctx, p, b->ntask, mv_groups(b), st);
   if (rc == KR_OK) b->launches++;
   return rc;
@@ -1066,7 +1074,8 @@ extern "C" int kr_batch_populations(kr_batch* b, double* out, void* stream) {
 }
 
 extern "C" int kr_batch_set_matvec(kr_batch* b, int32_t kind) {
-  if (!b || (kind != KR_MATVEC_TENSOR && kind != KR_MATVEC_FP32 && kind != KR_MATVEC_TENSOR_TMEM))
+  if (!b || (kind != KR_MATVEC_TENSOR && kind != KR_MATVEC_FP32 && kind != KR_MATVEC_TENSOR_TMEM &&
+             kind != KR_MATVEC_FP32_REG))
     return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_set_matvec: bad argument");
   b->mv_kind = kind;
   return KR_OK;

@@ -28,6 +28,7 @@ struct BatchMV {
   const int* task_nr;
   const int* grp_active;  // per 32-vector group: any vector active (null: all)
   const double* yscale;   // per vector: output scale (null: 1)
+  int* err;               // error word (a term outside the tile shape), or null
 };
 
 // arguments of the tensor-core mat-vec kb_matvec_tc (kr_batch_tc.cu)
@@ -75,4 +76,11 @@ int kb_launch_simt(kr_ctx* ctx, const BatchMV& p, int ntask, int ngrp, cudaStrea
 // tmem_a: the persistent launches keep their A tiles in tensor memory (written by
 // tcgen05.st; the shared memory holds a deeper TMA ring), else in shared memory
 int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, const int* cls, int* work, bool tmem_a,
+                 cudaStream_t st);
+
+// launch the register-tiled FP32 mat-vec kb_matvec_zr (kr_batch_zr.cu) over
+// its tile table (op->zr_task: [4][ntask] slab, first row, rows, NKP; the
+// tiles of NKP = 8, 16, 32 from cls[0], cls[1], cls[2] to cls[3]) x ngrp
+// 32-vector groups, one launch per NKP class
+int kb_launch_zr(kr_ctx* ctx, const BatchMV& p, const int* task, int ntask, const int* cls, int ngrp,
                  cudaStream_t st);

@@ -111,6 +111,10 @@ struct kr_op {
   int tc_ntask = 0;
   int* tc_task = nullptr;
   int tc_class[4] = {0, 0, 0, 0};  // first tile of KP = 8, 16, 32 in tc_task, and the end
+  // tiles of the register-tiled FP32 batched mat-vec: [4][zr_ntask] = slab, first row, rows, NKP
+  int zr_ntask = 0;
+  int* zr_task = nullptr;
+  int zr_class[4] = {0, 0, 0, 0};  // first tile of NKP = 8, 16, 32 in zr_task, and the end
   // workspace of kr_expv / kr_op_norm1 (grown on demand, freed with the operator)
   void* expv_ws = nullptr;
   size_t expv_bytes = 0;

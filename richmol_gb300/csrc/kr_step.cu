@@ -1208,6 +1208,59 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
     op->tc_ntask = n;
   }
 
+  // ---- tiles of the register-tiled FP32 batched mat-vec --------------------
+  // per output slab: NKP = the largest n_k of the slab and its terms' input
+  // slabs, padded to 8, 16 or 32; tiles of 4 * RW rows (RW = 2, or 1 at
+  // NKP = 32: one row of outputs per thread and warp); heaviest tiles first
+  std::vector<int> zr_task;
+  {
+    std::vector<int> ts, ti, tn, tk;
+    std::vector<double> tcost;
+    bool fits = true;
+    for (int s = 0; s < d->nslab_out && fits; ++s) {
+      int nkmax = d->out_dk[s];
+      double terms_nk = 0;
+      for (int t : by_out[s]) {
+        nkmax = std::max(nkmax, d->in_dk[d->t_in[t]]);
+        terms_nk += d->in_dk[d->t_in[t]];
+      }
+      if (nkmax > 32) {
+        fits = false;
+        break;
+      }
+      const int nkp = nkmax <= 8 ? 8 : nkmax <= 16 ? 16 : 32;
+      const int rows = 4 * (nkp == 32 ? 1 : 2);
+      for (int i0 = 0; i0 < d->out_dm[s]; i0 += rows) {
+        const int nr = std::min(rows, d->out_dm[s] - i0);
+        ts.push_back(s);
+        ti.push_back(i0);
+        tn.push_back(nr);
+        tk.push_back(nkp);
+        tcost.push_back((double)nr * d->out_dk[s] * (terms_nk + 1));
+      }
+    }
+    const int n = fits ? (int)ts.size() : 0;
+    std::vector<int> ord(n);
+    std::iota(ord.begin(), ord.end(), 0);
+    // classes of NKP together (one launch per class), heaviest tiles first
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int x, int y) { return tk[x] != tk[y] ? tk[x] < tk[y] : tcost[x] > tcost[y]; });
+    for (int c = 0; c < 3; ++c) {
+      const int kpc = 8 << c;
+      op->zr_class[c] = (int)(std::lower_bound(ord.begin(), ord.end(), kpc,
+                                               [&](int x, int kv) { return tk[x] < kv; }) - ord.begin());
+    }
+    op->zr_class[3] = n;
+    zr_task.resize((size_t)4 * n);
+    for (int q = 0; q < n; ++q) {
+      zr_task[q] = ts[ord[q]];
+      zr_task[n + q] = ti[ord[q]];
+      zr_task[2 * n + q] = tn[ord[q]];
+      zr_task[3 * n + q] = tk[ord[q]];
+    }
+    op->zr_ntask = n;
+  }
+
   // K blocks transposed: KT[b][a] (complex blocks keep (re, im) pairs)
   std::vector<double> k_t(d->k_data, d->k_data + d->k_data_len);
   for (int b = 0; b < d->nk; ++b) {
@@ -1286,6 +1339,10 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   if (op->tc_ntask > 0) {
     UP(tc_task.data(), tc_task.size(), &p_i);
     op->tc_task = p_i;
+  }
+  if (op->zr_ntask > 0) {
+    UP(zr_task.data(), zr_task.size(), &p_i);
+    op->zr_task = p_i;
   }
   D.ntask = ntask;
   unsigned* p_u;

@@ -146,8 +146,11 @@ class Job:
         ens.load(v)
         trace = np.zeros(len(tc))
         for i, t in enumerate(tc):
-            ens.step(self.wl.hamiltonian(t))
+            # the step is queued whole (its Krylov loop runs on the device); the
+            # observable's read-back is the one host synchronisation per step
+            ens.step(self.wl.hamiltonian(t), sync=False)
             trace[i] = float(self.weights @ ens.expect(self.wl.cos2).real) + 1.0 / 3.0
+        ens.sync()  # a step error (Krylov order above mmax) is raised here
         self.state_steps = self.nvec * len(tc)
         del ens
         return trace

@@ -18,8 +18,8 @@ OBS_ATOL = 1e-6
 # relative max-norm error of one batched mat-vec against the FP64 mat-vec, per
 # kind: FP32 products (2^-24 rounding) and split-TF32 tensor-core products
 # (about 2^-21 per product)
-MV_RTOL = {"fp32": 2e-6, "tensor": 1e-5, "tensor_tmem": 1e-5}
-MATVECS = ["tensor", "tensor_tmem", "fp32"]
+MV_RTOL = {"fp32": 2e-6, "fp32_reg": 2e-6, "tensor": 1e-5, "tensor_tmem": 1e-5}
+MATVECS = ["tensor", "tensor_tmem", "fp32", "fp32_reg"]
 
 
 def _ct(case, name):
