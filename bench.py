@@ -55,9 +55,10 @@ def parse(argv=None):
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="bound of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="headline measurement only")
-    p.add_argument("--matvec", choices=["tensor", "tensor_tmem", "fp32", "fp32_reg"], default="tensor",
+    p.add_argument("--matvec", choices=["auto", "tensor", "tensor_tmem", "fp32", "fp32_reg"], default="auto",
                    help="batched mat-vec kind: tensor-core K contraction (split TF32; A operands in shared "
-                        "or tensor memory) or FP32 FMAs")
+                        "or tensor memory) or FP32 FMAs; auto: every kind timed on the first step's operator, "
+                        "the fastest kept (richmol_gb300.tune)")
     p.add_argument("--serve-rate", type=float, default=2.0, help="requests per second of the serving sample")
     p.add_argument("--serve-duration", type=float, default=3.0, help="seconds of arrivals of the serving sample")
     p.add_argument("--serve-jmax", type=int, nargs=2, default=[10, 50], help="Jmax range of the requests")
@@ -248,7 +249,7 @@ def run_ours(args, ws, rank, local):
     td = TDSE(t_start=wl.t_start, t_end=wl.t_end, dt=wl.dt)
     tc = td.time_grid()
     nsteps = len(tc)
-    ens = Ensemble(td, wl.h0, nvec, tol=1e-8, matvec=args.matvec)
+    ens = Ensemble(td, wl.h0, nvec, tol=1e-8, matvec=args.matvec, tune_cache=False)
     ens.load(ensd.vectors(dim))
     for i in range(args.warmup):
         ens.step(wl.hamiltonian(tc[i]))
@@ -296,14 +297,15 @@ def run_ours(args, ws, rank, local):
     kinds = {"tensor": _native.KR_MATVEC_TENSOR, "tensor_tmem": _native.KR_MATVEC_TENSOR_TMEM,
              "fp32": _native.KR_MATVEC_FP32, "fp32_reg": _native.KR_MATVEC_FP32_REG}
     kind_s = {k: time_matvec(code) for k, code in kinds.items()}
-    _native.check(_native.lib().kr_batch_set_matvec(ens.handle, kinds[args.matvec]), ctx)
-    mv_s = kind_s[args.matvec]
+    kind = ens.matvec  # the kind the ensemble steps with (picked by the autotuner with "auto")
+    _native.check(_native.lib().kr_batch_set_matvec(ens.handle, kinds[kind]), ctx)
+    mv_s = kind_s[kind]
     fma_mv, bytes_mv = plan.work()
     mv_flops = 2.0 * fma_mv * nvec
     mv_bytes = 8.0 * 2 * dim * nvec  # complex64 X in + Y out (factors are shared by all vectors)
     # ncu DRAM bytes of one launch at 4096 vectors (profiles/traffic.json), in proportion to the vectors
     tkey = {"fp32": "kb_matvec_per_launch_bytes_4096", "fp32_reg": "kb_matvec_zr_per_launch_bytes_4096"}.get(
-        args.matvec, "kb_matvec_tc_per_launch_bytes_4096")
+        kind, "kb_matvec_tc_per_launch_bytes_4096")
     t4096 = load_traffic().get(tkey)
     traffic = None if t4096 is None else int(round(t4096 * nvec / 4096))
     gbs = mv_bytes / mv_s / 1e9
@@ -314,7 +316,9 @@ def run_ours(args, ws, rank, local):
         "kernel": {"tensor": "kb_matvec_tcp (complex64 batched mat-vec, K contraction on tcgen05, A in shared memory)",
                    "tensor_tmem": "kb_matvec_tcp (complex64 batched mat-vec, K contraction on tcgen05, A in TMEM)",
                    "fp32": "kb_matvec (complex64 batched mat-vec, FP32 FMAs)",
-                   "fp32_reg": "kb_matvec_zr (complex64 batched mat-vec, FP32 FMAs, register-tiled)"}[args.matvec],
+                   "fp32_reg": "kb_matvec_zr (complex64 batched mat-vec, FP32 FMAs, register-tiled)"}[kind],
+        "kind_choice": ({"tuned_ms": {k: round(v, 3) for k, v in ens.tuned.items()}}
+                        if ens.tuned else {"fixed": kind}),
         "kernel_ms": round(mv_s * 1e3, 3),
         "kernel_ms_by_kind": {k: round(t * 1e3, 3) for k, t in kind_s.items()},
         "alg_bytes_per_launch": mv_bytes,
@@ -325,7 +329,7 @@ def run_ours(args, ws, rank, local):
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
         "ms_per_step": round(total_s * 1e3 / K, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": ("c64 mat-vec (FP32 FMAs)" if args.matvec.startswith("fp32") else
+        "vs_baseline": None, "dtype": ("c64 mat-vec (FP32 FMAs)" if kind.startswith("fp32") else
                                        "c64 mat-vec (K contraction as split-TF32 tcgen05 MMAs, FP32 accumulate)")
         + " / f64 Lanczos scalars, double-float state",
         "data": "synthetic",
