@@ -647,6 +647,7 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
 }  // namespace
 
 extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch** out) {
+  std::lock_guard<std::recursive_mutex> dlk(kr_device_mutex());
   if (!op || !out || nvec <= 0 || mmax < 2 || mmax > KB_NK_MAX - 1)
     return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_batch_create: bad argument (2 <= mmax <= 31)");
   *out = nullptr;
@@ -727,6 +728,7 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
 
 extern "C" void kr_batch_destroy(kr_batch* b) {
   if (!b) return;
+  std::lock_guard<std::recursive_mutex> dlk(kr_device_mutex());
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   for (cudaStream_t s : {b->cap, b->side0, b->side1})
     if (s) cudaStreamDestroy(s);
@@ -917,12 +919,16 @@ extern "C" int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double f
   if (cs == cudaStreamCaptureStatusActive) {
     // the caller records: the step's nodes go into the caller's graph
     if (kmax_out) return set_err(ctx, KR_ERR_ARG, "kr_batch_step: kmax_out must be NULL while the stream captures");
+    std::lock_guard<std::recursive_mutex> dlk(kr_device_mutex());
     return record_step(b, op, (const double2*)phase, fac, tol, st);
   }
   // a call: the step recorded once per (operator, phase, factor, tolerance,
   // mat-vec kind) and launched as one graph
   if (!b->gexec || b->g_op != op || b->g_uid != op->uid || b->g_phase != phase || b->g_fac[0] != fac_re ||
       b->g_fac[1] != fac_im || b->g_tol != tol || b->g_kind != b->mv_kind) {
+    // recording and instantiation under the device mutex: no allocation, free or
+    // device-wide synchronisation of the library's other threads runs meanwhile
+    std::lock_guard<std::recursive_mutex> dlk(kr_device_mutex());
     if (b->gexec) {
       KR_CUDA(ctx, cudaGraphExecDestroy(b->gexec));
       b->gexec = nullptr;

@@ -53,6 +53,12 @@ struct kr_ctx {
 
 // records the error message of a failed call (per context and library-wide)
 int kr_set_err(kr_ctx* ctx, int code, const std::string& msg);
+
+// Held while the library records a step into a CUDA graph and while it creates
+// or frees device objects (allocation, frees, device-wide synchronisation),
+// so that, with several host threads driving one GPU, none of the library's
+// own allocations or synchronisations runs in the middle of a recording.
+std::recursive_mutex& kr_device_mutex();
 #define set_err kr_set_err
 
 #define KR_CUDA(ctx, call)                                                                 \

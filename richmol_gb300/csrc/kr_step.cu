@@ -718,10 +718,16 @@ std::string g_err;
 }  // namespace
 
 int kr_set_err(kr_ctx* ctx, int code, const std::string& msg) {
-  if (ctx) ctx->err = msg;
+  // one context serves every thread of a process: its message is guarded too
   std::lock_guard<std::mutex> lk(g_err_mu);
+  if (ctx) ctx->err = msg;
   g_err = msg;
   return code;
+}
+
+std::recursive_mutex& kr_device_mutex() {
+  static std::recursive_mutex mu;
+  return mu;
 }
 
 
@@ -773,11 +779,9 @@ extern "C" void kr_ctx_destroy(kr_ctx* ctx) { delete ctx; }
 extern "C" int kr_last_error(const kr_ctx* ctx, char* buf, size_t len) {
   if (!buf || len == 0) return KR_ERR_ARG;
   std::string m;
-  if (ctx) {
-    m = ctx->err;
-  } else {
+  {
     std::lock_guard<std::mutex> lk(g_err_mu);
-    m = g_err;
+    m = ctx ? ctx->err : g_err;
   }
   std::snprintf(buf, len, "%s", m.c_str());
   return KR_OK;
@@ -785,6 +789,7 @@ extern "C" int kr_last_error(const kr_ctx* ctx, char* buf, size_t len) {
 
 extern "C" void kr_op_destroy(kr_op* op) {
   if (!op) return;
+  std::lock_guard<std::recursive_mutex> dlk(kr_device_mutex());
   for (void* p : op->allocs) cudaFree(p);
   if (op->expv_ws) cudaFree(op->expv_ws);
   if (op->fs_buf) cudaFree(op->fs_buf);
@@ -965,6 +970,7 @@ extern "C" int kr_op_check(const kr_op_desc* d, char* buf, size_t len) {
 }
 
 extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
+  std::lock_guard<std::recursive_mutex> dlk(kr_device_mutex());
   if (!ctx || !d || !out) return set_err(ctx, KR_ERR_ARG, "kr_op_create: NULL argument");
   *out = nullptr;
   KR_DEVICE_SCOPE(ctx, ctx->device);
@@ -1896,6 +1902,7 @@ extern "C" int kr_seg_set_precision(kr_seg* g, int32_t mode) {
 
 extern "C" void kr_seg_destroy(kr_seg* g) {
   if (!g) return;
+  std::lock_guard<std::recursive_mutex> dlk(kr_device_mutex());
   for (void* p : g->allocs) cudaFree(p);
   delete g;
 }
@@ -1918,6 +1925,7 @@ int seg_upload(kr_seg* g, const T* host, size_t count, T** dev) {
 }  // namespace
 
 extern "C" int kr_seg_create(kr_op* op, int32_t nseg, const int32_t* slab_seg, kr_seg** out) {
+  std::lock_guard<std::recursive_mutex> dlk(kr_device_mutex());
   if (!op || !slab_seg || !out || nseg <= 0) return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_seg_create: bad argument");
   *out = nullptr;
   if (!op->square || op->split) return set_err(op->ctx, KR_ERR_ARG, "kr_seg_create: operator is not square or has column chunks");

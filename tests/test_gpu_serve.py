@@ -67,3 +67,22 @@ def test_realtime_stream_reports_latency():
     assert all(not isinstance(v, Exception) for v in results.values())
     s = stats.summary()
     assert s["requests"] == len(rs) and s["p50_ms"] > 0
+
+
+def test_many_jobs_created_and_stepped_at_once():
+    """Twelve jobs on twelve host threads at once, every one building its
+    operators, recording its step graph and stepping while the others do the
+    same (the library serialises its recordings and allocations): every trace
+    equals the same request run alone."""
+    reqs = small_requests(12, seed=23)
+    alone = {}
+    for r in reqs[:3]:
+        res, _ = serve.Server(budget_bytes=40e9, max_active=1).serve([r], realtime=False)
+        alone[r.rid] = res[r.rid]
+    for _ in range(2):
+        mix, stats = serve.Server(budget_bytes=80e9, max_active=12).serve(reqs, realtime=False)
+        assert stats.max_active >= 4
+        for r in reqs:
+            assert not isinstance(mix[r.rid], Exception), mix[r.rid]
+        for rid, tr in alone.items():
+            np.testing.assert_allclose(mix[rid], tr, rtol=0, atol=MIX_TOL)
