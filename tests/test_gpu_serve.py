@@ -79,9 +79,11 @@ def test_many_jobs_created_and_stepped_at_once():
     for r in reqs[:3]:
         res, _ = serve.Server(budget_bytes=40e9, max_active=1).serve([r], realtime=False)
         alone[r.rid] = res[r.rid]
-    for _ in range(2):
-        mix, stats = serve.Server(budget_bytes=80e9, max_active=12).serve(reqs, realtime=False)
-        assert stats.max_active >= 4
+    # without prebuild every job thread builds its own factors and operators
+    # while the others record and step; with it, one builder thread feeds them
+    for prebuild in (False, True):
+        mix, stats = serve.Server(budget_bytes=80e9, max_active=12, prebuild=prebuild).serve(reqs, realtime=False)
+        assert stats.max_active >= (4 if not prebuild else 2)
         for r in reqs:
             assert not isinstance(mix[r.rid], Exception), mix[r.rid]
         for rid, tr in alone.items():
