@@ -406,6 +406,8 @@ def run_ours(args, ws, rank, local):
         # ---- plain FP64 drop-in configuration (J <= 40, one vector, dt 5 fs) ----
         note("plain drop-in")
         out["plain_fp64_drop_in"] = run_plain(args, dev, peaks, peak_kind, fp64.value)
+        note("plain step, double-float products")
+        out["plain_fp64_drop_in"]["df_products"] = run_plain(args, dev, peaks, peak_kind, fp64.value, products="df")
 
         # ---- serving: a Poisson stream of requests, continuous batching ----
         note("serving")
@@ -672,9 +674,12 @@ def ens_expect_plain(ref, O):
     return torch.sum(torch.conj(ref) * y, dim=1).real.cpu().numpy()
 
 
-def run_plain(args, dev, peaks, peak_kind, fp64_peak):
+def run_plain(args, dev, peaks, peak_kind, fp64_peak, products="f64"):
     """The plain FP64 drop-in configuration: J <= 40 (dim 91,881), one vector,
-    dt = 5 fs, L2 flushed before every step; kernel roofline on the FP64 pipe."""
+    dt = 5 fs, L2 flushed before every step; kernel roofline on the FP64 pipe.
+    products="df": the same steps with double-float mat-vec products (FP32
+    pipes), with their largest state difference from the FP64 products' over
+    the timed steps."""
     import torch
     from richmol_gb300 import TDSE, workloads
     wl = workloads.asym_top(Jmax=args.jmax_plain)
@@ -686,8 +691,11 @@ def run_plain(args, dev, peaks, peak_kind, fp64_peak):
     fac = td.exp_fac
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     for i in range(5):
-        wl.hamiltonian(tc[i]).device_operator().step(v, phase, fac, 1e-15)
+        pl = wl.hamiltonian(tc[i]).device_operator()
+        pl.set_precision(products)
+        pl.step(v, phase, fac, 1e-15)
     K = args.plain_steps
+    vref = v.clone() if products != "f64" else None
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     ek = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     torch.cuda.synchronize()
@@ -701,6 +709,15 @@ def run_plain(args, dev, peaks, peak_kind, fp64_peak):
         ev[j][1].record()
     torch.cuda.synchronize()
     plan.sync_status()
+    df_err = None
+    if vref is not None:  # the same K steps with FP64 products, untimed
+        for j in range(K):
+            pl = wl.hamiltonian(tc[5 + j]).device_operator()
+            pl.set_precision("f64")
+            pl.step(vref, phase, fac, 1e-15)
+            pl.set_precision(products)
+        torch.cuda.synchronize()
+        df_err = float((v - vref).abs().max() / vref.abs().max())
     step_ms = [a.elapsed_time(b) for a, b in ev]
     kern_s = statistics.mean(a.elapsed_time(b) for a, b in ek) / 1e3
     kord = np.zeros(1, np.int32)
@@ -718,7 +735,7 @@ def run_plain(args, dev, peaks, peak_kind, fp64_peak):
     # the same steps recorded once as a CUDA graph (field + step launches per
     # step, L2 flush recorded ahead of each) and replayed with one launch
     from richmol_gb300.graph import StepGraph
-    sg = StepGraph(td, wl.h0, v, wl.hamiltonian, tc[5 + K:5 + 2 * K], before_step=flush.zero_)
+    sg = StepGraph(td, wl.h0, v, wl.hamiltonian, tc[5 + K:5 + 2 * K], before_step=flush.zero_, products=products)
     ga, gb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     ga.record()
@@ -736,14 +753,14 @@ def run_plain(args, dev, peaks, peak_kind, fp64_peak):
     # e2e through the reference-facing API with host (numpy) buffers
     td2 = TDSE(t_start=wl.t_start, t_end=wl.t_end, dt=wl.dt)
     tc2 = td2.time_grid()
-    vh, _ = td2.update(wl.hamiltonian(tc2[0]), v0, H0=wl.h0)
+    vh, _ = td2.update(wl.hamiltonian(tc2[0]), v0, H0=wl.h0, products=products)
     torch.cuda.synchronize()
     K2 = 100
     t0 = time.perf_counter()
     for j in range(1, K2 + 1):
-        vh, _ = td2.update(wl.hamiltonian(tc2[j]), vh, H0=wl.h0)
+        vh, _ = td2.update(wl.hamiltonian(tc2[j]), vh, H0=wl.h0, products=products)
     e2e = K2 / (time.perf_counter() - t0)
-    return {
+    out = {
         "value": round(K / (sum(step_ms) / 1e3), 1), "unit": UNIT, "steps": K,
         "workload": f"asymmetric top D2 J=0..{args.jmax_plain} (dim {n}), 1 vector, dt 5 fs, L2 flushed per step",
         "step_ms_p50": round(statistics.median(step_ms), 4), "kernel": "kr_step_kernel",
@@ -763,7 +780,18 @@ def run_plain(args, dev, peaks, peak_kind, fp64_peak):
                              "frac": round(gbs / peaks["hbm_gbs"], 5)}},
         "e2e": {"value": round(e2e, 1), "unit": UNIT, "h2d_bytes_per_step": int(v0.nbytes),
                 "d2h_bytes_per_step": int(v0.nbytes), "api": "TDSE.update(H, numpy vecs, H0=h0)"},
+        "products": products,
     }
+    if df_err is not None:
+        out["max_rel_state_diff_vs_fp64_products"] = df_err
+        out["sample_diff"] = f"{K} timed steps from the same state, FP64 products run beside them untimed"
+        # the FP64 pipe no longer carries the products: report the kernel
+        # against the HBM roofline only, with the FP64-equivalent rate beside it
+        out["roofline"] = {"bound": "latency", "achieved_fp64_equiv_tflops": out["roofline"]["achieved"],
+                           "hbm": out["roofline"]["hbm"],
+                           "note": "double-float products on the FP32 pipes; grid barriers and the "
+                                   "row-task tail bound the step"}
+    return out
 
 
 def run_reference(args, ws, rank, local):

@@ -248,6 +248,15 @@ int kr_step_static(kr_op* op, void* states, int64_t nvec, const void* phase,
                    double fac_re, double fac_im, double tol, uint32_t flags,
                    int32_t* korder, void* stream);
 
+/* Arithmetic of the mat-vec products of kr_step and kr_step_static (no
+ * counterpart in the reference, which is FP64 throughout): KR_PREC_F64
+ * (default), or KR_PREC_DF, double-float products on the FP32 pipes (each FP64
+ * value held as an FP32 pair, about 48 significant bits; 1e-14 relative per
+ * product) with the states, Krylov vectors, Lanczos scalars, exponential and
+ * stopping test in FP64. */
+enum { KR_PREC_F64 = 0, KR_PREC_DF = 1 };
+int kr_op_set_precision(kr_op* op, int32_t prec);
+
 /* Bytes of static scratch kr_step_static needs for op, and the capacity. */
 int kr_static_scratch_bytes(const kr_op* op, size_t* needed, size_t* capacity);
 

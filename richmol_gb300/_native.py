@@ -28,6 +28,7 @@ KR_PART_INLINE = 16  # parts whose field coefficients go as kernel parameters
 KR_STEP_SKIP_KRYLOV = 1
 KR_MATVEC_TENSOR, KR_MATVEC_FP32, KR_MATVEC_TENSOR_TMEM, KR_MATVEC_FP32_REG = 0, 1, 2, 3
 KR_SEG_F64, KR_SEG_F32_MATVEC = 0, 1
+KR_PREC_F64, KR_PREC_DF = 0, 1
 # bytes of per-step field input that travel host -> device (the field
 # coefficients, scales and thresholds of kr_set_field, passed as kernel
 # parameters): int npart (padded to 8) + 16 x 9 complex + 16 complex + 16 double
@@ -43,6 +44,7 @@ EXPORTED = [
     "kr_batch_populations",
     "kr_expv", "kr_op_norm1", "kr_observables",
     "kr_seg_create", "kr_seg_destroy", "kr_seg_step", "kr_seg_launch_count", "kr_seg_set_precision",
+    "kr_op_set_precision",
 ]
 
 
@@ -183,6 +185,8 @@ def lib():
         L.kr_seg_launch_count.restype = i64
         L.kr_seg_set_precision.argtypes = [vp, i32]
         L.kr_seg_set_precision.restype = ctypes.c_int
+        L.kr_op_set_precision.argtypes = [vp, i32]
+        L.kr_op_set_precision.restype = ctypes.c_int
         L.kr_batch_matvec.argtypes = [vp, vp, vp]
         L.kr_batch_matvec.restype = ctypes.c_int
         L.kr_batch_launch_count.argtypes = [vp]

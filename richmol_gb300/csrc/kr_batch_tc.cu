@@ -80,10 +80,10 @@ __device__ __forceinline__ void kbt_mdia(float2 (&z)[64 / KP][KP / 2], const Kbt
 }
 
 // M step of a term with stored columns (ELL), one input row per slot
-template <int KP, int MT>
-__device__ __forceinline__ void kbt_mell(float2 (&z)[64 / KP][KP / 2], const float2* Xs2, long long nb, int nk2,
+template <int KP, int MT, int BH = KP / 2>
+__device__ __forceinline__ void kbt_mell(float2 (&z)[64 / KP][BH], const float2* Xs2, long long nb, int nk2,
                                          int ld2, int nr, int W, int b0, const float2* MFs, const int* Cs) {
-  constexpr int R = 64 / KP, BH = KP / 2;
+  constexpr int R = 64 / KP;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     if (r >= nr) continue;
@@ -203,52 +203,48 @@ __device__ __forceinline__ void kbt_zstep(float2 (&z)[64 / KP][KP / 2], KbtWin<K
 }
 
 // producer-only barrier (warps 0-7) that leaves the MMA warp out
-__device__ __forceinline__ void kbt_producer_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+template <int PT = 256>
+__device__ __forceinline__ void kbt_producer_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(PT) : "memory");
+}
 
-// issues the MMAs of tile row r of one term (one thread): D_re += Z_re K_re -
-// Z_im K_im, D_im += Z_re K_im + Z_im K_re, each product as three TF32 MMAs per
-// K step (A hi B hi, A hi B lo, A lo B hi); zero parts of K skipped
+// MMAs of a term (one thread): per tile row r, D_re += Z_re K_re - Z_im K_im,
+// D_im += Z_re K_im + Z_im K_re, each product as three TF32 MMAs per K step
+// (A hi B hi, A hi B lo, A lo B hi); zero parts of K skipped.
+// Per row, the MMAs into D_re, then those into D_im (runs on one accumulator).
 template <int KP>
-__device__ __forceinline__ void kbt_issue_row(uint32_t tmem, uint64_t adesc0, uint64_t bdesc, uint32_t idesc,
-                                              int NP, int r, int ktype, int nk2, uint32_t& dinit,
-                                              int bpart = TC_BPART) {
+__device__ __forceinline__ void kbt_issue(uint32_t tmem, uint64_t adesc0, uint64_t bdesc, uint32_t idesc, int NP,
+                                          int nr, int ktype, int nk2, uint32_t& dinit, int bpart = TC_BPART,
+                                          int r0 = 0, int rs = 1) {
   constexpr int ATILE = 128 * KP;
+  // (D part, A part, B part) of each product, D_re ones first
   int pd[4], pa[4], pb[4];
   int np = 0;
-  if (ktype != 2) {
-    pd[np] = 0; pa[np] = 0; pb[np] = 0; ++np;  // re <- Z_re K_re
-    pd[np] = 1; pa[np] = 2; pb[np] = 0; ++np;  // im <- Z_im K_re
-  }
-  if (ktype != 1) {
-    pd[np] = 0; pa[np] = 2; pb[np] = 4; ++np;  // re <- Z_im (-K_im)
-    pd[np] = 1; pa[np] = 0; pb[np] = 2; ++np;  // im <- Z_re K_im
-  }
+  if (ktype != 2) { pd[np] = 0; pa[np] = 0; pb[np] = 0; ++np; }  // re <- Z_re K_re
+  if (ktype != 1) { pd[np] = 0; pa[np] = 2; pb[np] = 4; ++np; }  // re <- Z_im (-K_im)
+  if (ktype != 2) { pd[np] = 1; pa[np] = 2; pb[np] = 0; ++np; }  // im <- Z_im K_re
+  if (ktype != 1) { pd[np] = 1; pa[np] = 0; pb[np] = 2; ++np; }  // im <- Z_re K_im
   const int nks = (nk2 + 7) >> 3;
-  // descriptor start addresses advance by (byte offset >> 4)
-  for (int q = 0; q < np; ++q) {
-    const uint32_t dcol = tmem + (uint32_t)((2 * r + pd[q]) * NP);
-    const uint32_t dbit = 1u << (2 * r + pd[q]);
-    const uint64_t ad = adesc0 + (uint64_t)(((r * 4 + pa[q]) * ATILE * 4) >> 4);
-    const uint64_t bd = bdesc + (uint64_t)((pb[q] * bpart) >> 4);
+  for (int r = r0; r < nr; r += rs) {
+    for (int q = 0; q < np; ++q) {
+      const uint32_t dcol = tmem + (uint32_t)((2 * r + pd[q]) * NP);
+      const uint32_t dbit = 1u << (2 * r + pd[q]);
+      const uint64_t ad = adesc0 + (uint64_t)(((r * 4 + pa[q]) * ATILE * 4) >> 4);
+      const uint64_t bd = bdesc + (uint64_t)((pb[q] * bpart) >> 4);
 #pragma unroll
-    for (int sp = 0; sp < 3; ++sp) {
-      const uint64_t a2 = ad + (sp == 2 ? (uint64_t)((ATILE * 4) >> 4) : 0);
-      const uint64_t b2 = bd + (sp == 1 ? (uint64_t)(bpart >> 4) : 0);
+      for (int sp = 0; sp < 3; ++sp) {
+        const uint64_t a2 = ad + (sp == 2 ? (uint64_t)((ATILE * 4) >> 4) : 0);
+        const uint64_t b2 = bd + (sp == 1 ? (uint64_t)(bpart >> 4) : 0);
 #pragma unroll
-      for (int ks = 0; ks < KP / 8; ++ks) {
-        if (ks < nks) {
-          tc_mma_tf32(dcol, a2 + 16u * ks, b2 + 16u * ks, idesc, (dinit & dbit) ? 1u : 0u);
-          dinit |= dbit;
+        for (int ks = 0; ks < KP / 8; ++ks) {
+          if (ks < nks) {
+            tc_mma_tf32(dcol, a2 + 16u * ks, b2 + 16u * ks, idesc, (dinit & dbit) ? 1u : 0u);
+            dinit |= dbit;
+          }
         }
       }
     }
   }
-}
-
-template <int KP>
-__device__ __forceinline__ void kbt_issue(uint32_t tmem, uint64_t adesc0, uint64_t bdesc, uint32_t idesc, int NP,
-                                          int nr, int ktype, int nk2, uint32_t& dinit, int bpart = TC_BPART) {
-  for (int r = 0; r < nr; ++r) kbt_issue_row<KP>(tmem, adesc0, bdesc, idesc, NP, r, ktype, nk2, dinit, bpart);
 }
 
 // MMAs of one term with K_hi and K_lo merged along N (one thread): per row r
@@ -259,11 +255,14 @@ __device__ __forceinline__ void kbt_issue(uint32_t tmem, uint64_t adesc0, uint64
 // acc0: 0 for the first committed term of the tile (fresh accumulators).
 template <int KP, int KT>
 __device__ __forceinline__ void kbt_issue_merged(uint32_t tmem, uint64_t adesc0, uint64_t bdesc, uint32_t id1,
-                                                 uint32_t id2, int NP, int nr, int nk2, uint32_t acc0, int bpart) {
+                                                 uint32_t id2, int NP, int nr, int nk2, uint32_t acc0, int bpart,
+                                                 int r0 = 0, int rs = 1) {
   constexpr uint64_t AP = (uint64_t)((128 * KP * 4) >> 4);  // descriptor step of one A part
   const uint64_t BP = (uint64_t)(bpart >> 4);               // of one B part
   const int nks = (nk2 + 7) >> 3;
-  for (int r = 0; r < nr; ++r) {
+  // per row (rows r0, r0 + rs, ...), all MMAs into D_re, then all into D_im:
+  // runs of MMAs on one accumulator (faster than switching regions between MMAs)
+  for (int r = r0; r < nr; r += rs) {
     const uint32_t dre = tmem + (uint32_t)(4 * r * NP), dim = dre + (uint32_t)(2 * NP);
     const uint64_t a = adesc0 + (uint64_t)(4 * r) * AP;
 #pragma unroll
@@ -274,15 +273,24 @@ __device__ __forceinline__ void kbt_issue_merged(uint32_t tmem, uint64_t adesc0,
       if (KT != 2) {
         tc_mma_tf32(dre, ak + 0 * AP, bk + 0 * BP, id2, f);   // Z_re_hi [K_re_hi; K_re_lo]
         tc_mma_tf32(dre, ak + 1 * AP, bk + 0 * BP, id1, 1u);  // Z_re_lo K_re_hi
+      }
+      if (KT != 1) {
+        tc_mma_tf32(dre, ak + 2 * AP, bk + 4 * BP, id2, KT == 2 ? f : 1u);  // Z_im_hi [-K_im_hi; -K_im_lo]
+        tc_mma_tf32(dre, ak + 3 * AP, bk + 4 * BP, id1, 1u);               // Z_im_lo (-K_im_hi)
+      }
+    }
+#pragma unroll
+    for (int ks = 0; ks < KP / 8; ++ks) {
+      if (ks >= nks) break;
+      const uint32_t f = ks == 0 ? acc0 : 1u;
+      const uint64_t ak = a + 16u * ks, bk = bdesc + 16u * ks;
+      if (KT != 2) {
         tc_mma_tf32(dim, ak + 2 * AP, bk + 0 * BP, id2, f);   // Z_im_hi [K_re_hi; K_re_lo]
         tc_mma_tf32(dim, ak + 3 * AP, bk + 0 * BP, id1, 1u);  // Z_im_lo K_re_hi
       }
       if (KT != 1) {
-        const uint32_t g = KT == 2 ? f : 1u;
-        tc_mma_tf32(dre, ak + 2 * AP, bk + 4 * BP, id2, g);   // Z_im_hi [-K_im_hi; -K_im_lo]
-        tc_mma_tf32(dre, ak + 3 * AP, bk + 4 * BP, id1, 1u);  // Z_im_lo (-K_im_hi)
-        tc_mma_tf32(dim, ak + 0 * AP, bk + 2 * BP, id2, g);   // Z_re_hi [K_im_hi; K_im_lo]
-        tc_mma_tf32(dim, ak + 1 * AP, bk + 2 * BP, id1, 1u);  // Z_re_lo K_im_hi
+        tc_mma_tf32(dim, ak + 0 * AP, bk + 2 * BP, id2, KT == 2 ? f : 1u);  // Z_re_hi [K_im_hi; K_im_lo]
+        tc_mma_tf32(dim, ak + 1 * AP, bk + 2 * BP, id1, 1u);               // Z_re_lo K_im_hi
       }
     }
   }
@@ -530,11 +538,12 @@ struct KbtPre {
   int col;
 };
 
-template <int KP>
+// PT producer threads (256 or 512) cover the NP x KP <= 512 B entries
+template <int KP, int PT = 256>
 __device__ __forceinline__ void kbt_preload(const KbtTerm& t, int nk1, int NP, int i0, int nr, int tid, KbtPre& q) {
 #pragma unroll
-  for (int u = 0; u < 2; ++u) {
-    const int e = tid + 256 * u;
+  for (int u = 0; u < 512 / PT; ++u) {
+    const int e = tid + PT * u;
     const int a = e / KP, b = e - (e / KP) * KP;
     float kr = 0.f, ki = 0.f;
     if (e < NP * KP && a < nk1 && b < t.nk2) {
@@ -565,12 +574,12 @@ __device__ __forceinline__ void kbt_preload(const KbtTerm& t, int nk1, int NP, i
   }
 }
 
-template <int KP>
+template <int KP, int PT = 256>
 __device__ __forceinline__ void kbt_stage_pre(const KbtTerm& t, const KbtPre& q, int NP, int nr, float* Bt,
                                               float2* MFs, int* Cs, float4* MFd, int tid, int bpart) {
 #pragma unroll
-  for (int u = 0; u < 2; ++u) {
-    const int e = tid + 256 * u;
+  for (int u = 0; u < 512 / PT; ++u) {
+    const int e = tid + PT * u;
     if (e >= NP * KP) break;
     const int a = e / KP, b = e - (e / KP) * KP;
     const uint32_t o = tc_kmajor_off(a, b, KP) >> 2;
@@ -606,27 +615,50 @@ __device__ __forceinline__ void macc2(float2& z, const float4& m, float2 x) {
   if (MT != 1) z = tc_ffma2(make_float2(m.z, m.w), make_float2(x.y, x.x), z);
 }
 
-// M step of a diagonal term from the ring; g: ring row counter (advanced).
-// Window row c feeds tile rows r = c - W + 1 .. c through the dense band
-// MFd[c][r] (zero outside the band); rows go in groups of G, a group skipped
-// (warp-uniform) when the band misses it. Input columns at or beyond n_k2 hold
-// finite data of the neighbouring rows and meet zero rows of K^T in the MMA.
-template <int KP, int MT, int NSLOT>
-__device__ __forceinline__ bool kbt_mdia_ring(float2 (&z)[64 / KP][KP / 2], const char* ring, uint64_t* rfull,
-                                              uint64_t* rempty, int& g, int nwin, int nr, int W, int b0,
+// position of the producers in the ring: the next row's slot and the phase
+// parity that slot's full barrier completes with
+struct KbtRingPos {
+  int slot;
+  uint32_t phase;
+};
+template <int NSLOT>
+__device__ __forceinline__ void kbt_ring_next(KbtRingPos& rp) {
+  if (++rp.slot == NSLOT) {
+    rp.slot = 0;
+    rp.phase ^= 1u;
+  }
+}
+
+// takes the next ring row: waits until it has landed, reads this thread's
+// vector and KP/2 columns, and gives the slot back (one arrival per warp)
+template <int KP, int BQ, int NSLOT>
+__device__ __forceinline__ bool kbt_ring_take(float2 (&x)[BQ], const char* ring, uint64_t* rfull,
+                                              uint64_t* rempty, KbtRingPos& rp, int b0, int vloc, int lane) {
+  const bool ok = tc_mbar_wait(rfull + rp.slot, rp.phase);
+  const float2* xs = reinterpret_cast<const float2*>(ring + (size_t)rp.slot * KbtRing<KP>::SLOT) + vloc;
+#pragma unroll
+  for (int q = 0; q < BQ; ++q) x[q] = xs[(b0 + q) * 128];
+  __syncwarp();
+  if (lane == 0) tc_mbar_arrive(rempty + rp.slot);
+  kbt_ring_next<NSLOT>(rp);
+  return ok;
+}
+
+// M step of a diagonal term from the ring. Window row c feeds tile rows
+// r = c - W + 1 .. c through the dense band MFd[c][r] (zero outside the band);
+// rows go in groups of G, a group skipped (warp-uniform) when the band misses
+// it. Input columns at or beyond n_k2 hold finite data of the neighbouring rows
+// and meet zero rows of K^T in the MMA.
+template <int KP, int BH, int MT, int NSLOT>
+__device__ __forceinline__ bool kbt_mdia_ring(float2 (&z)[64 / KP][BH], const char* ring, uint64_t* rfull,
+                                              uint64_t* rempty, KbtRingPos& rp, int nwin, int nr, int W, int b0,
                                               int vloc, int lane, const float4* MFd) {
-  constexpr int R = 64 / KP, BH = KP / 2;
+  constexpr int R = 64 / KP;
   constexpr int G = R >= 8 ? 2 : 1;
   bool ok = true;
-  for (int c = 0; c < nwin; ++c, ++g) {
-    const int slot = g % NSLOT;
-    if (!tc_mbar_wait(rfull + slot, (uint32_t)(g / NSLOT) & 1u)) ok = false;
-    const float2* xs = reinterpret_cast<const float2*>(ring + (size_t)slot * KbtRing<KP>::SLOT) + vloc;
+  for (int c = 0; c < nwin; ++c) {
     float2 x[BH];
-#pragma unroll
-    for (int q = 0; q < BH; ++q) x[q] = xs[(b0 + q) * 128];
-    __syncwarp();
-    if (lane == 0) tc_mbar_arrive(rempty + slot);
+    if (!kbt_ring_take<KP, BH, NSLOT>(x, ring, rfull, rempty, rp, b0, vloc, lane)) ok = false;
     const float4* mrow = MFd + c * R;
 #pragma unroll
     for (int gr = 0; gr < R / G; ++gr) {
@@ -644,12 +676,49 @@ __device__ __forceinline__ bool kbt_mdia_ring(float2 (&z)[64 / KP][KP / 2], cons
   return ok;
 }
 
-template <int KP, int NSLOT>
-__device__ __forceinline__ bool kbt_zstep_ring(float2 (&z)[64 / KP][KP / 2], const KbtTerm& t, long long nb, int nr,
+// the same for a band of WT slots (1, 3, 5), unrolled over the window: the
+// band tests fold at compile time. Rows from nwin on (tiles of fewer than R
+// rows) are neither taken nor used: they feed only tile rows at or beyond nr.
+template <int KP, int BH, int MT, int WT, int NSLOT>
+__device__ __forceinline__ bool kbt_mdia_ring_u(float2 (&z)[64 / KP][BH], const char* ring, uint64_t* rfull,
+                                                uint64_t* rempty, KbtRingPos& rp, int nwin, int b0, int vloc,
+                                                int lane, const float4* MFd) {
+  constexpr int R = 64 / KP, NW = R + WT - 1;
+  bool ok = true;
+#pragma unroll
+  for (int c = 0; c < NW; ++c) {
+    if (c < nwin) {
+      float2 x[BH];
+      if (!kbt_ring_take<KP, BH, NSLOT>(x, ring, rfull, rempty, rp, b0, vloc, lane)) ok = false;
+      const float4* mrow = MFd + c * R;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (r < c - WT + 1 || r > c) continue;
+        const float4 m = mrow[r];
+#pragma unroll
+        for (int q = 0; q < BH; ++q) macc2<MT>(z[r][q], m, x[q]);
+      }
+    }
+  }
+  return ok;
+}
+
+template <int KP, int BH, int MT, int NSLOT>
+__device__ __forceinline__ bool kbt_mdia_ring_w(float2 (&z)[64 / KP][BH], const char* ring, uint64_t* rfull,
+                                                uint64_t* rempty, KbtRingPos& rp, int nwin, int nr, int W, int b0,
+                                                int vloc, int lane, const float4* MFd) {
+  if (W == 5) return kbt_mdia_ring_u<KP, BH, MT, 5, NSLOT>(z, ring, rfull, rempty, rp, nwin, b0, vloc, lane, MFd);
+  if (W == 3) return kbt_mdia_ring_u<KP, BH, MT, 3, NSLOT>(z, ring, rfull, rempty, rp, nwin, b0, vloc, lane, MFd);
+  if (W == 1) return kbt_mdia_ring_u<KP, BH, MT, 1, NSLOT>(z, ring, rfull, rempty, rp, nwin, b0, vloc, lane, MFd);
+  return kbt_mdia_ring<KP, BH, MT, NSLOT>(z, ring, rfull, rempty, rp, nwin, nr, W, b0, vloc, lane, MFd);
+}
+
+template <int KP, int BH, int NSLOT>
+__device__ __forceinline__ bool kbt_zstep_ring(float2 (&z)[64 / KP][BH], const KbtTerm& t, long long nb, int nr,
                                                int b0, int vloc, int lane, const float2* MFs, const int* Cs,
                                                const float4* MFd, const char* ring, uint64_t* rfull,
-                                               uint64_t* rempty, int& g) {
-  constexpr int R = 64 / KP, BH = KP / 2;
+                                               uint64_t* rempty, KbtRingPos& rp) {
+  constexpr int R = 64 / KP;
 #pragma unroll
   for (int r = 0; r < R; ++r)
 #pragma unroll
@@ -657,13 +726,13 @@ __device__ __forceinline__ bool kbt_zstep_ring(float2 (&z)[64 / KP][KP / 2], con
   if (!t.ok || t.empty) return true;
   const int nwin = kbt_ring_rows(t, nr);
   if (t.dia) {
-    if (t.mtype == 1) return kbt_mdia_ring<KP, 1, NSLOT>(z, ring, rfull, rempty, g, nwin, nr, t.W, b0, vloc, lane, MFd);
-    if (t.mtype == 2) return kbt_mdia_ring<KP, 2, NSLOT>(z, ring, rfull, rempty, g, nwin, nr, t.W, b0, vloc, lane, MFd);
-    return kbt_mdia_ring<KP, 0, NSLOT>(z, ring, rfull, rempty, g, nwin, nr, t.W, b0, vloc, lane, MFd);
+    if (t.mtype == 1) return kbt_mdia_ring_w<KP, BH, 1, NSLOT>(z, ring, rfull, rempty, rp, nwin, nr, t.W, b0, vloc, lane, MFd);
+    if (t.mtype == 2) return kbt_mdia_ring_w<KP, BH, 2, NSLOT>(z, ring, rfull, rempty, rp, nwin, nr, t.W, b0, vloc, lane, MFd);
+    return kbt_mdia_ring_w<KP, BH, 0, NSLOT>(z, ring, rfull, rempty, rp, nwin, nr, t.W, b0, vloc, lane, MFd);
   }
-  if (t.mtype == 1) kbt_mell<KP, 1>(z, t.Xs2, nb, t.nk2, t.ld2, nr, t.W, b0, MFs, Cs);
-  else if (t.mtype == 2) kbt_mell<KP, 2>(z, t.Xs2, nb, t.nk2, t.ld2, nr, t.W, b0, MFs, Cs);
-  else kbt_mell<KP, 0>(z, t.Xs2, nb, t.nk2, t.ld2, nr, t.W, b0, MFs, Cs);
+  if (t.mtype == 1) kbt_mell<KP, 1, BH>(z, t.Xs2, nb, t.nk2, t.ld2, nr, t.W, b0, MFs, Cs);
+  else if (t.mtype == 2) kbt_mell<KP, 2, BH>(z, t.Xs2, nb, t.nk2, t.ld2, nr, t.W, b0, MFs, Cs);
+  else kbt_mell<KP, 0, BH>(z, t.Xs2, nb, t.nk2, t.ld2, nr, t.W, b0, MFs, Cs);
   return true;
 }
 
@@ -690,17 +759,28 @@ struct KbtPers {
   static constexpr int OFF_HDR = OFF_BAR + 8 * (2 + 2 * NSLOT + 4) + 16;
   static constexpr int OFF_TAB = OFF_HDR + 2 * 8 * 4;
   static constexpr int TOTAL = OFF_TAB + 2 * KBT_MAXT_P * (int)sizeof(KbtTerm);
+  // producer warps: 16 with the A tiles in TMEM (each thread a quarter of the
+  // K columns of its vector), 8 with them in shared memory (a half); then the
+  // MMA warp and the loader warp
+  static constexpr int PW = TA ? 16 : 8;
+  static constexpr int PT = 32 * PW;       // producer threads
+  static constexpr int NQ = PW / 4;        // K-column groups per vector
+  static constexpr int BQ = KP / NQ;       // K columns per producer thread
+  // MMA warps: one thread of each issues the MMAs of tile rows r = j, j + NMW,
+  // ... (a thread issues about one tcgen05.mma per 120 cycles whatever the
+  // tile width; two issuers double that rate)
+  static constexpr int NMW = 2;
+  static constexpr int NT = PT + 32 * (NMW + 1);  // threads of the CTA
 };
 static_assert(KbtPers<8>::TOTAL <= 232448 && KbtPers<16>::TOTAL <= 232448, "persistent tile exceeds shared memory");
 static_assert(KbtPers<8, true>::TOTAL <= 232448 && KbtPers<16, true>::TOTAL <= 232448,
               "persistent tile (A in TMEM) exceeds shared memory");
 
 // A tiles of tile row r in TMEM (the TA form): parts Z_re hi, lo, Z_im hi, lo,
-// KP columns each, from column abase + 4 r KP; this thread's lane, its half of
-// the K columns (b0 .. b0 + KP/2). The TF32 split is the one of kbt_store_row.
-template <int KP>
-__device__ __forceinline__ void kbt_store_row_tmem(uint32_t arow, const float2 (&zr)[KP / 2], int b0) {
-  constexpr int BH = KP / 2;
+// KP columns each, from column abase + 4 r KP; this thread's lane, its BH of
+// the K columns (b0 .. b0 + BH). The TF32 split is the one of kbt_store_row.
+template <int KP, int BH>
+__device__ __forceinline__ void kbt_store_row_tmem(uint32_t arow, const float2 (&zr)[BH], int b0) {
   float rh[BH], rl[BH], ih[BH], il[BH];
 #pragma unroll
   for (int q = 0; q < BH; ++q) {
@@ -719,11 +799,17 @@ __device__ __forceinline__ void kbt_store_row_tmem(uint32_t arow, const float2 (
     tc_st8(c + 1 * KP, rl);
     tc_st8(c + 2 * KP, ih);
     tc_st8(c + 3 * KP, il);
-  } else {
+  } else if constexpr (BH == 4) {
     tc_st4(c + 0 * KP, rh);
     tc_st4(c + 1 * KP, rl);
     tc_st4(c + 2 * KP, ih);
     tc_st4(c + 3 * KP, il);
+  } else {
+    static_assert(BH == 2, "2, 4 or 8 K columns per thread");
+    tc_st2(c + 0 * KP, rh);
+    tc_st2(c + 1 * KP, rl);
+    tc_st2(c + 2 * KP, ih);
+    tc_st2(c + 3 * KP, il);
   }
 }
 
@@ -731,10 +817,10 @@ __device__ __forceinline__ void kbt_store_row_tmem(uint32_t arow, const float2 (
 template <int KP, int KT>
 __device__ __forceinline__ void kbt_issue_merged_ta(uint32_t tmem, uint32_t atm, uint64_t bdesc, uint32_t id1,
                                                     uint32_t id2, int NP, int nr, int nk2, uint32_t acc0,
-                                                    int bpart) {
+                                                    int bpart, int r0, int rs) {
   const uint64_t BP = (uint64_t)(bpart >> 4);
   const int nks = (nk2 + 7) >> 3;
-  for (int r = 0; r < nr; ++r) {
+  for (int r = r0; r < nr; r += rs) {
     const uint32_t dre = tmem + (uint32_t)(4 * r * NP), dim = dre + (uint32_t)(2 * NP);
     const uint32_t a = atm + (uint32_t)(4 * r * KP);
 #pragma unroll
@@ -746,37 +832,44 @@ __device__ __forceinline__ void kbt_issue_merged_ta(uint32_t tmem, uint32_t atm,
       if (KT != 2) {
         tc_mma_tf32_ta(dre, ak + 0 * KP, bk + 0 * BP, id2, f);
         tc_mma_tf32_ta(dre, ak + 1 * KP, bk + 0 * BP, id1, 1u);
+      }
+      if (KT != 1) {
+        tc_mma_tf32_ta(dre, ak + 2 * KP, bk + 4 * BP, id2, KT == 2 ? f : 1u);
+        tc_mma_tf32_ta(dre, ak + 3 * KP, bk + 4 * BP, id1, 1u);
+      }
+    }
+#pragma unroll
+    for (int ks = 0; ks < KP / 8; ++ks) {
+      if (ks >= nks) break;
+      const uint32_t f = ks == 0 ? acc0 : 1u;
+      const uint32_t ak = a + 8u * ks;
+      const uint64_t bk = bdesc + 16u * ks;
+      if (KT != 2) {
         tc_mma_tf32_ta(dim, ak + 2 * KP, bk + 0 * BP, id2, f);
         tc_mma_tf32_ta(dim, ak + 3 * KP, bk + 0 * BP, id1, 1u);
       }
       if (KT != 1) {
-        const uint32_t g = KT == 2 ? f : 1u;
-        tc_mma_tf32_ta(dre, ak + 2 * KP, bk + 4 * BP, id2, g);
-        tc_mma_tf32_ta(dre, ak + 3 * KP, bk + 4 * BP, id1, 1u);
-        tc_mma_tf32_ta(dim, ak + 0 * KP, bk + 2 * BP, id2, g);
+        tc_mma_tf32_ta(dim, ak + 0 * KP, bk + 2 * BP, id2, KT == 2 ? f : 1u);
         tc_mma_tf32_ta(dim, ak + 1 * KP, bk + 2 * BP, id1, 1u);
       }
     }
   }
 }
 
-// kbt_issue (three MMAs per part and K step, D regions 2 r NP) with the A
-// tiles in TMEM
+// kbt_issue (three MMAs per part and K step, D regions 2 r NP, D_re ones
+// first) with the A tiles in TMEM
 template <int KP>
 __device__ __forceinline__ void kbt_issue_ta(uint32_t tmem, uint32_t atm, uint64_t bdesc, uint32_t idesc, int NP,
-                                             int nr, int ktype, int nk2, uint32_t& dinit, int bpart) {
+                                             int nr, int ktype, int nk2, uint32_t& dinit, int bpart, int r0,
+                                             int rs) {
   const int nks = (nk2 + 7) >> 3;
-  for (int r = 0; r < nr; ++r) {
-    int pd[4], pa[4], pb[4];
-    int np = 0;
-    if (ktype != 2) {
-      pd[np] = 0; pa[np] = 0; pb[np] = 0; ++np;
-      pd[np] = 1; pa[np] = 2; pb[np] = 0; ++np;
-    }
-    if (ktype != 1) {
-      pd[np] = 0; pa[np] = 2; pb[np] = 4; ++np;
-      pd[np] = 1; pa[np] = 0; pb[np] = 2; ++np;
-    }
+  int pd[4], pa[4], pb[4];
+  int np = 0;
+  if (ktype != 2) { pd[np] = 0; pa[np] = 0; pb[np] = 0; ++np; }
+  if (ktype != 1) { pd[np] = 0; pa[np] = 2; pb[np] = 4; ++np; }
+  if (ktype != 2) { pd[np] = 1; pa[np] = 2; pb[np] = 0; ++np; }
+  if (ktype != 1) { pd[np] = 1; pa[np] = 0; pb[np] = 2; ++np; }
+  for (int r = r0; r < nr; r += rs) {
     for (int q = 0; q < np; ++q) {
       const uint32_t dcol = tmem + (uint32_t)((2 * r + pd[q]) * NP);
       const uint32_t dbit = 1u << (2 * r + pd[q]);
@@ -802,11 +895,11 @@ template <int KP, bool TA>
 __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* smem) {
   using L = KbtPers<KP, TA>;
   using Rg = KbtRing<KP, TA>;
-  constexpr int R = 64 / KP, BH = KP / 2, NSLOT = L::NSLOT;
+  constexpr int R = 64 / KP, BH = L::BQ, NSLOT = L::NSLOT, PW = L::PW, PT = L::PT;
   constexpr int ATILE = 128 * KP;
   const DevOp& op = p.op;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int vq = wid & 3, b0 = ((wid >> 2) & 1) * BH;
+  const int vq = wid & 3, b0 = (wid >> 2) * BH;  // producers: lane quarter, first K column
   const int vloc = vq * 32 + lane;
   const long long nb = p.nb;
   float* As = reinterpret_cast<float*>(smem);
@@ -830,17 +923,18 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
   constexpr uint32_t NCOLS = 512;
   constexpr uint32_t TA_ACOL = 256;
   constexpr int DMAX = TA ? 256 : 512;
-  if (wid == 8) tc_alloc(tslot, NCOLS);
-  if (tid == 256) {
-    tc_mbar_init(full, 8);
-    tc_mbar_init(empty, 1);
+  constexpr int NMW = L::NMW;
+  if (wid == PW) tc_alloc(tslot, NCOLS);
+  if (tid == PT) {
+    tc_mbar_init(full, PW);
+    tc_mbar_init(empty, NMW);  // one commit per MMA warp and term
     for (int i = 0; i < NSLOT; ++i) {
       tc_mbar_init(rfull + i, 1);
-      tc_mbar_init(rempty + i, 8);
+      tc_mbar_init(rempty + i, PW);
     }
     for (int b = 0; b < 2; ++b) {
       tc_mbar_init(tready + b, 1);
-      tc_mbar_init(tfree + b, 9);
+      tc_mbar_init(tfree + b, PW + NMW);
     }
   }
   tc_fence_before();
@@ -851,7 +945,7 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
   const int nct = p.tend - p.tfirst;
   const int nwork = nct * p.nvb;
 
-  if (wid == 9) {
+  if (wid == PW + NMW) {
     // ---- work items, term tables and X window loads -------------------------
     const int zslot = kb_slot(p.kslot);  // basis slot of X (third TMA coordinate)
     int g = 0;
@@ -911,8 +1005,9 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
       }
       __syncwarp();
     }
-  } else if (wid == 8) {
-    // ---- MMA issue -------------------------------------------------------------
+  } else if (wid >= PW) {
+    // ---- MMA issue: warp PW + j takes tile rows j, j + NMW, ... ------------------
+    const int r0 = wid - PW;
     int ncommit = 0;
     const uint64_t adesc0 = tc_desc(tc_smem_u32(As), 128u, 32u * KP);
     const uint64_t bdesc0 = tc_desc(tc_smem_u32(Bs), 128u, 32u * KP);
@@ -944,21 +1039,21 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
             const uint32_t atm = tmem + TA_ACOL;
             if (merged) {
               const uint32_t acc0 = ncommit > c0 ? 1u : 0u;
-              if (tt.ktype == 1) kbt_issue_merged_ta<KP, 1>(tmem, atm, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
-              else if (tt.ktype == 2) kbt_issue_merged_ta<KP, 2>(tmem, atm, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
-              else kbt_issue_merged_ta<KP, 0>(tmem, atm, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
+              if (tt.ktype == 1) kbt_issue_merged_ta<KP, 1>(tmem, atm, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart, r0, NMW);
+              else if (tt.ktype == 2) kbt_issue_merged_ta<KP, 2>(tmem, atm, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart, r0, NMW);
+              else kbt_issue_merged_ta<KP, 0>(tmem, atm, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart, r0, NMW);
             } else {
-              kbt_issue_ta<KP>(tmem, atm, bdesc, idesc, NP, nr, tt.ktype, tt.nk2, dinit, Rg::BPART);
+              kbt_issue_ta<KP>(tmem, atm, bdesc, idesc, NP, nr, tt.ktype, tt.nk2, dinit, Rg::BPART, r0, NMW);
             }
           } else if (merged) {
             const uint32_t acc0 = ncommit > c0 ? 1u : 0u;
-            if (tt.ktype == 1) kbt_issue_merged<KP, 1>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
-            else if (tt.ktype == 2) kbt_issue_merged<KP, 2>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
-            else kbt_issue_merged<KP, 0>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart);
+            if (tt.ktype == 1) kbt_issue_merged<KP, 1>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart, r0, NMW);
+            else if (tt.ktype == 2) kbt_issue_merged<KP, 2>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart, r0, NMW);
+            else kbt_issue_merged<KP, 0>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart, r0, NMW);
           } else {
-            kbt_issue<KP>(tmem, adesc0, bdesc, idesc, NP, nr, tt.ktype, tt.nk2, dinit, Rg::BPART);
+            kbt_issue<KP>(tmem, adesc0, bdesc, idesc, NP, nr, tt.ktype, tt.nk2, dinit, Rg::BPART, r0, NMW);
           }
-          tc_commit(empty);
+          tc_commit(empty);  // arrives once this thread's MMAs (if any) are done
           ++ncommit;
         }
       }
@@ -968,7 +1063,8 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
     }
   } else {
     // ---- producers ---------------------------------------------------------------
-    int g = 0, ncommit = 0;
+    int ncommit = 0;
+    KbtRingPos rp{0, 0u};
     float2 z[R][BH];
     for (int it = 0;; ++it) {
       const int b = it & 1;
@@ -994,7 +1090,7 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
       const bool merged = 4 * R * NP <= DMAX;
       const int bpart = merged ? NP * KP * 4 : Rg::BPART;
       if (te == tb) {  // no term reaches this slab
-        for (int e = wid >> 2; e < nr * nk1; e += 2)
+        for (int e = wid >> 2; e < nr * nk1; e += L::NQ)
           Y[((long long)(e / nk1) * ld1 + e % nk1) * nb] = make_float2(0.f, 0.f);
         __syncwarp();
         if (lane == 0) tc_mbar_arrive(tfree + b);
@@ -1005,11 +1101,11 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
       KbtPre pre;
       // every producer is past the previous tile's use of the B / MF buffers
       // (its epilogue waited for the last MMAs); the staging below reuses them
-      kbt_preload<KP>(cur, nk1, NP, i0, nr, tid, pre);
-      kbt_producer_sync();
-      kbt_stage_pre<KP>(cur, pre, NP, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, MFd0, tid, bpart);
-      kbt_producer_sync();
-      if (!kbt_zstep_ring<KP, L::NSLOT>(z, cur, nb, nr, b0, vloc, lane, MFs0, Cs0, MFd0, ring, rfull, rempty, g))
+      kbt_preload<KP, PT>(cur, nk1, NP, i0, nr, tid, pre);
+      kbt_producer_sync<PT>();
+      kbt_stage_pre<KP, PT>(cur, pre, NP, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, MFd0, tid, bpart);
+      kbt_producer_sync<PT>();
+      if (!kbt_zstep_ring<KP, BH, L::NSLOT>(z, cur, nb, nr, b0, vloc, lane, MFs0, Cs0, MFd0, ring, rfull, rempty, rp))
         ok = false;
       for (int term = tb; term < te; ++term) {
         const int buf = (term - tb) & 1;
@@ -1017,7 +1113,7 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
         KbtTerm nxt;
         if (has_next) {
           nxt = term_at(term + 1 - tb);
-          kbt_preload<KP>(nxt, nk1, NP, i0, nr, tid, pre);
+          kbt_preload<KP, PT>(nxt, nk1, NP, i0, nr, tid, pre);
         }
         if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
         tc_fence_after();
@@ -1026,7 +1122,7 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
             const uint32_t arow = tmem + TA_ACOL + ((uint32_t)(vq * 32) << 16);
 #pragma unroll
             for (int r = 0; r < R; ++r)
-              if (r < nr) kbt_store_row_tmem<KP>(arow + (uint32_t)(4 * r * KP), z[r], b0);
+              if (r < nr) kbt_store_row_tmem<KP, BH>(arow + (uint32_t)(4 * r * KP), z[r], b0);
             tc_wait_st();
             tc_fence_before();
           } else {
@@ -1042,12 +1138,12 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
           atomicExch(p.err, KR_ERR_ARG);  // outside the tile shape: skipped
         }
         if (has_next) {
-          kbt_stage_pre<KP>(nxt, pre, NP, nr, reinterpret_cast<float*>(Bs + (buf ^ 1) * Rg::BBUF),
+          kbt_stage_pre<KP, PT>(nxt, pre, NP, nr, reinterpret_cast<float*>(Bs + (buf ^ 1) * Rg::BBUF),
                             MFs0 + (buf ^ 1) * 8 * KB_WMAX, Cs0 + (buf ^ 1) * 8 * KB_WMAX,
                             MFd0 + (buf ^ 1) * Rg::MFD, tid, bpart);
-          kbt_producer_sync();
-          if (!kbt_zstep_ring<KP, L::NSLOT>(z, nxt, nb, nr, b0, vloc, lane, MFs0 + (buf ^ 1) * 8 * KB_WMAX,
-                                  Cs0 + (buf ^ 1) * 8 * KB_WMAX, MFd0 + (buf ^ 1) * Rg::MFD, ring, rfull, rempty, g))
+          kbt_producer_sync<PT>();
+          if (!kbt_zstep_ring<KP, BH, L::NSLOT>(z, nxt, nb, nr, b0, vloc, lane, MFs0 + (buf ^ 1) * 8 * KB_WMAX,
+                                  Cs0 + (buf ^ 1) * 8 * KB_WMAX, MFd0 + (buf ^ 1) * Rg::MFD, ring, rfull, rempty, rp))
             ok = false;
           cur = nxt;
         }
@@ -1055,7 +1151,7 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
       if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
       tc_fence_after();
       const bool any = ncommit > c0;
-      for (int r = wid >> 2; r < nr; r += 2) {
+      for (int r = wid >> 2; r < nr; r += L::NQ) {
         for (int cc = 0; cc < NP; cc += 16) {
           float re[16], im[16];
           const uint32_t lanebase = (uint32_t)(vq * 32) << 16;
@@ -1088,11 +1184,12 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
   if (!ok && lane == 0) atomicExch(p.err, KR_ERR_TIMEOUT);
   tc_fence_before();
   __syncthreads();
-  if (wid == 8) tc_dealloc(tmem, NCOLS);
+  if (wid == PW) tc_dealloc(tmem, NCOLS);
 }
 
 template <int KP, bool TA>
-__global__ void __launch_bounds__(320, 1) kb_matvec_tcp(BatchTC p, const __grid_constant__ CUtensorMap xmap) {
+__global__ void __launch_bounds__(KbtPers<KP, TA>::NT, 1) kb_matvec_tcp(BatchTC p,
+                                                                       const __grid_constant__ CUtensorMap xmap) {
   extern __shared__ __align__(1024) char kbt_smem[];
   kbt_persist<KP, TA>(p, &xmap, kbt_smem);
 }
@@ -1161,20 +1258,20 @@ int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, const int* cls, i
       if (c == 0) {
         KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tcp<8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           KbtPers<8, true>::TOTAL));
-        kb_matvec_tcp<8, true><<<grid, 320, KbtPers<8, true>::TOTAL, st>>>(q, xmap);
+        kb_matvec_tcp<8, true><<<grid, KbtPers<8, true>::NT, KbtPers<8, true>::TOTAL, st>>>(q, xmap);
       } else {
         KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tcp<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           KbtPers<16, true>::TOTAL));
-        kb_matvec_tcp<16, true><<<grid, 320, KbtPers<16, true>::TOTAL, st>>>(q, xmap);
+        kb_matvec_tcp<16, true><<<grid, KbtPers<16, true>::NT, KbtPers<16, true>::TOTAL, st>>>(q, xmap);
       }
     } else if (c == 0) {
       KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tcp<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         KbtPers<8>::TOTAL));
-      kb_matvec_tcp<8, false><<<grid, 320, KbtPers<8>::TOTAL, st>>>(q, xmap);
+      kb_matvec_tcp<8, false><<<grid, KbtPers<8>::NT, KbtPers<8>::TOTAL, st>>>(q, xmap);
     } else {
       KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tcp<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         KbtPers<16>::TOTAL));
-      kb_matvec_tcp<16, false><<<grid, 320, KbtPers<16>::TOTAL, st>>>(q, xmap);
+      kb_matvec_tcp<16, false><<<grid, KbtPers<16>::NT, KbtPers<16>::TOTAL, st>>>(q, xmap);
     }
     KR_CUDA(ctx, cudaGetLastError());
   }

@@ -50,11 +50,13 @@ struct DevOp {
   // K blocks
   const long long* k_off; const int* k_rows; const int* k_cols; const int* k_type; const double* k_data;
   const float* k_f32;   // FP32 copy of k_data (same offsets), for the batched complex64 path
+  const float* k_lo;    // k_data - k_f32 rounded to FP32: with k_f32 the double-float K
   // MF instances (ELL): values at mf_val + mf_off[i], columns at m_col + mf_col_off[i]
   const long long* mf_off; const long long* mf_col_off; const int* mf_width;
   const int* mf_diag;   // per MF instance: first diagonal d0 if slot w of row i holds column i + d0 + w, else KR_NO_DIAG
   const int* m_col; double2* mf_val;
   float2* mf_f32;       // FP32 copy of mf_val, written with it by the field kernel
+  float2* mf_lo;        // mf_val - mf_f32 rounded to FP32 (double-float MF), written with it
   // terms grouped by output slab
   const int* term_ptr; const int* t_in; const int* t_k; const int* t_mf;
   const int* mf_type;   // per MF instance: 0 complex, 1 real, 2 imaginary (set with the field)
@@ -275,6 +277,193 @@ __device__ void matvec_cta_tasks_f32(const DevOp& op, const double2* __restrict_
       const int p = tid + blockDim.x * q;
       if (p < npair) {
         const double2 yv = make_double2((double)acc[q].x, (double)acc[q].y);
+        y[obase + p] = yv;
+        if (ALPHA) {
+          const double2 v = cscale(ldcg2(x + obase + p), xscale);
+          al = cadd(al, cconjmul(yv, v));
+        }
+      }
+    }
+    if (ALPHA) {
+      al = block_sum2(al, red);
+      if (tid == 0) task_alpha[task] = al;
+    } else {
+      __syncthreads();
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Double-float arithmetic on both FP32 lanes (f32x2): a complex value is held
+// as hi + lo pairs, h = (re_h, im_h), l = (re_l, im_l), hi the FP32 rounding of
+// the FP64 value and lo the FP32 rounding of the remainder (about 48 bits in
+// all). Products are exact to the lo * lo term (Dekker's product with an FMA),
+// sums are Knuth's two-sum with the errors gathered in lo. GB300 runs FP32 at
+// 58x its FP64 rate; one double-float multiply-add of a complex by a real
+// takes 12 f32x2 instructions where FP64 takes 2 DFMA.
+// ---------------------------------------------------------------------------
+struct DF2 {
+  float2 h, l;
+};
+__device__ __forceinline__ float2 f2_add(float2 a, float2 b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d)
+      : "l"(*reinterpret_cast<const uint64_t*>(&a)), "l"(*reinterpret_cast<const uint64_t*>(&b)));
+  return *reinterpret_cast<const float2*>(&d);
+}
+__device__ __forceinline__ float2 f2_sub(float2 a, float2 b) {
+  uint64_t d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d)
+      : "l"(*reinterpret_cast<const uint64_t*>(&a)), "l"(*reinterpret_cast<const uint64_t*>(&b)));
+  return *reinterpret_cast<const float2*>(&d);
+}
+__device__ __forceinline__ float2 f2_mul(float2 a, float2 b) {
+  uint64_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d)
+      : "l"(*reinterpret_cast<const uint64_t*>(&a)), "l"(*reinterpret_cast<const uint64_t*>(&b)));
+  return *reinterpret_cast<const float2*>(&d);
+}
+__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d)
+      : "l"(*reinterpret_cast<const uint64_t*>(&a)), "l"(*reinterpret_cast<const uint64_t*>(&b)),
+        "l"(*reinterpret_cast<const uint64_t*>(&c)));
+  return *reinterpret_cast<const float2*>(&d);
+}
+// s += a * b lane by lane, a = ah + al per lane (for a real factor both lanes
+// hold it; an imaginary one takes b with its lanes swapped and -a on the re lane)
+__device__ __forceinline__ void df2_fma(DF2& s, float2 ah, float2 al, const DF2& b) {
+  const float2 q = f2_mul(make_float2(-ah.x, -ah.y), b.h);  // -p, p = ah bh rounded
+  float2 e = f2_fma(ah, b.h, q);                            // ah bh - p, exact
+  e = f2_fma(ah, b.l, e);
+  e = f2_fma(al, b.h, e);
+  const float2 t = f2_sub(s.h, q);                          // s.h + p
+  const float2 bv = f2_sub(t, s.h);
+  const float2 err = f2_sub(f2_sub(s.h, f2_sub(t, bv)), f2_add(q, bv));  // two-sum error
+  s.l = f2_add(s.l, f2_add(err, e));
+  s.h = t;
+}
+// renormalise: |l| below half an ulp of h
+__device__ __forceinline__ void df2_norm(DF2& s) {
+  const float2 t = f2_add(s.h, s.l);
+  s.l = f2_sub(s.l, f2_sub(t, s.h));
+  s.h = t;
+}
+__device__ __forceinline__ DF2 df2_swap(const DF2& b) {
+  return DF2{make_float2(b.h.y, b.h.x), make_float2(b.l.y, b.l.x)};
+}
+// s += m b for a complex m = (mh, ml) of class mtype (1 real, 2 imaginary, 0 complex)
+__device__ __forceinline__ void df2_cfma(DF2& s, float2 mh, float2 ml, int mtype, const DF2& b) {
+  if (mtype != 2) df2_fma(s, make_float2(mh.x, mh.x), make_float2(ml.x, ml.x), b);
+  if (mtype != 1) df2_fma(s, make_float2(-mh.y, mh.y), make_float2(-ml.y, ml.y), df2_swap(b));
+}
+__device__ __forceinline__ DF2 df2_split(double2 v) {
+  const float2 h = make_float2((float)v.x, (float)v.y);
+  return DF2{h, make_float2((float)(v.x - (double)h.x), (float)(v.y - (double)h.y))};
+}
+__device__ __forceinline__ double2 df2_value(const DF2& s) {
+  return make_double2((double)s.h.x + (double)s.l.x, (double)s.h.y + (double)s.l.y);
+}
+__device__ __forceinline__ DF2 df2_ld(const float4* p) {
+  const float4 v = __ldcg(p);
+  return DF2{make_float2(v.x, v.y), make_float2(v.z, v.w)};
+}
+__device__ __forceinline__ void df2_st(float4* p, const DF2& v) { *p = make_float4(v.h.x, v.h.y, v.l.x, v.l.y); }
+
+// The row-task mat-vec below (matvec_cta_tasks) with double-float products:
+// x from its double-float copy xdf (the same vector, unscaled), MF and K as
+// mf_f32 + mf_lo and k_f32 + k_lo, Z and the sums double-float, Z scaled by
+// xscale in FP64, y and the alpha partial in FP64.
+template <bool ALPHA>
+__device__ void matvec_cta_tasks_df(const DevOp& op, const double2* __restrict__ x, const float4* __restrict__ xdf,
+                                    double xscale, double2* __restrict__ y, unsigned* counter,
+                                    double2* task_alpha, double2* smem, double2* red) {
+  __shared__ int s_task;
+  const int tid = threadIdx.x;
+  float4* zb[2] = {reinterpret_cast<float4*>(smem), reinterpret_cast<float4*>(smem) + op.zmax};
+  for (;;) {
+    if (tid == 0) s_task = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    const int t = s_task;
+    __syncthreads();
+    if (t >= op.ntask) break;
+    const int task = __ldg(op.task_order + t);
+    const int s1 = __ldg(op.task_slab + task);
+    const int i0 = __ldg(op.task_row0 + task);
+    const int nr = __ldg(op.task_nrows + task);
+    const int nk1 = __ldg(op.out_dk + s1);
+    const int npair = nr * nk1;
+    DF2 acc[KR_QMAX];
+#pragma unroll
+    for (int q = 0; q < KR_QMAX; ++q) acc[q] = DF2{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    const int tb = __ldg(op.term_ptr + s1), te = __ldg(op.term_ptr + s1 + 1);
+    for (int term = tb; term < te; ++term) {
+      float4* Z = zb[(term - tb) & 1];
+      const int s2 = __ldg(op.t_in + term);
+      const int kbk = __ldg(op.t_k + term);
+      const int mfi = __ldg(op.t_mf + term);
+      const int nk2 = __ldg(op.in_dk + s2);
+      const float4* X = xdf + __ldg(op.in_off + s2);
+      const int W = __ldg(op.mf_width + mfi);
+      const int* col = op.m_col + __ldg(op.mf_col_off + mfi);
+      const long long mo = __ldg(op.mf_off + mfi);
+      const float2* mfh = op.mf_f32 + mo;
+      const float2* mfl = op.mf_lo + mo;
+      const int mtype = __ldcg(op.mf_type + mfi);
+      const int nz = nr * nk2;
+      for (int p = tid; p < nz; p += blockDim.x) {
+        const int r = p / nk2;
+        const int b = p - r * nk2;
+        const int base = (i0 + r) * W;
+        DF2 z{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        for (int w = 0; w < W; ++w)
+          df2_cfma(z, __ldcg(mfh + base + w), __ldcg(mfl + base + w), mtype,
+                   df2_ld(X + (long long)__ldg(col + base + w) * nk2 + b));
+        const double2 zd = df2_value(z);
+        df2_st(Z + p, df2_split(make_double2(zd.x * xscale, zd.y * xscale)));
+      }
+      const long long ko = __ldg(op.k_off + kbk);
+      const int ktype = __ldg(op.k_type + kbk);
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < KR_QMAX; ++q) {
+        const int p = tid + blockDim.x * q;
+        if (p < npair) {
+          const int r = p / nk1;
+          const int a = p - r * nk1;
+          const float4* zr = Z + r * nk2;
+          DF2 s = acc[q];
+          if (ktype == 1 || ktype == 2) {  // real K, or K = i Ki
+            const float* KH = op.k_f32 + ko;
+            const float* KL = op.k_lo + ko;
+            for (int b = 0; b < nk2; ++b) {
+              const float kh = __ldg(KH + b * nk1 + a), kl = __ldg(KL + b * nk1 + a);
+              const float4 zv = zr[b];
+              const DF2 z{make_float2(zv.x, zv.y), make_float2(zv.z, zv.w)};
+              if (ktype == 1) df2_fma(s, make_float2(kh, kh), make_float2(kl, kl), z);
+              else df2_fma(s, make_float2(-kh, kh), make_float2(-kl, kl), df2_swap(z));
+            }
+          } else {  // complex K, interleaved (re, im)
+            const float2* KH = reinterpret_cast<const float2*>(op.k_f32 + ko);
+            const float2* KL = reinterpret_cast<const float2*>(op.k_lo + ko);
+            for (int b = 0; b < nk2; ++b) {
+              const float4 zv = zr[b];
+              df2_cfma(s, __ldg(KH + b * nk1 + a), __ldg(KL + b * nk1 + a), 0,
+                       DF2{make_float2(zv.x, zv.y), make_float2(zv.z, zv.w)});
+            }
+          }
+          df2_norm(s);
+          acc[q] = s;
+        }
+      }
+    }
+    const long long obase = __ldg(op.out_off + s1) + (long long)i0 * nk1;
+    double2 al = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int q = 0; q < KR_QMAX; ++q) {
+      const int p = tid + blockDim.x * q;
+      if (p < npair) {
+        const double2 yv = df2_value(acc[q]);
         y[obase + p] = yv;
         if (ALPHA) {
           const double2 v = cscale(ldcg2(x + obase + p), xscale);

@@ -42,6 +42,7 @@ struct DevField {
   const double2* m_val;
   double2* mf_val;
   float2* mf_f32;
+  float2* mf_lo;
   int* mf_band;                 // out: per MF instance [W - 1 - lowest, highest] slot with a non-zero value (-1: none)
 };
 
@@ -137,5 +138,7 @@ struct kr_op {
   double* beta = nullptr;
   unsigned* bar = nullptr;  // [count, gen]
   int* status = nullptr;    // [status, kout]
+  float4* xdf = nullptr;    // double-float copy of the vector the next mat-vec reads (KR_PREC_DF)
+  int prec = 0;             // products of the plain step: KR_PREC_F64 or KR_PREC_DF
 };
 

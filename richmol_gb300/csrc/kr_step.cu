@@ -76,7 +76,9 @@ __global__ void __launch_bounds__(256) kr_field_kernel(DevField f, Coef c) {
     if (c.t(p) > 0.0 && sqrt(cabs2(v)) < c.t(p)) v = make_double2(0.0, 0.0);
     const double2 mfv = cmul(c.s(p), v);
     f.mf_val[e] = mfv;
-    f.mf_f32[e] = make_float2((float)mfv.x, (float)mfv.y);
+    const float2 mh = make_float2((float)mfv.x, (float)mfv.y);
+    f.mf_f32[e] = mh;
+    f.mf_lo[e] = make_float2((float)(mfv.x - (double)mh.x), (float)(mfv.y - (double)mh.y));
     if (mfv.x != 0.0 || mfv.y != 0.0) {  // band of slots that carry a value with this field
       const int W = __ldg(f.m_width + g);
       const int w = (int)(local % W);
@@ -269,6 +271,7 @@ struct StepArgs {
   unsigned* bar_gen;
   int* status;
   int* kout;
+  float4* xdf;  // double-float copy of the vector the next mat-vec reads (DF kernels)
   double2 fac;
   double tol;
   int maxorder;
@@ -285,6 +288,16 @@ struct StepSmem {
   double scalar[4];
 };
 
+// the mat-vec of the plain step: FP64 products, or double-float ones (DF) from
+// the copy a.xdf of the vector, which the vector phases write beside it
+template <bool DF>
+__device__ __forceinline__ void step_matvec(const StepArgs& a, const double2* x, double xscale, unsigned* counter,
+                                            double2* smem, double2* red) {
+  if constexpr (DF) matvec_cta_tasks_df<true>(a.op, x, a.xdf, xscale, a.w, counter, a.task_alpha, smem, red);
+  else matvec_cta_tasks<true>(a.op, x, xscale, a.w, counter, a.task_alpha, smem, red);
+}
+
+template <bool DF>
 __global__ void __launch_bounds__(KR_THREADS, 2) kr_step_kernel(StepArgs a) {
   extern __shared__ double2 smem_dyn[];
   __shared__ StepSmem ss;
@@ -304,11 +317,12 @@ __global__ void __launch_bounds__(KR_THREADS, 2) kr_step_kernel(StepArgs a) {
     double2 v = a.state[e];
     if (a.phase) v = cmul(v, a.phase[e]);
     V0[e] = v;
+    if (DF) df2_st(a.xdf + e, df2_split(v));
   }
   if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
 
   // ---- k = 0: w = H V0, T00 = vdot(w, V0), W0 = w - T00 V0 (tdse.py:443-446)
-  matvec_cta_tasks<true>(a.op, V0, 1.0, a.w, a.counters, a.task_alpha, smem_dyn, ss.red);
+  step_matvec<DF>(a, V0, 1.0, a.counters, smem_dyn, ss.red);
   if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
   {
     const double2 a0 = grid_partials_sum2(a.task_alpha, a.op.ntask, ss.red);
@@ -320,6 +334,7 @@ __global__ void __launch_bounds__(KR_THREADS, 2) kr_step_kernel(StepArgs a) {
       const double2 v = ldcg2(V0 + e);
       r = csub(r, cmul(a0, v));
       W0[e] = r;
+      if (DF) df2_st(a.xdf + e, df2_split(r));
       bp += cabs2(r);
     }
     const double2 s = block_sum2(make_double2(bp, 0.0), ss.red);
@@ -390,6 +405,7 @@ __global__ void __launch_bounds__(KR_THREADS, 2) kr_step_kernel(StepArgs a) {
       for (long long e = gtid; e < n; e += gstride) {
         const double2 v = ldcg2(Vk + e);
         Vk[e] = make_double2(v.x / nrm, v.y / nrm);
+        if (DF) df2_st(a.xdf + e, df2_split(make_double2(v.x / nrm, v.y / nrm)));
       }
       if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
       xsrc = Vk;
@@ -397,7 +413,7 @@ __global__ void __launch_bounds__(KR_THREADS, 2) kr_step_kernel(StepArgs a) {
     }
 
     // w = H V_k and T_kk = vdot(w, V_k) (tdse.py:467-468)
-    matvec_cta_tasks<true>(a.op, xsrc, xscale, a.w, a.counters + k, a.task_alpha, smem_dyn, ss.red);
+    step_matvec<DF>(a, xsrc, xscale, a.counters + k, smem_dyn, ss.red);
     if (!grid_barrier(a.bar_count, a.bar_gen, a.status, KR_ERR_TIMEOUT)) return;
 
     // T_kk, then exp(fac T_{0..k}) e0 in every CTA (tdse.py:474)
@@ -424,6 +440,7 @@ __global__ void __launch_bounds__(KR_THREADS, 2) kr_step_kernel(StepArgs a) {
         double2 r = csub(ldcg2(a.w + e), cmul(ak, vk));
         r = csub(r, cscale(ldcg2(Vkm1 + e), beta_k));
         Wk[e] = r;
+        if (DF) df2_st(a.xdf + e, df2_split(r));
         bp += cabs2(r);
         double2 u = make_double2(0.0, 0.0);
         for (int i = 0; i <= k; ++i) cfma(u, ss.c[i], ldcg2(a.V + (long long)i * n + e));
@@ -831,7 +848,9 @@ static size_t g_smem_max = 0;
 static cudaError_t ensure_step_smem(size_t smem) {
   std::lock_guard<std::mutex> lk(g_smem_mu);
   if (smem <= g_smem_max) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(kr_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(kr_step_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(kr_step_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(kr_matvec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess)
@@ -840,6 +859,18 @@ static cudaError_t ensure_step_smem(size_t smem) {
     e = cudaFuncSetAttribute(kr_seg_step_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess) g_smem_max = smem;
   return e;
+}
+
+// the plain step kernel of an operator's precision
+static void* step_kernel(const kr_op* op) {
+  return op->prec == KR_PREC_DF ? (void*)kr_step_kernel<true> : (void*)kr_step_kernel<false>;
+}
+
+extern "C" int kr_op_set_precision(kr_op* op, int32_t prec) {
+  if (!op || (prec != KR_PREC_F64 && prec != KR_PREC_DF))
+    return set_err(op ? op->ctx : nullptr, KR_ERR_ARG, "kr_op_set_precision: bad argument");
+  op->prec = prec;
+  return KR_OK;
 }
 
 namespace {
@@ -1149,7 +1180,11 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
     return set_err(ctx, KR_ERR_CUDA, "cannot raise the dynamic shared memory of the step kernels");
   }
   int occ = 0;
-  cudaError_t ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kr_step_kernel, KR_THREADS, op->smem);
+  cudaError_t ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kr_step_kernel<false>, KR_THREADS, op->smem);
+  int occ_df = 0;
+  if (ce == cudaSuccess)
+    ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_df, kr_step_kernel<true>, KR_THREADS, op->smem);
+  occ = std::min(occ, occ_df);
   if (ce != cudaSuccess || occ < 1) {
     kr_op_destroy(op);
     return set_err(ctx, KR_ERR_CUDA, "kr_step_kernel cannot be resident");
@@ -1322,6 +1357,8 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
     std::vector<float> k32(k_t.begin(), k_t.end());
     float* p_f;
     UP(k32.data(), k32.size(), &p_f); D.k_f32 = p_f;
+    for (size_t i = 0; i < k32.size(); ++i) k32[i] = (float)(k_t[i] - (double)k32[i]);  // the double-float lo part
+    UP(k32.data(), k32.size(), &p_f); D.k_lo = p_f;
   }
   UP((const long long*)inst_ptr.data(), d->nmf, &p_l); D.mf_off = p_l;
   UP((const long long*)mf_col_off.data(), d->nmf, &p_l); D.mf_col_off = p_l;
@@ -1333,6 +1370,7 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   {
     float2* p_f2;
     UP((const float2*)nullptr, nent, &p_f2); D.mf_f32 = p_f2;
+    UP((const float2*)nullptr, nent, &p_f2); D.mf_lo = p_f2;
   }
   UP(term_ptr.data(), term_ptr.size(), &p_i); D.term_ptr = p_i;
   UP(t_in.data(), t_in.size(), &p_i); D.t_in = p_i;
@@ -1371,6 +1409,7 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   UP((const double2*)d->m_val, d->m_val_len / 2, &p_c); F.m_val = p_c;
   F.mf_val = D.mf_val;
   F.mf_f32 = D.mf_f32;
+  F.mf_lo = D.mf_lo;
   F.nmf = d->nmf;
   F.mf_type = const_cast<int*>(D.mf_type);
   signed char* p_s;
@@ -1400,6 +1439,8 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
     UP((const double*)nullptr, (size_t)d->maxorder + 1, &p_d); op->beta = p_d;
     UP((const unsigned*)nullptr, 2, &p_u); op->bar = p_u;
     UP((const int*)nullptr, 2, &p_i); op->status = p_i;
+    float4* p_f4;
+    UP((const float4*)nullptr, (size_t)n, &p_f4); op->xdf = p_f4;
   }
 #undef UP
   KR_CUDA(ctx, cudaDeviceSynchronize());
@@ -1546,6 +1587,7 @@ extern "C" int kr_step(kr_op* op, void* states, int64_t nvec, const void* phase,
   a.bar_gen = op->bar + 1;
   a.status = op->status;
   a.kout = op->status + 1;
+  a.xdf = op->xdf;
   a.fac = make_double2(fac_re, fac_im);
   a.tol = tol;
   a.maxorder = op->maxorder;
@@ -1555,7 +1597,7 @@ extern "C" int kr_step(kr_op* op, void* states, int64_t nvec, const void* phase,
     KR_CUDA(op->ctx, cudaMemsetAsync(op->bar, 0, sizeof(unsigned), st));  // arrival count only
     void* args[] = {&a};
     KR_CUDA(op->ctx, ensure_step_smem(op->smem));
-    KR_CUDA(op->ctx, cudaLaunchCooperativeKernel((void*)kr_step_kernel, dim3(op->grid), dim3(KR_THREADS), args,
+    KR_CUDA(op->ctx, cudaLaunchCooperativeKernel(step_kernel(op), dim3(op->grid), dim3(KR_THREADS), args,
                                                  op->smem, st));
     op->launches++;
     if (korder) {
@@ -1753,6 +1795,7 @@ extern "C" int kr_static_scratch_bytes(const kr_op* op, size_t* needed, size_t* 
   b += round256(sizeof(double) * (m + 1));                   // beta
   b += round256(sizeof(unsigned) * 2);                       // barrier
   b += round256(sizeof(int) * 2);                            // status, Krylov order
+  b += round256(sizeof(float4) * n);                         // double-float copy of x
   if (needed) *needed = b;
   return KR_OK;
 }
@@ -1827,6 +1870,7 @@ extern "C" int kr_step_static(kr_op* op, void* states, int64_t nvec, const void*
   a.beta = (double*)carve(sizeof(double) * (m + 1));
   unsigned* bar = (unsigned*)carve(sizeof(unsigned) * 2);
   int* status = (int*)carve(sizeof(int) * 2);
+  a.xdf = (float4*)carve(sizeof(float4) * n);
   a.bar_count = bar;
   a.bar_gen = bar + 1;
   a.status = status;
@@ -1847,7 +1891,7 @@ extern "C" int kr_step_static(kr_op* op, void* states, int64_t nvec, const void*
     KR_CUDA(op->ctx, cudaMemsetAsync(bar, 0, sizeof(unsigned), st));
     void* args[] = {&a};
     KR_CUDA(op->ctx, ensure_step_smem(op->smem));
-    KR_CUDA(op->ctx, cudaLaunchCooperativeKernel((void*)kr_step_kernel, dim3(op->grid), dim3(KR_THREADS), args,
+    KR_CUDA(op->ctx, cudaLaunchCooperativeKernel(step_kernel(op), dim3(op->grid), dim3(KR_THREADS), args,
                                                  op->smem, st));
     op->launches++;
     if (korder) {

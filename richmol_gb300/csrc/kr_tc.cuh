@@ -113,6 +113,11 @@ __device__ __forceinline__ void tc_st4(uint32_t taddr, const float* v) {
                "r"(__float_as_uint(v[3]))
                : "memory");
 }
+__device__ __forceinline__ void tc_st2(uint32_t taddr, const float* v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1, %2};" ::"r"(taddr), "r"(__float_as_uint(v[0])),
+               "r"(__float_as_uint(v[1]))
+               : "memory");
+}
 __device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // d = a * b + c on both FP32 lanes (PTX fma.rn.f32x2, one instruction)

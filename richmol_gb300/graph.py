@@ -39,10 +39,12 @@ class StepGraph:
                       L2 flush for timing)
         schedule : None (fields from device memory above 16 parts), or True /
                    False to force either form
+        products : "f64" or "df", the arithmetic of the mat-vec products (as
+                   TDSE.update's products), fixed when the steps are recorded
     """
 
     def __init__(self, tdse, H0, vecs, hamiltonian, times, tol=1e-15, maxorder=100, before_step=None,
-                 schedule=None):
+                 schedule=None, products="f64"):
         assert torch.is_tensor(vecs) and vecs.is_cuda and vecs.dtype == torch.complex128
         self.vecs = vecs if vecs.dim() == 2 else vecs.reshape(1, -1)
         self.times = list(times)
@@ -50,6 +52,7 @@ class StepGraph:
         phase = tdse._h0_phase(H0, fac, vecs.device) if H0 is not None else None
         # operators are created (and uploaded) outside the recording
         self.plan = hamiltonian(self.times[0]).device_operator(maxorder=maxorder)
+        self.plan.set_precision(products)
         if schedule is None:
             schedule = len(self.plan.sources) > _native.KR_PART_INLINE
         elif not schedule and len(self.plan.sources) > _native.KR_PART_INLINE:
@@ -76,6 +79,7 @@ class StepGraph:
                     plan.set_field_step(i)  # field launch of this step, from the schedule
                 else:
                     plan = hamiltonian(t).device_operator(maxorder=maxorder)  # field launch of this step
+                    plan.set_precision(products)
                 plan.step(self.vecs, phase, fac, tol, flags=0, korder=None)
         torch.cuda.current_stream().wait_stream(stream)
 

@@ -464,6 +464,17 @@ class OperatorPlan:
         _native.check(_native.lib().kr_matvec(self.op, _native.ptr(x), _native.ptr(y), nvec,
                                               stream_ptr(stream)), self.ctx)
 
+    def set_precision(self, products):
+        """Arithmetic of the plain step's mat-vec products (kr_op_set_precision):
+        "f64" (FP64, the default) or "df" (double-float on the FP32 pipes, about
+        1e-14 relative per product; vectors, Lanczos scalars and exponential
+        stay FP64)."""
+        prec = {"f64": _native.KR_PREC_F64, "df": _native.KR_PREC_DF}.get(products)
+        if prec is None:
+            raise ValueError(f"products must be 'f64' or 'df', not {products!r}")
+        _native.check(_native.lib().kr_op_set_precision(self.op, prec), self.ctx)
+        self.products = products
+
     def step(self, states, phase, fac, tol, flags=0, korder=None, stream=None):
         nvec = states.shape[0] if states.dim() == 2 else 1
         kp = None

@@ -15,9 +15,10 @@ the reference cannot build here):
   through the pulse maximum for 256 vectors of the thermal ensemble on the
   batched mixed-precision path, four of them checked against the oracle.
 
-Tolerances: plain FP64 path, states 1e-10 relative per step and observables
-1e-9 absolute; batched mixed-precision path, observables 1e-6 absolute (the
-stated bound of that form) and states 1e-6 relative.
+Tolerances: plain path, states 1e-10 relative per step and observables 1e-9
+absolute, with FP64 products and with double-float ones (products="df");
+batched mixed-precision path, observables 1e-6 absolute (the stated bound of
+that form) and states 1e-6 relative.
 """
 import os
 
@@ -80,7 +81,11 @@ def _pops(T, v):
     return out
 
 
-def test_ocs_c1_configuration_matches_reference():
+PRODUCTS = ["f64", "df"]
+
+
+@pytest.mark.parametrize("products", PRODUCTS)
+def test_ocs_c1_configuration_matches_reference(products):
     from richmol_gb300 import TDSE
     case = "ocs_c1_j20.npz"
     d, meta = _load(case)
@@ -97,7 +102,7 @@ def test_ocs_c1_configuration_matches_reference():
     worst = dict(state=0.0, cos2=0.0, cos=0.0, pops=0.0)
     for i in range(len(tc)):
         Hac.field(d["fields"][i])
-        v, t2 = td.update(Hac, v, H0=h0)
+        v, t2 = td.update(Hac, v, H0=h0, products=products)
         assert abs(t2 - d["times"][i]) < 1e-12
         vh = v.cpu().numpy()
         worst["cos2"] = max(worst["cos2"], abs(_dev_expect(cos2, v)[0] + 1 / 3 - d["cos2"][i]))
@@ -105,7 +110,7 @@ def test_ocs_c1_configuration_matches_reference():
         worst["pops"] = max(worst["pops"], np.abs(_pops(h0, vh)[0] - d["pops"][i]).max())
         if i in saved:
             worst["state"] = max(worst["state"], _rel(vh[0], d["states"][saved[i]]))
-    print("ocs c1 (300 steps):", worst)
+    print("ocs c1 (300 steps, %s products):" % products, worst)
     assert worst["state"] < STATE_RTOL
     assert worst["cos2"] < OBS_ATOL and worst["cos"] < OBS_ATOL and worst["pops"] < OBS_ATOL
 
@@ -124,7 +129,8 @@ def _asym_j10():
     return case, d, h0, Hdc, Hac, td, tc
 
 
-def test_asym_j10_ensemble_matches_reference():
+@pytest.mark.parametrize("products", PRODUCTS)
+def test_asym_j10_ensemble_matches_reference(products):
     case, d, h0, Hdc, Hac, td, tc = _asym_j10()
     cos2, cos = _ct(case, "cos2"), _ct(case, "cos")
     v0 = td.init_state(h0, temp=5, thresh=1e-3)
@@ -134,7 +140,7 @@ def test_asym_j10_ensemble_matches_reference():
     worst = dict(state=0.0, cos2=0.0, cos=0.0, pops=0.0)
     for i in range(len(tc)):
         Hac.field(d["fields"][i])
-        v, _ = td.update(Hdc + Hac, v, H0=h0)
+        v, _ = td.update(Hdc + Hac, v, H0=h0, products=products)
         vh = v.cpu().numpy()
         worst["cos2"] = max(worst["cos2"], np.abs(_dev_expect(cos2, v) - d["cos2"][i]).max())
         worst["cos"] = max(worst["cos"], np.abs(_dev_expect(cos, v) - d["cos"][i]).max())
@@ -142,7 +148,7 @@ def test_asym_j10_ensemble_matches_reference():
         if i in saved:
             worst["state"] = max(worst["state"], _rel(vh[:2], d["states"][saved[i]]))
     worst["state"] = max(worst["state"], _rel(v.cpu().numpy(), d["final"]))
-    print("asym j10 (50 steps, 22 vectors):", worst)
+    print("asym j10 (50 steps, 22 vectors, %s products):" % products, worst)
     assert worst["state"] < STATE_RTOL
     assert worst["cos2"] < OBS_ATOL and worst["cos"] < OBS_ATOL and worst["pops"] < OBS_ATOL
 
@@ -171,7 +177,8 @@ def test_asym_j10_batched_ensemble_within_mixed_precision_bound():
     assert state < MIXED_STATE_RTOL
 
 
-def test_c1_molecule_matches_reference():
+@pytest.mark.parametrize("products", PRODUCTS)
+def test_c1_molecule_matches_reference(products):
     from richmol_gb300 import TDSE
     case = "c1_j10.npz"
     d, meta = _load(case)
@@ -186,10 +193,10 @@ def test_c1_molecule_matches_reference():
     worst = 0.0
     for i in range(len(tc)):
         Hac.field(d["fields"][i])
-        v, _ = td.update(Hac, v, H0=h0)
+        v, _ = td.update(Hac, v, H0=h0, products=products)
         worst = max(worst, np.abs(_dev_expect(cos2, v) - d["cos2"][i]).max())
     state = _rel(v.cpu().numpy()[:4], d["final"])
-    print("c1 j10 (10 steps):", worst, state)
+    print("c1 j10 (10 steps, %s products):" % products, worst, state)
     assert worst < OBS_ATOL and state < STATE_RTOL
 
 
@@ -217,22 +224,27 @@ def test_plain_j40_steps_through_pulse_match_oracle():
     ot = OTDSE(t_start=wl.t_start, t_end=wl.t_end, dt=wl.dt)
     ot.time_grid()
     v0 = td.init_state(wl.h0, temp=0)
-    v = torch.from_numpy(v0).cuda()
+    vs = {p: torch.from_numpy(v0).cuda() for p in PRODUCTS}  # FP64 and double-float products
     r = v0.copy()
     c2 = from_oracle_mat(wl.cos2)
     c1 = from_oracle_mat(wl.cos)
-    worst = dict(state=0.0, cos2=0.0, cos=0.0)
+    worst = {p: dict(state=0.0, cos2=0.0, cos=0.0) for p in PRODUCTS}
     for i in range(i0, i0 + 10):
         H = wl.hamiltonian(tc[i])
-        v, _ = td.update(H, v, H0=wl.h0)
         oHac.field(wl.field(tc[i]))
         r, _ = ot.update(add_cartens(oHdc, oHac), r, H0=oh0)
-        vh = v.cpu().numpy()
-        worst["state"] = max(worst["state"], _rel(vh, r))
-        worst["cos2"] = max(worst["cos2"], abs(_dev_expect(wl.cos2, v)[0] - np.vdot(r[0], c2.dot(r[0])).real))
-        worst["cos"] = max(worst["cos"], abs(_dev_expect(wl.cos, v)[0] - np.vdot(r[0], c1.dot(r[0])).real))
+        for p in PRODUCTS:
+            v, _ = td.update(H, vs[p], H0=wl.h0, products=p)
+            vs[p] = v
+            vh = v.cpu().numpy()
+            w = worst[p]
+            w["state"] = max(w["state"], _rel(vh, r))
+            w["cos2"] = max(w["cos2"], abs(_dev_expect(wl.cos2, v)[0] - np.vdot(r[0], c2.dot(r[0])).real))
+            w["cos"] = max(w["cos"], abs(_dev_expect(wl.cos, v)[0] - np.vdot(r[0], c1.dot(r[0])).real))
     print("J<=40 plain (10 steps through the pulse):", worst, "Krylov orders", td.last_korder.tolist())
-    assert worst["state"] < STATE_RTOL and worst["cos2"] < OBS_ATOL and worst["cos"] < OBS_ATOL
+    for p in PRODUCTS:
+        w = worst[p]
+        assert w["state"] < STATE_RTOL and w["cos2"] < OBS_ATOL and w["cos"] < OBS_ATOL, p
 
 
 def from_oracle_mat(T):
