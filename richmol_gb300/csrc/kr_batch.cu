@@ -609,6 +609,8 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
     q.ntask = op->tc_ntask;
     q.grp_active = masked ? b->grp_active : nullptr;
     q.yscale = yscale;
+    q.tcb = op->tc_b;
+    q.tcb_off = op->tc_boff;
     q.err = b->counts + 2;
     q.tfirst = 0;
     q.tend = op->tc_ntask;

@@ -48,6 +48,8 @@ struct BatchTC {
   int* work;              // persistent kernel: work-item counter (zero at launch)
   const int* grp_active;  // per 32-vector group: any vector active (null: all)
   const double* yscale;   // per vector: output scale (null: 1)
+  const float* tcb;       // B operands of the persistent tiles' terms (kb_build_tc_b)
+  const long long* tcb_off;  // per term: first float of its B block
   int* err;
 };
 

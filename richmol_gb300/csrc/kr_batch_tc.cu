@@ -531,73 +531,28 @@ struct KbtRing {
 };
 static_assert(KbtRing<8>::MFD <= 256 && KbtRing<16>::MFD <= 256, "one dense-band entry per producer thread");
 
-// the next term's B and MF values, loaded into registers before they are staged
-struct KbtPre {
-  float kr[2], ki[2];
-  float2 mf;
-  int col;
-};
-
-// PT producer threads (256 or 512) cover the NP x KP <= 512 B entries
-template <int KP, int PT = 256>
-__device__ __forceinline__ void kbt_preload(const KbtTerm& t, int nk1, int NP, int i0, int nr, int tid, KbtPre& q) {
-#pragma unroll
-  for (int u = 0; u < 512 / PT; ++u) {
-    const int e = tid + PT * u;
-    const int a = e / KP, b = e - (e / KP) * KP;
-    float kr = 0.f, ki = 0.f;
-    if (e < NP * KP && a < nk1 && b < t.nk2) {
-      if (t.ktype == 0) {
-        kr = __ldg(t.KT + ((long long)b * nk1 + a) * 2);
-        ki = __ldg(t.KT + ((long long)b * nk1 + a) * 2 + 1);
-      } else if (t.ktype == 1) {
-        kr = __ldg(t.KT + (long long)b * nk1 + a);
-      } else {
-        ki = __ldg(t.KT + (long long)b * nk1 + a);
-      }
-    }
-    q.kr[u] = kr;
-    q.ki[u] = ki;
-  }
-  q.mf = make_float2(0.f, 0.f);
-  q.col = 0;
-  if (t.dia) {  // dense band entry (c, r) = (tid / R, tid % R): MF[r, c - r]
-    constexpr int R = 64 / KP;
-    const int c = tid / R, r = tid - (tid / R) * R, w = c - r;
-    if (tid < KbtRing<KP>::MFD && r < nr && w >= 0 && w < t.W)
-      q.mf = __ldcg(t.mf + (long long)(i0 + r) * t.Wst + w);
-  } else if (tid < nr * t.W) {
-    const int r = tid / t.W, w = tid - (tid / t.W) * t.W;
-    const long long src = (long long)(i0 + r) * t.Wst + w;
-    q.mf = __ldcg(t.mf + src);
-    q.col = __ldg(t.col + src);
-  }
-}
-
-template <int KP, int PT = 256>
-__device__ __forceinline__ void kbt_stage_pre(const KbtTerm& t, const KbtPre& q, int NP, int nr, float* Bt,
-                                              float2* MFs, int* Cs, float4* MFd, int tid, int bpart) {
-#pragma unroll
-  for (int u = 0; u < 512 / PT; ++u) {
-    const int e = tid + PT * u;
-    if (e >= NP * KP) break;
-    const int a = e / KP, b = e - (e / KP) * KP;
-    const uint32_t o = tc_kmajor_off(a, b, KP) >> 2;
-    const float kr = q.kr[u], ki = q.ki[u];
-    const float krh = tc_tf32(kr), kih = tc_tf32(ki);
-    Bt[0 * (bpart / 4) + o] = krh;
-    Bt[1 * (bpart / 4) + o] = kr - krh;
-    Bt[2 * (bpart / 4) + o] = kih;
-    Bt[3 * (bpart / 4) + o] = ki - kih;
-    Bt[4 * (bpart / 4) + o] = -kih;
-    Bt[5 * (bpart / 4) + o] = -(ki - kih);
-  }
+// M band of a term into a stage buffer (stager warp, its 32 lanes): for a
+// diagonal term the dense band MFd[c][r] = (m_re, m_re, -m_im, m_im) of
+// MF[i0 + r, c - r] (zero outside the band and below nr rows), else the ELL
+// values and columns of the tile's rows
+template <int KP>
+__device__ __forceinline__ void kbt_stage_mf(const KbtTerm& t, int i0, int nr, float4* MFd, float2* MFs, int* Cs,
+                                             int lane) {
+  constexpr int R = 64 / KP;
   if (t.dia) {
-    if (tid < KbtRing<KP>::MFD) MFd[tid] = make_float4(q.mf.x, q.mf.x, -q.mf.y, q.mf.y);
-  } else if (tid < nr * t.W) {
-    const int r = tid / t.W, w = tid - (tid / t.W) * t.W;
-    MFs[r * KB_WMAX + w] = q.mf;
-    Cs[r * KB_WMAX + w] = q.col;
+    for (int e = lane; e < KbtRing<KP>::MFD; e += 32) {
+      const int c = e / R, r = e - (e / R) * R, w = c - r;
+      float2 m = make_float2(0.f, 0.f);
+      if (r < nr && w >= 0 && w < t.W) m = __ldcg(t.mf + (long long)(i0 + r) * t.Wst + w);
+      MFd[e] = make_float4(m.x, m.x, -m.y, m.y);
+    }
+  } else {
+    for (int e = lane; e < nr * t.W; e += 32) {
+      const int r = e / t.W, w = e - (e / t.W) * t.W;
+      const long long src = (long long)(i0 + r) * t.Wst + w;
+      MFs[r * KB_WMAX + w] = __ldcg(t.mf + src);
+      Cs[r * KB_WMAX + w] = __ldg(t.col + src);
+    }
   }
 }
 
@@ -755,8 +710,9 @@ struct KbtPers {
   using Rg = KbtRing<KP, TA>;
   static constexpr int NSLOT = Rg::NSLOT;
   static constexpr int OFF_BAR = Rg::OFF_MFD + 2 * Rg::MFD * 16;
-  // full, empty, rfull[NSLOT], rempty[NSLOT], ready[2], free[2], TMEM slot
-  static constexpr int OFF_HDR = OFF_BAR + 8 * (2 + 2 * NSLOT + 4) + 16;
+  // full, empty, rfull[NSLOT], rempty[NSLOT], ready[2], free[2], staged[2],
+  // sfree[2], TMEM slot
+  static constexpr int OFF_HDR = OFF_BAR + 8 * (2 + 2 * NSLOT + 8) + 16;
   static constexpr int OFF_TAB = OFF_HDR + 2 * 8 * 4;
   static constexpr int TOTAL = OFF_TAB + 2 * KBT_MAXT_P * (int)sizeof(KbtTerm);
   // producer warps: 16 with the A tiles in TMEM (each thread a quarter of the
@@ -770,7 +726,9 @@ struct KbtPers {
   // ... (a thread issues about one tcgen05.mma per 120 cycles whatever the
   // tile width; two issuers double that rate)
   static constexpr int NMW = 2;
-  static constexpr int NT = PT + 32 * (NMW + 1);  // threads of the CTA
+  // then the loader warp (work items, term tables, X rows) and the stager warp
+  // (each term's B operands and M band into one of two stage buffers)
+  static constexpr int NT = PT + 32 * (NMW + 2);  // threads of the CTA
 };
 static_assert(KbtPers<8>::TOTAL <= 232448 && KbtPers<16>::TOTAL <= 232448, "persistent tile exceeds shared memory");
 static_assert(KbtPers<8, true>::TOTAL <= 232448 && KbtPers<16, true>::TOTAL <= 232448,
@@ -914,7 +872,9 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
   uint64_t* rempty = rfull + NSLOT;
   uint64_t* tready = rempty + NSLOT;
   uint64_t* tfree = tready + 2;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(tfree + 2);
+  uint64_t* staged = tfree + 2;  // stage buffer g & 1 holds term g (B by bulk copy, M band)
+  uint64_t* sfree = staged + 2;  // every producer warp is done with it (its term's MMAs included)
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sfree + 2);
   int* hdr0 = reinterpret_cast<int*>(smem + L::OFF_HDR);  // [2][8]: item (-1: none), s1, i0, nr, vb, tb, te
   KbtTerm* tab0 = reinterpret_cast<KbtTerm*>(smem + L::OFF_TAB);
   // TMEM: the D regions of a tile (4 R NP <= 512 columns merged, else 2 R NP);
@@ -934,7 +894,9 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
     }
     for (int b = 0; b < 2; ++b) {
       tc_mbar_init(tready + b, 1);
-      tc_mbar_init(tfree + b, PW + NMW);
+      tc_mbar_init(tfree + b, PW + NMW + 1);
+      tc_mbar_init(staged + b, 1);
+      tc_mbar_init(sfree + b, PW);
     }
   }
   tc_fence_before();
@@ -1005,10 +967,47 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
       }
       __syncwarp();
     }
+  } else if (wid == PW + NMW + 1) {
+    // ---- stage buffers: term g's B operands (one bulk copy of its prebuilt
+    // block) and M band into buffer g & 1, once the producers gave it back ----
+    int g = 0;
+    for (int it = 0;; ++it) {
+      const int b = it & 1;
+      if (!tc_mbar_wait(tready + b, (uint32_t)(it >> 1) & 1u)) {
+        ok = false;
+        break;
+      }
+      const int* hdr = hdr0 + 8 * b;
+      if (hdr[0] < 0) break;
+      const int s1 = hdr[1], i0 = hdr[2], nr = hdr[3], tb = hdr[5], te = hdr[6];
+      const KbtTerm* tab = tab0 + KBT_MAXT_P * b;
+      const int NP = __ldg(op.out_dk + s1) <= 16 ? 16 : 32;
+      const uint32_t bbytes = (uint32_t)(6 * NP * KP * 4);
+      for (int term = tb; term < te; ++term, ++g) {
+        const int buf = g & 1;
+        if (g >= 2 && !tc_mbar_wait(sfree + buf, (uint32_t)((g - 2) >> 1) & 1u)) ok = false;
+        const KbtTerm tt = (term - tb < KBT_MAXT_P) ? tab[term - tb] : kbt_term(op, p, term, KP, 0, nb);
+        const bool live = tt.ok && !tt.empty;
+        if (live)
+          kbt_stage_mf<KP>(tt, i0, nr, MFd0 + buf * Rg::MFD, MFs0 + buf * 8 * KB_WMAX, Cs0 + buf * 8 * KB_WMAX, lane);
+        __syncwarp();
+        if (lane == 0) {
+          if (live) {
+            tc_mbar_expect_tx(staged + buf, bbytes);
+            tc_bulk_load(Bs + buf * Rg::BBUF, p.tcb + __ldg(p.tcb_off + term), bbytes, staged + buf);
+          } else {
+            tc_mbar_arrive(staged + buf);
+          }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) tc_mbar_arrive(tfree + b);
+    }
   } else if (wid >= PW) {
     // ---- MMA issue: warp PW + j takes tile rows j, j + NMW, ... ------------------
     const int r0 = wid - PW;
     int ncommit = 0;
+    int g = 0;  // term counter (stage buffer g & 1)
     const uint64_t adesc0 = tc_desc(tc_smem_u32(As), 128u, 32u * KP);
     const uint64_t bdesc0 = tc_desc(tc_smem_u32(Bs), 128u, 32u * KP);
     for (int it = 0;; ++it) {
@@ -1025,16 +1024,16 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
         const int nk1 = __ldg(op.out_dk + s1);
         const int NP = nk1 <= 16 ? 16 : 32;
         const bool merged = 4 * R * NP <= DMAX;
-        const int bpart = merged ? NP * KP * 4 : Rg::BPART;
+        const int bpart = NP * KP * 4;  // the prebuilt blocks' part stride
         const uint32_t idesc = tc_idesc_tf32(128, NP), idesc2 = tc_idesc_tf32(128, 2 * NP);
         const int c0 = ncommit;
         uint32_t dinit = 0;
-        for (int term = tb; term < te; ++term) {
+        for (int term = tb; term < te; ++term, ++g) {
           const KbtTerm tt = (term - tb < KBT_MAXT_P) ? tab[term - tb] : kbt_term(op, p, term, KP, 0, nb);
           if (!tt.ok || tt.empty) continue;  // skipped by the producers as well
           if (!tc_mbar_wait(full, (uint32_t)ncommit & 1u)) ok = false;
           tc_fence_after();
-          const uint64_t bdesc = bdesc0 + (uint64_t)((((term - tb) & 1) * Rg::BBUF) >> 4);
+          const uint64_t bdesc = bdesc0 + (uint64_t)(((g & 1) * Rg::BBUF) >> 4);
           if constexpr (TA) {
             const uint32_t atm = tmem + TA_ACOL;
             if (merged) {
@@ -1043,7 +1042,7 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
               else if (tt.ktype == 2) kbt_issue_merged_ta<KP, 2>(tmem, atm, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart, r0, NMW);
               else kbt_issue_merged_ta<KP, 0>(tmem, atm, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart, r0, NMW);
             } else {
-              kbt_issue_ta<KP>(tmem, atm, bdesc, idesc, NP, nr, tt.ktype, tt.nk2, dinit, Rg::BPART, r0, NMW);
+              kbt_issue_ta<KP>(tmem, atm, bdesc, idesc, NP, nr, tt.ktype, tt.nk2, dinit, bpart, r0, NMW);
             }
           } else if (merged) {
             const uint32_t acc0 = ncommit > c0 ? 1u : 0u;
@@ -1051,13 +1050,14 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
             else if (tt.ktype == 2) kbt_issue_merged<KP, 2>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart, r0, NMW);
             else kbt_issue_merged<KP, 0>(tmem, adesc0, bdesc, idesc, idesc2, NP, nr, tt.nk2, acc0, bpart, r0, NMW);
           } else {
-            kbt_issue<KP>(tmem, adesc0, bdesc, idesc, NP, nr, tt.ktype, tt.nk2, dinit, Rg::BPART, r0, NMW);
+            kbt_issue<KP>(tmem, adesc0, bdesc, idesc, NP, nr, tt.ktype, tt.nk2, dinit, bpart, r0, NMW);
           }
           tc_commit(empty);  // arrives once this thread's MMAs (if any) are done
           ++ncommit;
         }
       }
       ncommit = __shfl_sync(0xffffffffu, ncommit, 0);
+      g = __shfl_sync(0xffffffffu, g, 0);
       __syncwarp();
       if (lane == 0) tc_mbar_arrive(tfree + b);
     }
@@ -1066,6 +1066,13 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
     int ncommit = 0;
     KbtRingPos rp{0, 0u};
     float2 z[R][BH];
+    int g = 0;     // term counter: stage buffer g & 1
+    int rel = -1;  // term whose stage buffer goes back once its MMAs are seen done
+    // gives the stage buffer of term gg back to the stager (one arrival per warp)
+    auto release = [&](int gg) {
+      __syncwarp();
+      if (lane == 0) tc_mbar_arrive(sfree + (gg & 1));
+    };
     for (int it = 0;; ++it) {
       const int b = it & 1;
       if (!tc_mbar_wait(tready + b, (uint32_t)(it >> 1) & 1u)) {
@@ -1088,7 +1095,6 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
       const float sc = p.yscale ? (float)p.yscale[(long long)kb_slot(p.kslot) * nb + v] : 1.f;
       const int NP = nk1 <= 16 ? 16 : 32;
       const bool merged = 4 * R * NP <= DMAX;
-      const int bpart = merged ? NP * KP * 4 : Rg::BPART;
       if (te == tb) {  // no term reaches this slab
         for (int e = wid >> 2; e < nr * nk1; e += L::NQ)
           Y[((long long)(e / nk1) * ld1 + e % nk1) * nb] = make_float2(0.f, 0.f);
@@ -1097,26 +1103,26 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
         continue;
       }
       const int c0 = ncommit;
+      // M step of the term in stage buffer g & 1, once the stager filled it
+      auto zstep = [&](const KbtTerm& t) {
+        const int sb = g & 1;
+        if (!tc_mbar_wait(staged + sb, (uint32_t)(g >> 1) & 1u)) ok = false;
+        if (!kbt_zstep_ring<KP, BH, L::NSLOT>(z, t, nb, nr, b0, vloc, lane, MFs0 + sb * 8 * KB_WMAX,
+                                              Cs0 + sb * 8 * KB_WMAX, MFd0 + sb * Rg::MFD, ring, rfull, rempty, rp))
+          ok = false;
+      };
       KbtTerm cur = term_at(0);
-      KbtPre pre;
-      // every producer is past the previous tile's use of the B / MF buffers
-      // (its epilogue waited for the last MMAs); the staging below reuses them
-      kbt_preload<KP, PT>(cur, nk1, NP, i0, nr, tid, pre);
-      kbt_producer_sync<PT>();
-      kbt_stage_pre<KP, PT>(cur, pre, NP, nr, reinterpret_cast<float*>(Bs), MFs0, Cs0, MFd0, tid, bpart);
-      kbt_producer_sync<PT>();
-      if (!kbt_zstep_ring<KP, BH, L::NSLOT>(z, cur, nb, nr, b0, vloc, lane, MFs0, Cs0, MFd0, ring, rfull, rempty, rp))
-        ok = false;
+      zstep(cur);
       for (int term = tb; term < te; ++term) {
-        const int buf = (term - tb) & 1;
         const bool has_next = term + 1 < te;
-        KbtTerm nxt;
-        if (has_next) {
-          nxt = term_at(term + 1 - tb);
-          kbt_preload<KP, PT>(nxt, nk1, NP, i0, nr, tid, pre);
-        }
+        // the MMAs of the last committed term are done: the A tiles are free,
+        // and that term's stage buffer goes back
         if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
         tc_fence_after();
+        if (rel >= 0) {
+          release(rel);
+          rel = -1;
+        }
         if (cur.ok && !cur.empty) {
           if constexpr (TA) {
             const uint32_t arow = tmem + TA_ACOL + ((uint32_t)(vq * 32) << 16);
@@ -1130,26 +1136,28 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
             for (int r = 0; r < R; ++r)
               if (r < nr) kbt_store_row<KP>(As + r * 4 * ATILE, z[r], vloc, b0);
           }
-          tc_fence_proxy();  // the B tiles staged by generic stores, and the A tiles
+          tc_fence_proxy();  // the A tiles (shared-memory form) to the async proxy
           __syncwarp();
           if (lane == 0) tc_mbar_arrive(full);
           ++ncommit;
-        } else if (!cur.ok && tid == 0) {
-          atomicExch(p.err, KR_ERR_ARG);  // outside the tile shape: skipped
+          rel = g;
+        } else {
+          if (!cur.ok && tid == 0) atomicExch(p.err, KR_ERR_ARG);  // outside the tile shape: skipped
+          release(g);  // no MMA reads this term's buffer
         }
         if (has_next) {
-          kbt_stage_pre<KP, PT>(nxt, pre, NP, nr, reinterpret_cast<float*>(Bs + (buf ^ 1) * Rg::BBUF),
-                            MFs0 + (buf ^ 1) * 8 * KB_WMAX, Cs0 + (buf ^ 1) * 8 * KB_WMAX,
-                            MFd0 + (buf ^ 1) * Rg::MFD, tid, bpart);
-          kbt_producer_sync<PT>();
-          if (!kbt_zstep_ring<KP, BH, L::NSLOT>(z, nxt, nb, nr, b0, vloc, lane, MFs0 + (buf ^ 1) * 8 * KB_WMAX,
-                                  Cs0 + (buf ^ 1) * 8 * KB_WMAX, MFd0 + (buf ^ 1) * Rg::MFD, ring, rfull, rempty, rp))
-            ok = false;
-          cur = nxt;
+          ++g;
+          cur = term_at(term + 1 - tb);
+          zstep(cur);
         }
       }
+      ++g;
       if (ncommit > 0 && !tc_mbar_wait(empty, (uint32_t)(ncommit - 1) & 1u)) ok = false;
       tc_fence_after();
+      if (rel >= 0) {
+        release(rel);
+        rel = -1;
+      }
       const bool any = ncommit > c0;
       for (int r = wid >> 2; r < nr; r += L::NQ) {
         for (int cc = 0; cc < NP; cc += 16) {
@@ -1207,6 +1215,55 @@ __global__ void __launch_bounds__(320, 1) kb_matvec_tc(BatchTC p, const __grid_c
   const int kp = __ldg(p.task + 3 * p.ntask + task);
   if (kp == 32) kbt_tile<32>(p, s1, i0, nr, kbt_smem);
   else if (threadIdx.x == 0) atomicExch(p.err, KR_ERR_ARG);  // KP = 8, 16 tiles go to kb_matvec_tcp
+}
+
+// ---------------------------------------------------------------------------
+// B operands of every term of the persistent tiles, built once per operator
+// (K does not change with the field): per term, the six parts K_re hi, lo,
+// K_im hi, lo, -K_im hi, lo (TF32 split of the FP32 copy of K), each NP x KP
+// in the K-major layout of the MMA, NP x KP x 4 bytes apart. A stager warp of
+// the persistent kernel copies a term's block into shared memory in one bulk
+// copy. prm: [6][nterm] int64 = K offset, K type, n_k1, n_k2, KP (0: none), B offset.
+// ---------------------------------------------------------------------------
+__global__ void kbt_build_b(const float* __restrict__ kf32, const long long* __restrict__ prm, int nterm,
+                            float* __restrict__ tcb) {
+  const int t = blockIdx.x;
+  const int KP = (int)prm[4 * nterm + t];
+  if (KP == 0) return;
+  const float* KT = kf32 + prm[t];
+  const int ktype = (int)prm[nterm + t], nk1 = (int)prm[2 * nterm + t], nk2 = (int)prm[3 * nterm + t];
+  const int NP = nk1 <= 16 ? 16 : 32;
+  const int part = NP * KP;
+  float* Bt = tcb + prm[5 * nterm + t];
+  for (int e = threadIdx.x; e < NP * KP; e += blockDim.x) {
+    const int a = e / KP, b = e - (e / KP) * KP;
+    float kr = 0.f, ki = 0.f;
+    if (a < nk1 && b < nk2) {
+      if (ktype == 0) {
+        kr = KT[((long long)b * nk1 + a) * 2];
+        ki = KT[((long long)b * nk1 + a) * 2 + 1];
+      } else if (ktype == 1) {
+        kr = KT[(long long)b * nk1 + a];
+      } else {
+        ki = KT[(long long)b * nk1 + a];
+      }
+    }
+    const uint32_t o = tc_kmajor_off(a, b, KP) >> 2;
+    const float krh = tc_tf32(kr), kih = tc_tf32(ki);
+    Bt[0 * part + o] = krh;
+    Bt[1 * part + o] = kr - krh;
+    Bt[2 * part + o] = kih;
+    Bt[3 * part + o] = ki - kih;
+    Bt[4 * part + o] = -kih;
+    Bt[5 * part + o] = -(ki - kih);
+  }
+}
+
+int kb_build_tc_b(kr_ctx* ctx, const float* kf32, const long long* prm, int nterm, float* tcb) {
+  if (nterm <= 0) return KR_OK;
+  kbt_build_b<<<nterm, 256>>>(kf32, prm, nterm, tcb);
+  KR_CUDA(ctx, cudaGetLastError());
+  return KR_OK;
 }
 
 // TMA descriptor of the basis slots behind X, [nslots][dim][nb] (complex64 as

@@ -60,6 +60,10 @@ int kr_set_err(kr_ctx* ctx, int code, const std::string& msg);
 // so that, with several host threads driving one GPU, none of the library's
 // own allocations or synchronisations runs in the middle of a recording.
 std::recursive_mutex& kr_device_mutex();
+
+// fills the B blocks of the persistent tensor-core tiles' terms (kr_batch_tc.cu);
+// prm: [6][nterm] int64 = K offset, K type, n_k1, n_k2, KP (0: no block), B offset
+int kb_build_tc_b(kr_ctx* ctx, const float* kf32, const long long* prm, int nterm, float* tcb);
 #define set_err kr_set_err
 
 #define KR_CUDA(ctx, call)                                                                 \
@@ -118,6 +122,9 @@ struct kr_op {
   int tc_ntask = 0;
   int* tc_task = nullptr;
   int tc_class[4] = {0, 0, 0, 0};  // first tile of KP = 8, 16, 32 in tc_task, and the end
+  // B operands of the terms of the KP = 8, 16 tiles (kb_build_tc_b) and each term's offset
+  float* tc_b = nullptr;
+  long long* tc_boff = nullptr;
   // tiles of the register-tiled FP32 batched mat-vec: [4][zr_ntask] = slab, first row, rows, NKP
   int zr_ntask = 0;
   int* zr_task = nullptr;

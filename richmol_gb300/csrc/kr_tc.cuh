@@ -175,6 +175,14 @@ __device__ __forceinline__ void tc_mbar_expect_tx(uint64_t* bar, uint32_t bytes)
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc_smem_u32(bar)), "r"(bytes)
                : "memory");
 }
+// untiled bulk copy of bytes (a multiple of 16; both addresses 16-byte
+// aligned) from global to shared memory, completion counted on bar in bytes
+__device__ __forceinline__ void tc_bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   tc_smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(tc_smem_u32(bar))
+               : "memory");
+}
 // 2-D TMA tile load (tensor map in kernel-parameter space): box at element
 // coordinates (x, y) into shared memory, completion counted on bar in bytes.
 // x times the element size must be a multiple of 16 bytes.
