@@ -357,6 +357,15 @@ __device__ __forceinline__ void df2_cfma(DF2& s, float2 mh, float2 ml, int mtype
   if (mtype != 2) df2_fma(s, make_float2(mh.x, mh.x), make_float2(ml.x, ml.x), b);
   if (mtype != 1) df2_fma(s, make_float2(-mh.y, mh.y), make_float2(-ml.y, ml.y), df2_swap(b));
 }
+// a + b of two double-float values (two-sum of the hi parts, lo parts added)
+__device__ __forceinline__ DF2 df2_add(const DF2& a, const DF2& b) {
+  const float2 t = f2_add(a.h, b.h);
+  const float2 bv = f2_sub(t, a.h);
+  const float2 err = f2_add(f2_sub(a.h, f2_sub(t, bv)), f2_sub(b.h, bv));
+  DF2 s{t, f2_add(f2_add(a.l, b.l), err)};
+  df2_norm(s);
+  return s;
+}
 __device__ __forceinline__ DF2 df2_split(double2 v) {
   const float2 h = make_float2((float)v.x, (float)v.y);
   return DF2{h, make_float2((float)(v.x - (double)h.x), (float)(v.y - (double)h.y))};
@@ -381,6 +390,7 @@ __device__ void matvec_cta_tasks_df(const DevOp& op, const double2* __restrict__
   __shared__ int s_task;
   const int tid = threadIdx.x;
   float4* zb[2] = {reinterpret_cast<float4*>(smem), reinterpret_cast<float4*>(smem) + op.zmax};
+  const float xsh = (float)xscale, xsl = (float)(xscale - (double)xsh);  // xscale as a double-float
   for (;;) {
     if (tid == 0) s_task = (int)atomicAdd(counter, 1u);
     __syncthreads();
@@ -419,8 +429,11 @@ __device__ void matvec_cta_tasks_df(const DevOp& op, const double2* __restrict__
         for (int w = 0; w < W; ++w)
           df2_cfma(z, __ldcg(mfh + base + w), __ldcg(mfl + base + w), mtype,
                    df2_ld(X + (long long)__ldg(col + base + w) * nk2 + b));
-        const double2 zd = df2_value(z);
-        df2_st(Z + p, df2_split(make_double2(zd.x * xscale, zd.y * xscale)));
+        df2_norm(z);
+        DF2 zs{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};  // z * xscale, on the FP32 pipes
+        df2_fma(zs, make_float2(xsh, xsh), make_float2(xsl, xsl), z);
+        df2_norm(zs);
+        df2_st(Z + p, zs);
       }
       const long long ko = __ldg(op.k_off + kbk);
       const int ktype = __ldg(op.k_type + kbk);
@@ -432,28 +445,43 @@ __device__ void matvec_cta_tasks_df(const DevOp& op, const double2* __restrict__
           const int r = p / nk1;
           const int a = p - r * nk1;
           const float4* zr = Z + r * nk2;
-          DF2 s = acc[q];
+          // two partial sums (even and odd b): independent chains
+          DF2 s0 = acc[q], s1{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
           if (ktype == 1 || ktype == 2) {  // real K, or K = i Ki
             const float* KH = op.k_f32 + ko;
             const float* KL = op.k_lo + ko;
-            for (int b = 0; b < nk2; ++b) {
-              const float kh = __ldg(KH + b * nk1 + a), kl = __ldg(KL + b * nk1 + a);
-              const float4 zv = zr[b];
-              const DF2 z{make_float2(zv.x, zv.y), make_float2(zv.z, zv.w)};
-              if (ktype == 1) df2_fma(s, make_float2(kh, kh), make_float2(kl, kl), z);
-              else df2_fma(s, make_float2(-kh, kh), make_float2(-kl, kl), df2_swap(z));
+            const float sg = ktype == 1 ? 1.f : -1.f;
+            int b = 0;
+            for (; b + 1 < nk2; b += 2) {
+              const float kh0 = __ldg(KH + b * nk1 + a), kl0 = __ldg(KL + b * nk1 + a);
+              const float kh1 = __ldg(KH + (b + 1) * nk1 + a), kl1 = __ldg(KL + (b + 1) * nk1 + a);
+              const float4 z0 = zr[b], z1 = zr[b + 1];
+              DF2 x0{make_float2(z0.x, z0.y), make_float2(z0.z, z0.w)};
+              DF2 x1{make_float2(z1.x, z1.y), make_float2(z1.z, z1.w)};
+              if (ktype == 2) {
+                x0 = df2_swap(x0);
+                x1 = df2_swap(x1);
+              }
+              df2_fma(s0, make_float2(sg * kh0, kh0), make_float2(sg * kl0, kl0), x0);
+              df2_fma(s1, make_float2(sg * kh1, kh1), make_float2(sg * kl1, kl1), x1);
+            }
+            if (b < nk2) {
+              const float kh0 = __ldg(KH + b * nk1 + a), kl0 = __ldg(KL + b * nk1 + a);
+              const float4 z0 = zr[b];
+              DF2 x0{make_float2(z0.x, z0.y), make_float2(z0.z, z0.w)};
+              if (ktype == 2) x0 = df2_swap(x0);
+              df2_fma(s0, make_float2(sg * kh0, kh0), make_float2(sg * kl0, kl0), x0);
             }
           } else {  // complex K, interleaved (re, im)
             const float2* KH = reinterpret_cast<const float2*>(op.k_f32 + ko);
             const float2* KL = reinterpret_cast<const float2*>(op.k_lo + ko);
             for (int b = 0; b < nk2; ++b) {
               const float4 zv = zr[b];
-              df2_cfma(s, __ldg(KH + b * nk1 + a), __ldg(KL + b * nk1 + a), 0,
+              df2_cfma((b & 1) ? s1 : s0, __ldg(KH + b * nk1 + a), __ldg(KL + b * nk1 + a), 0,
                        DF2{make_float2(zv.x, zv.y), make_float2(zv.z, zv.w)});
             }
           }
-          df2_norm(s);
-          acc[q] = s;
+          acc[q] = df2_add(s0, s1);
         }
       }
     }

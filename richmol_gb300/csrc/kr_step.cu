@@ -1203,6 +1203,7 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   // per output slab: KP = largest input n_k of its terms padded to 8 (the MMA K),
   // R = 64 / KP rows per tile; heaviest slabs first
   std::vector<int> tc_task;
+  std::vector<int> slab_kp(d->nslab_out, 0);  // KP of each output slab's tiles
   {
     std::vector<int> ts, ti, tn, tk;
     std::vector<double> tcost;
@@ -1218,6 +1219,7 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
       // (KP >= 16), so that its accumulators (2 R NP TMEM columns, NP = 32)
       // leave half of the tensor memory to the A tiles of the TMEM form
       const int kp = (maxnk2 <= 8 && d->out_dk[s] <= 16) ? 8 : maxnk2 <= 16 ? 16 : 32;
+      slab_kp[s] = kp;
       const int R = 64 / kp, dm1 = d->out_dm[s];
       for (int i0 = 0; i0 < dm1; i0 += R) {
         ts.push_back(s);
@@ -1383,6 +1385,38 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   if (op->tc_ntask > 0) {
     UP(tc_task.data(), tc_task.size(), &p_i);
     op->tc_task = p_i;
+    // B blocks of the terms of the KP = 8, 16 tiles, 6 NP KP floats each
+    const int nterm = (int)t_in.size();
+    std::vector<long long> prm((size_t)6 * std::max(1, nterm), 0), boff(std::max(1, nterm), 0);
+    long long tot = 0;
+    for (int s = 0; s < d->nslab_out; ++s) {
+      const int kp = slab_kp[s];
+      if (kp != 8 && kp != 16) continue;
+      const int np = d->out_dk[s] <= 16 ? 16 : 32;
+      for (size_t k = 0; k < by_out[s].size(); ++k) {
+        const int t = by_out[s][k], j = term_ptr[s] + (int)k;  // original and device term index
+        const int kb = d->t_k[t];
+        prm[j] = d->k_off[kb];
+        prm[nterm + j] = d->k_type[kb];
+        prm[2 * nterm + j] = d->out_dk[s];
+        prm[3 * nterm + j] = d->in_dk[d->t_in[t]];
+        prm[4 * nterm + j] = kp;
+        prm[5 * nterm + j] = tot;
+        boff[j] = tot;
+        tot += 6LL * np * kp;
+      }
+    }
+    if (tot > 0) {
+      long long* p_prm;
+      float* p_b;
+      UP(prm.data(), prm.size(), &p_prm);
+      UP(boff.data(), boff.size(), &p_l); op->tc_boff = p_l;
+      UP((const float*)nullptr, (size_t)tot, &p_b); op->tc_b = p_b;
+      if ((rc = kb_build_tc_b(ctx, D.k_f32, p_prm, nterm, op->tc_b)) != KR_OK) {
+        kr_op_destroy(op);
+        return rc;
+      }
+    }
   }
   if (op->zr_ntask > 0) {
     UP(zr_task.data(), zr_task.size(), &p_i);
