@@ -304,8 +304,8 @@ def run_ours(args, ws, rank, local):
     mv_flops = 2.0 * fma_mv * nvec
     mv_bytes = 8.0 * 2 * dim * nvec  # complex64 X in + Y out (factors are shared by all vectors)
     # ncu DRAM bytes of one launch at 4096 vectors (profiles/traffic.json), in proportion to the vectors
-    tkey = {"fp32": "kb_matvec_per_launch_bytes_4096", "fp32_reg": "kb_matvec_zr_per_launch_bytes_4096"}.get(
-        kind, "kb_matvec_tc_per_launch_bytes_4096")
+    tkey = {"fp32": "kb_matvec_per_launch_bytes_4096", "fp32_reg": "kb_matvec_zr_per_launch_bytes_4096",
+            "tensor_tmem": "kb_matvec_tcp_tmem_per_launch_bytes_4096"}.get(kind, "kb_matvec_tc_per_launch_bytes_4096")
     t4096 = load_traffic().get(tkey)
     traffic = None if t4096 is None else int(round(t4096 * nvec / 4096))
     gbs = mv_bytes / mv_s / 1e9

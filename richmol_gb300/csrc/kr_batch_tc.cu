@@ -501,9 +501,10 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
 
 // ---------------------------------------------------------------------------
 // X windows streamed by TMA (KP = 8, 16): the loader warp walks the window
-// rows of every diagonal term in order and loads each (KP input rows x 128
-// vectors, KP/8 boxes of 8 rows) into a ring of shared-memory slots (full: tx
-// bytes; empty: one arrival per producer warp); the producer warps read X from
+// rows of every diagonal term in order and loads them two by two (each KP input
+// columns x 128 vectors, KP/8 boxes of 8 columns) into a ring of shared-memory
+// slots (full: tx bytes; empty: one arrival per producer warp; an odd window's
+// last slot also carries the row after it); the producer warps read X from
 // the ring, so no global-load latency sits in their M step. Rows outside the
 // input slab read whatever lies there (finite data of other slabs, or zeros
 // beyond the array) and meet zero MF slots. Terms stored as ELL load X
@@ -512,10 +513,12 @@ __device__ void kbt_tile(const BatchTC& p, int s1, int i0, int nr, char* smem) {
 
 template <int KP, bool TA = false>
 struct KbtRing {
-  // slots of KP rows x 128 vectors x 8 bytes: with the A tiles in TMEM (TA) the
-  // shared memory they took holds a ring about three times as deep
-  static constexpr int NSLOT = TA ? (KP == 16 ? 11 : 22) : 64 / KP;
-  static constexpr int SLOT = KP * 1024;
+  // slots of two window rows of KP columns x 128 vectors x 8 bytes: with the A
+  // tiles in TMEM (TA) the shared memory they took holds a ring about three
+  // times as deep
+  static constexpr int NSLOT = TA ? (KP == 16 ? 5 : 11) : 32 / KP;
+  static constexpr int ROW = KP * 1024;  // bytes of one window row in a slot
+  static constexpr int SLOT = 2 * ROW;
   static constexpr int BPART = 128 * KP;         // one B part: NP (<= 32) x KP FP32
   static constexpr int BBUF = 6 * BPART;
   static constexpr int OFF_B = TA ? 0 : TC_ABYTES;
@@ -584,15 +587,18 @@ __device__ __forceinline__ void kbt_ring_next(KbtRingPos& rp) {
   }
 }
 
-// takes the next ring row: waits until it has landed, reads this thread's
-// vector and KP/2 columns, and gives the slot back (one arrival per warp)
+// takes the next ring slot: waits until it has landed, reads this thread's
+// vector and BQ columns of its two rows (x[0], x[1]), and gives the slot back
+// (one arrival per warp)
 template <int KP, int BQ, int NSLOT>
-__device__ __forceinline__ bool kbt_ring_take(float2 (&x)[BQ], const char* ring, uint64_t* rfull,
+__device__ __forceinline__ bool kbt_ring_take(float2 (&x)[2][BQ], const char* ring, uint64_t* rfull,
                                               uint64_t* rempty, KbtRingPos& rp, int b0, int vloc, int lane) {
   const bool ok = tc_mbar_wait(rfull + rp.slot, rp.phase);
   const float2* xs = reinterpret_cast<const float2*>(ring + (size_t)rp.slot * KbtRing<KP>::SLOT) + vloc;
 #pragma unroll
-  for (int q = 0; q < BQ; ++q) x[q] = xs[(b0 + q) * 128];
+  for (int h = 0; h < 2; ++h)
+#pragma unroll
+    for (int q = 0; q < BQ; ++q) x[h][q] = xs[h * (KbtRing<KP>::ROW / 8) + (b0 + q) * 128];
   __syncwarp();
   if (lane == 0) tc_mbar_arrive(rempty + rp.slot);
   kbt_ring_next<NSLOT>(rp);
@@ -611,19 +617,24 @@ __device__ __forceinline__ bool kbt_mdia_ring(float2 (&z)[64 / KP][BH], const ch
   constexpr int R = 64 / KP;
   constexpr int G = R >= 8 ? 2 : 1;
   bool ok = true;
-  for (int c = 0; c < nwin; ++c) {
-    float2 x[BH];
+  for (int c = 0; c < nwin; c += 2) {
+    float2 x[2][BH];
     if (!kbt_ring_take<KP, BH, NSLOT>(x, ring, rfull, rempty, rp, b0, vloc, lane)) ok = false;
-    const float4* mrow = MFd + c * R;
 #pragma unroll
-    for (int gr = 0; gr < R / G; ++gr) {
-      if (c >= gr * G && c < gr * G + G - 1 + W && gr * G < nr) {
+    for (int h = 0; h < 2; ++h) {
+      const int cc = c + h;
+      if (cc >= nwin) break;  // an odd window's last slot: its second row is not used
+      const float4* mrow = MFd + cc * R;
 #pragma unroll
-        for (int rr = 0; rr < G; ++rr) {
-          const int r = gr * G + rr;
-          const float4 m = mrow[r];
+      for (int gr = 0; gr < R / G; ++gr) {
+        if (cc >= gr * G && cc < gr * G + G - 1 + W && gr * G < nr) {
 #pragma unroll
-          for (int q = 0; q < BH; ++q) macc2<MT>(z[r][q], m, x[q]);
+          for (int rr = 0; rr < G; ++rr) {
+            const int r = gr * G + rr;
+            const float4 m = mrow[r];
+#pragma unroll
+            for (int q = 0; q < BH; ++q) macc2<MT>(z[r][q], m, x[h][q]);
+          }
         }
       }
     }
@@ -632,8 +643,9 @@ __device__ __forceinline__ bool kbt_mdia_ring(float2 (&z)[64 / KP][BH], const ch
 }
 
 // the same for a band of WT slots (1, 3, 5), unrolled over the window: the
-// band tests fold at compile time. Rows from nwin on (tiles of fewer than R
-// rows) are neither taken nor used: they feed only tile rows at or beyond nr.
+// band tests fold at compile time. Slots from row nwin on (tiles of fewer than
+// R rows) are not taken; a slot's second row at or beyond nwin (an odd
+// window) feeds only tile rows at or beyond nr, whose Z is never stored.
 template <int KP, int BH, int MT, int WT, int NSLOT>
 __device__ __forceinline__ bool kbt_mdia_ring_u(float2 (&z)[64 / KP][BH], const char* ring, uint64_t* rfull,
                                                 uint64_t* rempty, KbtRingPos& rp, int nwin, int b0, int vloc,
@@ -641,17 +653,22 @@ __device__ __forceinline__ bool kbt_mdia_ring_u(float2 (&z)[64 / KP][BH], const 
   constexpr int R = 64 / KP, NW = R + WT - 1;
   bool ok = true;
 #pragma unroll
-  for (int c = 0; c < NW; ++c) {
+  for (int c = 0; c < NW; c += 2) {
     if (c < nwin) {
-      float2 x[BH];
+      float2 x[2][BH];
       if (!kbt_ring_take<KP, BH, NSLOT>(x, ring, rfull, rempty, rp, b0, vloc, lane)) ok = false;
-      const float4* mrow = MFd + c * R;
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        if (r < c - WT + 1 || r > c) continue;
-        const float4 m = mrow[r];
+      for (int h = 0; h < 2; ++h) {
+        const int cc = c + h;  // a row at or beyond nwin feeds only tile rows at or beyond nr
+        if (cc >= NW) continue;
+        const float4* mrow = MFd + cc * R;
 #pragma unroll
-        for (int q = 0; q < BH; ++q) macc2<MT>(z[r][q], m, x[q]);
+        for (int r = 0; r < R; ++r) {
+          if (r < cc - WT + 1 || r > cc) continue;
+          const float4 m = mrow[r];
+#pragma unroll
+          for (int q = 0; q < BH; ++q) macc2<MT>(z[r][q], m, x[h][q]);
+        }
       }
     }
   }
@@ -953,15 +970,20 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
           const KbtTerm t = (term - tb < KBT_MAXT_P) ? tab[term - tb] : kbt_term(op, p, term, KP, 0, nb);
           const int nwin = kbt_ring_rows(t, nr);
           const long long row0 = __ldg(op.in_off + t.s2);
-          for (int c = 0; c < nwin; ++c, ++g) {
+          for (int c = 0; c < nwin; c += 2, ++g) {  // two window rows per slot
             const int slot = g % NSLOT;
             if (g >= NSLOT && !tc_mbar_wait(rempty + slot, (uint32_t)(g / NSLOT - 1) & 1u)) ok = false;
+            // both rows of the slot, also past an odd window's end (a row
+            // outside the slot's basis array reads as zeros; the producers'
+            // FMAs on such a row reach no stored Z)
             tc_mbar_expect_tx(rfull + slot, (uint32_t)Rg::SLOT);
-            const long long y = row0 + (long long)(i0 + t.d0 + c) * t.ld2;
-            char* dst = ring + (size_t)slot * Rg::SLOT;
+            for (int rr = 0; rr < 2; ++rr) {
+              const long long y = row0 + (long long)(i0 + t.d0 + c + rr) * t.ld2;
+              char* dst = ring + (size_t)slot * Rg::SLOT + rr * Rg::ROW;
 #pragma unroll
-            for (int h = 0; h < KP / 8; ++h)
-              tc_tma_load_3d(dst + h * 8192, xmap, vb * 128, (int)(y + 8 * h), zslot, rfull + slot);
+              for (int h = 0; h < KP / 8; ++h)
+                tc_tma_load_3d(dst + h * 8192, xmap, vb * 128, (int)(y + 8 * h), zslot, rfull + slot);
+            }
           }
         }
       }
