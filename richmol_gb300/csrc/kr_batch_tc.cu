@@ -516,9 +516,10 @@ struct KbtRing {
   // slots of two window rows of KP columns x 128 vectors x 8 bytes: with the A
   // tiles in TMEM (TA) the shared memory they took holds a ring about three
   // times as deep
+  static constexpr int RS = 2;  // window rows per slot (4 with A in TMEM measured slower)
   static constexpr int NSLOT = TA ? (KP == 16 ? 5 : 11) : 32 / KP;
   static constexpr int ROW = KP * 1024;  // bytes of one window row in a slot
-  static constexpr int SLOT = 2 * ROW;
+  static constexpr int SLOT = RS * ROW;
   static constexpr int BPART = 128 * KP;         // one B part: NP (<= 32) x KP FP32
   static constexpr int BBUF = 6 * BPART;
   static constexpr int OFF_B = TA ? 0 : TC_ABYTES;
@@ -590,15 +591,15 @@ __device__ __forceinline__ void kbt_ring_next(KbtRingPos& rp) {
 // takes the next ring slot: waits until it has landed, reads this thread's
 // vector and BQ columns of its two rows (x[0], x[1]), and gives the slot back
 // (one arrival per warp)
-template <int KP, int BQ, int NSLOT>
-__device__ __forceinline__ bool kbt_ring_take(float2 (&x)[2][BQ], const char* ring, uint64_t* rfull,
+template <int KP, int BQ, int RS, int NSLOT>
+__device__ __forceinline__ bool kbt_ring_take(float2 (&x)[RS][BQ], const char* ring, uint64_t* rfull,
                                               uint64_t* rempty, KbtRingPos& rp, int b0, int vloc, int lane) {
   const bool ok = tc_mbar_wait(rfull + rp.slot, rp.phase);
-  const float2* xs = reinterpret_cast<const float2*>(ring + (size_t)rp.slot * KbtRing<KP>::SLOT) + vloc;
+  const float2* xs = reinterpret_cast<const float2*>(ring + (size_t)rp.slot * RS * KP * 1024) + vloc;
 #pragma unroll
-  for (int h = 0; h < 2; ++h)
+  for (int h = 0; h < RS; ++h)
 #pragma unroll
-    for (int q = 0; q < BQ; ++q) x[h][q] = xs[h * (KbtRing<KP>::ROW / 8) + (b0 + q) * 128];
+    for (int q = 0; q < BQ; ++q) x[h][q] = xs[h * KP * 128 + (b0 + q) * 128];
   __syncwarp();
   if (lane == 0) tc_mbar_arrive(rempty + rp.slot);
   kbt_ring_next<NSLOT>(rp);
@@ -610,18 +611,18 @@ __device__ __forceinline__ bool kbt_ring_take(float2 (&x)[2][BQ], const char* ri
 // rows go in groups of G, a group skipped (warp-uniform) when the band misses
 // it. Input columns at or beyond n_k2 hold finite data of the neighbouring rows
 // and meet zero rows of K^T in the MMA.
-template <int KP, int BH, int MT, int NSLOT>
+template <int KP, int BH, int MT, int RS, int NSLOT>
 __device__ __forceinline__ bool kbt_mdia_ring(float2 (&z)[64 / KP][BH], const char* ring, uint64_t* rfull,
                                               uint64_t* rempty, KbtRingPos& rp, int nwin, int nr, int W, int b0,
                                               int vloc, int lane, const float4* MFd) {
   constexpr int R = 64 / KP;
   constexpr int G = R >= 8 ? 2 : 1;
   bool ok = true;
-  for (int c = 0; c < nwin; c += 2) {
-    float2 x[2][BH];
-    if (!kbt_ring_take<KP, BH, NSLOT>(x, ring, rfull, rempty, rp, b0, vloc, lane)) ok = false;
+  for (int c = 0; c < nwin; c += RS) {
+    float2 x[RS][BH];
+    if (!kbt_ring_take<KP, BH, RS, NSLOT>(x, ring, rfull, rempty, rp, b0, vloc, lane)) ok = false;
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < RS; ++h) {
       const int cc = c + h;
       if (cc >= nwin) break;  // an odd window's last slot: its second row is not used
       const float4* mrow = MFd + cc * R;
@@ -646,19 +647,19 @@ __device__ __forceinline__ bool kbt_mdia_ring(float2 (&z)[64 / KP][BH], const ch
 // band tests fold at compile time. Slots from row nwin on (tiles of fewer than
 // R rows) are not taken; a slot's second row at or beyond nwin (an odd
 // window) feeds only tile rows at or beyond nr, whose Z is never stored.
-template <int KP, int BH, int MT, int WT, int NSLOT>
+template <int KP, int BH, int MT, int WT, int RS, int NSLOT>
 __device__ __forceinline__ bool kbt_mdia_ring_u(float2 (&z)[64 / KP][BH], const char* ring, uint64_t* rfull,
                                                 uint64_t* rempty, KbtRingPos& rp, int nwin, int b0, int vloc,
                                                 int lane, const float4* MFd) {
   constexpr int R = 64 / KP, NW = R + WT - 1;
   bool ok = true;
 #pragma unroll
-  for (int c = 0; c < NW; c += 2) {
+  for (int c = 0; c < NW; c += RS) {
     if (c < nwin) {
-      float2 x[2][BH];
-      if (!kbt_ring_take<KP, BH, NSLOT>(x, ring, rfull, rempty, rp, b0, vloc, lane)) ok = false;
+      float2 x[RS][BH];
+      if (!kbt_ring_take<KP, BH, RS, NSLOT>(x, ring, rfull, rempty, rp, b0, vloc, lane)) ok = false;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
+      for (int h = 0; h < RS; ++h) {
         const int cc = c + h;  // a row at or beyond nwin feeds only tile rows at or beyond nr
         if (cc >= NW) continue;
         const float4* mrow = MFd + cc * R;
@@ -675,17 +676,17 @@ __device__ __forceinline__ bool kbt_mdia_ring_u(float2 (&z)[64 / KP][BH], const 
   return ok;
 }
 
-template <int KP, int BH, int MT, int NSLOT>
+template <int KP, int BH, int MT, int RS, int NSLOT>
 __device__ __forceinline__ bool kbt_mdia_ring_w(float2 (&z)[64 / KP][BH], const char* ring, uint64_t* rfull,
                                                 uint64_t* rempty, KbtRingPos& rp, int nwin, int nr, int W, int b0,
                                                 int vloc, int lane, const float4* MFd) {
-  if (W == 5) return kbt_mdia_ring_u<KP, BH, MT, 5, NSLOT>(z, ring, rfull, rempty, rp, nwin, b0, vloc, lane, MFd);
-  if (W == 3) return kbt_mdia_ring_u<KP, BH, MT, 3, NSLOT>(z, ring, rfull, rempty, rp, nwin, b0, vloc, lane, MFd);
-  if (W == 1) return kbt_mdia_ring_u<KP, BH, MT, 1, NSLOT>(z, ring, rfull, rempty, rp, nwin, b0, vloc, lane, MFd);
-  return kbt_mdia_ring<KP, BH, MT, NSLOT>(z, ring, rfull, rempty, rp, nwin, nr, W, b0, vloc, lane, MFd);
+  if (W == 5) return kbt_mdia_ring_u<KP, BH, MT, 5, RS, NSLOT>(z, ring, rfull, rempty, rp, nwin, b0, vloc, lane, MFd);
+  if (W == 3) return kbt_mdia_ring_u<KP, BH, MT, 3, RS, NSLOT>(z, ring, rfull, rempty, rp, nwin, b0, vloc, lane, MFd);
+  if (W == 1) return kbt_mdia_ring_u<KP, BH, MT, 1, RS, NSLOT>(z, ring, rfull, rempty, rp, nwin, b0, vloc, lane, MFd);
+  return kbt_mdia_ring<KP, BH, MT, RS, NSLOT>(z, ring, rfull, rempty, rp, nwin, nr, W, b0, vloc, lane, MFd);
 }
 
-template <int KP, int BH, int NSLOT>
+template <int KP, int BH, int RS, int NSLOT>
 __device__ __forceinline__ bool kbt_zstep_ring(float2 (&z)[64 / KP][BH], const KbtTerm& t, long long nb, int nr,
                                                int b0, int vloc, int lane, const float2* MFs, const int* Cs,
                                                const float4* MFd, const char* ring, uint64_t* rfull,
@@ -698,9 +699,9 @@ __device__ __forceinline__ bool kbt_zstep_ring(float2 (&z)[64 / KP][BH], const K
   if (!t.ok || t.empty) return true;
   const int nwin = kbt_ring_rows(t, nr);
   if (t.dia) {
-    if (t.mtype == 1) return kbt_mdia_ring_w<KP, BH, 1, NSLOT>(z, ring, rfull, rempty, rp, nwin, nr, t.W, b0, vloc, lane, MFd);
-    if (t.mtype == 2) return kbt_mdia_ring_w<KP, BH, 2, NSLOT>(z, ring, rfull, rempty, rp, nwin, nr, t.W, b0, vloc, lane, MFd);
-    return kbt_mdia_ring_w<KP, BH, 0, NSLOT>(z, ring, rfull, rempty, rp, nwin, nr, t.W, b0, vloc, lane, MFd);
+    if (t.mtype == 1) return kbt_mdia_ring_w<KP, BH, 1, RS, NSLOT>(z, ring, rfull, rempty, rp, nwin, nr, t.W, b0, vloc, lane, MFd);
+    if (t.mtype == 2) return kbt_mdia_ring_w<KP, BH, 2, RS, NSLOT>(z, ring, rfull, rempty, rp, nwin, nr, t.W, b0, vloc, lane, MFd);
+    return kbt_mdia_ring_w<KP, BH, 0, RS, NSLOT>(z, ring, rfull, rempty, rp, nwin, nr, t.W, b0, vloc, lane, MFd);
   }
   if (t.mtype == 1) kbt_mell<KP, 1, BH>(z, t.Xs2, nb, t.nk2, t.ld2, nr, t.W, b0, MFs, Cs);
   else if (t.mtype == 2) kbt_mell<KP, 2, BH>(z, t.Xs2, nb, t.nk2, t.ld2, nr, t.W, b0, MFs, Cs);
@@ -970,14 +971,14 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
           const KbtTerm t = (term - tb < KBT_MAXT_P) ? tab[term - tb] : kbt_term(op, p, term, KP, 0, nb);
           const int nwin = kbt_ring_rows(t, nr);
           const long long row0 = __ldg(op.in_off + t.s2);
-          for (int c = 0; c < nwin; c += 2, ++g) {  // two window rows per slot
+          for (int c = 0; c < nwin; c += Rg::RS, ++g) {  // RS window rows per slot
             const int slot = g % NSLOT;
             if (g >= NSLOT && !tc_mbar_wait(rempty + slot, (uint32_t)(g / NSLOT - 1) & 1u)) ok = false;
             // both rows of the slot, also past an odd window's end (a row
             // outside the slot's basis array reads as zeros; the producers'
             // FMAs on such a row reach no stored Z)
             tc_mbar_expect_tx(rfull + slot, (uint32_t)Rg::SLOT);
-            for (int rr = 0; rr < 2; ++rr) {
+            for (int rr = 0; rr < Rg::RS; ++rr) {
               const long long y = row0 + (long long)(i0 + t.d0 + c + rr) * t.ld2;
               char* dst = ring + (size_t)slot * Rg::SLOT + rr * Rg::ROW;
 #pragma unroll
@@ -1129,7 +1130,7 @@ __device__ void kbt_persist(const BatchTC& p, const CUtensorMap* xmap, char* sme
       auto zstep = [&](const KbtTerm& t) {
         const int sb = g & 1;
         if (!tc_mbar_wait(staged + sb, (uint32_t)(g >> 1) & 1u)) ok = false;
-        if (!kbt_zstep_ring<KP, BH, L::NSLOT>(z, t, nb, nr, b0, vloc, lane, MFs0 + sb * 8 * KB_WMAX,
+        if (!kbt_zstep_ring<KP, BH, Rg::RS, L::NSLOT>(z, t, nb, nr, b0, vloc, lane, MFs0 + sb * 8 * KB_WMAX,
                                               Cs0 + sb * 8 * KB_WMAX, MFd0 + sb * Rg::MFD, ring, rfull, rempty, rp))
           ok = false;
       };

@@ -34,7 +34,8 @@ def _call(entry, plan, v, phase, fac, korder):
     _native.check(rc, plan.ctx)
 
 
-def test_static_scratch_step_matches_kr_step_twice():
+@pytest.mark.parametrize("products", ["f64", "df"])
+def test_static_scratch_step_matches_kr_step_twice(products):
     from richmol_gb300 import CarTens, TDSE, _native
     if not os.path.exists(_native.LIB_PATH):
         _native.build_library()
@@ -55,16 +56,33 @@ def test_static_scratch_step_matches_kr_step_twice():
     for i in range(2):  # two calls in a row: the array keeps the previous call's contents
         Hac.field(d["split/fields"][i])
         plan = (Hdc + Hac).device_operator()
+        plan.set_precision(products)  # the static step has the double-float copy of x in its array too
         ka = np.zeros(a.shape[0], np.int32)
         kb = np.zeros(b.shape[0], np.int32)
         _call(L.kr_step, plan, a, phase, td.exp_fac, ka)
         _call(L.kr_step_static, plan, b, phase, td.exp_fac, kb)
         torch.cuda.synchronize()
         assert np.array_equal(ka, kb)
-        assert _rel(b.cpu().numpy(), a.cpu().numpy()) < STATE_RTOL
+        assert np.array_equal(b.cpu().numpy(), a.cpu().numpy())  # the same kernel, bit for bit
     # and it follows the reference's own propagation
     ref = d["split/states_first2"][1]
     assert _rel(b.cpu().numpy()[:2], ref) < STATE_RTOL
+    plan.set_precision("f64")
+
+
+def test_product_precision_argument_checked():
+    from richmol_gb300 import CarTens, _native
+    from oracle import fixtures
+    path = os.path.join(GOLDEN, "asym_j4.npz")
+    d, meta = fixtures.load(path)
+    Hac = CarTens(path, name="pol") * meta["scales"]["ac"]
+    Hac.field(d["split/fields"][0])
+    plan = Hac.device_operator()
+    with pytest.raises(ValueError):
+        plan.set_precision("f32")
+    assert _native.lib().kr_op_set_precision(plan.op, 7) == _native.KR_ERR_ARG
+    plan.set_precision("df")
+    plan.set_precision("f64")
 
 
 def test_static_scratch_rejects_oversized_operator():
