@@ -305,6 +305,12 @@ int kr_batch_korder(kr_batch* b, int32_t* korder, void* stream);
  * with its field set (e.g. cos^2 theta with field [0, 0, 1]); complex64
  * mat-vec, FP64 dot products. Synchronises. */
 int kr_batch_expect(kr_batch* b, kr_op* obs, double* out, void* stream);
+/* sum_v w_v Re <v|O|v> into one device double (out), weights: device
+ * double[nvec] or NULL (all 1); stream-ordered, no synchronisation, so a time
+ * loop can keep an observable's trace on the device and read it once. A
+ * mat-vec error of the observable is kept as the batch's step error (reported
+ * by kr_batch_sync). No counterpart in the reference. */
+int kr_batch_expect_dev(kr_batch* b, kr_op* obs, const double* weights, double* out, void* stream);
 /* Populations of every slab (the (J, sym) blocks of the flat vector order) for
  * every vector: out[slab * nvec + v] = sum over the slab of |S_v|^2 (host array,
  * nslab x nvec doubles); summed over the symmetries of a J they are the

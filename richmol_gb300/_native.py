@@ -44,7 +44,7 @@ EXPORTED = [
     "kr_batch_populations",
     "kr_expv", "kr_op_norm1", "kr_observables",
     "kr_seg_create", "kr_seg_destroy", "kr_seg_step", "kr_seg_launch_count", "kr_seg_set_precision",
-    "kr_op_set_precision",
+    "kr_op_set_precision", "kr_batch_expect_dev",
 ]
 
 
@@ -169,6 +169,8 @@ def lib():
         L.kr_batch_korder.restype = ctypes.c_int
         L.kr_batch_expect.argtypes = [vp, vp, vp, vp]
         L.kr_batch_expect.restype = ctypes.c_int
+        L.kr_batch_expect_dev.argtypes = [vp, vp, vp, vp, vp]
+        L.kr_batch_expect_dev.restype = ctypes.c_int
         L.kr_batch_populations.argtypes = [vp, vp, vp]
         L.kr_batch_populations.restype = ctypes.c_int
         L.kr_batch_set_matvec.argtypes = [vp, i32]

@@ -172,6 +172,22 @@ class Ensemble:
         _native.check(_native.lib().kr_batch_expect(self.handle, plan.op, out.ctypes.data, stream_ptr()), self.ctx)
         return out.view(np.complex128)
 
+    def expect_into(self, O, out, weights=None):
+        """sum_v w_v Re <v|O|v> into ``out`` (a float64 CUDA tensor of one element,
+        e.g. one entry of a trace), ordered on the current stream without a host
+        synchronisation (kr_batch_expect_dev); ``weights`` a float64 CUDA tensor of
+        nvec weights, or None for all 1. O as in ``expect``."""
+        if not O._is_sum and O._parts[0].prods is None:
+            O.field([0, 0, 1])
+        plan = O.device_operator(split=self.split)
+        assert out.is_cuda and out.dtype == torch.float64 and out.numel() >= 1
+        wp = None
+        if weights is not None:
+            assert weights.is_cuda and weights.dtype == torch.float64 and weights.numel() >= self.nvec
+            wp = weights.data_ptr()
+        _native.check(_native.lib().kr_batch_expect_dev(self.handle, plan.op, wp, out.data_ptr(), stream_ptr()),
+                      self.ctx)
+
     def populations(self):
         """{J: (nvec,) array} J-populations of every vector (sum of |v|^2 over the
         slabs of each J), as the reference's observables (tests/test_tdse.py:63-67)."""

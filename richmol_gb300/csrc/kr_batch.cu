@@ -1010,6 +1010,42 @@ extern "C" int kr_batch_expect(kr_batch* b, kr_op* obs, double* out, void* strea
   return KR_OK;
 }
 
+// out = sum_v w_v Re <v|O|v> over the vectors (w: device weights, null = 1),
+// summed in vector order by one warp; a mat-vec error of the observable goes
+// into the sticky status (reported by kr_batch_sync)
+__global__ void kb_expect_wsum(const double2* h, const double* w, int nvec, double* out, const int* mverr,
+                               int* status) {
+  const int lane = threadIdx.x;
+  double s = 0.0;
+  for (int v = lane; v < nvec; v += 32) s += (w ? w[v] : 1.0) * h[v].x;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    *out = s;
+    if (*mverr != 0 && *status == 0) *status = *mverr;
+  }
+}
+
+extern "C" int kr_batch_expect_dev(kr_batch* b, kr_op* obs, const double* weights, double* out, void* stream) {
+  if (!b || !obs || !out) return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_expect_dev: bad argument");
+  if (obs->dev.dim_out != b->dim || !obs->square)
+    return set_err(obs->ctx, KR_ERR_ARG, "kr_batch_expect_dev: observable does not match the batch basis");
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long n = b->dim * b->nb;
+  float2* X = b->V;  // basis slot 0 and W are free between steps
+  KR_CUDA(obs->ctx, cudaMemsetAsync(b->counts + 2, 0, sizeof(int), st));
+  kb_to_f32<<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, st>>>(b->S, X, n);
+  int rc = launch_matvec(b, obs, X, b->W, false, nullptr, nullptr, st);
+  if (rc) return rc;
+  const dim3 eg(KB_RED_CHUNKS, b->nb / 32), eb(32, 8);
+  kb_expect_dots<<<eg, eb, 0, st>>>(b->S, b->W, b->dim, b->nb, b->part);
+  kb_reduce<<<(b->nb + 255) / 256, 256, 0, st>>>(b->part, 1, b->nb, 1, b->h, nullptr);
+  kb_expect_wsum<<<1, 32, 0, st>>>(b->h, weights, b->nvec, out, b->counts + 2, b->status);
+  b->launches += 4;
+  KR_CUDA(obs->ctx, cudaGetLastError());
+  return KR_OK;
+}
+
 // (nvec, dim) complex128 <-> [dim][nb] complex64
 __global__ void kb_transpose_in32(const double2* src, float2* X, long long dim, int nvec, int nb) {
   __shared__ float2 tile[32][33];

@@ -144,13 +144,17 @@ class Job:
         v = np.zeros((self.nvec, self.dim), np.complex128)
         v[np.arange(self.nvec), self.index] = 1.0
         ens.load(v)
-        trace = np.zeros(len(tc))
+        # the trace stays on the device: every step and its observable are queued
+        # whole (the Krylov loop runs on the device), with no host synchronisation
+        # until the end, so the steps of different jobs overlap on the GPU
+        import torch
+        w = torch.from_numpy(np.ascontiguousarray(self.weights, np.float64)).cuda()
+        trace_d = torch.zeros(len(tc), dtype=torch.float64, device="cuda")
         for i, t in enumerate(tc):
-            # the step is queued whole (its Krylov loop runs on the device); the
-            # observable's read-back is the one host synchronisation per step
             ens.step(self.wl.hamiltonian(t), sync=False)
-            trace[i] = float(self.weights @ ens.expect(self.wl.cos2).real) + 1.0 / 3.0
-        ens.sync()  # a step error (Krylov order above mmax) is raised here
+            ens.expect_into(self.wl.cos2, trace_d[i:i + 1], w)
+        ens.sync()  # a step error (Krylov order above mmax, observable mat-vec) is raised here
+        trace = trace_d.cpu().numpy() + 1.0 / 3.0
         self.state_steps = self.nvec * len(tc)
         del ens
         return trace

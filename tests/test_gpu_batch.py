@@ -367,3 +367,44 @@ def test_batch_wide_k_column_chunks_match_fp64(matvec):
         pops_ref = np.sum(np.abs(blk) ** 2, axis=1)
         pops[J] = pops[J] - pops_ref
     assert max(np.abs(p).max() for p in pops.values()) < 1e-6
+
+
+def test_batch_expect_on_device_matches_host_expect():
+    """Ensemble.expect_into (the weighted observable written to device memory,
+    no synchronisation) against the weighted sum of Ensemble.expect, over a trace
+    of unsynchronised steps read once at the end."""
+    from oracle import fixtures
+    from richmol_gb300 import TDSE
+    from richmol_gb300.batch import Ensemble
+    d, meta = fixtures.load(os.path.join(GOLDEN, "asym_j4.npz"))
+    sc = meta["scales"]
+    h0 = _ct("asym_j4.npz", "h0")
+    cos2 = _ct("asym_j4.npz", "cos2")
+    Hdc = (_ct("asym_j4.npz", "dip") * meta["dc"]) * sc["dc"]
+    Hac = _ct("asym_j4.npz", "pol") * sc["ac"]
+    sp = meta["split"]
+    td = TDSE(t_start=sp["t_start"], t_end=sp["t_end"], dt=sp["dt"])
+    tc = td.time_grid()
+    v0 = td.init_state(h0, temp=5, thresh=1e-3)
+    w = np.random.default_rng(3).uniform(0.1, 1.0, v0.shape[0])
+    wd = torch.from_numpy(w).cuda()
+    a = Ensemble(td, h0, v0.shape[0], tol=1e-10, matvec="tensor_tmem")
+    b = Ensemble(td, h0, v0.shape[0], tol=1e-10, matvec="tensor_tmem")
+    a.load(v0)
+    b.load(v0)
+    n = len(tc)
+    trace = torch.zeros(n, dtype=torch.float64, device="cuda")
+    ones = torch.zeros(n, dtype=torch.float64, device="cuda")
+    ref, ref1 = np.zeros(n), np.zeros(n)
+    for i in range(n):
+        Hac.field(d["split/fields"][i])
+        a.step(Hdc + Hac, sync=False)
+        a.expect_into(cos2, trace[i:i + 1], wd)
+        a.expect_into(cos2, ones[i:i + 1])
+        b.step(Hdc + Hac)
+        e = b.expect(cos2).real
+        ref[i] = float(w @ e)
+        ref1[i] = float(e.sum())
+    a.sync()
+    assert np.abs(trace.cpu().numpy() - ref).max() < 1e-13
+    assert np.abs(ones.cpu().numpy() - ref1).max() < 1e-13
