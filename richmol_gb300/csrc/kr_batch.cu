@@ -53,7 +53,7 @@ struct kr_batch {
   double* err = nullptr;     // [nb]
   double2* part = nullptr;   // [KB_RED_CHUNKS][mmax + 2][nb] partial sums
   int* counts = nullptr;     // [3]: active vectors, vectors that hit mmax, mat-vec error word
-  int* tc_work = nullptr;    // [2] work-item counters of the persistent tensor-core launches
+  int* tc_work = nullptr;    // [3] work-item counters of the persistent tensor-core launches
   int* kdev = nullptr;       // [2]: Krylov index of the running iteration, orders used by the last step
   int* status = nullptr;     // [1] sticky error of a step (0: none), read by kr_batch_sync / kr_batch_step
   // the step as a CUDA graph (prologue, a WHILE node over the Krylov
@@ -692,7 +692,7 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
   BA(nb, &b->err);
   BA((size_t)KB_RED_CHUNKS * (m1 + 1) * nb, &b->part);
   BA(3, &b->counts);
-  BA(2, &b->tc_work);
+  BA(3, &b->tc_work);
   BA(2, &b->kdev);
   BA(1, &b->status);
   // output tiles: R = 128 / NKP rows of one slab (NKP = n_k rounded up to 4, 8, 16, 32)

@@ -517,7 +517,7 @@ struct KbtRing {
   // tiles in TMEM (TA) the shared memory they took holds a ring about three
   // times as deep
   static constexpr int RS = 2;  // window rows per slot (4 with A in TMEM measured slower)
-  static constexpr int NSLOT = TA ? (KP == 16 ? 5 : 11) : 32 / KP;
+  static constexpr int NSLOT = TA ? (KP == 32 ? 2 : KP == 16 ? 5 : 11) : 32 / KP;
   static constexpr int ROW = KP * 1024;  // bytes of one window row in a slot
   static constexpr int SLOT = RS * ROW;
   static constexpr int BPART = 128 * KP;         // one B part: NP (<= 32) x KP FP32
@@ -749,7 +749,8 @@ struct KbtPers {
   static constexpr int NT = PT + 32 * (NMW + 2);  // threads of the CTA
 };
 static_assert(KbtPers<8>::TOTAL <= 232448 && KbtPers<16>::TOTAL <= 232448, "persistent tile exceeds shared memory");
-static_assert(KbtPers<8, true>::TOTAL <= 232448 && KbtPers<16, true>::TOTAL <= 232448,
+static_assert(KbtPers<8, true>::TOTAL <= 232448 && KbtPers<16, true>::TOTAL <= 232448 &&
+                  KbtPers<32, true>::TOTAL <= 232448,
               "persistent tile (A in TMEM) exceeds shared memory");
 
 // A tiles of tile row r in TMEM (the TA form): parts Z_re hi, lo, Z_im hi, lo,
@@ -1323,9 +1324,10 @@ int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, const int* cls, i
   const int rc = encode_xmap(ctx, p.X, dim, p.nb, p.nslots, &xmap);
   if (rc != KR_OK) return rc;
   const int nvb = p.nb / 128;
-  KR_CUDA(ctx, cudaMemsetAsync(work, 0, 2 * sizeof(int), st));
-  // persistent launches, one per KP class (8, 16): one CTA per SM at most
-  for (int c = 0; c < 2; ++c) {
+  KR_CUDA(ctx, cudaMemsetAsync(work, 0, 3 * sizeof(int), st));
+  // persistent launches, one per KP class (8, 16, and 32 with the A tiles in
+  // TMEM): one CTA per SM at most
+  for (int c = 0; c < (tmem_a ? 3 : 2); ++c) {
     const int n = cls[c + 1] - cls[c];
     if (n <= 0) continue;
     BatchTC q = p;
@@ -1339,6 +1341,10 @@ int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, const int* cls, i
         KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tcp<8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           KbtPers<8, true>::TOTAL));
         kb_matvec_tcp<8, true><<<grid, KbtPers<8, true>::NT, KbtPers<8, true>::TOTAL, st>>>(q, xmap);
+      } else if (c == 2) {
+        KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tcp<32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          KbtPers<32, true>::TOTAL));
+        kb_matvec_tcp<32, true><<<grid, KbtPers<32, true>::NT, KbtPers<32, true>::TOTAL, st>>>(q, xmap);
       } else {
         KR_CUDA(ctx, cudaFuncSetAttribute(kb_matvec_tcp<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           KbtPers<16, true>::TOTAL));
@@ -1355,9 +1361,9 @@ int kb_launch_tc(kr_ctx* ctx, const BatchTC& p, long long dim, const int* cls, i
     }
     KR_CUDA(ctx, cudaGetLastError());
   }
-  // KP = 32: one CTA per tile and vector block
+  // KP = 32 with the A tiles in shared memory: one CTA per tile and vector block
   const int n32 = cls[3] - cls[2];
-  if (n32 > 0) {
+  if (n32 > 0 && !tmem_a) {
     BatchTC q = p;
     q.tfirst = cls[2];
     q.tend = cls[3];

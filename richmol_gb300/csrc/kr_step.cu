@@ -1385,13 +1385,13 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   if (op->tc_ntask > 0) {
     UP(tc_task.data(), tc_task.size(), &p_i);
     op->tc_task = p_i;
-    // B blocks of the terms of the KP = 8, 16 tiles, 6 NP KP floats each
+    // B blocks of the terms of the persistent tiles (KP = 8, 16, 32), 6 NP KP floats each
     const int nterm = (int)t_in.size();
     std::vector<long long> prm((size_t)6 * std::max(1, nterm), 0), boff(std::max(1, nterm), 0);
     long long tot = 0;
     for (int s = 0; s < d->nslab_out; ++s) {
       const int kp = slab_kp[s];
-      if (kp != 8 && kp != 16) continue;
+      if (kp != 8 && kp != 16 && kp != 32) continue;
       const int np = d->out_dk[s] <= 16 ? 16 : 32;
       for (size_t k = 0; k < by_out[s].size(); ++k) {
         const int t = by_out[s][k], j = term_ptr[s] + (int)k;  // original and device term index

@@ -105,7 +105,7 @@ class Job:
     C1 basis size and ``max_vectors``); ``run`` builds the molecule's factors on
     the host, then propagates."""
 
-    def __init__(self, req, mmax=20, tol=1e-8, matvec="tensor"):
+    def __init__(self, req, mmax=20, tol=1e-8, matvec="tensor_tmem"):
         # a fixed kernel kind: a timed choice (matvec="auto") could differ between a
         # job alone and the same job among others, and so could its last digits
         self.req = req
@@ -116,8 +116,9 @@ class Job:
         dim = c1_dim(self.req.jmax)
         nvec = min(self.req.max_vectors, dim)
         # batch buffers, the loaded vectors (complex128) and the H0 phase, plus
-        # the operators (factors in FP64 and FP32, MF buffers): a margin
-        return batch_device_bytes(dim, nvec, self.mmax, 2 * (self.req.jmax + 1)) + 16 * dim * (nvec + 1) + (64 << 20)
+        # the operators (factors in FP64 and FP32, MF buffers, the tensor-core
+        # tiles' prebuilt B blocks): a margin
+        return batch_device_bytes(dim, nvec, self.mmax, 2 * (self.req.jmax + 1)) + 16 * dim * (nvec + 1) + (256 << 20)
 
     def build(self):
         if hasattr(self, "wl"):
