@@ -55,6 +55,8 @@ def parse(argv=None):
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="bound of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="headline measurement only")
+    p.add_argument("--plain-only", action="store_true",
+                   help="only the plain drop-in step (FP64 and double-float products; for profiling)")
     p.add_argument("--matvec", choices=["auto", "tensor", "tensor_tmem", "fp32", "fp32_reg"], default="auto",
                    help="batched mat-vec kind: tensor-core K contraction (split TF32; A operands in shared "
                         "or tensor memory) or FP32 FMAs; auto: every kind timed on the first step's operator, "
@@ -239,6 +241,11 @@ def run_ours(args, ws, rank, local):
     _native.check(_native.lib().kr_probe_fp64(ctx, ctypes.byref(fp64)), ctx)
     _native.check(_native.lib().kr_probe_fp32(ctx, ctypes.byref(fp32)), ctx)
     peaks, peak_kind = load_peaks()
+    if args.plain_only:
+        out = {"metric": "plain drop-in step only (--plain-only)", "unit": UNIT}
+        out["plain_fp64_drop_in"] = run_plain(args, dev, peaks, peak_kind, fp64.value)
+        out["plain_fp64_drop_in"]["df_products"] = run_plain(args, dev, peaks, peak_kind, fp64.value, products="df")
+        return out
 
     # ---- batched ensemble: the headline --------------------------------------
     note("headline")
@@ -417,6 +424,8 @@ def run_ours(args, ws, rank, local):
             out["serving"] = run_serving(args)
             note("uneven batch")
             out["uneven_batch"] = run_uneven(args)
+            note("wide-K mat-vec")
+            out["wide_k_matvec"] = run_widek(args)
 
     if rank == 0 and not args.no_cpu_baseline:
         rate, nst, tt = cpu_reference_rate(wl, args.cpu_seconds, vec=ensd.vectors(dim)[0])
@@ -584,6 +593,49 @@ def run_serving(args):
         "fp64_check": {"rid": small.rid, "jmax": small.jmax, "vectors": job.nvec, "steps": ncheck,
                        "max_abs_err_cos2": worst, "bound": 1e-6},
     }
+
+
+def run_widek(args, jmax=40, nvec=512):
+    """The batched mat-vec of one served-size request with wide K blocks: a C1
+    molecule (no symmetry, n_k = 2J + 1 up to 81, slabs cut into column chunks
+    of 32) at J <= 40, 512 vectors, every kernel kind; CUDA events over 5
+    launches after 2."""
+    import torch
+    from richmol_gb300 import TDSE, _native, rot, workloads
+    from richmol_gb300.batch import Ensemble
+    from richmol_gb300.device import stream_ptr
+    from richmol_gb300.serve import draw_request
+    L = _native.lib()
+    req = draw_request(np.random.default_rng(7), 0, 0.0, jmax_range=(jmax, jmax), t_end=5.0, dt=0.01)
+    mol = rot.Molecule(B=req.abc, sym="C1", pol=req.pol)
+    wl = workloads.Workload("c1_j%d" % jmax, mol, jmax, 0.0, 5.0, 0.01, None, req.pulse)
+    td = TDSE(t_start=0.0, t_end=5.0, dt=0.01)
+    tc = td.time_grid()
+    res = {}
+    for kind in ("tensor_tmem", "tensor", "fp32", "fp32_reg"):
+        ens = Ensemble(td, wl.h0, nvec, tol=1e-8, matvec=kind)
+        v = np.zeros((nvec, wl.dim), np.complex128)
+        v[np.arange(nvec), np.arange(nvec)] = 1.0
+        ens.load(v)
+        ens.step(wl.hamiltonian(tc[250]))
+        plan = wl.hamiltonian(tc[251]).device_operator(split=ens.split)
+        for _ in range(2):
+            _native.check(L.kr_batch_matvec(ens.handle, plan.op, stream_ptr()), ens.ctx)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(5):
+            _native.check(L.kr_batch_matvec(ens.handle, plan.op, stream_ptr()), ens.ctx)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / 5
+        fma, _ = plan.work()
+        res[kind] = {"ms": round(ms, 3), "alg_gbs": round(16.0 * wl.dim * nvec / ms / 1e6, 1),
+                     "fp32_tflops": round(2.0 * fma * nvec / ms / 1e9, 1)}
+        del ens
+        torch.cuda.empty_cache()
+    return {"workload": f"C1 asymmetric top J=0..{jmax} (dim {wl.dim}, n_k up to {2 * jmax + 1}, column chunks "
+                        f"of 32), {nvec} vectors, one batched mat-vec", "by_kind": res}
 
 
 def run_uneven(args):
