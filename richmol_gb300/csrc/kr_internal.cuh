@@ -99,7 +99,8 @@ struct kr_op {
   DevOp dev{};
   DevField field{};
   std::vector<void*> allocs;
-  int grid = 1;
+  int grid = 1;     // cooperative grid of the plain step (FP64 products)
+  int grid_df = 1;  // the same with double-float products
   size_t smem = 0;
   int maxorder = 100;
   bool square = false;

@@ -298,7 +298,7 @@ __device__ __forceinline__ void step_matvec(const StepArgs& a, const double2* x,
 }
 
 template <bool DF>
-__global__ void __launch_bounds__(KR_THREADS, 2) kr_step_kernel(StepArgs a) {
+__global__ void __launch_bounds__(KR_THREADS, DF ? 3 : 2) kr_step_kernel(StepArgs a) {
   extern __shared__ double2 smem_dyn[];
   __shared__ StepSmem ss;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -861,10 +861,11 @@ static cudaError_t ensure_step_smem(size_t smem) {
   return e;
 }
 
-// the plain step kernel of an operator's precision
+// the plain step kernel of an operator's precision, and its cooperative grid
 static void* step_kernel(const kr_op* op) {
   return op->prec == KR_PREC_DF ? (void*)kr_step_kernel<true> : (void*)kr_step_kernel<false>;
 }
+static int step_grid(const kr_op* op) { return op->prec == KR_PREC_DF ? op->grid_df : op->grid; }
 
 extern "C" int kr_op_set_precision(kr_op* op, int32_t prec) {
   if (!op || (prec != KR_PREC_F64 && prec != KR_PREC_DF))
@@ -1184,14 +1185,17 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
   int occ_df = 0;
   if (ce == cudaSuccess)
     ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_df, kr_step_kernel<true>, KR_THREADS, op->smem);
-  occ = std::min(occ, occ_df);
-  if (ce != cudaSuccess || occ < 1) {
+  if (ce != cudaSuccess || occ < 1 || occ_df < 1) {
     kr_op_destroy(op);
     return set_err(ctx, KR_ERR_CUDA, "kr_step_kernel cannot be resident");
   }
+  // two CTAs per SM for FP64 products; three with double-float products (fewer
+  // registers: more warps to hide the latency of the barrier-bound step)
   int grid = ctx->nsm * std::min(occ, 2);
   grid = std::max(1, std::min(grid, ntask));
   op->grid = grid;
+  op->grid_df = std::max(1, std::min(ctx->nsm * std::min(occ_df, 3), ntask));
+  const int grid_max = std::max(op->grid, op->grid_df);
 
   // tasks are handed out dynamically, most expensive first
   std::vector<int> task_order(ntask);
@@ -1464,11 +1468,11 @@ extern "C" int kr_op_create(kr_ctx* ctx, const kr_op_desc* d, kr_op** out) {
     UP((const double2*)nullptr, (size_t)n, &p_c); op->w = p_c;
     UP((const double2*)nullptr, (size_t)n, &p_c); op->ub0 = p_c;
     UP((const double2*)nullptr, (size_t)n, &p_c); op->ub1 = p_c;
-    UP((const double2*)nullptr, (size_t)grid, &p_c); op->part_a = p_c;
+    UP((const double2*)nullptr, (size_t)grid_max, &p_c); op->part_a = p_c;
     UP((const double2*)nullptr, (size_t)ntask, &p_c); op->task_alpha = p_c;
     UP((const unsigned*)nullptr, (size_t)d->maxorder + 2, &p_u); op->counters = p_u;
-    UP((const double*)nullptr, (size_t)grid, &p_d); op->part_b = p_d;
-    UP((const double*)nullptr, (size_t)grid, &p_d); op->part_c = p_d;
+    UP((const double*)nullptr, (size_t)grid_max, &p_d); op->part_b = p_d;
+    UP((const double*)nullptr, (size_t)grid_max, &p_d); op->part_c = p_d;
     UP((const double2*)nullptr, (size_t)d->maxorder + 1, &p_c); op->alpha = p_c;
     UP((const double*)nullptr, (size_t)d->maxorder + 1, &p_d); op->beta = p_d;
     UP((const unsigned*)nullptr, 2, &p_u); op->bar = p_u;
@@ -1631,7 +1635,7 @@ extern "C" int kr_step(kr_op* op, void* states, int64_t nvec, const void* phase,
     KR_CUDA(op->ctx, cudaMemsetAsync(op->bar, 0, sizeof(unsigned), st));  // arrival count only
     void* args[] = {&a};
     KR_CUDA(op->ctx, ensure_step_smem(op->smem));
-    KR_CUDA(op->ctx, cudaLaunchCooperativeKernel(step_kernel(op), dim3(op->grid), dim3(KR_THREADS), args,
+    KR_CUDA(op->ctx, cudaLaunchCooperativeKernel(step_kernel(op), dim3(step_grid(op)), dim3(KR_THREADS), args,
                                                  op->smem, st));
     op->launches++;
     if (korder) {
@@ -1821,8 +1825,9 @@ extern "C" int kr_static_scratch_bytes(const kr_op* op, size_t* needed, size_t* 
   size_t b = 0;
   b += round256(sizeof(double2) * n * m);                    // V
   b += 5 * round256(sizeof(double2) * n);                    // W[2], w, u[2]
-  b += round256(sizeof(double2) * op->grid);                 // part_a
-  b += 2 * round256(sizeof(double) * op->grid);              // part_b, part_c
+  const size_t gm = (size_t)std::max(op->grid, op->grid_df);
+  b += round256(sizeof(double2) * gm);                       // part_a
+  b += 2 * round256(sizeof(double) * gm);                    // part_b, part_c
   b += round256(sizeof(double2) * op->dev.ntask);            // task_alpha
   b += round256(sizeof(unsigned) * (m + 2));                 // counters
   b += round256(sizeof(double2) * (m + 1));                  // alpha
@@ -1895,9 +1900,10 @@ extern "C" int kr_step_static(kr_op* op, void* states, int64_t nvec, const void*
   a.w = (double2*)carve(sizeof(double2) * n);
   a.ub[0] = (double2*)carve(sizeof(double2) * n);
   a.ub[1] = (double2*)carve(sizeof(double2) * n);
-  a.part_a = (double2*)carve(sizeof(double2) * op->grid);
-  a.part_b = (double*)carve(sizeof(double) * op->grid);
-  a.part_c = (double*)carve(sizeof(double) * op->grid);
+  const size_t gm = (size_t)std::max(op->grid, op->grid_df);
+  a.part_a = (double2*)carve(sizeof(double2) * gm);
+  a.part_b = (double*)carve(sizeof(double) * gm);
+  a.part_c = (double*)carve(sizeof(double) * gm);
   a.task_alpha = (double2*)carve(sizeof(double2) * op->dev.ntask);
   a.counters = (unsigned*)carve(sizeof(unsigned) * (m + 2));
   a.alpha = (double2*)carve(sizeof(double2) * (m + 1));
@@ -1925,7 +1931,7 @@ extern "C" int kr_step_static(kr_op* op, void* states, int64_t nvec, const void*
     KR_CUDA(op->ctx, cudaMemsetAsync(bar, 0, sizeof(unsigned), st));
     void* args[] = {&a};
     KR_CUDA(op->ctx, ensure_step_smem(op->smem));
-    KR_CUDA(op->ctx, cudaLaunchCooperativeKernel(step_kernel(op), dim3(op->grid), dim3(KR_THREADS), args,
+    KR_CUDA(op->ctx, cudaLaunchCooperativeKernel(step_kernel(op), dim3(step_grid(op)), dim3(KR_THREADS), args,
                                                  op->smem, st));
     op->launches++;
     if (korder) {
