@@ -542,7 +542,7 @@ __device__ __forceinline__ double seg_warp_sum(const double* part, int b, int e,
 }
 
 template <bool F32>
-__global__ void __launch_bounds__(KR_THREADS, 2) kr_seg_step_kernel(SegArgs a) {
+__global__ void __launch_bounds__(KR_THREADS, F32 ? 3 : 2) kr_seg_step_kernel(SegArgs a) {
   extern __shared__ double2 smem_dyn[];
   __shared__ StepSmem ss;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -1964,7 +1964,7 @@ extern "C" int kr_step_static(kr_op* op, void* states, int64_t nvec, const void*
 // ===========================================================================
 struct kr_seg {
   kr_op* op = nullptr;
-  int nseg = 0, nchunk = 0, grid = 1;
+  int nseg = 0, nchunk = 0, grid = 1, grid32 = 1;  // cooperative grids: FP64, FP32 products
   std::vector<void*> allocs;
   int *slab_seg = nullptr, *chunk_seg = nullptr, *seg_chunk_ptr = nullptr, *seg_task_ptr = nullptr,
       *seg_tasks = nullptr;
@@ -2093,12 +2093,12 @@ extern "C" int kr_seg_create(kr_op* op, int32_t nseg, const int32_t* slab_seg, k
   cudaError_t ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kr_seg_step_kernel<false>, KR_THREADS, op->smem);
   if (ce == cudaSuccess)
     ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ32, kr_seg_step_kernel<true>, KR_THREADS, op->smem);
-  occ = std::min(occ, occ32);
-  if (ce != cudaSuccess || occ < 1) {
+  if (ce != cudaSuccess || occ < 1 || occ32 < 1) {
     kr_seg_destroy(g);
     return set_err(op->ctx, KR_ERR_CUDA, "kr_seg_step_kernel cannot be resident");
   }
   g->grid = std::max(1, op->ctx->nsm * std::min(occ, 2));
+  g->grid32 = std::max(1, op->ctx->nsm * std::min(occ32, 3));  // FP32 products: 3 CTAs per SM
   *out = g;
   return KR_OK;
 }
@@ -2149,7 +2149,7 @@ extern "C" int kr_seg_step(kr_seg* g, void* states, const void* phase, double fa
   KR_CUDA(op->ctx, ensure_step_smem(op->smem));
   void* args[] = {&a};
   KR_CUDA(op->ctx, cudaLaunchCooperativeKernel(g->f32 ? (void*)kr_seg_step_kernel<true> : (void*)kr_seg_step_kernel<false>,
-                                               dim3(g->grid), dim3(KR_THREADS), args, op->smem, st));
+                                               dim3(g->f32 ? g->grid32 : g->grid), dim3(KR_THREADS), args, op->smem, st));
   g->launches++;
   int hs = 0;
   KR_CUDA(op->ctx, cudaMemcpyAsync(&hs, op->status, sizeof(int), cudaMemcpyDeviceToHost, st));
