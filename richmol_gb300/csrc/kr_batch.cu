@@ -50,6 +50,7 @@ struct kr_batch {
   int* kconv = nullptr;      // [nb] converged Krylov order (0: still active)
   int* active = nullptr;     // [nb]
   int* grp_active = nullptr; // [nb / KB_MV_THREADS rounded up]
+  int* grp_w = nullptr;      // [the same]: groups with a vector of non-zero weight (kr_batch_expect_dev)
   double* err = nullptr;     // [nb]
   double2* part = nullptr;   // [KB_RED_CHUNKS][mmax + 2][nb] partial sums
   int* counts = nullptr;     // [3]: active vectors, vectors that hit mmax, mat-vec error word
@@ -486,10 +487,37 @@ __global__ void kb_to_f32(const float4* S, float2* X, long long n) {
   }
 }
 
-// partial <S_v | Y_v> with Y in complex64 (double-float accumulation)
-__global__ void kb_expect_dots(const float4* S, const float2* Y, long long dim, int nb, double2* part) {
+// 32-vector groups that hold a vector of non-zero weight (w null: every
+// vector below nvec): grp[g] = 1, else 0
+__global__ void kb_weight_groups(const double* w, int nvec, int nb, int* grp) {
+  const int g = blockIdx.x * blockDim.y + threadIdx.y;
+  if (g * 32 >= nb) return;
+  const int v = g * 32 + threadIdx.x;
+  const bool on = v < nvec && (w == nullptr || w[v] != 0.0);
+  const unsigned any = __ballot_sync(0xffffffffu, on);
+  if (threadIdx.x == 0) grp[g] = any != 0u;
+}
+
+// kb_to_f32 over the vectors of active 32-vector groups only (grid.y: group)
+__global__ void kb_to_f32_groups(const float4* S, float2* X, long long dim, int nb, const int* grp) {
+  if (!grp[blockIdx.y]) return;
+  const int v = blockIdx.y * 32 + threadIdx.x;
+  for (long long e = blockIdx.x * (long long)blockDim.y + threadIdx.y; e < dim; e += (long long)gridDim.x * blockDim.y) {
+    const float4 s = S[e * nb + v];
+    X[e * nb + v] = make_float2(__fadd_rn(s.x, s.y), __fadd_rn(s.z, s.w));
+  }
+}
+
+// partial <S_v | Y_v> with Y in complex64 (double-float accumulation); with
+// grp, the vectors of inactive groups get zero partials without reading S or Y
+__global__ void kb_expect_dots(const float4* S, const float2* Y, long long dim, int nb, double2* part,
+                               const int* grp = nullptr) {
   __shared__ double2 sh[8][32];
   const int v = blockIdx.y * 32 + threadIdx.x;
+  if (grp && !grp[blockIdx.y]) {
+    if (threadIdx.y == 0) part[(long long)blockIdx.x * nb + v] = make_double2(0.0, 0.0);
+    return;
+  }
   const Chunk ch = chunk_of(dim);
   dfl ar = {0.f, 0.f}, ai = {0.f, 0.f};
   for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
@@ -594,7 +622,7 @@ const char* const mv_error_text =
 // array b->V (b->vscale); with kslot its slot is the device-side Krylov index
 // *kslot, else slot 0.
 int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool masked, const double* yscale,
-                  const int* kslot, cudaStream_t st) {
+                  const int* kslot, cudaStream_t st, const int* grp = nullptr) {
   const long long slot_elems = b->dim * (long long)b->nb;
   if ((b->mv_kind == KR_MATVEC_TENSOR || b->mv_kind == KR_MATVEC_TENSOR_TMEM) && op->tc_ntask > 0) {
     BatchTC q;
@@ -607,7 +635,7 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
     q.nslots = kslot ? b->mmax + 1 : 1;
     q.task = op->tc_task;
     q.ntask = op->tc_ntask;
-    q.grp_active = masked ? b->grp_active : nullptr;
+    q.grp_active = grp ? grp : (masked ? b->grp_active : nullptr);
     q.yscale = yscale;
     q.tcb = op->tc_b;
     q.tcb_off = op->tc_boff;
@@ -633,7 +661,7 @@ int launch_matvec(kr_batch* b, kr_op* op, const float2* X, float2* Y, bool maske
   p.task_slab = b->task_slab;
   p.task_i0 = b->task_i0;
   p.task_nr = b->task_nr;
-  p.grp_active = masked ? b->grp_active : nullptr;
+  p.grp_active = grp ? grp : (masked ? b->grp_active : nullptr);
   p.yscale = yscale;
   if (b->mv_kind == KR_MATVEC_FP32_REG && op->zr_ntask > 0) {
     const int rc = kb_launch_zr(op->ctx, p, op->zr_task, op->zr_ntask, op->zr_class, mv_groups(b), st);
@@ -689,6 +717,7 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
   BA(nb, &b->kconv);
   BA(nb, &b->active);
   BA((size_t)mv_groups(b), &b->grp_active);
+  BA((size_t)mv_groups(b), &b->grp_w);
   BA(nb, &b->err);
   BA((size_t)KB_RED_CHUNKS * (m1 + 1) * nb, &b->part);
   BA(3, &b->counts);
@@ -1017,7 +1046,8 @@ __global__ void kb_expect_wsum(const double2* h, const double* w, int nvec, doub
                                int* status) {
   const int lane = threadIdx.x;
   double s = 0.0;
-  for (int v = lane; v < nvec; v += 32) s += (w ? w[v] : 1.0) * h[v].x;
+  for (int v = lane; v < nvec; v += 32)
+    if (w == nullptr || w[v] != 0.0) s += (w ? w[v] : 1.0) * h[v].x;  // zero-weight vectors are not computed
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) {
@@ -1031,17 +1061,20 @@ extern "C" int kr_batch_expect_dev(kr_batch* b, kr_op* obs, const double* weight
   if (obs->dev.dim_out != b->dim || !obs->square)
     return set_err(obs->ctx, KR_ERR_ARG, "kr_batch_expect_dev: observable does not match the batch basis");
   cudaStream_t st = (cudaStream_t)stream;
-  const long long n = b->dim * b->nb;
   float2* X = b->V;  // basis slot 0 and W are free between steps
   KR_CUDA(obs->ctx, cudaMemsetAsync(b->counts + 2, 0, sizeof(int), st));
-  kb_to_f32<<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, st>>>(b->S, X, n);
-  int rc = launch_matvec(b, obs, X, b->W, false, nullptr, nullptr, st);
+  // only the 32-vector groups with a vector of non-zero weight are computed
+  const int ng = b->nb / 32;
+  kb_weight_groups<<<(ng + 7) / 8, dim3(32, 8), 0, st>>>(weights, b->nvec, b->nb, b->grp_w);
+  kb_to_f32_groups<<<dim3((unsigned)std::min<long long>((b->dim + 7) / 8, 1024), ng), dim3(32, 8), 0, st>>>(
+      b->S, X, b->dim, b->nb, b->grp_w);
+  int rc = launch_matvec(b, obs, X, b->W, false, nullptr, nullptr, st, b->grp_w);
   if (rc) return rc;
   const dim3 eg(KB_RED_CHUNKS, b->nb / 32), eb(32, 8);
-  kb_expect_dots<<<eg, eb, 0, st>>>(b->S, b->W, b->dim, b->nb, b->part);
+  kb_expect_dots<<<eg, eb, 0, st>>>(b->S, b->W, b->dim, b->nb, b->part, b->grp_w);
   kb_reduce<<<(b->nb + 255) / 256, 256, 0, st>>>(b->part, 1, b->nb, 1, b->h, nullptr);
   kb_expect_wsum<<<1, 32, 0, st>>>(b->h, weights, b->nvec, out, b->counts + 2, b->status);
-  b->launches += 4;
+  b->launches += 6;
   KR_CUDA(obs->ctx, cudaGetLastError());
   return KR_OK;
 }

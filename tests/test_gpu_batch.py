@@ -408,3 +408,37 @@ def test_batch_expect_on_device_matches_host_expect():
     a.sync()
     assert np.abs(trace.cpu().numpy() - ref).max() < 1e-13
     assert np.abs(ones.cpu().numpy() - ref1).max() < 1e-13
+
+
+def test_batch_expect_on_device_skips_zero_weight_groups():
+    """Vector groups of zero weight are left out of the device observable's
+    mat-vec; the weighted sum equals the host one over the weighted vectors."""
+    from oracle import fixtures
+    from richmol_gb300 import TDSE
+    from richmol_gb300.batch import Ensemble
+    d, meta = fixtures.load(os.path.join(GOLDEN, "asym_j4.npz"))
+    sc = meta["scales"]
+    h0 = _ct("asym_j4.npz", "h0")
+    cos2 = _ct("asym_j4.npz", "cos2")
+    Hac = _ct("asym_j4.npz", "pol") * sc["ac"]
+    sp = meta["split"]
+    td = TDSE(t_start=sp["t_start"], t_end=sp["t_end"], dt=sp["dt"])
+    tc = td.time_grid()
+    v0 = td.init_state(h0, temp=5, thresh=1e-3)
+    nvec = 96
+    rng = np.random.default_rng(5)
+    v = np.zeros((nvec, v0.shape[1]), np.complex128)
+    v[: v0.shape[0]] = v0
+    v[v0.shape[0]:] = rng.normal(size=(nvec - v0.shape[0], v0.shape[1]))
+    v[v0.shape[0]:] /= np.linalg.norm(v[v0.shape[0]:], axis=1)[:, None]
+    w = np.zeros(nvec)
+    w[: v0.shape[0]] = rng.uniform(0.1, 1.0, v0.shape[0])
+    w[70] = 0.5  # one weighted vector in the third group
+    ens = Ensemble(td, h0, nvec, tol=1e-10, matvec="tensor_tmem")
+    ens.load(v)
+    Hac.field(d["split/fields"][0])
+    ens.step(Hac)
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    ens.expect_into(cos2, out, torch.from_numpy(w).cuda())
+    e = ens.expect(cos2).real
+    assert abs(float(out.cpu()[0]) - float(w @ e)) < 1e-13
