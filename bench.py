@@ -57,6 +57,8 @@ def parse(argv=None):
     p.add_argument("--no-extras", action="store_true", help="headline measurement only")
     p.add_argument("--plain-only", action="store_true",
                    help="only the plain drop-in step (FP64 and double-float products; for profiling)")
+    p.add_argument("--widek-only", action="store_true",
+                   help="only the wide-K (C1, KP = 32 tiles) batched mat-vec of every kind (for profiling)")
     p.add_argument("--matvec", choices=["auto", "tensor", "tensor_tmem", "fp32", "fp32_reg"], default="auto",
                    help="batched mat-vec kind: tensor-core K contraction (split TF32; A operands in shared "
                         "or tensor memory) or FP32 FMAs; auto: every kind timed on the first step's operator, "
@@ -241,6 +243,9 @@ def run_ours(args, ws, rank, local):
     _native.check(_native.lib().kr_probe_fp64(ctx, ctypes.byref(fp64)), ctx)
     _native.check(_native.lib().kr_probe_fp32(ctx, ctypes.byref(fp32)), ctx)
     peaks, peak_kind = load_peaks()
+    if args.widek_only:
+        return {"metric": "wide-K batched mat-vec only (--widek-only)", "unit": "ms",
+                "wide_k_matvec": run_widek(args)}
     if args.plain_only:
         out = {"metric": "plain drop-in step only (--plain-only)", "unit": UNIT}
         out["plain_fp64_drop_in"] = run_plain(args, dev, peaks, peak_kind, fp64.value)
