@@ -88,8 +88,11 @@ class CarTens:
     """GPU drop-in for richmol.field.CarTens on the propagation path.
 
     Args:
-        filename : str   factor file (``.npz``, see richmol_gb300.io)
+        filename : str   factor file: ``.npz`` (richmol_gb300.io) or the
+                         reference's HDF5 layout (field.py:1304-1848)
         name : str       tensor name inside the file
+        thresh : float   matrix elements below it are dropped on reading, and
+                         blocks left empty with them (field.py:1600-1848 read)
     """
 
     def __init__(self, filename=None, name=None, **kwargs):
@@ -98,7 +101,7 @@ class CarTens:
         if filename is not None:
             if name is None:
                 raise ValueError(f"please specify the name of the data group in file '{filename}'")
-            basis, kmat, mmat, mfmat, rank, cart = _io.read_tensor(filename, name)
+            basis, kmat, mmat, mfmat, rank, cart = _io.read_tensor(filename, name, thresh=kwargs.get("thresh"))
             if not mmat and mfmat is not None:
                 # stored field-contracted operator: a frozen single-component source
                 mmat = _nested()

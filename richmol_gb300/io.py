@@ -10,15 +10,21 @@ Layout (one archive may hold several tensors, each under its own name):
   dim_m, dim_k), ``rank``, ``cart`` and the block list
   (kind, J1, J2, sym1, sym2, irrep, cart, matrix index), kind "k", "m" or "mf".
 
-This stands in for the reference's HDF5 layout (richmol/field.py:1304-1848,
-groups ``J:<J1>,<J2>/sym:<s1>,<s2>`` with kmat_* / mmat_* datasets), which
-needs h5py; the block keys and the CSR content are the same.
+``read_tensor`` also reads the reference's own HDF5 files (richmol/field.py:
+1304-1848: a group per tensor holding ``J:<J1>,<J2>/sym:<s1>,<s2>`` groups with
+kmat_* / mmat_* datasets and their split attributes), through the numpy
+HDF5 reader in richmol_gb300.hdf5, so factor files from richmol's database
+load directly. Writing stays in the ``.npz`` layout above; the block keys and
+the CSR content are the same in both.
 """
 import json
+import re
 from collections import defaultdict
 
 import numpy as np
 from scipy.sparse import csr_matrix
+
+from . import hdf5
 
 
 def _nested():
@@ -29,8 +35,135 @@ def jkey(J):
     return round(float(J), 1)
 
 
-def read_tensor(filename, name):
-    """Returns (basis dict, kmat, mmat, mfmat or None, rank, cart)."""
+# group names of field.py:1885-1898 (J_group_key, sym_group_key)
+_J_GROUP = re.compile(r"^J:(\d+\.\d+),(\d+\.\d+)$")
+_SYM_GROUP = re.compile(r"^sym:(\w+),(\w+)$")
+
+
+def _h5_attrs(group):
+    """Attributes with the ``__json`` ones decoded (field.py:1647-1655)."""
+    out = {}
+    for key, val in group.attrs.items():
+        if key.endswith("__json"):
+            out[key[: -len("__json")]] = json.loads(val)
+        else:
+            out[key] = val
+    return out
+
+
+def _str(x):
+    return x.decode("utf-8") if isinstance(x, (bytes, np.bytes_)) else str(x)
+
+
+def _irrep(x):
+    s = _str(x)
+    try:
+        return int(s)
+    except ValueError:
+        return s
+
+
+def _h5_split(group, prefix, n):
+    """The n CSR matrices of kmat_* or mmat_* (field.py:1755-1830): the
+    concatenated datasets split by the per-matrix counts in the attributes."""
+    a = group.attrs
+    data = group[prefix + "_data"][()]
+    ind = group[prefix + "_indices"][()]
+    ptr = group[prefix + "_indptr"][()]
+    cd, ci, cp = (np.concatenate([[0], np.cumsum(a[prefix + k])]) for k in ("_nnz", "_nind", "_nptr"))
+    shape = np.asarray(a[prefix + "_shape"]).reshape(n, 2)
+    out = []
+    for i in range(n):
+        out.append(csr_matrix((data[cd[i]: cd[i + 1]].astype(np.complex128),
+                               ind[ci[i]: ci[i + 1]], ptr[cp[i]: cp[i + 1]]),
+                              shape=(int(shape[i, 0]), int(shape[i, 1]))))
+    return out
+
+
+def read_tensor_h5(filename, name):
+    """Reads a tensor stored by the reference's CarTens.store (field.py:
+    1600-1848, without state filters or threshold). Returns the same tuple as
+    read_tensor; mfmat is None (the reference stores kmat and mmat only)."""
+    with hdf5.File(filename) as fl:
+        if name not in fl:
+            raise KeyError(f"file '{filename}' has no dataset with the name '{name}'")
+        group = fl[name]
+        attrs = _h5_attrs(group)
+        cls = _str(attrs.get("__class_name__", ""))
+        if not cls.endswith("CarTens") and not cls.endswith("LabTensor"):
+            raise TypeError(f"dataset with the name '{name}' in file '{filename}' has different type: '{cls}'")
+        basis = {}
+        for side in ("1", "2"):
+            Jlist = [jkey(J) for J in np.atleast_1d(attrs["Jlist" + side])]
+            syml = {jkey(J): list(v) for J, v in attrs["symlist" + side].items()}
+            basis["Jlist" + side] = Jlist
+            basis["symlist" + side] = {J: syml[J] for J in Jlist}
+            for kind in ("dim_m", "dim_k"):
+                d = {jkey(J): {s: int(n) for s, n in v.items()} for J, v in attrs[kind + side].items()}
+                basis[kind + side] = {J: d[J] for J in Jlist}
+        rank = int(attrs["rank"])
+        cart = [_str(c) for c in np.atleast_1d(attrs["cart"])]
+        kmat, mmat = _nested(), _nested()
+        for jname in group.keys():
+            mj = _J_GROUP.match(jname)
+            if mj is None:
+                continue
+            Jp = (jkey(mj.group(1)), jkey(mj.group(2)))
+            gj = group[jname]
+            for sname in gj.keys():
+                ms = _SYM_GROUP.match(sname)
+                if ms is None:
+                    continue
+                sp = (ms.group(1), ms.group(2))
+                gs = gj[sname]
+                if "kmat_irreps" in gs.attrs:
+                    irreps = [_irrep(x) for x in np.atleast_1d(gs.attrs["kmat_irreps"])]
+                    for irrep, m in zip(irreps, _h5_split(gs, "kmat", len(irreps))):
+                        kmat[Jp][sp][irrep] = m
+                if "mmat_irrep_cart" in gs.attrs:
+                    ic = np.asarray(gs.attrs["mmat_irrep_cart"]).reshape(-1, 2)
+                    for (irrep, c), m in zip(ic, _h5_split(gs, "mmat", len(ic))):
+                        mmat[Jp][sp][_irrep(irrep)][_str(c)] = m
+    return basis, kmat, mmat, None, rank, cart
+
+
+def _drop_small(blocks, depth, thresh):
+    """Zeroes elements below thresh in nested dicts of CSR matrices (depth =
+    the number of dict levels above a matrix) and removes matrices, then
+    dicts, left empty (field.py:1780-1840)."""
+    for key in list(blocks.keys()):
+        val = blocks[key]
+        if depth == 1:
+            m = val.copy()
+            m.data[np.abs(m.data) < thresh] = 0
+            m.eliminate_zeros()
+            if m.nnz > 0:
+                blocks[key] = m
+            else:
+                del blocks[key]
+        else:
+            _drop_small(val, depth - 1, thresh)
+            if len(val) == 0:
+                del blocks[key]
+
+
+def read_tensor(filename, name, thresh=None):
+    """Returns (basis dict, kmat, mmat, mfmat or None, rank, cart); with
+    thresh, matrix elements below it are dropped (field.py:1600-1848)."""
+    if hdf5.is_hdf5(filename):
+        out = read_tensor_h5(filename, name)
+    else:
+        out = _read_tensor_npz(filename, name)
+    if thresh is not None:
+        basis, kmat, mmat, mfmat, rank, cart = out
+        _drop_small(kmat, 3, thresh)   # [J pair][sym pair][irrep]
+        _drop_small(mmat, 4, thresh)   # [J pair][sym pair][irrep][cart]
+        if mfmat is not None:
+            _drop_small(mfmat, 3, thresh)
+    return out
+
+
+def _read_tensor_npz(filename, name):
     d = np.load(filename, allow_pickle=False)
     meta = json.loads(str(d["meta"]))
     if name not in meta:

@@ -182,19 +182,135 @@ def _j_matrices(J):
     return Jx, Jy, np.diag(ks.astype(float))
 
 
+def _inertia_origin(m, r):
+    """Inertia tensor about the coordinate origin, sum_i m_i (|r_i|^2 - r_i r_i^T).
+    The reference's G matrix (rot/molecule.py:189-260) is the inverse of this
+    tensor of the frame-rotated coordinates, not shifted to the centre of mass."""
+    return np.eye(3) * np.sum(m * np.sum(r * r, axis=1)) - (m[:, None] * r).T @ r
+
+
+def _inertia_com(m, r):
+    """Inertia tensor about the centre of mass (rot/molecule.py:169-186)."""
+    r0 = r - (m[:, None] * r).sum(0) / m.sum()
+    return _inertia_origin(m, r0)
+
+
+# h N_A 1e16 / (4 pi^2 c) 1e5: amu*Angstrom^2 -> cm^-1 for G (rot/molecule.py:191-192)
+_G_CONV = (const.value("Planck constant") * const.value("Avogadro constant") * 1e16
+           / (4.0 * np.pi ** 2 * const.value("speed of light in vacuum")) * 1e5)
+
+
 class Molecule:
     """Rotational constants (cm^-1), Watson-A centrifugal terms, symmetry and
-    molecular-frame tensors (dipole, polarizability) of one molecule."""
+    molecular-frame tensors (dipole, polarizability) of one molecule.
 
-    def __init__(self, B=None, xyz=None, linear=None, sym="C1", watson=None, dip=None, pol=None):
+    The rigid-rotor part is either B = (Bx, By, Bz), H = sum_a B_a J_a^2
+    (rot/solution.py:251-257), or a full rotational kinetic-energy matrix G
+    (cm^-1), H = 1/2 sum_ab G_ab J_a J_b (rot/solution.py:259-272), as the
+    reference builds for a geometry in a frame where the inertia tensor is not
+    diagonal (``from_geometry``)."""
+
+    def __init__(self, B=None, xyz=None, linear=None, sym="C1", watson=None, dip=None, pol=None, G=None):
+        self.G = None if G is None else np.asarray(G, dtype=np.float64).reshape(3, 3)
         if B is None and xyz is not None:
             B = self.B_from_geometry(xyz)
+        if B is None and self.G is not None:
+            B = 0.5 * np.diag(self.G)
         self.B = tuple(float(b) for b in B)
         self.linear = linear if linear is not None else (sum(b == 0 for b in self.B) == 1)
+        if self.G is not None and self.linear:
+            raise ValueError("a G matrix describes a non-linear molecule; give B for a linear one")
         self.sym = sym
         self.watson = dict(watson or {})
         self.dip = None if dip is None else np.asarray(dip, dtype=np.float64)
         self.pol = None if pol is None else np.asarray(pol, dtype=np.float64)
+        self.frame_rotation = np.eye(3)
+
+    @staticmethod
+    def frame_matrix(frame, masses, xyz, pol=None):
+        """Rotation R to a molecular frame, r' = R r (rot/mol_frames.py:29-140):
+        None or "eye" (identity), "ipas" / "diag(inertia)" (eigenvectors of the
+        centre-of-mass inertia tensor, ascending), "diag(pol)" (of the
+        polarizability), or an explicit 3x3 matrix."""
+        if frame is None or (isinstance(frame, str) and frame.lower() in ("eye", "none", "null")):
+            return np.eye(3)
+        if not isinstance(frame, str):
+            R = np.asarray(frame, dtype=np.float64).reshape(3, 3)
+        else:
+            f = frame.strip().lower()
+            if f in ("ipas", "diag(inertia)"):
+                mat = _inertia_com(masses, xyz)
+            elif f == "diag(pol)":
+                if pol is None:
+                    raise TypeError("tensor 'pol' is not available")
+                mat = np.asarray(pol, dtype=np.float64)
+                if np.any(np.abs(mat - mat.T) > 1e-12):
+                    raise ValueError("tensor is not symmetric")
+            else:
+                raise ValueError(f"frame '{frame}' is not available")
+            _, vec = np.linalg.eigh(mat)
+            R = vec.T
+        if np.abs(R @ R.T - np.eye(3)).max() > 1e-12:
+            raise ValueError("frame rotation matrix is not orthogonal")
+        return R
+
+    @classmethod
+    def from_geometry(cls, atoms, frame=None, sym="C1", dip=None, pol=None, watson=None, units="angstrom"):
+        """Molecule from atoms [(label, x, y, z)] or [(label, mass, x, y, z)].
+
+        Coordinates, dipole and polarizability are rotated to ``frame``
+        (r' = R r, mu' = R mu, alpha' = R alpha R^T, as the reference's tensors
+        follow its frame, rot/molecule.py:45-165). The Hamiltonian takes the G
+        matrix of the rotated coordinates (rot/molecule.py:189-260): the
+        inverse of their inertia tensor about the origin times h N_A/(4 pi^2 c),
+        through an SVD with singular values below 1e-12 rejected. ``units``:
+        "angstrom" or "bohr" (Bohr radius from scipy.constants, as
+        rot/atomdata.py:89-90)."""
+        labels, masses, xyz = [], [], []
+        for a in atoms:
+            if len(a) == 5:
+                lab, mass, x, y, z = a
+            else:
+                lab, x, y, z = a
+                mass = MASSES[lab]
+            labels.append(lab)
+            masses.append(float(mass))
+            xyz.append((float(x), float(y), float(z)))
+        m = np.array(masses)
+        r = np.array(xyz)
+        if units.lower() == "bohr":
+            r = r * const.value("Bohr radius") * 1e10
+        elif units.lower() != "angstrom":
+            raise ValueError(f"unknown units '{units}'")
+        R = cls.frame_matrix(frame, m, r, pol)
+        r = r @ R.T
+        u, sv, vt = np.linalg.svd(_inertia_origin(m, r))
+        if np.any(sv <= 1e-12):
+            raise ValueError("rotational kinetic energy matrix is singular (linear molecule?): give B instead")
+        G = (u @ np.diag(1.0 / sv) @ vt) * _G_CONV
+        dip_r = None if dip is None else R @ np.asarray(dip, dtype=np.float64)
+        pol_r = None if pol is None else R @ np.asarray(pol, dtype=np.float64) @ R.T
+        mol = cls(G=G, sym=sym, dip=dip_r, pol=pol_r, watson=watson)
+        mol.frame_rotation = R
+        mol.atoms = list(zip(labels, masses, map(tuple, r)))
+        return mol
+
+    @classmethod
+    def read(cls, filename, name, sym="C1", dip=None, pol=None, watson=None):
+        """Molecule stored by the reference's Molecule.store (rot/molecule.py:
+        390-470): atoms (label, mass, xyz in Angstrom) and frame_rotation; the
+        G matrix follows from them as in ``from_geometry``. Tensors given here
+        are in the input frame and are rotated with the stored frame."""
+        import json
+        from . import hdf5
+        with hdf5.File(filename) as fl:
+            if name not in fl:
+                raise KeyError(f"file '{filename}' has no dataset with the name '{name}'")
+            at = fl[name].attrs
+            atoms = json.loads(at["atoms__json"])["val"]
+            R = np.asarray(at.get("frame_rotation", np.eye(3)), dtype=np.float64)
+        rows = [(a[0], a[1], *(a[2]["val"] if isinstance(a[2], dict) else a[2])) for a in atoms]
+        return cls.from_geometry(rows, frame=R, sym=sym, dip=dip, pol=pol, watson=watson)
 
     @staticmethod
     def B_from_geometry(xyz):
@@ -215,7 +331,11 @@ class Molecule:
             Bl = [b for b in self.B if b != 0][0]
             return np.array([[Bl * J * (J + 1)]], dtype=np.complex128)
         Jx, Jy, Jz = _j_matrices(J)
-        H = self.B[0] * Jx @ Jx + self.B[1] * Jy @ Jy + self.B[2] * Jz @ Jz
+        if self.G is not None:
+            Js = (Jx, Jy, Jz)
+            H = 0.5 * sum(self.G[a, b] * (Js[a] @ Js[b]) for a in range(3) for b in range(3))
+        else:
+            H = self.B[0] * Jx @ Jx + self.B[1] * Jy @ Jy + self.B[2] * Jz @ Jz
         J2 = J * (J + 1)
         Jz2 = Jz @ Jz
         w = self.watson

@@ -658,7 +658,69 @@ def case_c1_j10(nsteps=10):
     save("c1_j10", out, meta)
 
 
+def _notebook_outputs(nb, cell):
+    """Text output of the cell-th code cell of a reference notebook."""
+    with open(os.path.join(REF, "docs/source/notebooks", nb)) as f:
+        cells = [c for c in json.load(f)["cells"] if c["cell_type"] == "code"]
+    return "".join("".join(o.get("text", [])) for o in cells[cell].get("outputs", []))
+
+
+def case_h5_files():
+    """The reference's own HDF5 factor files (docs/source/notebooks/water.h5
+    and camphor.h5, written by CarTens.store, Molecule.store and
+    Solution.store of the reference) as compressed bytes, so that the reader
+    of richmol_gb300.hdf5 is tested where the reference is absent, with what
+    the reference's notebooks printed from the same files:
+
+    * rotations_quickstart.ipynb, code cell 4: the entries scipy printed of
+      the full-matrix dipole X, polarizability XZ and H0 of water.h5;
+    * hdf5_files.ipynb, code cell 3: camphor's J = 0..10 energies (6 decimals);
+
+    and the inputs those notebooks gave (water: geometry in bohr, frame ipas,
+    D2, J <= 5, dipole and polarizability; camphor: dipole and polarizability
+    in the input frame, frame diag(pol), C1, J <= 10)."""
+    out, meta = {}, {}
+    nbdir = os.path.join(REF, "docs/source/notebooks")
+    for nm in ("water", "camphor"):
+        with open(os.path.join(nbdir, nm + ".h5"), "rb") as f:
+            out[nm + "_h5"] = np.frombuffer(f.read(), dtype=np.uint8)
+    text = _notebook_outputs("rotations_quickstart.ipynb", 3)
+    sections, cur = {}, None
+    for line in text.splitlines():
+        for key, tag in (("dipole X:", "dip_x"), ("polarizability XZ:", "pol_xz"), ("field-free Hamiltonian:", "h0")):
+            if line.startswith(key):
+                cur = tag
+                line = line[len(key):]
+        if cur is None:
+            continue
+        line = line.strip()
+        if line.startswith("("):
+            ij, val = line.split("\t")
+            i, j = (int(x) for x in ij.strip("()").split(","))
+            sections.setdefault(cur, []).append((i, j, complex(val.strip("()"))))
+    for tag, rows in sections.items():
+        out["water_" + tag + "_ij"] = np.array([[i, j] for i, j, _ in rows], np.int64)
+        out["water_" + tag + "_val"] = np.array([v for _, _, v in rows], np.complex128)
+    enr = []
+    for line in _notebook_outputs("hdf5_files.ipynb", 2).splitlines():
+        w = line.split()
+        if len(w) == 6 and w[0].isdigit():
+            enr.append((int(w[0]), w[1], int(w[2]), float(w[3])))
+    out["camphor_enr_J"] = np.array([e[0] for e in enr], np.int64)
+    out["camphor_enr_i"] = np.array([e[2] for e in enr], np.int64)
+    out["camphor_enr"] = np.array([e[3] for e in enr])
+    meta["water"] = dict(atoms=[["O", 0.0, 0.0, 0.12395915], ["H", 0.0, -1.43102686, -0.98366080],
+                                ["H", 0.0, 1.43102686, -0.98366080]], units="bohr", frame="ipas",
+                         sym="D2", Jmax=5, dip=[0, 0, -0.7288],
+                         pol=[[9.1369, 0, 0], [0, 9.8701, 0], [0, 0, 9.4486]])
+    meta["camphor"] = dict(frame="diag(pol)", sym="C1", Jmax=10, dip=[1.21615, -0.30746, 0.01140],
+                           pol=[[115.80434, -0.58739, 0.03276], [-0.58739, 112.28245, 1.36146],
+                                [0.03276, 1.36146, 108.47809]])
+    save("h5_files", out, meta)
+
+
 CASES = {
+    "h5_files": case_h5_files,
     "ocs_c1": case_ocs_c1,
     "asym_j10": case_asym_j10,
     "c1_j10": case_c1_j10,

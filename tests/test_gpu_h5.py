@@ -1,0 +1,94 @@
+"""GPU propagation of the reference's own HDF5 factor files.
+
+water.h5 (D2, J <= 5, dim 286) and camphor.h5 (C1, J <= 10, dim 1,771; complex
+K factors), written by the reference's CarTens.store (richmol/field.py:
+1304-1598) and carried as bytes in tests/golden/h5_files.npz, are read by
+CarTens(filename=..., name=...) and propagated through the C ABI under a tilted
+pulse (-alpha E E / 2, field.py:1094-1142 products) from a thermal ensemble,
+10 steps through the pulse maximum, against the oracle on the same factors:
+states 1e-10 relative per step and <alpha_ZZ> (the stored polarizability, au)
+1e-9 absolute, with FP64 and with double-float products. camphor's stored
+field-free tensor carries round-off off-diagonal K elements (below 6e-15
+cm^-1), dropped by reading it with thresh=1e-10 as the reference's read
+allows, so that it is diagonal for the split-operator step."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+STATE_RTOL = 1e-10
+OBS_ATOL = 1e-9
+
+CASES = {
+    # file, field-free tensor, temperature (K), vectors kept, pulse (t0 ps, fwhm ps, W/cm^2);
+    # camphor's constants are near 0.04 cm^-1, so 1 K already populates 1,690
+    # states: its first four ensemble vectors are propagated
+    "water": ("h0", 20.0, None, (0.5, 0.1, 5e12)),
+    "camphor": ("h", 1.0, 4, (0.5, 0.1, 2e12)),
+}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from richmol_gb300 import _native
+    if not os.path.exists(_native.LIB_PATH):
+        _native.build_library()
+    assert torch.cuda.is_available()
+
+
+def _rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("products", ["f64", "df"])
+@pytest.mark.parametrize("mol", sorted(CASES))
+def test_h5_factors_propagate_like_oracle(mol, products, tmp_path):
+    from oracle.fixtures import from_cartens, load
+    from oracle.tdse import OTDSE
+    from richmol_gb300 import CarTens, TDSE, rot
+    from richmol_gb300.convert_units import AUpol_x_Vm_to_invcm
+    d, _ = load(os.path.join(GOLDEN, "h5_files.npz"))
+    path = tmp_path / (mol + ".h5")
+    path.write_bytes(d[mol + "_h5"].tobytes())
+    hname, temp, nkeep, (t0, fwhm, inten) = CASES[mol]
+    h0 = CarTens(str(path), name=hname, thresh=1e-10)
+    pol = CarTens(str(path), name="pol")
+    scale = -0.5 * AUpol_x_Vm_to_invcm()
+    Hac = CarTens(str(path), name="pol") * scale
+    oh0 = from_cartens(h0)
+    oHac = from_cartens(pol) * scale
+    opol = from_cartens(pol)
+    opol.field([0, 0, 1])
+    azz = opol.tomat(form="full")
+    pol.field([0, 0, 1])
+    aop = pol.device_operator()
+
+    td = TDSE(t_start=t0 - 0.05, t_end=t0 + 0.05, dt=0.01)
+    tc = td.time_grid()
+    ot = OTDSE(t_start=t0 - 0.05, t_end=t0 + 0.05, dt=0.01)
+    ot.time_grid()
+    v0 = td.init_state(h0, temp=temp, thresh=1e-3)[:nkeep]
+    assert v0.shape[0] >= 4
+    v = torch.from_numpy(v0).cuda()
+    r = v0.copy()
+    direction = [0.3, -0.2, 0.93]
+    worst = dict(state=0.0, azz=0.0)
+    for t in tc:
+        E = rot.pulse_field(t, t0, fwhm, inten, direction)
+        Hac.field(E)
+        oHac.field(E)
+        v, _ = td.update(Hac, v, H0=h0, products=products)
+        r, _ = ot.update(oHac, r, H0=oh0)
+        worst["state"] = max(worst["state"], _rel(v.cpu().numpy(), r))
+        got = aop.observables(v)[0].real
+        ref = np.array([np.vdot(x, azz.dot(x)).real for x in r])
+        worst["azz"] = max(worst["azz"], np.abs(got - ref).max())
+    print(mol, products, "vectors", v0.shape[0], worst, "Krylov orders", td.last_korder.tolist())
+    assert worst["state"] < STATE_RTOL and worst["azz"] < OBS_ATOL
