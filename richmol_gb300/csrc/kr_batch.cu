@@ -53,6 +53,11 @@ struct kr_batch {
   int* grp_w = nullptr;      // [the same]: groups with a vector of non-zero weight (kr_batch_expect_dev)
   double* err = nullptr;     // [nb]
   double2* part = nullptr;   // [KB_RED_CHUNKS][mmax + 2][nb] partial sums
+  // The next step's V_0 = P S and its ||.||^2 partials, written by the state
+  // combination (kb_combine) so that the step's prologue need not read S:
+  // v0_ready holds the token of the phase they were made with (0: none).
+  double2* part0 = nullptr;  // [KB_RED_CHUNKS][nb]
+  int* v0_ready = nullptr;   // [1]
   int* counts = nullptr;     // [3]: active vectors, vectors that hit mmax, mat-vec error word
   int* tc_work = nullptr;    // [3] work-item counters of the persistent tensor-core launches
   int* kdev = nullptr;       // [2]: Krylov index of the running iteration, orders used by the last step
@@ -97,6 +102,9 @@ struct BatchDev {
   int* counts;
   const int* kdev;  // device Krylov index (null: the k argument of the kernel)
   int* status;
+  double2* part0;       // partials of the next step's ||V_0||^2
+  const int* v0_ready;  // token of the phase of a V_0 made by the last combination
+  int v0_token;         // token of this step's phase
 };
 
 static BatchDev dev_view(const kr_batch* b) {
@@ -119,6 +127,9 @@ static BatchDev dev_view(const kr_batch* b) {
   d.counts = b->counts;
   d.kdev = b->kdev;
   d.status = b->status;
+  d.part0 = b->part0;
+  d.v0_ready = b->v0_ready;
+  d.v0_token = 0;
   return d;
 }
 
@@ -204,11 +215,15 @@ __global__ void kb_phase_df(const double2* phase, float4* pdf, long long dim) {
     pdf[e] = dfc_st(dfc_from(phase[e]));
 }
 
-// S <- phase * S (optional); V_0 = S in complex64 (unnormalised); partial ||S_v||^2
+// S <- phase * S (optional); V_0 = S in complex64 (unnormalised); partial ||S_v||^2.
+// Nothing to do when the last state combination already wrote V_0 = phase * S
+// and its partials with this phase (*v0_ready == token): S then holds the
+// state without the step's first half-phase, which kb_combine applies.
 __global__ void kb_phase_norm(float4* S, const float4* phase, float2* V0, long long dim, int nb, double2* part,
-                              const int* status) {
+                              const int* status, const int* v0_ready, int token) {
   __shared__ double2 sh[8][32];
   if (status && *((volatile const int*)status) != 0) return;  // an error is pending: the step does nothing
+  if (*((volatile const int*)v0_ready) == token) return;
   const int v = blockIdx.y * 32 + threadIdx.x;
   const Chunk ch = chunk_of(dim);
   dfl acc = {0.f, 0.f};
@@ -404,15 +419,21 @@ __global__ void kb_small(BatchDev b, int k, double2 fac, double tol, const doubl
   }
 }
 
-// S <- phase * (c_0 S + ||v|| sum_{i>=1} c_i V_i)   (double-float state; the
-// complex64 Krylov corrections summed in FP32)
-// S <- P (c_0 S + ||S|| sum_{1 <= i < K} c_i V_i), K < KM + 1 per vector
+// S <- P (c_0 P0 S + ||S|| sum_{1 <= i < K} c_i V_i), K < KM + 1 per vector
+// (double-float state; the complex64 Krylov corrections summed in FP32), where
+// P0 = P when the step's prologue left S without its first half-phase
+// (*v0_ready == v0_token), else 1. Then the next step's prologue in the same
+// pass: V_0 = P S in complex64 (unnormalised) and the partials of ||P S||^2,
+// the values kb_phase_norm would compute from the stored S, element for
+// element and in its order. A vector without a Krylov step (K == 0: zero,
+// padding, or an error pending) keeps its S.
 template <int KM>
 __global__ void kb_combine(BatchDev b, const float4* phase) {
+  __shared__ double2 sh[8][32];
   const int v = blockIdx.y * 32 + threadIdx.x;
   const int nb = b.nb;
   const int K = b.kconv[v];
-  if (K == 0) return;  // no Krylov step (zero vector or padding)
+  const bool pre = phase && *b.v0_ready == b.v0_token;
   float2 cf[KM];
 #pragma unroll
   for (int i = 1; i < KM; ++i)
@@ -422,25 +443,39 @@ __global__ void kb_combine(BatchDev b, const float4* phase) {
   const dfc c0 = dfc_from(b.c[v]);
   const dfl n0 = df_from(b.norm0[v]);
   const Chunk ch = chunk_of(b.dim);
+  dfl acc = {0.f, 0.f};
   for (long long e = ch.e0 + threadIdx.y; e < ch.e1; e += 8) {
-    float2 sacc = make_float2(0.f, 0.f);
+    dfc u = dfc_ld(b.S[e * nb + v]);
+    const dfc p = phase ? dfc_ld(__ldg(phase + e)) : dfc_ld(make_float4(1.f, 0.f, 0.f, 0.f));
+    if (K > 0) {
+      float2 sacc = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int i = 1; i < KM; ++i) {
-      if (i < K) {
-        const float2 a = b.V[((long long)i * b.dim + e) * nb + v];
-        sacc.x = fmaf(cf[i].x, a.x, sacc.x);
-        sacc.x = fmaf(-cf[i].y, a.y, sacc.x);
-        sacc.y = fmaf(cf[i].x, a.y, sacc.y);
-        sacc.y = fmaf(cf[i].y, a.x, sacc.y);
+      for (int i = 1; i < KM; ++i) {
+        if (i < K) {
+          const float2 a = b.V[((long long)i * b.dim + e) * nb + v];
+          sacc.x = fmaf(cf[i].x, a.x, sacc.x);
+          sacc.x = fmaf(-cf[i].y, a.y, sacc.x);
+          sacc.y = fmaf(cf[i].x, a.y, sacc.y);
+          sacc.y = fmaf(cf[i].y, a.x, sacc.y);
+        }
       }
+      if (pre) u = dfc_mul(u, p);
+      u = dfc_mul(c0, u);
+      u.re = df_add(u.re, df_mulf(n0, sacc.x));
+      u.im = df_add(u.im, df_mulf(n0, sacc.y));
+      if (phase) u = dfc_mul(u, p);
+      b.S[e * nb + v] = dfc_st(u);
     }
-    dfc u = dfc_mul(c0, dfc_ld(b.S[e * nb + v]));
-    u.re = df_add(u.re, df_mulf(n0, sacc.x));
-    u.im = df_add(u.im, df_mulf(n0, sacc.y));
-    if (phase) u = dfc_mul(u, dfc_ld(__ldg(phase + e)));
-    b.S[e * nb + v] = dfc_st(u);
+    if (phase) u = dfc_mul(u, p);
+    b.V[e * nb + v] = make_float2(__fadd_rn(u.re.hi, u.re.lo), __fadd_rn(u.im.hi, u.im.lo));
+    acc = df_add(acc, df_add(df_mul(u.re, u.re), df_mul(u.im, u.im)));
   }
+  const double2 t = warps_sum(make_double2(df_to(acc), 0.0), sh);
+  if (threadIdx.y == 0) b.part0[(long long)blockIdx.x * nb + v] = t;
 }
+
+// the V_0 of the next step, written by kb_combine, belongs to the phase of token
+__global__ void kb_v0_mark(int* v0_ready, int token) { *v0_ready = token; }
 
 // (nvec, dim) row-major <-> [dim][nb] vector-minor, tiled through shared memory
 __global__ void kb_transpose_in(const double2* src, float4* S, long long dim, int nvec, int nb) {
@@ -720,6 +755,8 @@ extern "C" int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch**
   BA((size_t)mv_groups(b), &b->grp_w);
   BA(nb, &b->err);
   BA((size_t)KB_RED_CHUNKS * (m1 + 1) * nb, &b->part);
+  BA((size_t)KB_RED_CHUNKS * nb, &b->part0);
+  BA(1, &b->v0_ready);
   BA(3, &b->counts);
   BA(3, &b->tc_work);
   BA(2, &b->kdev);
@@ -773,6 +810,8 @@ extern "C" int kr_batch_load(kr_batch* b, const void* states, void* stream) {
   kb_transpose_in<<<grid, dim3(32, 8), 0, (cudaStream_t)stream>>>((const double2*)states, b->S, b->dim, b->nvec, b->nb);
   b->launches++;
   KR_CUDA(b->op->ctx, cudaGetLastError());
+  // a V_0 kept from the last step belongs to the old states
+  KR_CUDA(b->op->ctx, cudaMemsetAsync(b->v0_ready, 0, sizeof(int), (cudaStream_t)stream));
   return KR_OK;
 }
 
@@ -823,15 +862,24 @@ int record_switch(kr_ctx* ctx, cudaStream_t s, cudaGraph_t* bodies, F launch) {
   return KR_OK;
 }
 
+// token of a phase array for v0_ready: its address (0 is never a token)
+int v0_token(const double2* phase) {
+  if (!phase) return 1;
+  return (int)((((uintptr_t)phase) >> 4) & 0x3fffffffu) | 0x40000000;
+}
+
 // Records one batched step into the graph that stream s is capturing into:
-//   prologue   counts = 0; H0 half-phase to double-float; S <- P S, V_0, ||S||^2;
-//              per-vector start; loop control (iteration 0 runs?)
+//   prologue   counts = 0; H0 half-phase to double-float; S <- P S, V_0, ||S||^2
+//              (skipped when the last step's combination left V_0 = P S and
+//              its partials for this phase); per-vector start; loop control
+//              (iteration 0 runs?)
 //   WHILE      mask of active vector groups (+ Gram-Schmidt kernel class);
 //              W = H V_k (mat-vec of the device-side slot k); dots <V_j, W>;
 //              their sums; SWITCH: V_{k+1} = W - sum h_j V_j (bound class of k);
 //              per-vector T, exp(fac T) e0, error estimate, convergence;
 //              loop control (k + 1, errors, iteration k + 1 runs?)
-//   SWITCH     state combination S <- P (c_0 S + ||S|| sum c_i V_i) (class of the orders used)
+//   SWITCH     state combination S <- P (c_0 S + ||S|| sum c_i V_i) (class of the orders used),
+//              with the next step's V_0 = P S and ||V_0||^2 partials; then v0_ready = token
 // The Krylov index lives in device memory (b->kdev), so nothing of the loop
 // depends on the host: a recorded step replays as it is.
 int record_step(kr_batch* b, kr_op* op, const double2* phase, double2 fac, double tol, cudaStream_t s) {
@@ -857,8 +905,9 @@ int record_step(kr_batch* b, kr_op* op, const double2* phase, double2 fac, doubl
     pdf = b->phase_df;
     ++fixed;
   }
-  kb_phase_norm<<<eg, eb, 0, s>>>(b->S, pdf, b->V, dim, nb, b->part, b->status);
-  kb_reduce<<<(nb + 255) / 256, 256, 0, s>>>(b->part, 1, nb, 1, b->h, nullptr);
+  const int token = v0_token(phase);
+  kb_phase_norm<<<eg, eb, 0, s>>>(b->S, pdf, b->V, dim, nb, b->part0, b->status, b->v0_ready, token);
+  kb_reduce<<<(nb + 255) / 256, 256, 0, s>>>(b->part0, 1, nb, 1, b->h, nullptr);
   kb_start<<<(nb + 255) / 256, 256, 0, s>>>(b->h, b->norm0, b->active, b->kconv, b->vscale, nb, b->nvec, b->counts,
                                             b->status);
   kb_ctl_init<<<1, 1, 0, s>>>(b->counts, b->kdev, b->status, hloop);
@@ -904,7 +953,8 @@ int record_step(kr_batch* b, kr_op* op, const double2* phase, double2 fac, doubl
   cudaGraph_t cb[4];
   rc = add_conditional(ctx, s, hcomb, cudaGraphCondTypeSwitch, 4, cb);
   if (rc) return rc;
-  const BatchDev bd = dev_view(b);
+  BatchDev bd = dev_view(b);
+  bd.v0_token = token;
   rc = record_switch(ctx, b->side1, cb, [&](int c, cudaStream_t t) {
     if (c == 0) kb_combine<4><<<eg, eb, 0, t>>>(bd, pdf);
     else if (c == 1) kb_combine<8><<<eg, eb, 0, t>>>(bd, pdf);
@@ -912,7 +962,8 @@ int record_step(kr_batch* b, kr_op* op, const double2* phase, double2 fac, doubl
     else kb_combine<32><<<eg, eb, 0, t>>>(bd, pdf);
   });
   if (rc) return rc;
-  fixed += 2;
+  kb_v0_mark<<<1, 1, 0, s>>>(b->v0_ready, token);
+  fixed += 3;
   KR_CUDA(ctx, cudaGetLastError());
   b->nodes_fixed = fixed;
   b->nodes_iter = iter;
@@ -1016,7 +1067,7 @@ extern "C" int kr_batch_expect(kr_batch* b, kr_op* obs, double* out, void* strea
     return set_err(obs->ctx, KR_ERR_ARG, "kr_batch_expect: observable does not match the batch basis");
   cudaStream_t st = (cudaStream_t)stream;
   const long long n = b->dim * b->nb;
-  float2* X = b->V;  // basis slot 0 and W are free between steps
+  float2* X = b->V + b->dim * b->nb;  // basis slot 1 and W are free between steps (slot 0 holds the next V_0)
   KR_CUDA(obs->ctx, cudaMemsetAsync(b->counts + 2, 0, sizeof(int), st));
   kb_to_f32<<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, st>>>(b->S, X, n);
   int rc = launch_matvec(b, obs, X, b->W, false, nullptr, nullptr, st);
@@ -1061,7 +1112,7 @@ extern "C" int kr_batch_expect_dev(kr_batch* b, kr_op* obs, const double* weight
   if (obs->dev.dim_out != b->dim || !obs->square)
     return set_err(obs->ctx, KR_ERR_ARG, "kr_batch_expect_dev: observable does not match the batch basis");
   cudaStream_t st = (cudaStream_t)stream;
-  float2* X = b->V;  // basis slot 0 and W are free between steps
+  float2* X = b->V + b->dim * b->nb;  // basis slot 1 and W are free between steps (slot 0 holds the next V_0)
   KR_CUDA(obs->ctx, cudaMemsetAsync(b->counts + 2, 0, sizeof(int), st));
   // only the 32-vector groups with a vector of non-zero weight are computed
   const int ng = b->nb / 32;
@@ -1121,8 +1172,9 @@ extern "C" int kr_batch_apply(kr_batch* b, kr_op* op, const void* x, void* y, vo
   cudaStream_t st = (cudaStream_t)stream;
   const dim3 grid((unsigned)((b->dim + 31) / 32), b->nb / 32);
   KR_CUDA(op->ctx, cudaMemsetAsync(b->counts + 2, 0, sizeof(int), st));
-  kb_transpose_in32<<<grid, dim3(32, 8), 0, st>>>((const double2*)x, b->V, b->dim, b->nvec, b->nb);
-  const int rc = launch_matvec(b, op, b->V, b->W, false, nullptr, nullptr, st);
+  float2* X = b->V + b->dim * b->nb;  // basis slot 1 (slot 0 holds the next step's V_0)
+  kb_transpose_in32<<<grid, dim3(32, 8), 0, st>>>((const double2*)x, X, b->dim, b->nvec, b->nb);
+  const int rc = launch_matvec(b, op, X, b->W, false, nullptr, nullptr, st);
   if (rc) return rc;
   kb_transpose_out32<<<grid, dim3(32, 8), 0, st>>>(b->W, (double2*)y, b->dim, b->nvec, b->nb);
   b->launches += 2;
@@ -1161,7 +1213,7 @@ extern "C" int kr_batch_set_matvec(kr_batch* b, int32_t kind) {
 extern "C" int kr_batch_matvec(kr_batch* b, kr_op* op, void* stream) {
   if (!b || !op || op->dev.dim_out != b->dim || !op->square)
     return set_err(b ? b->op->ctx : nullptr, KR_ERR_ARG, "kr_batch_matvec: operator does not match the batch basis");
-  return launch_matvec(b, op, b->V, b->W, false, nullptr, nullptr, (cudaStream_t)stream);
+  return launch_matvec(b, op, b->V + b->dim * b->nb, b->W, false, nullptr, nullptr, (cudaStream_t)stream);
 }
 
 extern "C" int64_t kr_batch_launch_count(const kr_batch* b) { return b ? b->launches : -1; }

@@ -442,3 +442,50 @@ def test_batch_expect_on_device_skips_zero_weight_groups():
     ens.expect_into(cos2, out, torch.from_numpy(w).cuda())
     e = ens.expect(cos2).real
     assert abs(float(out.cpu()[0]) - float(w @ e)) < 1e-13
+
+
+@pytest.mark.parametrize("matvec", ["tensor_tmem", "fp32"])
+def test_batch_next_prologue_kept_through_calls_between_steps(matvec):
+    """The state combination of a step also writes the next step's first
+    Krylov vector (H0 half-phase times the state) and its norm partials, so the
+    next prologue skips its pass over the state. Observables, device
+    observables, populations and a standalone product between the steps use
+    other buffers: the states come out bit for bit as without them. A reload
+    after every step (the prologue then recomputes the vector from the state)
+    agrees to the rounding of the store/load round trip."""
+    from oracle import fixtures
+    from richmol_gb300 import TDSE
+    from richmol_gb300.batch import Ensemble
+    d, meta = fixtures.load(os.path.join(GOLDEN, "asym_j4.npz"))
+    sc = meta["scales"]
+    h0 = _ct("asym_j4.npz", "h0")
+    cos2 = _ct("asym_j4.npz", "cos2")
+    Hdc = (_ct("asym_j4.npz", "dip") * meta["dc"]) * sc["dc"]
+    Hac = _ct("asym_j4.npz", "pol") * sc["ac"]
+    sp = meta["split"]
+    td = TDSE(t_start=sp["t_start"], t_end=sp["t_end"], dt=sp["dt"])
+    tc = td.time_grid()
+    v0 = td.init_state(h0, temp=5, thresh=1e-3)
+    n = v0.shape[0]
+    ens = {k: Ensemble(td, h0, n, tol=1e-10, matvec=matvec) for k in ("plain", "calls", "reload")}
+    for e in ens.values():
+        e.load(v0)
+    w = torch.full((n,), 1.0 / n, dtype=torch.float64, device="cuda")
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    x = torch.from_numpy(np.ascontiguousarray(v0)).cuda()
+    for i in range(len(tc)):
+        Hac.field(d["split/fields"][i])
+        H = Hdc + Hac
+        for k, e in ens.items():
+            e.step(H)
+            if k == "calls":
+                e.expect(cos2)
+                e.expect_into(cos2, out, w)
+                e.populations()
+                e.apply(H, x)
+            elif k == "reload":
+                e.load(e.store())
+    a = ens["plain"].store()
+    assert torch.equal(a, ens["calls"].store())
+    r = ens["reload"].store()
+    assert (r - a).abs().max().item() <= 1e-13 * a.abs().max().item()
