@@ -205,3 +205,23 @@ def test_molecule_frame_rules():
         rot.Molecule.frame_matrix("zxy", m, r)
     with pytest.raises(ValueError):
         rot.Molecule.from_geometry([("C", 0, 0, 0), ("O", 0, 0, -1.16), ("S", 0, 0, 1.56)])  # linear: B only
+
+
+def test_reader_matlab_user_block_file():
+    """A file written by another HDF5 library (MATLAB 7.3 format, in scipy's
+    test data): the superblock sits behind a 512-byte user block and its
+    addresses are relative to that base; one contiguous float64 dataset
+    (linspace(0, 2 pi, 9) as a 9 x 1 column) with a fixed-length string
+    attribute."""
+    scipy_io = pytest.importorskip("scipy.io.matlab")
+    from richmol_gb300 import hdf5
+    path = os.path.join(os.path.dirname(scipy_io.__file__), "tests", "data", "testhdf5_7.4_GLNX86.mat")
+    if not os.path.exists(path):
+        pytest.skip("scipy's MATLAB test data is not installed")
+    assert not hdf5.is_hdf5(path)  # the signature is not at offset 0
+    with hdf5.File(path) as f:
+        assert f.keys() == ["testdouble"]
+        ds = f["testdouble"]
+        assert ds.shape == (9, 1) and ds.dtype == np.float64
+        assert np.array_equal(ds[()][:, 0], np.linspace(0, 2 * np.pi, 9))
+        assert ds.attrs["MATLAB_class"] == b"double"
