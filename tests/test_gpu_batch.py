@@ -489,3 +489,31 @@ def test_batch_next_prologue_kept_through_calls_between_steps(matvec):
     assert torch.equal(a, ens["calls"].store())
     r = ens["reload"].store()
     assert (r - a).abs().max().item() <= 1e-13 * a.abs().max().item()
+
+
+def test_batch_full_h_without_phase_matches_reference():
+    """Full-H steps (no H0 split, so no phase array: the first Krylov vector the
+    state combination keeps for the next step is the state itself) on the
+    batched path against the reference's own full-H states (linear OCS J<=6,
+    five steps), with observables and populations read between the steps."""
+    from oracle import fixtures
+    from richmol_gb300 import TDSE
+    from richmol_gb300.batch import Ensemble
+    d, meta = fixtures.load(os.path.join(GOLDEN, "ocs_j6.npz"))
+    h0 = _ct("ocs_j6.npz", "h0")
+    cos2 = _ct("ocs_j6.npz", "cos2")
+    f = meta["full"]
+    Hac = _ct("ocs_j6.npz", "pol") * meta["split"]["scale"]
+    td = TDSE(t_start=f["t_start"], t_end=f["t_end"], dt=f["dt"])
+    td.time_grid()
+    v0 = np.atleast_2d(d["full/vec0"])
+    ens = Ensemble(td, None, v0.shape[0], tol=1e-8, template=h0, matvec="fp32")
+    ens.load(v0)
+    for i in range(5):
+        Hac.field(f["field"])
+        ens.step(Hac + h0)
+        ens.expect(cos2)
+        ens.populations()
+        got = ens.store().cpu().numpy()
+        ref = np.atleast_2d(d["full/states"][i])
+        assert np.abs(got - ref).max() / np.abs(ref).max() < 1e-5, i
