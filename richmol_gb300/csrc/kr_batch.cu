@@ -426,9 +426,11 @@ __global__ void kb_small(BatchDev b, int k, double2 fac, double tol, const doubl
 // pass: V_0 = P S in complex64 (unnormalised) and the partials of ||P S||^2,
 // the values kb_phase_norm would compute from the stored S, element for
 // element and in its order. A vector without a Krylov step (K == 0: zero,
-// padding, or an error pending) keeps its S.
+// padding, or an error pending) keeps its S. KM = 4 (the class of Krylov
+// orders up to 4) has the register budget of 5 CTAs per SM (48 registers, 8
+// bytes of spills; 56 and 4 CTAs without it): 0.05 ms less per step at C3.
 template <int KM>
-__global__ void kb_combine(BatchDev b, const float4* phase) {
+__global__ void __launch_bounds__(256, KM == 4 ? 5 : 1) kb_combine(BatchDev b, const float4* phase) {
   __shared__ double2 sh[8][32];
   const int v = blockIdx.y * 32 + threadIdx.x;
   const int nb = b.nb;
