@@ -255,7 +255,8 @@ class Molecule:
         return R
 
     @classmethod
-    def from_geometry(cls, atoms, frame=None, sym="C1", dip=None, pol=None, watson=None, units="angstrom"):
+    def from_geometry(cls, atoms, frame=None, sym="C1", dip=None, pol=None, watson=None, units="angstrom",
+                      center=False):
         """Molecule from atoms [(label, x, y, z)] or [(label, mass, x, y, z)].
 
         Coordinates, dipole and polarizability are rotated to ``frame``
@@ -265,7 +266,9 @@ class Molecule:
         inverse of their inertia tensor about the origin times h N_A/(4 pi^2 c),
         through an SVD with singular values below 1e-12 rejected. ``units``:
         "angstrom" or "bohr" (Bohr radius from scipy.constants, as
-        rot/atomdata.py:89-90)."""
+        rot/atomdata.py:89-90). The reference keeps the input origin (its G of
+        an off-centre geometry carries the parallel-axis term); ``center=True``
+        moves the origin to the centre of mass first."""
         labels, masses, xyz = [], [], []
         for a in atoms:
             if len(a) == 5:
@@ -282,6 +285,8 @@ class Molecule:
             r = r * const.value("Bohr radius") * 1e10
         elif units.lower() != "angstrom":
             raise ValueError(f"unknown units '{units}'")
+        if center:
+            r = r - (m[:, None] * r).sum(0) / m.sum()
         R = cls.frame_matrix(frame, m, r, pol)
         r = r @ R.T
         u, sv, vt = np.linalg.svd(_inertia_origin(m, r))

@@ -198,3 +198,37 @@ def test_propagation_observable_is_basis_invariant():
         vecs, _ = td.update(Hac, vecs, H0=h0)
         c = np.vdot(vecs[0], c2.dot(vecs[0])).real + 1 / 3
         assert abs(c - d["split/cos2"][i]) < 1e-9
+
+
+def test_g_matrix_energies_do_not_depend_on_the_frame():
+    """The rigid rotor 1/2 G_ab J_a J_b of one geometry in three frames
+    (principal axes, a random rotation, the polarizability's axes): the
+    rotational energies agree to rounding, and the symmetric-top basis
+    solution (the real part of H in the Wang basis, as rot/solution.py:207
+    diagonalises) equals the full Hermitian diagonalisation, so nothing is
+    dropped with the imaginary part for a non-diagonal G."""
+    from richmol_gb300 import rot
+    rng = np.random.default_rng(17)
+    atoms = [(a, *rng.uniform(-1.5, 1.5, 3)) for a in ("C", "O", "N", "H", "H")]
+    p = rng.normal(size=(3, 3))
+    pol = p @ p.T + 20 * np.eye(3)
+    q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    mols = [rot.Molecule.from_geometry(atoms, frame=f, pol=pol, center=True) for f in ("ipas", q, "diag(pol)")]
+    assert np.abs(mols[0].G - np.diag(np.diag(mols[0].G))).max() < 1e-12
+    assert min(np.abs(m.G - np.diag(np.diag(m.G))).max() for m in mols[1:]) > 1e-3
+    # the reference's own form keeps the input origin: an off-centre geometry's
+    # G carries the parallel-axis term, a centred one gives the same G
+    off = rot.Molecule.from_geometry(atoms, frame="ipas", pol=pol)
+    assert np.abs(off.G - mols[0].G).max() > 1e-3
+    m = np.array([rot.MASSES[a[0]] for a in atoms])
+    r = np.array([a[1:] for a in atoms])
+    r0 = r - (m[:, None] * r).sum(0) / m.sum()
+    cen = rot.Molecule.from_geometry([(a[0], *x) for a, x in zip(atoms, r0)], frame="ipas", pol=pol)
+    assert np.abs(cen.G - mols[0].G).max() < 1e-12 * np.abs(cen.G).max()
+    for J in (1, 4, 8):
+        full = [np.linalg.eigvalsh(m.hamiltonian(J)) for m in mols]
+        sol = [np.sort(rot.Solution(m, Jmin=J, Jmax=J).states[J]["A"][0]) for m in mols]
+        scale = max(1.0, np.abs(full[0]).max())
+        for f, s in zip(full, sol):
+            assert np.abs(f - full[0]).max() < 1e-13 * scale, J
+            assert np.abs(s - f).max() < 1e-13 * scale, J
