@@ -369,6 +369,40 @@ class Solution:
                 e, v = np.linalg.eigh(hmat)
                 self.states[J][lab] = (e, Cs @ v)
 
+    @classmethod
+    def read(cls, filename, name, mol):
+        """Solutions stored by the reference's Solution.store (rot/solution.py:
+        60-130, the ``data__json`` attribute): per J and symmetry the energies
+        and the states' coefficients on the symmetric-top functions |J,k> (each
+        row of ``k.table`` a primitive (J, k) and its coefficient in every
+        state). ``mol`` gives what the factors need besides (linear or not)."""
+        import json
+        from . import hdf5
+
+        def cplx(x):
+            return complex(x["real"], x["imag"]) if isinstance(x, dict) else complex(x)
+
+        with hdf5.File(filename) as fl:
+            if name not in fl:
+                raise KeyError(f"file '{filename}' has no dataset with the name '{name}'")
+            data = json.loads(fl[name].attrs["data__json"])
+        sol = cls.__new__(cls)
+        sol.mol = mol
+        sol.Jlist = sorted(int(J) for J in data)
+        sol.states = {}
+        for J in sol.Jlist:
+            sol.states[J] = {}
+            for sym, tab in data[str(J)].items():
+                enr = np.asarray(tab["enr"], dtype=np.float64)
+                C = np.zeros((1 if mol.linear else 2 * J + 1, len(enr)), dtype=np.complex128)
+                for prim, _, c in tab["k.table"]["val"]:
+                    j, k = (int(x) for x in (prim["val"] if isinstance(prim, dict) else prim))
+                    if j != J:
+                        raise ValueError(f"primitive J = {j} in the table of J = {J}")
+                    C[0 if mol.linear else k + J] = [cplx(x) for x in (c["val"] if isinstance(c, dict) else c)]
+                sol.states[J][sym] = (enr, C)
+        return sol
+
     def basis(self):
         Jl = [float(J) for J in self.Jlist]
         syml = {float(J): list(self.states[J].keys()) for J in self.Jlist}

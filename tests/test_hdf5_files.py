@@ -225,3 +225,38 @@ def test_reader_matlab_user_block_file():
         assert ds.shape == (9, 1) and ds.dtype == np.float64
         assert np.array_equal(ds[()][:, 0], np.linspace(0, 2 * np.pi, 9))
         assert ds.attrs["MATLAB_class"] == b"double"
+
+
+def test_stored_solution_gives_the_files_k_factors_element_by_element(h5):
+    """camphor.h5 also holds the reference's rotational solutions (sol, the
+    eigenvectors the stored dip and pol were built from). With those
+    eigenvectors there is no phase freedom left: the builder's K factors equal
+    the file's element by element, and the stored energies the builder's."""
+    from richmol_gb300 import rot
+    from richmol_gb300.field import CarTens
+    from richmol_gb300 import hdf5
+    _, meta, paths = h5
+    c = meta["camphor"]
+    mol = rot.Molecule.read(paths["camphor"], "camphor", sym=c["sym"], dip=c["dip"], pol=np.array(c["pol"]))
+    stored = rot.Solution.read(paths["camphor"], "sol", mol)
+    ours = rot.Solution(mol, Jmax=c["Jmax"])
+    assert stored.Jlist == ours.Jlist
+    for J in ours.Jlist:
+        e, C = stored.states[J]["A"]
+        assert np.abs(e - ours.states[J]["A"][0]).max() < 1e-12 * max(1.0, np.abs(e).max())
+        assert np.abs(C.conj().T @ C - np.eye(C.shape[1])).max() < 1e-12  # orthonormal states
+    with hdf5.File(paths["camphor"]) as f:
+        flat = {nm: np.asarray(f[nm].attrs["tens_flat"]) for nm in ("dip", "pol")}
+    for nm, tens in (("dip", mol.dip), ("pol", mol.pol)):
+        assert np.abs(np.asarray(tens).reshape(-1) - flat[nm]).max() < 1e-12
+        ref = CarTens(filename=paths["camphor"], name=nm)
+        got = rot.lab_tensor(tens, stored)._parts[0].src
+        n = 0
+        for Jp in ref.kmat:
+            for sp in ref.kmat[Jp]:
+                for i in ref.kmat[Jp][sp]:
+                    a = ref.kmat[Jp][sp][i].toarray()
+                    b = got.kmat[Jp][sp][i].toarray()
+                    assert np.abs(a - b).max() < 1e-12 * max(1.0, np.abs(a).max()), (nm, Jp, i)
+                    n += 1
+        assert n == (30 if nm == "dip" else 57)
