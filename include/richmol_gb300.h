@@ -274,7 +274,9 @@ typedef struct kr_batch kr_batch;
  * (mmax basis vectors, 2 <= mmax <= 31). */
 int kr_batch_create(kr_op* op, int64_t nvec, int32_t mmax, kr_batch** out);
 void kr_batch_destroy(kr_batch* b);
-/* states (nvec, dim) complex128 device <-> the batch's internal layout. */
+/* states (nvec, dim) complex128 device <-> the batch's internal layout
+ * (kr_batch_load also discards the first Krylov vector kept for the next
+ * step, see kr_batch_step). */
 int kr_batch_load(kr_batch* b, const void* states, void* stream);
 int kr_batch_store(kr_batch* b, void* states, void* stream);
 /* One TDSE.update of every vector (split operator when phase != NULL):
@@ -292,7 +294,13 @@ int kr_batch_store(kr_batch* b, void* states, void* stream);
  *     graph) the step's nodes go into the caller's graph; kmax_out must be
  *     NULL and errors are read by kr_batch_sync after the replay.
  * A pending error makes later steps leave the states unchanged until it has
- * been read. */
+ * been read. A step's state combination also writes the next step's first
+ * Krylov vector (phase times the new states) and its norm, for the phase
+ * array at that address; the next step with the same phase address skips
+ * that pass, and kr_batch_load discards it. Rewriting a phase array's
+ * contents in place between steps is therefore not allowed. Between steps,
+ * kr_batch_expect*, kr_batch_apply, kr_batch_matvec and kr_batch_populations
+ * leave it intact. */
 int kr_batch_step(kr_batch* b, kr_op* op, const void* phase, double fac_re, double fac_im,
                   double tol, int32_t* kmax_out, void* stream);
 /* Synchronises the stream and reports (and clears) the error of an earlier
