@@ -43,7 +43,12 @@ def _nested():
 
 
 class FactorSource:
-    """Immutable factor blocks of one tensor: bases, kmat, mmat, rank, cart."""
+    """Immutable factor blocks of one tensor: bases, kmat, mmat, rank, cart.
+
+    The bases carry the reference's state quanta (field.py:58-170): per J and
+    symmetry ``quanta_m`` (the m of each M row) and ``quanta_k`` ((label,
+    energy) of each K state). Sources without them get m = -J..J for full M
+    sets and labels "J sym i" with no energy."""
 
     def __init__(self, basis, kmat, mmat, rank, carts):
         for k, v in basis.items():
@@ -52,10 +57,85 @@ class FactorSource:
             dm = getattr(self, "dim_m" + side)
             dk = getattr(self, "dim_k" + side)
             setattr(self, "dim" + side, {J: {s: dm[J][s] * dk[J][s] for s in dm[J]} for J in dm})
+            sl = getattr(self, "symlist" + side)
+            if not hasattr(self, "quanta_m" + side):
+                setattr(self, "quanta_m" + side, {
+                    J: {s: (list(range(-int(J), int(J) + 1)) if dm[J][s] == 2 * int(J) + 1 else list(range(dm[J][s])))
+                        for s in sl[J]} for J in getattr(self, "Jlist" + side)})
+            if not hasattr(self, "quanta_k" + side):
+                setattr(self, "quanta_k" + side, {
+                    J: {s: [(f"{int(J)} {s} {i}", None) for i in range(dk[J][s])] for s in sl[J]}
+                    for J in getattr(self, "Jlist" + side)})
         self.kmat = kmat
         self.mmat = mmat
         self.rank = rank
         self.carts = list(carts)
+
+    def filtered(self, bra, ket, thresh=None):
+        """A new source with the states for which bra (rows) and ket (columns)
+        hold (field.py:187-447): K states are tested with (J, sym, k=label,
+        enr=energy), M rows with (J, sym, m); J values and symmetries left
+        without states are dropped (symmetries sorted, as the reference), the
+        blocks are cut to the kept rows and columns, elements below thresh
+        dropped, and irreps whose K or M blocks end up empty removed."""
+        basis, ind = {}, {}
+        for side, f in (("1", bra), ("2", ket)):
+            Jl = getattr(self, "Jlist" + side)
+            sl = getattr(self, "symlist" + side)
+            qk = getattr(self, "quanta_k" + side)
+            qm = getattr(self, "quanta_m" + side)
+            ik = {J: {s: [i for i, (q, e) in enumerate(qk[J][s]) if f(J=J, sym=s, k=q, enr=e)] for s in sl[J]}
+                  for J in Jl}
+            im = {J: {s: [i for i, q in enumerate(qm[J][s]) if f(J=J, sym=s, m=q)] for s in sl[J]} for J in Jl}
+            ik = {J: {s: v for s, v in d.items() if v} for J, d in ik.items()}
+            im = {J: {s: v for s, v in d.items() if v} for J, d in im.items()}
+            Jnew = sorted(J for J in Jl if ik[J] and im[J])
+            snew = {J: sorted(set(ik[J]) & set(im[J])) for J in Jnew}
+            Jnew = [J for J in Jnew if snew[J]]
+            basis["Jlist" + side] = Jnew
+            basis["symlist" + side] = {J: snew[J] for J in Jnew}
+            basis["dim_m" + side] = {J: {s: len(im[J][s]) for s in snew[J]} for J in Jnew}
+            basis["dim_k" + side] = {J: {s: len(ik[J][s]) for s in snew[J]} for J in Jnew}
+            basis["quanta_m" + side] = {J: {s: [qm[J][s][i] for i in im[J][s]] for s in snew[J]} for J in Jnew}
+            basis["quanta_k" + side] = {J: {s: [qk[J][s][i] for i in ik[J][s]] for s in snew[J]} for J in Jnew}
+            ind[side] = (ik, im, basis["symlist" + side])
+
+        def cut(mat, rows, cols):
+            return csr_matrix(mat)[rows, :].tocsc()[:, cols].tocsr()
+
+        def drop(m):
+            m.data[np.abs(m.data) < thresh] = 0
+            m.eliminate_zeros()
+            return m
+
+        kmat, mmat = _nested(), _nested()
+        (ik1, im1, s1l), (ik2, im2, s2l) = ind["1"], ind["2"]
+        for Jp in set(self.kmat.keys()) & set(self.mmat.keys()):
+            J1, J2 = Jp
+            if J1 not in s1l or J2 not in s2l:
+                continue
+            for sp in set(self.kmat[Jp].keys()) & set(self.mmat[Jp].keys()):
+                a, b = sp
+                if a not in s1l[J1] or b not in s2l[J2]:
+                    continue
+                kS = {irrep: cut(m, ik1[J1][a], ik2[J2][b]) for irrep, m in self.kmat[Jp][sp].items()}
+                mS = {irrep: {c: cut(m, im1[J1][a], im2[J2][b]) for c, m in mI.items()}
+                      for irrep, mI in self.mmat[Jp][sp].items()}
+                # irreps in both: thresh, then dropped if K or every M is empty
+                # (irreps in one of them only stay as cut, field.py:417-443)
+                for irrep in set(kS) & set(mS):
+                    if thresh is not None:
+                        kS[irrep] = drop(kS[irrep])
+                        mS[irrep] = {c: m for c, m in ((c, drop(m)) for c, m in mS[irrep].items()) if m.nnz > 0}
+                    if kS[irrep].nnz == 0 or len(mS[irrep]) == 0:
+                        del kS[irrep], mS[irrep]
+                if kS and mS:
+                    for irrep, m in kS.items():
+                        kmat[Jp][sp][irrep] = m
+                    for irrep, mI in mS.items():
+                        for c, m in mI.items():
+                            mmat[Jp][sp][irrep][c] = m
+        return FactorSource(basis, kmat, mmat, self.rank, self.carts)
 
     def basis(self, side):
         Jl = getattr(self, "Jlist" + side)
@@ -111,6 +191,8 @@ class CarTens:
                             mmat[Jp][sp][irrep]["0"] = m
                 rank, cart = 0, ["0"]
             self._init_source(FactorSource(basis, kmat, mmat, rank, cart))
+            if "bra" in kwargs or "ket" in kwargs:  # field.py:172, read with state filters
+                self.filter(bra=kwargs.get("bra", lambda **kw: True), ket=kwargs.get("ket", lambda **kw: True))
 
     @classmethod
     def from_factors(cls, basis, kmat, mmat, rank, cart):
@@ -226,6 +308,18 @@ class CarTens:
             raise TypeError(f"bad argument type for `arg` : '{type(arg)}'")
         for part in self._parts:
             part.kscale = part.kscale * arg
+
+    def filter(self, thresh=None, bra=lambda **kw: True, ket=lambda **kw: True):
+        """Keeps the states for which ``bra`` (bra states) and ``ket`` (ket
+        states) return True (field.py:187-447): each is called with J, sym and
+        k (the state's label), enr (its energy) for K states, and with J, sym
+        and m for M states. Every part of a sum is cut alike; the field
+        products are kept. Matrix elements below ``thresh`` are dropped."""
+        done = {}
+        for p in self._parts:
+            if id(p.src) not in done:
+                done[id(p.src)] = p.src.filtered(bra, ket, thresh)
+            p.src = done[id(p.src)]
 
     def _copy(self):
         res = CarTens()
@@ -382,3 +476,12 @@ class CarTens:
     def store(self, filename, name):
         """Writes the factors (K scale applied) to a factor file."""
         _io.write_tensors(filename, {name: self})
+
+
+def filter(obj, bra, ket, thresh=None):
+    """A copy of ``obj`` with the state filters applied (field.py:1859-1882)."""
+    if not isinstance(obj, CarTens):
+        raise TypeError(f"bad argument type for 'obj': '{type(obj)}'")
+    res = obj._copy()
+    res.filter(bra=bra, ket=ket, thresh=thresh)
+    return res

@@ -101,6 +101,15 @@ def read_tensor_h5(filename, name):
             for kind in ("dim_m", "dim_k"):
                 d = {jkey(J): {s: int(n) for s, n in v.items()} for J, v in attrs[kind + side].items()}
                 basis[kind + side] = {J: d[J] for J in Jlist}
+            # state quanta (field.py:58-170): m of each M row, (label, energy) of each K state
+            if "quanta_m" + side in attrs:
+                q = {jkey(J): {s: [int(m) for m in ms] for s, ms in v.items()}
+                     for J, v in attrs["quanta_m" + side].items()}
+                basis["quanta_m" + side] = {J: q[J] for J in Jlist}
+            if "quanta_k" + side in attrs:
+                q = {jkey(J): {s: [(str(a), None if e is None else float(e)) for a, e in ks] for s, ks in v.items()}
+                     for J, v in attrs["quanta_k" + side].items()}
+                basis["quanta_k" + side] = {J: q[J] for J in Jlist}
         rank = int(attrs["rank"])
         cart = [_str(c) for c in np.atleast_1d(attrs["cart"])]
         kmat, mmat = _nested(), _nested()
@@ -187,6 +196,11 @@ def _read_tensor_npz(filename, name):
         basis["symlist" + side] = {J: list(s) for J, s in zip(Jlist, syml)}
         basis["dim_m" + side] = {J: dict(zip(syml[i], info["dim_m" + side][i])) for i, J in enumerate(Jlist)}
         basis["dim_k" + side] = {J: dict(zip(syml[i], info["dim_k" + side][i])) for i, J in enumerate(Jlist)}
+        if "quanta_m" + side in info:
+            basis["quanta_m" + side] = {J: dict(zip(syml[i], info["quanta_m" + side][i])) for i, J in enumerate(Jlist)}
+        if "quanta_k" + side in info:
+            basis["quanta_k" + side] = {J: {s: [(str(a), e) for a, e in ks] for s, ks in zip(syml[i], info["quanta_k" + side][i])}
+                                        for i, J in enumerate(Jlist)}
     kmat, mmat, mfmat = _nested(), _nested(), None
     for kind, J1, J2, s1, s2, irrep, cart, idx in info["blocks"]:
         key = (jkey(J1), jkey(J2))
@@ -239,6 +253,11 @@ def write_tensors(filename, tensors):
             info["symlist" + side] = [list(sl[J]) for J in Jl]
             info["dim_m" + side] = [[int(getattr(src, "dim_m" + side)[J][s]) for s in sl[J]] for J in Jl]
             info["dim_k" + side] = [[int(getattr(src, "dim_k" + side)[J][s]) for s in sl[J]] for J in Jl]
+            qm = getattr(src, "quanta_m" + side)
+            qk = getattr(src, "quanta_k" + side)
+            info["quanta_m" + side] = [[[int(m) for m in qm[J][s]] for s in sl[J]] for J in Jl]
+            info["quanta_k" + side] = [[[[str(a), None if e is None else float(e)] for a, e in qk[J][s]] for s in sl[J]]
+                                       for J in Jl]
         meta[name] = info
         cat = lambda xs, dt: np.concatenate(xs).astype(dt) if xs else np.zeros(0, dt)
         out[name + "/csr_data"] = cat(data, np.complex128)

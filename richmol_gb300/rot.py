@@ -403,17 +403,37 @@ class Solution:
                 sol.states[J][sym] = (enr, C)
         return sol
 
+    def quanta(self):
+        """{J: {sym: [(label, energy), ...]}} in the reference's form
+        (quanta_k of field.py:58-170, labels of rot/solution.py): J, then k and
+        tau of the state's largest Wang component and its weight |c|^2 as
+        "%9.6f", joined by spaces."""
+        out = {}
+        for J in self.Jlist:
+            Cw, bas = wang_coefficients(J, self.mol.linear)
+            out[float(J)] = {}
+            for sym, (e, C) in self.states[J].items():
+                w = np.abs(np.conj(Cw.T) @ C) ** 2
+                lead = np.argmax(w, axis=0)
+                out[float(J)][sym] = [(" ".join([str(J), str(bas[i][0]), str(bas[i][1]), "%9.6f" % w[i, n]]),
+                                       float(e[n])) for n, i in enumerate(lead)]
+        return out
+
     def basis(self):
         Jl = [float(J) for J in self.Jlist]
         syml = {float(J): list(self.states[J].keys()) for J in self.Jlist}
         dm = {float(J): {s: 2 * J + 1 for s in self.states[J]} for J in self.Jlist}
         dk = {float(J): {s: self.states[J][s][1].shape[1] for s in self.states[J]} for J in self.Jlist}
         b = {}
+        qk = self.quanta()
+        qm = {float(J): {s: list(range(-J, J + 1)) for s in self.states[J]} for J in self.Jlist}
         for side in ("1", "2"):
             b["Jlist" + side] = Jl
             b["symlist" + side] = syml
             b["dim_m" + side] = dm
             b["dim_k" + side] = dk
+            b["quanta_k" + side] = qk
+            b["quanta_m" + side] = qm
         return b
 
 

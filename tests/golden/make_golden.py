@@ -86,7 +86,7 @@ def _key(x):
     return str(x)
 
 
-def export_cartens(T, prefix, out, meta, with_mmat=True, with_mfmat=True):
+def export_cartens(T, prefix, out, meta, with_mmat=True, with_mfmat=True, with_quanta=False):
     pk = Packer()
     info = {}
     for side in ("1", "2"):
@@ -97,6 +97,11 @@ def export_cartens(T, prefix, out, meta, with_mmat=True, with_mfmat=True):
         for attr in ("dim_m", "dim_k"):
             d = getattr(T, attr + side)
             info[attr + side] = [[int(d[J][s]) for s in symlist[J]] for J in Jlist]
+        if with_quanta:  # state quanta: m of each M row, (label, energy) of each K state
+            qm, qk = getattr(T, "quanta_m" + side), getattr(T, "quanta_k" + side)
+            info["quanta_m" + side] = [[[int(m) for m in qm[J][s]] for s in symlist[J]] for J in Jlist]
+            info["quanta_k" + side] = [[[[str(q), float(e)] for q, e in qk[J][s]] for s in symlist[J]]
+                                       for J in Jlist]
     for attr in ("rank", "cart", "os"):
         if hasattr(T, attr):
             v = getattr(T, attr)
@@ -658,6 +663,47 @@ def case_c1_j10(nsteps=10):
     save("c1_j10", out, meta)
 
 
+def filter_predicates():
+    """The state filters of case_filter, as (bra, ket, thresh) per name; the
+    test restates them."""
+    m0 = lambda **kw: kw["m"] == 0 if "m" in kw else True
+    low = lambda **kw: kw["enr"] < 60.0 if "enr" in kw else True
+    j3 = lambda **kw: kw["J"] <= 3 and kw["sym"] != "B3"
+    return {"m0": (m0, m0, None), "enr_j": (low, j3, None), "m0_thresh": (m0, m0, 1e-3)}
+
+
+def case_filter(Jmax=4):
+    """The reference's state filters (field.py:187-447, 1859-1882) applied to
+    its own D2 asymmetric-top tensors at J <= 4: the unfiltered h0 and pol with
+    their state quanta, and for each filter of filter_predicates the filtered
+    tensors (bases, quanta and blocks)."""
+    import copy
+
+    def ref_filter(T, bra, ket, thresh=None):
+        # field.py:1859-1882 (deepcopy, then CarTens.filter). The reference's
+        # filter raises RuntimeError when a filter removes a symmetry of a J it
+        # keeps and the tensor holds symtop_basis (field.py:348-352 deletes
+        # from the dict it iterates over); that loop only trims symtop_basis,
+        # which the blocks do not depend on, so the copy drops it first.
+        res = copy.deepcopy(T)
+        if hasattr(res, "symtop_basis"):
+            del res.symtop_basis
+        res.filter(bra=bra, ket=ket, thresh=thresh)
+        return res
+
+    out, meta = {}, {"Jmax": Jmax}
+    mol = asym_molecule()
+    sol = solve(mol, Jmax=Jmax)
+    h0 = LabTensor(mol, sol, thresh=1e-9)
+    pol = LabTensor(mol.pol, sol)
+    for nm, T in (("h0", h0), ("pol", pol)):
+        export_cartens(T, nm, out, meta, with_mfmat=False, with_quanta=True)
+        for fname, (bra, ket, thresh) in filter_predicates().items():
+            export_cartens(ref_filter(T, bra, ket, thresh=thresh), f"{nm}_{fname}", out, meta, with_mfmat=False,
+                           with_quanta=True)
+    save("filter_j4", out, meta)
+
+
 def _notebook_outputs(nb, cell):
     """Text output of the cell-th code cell of a reference notebook."""
     with open(os.path.join(REF, "docs/source/notebooks", nb)) as f:
@@ -720,6 +766,7 @@ def case_h5_files():
 
 
 CASES = {
+    "filter": case_filter,
     "h5_files": case_h5_files,
     "ocs_c1": case_ocs_c1,
     "asym_j10": case_asym_j10,

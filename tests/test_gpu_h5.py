@@ -92,3 +92,47 @@ def test_h5_factors_propagate_like_oracle(mol, products, tmp_path):
         worst["azz"] = max(worst["azz"], np.abs(got - ref).max())
     print(mol, products, "vectors", v0.shape[0], worst, "Krylov orders", td.last_korder.tolist())
     assert worst["state"] < STATE_RTOL and worst["azz"] < OBS_ATOL
+
+
+@pytest.mark.parametrize("cut", ["m0", "enr"])
+def test_filtered_h5_factors_propagate_like_oracle(cut, tmp_path):
+    """water.h5 cut with state filters (field.py:187-447) before propagating:
+    m = 0 only (the m-resolved propagation of the reference's notebooks: every
+    slab one M row) or the states below 400 cm^-1; 10 steps through the pulse
+    on the GPU against the oracle on the same cut factors."""
+    from oracle.fixtures import from_cartens, load
+    from oracle.tdse import OTDSE
+    from richmol_gb300 import CarTens, TDSE, rot
+    from richmol_gb300.convert_units import AUpol_x_Vm_to_invcm
+    from richmol_gb300.field import filter
+    d, _ = load(os.path.join(GOLDEN, "h5_files.npz"))
+    path = tmp_path / "water.h5"
+    path.write_bytes(d["water_h5"].tobytes())
+    if cut == "m0":
+        f = lambda **kw: kw["m"] == 0 if "m" in kw else True
+    else:
+        f = lambda **kw: kw["enr"] < 400.0 if "enr" in kw else True
+    h0 = filter(CarTens(str(path), name="h0"), f, f)
+    pol = filter(CarTens(str(path), name="pol"), f, f)
+    scale = -0.5 * AUpol_x_Vm_to_invcm()
+    Hac = pol * scale
+    oh0 = from_cartens(h0)
+    oHac = from_cartens(pol) * scale
+    td = TDSE(t_start=0.45, t_end=0.55, dt=0.01)
+    tc = td.time_grid()
+    ot = OTDSE(t_start=0.45, t_end=0.55, dt=0.01)
+    ot.time_grid()
+    v0 = td.init_state(h0, temp=50.0, thresh=1e-3)
+    assert v0.shape[1] == (36 if cut == "m0" else v0.shape[1]) and v0.shape[0] >= 2
+    v = torch.from_numpy(v0).cuda()
+    r = v0.copy()
+    worst = 0.0
+    for t in tc:
+        E = rot.pulse_field(t, 0.5, 0.1, 5e12, [0.3, -0.2, 0.93])
+        Hac.field(E)
+        oHac.field(E)
+        v, _ = td.update(Hac, v, H0=h0)
+        r, _ = ot.update(oHac, r, H0=oh0)
+        worst = max(worst, _rel(v.cpu().numpy(), r))
+    print(cut, "dim", v0.shape[1], "vectors", v0.shape[0], "state", worst)
+    assert worst < STATE_RTOL

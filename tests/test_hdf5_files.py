@@ -260,3 +260,40 @@ def test_stored_solution_gives_the_files_k_factors_element_by_element(h5):
                     assert np.abs(a - b).max() < 1e-12 * max(1.0, np.abs(a).max()), (nm, Jp, i)
                     n += 1
         assert n == (30 if nm == "dip" else 57)
+
+
+def test_builder_state_labels_match_the_files(h5):
+    """The builder's state quanta (label: J, k and tau of the largest Wang
+    component and its weight; energy) against the quanta_k the reference
+    stored with water's and camphor's tensors. Inside K doublets closer than
+    1e-2 cm^-1 (camphor at J >= 8: 6e-10 apart) the eigenvectors mix by the
+    eigensolver's round-off, so there the weight is compared to 1e-4."""
+    import json
+    from richmol_gb300 import hdf5, rot
+    from test_rot_builder import CLUSTER_GAP
+    _, meta, paths = h5
+    w, c = meta["water"], meta["camphor"]
+    cases = [
+        (paths["water"], "dip", rot.Molecule.from_geometry([tuple(a) for a in w["atoms"]], frame=w["frame"],
+                                                            sym=w["sym"], dip=w["dip"], pol=np.array(w["pol"]),
+                                                            units=w["units"]), w["Jmax"], 2e-9),
+        (paths["camphor"], "dip", rot.Molecule.read(paths["camphor"], "camphor", sym=c["sym"], dip=c["dip"],
+                                                    pol=np.array(c["pol"])), c["Jmax"], 1e-12),
+    ]
+    for path, name, mol, Jmax, etol in cases:
+        q = rot.Solution(mol, Jmax=Jmax).quanta()
+        with hdf5.File(path) as f:
+            ref = json.loads(f[name].attrs["quanta_k1__json"])
+        n = 0
+        for J in range(Jmax + 1):
+            for s, states in ref[f"{J}.0"].items():
+                e = np.array([x[1] for x in states])
+                for i, ((a, ea), (b, eb)) in enumerate(zip(q[float(J)][s], states)):
+                    assert abs(ea - eb) < etol * max(1.0, abs(eb)), (J, s, i)
+                    near = np.sort(np.abs(e - e[i]))[1:2] if len(e) > 1 else np.array([np.inf])
+                    if near.size and near[0] < CLUSTER_GAP:
+                        assert a.split()[:3] == b.split()[:3] and abs(float(a.split()[3]) - float(b.split()[3])) < 1e-4
+                    else:
+                        assert a == b, (J, s, i, a, b)
+                    n += 1
+        assert n == sum(len(v) for d in ref.values() for v in d.values())
