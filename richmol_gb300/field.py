@@ -214,7 +214,7 @@ class CarTens:
 
     def __getattr__(self, name):
         if name in ("Jlist1", "Jlist2", "symlist1", "symlist2", "dim_m1", "dim_m2", "dim_k1", "dim_k2",
-                    "dim1", "dim2"):
+                    "dim1", "dim2", "quanta_m1", "quanta_m2", "quanta_k1", "quanta_k2"):
             return getattr(self._first(), name)
         if name in ("rank", "cart", "mmat") and not self.__dict__.get("_is_sum", False):
             src = self._first()
@@ -320,6 +320,75 @@ class CarTens:
             if id(p.src) not in done:
                 done[id(p.src)] = p.src.filtered(bra, ket, thresh)
             p.src = done[id(p.src)]
+
+    def assign(self, form="block"):
+        """Quantum numbers of the bra and ket states (field.py:572-657), in the
+        order of the rows and columns of ``tomat``: per J and symmetry the
+        product of the M states (outer) and K states (inner). form 'block':
+        assign[J][sym]['m'] and ['k']; form 'full': lists 'm', 'k', 'sym', 'J'
+        over the whole basis. A K entry is the state's (label, energy)."""
+        assert form in ("block", "full"), f"bad value of argument 'form' = '{form}' (use 'block' or 'full')"
+        out = []
+        for side in ("1", "2"):
+            Jl, sl = getattr(self, "Jlist" + side), getattr(self, "symlist" + side)
+            qm, qk = getattr(self, "quanta_m" + side), getattr(self, "quanta_k" + side)
+            if form == "block":
+                a = _nested()
+                for J in Jl:
+                    for sym in sl[J]:
+                        mk = list(itertools.product(qm[J][sym], qk[J][sym]))
+                        a[J][sym]["m"] = [e[0] for e in mk]
+                        a[J][sym]["k"] = [e[1] for e in mk]
+            else:
+                a = {"m": [], "k": [], "sym": [], "J": []}
+                for J in Jl:
+                    for sym in sl[J]:
+                        mk = list(itertools.product(qm[J][sym], qk[J][sym]))
+                        a["m"] += [e[0] for e in mk]
+                        a["k"] += [e[1] for e in mk]
+                        a["sym"] += [sym] * len(mk)
+                        a["J"] += [J] * len(mk)
+            out.append(a)
+        return tuple(out)
+
+    def full_form(self, mat, repres="csr_matrix", thresh=None):
+        """Block matrix {(J1, J2): {(sym1, sym2): block}} -> one 2D matrix in the
+        basis order of ``tomat`` (field.py:660-693); missing blocks are zero."""
+        rows = [(J, s) for J in self.Jlist1 for s in self.symlist1[J]]
+        cols = [(J, s) for J in self.Jlist2 for s in self.symlist2[J]]
+        res = scipy.sparse.bmat([[mat[(J1, J2)][(s1, s2)]
+                                  if (J1, J2) in mat and (s1, s2) in mat[(J1, J2)]
+                                  else csr_matrix((self.dim1[J1][s1], self.dim2[J2][s2]))
+                                  for J2, s2 in cols] for J1, s1 in rows])
+        if thresh is not None:
+            res = csr_matrix(res)
+            res.data[np.abs(res.data) < thresh] = 0
+            res.eliminate_zeros()
+        return res.toarray() if repres == "dense" else getattr(scipy.sparse, repres)(res)
+
+    def block_form(self, mat):
+        """2D matrix -> {(J1, J2): {(sym1, sym2): block}} for the bra and ket
+        J/symmetry slabs (field.py:696-737); all-zero blocks are left out, sparse
+        input gives blocks of its own format."""
+        rows = [(J, s) for J in self.Jlist1 for s in self.symlist1[J]]
+        cols = [(J, s) for J in self.Jlist2 for s in self.symlist2[J]]
+        r0 = np.cumsum([0] + [self.dim1[J][s] for J, s in rows])
+        c0 = np.cumsum([0] + [self.dim2[J][s] for J, s in cols])
+        sparse = scipy.sparse.issparse(mat)
+        m = csr_matrix(mat) if sparse else np.asarray(mat)
+        res = {}
+        for i, (J1, s1) in enumerate(rows):
+            for j, (J2, s2) in enumerate(cols):
+                blk = m[r0[i]:r0[i + 1], c0[j]:c0[j + 1]]
+                if sparse:
+                    blk = getattr(scipy.sparse, mat.getformat() + "_matrix")(blk)
+                    blk.eliminate_zeros()
+                    if blk.nnz == 0:
+                        continue
+                elif not np.any(blk):
+                    continue
+                res.setdefault((J1, J2), {})[(s1, s2)] = blk
+        return res
 
     def _copy(self):
         res = CarTens()

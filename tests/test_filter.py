@@ -117,3 +117,31 @@ def test_filter_m_subset_dimensions_match_notebook():
             flt = lambda **kw: kw["m"] == m_ if "m" in kw else True
             dims.append(filter(dip, flt, flt).tomat(form="full", cart="z").shape[0])
     assert dims == [11, 20, 27, 32, 35, 36, 35, 32, 27, 20, 11]
+
+
+def test_assign_full_and_block_forms_follow_the_reference_order():
+    """assign (field.py:572-657) lists the states in the row/column order of
+    tomat; full_form and block_form (field.py:660-737) convert between the
+    block dictionary and that matrix. For the reference's own D2 J<=4 h0 the
+    diagonal of tomat carries each state's energy (its K label's energy)."""
+    from richmol_gb300.field import CarTens, filter
+    h0 = CarTens(CASE, name="h0")
+    a1, a2 = h0.assign(form="full")
+    H = h0.tomat(form="full", cart="0")
+    assert len(a1["m"]) == H.shape[0] == sum(sum(v.values()) for v in h0.dim1.values())
+    assert np.allclose(H.diagonal().real, [e for _, e in a1["k"]], atol=1e-9)
+    blk = h0.assign(form="block")[0]
+    J, s = 2.0, "A"
+    assert blk[J][s]["m"][: h0.dim_k1[J][s]] == [-2] * h0.dim_k1[J][s]  # m outer, k inner
+    pol = CarTens(CASE, name="pol")
+    pol.field([0.2, -0.4, 1.0])
+    full = pol.tomat(form="full", repres="csr_matrix")
+    b = pol.block_form(full)
+    back = pol.full_form(b)
+    assert abs(back - full).max() == 0
+    dense = pol.block_form(full.toarray())
+    assert set(dense) == set(b)
+    # after a filter the assignment lists only the kept states
+    m0 = lambda **kw: kw["m"] == 0 if "m" in kw else True
+    f1, _ = filter(h0, m0, m0).assign(form="full")
+    assert set(f1["m"]) == {0} and len(f1["m"]) == sum(sum(v.values()) for v in filter(h0, m0, m0).dim1.values())
