@@ -704,6 +704,20 @@ def case_filter(Jmax=4):
     save("filter_j4", out, meta)
 
 
+def case_trove_files():
+    """The legacy OCS TROVE files (tests/benchmarks/data/alignment_ocs/matelem:
+    the states file and the alpha matrix-element files) as bytes, so that
+    richmol_gb300.trove is tested against ocs_trove.npz (the reference's own
+    CarTensTrove objects of the same files) where the reference is absent."""
+    out, meta = {}, {"files": []}
+    mdir = os.path.join(REF, "tests/benchmarks/data/alignment_ocs/matelem")
+    for i, fn in enumerate(sorted(f for f in os.listdir(mdir) if "energies" in f or "alpha" in f)):
+        with open(os.path.join(mdir, fn), "rb") as f:
+            out[f"file{i}"] = np.frombuffer(f.read(), dtype=np.uint8)
+        meta["files"].append(fn)
+    save("trove_files", out, meta)
+
+
 def _notebook_outputs(nb, cell):
     """Text output of the cell-th code cell of a reference notebook."""
     with open(os.path.join(REF, "docs/source/notebooks", nb)) as f:
@@ -766,6 +780,7 @@ def case_h5_files():
 
 
 CASES = {
+    "trove_files": case_trove_files,
     "filter": case_filter,
     "h5_files": case_h5_files,
     "ocs_c1": case_ocs_c1,
